@@ -1,0 +1,329 @@
+#!/usr/bin/env python
+"""Benchmark: umbreon ray-cast + shade on GB300 through the C-ABI.
+
+A step is one frame of the ball-and-stick workload (20,000 atoms r 0.4 on a
+1.5 A random walk + 19,999 capped bonds r 0.2, 2 lights with hard shadows,
+16 AO rays at distance 6, 1920x1080 with 2x2 supersampling, linear fog),
+rendered with the scene already built in device memory.  `value` is traced
+rays (closest-hit + AO/shadow any-hit) per second over the K timed frames;
+`e2e` is the same metric through the reference-facing call with HOST
+buffers: scene upload + GPU BVH build + render + copy of the frame back.
+
+--impl reference times the reference's CPU path on the host cores.  The
+reference itself (Embree 4 + oneTBB) cannot be built on the GPU host, so
+this arm runs the CPU restatement of the same path (oracle/, kind "port")
+on all host threads, on a row band of the same frame.
+
+Multi-GPU: frames are independent, so N GPUs run N replicas of the frame
+(weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "ms/frame & Mrays/s (batched vs per-frame GPU) at >=45 dB PSNR; adjoint ms/iter"
+WORKLOAD = "ball_and_stick_20k_1920x1080_ss2_ao16_2lights_shadows_fog"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return
+    from umbreon_gb300 import scenes
+    sc, opt = scenes.ball_and_stick()
+    threads = os.cpu_count() or 1
+    steps = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        r = _cpu_band(sc, opt, threads, target_s=args.cpu_seconds / max(1, args.steps))
+        if i >= args.warmup:
+            steps.append(r)
+        info = r
+    mrays = sum(s["rays"] for s in steps) / sum(s["secs"] for s in steps) / 1e6
+    ms_frame = sum(s["secs"] * s["frame_rays"] / s["rays"] for s in steps) / len(steps) * 1e3
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(mrays, 3), "unit": "Mrays/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_frame, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded PCG32 scene)",
+        "config": {"workload": WORKLOAD, "sample": f"rows {info['rows']} of {info['H']} hi-res rows per step"},
+        "cpu_baseline": {"value": round(mrays, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{info['rows']} hi-res rows of the frame per step (all host threads)"},
+        "e2e": {"value": round(mrays, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _cpu_band(sc, opt, threads, target_s):
+    """One CPU step: oracle on a band of rows, rays counted by the oracle's
+    own primary count plus the occlusion rays it traced (estimated from the
+    GPU-identical ray layout: AO samples and one ray per lit light per hit)."""
+    from oracle import oracle
+    osc = _cpu_band.cache.get(id(sc))
+    if osc is None:
+        osc = oracle.OracleScene(sc)
+        _cpu_band.cache[id(sc)] = osc
+    ss = max(1, opt.supersample)
+    H = opt.height * ss
+    W = opt.width * ss
+    mid = H // 2
+    if not hasattr(_cpu_band, "rate"):
+        rows = max(2, H // 200)
+        f = osc.render(sc, opt, threads=threads, rows=(mid - rows // 2, mid - rows // 2 + rows))
+        _cpu_band.rate = max(f.stats["render_ms"], 1e-3) / rows
+    want = int(min(H, max(2, target_s * 1e3 / _cpu_band.rate)))
+    r0 = max(0, mid - want // 2)
+    t0 = time.perf_counter()
+    f = osc.render(sc, opt, threads=threads, rows=(r0, r0 + want))
+    secs = time.perf_counter() - t0
+    hits = int((f.hit_geom[r0:r0 + want] != 0xFFFFFFFF).sum())
+    rays = f.stats["rays_primary"] + hits * (opt.aoSamples + (len(sc.lights) if opt.shadows else 0))
+    frame_rays = rays * H / want
+    return {"rays": rays, "secs": secs, "rows": want, "H": H, "W": W, "frame_rays": frame_rays}
+
+
+_cpu_band.cache = {}
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from umbreon_gb300 import abi, scenes
+    from umbreon_gb300.api import Context, make_render_desc
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    sc, opt = scenes.ball_and_stick()
+    ctx = Context(local)
+    built = ctx.build(sc)
+    info = built.info()
+    import ctypes as C
+    rd, keep = make_render_desc(sc, opt)
+    ss = opt.supersample
+    W, H = opt.width * ss, opt.height * ss
+    dev_color = torch.empty((opt.height, opt.width, 4), dtype=torch.float32, device=f"cuda:{local}")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")  # 256 MB > 129 MB L2
+
+    def frame(flags=0):
+        fr = abi.Frame()
+        fr.memory = abi.MEMORY_DEVICE
+        fr.flags = flags
+        fr.color = C.cast(C.c_void_p(dev_color.data_ptr()), abi.f32p)
+        st = ctx._L.ubr_render(ctx.handle, built.handle, C.byref(rd), C.byref(fr), None, None)
+        if st != abi.UBR_OK:
+            ctx._check(st)
+        return fr
+
+    for _ in range(args.warmup):
+        frame()
+    # one counting frame (untimed): algorithmic bytes per ray type
+    cf = frame(abi.FRAME_COUNT | abi.FRAME_PROFILE)
+    ctr = {"node_bytes": list(cf.node_bytes), "prim_bytes": list(cf.prim_bytes),
+           "nodes_visited": list(cf.nodes_visited), "rays": [cf.rays_primary, cf.rays_occlusion]}
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    total_ms, phase = 0.0, [0.0] * 5
+    rays = 0
+    kernels = 0
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            fr = frame(abi.FRAME_PROFILE)
+            total_ms += fr.total_ms
+            for k in range(5):
+                phase[k] += fr.phase_ms[k]
+            rays += fr.rays_primary + fr.rays_occlusion
+            kernels += fr.kernels
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if ws > 1:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_frame = total_ms / args.steps
+    value = rays * ws / (total_ms / 1e3) / 1e6
+
+    # roofline of the dominant kernel (per launch = per frame here)
+    names = ["trace_closest", "surface", "trace_occlusion", "shade", "post"]
+    dom = max(range(5), key=lambda k: phase[k])
+    per_launch_ms = phase[dom] / args.steps
+    if dom == 2:
+        alg = ctr["node_bytes"][1] + ctr["prim_bytes"][1]
+    elif dom == 0:
+        alg = ctr["node_bytes"][0] + ctr["prim_bytes"][0]
+    else:
+        alg = None
+    peak, peak_kind = _peaks()
+    roof = None
+    if alg is not None:
+        achieved = alg / (per_launch_ms / 1e3) / 1e9
+        traffic = None
+        tfile = ROOT / "profiles" / "traffic.json"
+        if tfile.exists():
+            traffic = json.loads(tfile.read_text()).get(names[dom])
+        roof = {"bound": "hbm", "kernel": f"k_{names[dom]}", "achieved": round(achieved, 1), "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic, "algorithmic_bytes_per_launch": int(alg),
+                "launch_ms": round(per_launch_ms, 3)}
+
+    # end to end through the C-ABI with host buffers: upload + BVH + render + D2H
+    host_color = np.zeros((opt.height, opt.width, 4), np.float32)
+    desc, keepd = sc.to_desc()
+    h2d = sum(a.nbytes for a in keepd)
+    e2e_steps = max(1, min(args.steps, 5))
+    e2e_rays = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        h = C.c_void_p()
+        ctx._check(ctx._L.ubr_scene_build(ctx.handle, C.byref(desc), C.byref(h)))
+        fr = abi.Frame()
+        fr.memory = abi.MEMORY_HOST
+        fr.color = abi.ptr(host_color)
+        ctx._check(ctx._L.ubr_render(ctx.handle, h, C.byref(rd), C.byref(fr), None, None))
+        e2e_rays += fr.rays_primary + fr.rays_occlusion
+        ctx._L.ubr_scene_release(h)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": round(e2e_rays * ws / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(host_color.nbytes), "ms_per_step": round(e2e_s / e2e_steps * 1e3, 2),
+           "steps": e2e_steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        r = _cpu_band(sc, opt, threads, target_s=args.cpu_seconds)
+        cpu = {"value": round(r["rays"] / r["secs"] / 1e6, 3), "unit": "Mrays/s", "cores": threads,
+               "kind": "port", "sample": f"{r['rows']} of {r['H']} hi-res rows of the same frame",
+               "ms_per_frame_est": round(r["secs"] * r["frame_rays"] / r["rays"] * 1e3, 1)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_frame, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded PCG32 random-walk chain)",
+            "config": {"workload": WORKLOAD, "frame": f"{opt.width}x{opt.height} ss{ss}",
+                       "primitives": info["prim_count"], "bvh_nodes": info["bvh_nodes"],
+                       "l2": "flushed (256 MB write) before every timed frame",
+                       "parallelism": f"replicas x{ws}"},
+            "ms_per_frame": round(ms_frame, 3),
+            "phase_ms_per_frame": {n: round(v / args.steps, 3) for n, v in zip(names, phase)},
+            "rays_per_frame": int(rays / args.steps),
+            "wall_s": round(wall, 3),
+            "roofline": roof, "counting_frame": ctr, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(kernels), "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    built.release()
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

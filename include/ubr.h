@@ -1,0 +1,298 @@
+/*
+ * ubr.h -- C-ABI of the GB300 ray-cast + shade library (libubr.so).
+ *
+ * This is the device boundary of the umbreon renderer.  The reference runs the
+ * whole pixel loop on the CPU through Embree and TBB; here the C++ host layer
+ * (umbreon::render, same public API) flattens Scene/RenderOptions into the
+ * plain structs below and calls these entry points, which run everything on
+ * one GPU.  Only plain pointers, sizes and POD structs cross the boundary: no
+ * C++ types, no torch types, no exceptions.  Every entry returns ubr_status.
+ *
+ * Reference interfaces replaced (paths inside the CueMol/umbreon project):
+ *   ubr_context_*        the RTCDevice the renderer creates per frame or
+ *                        shares across group-alpha passes
+ *                        (src/umbreon/render/embree_renderer.cpp:1267-1274,
+ *                         src/umbreon/umbreon.cpp:21-40)
+ *   ubr_scene_build      detail::buildEmbreeScene (render/scene_build.hpp:126,
+ *                        scene_build.cpp:133-170, curve_build.cpp:41-267)
+ *   ubr_render           EmbreeRenderer::render + the finishing steps of
+ *                        renderFrame (render/embree_renderer.cpp:1260-1745,
+ *                        render/pipeline.cpp:44-50,126-129,182-223,254)
+ *   ubr_occluded_batch   EmbreeRenderer::occluded (embree_renderer.cpp:294-357)
+ *   ubr_render_batch     no reference counterpart (many frames per launch)
+ *   ubr_adjoint          no reference counterpart (image-loss gradients)
+ */
+#ifndef UBR_H_
+#define UBR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UBR_ABI_VERSION 1u
+
+/* Status codes.  The reference throws std::runtime_error on device/BVH
+ * failure (scene_build.cpp:164-168, embree_renderer.cpp:1271-1286); the host
+ * layer maps every non-OK status to that exception, except UBR_CANCELLED
+ * which becomes FrameResult::cancelled = true (embree_renderer.cpp:1743). */
+typedef enum ubr_status {
+  UBR_OK = 0,
+  UBR_INVALID_ARGUMENT = 1,
+  UBR_OUT_OF_MEMORY = 2,
+  UBR_CUDA_ERROR = 3,
+  UBR_CANCELLED = 4,
+  UBR_TRAVERSAL_LIMIT = 5, /* a traversal stack overflowed; frame still written */
+  UBR_NO_DEVICE = 6,
+  UBR_INTERNAL = 7
+} ubr_status;
+
+/* Primitive kinds, in the geomID attach order of the reference
+ * (scene_build.cpp:159-161: mesh, spheres, open cylinders, capped cylinders).
+ * The geomID of a kind is its rank among the kinds present in the scene. */
+typedef enum ubr_kind {
+  UBR_KIND_MESH = 0,
+  UBR_KIND_SPHERE = 1,
+  UBR_KIND_CYLINDER_OPEN = 2,   /* ROUND_LINEAR_CURVE, chained */
+  UBR_KIND_CYLINDER_CAPPED = 3  /* CONE_LINEAR_CURVE, flat caps */
+} ubr_kind;
+
+#define UBR_INVALID_ID 0xFFFFFFFFu
+
+/* POV finish, field-for-field umbreon::Material (scene.hpp:130-224). */
+typedef struct ubr_material {
+  float ambient;
+  float diffuse;
+  float specular;
+  float roughness;
+  float brilliance;
+  float phong;
+  float phong_size;
+  uint32_t metallic;       /* bool */
+  float reflection;
+  float emission;
+  uint32_t model;          /* 0 Pov, 1 Principled, 2 Toon */
+  float pbr_metallic;
+  float pbr_roughness;
+  float pbr_specular;
+  float pbr_anisotropy;
+  float pbr_anisotropy_rotation;
+} ubr_material;
+
+/* Scene geometry, structure of arrays, HOST memory.  Mirrors umbreon::Scene's
+ * Mesh / Sphere / Cylinder vectors (scene.hpp:233-356) and instanceOffsets.
+ * NULL optional arrays take the reference's empty-vector meaning. */
+typedef struct ubr_scene_desc {
+  uint32_t abi_version;            /* UBR_ABI_VERSION */
+  /* mesh */
+  uint64_t mesh_vertex_count;
+  const float* mesh_positions;     /* 3 * vertex_count */
+  const float* mesh_normals;       /* 3 * vertex_count */
+  const float* mesh_colors;        /* 4 * vertex_count (rgb + opacity) */
+  uint64_t mesh_triangle_count;
+  const uint32_t* mesh_index;      /* 3 * triangle_count, NULL = de-indexed */
+  ubr_material mesh_material;      /* Mesh::material */
+  const ubr_material* mesh_materials; /* Mesh::materials (may be NULL) */
+  uint32_t mesh_material_count;
+  const uint8_t* mesh_tri_material;   /* triangle_count or NULL */
+  const uint16_t* mesh_tri_group;     /* triangle_count or NULL */
+  /* spheres */
+  uint64_t sphere_count;
+  const float* sphere_center_radius;  /* 4 * n: x y z r */
+  const float* sphere_color;          /* 4 * n */
+  const ubr_material* sphere_material;/* n */
+  const uint16_t* sphere_group;       /* n or NULL */
+  const uint8_t* sphere_from_edge;    /* n or NULL */
+  /* cylinders */
+  uint64_t cylinder_count;
+  const float* cyl_p0;                /* 3 * n */
+  const float* cyl_p1;                /* 3 * n */
+  const float* cyl_radius;            /* n */
+  const float* cyl_color;             /* 4 * n */
+  const float* cyl_opacity1;          /* n or NULL (NULL = all < 0) */
+  const ubr_material* cyl_material;   /* n */
+  const uint16_t* cyl_group;          /* n or NULL */
+  const uint8_t* cyl_open;            /* n or NULL (NULL = all capped) */
+  const uint8_t* cyl_from_edge;       /* n or NULL */
+  /* grid instances (offsets baked into the geometry, scene_build.cpp:150-152) */
+  uint64_t instance_count;
+  const float* instance_offsets;      /* 3 * n or NULL */
+} ubr_scene_desc;
+
+/* One distant light, umbreon::DistantLight (scene.hpp:390-405). */
+typedef struct ubr_light {
+  float direction[3];   /* direction the light travels */
+  float color[3];
+  float intensity;
+  uint32_t casts_highlight;
+  float angular_radius;
+} ubr_light;
+
+/* Flattened render request: the RenderOptions fields this path honours
+ * (render_options.hpp:14-328) plus Scene's camera, lights, ambient,
+ * background, fog, clip planes and assumed gamma (scene.hpp:380-479). */
+typedef struct ubr_render_desc {
+  uint32_t abi_version;
+  int32_t width;          /* FINAL output size */
+  int32_t height;
+  int32_t supersample;
+  /* camera */
+  float cam_position[3];
+  float cam_direction[3];
+  float cam_up[3];
+  float cam_fovy;
+  uint32_t cam_orthographic;
+  float cam_height;
+  /* lights and scene constants */
+  const ubr_light* lights;
+  uint32_t light_count;
+  float ambient_color[3];
+  float background[3];
+  uint32_t fog_enabled;
+  float fog_color[3];
+  float fog_start;
+  float fog_end;
+  float clip_near;        /* -inf = off */
+  float clip_far;         /* +inf = off */
+  float assumed_gamma;
+  /* ambient occlusion */
+  int32_t ao_samples;
+  float ao_distance;
+  float ao_intensity;
+  float ao_falloff_power;
+  uint32_t ao_multiscale;
+  uint32_t ao_bent_normal;
+  float ao_sky_color[3];
+  float ao_ground_color[3];
+  uint32_t ao_use_camera_up;
+  float ao_up[3];
+  uint32_t ao_multibounce;
+  uint32_t ao_low_discrepancy;
+  float ao_diffuse_factor;
+  /* shadows */
+  uint32_t shadows;
+  int32_t shadow_samples;
+  float light_radius_deg;
+  /* environment dome */
+  int32_t env_lights;
+  float env_intensity;
+  float env_key_scale;
+  float env_angle;
+  /* shading / transparency */
+  float specular_scale;
+  uint32_t transparency;
+  uint32_t transparent_background;
+  int32_t max_transparent_layers;
+  /* giIntegrator only selects the soft-shadow radius rule
+   * (embree_renderer.cpp:452-454); GI itself is out of this library */
+  int32_t gi_integrator;
+} ubr_render_desc;
+
+/* Where a frame's buffers live. */
+typedef enum ubr_memory {
+  UBR_MEMORY_HOST = 0,    /* pageable or pinned host memory; copied at the end */
+  UBR_MEMORY_DEVICE = 1   /* device pointers on the context's GPU */
+} ubr_memory;
+
+/* Caller-owned output buffers.  NULL pointers are skipped.  Sizes follow
+ * FrameResult (frame_result.hpp:43-124) as renderFrame leaves it:
+ *   color   : W*H*4 final (downsampled, fogged, gamma'd) linear RGBA
+ *   depth   : Wss*Hss  hi-res first-hit ray distance (renderFrame does not
+ *             downsample depth, pipeline.cpp:182-228)
+ *   view_z  : Wss*Hss  hi-res plane eye-z of the first hit
+ *   hit_geom, hit_prim : Wss*Hss first-hit (geomID, primID); UBR_INVALID_ID
+ *             on a miss (parity evidence, not a FrameResult field)
+ * Statistics are written back into the struct. */
+#define UBR_FRAME_PROFILE 1u  /* time each kernel phase with CUDA events */
+#define UBR_FRAME_COUNT 2u    /* count BVH node / primitive bytes fetched */
+
+typedef struct ubr_frame {
+  int32_t memory;         /* ubr_memory */
+  uint32_t flags;         /* UBR_FRAME_PROFILE | UBR_FRAME_COUNT */
+  float* color;
+  float* depth;
+  float* view_z;
+  uint32_t* hit_geom;
+  uint32_t* hit_prim;
+  /* out: statistics */
+  double render_ms;       /* device time of the pixel loop (renderSeconds) */
+  double total_ms;        /* device time of the whole ubr_render call */
+  uint64_t rays_primary;  /* closest-hit rays traced (all layers) */
+  uint64_t rays_occlusion;/* AO + shadow any-hit rays traced */
+  uint64_t capped_rays;   /* rays that reached the transparent-layer cap */
+  uint64_t stack_overflows;
+  uint32_t layers;        /* transparency rounds executed */
+  uint32_t kernels;       /* kernels launched by this call */
+  /* with UBR_FRAME_PROFILE: device ms per phase
+   * [0] closest-hit trace, [1] surface prep, [2] AO + shadow rays,
+   * [3] shade + composite, [4] fog/downsample/gamma */
+  double phase_ms[5];
+  /* with UBR_FRAME_COUNT: bytes of BVH nodes and of primitive records
+   * fetched, [0] closest-hit rays, [1] occlusion rays */
+  uint64_t node_bytes[2];
+  uint64_t prim_bytes[2];
+  uint64_t nodes_visited[2];
+} ubr_frame;
+
+/* Context: one GPU, one CUDA stream, one device arena. */
+typedef struct ubr_context ubr_context;
+typedef struct ubr_scene ubr_scene;
+
+typedef struct ubr_context_desc {
+  uint32_t abi_version;
+  int32_t device;              /* CUDA ordinal */
+  uint64_t arena_bytes;        /* 0 = grow on demand; >0 = hard cap */
+  void* stream;                /* cudaStream_t to run on, NULL = own stream */
+} ubr_context_desc;
+
+const char* ubr_status_string(ubr_status s);
+uint32_t ubr_abi_version(void);
+
+ubr_status ubr_context_create(ubr_context** out, const ubr_context_desc* desc);
+ubr_status ubr_context_destroy(ubr_context* ctx);
+/* Message of the last failure on this context (never NULL). */
+const char* ubr_context_last_error(const ubr_context* ctx);
+
+/* Upload the scene, build the side tables and the LBVH on the GPU.
+ * primIDs follow the reference order (scene_build.cpp:46-71,99-121,
+ * curve_build.cpp:95-175,221-247) so (geomID, primID) can be compared. */
+ubr_status ubr_scene_build(ubr_context* ctx, const ubr_scene_desc* desc,
+                           ubr_scene** out);
+ubr_status ubr_scene_release(ubr_scene* scene);
+/* Scene facts: primitive counts per kind, BVH node count, build time. */
+typedef struct ubr_scene_info {
+  uint64_t prim_count[4];
+  uint32_t geom_id[4];     /* UBR_INVALID_ID when the kind is absent */
+  uint64_t bvh_nodes;
+  uint64_t device_bytes;
+  double build_ms;
+  float bounds_lo[3];
+  float bounds_hi[3];
+} ubr_scene_info;
+ubr_status ubr_scene_get_info(const ubr_scene* scene, ubr_scene_info* info);
+
+/* Render one frame: primary rays, closest hits through the transparency walk,
+ * POV shading with AO and shadow rays, fog, box downsample, gamma.
+ * cancel_flag (host memory, may be NULL) is polled between kernel rounds;
+ * a set flag returns UBR_CANCELLED with a partial frame.
+ * progress_units (may be NULL) counts finished transparency rounds. */
+ubr_status ubr_render(ubr_context* ctx, const ubr_scene* scene,
+                      const ubr_render_desc* desc, ubr_frame* frame,
+                      const volatile int32_t* cancel_flag,
+                      uint64_t* progress_units);
+
+/* Segment occlusion for the stroke-edge pass: out[i] = 1 when any geometry
+ * lies strictly inside segment (p[i], q[i]) trimmed by eps
+ * (embree_renderer.cpp:294-315 plain any-hit branch).  segs = 6*n floats
+ * (px py pz qx qy qz), in the memory space given by `memory`. */
+ubr_status ubr_occluded_batch(ubr_context* ctx, const ubr_scene* scene,
+                              const float* segs, uint64_t n, float eps,
+                              uint8_t* out, int32_t memory);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* UBR_H_ */

@@ -1,0 +1,112 @@
+"""Python binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loads ``oracle/liboracle.so`` (the C++ restatement in ``oracle/src``) and
+renders a ``umbreon_gb300.api.Scene`` on the host cores.  Only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may use this
+module, and only as the checker or the timed CPU reference -- never as the
+product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from umbreon_gb300 import abi
+from umbreon_gb300.api import FrameResult, RenderOptions, Scene, make_render_desc
+
+HERE = Path(__file__).resolve().parent
+_L = None
+
+
+def lib():
+    global _L
+    if _L is None:
+        p = HERE / "liboracle.so"
+        if not p.exists():
+            from umbreon_gb300 import build
+            build.build_oracle()
+        L = C.CDLL(str(p))
+        L.oracle_scene_create.restype = C.c_void_p
+        L.oracle_scene_create.argtypes = [C.POINTER(abi.SceneDesc)]
+        L.oracle_scene_destroy.argtypes = [C.c_void_p]
+        L.oracle_scene_bvh_nodes.restype = C.c_uint64
+        L.oracle_scene_bvh_nodes.argtypes = [C.c_void_p]
+        L.oracle_scene_geom_id.restype = C.c_uint32
+        L.oracle_scene_geom_id.argtypes = [C.c_void_p, C.c_int]
+        L.oracle_render.restype = C.c_int
+        L.oracle_render.argtypes = [C.c_void_p, C.POINTER(abi.RenderDesc), C.POINTER(abi.Frame), C.c_int]
+        L.oracle_render_rows.restype = C.c_int
+        L.oracle_render_rows.argtypes = [C.c_void_p, C.POINTER(abi.RenderDesc), C.POINTER(abi.Frame), C.c_int,
+                                         C.c_int, C.c_int]
+        L.oracle_intersect.restype = C.c_int
+        L.oracle_intersect.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64] + [C.c_void_p] * 6
+        L.oracle_occluded.restype = C.c_int
+        L.oracle_occluded.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+        _L = L
+    return _L
+
+
+class OracleScene:
+    def __init__(self, scene: Scene):
+        d, self._keep = scene.to_desc()
+        self.h = lib().oracle_scene_create(C.byref(d))
+        if not self.h:
+            raise RuntimeError("oracle_scene_create failed")
+
+    def geom_id(self, kind: int) -> int:
+        return int(lib().oracle_scene_geom_id(self.h, kind))
+
+    def intersect(self, rays: np.ndarray):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = len(rays)
+        t = np.zeros(n, np.float32)
+        g = np.zeros(n, np.uint32)
+        p = np.zeros(n, np.uint32)
+        u = np.zeros(n, np.float32)
+        v = np.zeros(n, np.float32)
+        ng = np.zeros((n, 3), np.float32)
+        lib().oracle_intersect(self.h, rays.ctypes.data, n, t.ctypes.data, g.ctypes.data, p.ctypes.data,
+                               u.ctypes.data, v.ctypes.data, ng.ctypes.data)
+        return t, g, p, u, v, ng
+
+    def occluded(self, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        out = np.zeros(len(rays), np.uint8)
+        lib().oracle_occluded(self.h, rays.ctypes.data, len(rays), out.ctypes.data)
+        return out
+
+    def render(self, scene: Scene, opt: RenderOptions, threads: int = 0, rows: tuple | None = None) -> FrameResult:
+        rd, keep = make_render_desc(scene, opt)
+        ss = max(1, opt.supersample)
+        W, H = opt.width * ss, opt.height * ss
+        color = np.zeros((opt.height, opt.width, 4), np.float32)
+        depth = np.zeros((H, W), np.float32)
+        vz = np.zeros((H, W), np.float32)
+        hg = np.zeros((H, W), np.uint32)
+        hp = np.zeros((H, W), np.uint32)
+        fr = abi.Frame()
+        fr.color = abi.ptr(color)
+        fr.depth = abi.ptr(depth)
+        fr.view_z = abi.ptr(vz)
+        fr.hit_geom = abi.ptr(hg, C.c_uint32)
+        fr.hit_prim = abi.ptr(hp, C.c_uint32)
+        r0, r1 = rows if rows else (0, 0)
+        st = lib().oracle_render_rows(self.h, C.byref(rd), C.byref(fr), threads, r0, r1)
+        if st != 0:
+            raise RuntimeError("oracle: unsupported request (Principled material)")
+        stats = dict(render_ms=fr.render_ms, rays_primary=fr.rays_primary, capped_rays=fr.capped_rays)
+        return FrameResult(opt.width, opt.height, color, depth, vz, hg, hp, fr.render_ms / 1e3, stats)
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().oracle_scene_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def render(scene: Scene, opt: RenderOptions, threads: int = 0) -> FrameResult:
+    return OracleScene(scene).render(scene, opt, threads)

@@ -1,0 +1,955 @@
+// oracle_render.cpp -- TEST INFRASTRUCTURE (the oracle), never shipped.
+//
+// Plain C++ restatement, on the CPU, of umbreon's ray-cast + shade path, used
+// only by tests/, by __graft_entry__.smoke() and by bench.py's CPU baseline as
+// the checker.  Every function names the reference lines it follows (paths
+// inside the CueMol/umbreon project).  Float expressions keep the reference's
+// operation order so that, built with -ffp-contract=off, results match the
+// reference's own code on the same intersections bit for bit.
+//
+// Scope: the POV shading model (the Principled branch, shading.hpp:88, and
+// every GI / edge / adaptive-AA / coarse-AO branch are outside the path and
+// rejected or ignored as documented at each site).
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <array>
+#include <thread>
+#include <vector>
+
+#include "oracle_geom.hpp"
+#include "ubr.h"
+
+namespace oracle {
+namespace {
+
+constexpr float kInf = std::numeric_limits<float>::infinity();
+
+// scene.hpp:44-49 safeNormalize(a)
+inline V3 safeNormalize(V3 a) {
+  float s = 1.0f / std::sqrt(std::fmax(dot(a, a), 0x1.0p-126f));
+  return a * s;
+}
+// scene.hpp:53-57 safeNormalize(a, fallback)
+inline V3 safeNormalize(V3 a, V3 fb) {
+  float d = dot(a, a);
+  if (d < 1.0e-18f) return fb;
+  return a * (1.0f / std::sqrt(d));
+}
+struct Frame { V3 t, b, n; };
+// scene.hpp:69-76 frameFromNormal
+inline Frame frameFromNormal(V3 n) {
+  const V3 seed0{0.0f, n.z, -n.y};
+  const V3 seed1{-n.z, 0.0f, n.x};
+  const V3 t = safeNormalize(std::fabs(n.x) < std::fabs(n.y) ? seed0 : seed1, V3{1.0f, 0.0f, 0.0f});
+  const V3 b = cross(n, t);
+  return {t, b, n};
+}
+inline float radians(float deg) { return deg * 0.01745329252f; }  // scene.hpp:78
+
+struct Mat {  // umbreon::Material subset read by the POV shader
+  float ambient, diffuse, specular, roughness, brilliance, phong, phongSize;
+  bool metallic;
+  float reflection, emission;
+  uint32_t model;
+};
+Mat fromAbi(const ubr_material& m) {
+  return {m.ambient, m.diffuse, m.specular, m.roughness, m.brilliance, m.phong,
+          m.phong_size, m.metallic != 0, m.reflection, m.emission, m.model};
+}
+
+struct Light {  // secondary_rays.hpp:26-31
+  V3 L, color;
+  bool highlight = true;
+  float radius = 0.0f;
+};
+
+// Scene tables in primID order (scene_build.hpp:63-118).
+struct Scene {
+  GeomSet geo;
+  Bvh bvh;
+  // mesh (scene_build.cpp:16-88): attributes per baked vertex
+  std::vector<float> nrm, col;
+  size_t baseTri = 0;
+  std::vector<Mat> meshMats;     // Mesh::materials
+  Mat meshMat{};
+  std::vector<uint8_t> triMat;   // per base triangle
+  std::vector<uint16_t> triGroup;
+  // per kind side tables, index = kind (1..3), element = primID
+  std::vector<float> color[4];   // 4 per prim
+  std::vector<Mat> mat[4];
+  std::vector<uint16_t> group[4];
+  std::vector<uint8_t> fromEdge[4];
+  std::vector<float> opacity1[4];
+  bool principled = false;
+};
+
+float roundKey(float x) { return x; }
+
+// render/curve_build.cpp:41-267 buildCylinderGeometry (open chains + capped)
+void buildCylinders(const ubr_scene_desc& d, const std::vector<V3>& offs, Scene& s) {
+  const size_t n = d.cylinder_count;
+  if (n == 0) return;
+  std::vector<int> openIdx, capIdx;
+  for (size_t i = 0; i < n; ++i) {
+    if (d.cyl_open && d.cyl_open[i]) openIdx.push_back(static_cast<int>(i));
+    else capIdx.push_back(static_cast<int>(i));
+  }
+  auto P0 = [&](int i) { return V3(d.cyl_p0[3 * i], d.cyl_p0[3 * i + 1], d.cyl_p0[3 * i + 2]); };
+  auto P1 = [&](int i) { return V3(d.cyl_p1[3 * i], d.cyl_p1[3 * i + 1], d.cyl_p1[3 * i + 2]); };
+  auto op1 = [&](int i) { return d.cyl_opacity1 ? d.cyl_opacity1[i] : -1.0f; };
+  auto grp = [&](int i) { return d.cyl_group ? d.cyl_group[i] : uint16_t(0); };
+  auto pushSide = [&](int kind, int i) {
+    for (int k = 0; k < 4; ++k) s.color[kind].push_back(d.cyl_color[4 * i + k]);
+    s.mat[kind].push_back(fromAbi(d.cyl_material[i]));
+    s.group[kind].push_back(grp(i));
+    s.opacity1[kind].push_back(op1(i));
+    s.fromEdge[kind].push_back(d.cyl_from_edge && d.cyl_from_edge[i] ? 1 : 0);
+  };
+  if (!openIdx.empty()) {
+    const size_t no = openIdx.size();
+    const float eps = 1.0e-4f;  // curve_build.cpp:88
+    auto keyOf = [&](const V3& p) {
+      return std::array<long long, 3>{std::llround(p.x / eps), std::llround(p.y / eps),
+                                      std::llround(p.z / eps)};
+    };
+    for (const V3& off : offs) {
+      std::vector<V3> a0(no), a1(no);
+      for (size_t i = 0; i < no; ++i) {
+        a0[i] = P0(openIdx[i]) + off;
+        a1[i] = P1(openIdx[i]) + off;
+      }
+      std::map<std::array<long long, 3>, std::vector<std::pair<int, int>>> inc;
+      for (int i = 0; i < static_cast<int>(no); ++i) {
+        inc[keyOf(a0[i])].push_back({i, 0});
+        inc[keyOf(a1[i])].push_back({i, 1});
+      }
+      auto compatible = [&](int a, int b) {
+        return grp(openIdx[a]) == grp(openIdx[b]) &&
+               (op1(openIdx[a]) < 0.0f) == (op1(openIdx[b]) < 0.0f);
+      };
+      std::vector<int> next(no, -1), prev(no, -1);
+      for (int sg = 0; sg < static_cast<int>(no); ++sg) {
+        const auto& ends = inc[keyOf(a1[sg])];
+        if (ends.size() != 2) continue;
+        int t = -1;
+        for (const auto& e : ends)
+          if (e.first != sg) t = (e.second == 0) ? e.first : -1;
+        if (t >= 0 && t != sg && compatible(sg, t)) next[sg] = t;
+      }
+      for (int sg = 0; sg < static_cast<int>(no); ++sg)
+        if (next[sg] >= 0) prev[next[sg]] = sg;
+      std::vector<char> visited(no, 0);
+      auto emitChain = [&](int start) {
+        std::vector<int> chain;
+        for (int sg = start; sg >= 0 && !visited[sg]; sg = next[sg]) {
+          visited[sg] = 1;
+          chain.push_back(sg);
+        }
+        const uint32_t base = static_cast<uint32_t>(s.geo.rcV.size() / 4);
+        auto pushV = [&](const V3& p, float r) {
+          s.geo.rcV.push_back(p.x); s.geo.rcV.push_back(p.y);
+          s.geo.rcV.push_back(p.z); s.geo.rcV.push_back(r);
+        };
+        pushV(a0[chain[0]], d.cyl_radius[openIdx[chain[0]]]);
+        for (int cs : chain) pushV(a1[cs], d.cyl_radius[openIdx[cs]]);
+        const int nc = static_cast<int>(chain.size());
+        for (int j = 0; j < nc; ++j) {
+          s.geo.rcIdx.push_back(base + static_cast<uint32_t>(j));
+          uint8_t fl = 0;
+          if (j > 0) fl |= 1u;
+          if (j < nc - 1) fl |= 2u;
+          s.geo.rcFlags.push_back(fl);
+          pushSide(kRound, openIdx[chain[j]]);
+        }
+      };
+      for (int sg = 0; sg < static_cast<int>(no); ++sg)
+        if (prev[sg] < 0 && !visited[sg]) emitChain(sg);
+      for (int sg = 0; sg < static_cast<int>(no); ++sg)
+        if (!visited[sg]) emitChain(sg);
+    }
+  }
+  if (!capIdx.empty()) {
+    for (const V3& off : offs) {
+      for (int idx : capIdx) {
+        const uint32_t base = static_cast<uint32_t>(s.geo.ccV.size() / 4);
+        const V3 a = P0(idx) + off, b = P1(idx) + off;
+        const float r = d.cyl_radius[idx];
+        for (float f : {a.x, a.y, a.z, r, b.x, b.y, b.z, r}) s.geo.ccV.push_back(f);
+        s.geo.ccIdx.push_back(base);
+        pushSide(kCone, idx);
+      }
+    }
+  }
+}
+
+// render/scene_build.cpp:133-170 buildEmbreeScene (+ :16-129)
+Scene* buildScene(const ubr_scene_desc& d) {
+  Scene* s = new Scene();
+  std::vector<V3> offs;
+  for (size_t i = 0; i < d.instance_count; ++i)
+    offs.push_back({d.instance_offsets[3 * i], d.instance_offsets[3 * i + 1], d.instance_offsets[3 * i + 2]});
+  if (offs.empty()) offs.push_back(V3());
+  auto checkModel = [&](const ubr_material& m) { if (m.model == 1) s->principled = true; };
+  // mesh
+  const size_t baseV = d.mesh_vertex_count;
+  const size_t baseT = d.mesh_triangle_count;
+  uint32_t nextGeom = 0;
+  if (baseV >= 3 && baseT > 0) {
+    s->geo.geomID[kMesh] = nextGeom++;
+    for (size_t c = 0; c < offs.size(); ++c) {
+      for (size_t v = 0; v < baseV; ++v) {
+        const V3 p = V3(d.mesh_positions[3 * v], d.mesh_positions[3 * v + 1], d.mesh_positions[3 * v + 2]) + offs[c];
+        s->geo.triPos.push_back(p.x); s->geo.triPos.push_back(p.y); s->geo.triPos.push_back(p.z);
+        for (int k = 0; k < 3; ++k) s->nrm.push_back(d.mesh_normals ? d.mesh_normals[3 * v + k] : 0.0f);
+        for (int k = 0; k < 4; ++k) s->col.push_back(d.mesh_colors ? d.mesh_colors[4 * v + k] : (k == 3 ? 1.0f : 0.0f));
+      }
+    }
+    for (size_t c = 0; c < offs.size(); ++c)
+      for (size_t t = 0; t < baseT; ++t)
+        for (int k = 0; k < 3; ++k) {
+          const size_t corner = t * 3 + k;
+          const uint32_t cv = d.mesh_index ? d.mesh_index[corner] : static_cast<uint32_t>(corner);
+          s->geo.triIdx.push_back(static_cast<uint32_t>(c * baseV + cv));
+        }
+    s->baseTri = baseT;
+    s->meshMat = fromAbi(d.mesh_material);
+    checkModel(d.mesh_material);
+    for (uint32_t i = 0; i < d.mesh_material_count; ++i) {
+      s->meshMats.push_back(fromAbi(d.mesh_materials[i]));
+      checkModel(d.mesh_materials[i]);
+    }
+    if (d.mesh_tri_material) s->triMat.assign(d.mesh_tri_material, d.mesh_tri_material + baseT);
+    if (d.mesh_tri_group) s->triGroup.assign(d.mesh_tri_group, d.mesh_tri_group + baseT);
+  }
+  // spheres (scene_build.cpp:91-129)
+  if (d.sphere_count > 0) {
+    s->geo.geomID[kSphere] = nextGeom++;
+    for (const V3& off : offs)
+      for (size_t i = 0; i < d.sphere_count; ++i) {
+        const float* c = d.sphere_center_radius + 4 * i;
+        s->geo.sph.push_back(c[0] + off.x); s->geo.sph.push_back(c[1] + off.y);
+        s->geo.sph.push_back(c[2] + off.z); s->geo.sph.push_back(c[3]);
+        for (int k = 0; k < 4; ++k) s->color[kSphere].push_back(d.sphere_color[4 * i + k]);
+        s->mat[kSphere].push_back(fromAbi(d.sphere_material[i]));
+        checkModel(d.sphere_material[i]);
+        s->group[kSphere].push_back(d.sphere_group ? d.sphere_group[i] : 0);
+        s->fromEdge[kSphere].push_back(d.sphere_from_edge && d.sphere_from_edge[i] ? 1 : 0);
+      }
+  }
+  for (size_t i = 0; i < d.cylinder_count; ++i) checkModel(d.cyl_material[i]);
+  buildCylinders(d, offs, *s);
+  if (!s->geo.rcIdx.empty()) s->geo.geomID[kRound] = nextGeom++;
+  if (!s->geo.ccIdx.empty()) s->geo.geomID[kCone] = nextGeom++;
+  s->bvh.build(&s->geo);
+  return s;
+}
+
+int kindOfGeom(const Scene& s, uint32_t geomID) {
+  for (int k = 0; k < 4; ++k) if (s.geo.geomID[k] == geomID) return k;
+  return -1;
+}
+
+// ---------------------------------------------------------------------------
+// shading math
+
+// shading.hpp:27-30 faceForward
+inline V3 faceForward(V3 n, V3 rayDir) { return (dot(n, rayDir) > 0.0f) ? V3{-n.x, -n.y, -n.z} : n; }
+// shading.hpp:34-41 blinnExp
+inline float blinnExp(float roughness) {
+  float r = roughness;
+  if (r < 1e-6f) r = 1e-6f;
+  float e = 1.0f / r;
+  if (e < 1.0f) e = 1.0f;
+  if (e > 1.0e6f) e = 1.0e6f;
+  return e;
+}
+// secondary_rays.hpp:38-46 selfIntersectEps
+inline float selfIntersectEps(const V3& P, const V3& dir, float t) {
+  const float dirMax = std::fmax(std::fabs(dir.x), std::fmax(std::fabs(dir.y), std::fabs(dir.z)));
+  const float epsScale = std::fmax(std::fmax(std::fabs(P.x), std::fabs(P.y)), std::fmax(std::fabs(P.z), dirMax * t));
+  return epsScale * 0x1.0fp-21f;
+}
+// secondary_rays.hpp:51-58 tea2
+inline void tea2(uint32_t& v0, uint32_t& v1) {
+  uint32_t sum = 0;
+  for (int i = 0; i < 8; ++i) {
+    sum += 0x9E3779B9u;
+    v0 += ((v1 << 4) + 0xA341316Cu) ^ (v1 + sum) ^ ((v1 >> 5) + 0xC8013EA4u);
+    v1 += ((v0 << 4) + 0xAD90777Du) ^ (v0 + sum) ^ ((v0 >> 5) + 0x7E95761Eu);
+  }
+}
+inline float u32ToUnorm(uint32_t u) { return (u >> 8) * 0x1.0p-24f; }  // :61
+// secondary_rays.hpp:66-73
+inline V3 cosineSampleHemisphere(float u1, float u2, const Frame& f) {
+  const float phi = 6.2831853072f * u1;
+  const float r = std::sqrt(u2);
+  const float z = std::sqrt(std::fmax(0.0f, 1.0f - u2));
+  const float x = std::cos(phi) * r;
+  const float y = std::sin(phi) * r;
+  return f.t * x + f.b * y + f.n * z;
+}
+// secondary_rays.hpp:79-97 occluded
+inline bool occludedQ(const Scene& s, const V3& P, const V3& dir, float tnear, float tfar) {
+  Ray r;
+  r.org = P; r.dir = dir; r.tnear = tnear; r.tfar = tfar;
+  return s.bvh.occluded(r);
+}
+// secondary_rays.hpp:102-109
+inline V3 sampleLightDir(const Light& l, float u1, float u2) {
+  if (l.radius <= 0.0f) return l.L;
+  const Frame f = frameFromNormal(l.L);
+  const float phi = 6.2831853072f * u1;
+  const float rr = std::tan(l.radius) * std::sqrt(u2);
+  const V3 d = f.n + f.t * (rr * std::cos(phi)) + f.b * (rr * std::sin(phi));
+  return safeNormalize(d, l.L);
+}
+// secondary_rays.hpp:118-134
+inline float computeShadow(const Scene& s, const V3& P, const V3& Ng, const V3& N, float eps,
+                           const Light& l, int shadowSamples, uint32_t& s0, uint32_t& s1) {
+  V3 ng = (dot(Ng, N) < 0.0f) ? V3{-Ng.x, -Ng.y, -Ng.z} : Ng;
+  ng = safeNormalize(ng, N);
+  const V3 O = P + ng * eps;
+  if (shadowSamples <= 1 || l.radius <= 0.0f) return occludedQ(s, O, l.L, eps, kInf) ? 0.0f : 1.0f;
+  int hits = 0;
+  for (int i = 0; i < shadowSamples; ++i) {
+    tea2(s0, s1);
+    const V3 dir = sampleLightDir(l, u32ToUnorm(s0), u32ToUnorm(s1));
+    if (occludedQ(s, O, dir, eps, kInf)) ++hits;
+  }
+  return 1.0f - static_cast<float>(hits) / static_cast<float>(shadowSamples);
+}
+// ambient_occlusion.hpp:33-57 computeAO (legacy binary)
+inline float computeAO(const Scene& s, const V3& P, const V3& Ng, const V3& Ns, float eps, int nSamples,
+                       float aoRadius, uint32_t px, uint32_t py, int wHi) {
+  if (nSamples <= 0) return 1.0f;
+  const Frame f = frameFromNormal(Ns);
+  V3 ng = (dot(Ng, Ns) < 0.0f) ? V3{-Ng.x, -Ng.y, -Ng.z} : Ng;
+  ng = safeNormalize(ng, Ns);
+  const V3 O = P + ng * eps;
+  const uint32_t base = px + py * static_cast<uint32_t>(wHi);
+  int hits = 0;
+  for (int i = 0; i < nSamples; ++i) {
+    uint32_t s0 = base, s1 = static_cast<uint32_t>(i);
+    tea2(s0, s1);
+    const V3 dir = cosineSampleHemisphere(u32ToUnorm(s0), u32ToUnorm(s1), f);
+    if (dot(dir, Ns) < 0.01f) { ++hits; continue; }
+    if (occludedQ(s, O, dir, eps, aoRadius)) ++hits;
+  }
+  return 1.0f - static_cast<float>(hits) / static_cast<float>(nSamples);
+}
+// ambient_occlusion.hpp:72-94 intersectNearest
+inline float intersectNearest(const Scene& s, const V3& O, const V3& dir, float tnear, float tfar) {
+  Ray r;
+  r.org = O; r.dir = dir; r.tnear = tnear; r.tfar = tfar;
+  Hit h;
+  return s.bvh.closest(r, h) ? h.t : kInf;
+}
+// ambient_occlusion.hpp:98-105
+inline float radicalInverse2(uint32_t bits) {
+  bits = (bits << 16) | (bits >> 16);
+  bits = ((bits & 0x55555555u) << 1) | ((bits & 0xAAAAAAAAu) >> 1);
+  bits = ((bits & 0x33333333u) << 2) | ((bits & 0xCCCCCCCCu) >> 2);
+  bits = ((bits & 0x0F0F0F0Fu) << 4) | ((bits & 0xF0F0F0F0u) >> 4);
+  bits = ((bits & 0x00FF00FFu) << 8) | ((bits & 0xFF00FF00u) >> 8);
+  return static_cast<float>(bits) * 0x1.0p-32f;
+}
+// ambient_occlusion.hpp:112-127
+inline void aoSample2d(bool ld, uint32_t base, int i, int n, float cpx, float cpy, float& u1, float& u2) {
+  if (ld) {
+    u1 = static_cast<float>(i) / static_cast<float>(n) + cpx;
+    u2 = radicalInverse2(static_cast<uint32_t>(i)) + cpy;
+    if (u1 >= 1.0f) u1 -= 1.0f;
+    if (u2 >= 1.0f) u2 -= 1.0f;
+  } else {
+    uint32_t s0 = base, s1 = static_cast<uint32_t>(i);
+    tea2(s0, s1);
+    u1 = u32ToUnorm(s0);
+    u2 = u32ToUnorm(s1);
+  }
+}
+// ambient_occlusion.hpp:134-139
+inline float aoMultibounce(float ao, float albedo) {
+  const float a = 2.0404f * albedo - 0.3324f;
+  const float b = -4.7951f * albedo + 0.6417f;
+  const float c = 2.7552f * albedo + 0.6903f;
+  return std::fmax(ao, ((ao * a + b) * ao + c) * ao);
+}
+struct AOResult { float contact = 1.0f, shape = 1.0f, openness = 1.0f; V3 bent; float avgHitDist = 0.0f; };
+// ambient_occlusion.hpp:171-267 computeAOQuality
+inline AOResult computeAOQuality(const Scene& s, const V3& P, const V3& Ng, const V3& Ns, float eps,
+                                 int nSamples, float R, float power, bool multiScale, bool ld,
+                                 uint32_t px, uint32_t py, int wHi) {
+  AOResult r;
+  if (nSamples <= 0) { r.bent = Ns; return r; }
+  const Frame f = frameFromNormal(Ns);
+  V3 ng = (dot(Ng, Ns) < 0.0f) ? V3{-Ng.x, -Ng.y, -Ng.z} : Ng;
+  ng = safeNormalize(ng, Ns);
+  const V3 O = P + ng * eps;
+  const uint32_t base = px + py * static_cast<uint32_t>(wHi);
+  float radius[3], weight[3];
+  int K;
+  if (multiScale) {
+    K = 3;
+    radius[0] = 0.08f * R; radius[1] = 0.30f * R; radius[2] = 1.00f * R;
+    weight[0] = 0.55f; weight[1] = 0.35f; weight[2] = 0.10f;
+  } else {
+    K = 1;
+    radius[0] = radius[1] = radius[2] = R;
+    weight[0] = 1.0f; weight[1] = weight[2] = 0.0f;
+  }
+  uint32_t c0 = px + 1u, c1 = py + 1u;
+  tea2(c0, c1);
+  const float cpx = u32ToUnorm(c0), cpy = u32ToUnorm(c1);
+  float obsScale[3] = {0.0f, 0.0f, 0.0f};
+  float weightedObs = 0.0f;
+  V3 bentAccum{0.0f, 0.0f, 0.0f};
+  float hitDistSum = 0.0f;
+  int nHit = 0;
+  for (int i = 0; i < nSamples; ++i) {
+    float u1, u2;
+    aoSample2d(ld, base, i, nSamples, cpx, cpy, u1, u2);
+    const V3 dir = cosineSampleHemisphere(u1, u2, f);
+    if (dot(dir, Ns) < 0.01f) {
+      obsScale[0] += 1.0f; obsScale[1] += 1.0f; obsScale[2] += 1.0f;
+      weightedObs += 1.0f;
+      continue;
+    }
+    const float t = intersectNearest(s, O, dir, eps, R);
+    float perSample = 0.0f;
+    for (int k = 0; k < K; ++k) {
+      if (t < radius[k]) {
+        float fk = 1.0f;
+        if (power > 0.0f) {
+          float a = 1.0f - t / radius[k];
+          if (a < 0.0f) a = 0.0f;
+          fk = std::pow(a, power);
+        }
+        obsScale[k] += fk;
+        perSample += weight[k] * fk;
+      }
+    }
+    weightedObs += perSample;
+    bentAccum = bentAccum + dir * (1.0f - perSample);
+    if (t < R) { hitDistSum += t; ++nHit; }
+  }
+  const float invN = 1.0f / static_cast<float>(nSamples);
+  r.openness = 1.0f - weightedObs * invN;
+  r.contact = 1.0f - obsScale[0] * invN;
+  if (multiScale) {
+    const float wMid = weight[1] + weight[2];
+    r.shape = 1.0f - (weight[1] * obsScale[1] + weight[2] * obsScale[2]) / (wMid * static_cast<float>(nSamples));
+  } else {
+    r.shape = r.openness;
+  }
+  r.bent = safeNormalize(bentAccum, Ns);
+  r.avgHitDist = (nHit > 0) ? hitDistSum / static_cast<float>(nHit) : R;
+  return r;
+}
+
+struct Opt {  // the RenderOptions fields this path reads
+  int aoSamples; float aoDistance, aoIntensity, aoFalloffPower;
+  bool aoMultiScale, aoBentNormal, aoMultibounce, aoLowDiscrepancy;
+  float aoSky[3], aoGround[3], aoDiffuseFactor;
+  bool shadows; int shadowSamples; int envLights;
+  float specularScale; bool transparency, transparentBackground; int maxTransparentLayers;
+  bool aoEnhanced() const {  // render_options.hpp:79-82
+    return aoFalloffPower > 0.0f || aoMultiScale || aoBentNormal || aoMultibounce || aoLowDiscrepancy ||
+           aoDiffuseFactor > 0.0f;
+  }
+};
+
+struct AoShade { V3 aoFactor{1.0f, 1.0f, 1.0f}; V3 ambLight; float diffuseAo = 1.0f; };
+
+// ao_shade.hpp:80-117 aoApplyFactors
+inline AoShade aoApplyFactors(const Opt& o, const V3& ambLight, const V3& aoUp, float openness,
+                              const AOResult& aov, const V3& C) {
+  AoShade r;
+  r.ambLight = ambLight;
+  if (o.aoEnhanced() && o.aoBentNormal) {
+    const float w = 0.5f * (dot(aov.bent, aoUp) + 1.0f);
+    const float gx = o.aoGround[0], sx = o.aoSky[0];
+    const float gy = o.aoGround[1], sy = o.aoSky[1];
+    const float gz = o.aoGround[2], sz = o.aoSky[2];
+    r.ambLight = V3{ambLight.x * (gx + (sx - gx) * w), ambLight.y * (gy + (sy - gy) * w),
+                    ambLight.z * (gz + (sz - gz) * w)};
+  }
+  if (o.aoMultibounce) {
+    const float ox = aoMultibounce(openness, C.x);
+    const float oy = aoMultibounce(openness, C.y);
+    const float oz = aoMultibounce(openness, C.z);
+    r.aoFactor = V3{1.0f - o.aoIntensity * (1.0f - ox), 1.0f - o.aoIntensity * (1.0f - oy),
+                    1.0f - o.aoIntensity * (1.0f - oz)};
+  } else {
+    const float sv = 1.0f - o.aoIntensity * (1.0f - openness);
+    r.aoFactor = V3{sv, sv, sv};
+  }
+  if (o.aoDiffuseFactor > 0.0f) r.diffuseAo = 1.0f - o.aoDiffuseFactor * (1.0f - openness);
+  return r;
+}
+
+// ao_shade.hpp:44-72 aoGather + :128-141 computeAoShade (sampleMul 1, wSeed = hi-res width)
+inline AoShade computeAoShade(const Scene& s, const Opt& o, const V3& ambLight, const V3& aoUp,
+                              const V3& P, const V3& Ng, const V3& N, const V3& C, float secEps,
+                              uint32_t px, uint32_t py, int wSeed) {
+  if (o.aoSamples <= 0) { AoShade r; r.ambLight = ambLight; return r; }
+  AOResult aov;
+  float openness;
+  if (o.aoEnhanced()) {
+    aov = computeAOQuality(s, P, Ng, N, secEps, o.aoSamples, o.aoDistance, o.aoFalloffPower,
+                           o.aoMultiScale, o.aoLowDiscrepancy, px, py, wSeed);
+    openness = aov.openness;
+  } else {
+    openness = computeAO(s, P, Ng, N, secEps, o.aoSamples, o.aoDistance, px, py, wSeed);
+  }
+  return aoApplyFactors(o, ambLight, aoUp, openness, aov, C);
+}
+
+// shading.hpp:76-192 shadeLocal, POV branch
+inline V3 shadeLocal(const Scene& s, const Mat& mat, const V3& C, const V3& N, const V3& V,
+                     const std::vector<Light>& lights, const V3& ambLight, const V3& bg,
+                     float specularScale, const V3& aoFactor, float diffuseAo, const V3& P,
+                     const V3& Ng, float eps, bool shadowsOn, int shadowSamples, uint32_t px,
+                     uint32_t py) {
+  V3 out{mat.emission * C.x + aoFactor.x * mat.ambient * C.x * ambLight.x,
+         mat.emission * C.y + aoFactor.y * mat.ambient * C.y * ambLight.y,
+         mat.emission * C.z + aoFactor.z * mat.ambient * C.z * ambLight.z};
+  const float ex = blinnExp(mat.roughness);
+  uint32_t s0 = px, s1 = py;
+  for (const Light& l : lights) {
+    const float ndl = dot(N, l.L);
+    if (ndl <= 0.0f) continue;
+    const float shadowFactor = shadowsOn ? computeShadow(s, P, Ng, N, eps, l, shadowSamples, s0, s1) : 1.0f;
+    const V3 Lc{l.color.x * shadowFactor, l.color.y * shadowFactor, l.color.z * shadowFactor};
+    float d;
+    if (mat.brilliance == 1.0f) d = ndl;
+    else if (mat.brilliance == 0.0f) d = 1.0f;
+    else d = std::pow(ndl, mat.brilliance);
+    const float dk = mat.diffuse * d * diffuseAo;
+    out.x += dk * C.x * Lc.x;
+    out.y += dk * C.y * Lc.y;
+    out.z += dk * C.z * Lc.z;
+    if (!l.highlight) continue;
+    V3 hl;
+    if (mat.metallic) {
+      float c = ndl;
+      if (c > 1.0f) c = 1.0f;
+      const float x = std::acos(c) * 0.63661977f;
+      float f = 0.014567225f / ((x - 1.12f) * (x - 1.12f)) - 0.011612903f;
+      if (f < 0.0f) f = 0.0f;
+      if (f > 1.0f) f = 1.0f;
+      hl = V3{Lc.x * (f + (1.0f - f) * C.x), Lc.y * (f + (1.0f - f) * C.y), Lc.z * (f + (1.0f - f) * C.z)};
+    } else {
+      hl = Lc;
+    }
+    float specW = 0.0f;
+    if (mat.specular > 0.0f) {
+      const V3 H = normalize(V3{l.L.x + V.x, l.L.y + V.y, l.L.z + V.z});
+      float nh = dot(N, H);
+      if (nh > 0.0f) specW += mat.specular * std::pow(nh, ex);
+    }
+    if (mat.phong > 0.0f) {
+      const V3 Rr = 2.0f * ndl * N - l.L;
+      float rv = dot(Rr, V);
+      if (rv > 0.0f && (mat.phongSize < 60.0f || rv > 0.0008f)) specW += mat.phong * std::pow(rv, mat.phongSize);
+    }
+    if (specW > 0.0f) {
+      const float sc = specW * specularScale;
+      out.x += sc * hl.x;
+      out.y += sc * hl.y;
+      out.z += sc * hl.z;
+    }
+  }
+  if (mat.reflection > 0.0f) {
+    out.x += mat.reflection * bg.x;
+    out.y += mat.reflection * bg.y;
+    out.z += mat.reflection * bg.z;
+  }
+  return out;
+}
+
+struct Ctx {
+  const Scene* s;
+  std::vector<Light> lights;
+  V3 ambLight, bg, aoUp;
+  Opt o;
+  int wHi;
+  float clipNear, clipFar;
+};
+
+struct HitShade { V3 color; float opacity = 1.0f; };
+
+// hit_shader.hpp:147-496 shadeHit (POV; GI / edge / principled branches off)
+inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& org, uint32_t px, uint32_t py) {
+  const Scene& s = *c.s;
+  HitShade hs;
+  const bool shadowsActive = c.o.shadows || c.o.envLights > 0;
+  const int kind = kindOfGeom(s, hit.geomID);
+  const V3 V = normalize(V3{-rd.x, -rd.y, -rd.z});
+  const V3 Ng = hit.Ng;
+  const V3 P{org.x + rd.x * hit.t, org.y + rd.y * hit.t, org.z + rd.z * hit.t};
+  const float secEps = selfIntersectEps(P, rd, hit.t);
+  if (kind == kMesh) {
+    // rtcInterpolate0 of slots 0 (normal) and 1 (colour): (1-u-v) a0 + u a1 + v a2
+    const uint32_t* tri = &s.geo.triIdx[3 * hit.primID];
+    const float w0 = 1.0f - hit.u - hit.v;
+    float nbuf[3], cbuf[4];
+    for (int k = 0; k < 3; ++k)
+      nbuf[k] = w0 * s.nrm[3 * tri[0] + k] + hit.u * s.nrm[3 * tri[1] + k] + hit.v * s.nrm[3 * tri[2] + k];
+    for (int k = 0; k < 4; ++k)
+      cbuf[k] = w0 * s.col[4 * tri[0] + k] + hit.u * s.col[4 * tri[1] + k] + hit.v * s.col[4 * tri[2] + k];
+    const V3 NgF = faceForward(Ng, rd);
+    V3 N = normalize(V3{nbuf[0], nbuf[1], nbuf[2]});
+    if (dot(N, NgF) < 0.0f) N = V3{-N.x, -N.y, -N.z};
+    const V3 C{cbuf[0], cbuf[1], cbuf[2]};
+    const size_t bt = s.baseTri ? hit.primID % s.baseTri : 0;
+    const Mat& triMat = s.triMat.empty() ? s.meshMat : s.meshMats[s.triMat[bt]];
+    AoShade ao = computeAoShade(s, c.o, c.ambLight, c.aoUp, P, Ng, N, C, secEps, px, py, c.wHi);
+    hs.color = shadeLocal(s, triMat, C, N, V, c.lights, ao.ambLight, c.bg, c.o.specularScale, ao.aoFactor,
+                          ao.diffuseAo, P, Ng, secEps, shadowsActive, c.o.shadowSamples, px, py);
+    hs.opacity = cbuf[3];
+  } else {
+    const float* fc = &s.color[kind][4 * hit.primID];
+    const Mat& pm = s.mat[kind][hit.primID];
+    V3 N = faceForward(normalize(Ng), rd);
+    const V3 C{fc[0], fc[1], fc[2]};
+    const bool fromEdge = s.fromEdge[kind][hit.primID] != 0;
+    V3 aoFactor{1.0f, 1.0f, 1.0f};
+    V3 ambLight = c.ambLight;
+    float diffuseAo = 1.0f;
+    if (!fromEdge) {
+      AoShade ao = computeAoShade(s, c.o, c.ambLight, c.aoUp, P, Ng, N, C, secEps, px, py, c.wHi);
+      aoFactor = ao.aoFactor;
+      ambLight = ao.ambLight;
+      diffuseAo = ao.diffuseAo;
+    }
+    const bool primShadows = !fromEdge && shadowsActive;
+    hs.color = shadeLocal(s, pm, C, N, V, c.lights, ambLight, c.bg, c.o.specularScale, aoFactor, diffuseAo,
+                          P, Ng, secEps, primShadows, c.o.shadowSamples, px, py);
+    hs.opacity = fc[3];
+    if (kind != kSphere) {
+      const float op1 = s.opacity1[kind][hit.primID];
+      if (op1 >= 0.0f) {
+        float u = hit.u;
+        if (u < 0.0f) u = 0.0f;
+        if (u > 1.0f) u = 1.0f;
+        hs.opacity = fc[3] * (1.0f - u) + op1 * u;
+      }
+    }
+  }
+  return hs;
+}
+
+struct PixelOut { float r, g, b, a, depth, viewZ; uint32_t geom, prim; bool capped; uint32_t rays; };
+
+// transparency.hpp:311-522 integratePixel (colour, first-hit depth/viewZ/ids)
+inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32_t px, uint32_t py,
+                               const V3& camDir) {
+  PixelOut po{};
+  po.geom = kInvalid;
+  po.prim = kInvalid;
+  V3 Cf{0.0f, 0.0f, 0.0f};
+  float Af = 0.0f, nearDepth = 0.0f, firstViewZ = 0.0f;
+  V3 base = c.bg;
+  float baseCov = c.o.transparentBackground ? 0.0f : 1.0f;
+  // clipRangeT (transparency.hpp:118-129)
+  float ctn = 0.0f, ctf = kInf;
+  if (!(c.clipNear <= -kInf && c.clipFar >= kInf)) {
+    const float cosr = dot(rd, camDir);
+    if (!(cosr <= 1.0e-6f)) {
+      if (c.clipNear > 0.0f) ctn = c.clipNear / cosr;
+      if (c.clipFar < kInf) ctf = c.clipFar / cosr;
+    }
+  }
+  const float kOpaque = 1.0f - 1e-4f;
+  float tnear = ctn;
+  const int maxIters = c.o.transparency ? (c.o.maxTransparentLayers + 1) : 1;
+  for (int iter = 0; iter < maxIters; ++iter) {
+    Ray r;
+    r.org = org; r.dir = rd; r.tnear = tnear; r.tfar = ctf;
+    Hit h;
+    ++po.rays;
+    if (!c.s->bvh.closest(r, h)) break;
+    const HitShade hs = shadeHit(c, h, rd, org, px, py);
+    if (nearDepth == 0.0f) {
+      nearDepth = h.t;
+      firstViewZ = h.t * dot(rd, camDir);
+      po.geom = h.geomID;
+      po.prim = h.primID;
+    }
+    if (!c.o.transparency || hs.opacity >= kOpaque) {
+      base = hs.color;
+      baseCov = 1.0f;
+      break;
+    }
+    const float w = (1.0f - Af) * hs.opacity;
+    Cf.x += w * hs.color.x;
+    Cf.y += w * hs.color.y;
+    Cf.z += w * hs.color.z;
+    Af += w;
+    if (Af >= kOpaque) break;
+    const V3 hitP{org.x + rd.x * h.t, org.y + rd.y * h.t, org.z + rd.z * h.t};
+    const float dirMax = std::fmax(std::fabs(rd.x), std::fmax(std::fabs(rd.y), std::fabs(rd.z)));
+    const float epsScale = std::fmax(std::fmax(std::fabs(hitP.x), std::fabs(hitP.y)),
+                                     std::fmax(std::fabs(hitP.z), dirMax * h.t));
+    tnear = h.t + epsScale * 0x1.0fp-21f;
+    if (iter == maxIters - 1) po.capped = true;
+  }
+  const float floorW = (1.0f - Af) * baseCov;
+  float outA = Af + floorW;
+  outA = std::fmin(1.0f, std::fmax(0.0f, outA));
+  po.r = Cf.x + floorW * base.x;
+  po.g = Cf.y + floorW * base.y;
+  po.b = Cf.z + floorW * base.z;
+  po.a = outA;
+  po.depth = nearDepth;
+  po.viewZ = firstViewZ;
+  return po;
+}
+
+}  // namespace
+}  // namespace oracle
+
+using namespace oracle;
+
+extern "C" {
+
+void* oracle_scene_create(const ubr_scene_desc* d) {
+  if (!d) return nullptr;
+  return buildScene(*d);
+}
+
+void oracle_scene_destroy(void* s) { delete static_cast<Scene*>(s); }
+
+uint64_t oracle_scene_bvh_nodes(void* s) { return static_cast<Scene*>(s)->bvh.nodeCount(); }
+
+uint32_t oracle_scene_geom_id(void* s, int kind) { return static_cast<Scene*>(s)->geo.geomID[kind]; }
+
+// Closest hits for n rays: rays = 8 floats each (ox oy oz tnear dx dy dz tfar).
+// Outputs: t, geomID, primID, u, v, Ng (3 per ray). Any output may be NULL.
+int oracle_intersect(void* sp, const float* rays, uint64_t n, float* t, uint32_t* geom,
+                     uint32_t* prim, float* u, float* v, float* ng) {
+  const Scene& s = *static_cast<Scene*>(sp);
+  for (uint64_t i = 0; i < n; ++i) {
+    const float* q = rays + 8 * i;
+    Ray r;
+    r.org = V3(q[0], q[1], q[2]); r.tnear = q[3];
+    r.dir = V3(q[4], q[5], q[6]); r.tfar = q[7];
+    Hit h;
+    const bool hit = s.bvh.closest(r, h);
+    if (t) t[i] = hit ? h.t : kInf;
+    if (geom) geom[i] = hit ? h.geomID : kInvalid;
+    if (prim) prim[i] = hit ? h.primID : kInvalid;
+    if (u) u[i] = hit ? h.u : 0.0f;
+    if (v) v[i] = hit ? h.v : 0.0f;
+    if (ng) { ng[3 * i] = h.Ng.x; ng[3 * i + 1] = h.Ng.y; ng[3 * i + 2] = h.Ng.z; }
+  }
+  return 0;
+}
+
+int oracle_occluded(void* sp, const float* rays, uint64_t n, uint8_t* out) {
+  const Scene& s = *static_cast<Scene*>(sp);
+  for (uint64_t i = 0; i < n; ++i) {
+    const float* q = rays + 8 * i;
+    Ray r;
+    r.org = V3(q[0], q[1], q[2]); r.tnear = q[3];
+    r.dir = V3(q[4], q[5], q[6]); r.tfar = q[7];
+    out[i] = s.bvh.occluded(r) ? 1 : 0;
+  }
+  return 0;
+}
+
+// The frame: embree_renderer.cpp:1260-1427 pixel loop (rows [row0, row1) of the
+// hi-res grid, all rows when row1 <= row0), then pipeline.cpp:126-129 fog,
+// :182-192 box downsample, :254 assumed gamma.  `threads` <= 0 uses all cores.
+// Returns 0, or -1 for an unsupported request (Principled material).
+int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int threads, int row0,
+                       int row1) {
+  const Scene& s = *static_cast<Scene*>(sp);
+  const ubr_render_desc& d = *rdsc;
+  if (s.principled) return -1;
+  const int ss = std::max(1, d.supersample);
+  const int W = d.width * ss, H = d.height * ss;
+  // computeCameraBasis (embree_renderer.cpp:375-386)
+  const float aspect = static_cast<float>(W) / static_cast<float>(H);
+  const V3 camPos{d.cam_position[0], d.cam_position[1], d.cam_position[2]};
+  const V3 dir = normalize(V3{d.cam_direction[0], d.cam_direction[1], d.cam_direction[2]});
+  const V3 right = normalize(cross(dir, V3{d.cam_up[0], d.cam_up[1], d.cam_up[2]}));
+  const V3 trueUp = normalize(cross(right, dir));
+  const float halfH = d.cam_height * 0.5f;
+  const float halfW = halfH * aspect;
+  const float persHalfH = std::tan(radians(d.cam_fovy) * 0.5f);
+  const float persHalfW = persHalfH * aspect;
+
+  Ctx c;
+  c.s = &s;
+  c.o.aoSamples = d.ao_samples; c.o.aoDistance = d.ao_distance; c.o.aoIntensity = d.ao_intensity;
+  c.o.aoFalloffPower = d.ao_falloff_power; c.o.aoMultiScale = d.ao_multiscale != 0;
+  c.o.aoBentNormal = d.ao_bent_normal != 0; c.o.aoMultibounce = d.ao_multibounce != 0;
+  c.o.aoLowDiscrepancy = d.ao_low_discrepancy != 0;
+  for (int k = 0; k < 3; ++k) { c.o.aoSky[k] = d.ao_sky_color[k]; c.o.aoGround[k] = d.ao_ground_color[k]; }
+  c.o.aoDiffuseFactor = d.ao_diffuse_factor;
+  c.o.shadows = d.shadows != 0; c.o.shadowSamples = d.shadow_samples; c.o.envLights = d.env_lights;
+  c.o.specularScale = d.specular_scale; c.o.transparency = d.transparency != 0;
+  c.o.transparentBackground = d.transparent_background != 0;
+  c.o.maxTransparentLayers = d.max_transparent_layers;
+  // buildSceneLights (embree_renderer.cpp:436-458)
+  for (uint32_t i = 0; i < d.light_count; ++i) {
+    const ubr_light& dl = d.lights[i];
+    Light l;
+    l.L = normalize(V3{-dl.direction[0], -dl.direction[1], -dl.direction[2]});
+    l.color = V3{dl.color[0] * dl.intensity, dl.color[1] * dl.intensity, dl.color[2] * dl.intensity};
+    l.highlight = dl.casts_highlight != 0;
+    l.radius = (d.gi_integrator == 2 && dl.angular_radius > 0.0f) ? dl.angular_radius : radians(d.light_radius_deg);
+    c.lights.push_back(l);
+  }
+  // buildEnvDomeLights (ao/env_dome.hpp:33-64)
+  if (d.env_lights > 0) {
+    for (Light& l : c.lights) l.color = l.color * d.env_key_scale;
+    const int n = d.env_lights;
+    const float cosMax = std::cos(radians(d.env_angle));
+    const float ga = 3.14159265f * (3.0f - std::sqrt(5.0f));
+    float cosSum = 0.0f;
+    std::vector<V3> dirs;
+    for (int i = 0; i < n; ++i) {
+      const float z = 1.0f - (1.0f - cosMax) * ((i + 0.5f) / n);
+      const float r = std::sqrt(std::max(0.0f, 1.0f - z * z));
+      const float t = ga * i;
+      V3 dd = normalize(dir * z + right * (r * std::cos(t)) + trueUp * (r * std::sin(t)));
+      dirs.push_back(dd);
+      cosSum += z;
+    }
+    const float perLight = cosSum > 0.0f ? d.env_intensity / cosSum : 0.0f;
+    for (const V3& dd : dirs) {
+      Light l;
+      l.L = V3{-dd.x, -dd.y, -dd.z};
+      l.color = V3{perLight, perLight, perLight};
+      l.highlight = false;
+      l.radius = radians(d.light_radius_deg);
+      c.lights.push_back(l);
+    }
+  }
+  c.ambLight = V3{d.ambient_color[0], d.ambient_color[1], d.ambient_color[2]};
+  c.bg = V3{d.background[0], d.background[1], d.background[2]};
+  c.aoUp = d.ao_use_camera_up ? trueUp : safeNormalize(V3{d.ao_up[0], d.ao_up[1], d.ao_up[2]}, trueUp);
+  c.wHi = W;
+  c.clipNear = d.clip_near;
+  c.clipFar = d.clip_far;
+
+  const size_t npix = static_cast<size_t>(W) * H;
+  std::vector<float> color(npix * 4, 0.0f), viewZ(npix, 0.0f), depth(npix, 0.0f);
+  std::vector<uint32_t> hg(npix, kInvalid), hp(npix, kInvalid);
+  if (row1 <= row0) { row0 = 0; row1 = H; }
+  std::atomic<int> nextRow{row0};
+  std::atomic<uint64_t> rays{0}, capped{0};
+  auto worker = [&]() {
+    uint64_t myRays = 0, myCapped = 0;
+    for (;;) {
+      const int py = nextRow.fetch_add(1);
+      if (py >= row1) break;
+      const float v = 1.0f - 2.0f * (static_cast<float>(py) + 0.5f) / static_cast<float>(H);
+      for (int px = 0; px < W; ++px) {
+        const float u = 2.0f * (static_cast<float>(px) + 0.5f) / static_cast<float>(W) - 1.0f;
+        V3 org, rd;
+        if (d.cam_orthographic) {
+          org = camPos + right * (u * halfW) + trueUp * (v * halfH);
+          rd = dir;
+        } else {
+          org = camPos;
+          rd = normalize(dir + right * (u * persHalfW) + trueUp * (v * persHalfH));
+        }
+        const PixelOut po = integratePixel(c, org, rd, static_cast<uint32_t>(px), static_cast<uint32_t>(py), dir);
+        const size_t pix = static_cast<size_t>(py) * W + px;
+        color[4 * pix] = po.r; color[4 * pix + 1] = po.g; color[4 * pix + 2] = po.b; color[4 * pix + 3] = po.a;
+        depth[pix] = po.depth;
+        viewZ[pix] = po.viewZ;
+        hg[pix] = po.geom;
+        hp[pix] = po.prim;
+        myRays += po.rays;
+        myCapped += po.capped ? 1 : 0;
+      }
+    }
+    rays += myRays;
+    capped += myCapped;
+  };
+  int nt = threads > 0 ? threads : static_cast<int>(std::thread::hardware_concurrency());
+  if (nt < 1) nt = 1;
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> pool;
+  for (int i = 1; i < nt; ++i) pool.emplace_back(worker);
+  worker();
+  for (auto& th : pool) th.join();
+  const auto t1 = std::chrono::steady_clock::now();
+  fr->render_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  fr->rays_primary = rays.load();
+  fr->capped_rays = capped.load();
+
+  // fog.cpp:7-36 applyFog on the hi-res viewZ (pipeline.cpp:126-129)
+  if (d.fog_enabled) {
+    for (size_t i = 0; i < npix; ++i) {
+      const float z = viewZ[i];
+      if (z <= 0.0f) continue;
+      float f;
+      const float denom = d.fog_end - d.fog_start;
+      if (denom <= 0.0f) f = z < d.fog_end ? 1.0f : 0.0f;
+      else {
+        f = (d.fog_end - z) / denom;
+        if (f < 0.0f) f = 0.0f;
+        if (f > 1.0f) f = 1.0f;
+      }
+      float* cc = &color[4 * i];
+      if (d.transparent_background) {
+        cc[3] *= f;
+      } else {
+        cc[0] = d.fog_color[0] * (1.0f - f) + cc[0] * f;
+        cc[1] = d.fog_color[1] * (1.0f - f) + cc[1] * f;
+        cc[2] = d.fog_color[2] * (1.0f - f) + cc[2] * f;
+      }
+    }
+  }
+  // image_ops.cpp:9-35 boxDownsample
+  std::vector<float> fin;
+  if (ss > 1) {
+    const int ow = W / ss, oh = H / ss;
+    fin.assign(static_cast<size_t>(ow) * oh * 4, 0.0f);
+    const float inv = 1.0f / static_cast<float>(ss * ss);
+    for (int y = 0; y < oh; ++y)
+      for (int x = 0; x < ow; ++x)
+        for (int ch = 0; ch < 4; ++ch) {
+          float acc = 0.0f;
+          for (int dy = 0; dy < ss; ++dy)
+            for (int dx = 0; dx < ss; ++dx) {
+              const float vv = color[(static_cast<size_t>(y * ss + dy) * W + (x * ss + dx)) * 4 + ch];
+              acc += std::isfinite(vv) ? vv : 0.0f;
+            }
+          fin[(static_cast<size_t>(y) * ow + x) * 4 + ch] = acc * inv;
+        }
+  } else {
+    fin.swap(color);
+  }
+  // image_ops.cpp:37-46 applyAssumedGamma
+  const float g = d.assumed_gamma;
+  if (!(std::fabs(g - 1.0f) <= 1.0e-4f)) {
+    const size_t np = fin.size() / 4;
+    for (size_t i = 0; i < np; ++i)
+      for (int ch = 0; ch < 3; ++ch) {
+        float vv = fin[4 * i + ch];
+        fin[4 * i + ch] = (vv > 0.0f) ? std::pow(vv, g) : 0.0f;
+      }
+  }
+  if (fr->color) std::memcpy(fr->color, fin.data(), fin.size() * sizeof(float));
+  if (fr->depth) std::memcpy(fr->depth, depth.data(), npix * sizeof(float));
+  if (fr->view_z) std::memcpy(fr->view_z, viewZ.data(), npix * sizeof(float));
+  if (fr->hit_geom) std::memcpy(fr->hit_geom, hg.data(), npix * sizeof(uint32_t));
+  if (fr->hit_prim) std::memcpy(fr->hit_prim, hp.data(), npix * sizeof(uint32_t));
+  return 0;
+}
+
+int oracle_render(void* sp, const ubr_render_desc* d, ubr_frame* fr, int threads) {
+  return oracle_render_rows(sp, d, fr, threads, 0, 0);
+}
+
+}  // extern "C"

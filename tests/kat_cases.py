@@ -1,0 +1,311 @@
+"""Known-answer cases of the reference's own tests, restated as data.
+
+Each case builds a small scene the way the reference test does and lists the
+analytic values the reference asserts, with the reference's tolerances:
+  tests/test_render_shading.cpp:20-241, tests/test_render_transparency.cpp:230-301,
+  tests/test_render_shadows_gi.cpp:30-157, tests/test_render_ao.cpp:20-170.
+A case is (name, builder) where builder() returns a list of renders to make
+[(scene, opt), ...] and a check(frames) -> list of (label, ok) pairs.
+"""
+import numpy as np
+import sys, os
+sys.path.insert(0, os.path.dirname(__file__))
+
+from umbreon_gb300 import abi, scenes
+from umbreon_gb300.api import Camera, DistantLight, RenderOptions, Scene
+
+C = (2, 2)  # centre pixel of a 5x5 image
+
+
+def approx(a, b, eps):
+    return abs(float(a) - float(b)) <= eps
+
+
+def o5(**kw):
+    return RenderOptions(width=5, height=5, **kw)
+
+
+def centre(f):
+    return f.color[C[0], C[1]]
+
+
+def case_mesh_lambert():
+    sc = scenes.quad_scene()
+    def check(fs):
+        c = centre(fs[0])
+        return [("mesh R=0.30", approx(c[0], 0.30, 1e-4)), ("mesh G=0.36", approx(c[1], 0.36, 1e-4)),
+                ("mesh B=0.42", approx(c[2], 0.42, 1e-4)), ("mesh alpha=1", approx(c[3], 1.0, 1e-6)),
+                ("mesh depth=10", approx(fs[0].depth[2, 2], 10.0, 1e-3))]
+    return [(sc, o5())], check
+
+
+def case_background():
+    sc = scenes.quad_scene()
+    sc.mesh_positions = None
+    def check(fs):
+        c = centre(fs[0])
+        return [("bg R", approx(c[0], 0.4, 1e-6)), ("bg G", approx(c[1], 0.1, 1e-6)),
+                ("bg B", approx(c[2], 0.2, 1e-6)), ("bg depth 0", approx(fs[0].depth[2, 2], 0.0, 1e-6))]
+    return [(sc, o5())], check
+
+
+def case_outline_sphere():
+    sc = scenes.material_sphere_scene((0.3, 0.4, 0.5, 1.0), abi.flat_outline(), (0.4, 0.1, 0.2))
+    def check(fs):
+        c = centre(fs[0])
+        return [("outline R", approx(c[0], 0.3, 1e-4)), ("outline G", approx(c[1], 0.4, 1e-4)),
+                ("outline B", approx(c[2], 0.5, 1e-4))]
+    return [(sc, o5())], check
+
+
+def case_gamma():
+    sc = scenes.quad_scene(bg=(0, 0, 0))
+    sc.assumedGamma = 2.0
+    def check(fs):
+        c = centre(fs[0])
+        return [("gamma R", approx(c[0], 0.09, 1e-4)), ("gamma G", approx(c[1], 0.36 * 0.36, 1e-4)),
+                ("gamma alpha", approx(c[3], 1.0, 1e-6))]
+    return [(sc, o5())], check
+
+
+def case_supersample():
+    sc = scenes.quad_scene(bg=(0, 0, 0))
+    def check(fs):
+        f = fs[0]
+        return [("ss width", f.color.shape[1] == 5), ("ss height", f.color.shape[0] == 5),
+                ("ss value", approx(centre(f)[0], 0.30, 1e-4))]
+    return [(sc, o5(supersample=2))], check
+
+
+def _mat_sphere(color, bg, **m):
+    return scenes.material_sphere_scene(color, abi.material(**m), bg)
+
+
+def case_matte():
+    sc = _mat_sphere((0.6, 0.4, 0.2, 1.0), (0, 0, 0), ambient=0.0, diffuse=0.8, brilliance=0.0)
+    def check(fs):
+        c = centre(fs[0])
+        return [("matte R", approx(c[0], 0.24, 1e-4)), ("matte G", approx(c[1], 0.16, 1e-4)),
+                ("matte B", approx(c[2], 0.08, 1e-4))]
+    return [(sc, o5())], check
+
+
+def case_metallic():
+    kw = dict(ambient=0.35, diffuse=0.3, brilliance=2.0, specular=0.8, roughness=1.0 / 20.0, metallic=True,
+              reflection=0.10)
+    a = _mat_sphere((0.6, 0.4, 0.2, 1.0), (0, 0, 0), **kw)
+    b = _mat_sphere((0.6, 0.4, 0.2, 1.0), (1, 1, 1), **kw)
+    def check(fs):
+        c, d = centre(fs[0]), centre(fs[1])
+        return [("metallic R", approx(c[0], 0.54, 1e-3)), ("metallic G", approx(c[1], 0.36, 1e-3)),
+                ("metallic B", approx(c[2], 0.18, 1e-3)), ("reflection R", approx(d[0], 0.64, 1e-3)),
+                ("reflection G", approx(d[1], 0.46, 1e-3))]
+    return [(a, o5()), (b, o5())], check
+
+
+def case_phong():
+    sc = _mat_sphere((0.2, 0.4, 0.6, 1.0), (0, 0, 0), ambient=0.3, diffuse=0.5, brilliance=0.0, phong=10000.0,
+                     phong_size=50.0)
+    def check(fs):
+        c = centre(fs[0])
+        lr, lg, lb = c[0] - 0.11, c[1] - 0.22, c[2] - 0.33
+        return [("phong lift 5000", approx(lr, 5000.0, 1.0)), ("phong achromatic RG", approx(lr, lg, 1e-4)),
+                ("phong achromatic GB", approx(lg, lb, 1e-4))]
+    return [(sc, o5())], check
+
+
+def case_fill_light():
+    kw = dict(ambient=0.0, diffuse=0.0, brilliance=1.0, specular=0.5, roughness=0.05)
+    a = _mat_sphere((0.6, 0.4, 0.2, 1.0), (0, 0, 0), **kw)
+    b = _mat_sphere((0.6, 0.4, 0.2, 1.0), (0, 0, 0), **kw)
+    b.lights[0].castsHighlight = False
+    def check(fs):
+        return [("highlight R=0.25", approx(centre(fs[0])[0], 0.25, 1e-3)),
+                ("fill R=0", approx(centre(fs[1])[0], 0.0, 1e-4)),
+                ("fill G=0", approx(centre(fs[1])[1], 0.0, 1e-4))]
+    return [(a, o5()), (b, o5())], check
+
+
+def case_metallic_fresnel():
+    sc = scenes.quad_scene(color=(1.0, 0.0, 0.0, 1.0), bg=(0, 0, 0))
+    sc.mesh_material = abi.material(ambient=0.0, diffuse=0.0, specular=1.0, roughness=0.5, metallic=True)
+    sc.lights = [DistantLight(direction=(-0.8660254, 0.0, -0.5), intensity=1.0)]
+    def check(fs):
+        c = centre(fs[0])
+        return [("fresnel R", approx(c[0], 0.75, 2e-3)), ("fresnel G", approx(c[1], 0.04445, 2e-3)),
+                ("fresnel G==B", approx(c[1], c[2], 1e-5))]
+    return [(sc, o5())], check
+
+
+# --- transparency (test_render_transparency.cpp F1-F4) ---
+
+def _quads(spec, bg):
+    """spec = [(rgba, z, group)] -> flat-material scene of stacked quads."""
+    pos, col, grp = [], [], []
+    for rgba, z, g in spec:
+        for p in [(-2, -2, z), (2, -2, z), (2, 2, z), (-2, -2, z), (2, 2, z), (-2, 2, z)]:
+            pos.append(p)
+            col.append(rgba)
+        grp += [g, g]
+    pos = np.array(pos, np.float32)
+    sc = Scene(mesh_positions=pos, mesh_normals=np.tile([0, 0, 1], (len(pos), 1)).astype(np.float32),
+               mesh_colors=np.array(col, np.float32), mesh_material=abi.flat_outline(),
+               mesh_tri_group=np.array(grp, np.uint16))
+    sc.camera = scenes.ortho_cam()
+    sc.background = bg
+    sc.ambientColor = (1, 1, 1)
+    return sc
+
+
+def case_over_f1():
+    sc = _quads([((1, 0, 0, 1.0), 0.0, 0), ((0, 0, 1, 0.6), 1.0, 1)], (0, 0, 0))
+    def check(fs):
+        c = centre(fs[0])
+        return [("F1 R=0.4", approx(c[0], 0.4, 1e-4)), ("F1 B=0.6", approx(c[2], 0.6, 1e-4)),
+                ("F1 alpha", approx(c[3], 1.0, 1e-6))]
+    return [(sc, o5())], check
+
+
+def case_over_f2():
+    a = _quads([((1, 0, 0, 1.0), 0.0, 0), ((0, 0, 1, 0.5), 0.5, 2), ((0, 1, 0, 0.5), 1.0, 1)], (0, 0, 0))
+    b = _quads([((1, 0, 0, 1.0), 0.0, 0), ((0, 1, 0, 0.5), 0.5, 1), ((0, 0, 1, 0.5), 1.0, 2)], (0, 0, 0))
+    def check(fs):
+        c, d = centre(fs[0]), centre(fs[1])
+        return [("F2 green-front G", approx(c[1], 0.5, 1e-4)), ("F2 green-front B", approx(c[2], 0.25, 1e-4)),
+                ("F2 blue-front B", approx(d[2], 0.5, 1e-4)), ("F2 blue-front G", approx(d[1], 0.25, 1e-4))]
+    return [(a, o5()), (b, o5())], check
+
+
+def case_over_f3():
+    sc = _quads([((1, 0, 0, 1.0), 0.0, 0), ((0, 0, 1, 0.5), 0.5, 1), ((0, 0, 1, 0.5), 1.0, 1)], (0, 0, 0))
+    def check(fs):
+        c = centre(fs[0])
+        return [("F3 B=0.75", approx(c[2], 0.75, 1e-4)), ("F3 R=0.25", approx(c[0], 0.25, 1e-4))]
+    return [(sc, o5())], check
+
+
+def case_over_f4():
+    sc = _quads([((0, 0, 1, 0.6), 1.0, 1)], (0.2, 0.2, 0.2))
+    def check(fs):
+        c = centre(fs[0])
+        return [("F4 B=0.6", approx(c[2], 0.6, 1e-4)), ("F4 R=0", approx(c[0], 0.0, 1e-4)),
+                ("F4 alpha=0.6", approx(c[3], 0.6, 1e-4))]
+    return [(sc, o5(transparentBackground=True))], check
+
+
+# --- shadows (test_render_shadows_gi.cpp:30-157) ---
+
+def _floor_slab(floor_rgba=(1, 1, 1, 1), slab=True, ambient=0.2, diffuse=0.8):
+    pos, nrm, col = [], [], []
+    for p in [(-2, -2, 0), (2, -2, 0), (2, 2, 0), (-2, -2, 0), (2, 2, 0), (-2, 2, 0)]:
+        pos.append(p); nrm.append((0, 0, 1)); col.append(floor_rgba)
+    if slab:
+        z = 0.4
+        for p in [(0.1, -2, z), (4, -2, z), (4, 2, z), (0.1, -2, z), (4, 2, z), (0.1, 2, z)]:
+            pos.append(p); nrm.append((0, 0, -1)); col.append((0, 0, 0, 1))
+    sc = Scene(mesh_positions=np.array(pos, np.float32), mesh_normals=np.array(nrm, np.float32),
+               mesh_colors=np.array(col, np.float32), mesh_material=abi.material(ambient=ambient, diffuse=diffuse))
+    sc.camera = scenes.ortho_cam()
+    sc.ambientColor = (1, 1, 1)
+    sc.background = (0, 0, 0)
+    return sc
+
+
+def case_hard_shadow():
+    sc = _floor_slab()
+    sc.lights = [DistantLight(direction=(-0.6, 0.0, -0.8), intensity=1.0)]
+    def check(fs):
+        off, on = centre(fs[0])[0], centre(fs[1])[0]
+        return [("shadow off ~0.84", approx(off, 0.84, 0.03)), ("shadow on ~0.2", approx(on, 0.2, 0.03)),
+                ("on darker", on + 0.2 < off)]
+    return [(sc, o5(shadows=False)), (sc, o5(shadows=True))], check
+
+
+def case_soft_shadow():
+    pos, nrm, col = scenes.quad_mesh((1, 1, 1, 1))
+    sc = Scene(mesh_positions=pos, mesh_normals=nrm, mesh_colors=col,
+               mesh_material=abi.material(ambient=0.2, diffuse=0.8),
+               sphere_center_radius=np.array([[0.9, 0.0, 1.2, 0.45]], np.float32),
+               sphere_color=np.array([[0, 0, 0, 1]], np.float32),
+               sphere_material=np.array([abi.flat_outline()], abi.MATERIAL_DTYPE))
+    sc.camera = scenes.ortho_cam()
+    sc.background = (0, 0, 0)
+    sc.lights = [DistantLight(direction=(-0.6, 0.0, -0.8), intensity=1.0)]
+    soft = o5(shadows=True, lightRadius=22.0, shadowSamples=64)
+    def check(fs):
+        lit, hard, s1, s2 = (centre(f)[0] for f in fs)
+        return [("hard ~0.2", approx(hard, 0.2, 0.03)), ("lit ~0.84", approx(lit, 0.84, 0.03)),
+                ("penumbra between", hard + 0.05 < s1 and s1 + 0.05 < lit),
+                ("soft deterministic", np.array_equal(fs[2].color, fs[3].color))]
+    return [(sc, o5(shadows=False)), (sc, o5(shadows=True)), (sc, soft), (sc, soft)], check
+
+
+def case_acne_guard():
+    q = 100.0
+    pos = np.array([(-q, -q, 0), (q, -q, 0), (q, q, 0), (-q, -q, 0), (q, q, 0), (-q, q, 0)], np.float32)
+    sc = Scene(mesh_positions=pos, mesh_normals=np.tile([0, 0, 1], (6, 1)).astype(np.float32),
+               mesh_colors=np.ones((6, 4), np.float32), mesh_material=abi.material(ambient=0.2, diffuse=0.8))
+    sc.camera = Camera(position=(0.0, 1200.0, 1600.0), direction=(0.0, -0.6, -0.8), up=(0.0, 1.0, 0.0),
+                       orthographic=True, height=6.0)
+    sc.lights = [scenes.key_light()]
+    sc.background = (0, 0, 0)
+    def check(fs):
+        return [("acne guard min > 0.5", float(fs[0].color[..., 0].min()) > 0.5)]
+    return [(sc, o5(shadows=True))], check
+
+
+# --- ambient occlusion (test_render_ao.cpp:20-170) ---
+
+def case_ao_open():
+    sc = scenes.quad_scene(bg=(0, 0, 0))
+    def check(fs):
+        c = centre(fs[0])
+        return [("AO open R~0.30", approx(c[0], 0.30, 0.02)), ("AO open G~0.36", approx(c[1], 0.36, 0.02))]
+    return [(sc, o5(aoSamples=64, aoDistance=100.0))], check
+
+
+def case_ao_occlusion():
+    a = _floor_slab(slab=False, ambient=1.0, diffuse=0.0)
+    b = _floor_slab(slab=True, ambient=1.0, diffuse=0.0)
+    o = o5(aoSamples=128, aoDistance=10.0)
+    def check(fs):
+        op, oc = centre(fs[0])[0], centre(fs[1])[0]
+        return [("AO open floor ~1", approx(op, 1.0, 0.03)), ("AO slab darkens", oc + 0.05 < op),
+                ("AO not black", oc > 0.05)]
+    return [(a, o), (b, o)], check
+
+
+def case_ao_outline_gate():
+    def sph(probe_from_edge):
+        flat = abi.material(ambient=1.0, diffuse=0.0)
+        sc = Scene(sphere_center_radius=np.array([[0, 0, 0, 1.0], [0, 2.2, 0, 2.0]], np.float32),
+                   sphere_color=np.array([[1, 1, 1, 1], [0, 0, 0, 1]], np.float32),
+                   sphere_material=np.array([flat, flat], abi.MATERIAL_DTYPE),
+                   sphere_from_edge=np.array([1 if probe_from_edge else 0, 1], np.uint8))
+        sc.camera = scenes.ortho_cam()
+        sc.background = (0, 0, 0)
+        return sc
+    off = o5(aoSamples=0)
+    on = o5(aoSamples=128, aoDistance=10.0)
+    def check(fs):
+        diff = float(np.abs(fs[1].color - fs[0].color).sum())
+        return [("AO darkens real sphere", diff > 0.05),
+                ("AO outline gate identical", np.array_equal(fs[2].color, fs[3].color))]
+    return [(sph(False), off), (sph(False), on), (sph(True), off), (sph(True), on)], check
+
+
+def case_ao_determinism():
+    sc = scenes.quad_scene(bg=(0, 0, 0))
+    o = o5(aoSamples=32, aoDistance=100.0)
+    def check(fs):
+        return [("AO bit-identical", np.array_equal(fs[0].color, fs[1].color))]
+    return [(sc, o), (sc, o)], check
+
+
+CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
+
+
+def run_case(builder, render_fn):
+    renders, check = builder()
+    frames = [render_fn(sc, opt) for sc, opt in renders]
+    return check(frames)

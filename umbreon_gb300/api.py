@@ -1,0 +1,395 @@
+"""Python host mirror of the umbreon public API over the C-ABI.
+
+``Scene`` / ``RenderOptions`` / ``render()`` carry the same names, fields,
+defaults and meaning as ``umbreon::Scene`` (scene.hpp:430-479),
+``umbreon::RenderOptions`` (render/render_options.hpp:14-328, the fields this
+path honours) and ``umbreon::render`` (umbreon.hpp:29).  Geometry is held as
+numpy structure-of-arrays instead of vectors of structs; ``render`` returns a
+``FrameResult`` with the reference's field names and sizes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+
+INF = float("inf")
+
+
+@dataclass
+class Camera:
+    position: tuple = (0.0, 0.0, 1.0)
+    direction: tuple = (0.0, 0.0, -1.0)
+    up: tuple = (0.0, 1.0, 0.0)
+    fovy: float = 40.0
+    orthographic: bool = False
+    height: float = 1.0
+
+
+@dataclass
+class DistantLight:
+    direction: tuple = (0.0, -0.3, -1.0)
+    color: tuple = (1.0, 1.0, 1.0)
+    intensity: float = 1.0
+    castsHighlight: bool = True
+    angularRadius: float = 0.0
+
+
+@dataclass
+class Fog:
+    enabled: bool = False
+    color: tuple = (0.0, 0.0, 0.0)
+    start: float = 0.0
+    end: float = 0.0
+
+
+def _f32(a, cols=None):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    if cols is not None:
+        a = a.reshape(-1, cols)
+    return a
+
+
+@dataclass
+class Scene:
+    """umbreon::Scene as structure-of-arrays (scene.hpp:430-479)."""
+    # mesh
+    mesh_positions: np.ndarray = None   # (V,3)
+    mesh_normals: np.ndarray = None     # (V,3)
+    mesh_colors: np.ndarray = None      # (V,4)
+    mesh_index: np.ndarray = None       # (T,3) uint32 or None (de-indexed)
+    mesh_material: np.ndarray = field(default_factory=lambda: abi.material())
+    mesh_materials: np.ndarray = None   # (M,) MATERIAL_DTYPE
+    mesh_tri_material: np.ndarray = None  # (T,) uint8
+    mesh_tri_group: np.ndarray = None     # (T,) uint16
+    # spheres
+    sphere_center_radius: np.ndarray = None  # (N,4)
+    sphere_color: np.ndarray = None          # (N,4)
+    sphere_material: np.ndarray = None       # (N,) MATERIAL_DTYPE
+    sphere_group: np.ndarray = None
+    sphere_from_edge: np.ndarray = None
+    # cylinders
+    cyl_p0: np.ndarray = None
+    cyl_p1: np.ndarray = None
+    cyl_radius: np.ndarray = None
+    cyl_color: np.ndarray = None
+    cyl_opacity1: np.ndarray = None
+    cyl_material: np.ndarray = None
+    cyl_group: np.ndarray = None
+    cyl_open: np.ndarray = None
+    cyl_from_edge: np.ndarray = None
+    instance_offsets: np.ndarray = None
+    camera: Camera = field(default_factory=Camera)
+    lights: list = field(default_factory=list)
+    ambientIntensity: float = 0.25
+    ambientColor: tuple = (1.0, 1.0, 1.0)
+    background: tuple = (0.0, 0.0, 0.0)
+    fog: Fog = field(default_factory=Fog)
+    aoDistance: float = 1.0e20
+    assumedGamma: float = 1.0
+    clipNear: float = -INF
+    clipFar: float = INF
+
+    def triangle_count(self) -> int:
+        if self.mesh_positions is None:
+            return 0
+        if self.mesh_index is not None:
+            return int(np.asarray(self.mesh_index).size // 3)
+        return int(len(self.mesh_positions) // 3)
+
+    def sphere_count(self) -> int:
+        return 0 if self.sphere_center_radius is None else int(len(self.sphere_center_radius))
+
+    def cylinder_count(self) -> int:
+        return 0 if self.cyl_p0 is None else int(len(self.cyl_p0))
+
+    def to_desc(self):
+        """Build a ubr_scene_desc; returns (desc, keepalive)."""
+        keep = []
+
+        def P(a, dtype=np.float32, ctype=C.c_float):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(np.asarray(a, dtype=dtype))
+            keep.append(a)
+            return a.ctypes.data_as(C.POINTER(ctype))
+
+        def M(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(np.asarray(a, dtype=abi.MATERIAL_DTYPE)).reshape(-1)
+            keep.append(a)
+            return a.ctypes.data_as(C.POINTER(abi.Material))
+
+        d = abi.SceneDesc()
+        d.abi_version = abi.ABI_VERSION
+        if self.mesh_positions is not None:
+            pos = _f32(self.mesh_positions, 3)
+            d.mesh_vertex_count = len(pos)
+            d.mesh_positions = P(pos)
+            d.mesh_normals = P(_f32(self.mesh_normals, 3)) if self.mesh_normals is not None else None
+            d.mesh_colors = P(_f32(self.mesh_colors, 4)) if self.mesh_colors is not None else None
+            d.mesh_triangle_count = self.triangle_count()
+            d.mesh_index = P(self.mesh_index, np.uint32, C.c_uint32) if self.mesh_index is not None else None
+            mm = np.asarray(self.mesh_material, dtype=abi.MATERIAL_DTYPE).reshape(())
+            d.mesh_material = abi.Material.from_buffer_copy(mm.tobytes())
+            if self.mesh_materials is not None:
+                d.mesh_materials = M(self.mesh_materials)
+                d.mesh_material_count = len(np.asarray(self.mesh_materials).reshape(-1))
+            d.mesh_tri_material = P(self.mesh_tri_material, np.uint8, C.c_uint8)
+            d.mesh_tri_group = P(self.mesh_tri_group, np.uint16, C.c_uint16)
+        n = self.sphere_count()
+        if n:
+            d.sphere_count = n
+            d.sphere_center_radius = P(_f32(self.sphere_center_radius, 4))
+            d.sphere_color = P(_f32(self.sphere_color, 4))
+            mats = self.sphere_material
+            if mats is None:
+                mats = np.full(n, abi.flat_outline(), abi.MATERIAL_DTYPE)
+            d.sphere_material = M(np.broadcast_to(np.asarray(mats, abi.MATERIAL_DTYPE), (n,)))
+            d.sphere_group = P(self.sphere_group, np.uint16, C.c_uint16)
+            d.sphere_from_edge = P(self.sphere_from_edge, np.uint8, C.c_uint8)
+        n = self.cylinder_count()
+        if n:
+            d.cylinder_count = n
+            d.cyl_p0 = P(_f32(self.cyl_p0, 3))
+            d.cyl_p1 = P(_f32(self.cyl_p1, 3))
+            d.cyl_radius = P(_f32(self.cyl_radius))
+            d.cyl_color = P(_f32(self.cyl_color, 4))
+            d.cyl_opacity1 = P(_f32(self.cyl_opacity1)) if self.cyl_opacity1 is not None else None
+            mats = self.cyl_material
+            if mats is None:
+                mats = np.full(n, abi.flat_outline(), abi.MATERIAL_DTYPE)
+            d.cyl_material = M(np.broadcast_to(np.asarray(mats, abi.MATERIAL_DTYPE), (n,)))
+            d.cyl_group = P(self.cyl_group, np.uint16, C.c_uint16)
+            d.cyl_open = P(self.cyl_open, np.uint8, C.c_uint8)
+            d.cyl_from_edge = P(self.cyl_from_edge, np.uint8, C.c_uint8)
+        if self.instance_offsets is not None and len(self.instance_offsets):
+            offs = _f32(self.instance_offsets, 3)
+            d.instance_count = len(offs)
+            d.instance_offsets = P(offs)
+        return d, keep
+
+
+@dataclass
+class RenderOptions:
+    """The umbreon::RenderOptions fields of the ray-cast + shade path, with
+    the reference defaults (render_options.hpp:14-328)."""
+    width: int = 1024
+    height: int = 768
+    supersample: int = 1
+    aoSamples: int = 0
+    aoDistance: float = 1.0e20
+    aoIntensity: float = 1.0
+    aoFalloffPower: float = 0.0
+    aoMultiScale: bool = False
+    aoBentNormal: bool = False
+    aoSkyColor: tuple = (1.0, 1.0, 1.0)
+    aoGroundColor: tuple = (1.0, 1.0, 1.0)
+    aoUseCameraUp: bool = True
+    aoUp: tuple = (0.0, 1.0, 0.0)
+    aoMultibounce: bool = False
+    aoLowDiscrepancy: bool = False
+    aoDiffuseFactor: float = 0.0
+    shadows: bool = False
+    shadowSamples: int = 1
+    lightRadius: float = 0.0
+    envLights: int = 0
+    envIntensity: float = 1.0
+    envKeyScale: float = 0.0
+    envAngle: float = 90.0
+    specularScale: float = 1.0
+    transparency: bool = True
+    transparentBackground: bool = False
+    maxTransparentLayers: int = 256
+    giIntegrator: int = 2
+
+    def aoEnhanced(self) -> bool:
+        return (self.aoFalloffPower > 0.0 or self.aoMultiScale or self.aoBentNormal or self.aoMultibounce
+                or self.aoLowDiscrepancy or self.aoDiffuseFactor > 0.0)
+
+
+def make_render_desc(scene: Scene, opt: RenderOptions):
+    """Flatten scene constants + options into a ubr_render_desc."""
+    keep = []
+    d = abi.RenderDesc()
+    d.abi_version = abi.ABI_VERSION
+    d.width, d.height, d.supersample = opt.width, opt.height, opt.supersample
+    cam = scene.camera
+    d.cam_position[:] = cam.position
+    d.cam_direction[:] = cam.direction
+    d.cam_up[:] = cam.up
+    d.cam_fovy = cam.fovy
+    d.cam_orthographic = int(cam.orthographic)
+    d.cam_height = cam.height
+    n = len(scene.lights)
+    if n:
+        arr = (abi.Light * n)()
+        for i, l in enumerate(scene.lights):
+            arr[i].direction[:] = l.direction
+            arr[i].color[:] = l.color
+            arr[i].intensity = l.intensity
+            arr[i].casts_highlight = int(l.castsHighlight)
+            arr[i].angular_radius = l.angularRadius
+        keep.append(arr)
+        d.lights = C.cast(arr, C.POINTER(abi.Light))
+    d.light_count = n
+    d.ambient_color[:] = scene.ambientColor
+    d.background[:] = scene.background
+    d.fog_enabled = int(scene.fog.enabled)
+    d.fog_color[:] = scene.fog.color
+    d.fog_start, d.fog_end = scene.fog.start, scene.fog.end
+    d.clip_near, d.clip_far = scene.clipNear, scene.clipFar
+    d.assumed_gamma = scene.assumedGamma
+    d.ao_samples = opt.aoSamples
+    d.ao_distance = opt.aoDistance
+    d.ao_intensity = opt.aoIntensity
+    d.ao_falloff_power = opt.aoFalloffPower
+    d.ao_multiscale = int(opt.aoMultiScale)
+    d.ao_bent_normal = int(opt.aoBentNormal)
+    d.ao_sky_color[:] = opt.aoSkyColor
+    d.ao_ground_color[:] = opt.aoGroundColor
+    d.ao_use_camera_up = int(opt.aoUseCameraUp)
+    d.ao_up[:] = opt.aoUp
+    d.ao_multibounce = int(opt.aoMultibounce)
+    d.ao_low_discrepancy = int(opt.aoLowDiscrepancy)
+    d.ao_diffuse_factor = opt.aoDiffuseFactor
+    d.shadows = int(opt.shadows)
+    d.shadow_samples = opt.shadowSamples
+    d.light_radius_deg = opt.lightRadius
+    d.env_lights = opt.envLights
+    d.env_intensity = opt.envIntensity
+    d.env_key_scale = opt.envKeyScale
+    d.env_angle = opt.envAngle
+    d.specular_scale = opt.specularScale
+    d.transparency = int(opt.transparency)
+    d.transparent_background = int(opt.transparentBackground)
+    d.max_transparent_layers = opt.maxTransparentLayers
+    d.gi_integrator = opt.giIntegrator
+    return d, keep
+
+
+@dataclass
+class FrameResult:
+    """umbreon::FrameResult subset (frame_result.hpp:43-124) plus hit ids."""
+    width: int
+    height: int
+    color: np.ndarray        # (H, W, 4) final
+    depth: np.ndarray        # (Hss, Wss) hi-res
+    viewZ: np.ndarray        # (Hss, Wss) hi-res
+    hit_geom: np.ndarray     # (Hss, Wss)
+    hit_prim: np.ndarray
+    renderSeconds: float = 0.0
+    stats: dict = field(default_factory=dict)
+
+
+class Context:
+    """One GPU, one stream (ubr_context)."""
+
+    def __init__(self, device: int = 0, arena_bytes: int = 0, stream: int | None = None):
+        L = abi.lib()
+        self._L = L
+        h = C.c_void_p()
+        cd = abi.ContextDesc(abi.ABI_VERSION, device, arena_bytes, stream)
+        st = L.ubr_context_create(C.byref(h), C.byref(cd))
+        if st != abi.UBR_OK:
+            raise abi.UbrError(st, "ubr_context_create failed")
+        self.handle = h
+
+    def _check(self, st):
+        if st != abi.UBR_OK:
+            raise abi.UbrError(st, self._L.ubr_context_last_error(self.handle).decode())
+
+    def build(self, scene: Scene) -> "BuiltScene":
+        d, keep = scene.to_desc()
+        h = C.c_void_p()
+        self._check(self._L.ubr_scene_build(self.handle, C.byref(d), C.byref(h)))
+        return BuiltScene(self, h)
+
+    def render(self, built: "BuiltScene", scene: Scene, opt: RenderOptions, want_ids: bool = True,
+               cancel: np.ndarray | None = None) -> FrameResult:
+        rd, keep = make_render_desc(scene, opt)
+        ss = max(1, opt.supersample)
+        W, H = opt.width * ss, opt.height * ss
+        color = np.zeros((opt.height, opt.width, 4), np.float32)
+        depth = np.zeros((H, W), np.float32)
+        vz = np.zeros((H, W), np.float32)
+        hg = np.zeros((H, W), np.uint32) if want_ids else None
+        hp = np.zeros((H, W), np.uint32) if want_ids else None
+        fr = abi.Frame()
+        fr.memory = abi.MEMORY_HOST
+        fr.color = abi.ptr(color)
+        fr.depth = abi.ptr(depth)
+        fr.view_z = abi.ptr(vz)
+        fr.hit_geom = abi.ptr(hg, C.c_uint32)
+        fr.hit_prim = abi.ptr(hp, C.c_uint32)
+        cptr = cancel.ctypes.data_as(C.POINTER(C.c_int32)) if cancel is not None else None
+        st = self._L.ubr_render(self.handle, built.handle, C.byref(rd), C.byref(fr), cptr, None)
+        stats = dict(render_ms=fr.render_ms, total_ms=fr.total_ms, rays_primary=fr.rays_primary,
+                     rays_occlusion=fr.rays_occlusion, capped_rays=fr.capped_rays,
+                     stack_overflows=fr.stack_overflows, layers=fr.layers, kernels=fr.kernels)
+        if st not in (abi.UBR_OK,):
+            self._check(st)
+        return FrameResult(opt.width, opt.height, color, depth, vz, hg, hp, fr.render_ms / 1e3, stats)
+
+    def occluded(self, built: "BuiltScene", segs: np.ndarray, eps: float) -> np.ndarray:
+        segs = np.ascontiguousarray(segs, np.float32).reshape(-1, 6)
+        out = np.zeros(len(segs), np.uint8)
+        self._check(self._L.ubr_occluded_batch(self.handle, built.handle, segs.ctypes.data, len(segs),
+                                               eps, out.ctypes.data, abi.MEMORY_HOST))
+        return out
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._L.ubr_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BuiltScene:
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    def info(self) -> dict:
+        i = abi.SceneInfo()
+        self.ctx._check(self.ctx._L.ubr_scene_get_info(self.handle, C.byref(i)))
+        return dict(prim_count=list(i.prim_count), geom_id=list(i.geom_id), bvh_nodes=i.bvh_nodes,
+                    device_bytes=i.device_bytes, build_ms=i.build_ms, bounds_lo=list(i.bounds_lo),
+                    bounds_hi=list(i.bounds_hi))
+
+    def release(self):
+        if self.handle:
+            self.ctx._L.ubr_scene_release(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+_DEFAULT_CTX = None
+
+
+def render(scene: Scene, opt: RenderOptions) -> FrameResult:
+    """umbreon::render (umbreon.hpp:29): build, render, release, on GPU 0."""
+    global _DEFAULT_CTX
+    if _DEFAULT_CTX is None:
+        _DEFAULT_CTX = Context(0)
+    b = _DEFAULT_CTX.build(scene)
+    try:
+        return _DEFAULT_CTX.render(b, scene, opt)
+    finally:
+        b.release()

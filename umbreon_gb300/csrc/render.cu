@@ -1,0 +1,1111 @@
+// render.cu -- ubr_render: the wavefront ray-cast + shade frame.
+//
+// One frame is a loop of transparency rounds over a queue of live pixels
+// (reference: the layer loop of integratePixel, shading/transparency.hpp:364-467):
+//   k_trace_closest   closest hit of each live ray       (rtcIntersect1, :382)
+//   k_surface         hit point, shading normal, secondary-ray origin
+//                     (hit_shader.hpp:147-341, secondary_rays.hpp:118-124)
+//   k_trace_occlusion one thread per AO / shadow ray, rays of a hit
+//                     contiguous: AO sample i, then each light's samples
+//                     (ambient_occlusion.hpp:33-57 / 171-267,
+//                      secondary_rays.hpp:118-134)
+//   k_shade           POV local illumination (shading.hpp:76-192) from the
+//                     stored visibility, front-to-back "over" compositing,
+//                     first-hit capture, epsilon advance, warp-ballot
+//                     compaction of the rays that continue
+// then one fused pass k_post: linear fog on the hi-res view-z
+// (postprocess/fog.cpp:17-36), ss x ss box average with the non-finite guard
+// (image_ops.cpp:9-35) and assumed gamma (image_ops.cpp:37-46).
+// Per-pixel and per-ray results do not depend on launch order, so a frame is
+// bit-reproducible.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ubr_context.h"
+
+namespace ubr {
+
+ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out);
+
+namespace {
+
+constexpr int kStackDepth = 64;
+constexpr float kInfF = __builtin_huge_valf();
+
+struct Bufs {
+  float4* accum;      // per hi-res pixel: Cf.rgb, Af
+  float* tnear;       // per hi-res pixel
+  float4* colorHi;    // per hi-res pixel, pre-post colour
+  float* depth;       // per hi-res pixel (first-hit t, 0 = background)
+  float* viewZ;
+  uint32_t* hitGeom;
+  uint32_t* hitPrim;
+  float4* hitA;       // per queue slot: t, u, v, ref bits
+  float4* hitB;       // per queue slot: Ng.xyz
+  float4* surfA;      // O.xyz, eps
+  float4* surfB;      // N.xyz, -
+  uint2* surfC;       // pixel, flags (1 hit, 2 AO, 4 shadows)
+  uint8_t* occ;       // per slot * raysPerHit
+  float* aoT;         // per slot * aoSamples (enhanced AO nearest t)
+  const LightD* lights;
+  unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
+  uint32_t* counter;  // next-queue size
+};
+
+UBR_D f3 ld3(const float4 v) { return f3{v.x, v.y, v.z}; }
+
+UBR_D f3 safeInv(f3 d) {
+  auto f = [](float x) {
+    if (fabsf(x) < 1e-30f) x = copysignf(1e-30f, x);
+    return 1.0f / x;
+  };
+  return f3{f(d.x), f(d.y), f(d.z)};
+}
+
+// Primary ray of hi-res pixel (px, py): embree_renderer.cpp:1399-1414.
+UBR_D void primaryRay(const Params& p, int px, int py, f3& org, f3& rd) {
+  const float v = 1.0f - 2.0f * (float(py) + 0.5f) / float(p.H);
+  const float u = 2.0f * (float(px) + 0.5f) / float(p.W) - 1.0f;
+  if (p.ortho) {
+    org = p.camPos + p.right * (u * p.halfW) + p.up * (v * p.halfH);
+    rd = p.camDir;
+  } else {
+    org = p.camPos;
+    rd = normalize(p.camDir + p.right * (u * p.persHalfW) + p.up * (v * p.persHalfH));
+  }
+}
+
+// clipRangeT (transparency.hpp:118-129)
+UBR_D void clipRange(const Params& p, f3 rd, float& tn, float& tf) {
+  tn = 0.0f;
+  tf = kInfF;
+  if (p.clipNear <= -kInfF && p.clipFar >= kInfF) return;
+  const float cosr = dot(rd, p.camDir);
+  if (cosr <= 1.0e-6f) return;
+  if (p.clipNear > 0.0f) tn = p.clipNear / cosr;
+  if (p.clipFar < kInfF) tf = p.clipFar / cosr;
+}
+
+UBR_D bool slabHit(float lox, float hix, float loy, float hiy, float loz, float hiz, const f3& o,
+                   const f3& inv, float tnear, float tmax, float& tEntry) {
+  const float t0x = (lox - o.x) * inv.x, t1x = (hix - o.x) * inv.x;
+  const float t0y = (loy - o.y) * inv.y, t1y = (hiy - o.y) * inv.y;
+  const float t0z = (loz - o.z) * inv.z, t1z = (hiz - o.z) * inv.z;
+  const float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tnear));
+  const float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
+  tEntry = tmin;
+  return tmin <= tmx;
+}
+
+UBR_D bool testLeaf(const DScene& s, int slot, const Ray& r, const TriPre& pre, float tnear,
+                    float tmax, Hit& h, uint32_t& ref) {
+  ref = __ldg(&s.leafRef[slot]);
+  const int kind = refKind(ref);
+  const float4* g = s.leafGeo + kLeafF4 * slot;
+  if (kind == kSphere) {
+    const float4 q = __ldg(g);
+    return isectSphere(r, f3{q.x, q.y, q.z}, q.w, tnear, tmax, h);
+  }
+  if (kind == kMesh) {
+    const float4 a = __ldg(g), b = __ldg(g + 1), c = __ldg(g + 2);
+    return isectTriangle(r, pre, ld3(a), ld3(b), ld3(c), tnear, tmax, h);
+  }
+  const float4 a = __ldg(g), b = __ldg(g + 1);
+  if (kind == kCone) return isectConeCurve(r, ld3(a), a.w, ld3(b), b.w, tnear, tmax, h);
+  const uint32_t prim = refPrim(ref);
+  const uint32_t flags = __float_as_uint(__ldg(g + 2).x);
+  const float4 cl = __ldg(&s.rcClip[2 * prim]), cr = __ldg(&s.rcClip[2 * prim + 1]);
+  return isectRoundCurve(r, ld3(a), a.w, ld3(b), b.w, flags, ld3(cl), ld3(cr), tnear, tmax, h);
+}
+
+// Stack traversal of the binary LBVH, near child first.  ANY: return at the
+// first hit in [tnear, tfar].  Closest: smallest t, ties to lowest
+// (geomID, primID).
+// Bytes of the leaf record fetched for one primitive test, by kind
+// (leafRef 4 B + geometry float4s; round segments add their 32 B clip planes).
+UBR_D uint32_t leafBytes(int kind) {
+  return kind == kSphere ? 20u : kind == kMesh ? 52u : kind == kCone ? 36u : 84u;
+}
+
+struct Count {
+  uint32_t nodes = 0, primBytes = 0;
+};
+
+template <bool ANY, bool COUNT = false>
+__device__ bool traverse(const DScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt = nullptr) {
+  best.ref = kInvalid;
+  if (s.primCount == 0) return false;
+  const f3 inv = safeInv(r.dir);
+  const TriPre pre = triPre(r.dir);
+  float tmax = r.tfar;
+  int stack[kStackDepth];
+  int sp = 0;
+  int code = s.root;
+  uint32_t bestGeom = kInvalid, bestPrim = kInvalid;
+  // A valid tree visits each of its 2n-1 nodes at most once per ray; the
+  // bound turns a malformed tree into a reported overflow instead of a hang.
+  uint32_t steps = 0;
+  const uint32_t maxSteps = 2u * s.primCount + 16u;
+  for (;;) {
+    if (++steps > maxSteps) {
+      ++overflow;
+      break;
+    }
+    if (code >= 0) {
+      const float4* nd = s.nodes + kNodeF4 * code;
+      if (COUNT) ++cnt->nodes;
+      const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
+      float tl, tr;
+      const bool hl = slabHit(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r.org, inv, r.tnear, tmax, tl);
+      const bool hr = slabHit(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r.org, inv, r.tnear, tmax, tr);
+      const int cl = __float_as_int(n3.x), cr = __float_as_int(n3.y);
+      if (hl && hr) {
+        const bool leftFirst = tl <= tr;
+        if (sp < kStackDepth) stack[sp++] = leftFirst ? cr : cl;
+        else ++overflow;
+        code = leftFirst ? cl : cr;
+        continue;
+      }
+      if (hl) { code = cl; continue; }
+      if (hr) { code = cr; continue; }
+    } else {
+      Hit h;
+      uint32_t ref;
+      const bool hitLeaf = testLeaf(s, ~code, r, pre, r.tnear, tmax, h, ref);
+      if (COUNT) cnt->primBytes += leafBytes(refKind(ref));
+      if (hitLeaf) {
+        if (ANY) {
+          best = h;
+          best.ref = ref;
+          return true;
+        }
+        const int kind = refKind(ref);
+        const uint32_t gid = s.geomID[kind], prim = refPrim(ref);
+        const bool better = best.ref == kInvalid || h.t < best.t ||
+                            (h.t == best.t && (gid < bestGeom || (gid == bestGeom && prim < bestPrim)));
+        if (better) {
+          best = h;
+          best.ref = ref;
+          bestGeom = gid;
+          bestPrim = prim;
+          tmax = h.t;
+        }
+      }
+    }
+    if (sp == 0) break;
+    code = stack[--sp];
+  }
+  return best.ref != kInvalid;
+}
+
+// Shading surface of a hit (hit_shader.hpp:147-341 attribute + normal logic).
+struct Surf {
+  int kind;
+  uint32_t prim;
+  f3 P, N, Ng, C, V;
+  float opacity;
+  uint32_t mat;
+  float secEps;
+  bool aoOn, shOn;
+};
+
+// secondary_rays.hpp:38-46
+UBR_D float selfIntersectEps(f3 P, f3 dir, float t) {
+  const float dirMax = fmaxf(fabsf(dir.x), fmaxf(fabsf(dir.y), fabsf(dir.z)));
+  const float epsScale = fmaxf(fmaxf(fabsf(P.x), fabsf(P.y)), fmaxf(fabsf(P.z), dirMax * t));
+  return epsScale * 0x1.0fp-21f;
+}
+// shading.hpp:27-30
+UBR_D f3 faceForward(f3 n, f3 rd) { return dot(n, rd) > 0.0f ? neg(n) : n; }
+
+UBR_D Surf surfaceAt(const Params& p, const DScene& s, f3 org, f3 rd, float t, uint32_t ref, float u,
+                     float v, f3 Ng) {
+  Surf sf;
+  sf.kind = refKind(ref);
+  sf.prim = refPrim(ref);
+  sf.V = normalize(f3{-rd.x, -rd.y, -rd.z});
+  sf.Ng = Ng;
+  sf.P = f3{org.x + rd.x * t, org.y + rd.y * t, org.z + rd.z * t};
+  sf.secEps = selfIntersectEps(sf.P, rd, t);
+  const bool shadowsActive = p.shadowsActive != 0;
+  if (sf.kind == kMesh) {
+    const uint32_t i0 = __ldg(&s.meshIdx[3 * sf.prim]), i1 = __ldg(&s.meshIdx[3 * sf.prim + 1]),
+                   i2 = __ldg(&s.meshIdx[3 * sf.prim + 2]);
+    const float w0 = 1.0f - u - v;
+    float nb[3];
+    for (int k = 0; k < 3; ++k)
+      nb[k] = w0 * __ldg(&s.meshNrm[3 * i0 + k]) + u * __ldg(&s.meshNrm[3 * i1 + k]) +
+              v * __ldg(&s.meshNrm[3 * i2 + k]);
+    const float4 c0 = __ldg(&s.meshCol[i0]), c1 = __ldg(&s.meshCol[i1]), c2 = __ldg(&s.meshCol[i2]);
+    const float4 cb = make_float4(w0 * c0.x + u * c1.x + v * c2.x, w0 * c0.y + u * c1.y + v * c2.y,
+                                  w0 * c0.z + u * c1.z + v * c2.z, w0 * c0.w + u * c1.w + v * c2.w);
+    const f3 NgF = faceForward(Ng, rd);
+    f3 N = normalize(f3{nb[0], nb[1], nb[2]});
+    if (dot(N, NgF) < 0.0f) N = neg(N);
+    sf.N = N;
+    sf.C = f3{cb.x, cb.y, cb.z};
+    sf.opacity = cb.w;
+    sf.mat = s.meshTriMat ? __ldg(&s.meshTriMat[s.baseTri ? sf.prim % s.baseTri : 0]) : s.meshMat;
+    sf.aoOn = p.aoSamples > 0;
+    sf.shOn = shadowsActive;
+  } else {
+    const float4 fc = __ldg(&s.primColor[sf.kind][sf.prim]);
+    sf.mat = __ldg(&s.primMat[sf.kind][sf.prim]);
+    sf.N = faceForward(normalize(Ng), rd);
+    sf.C = f3{fc.x, fc.y, fc.z};
+    const bool fromEdge = __ldg(&s.primFromEdge[sf.kind][sf.prim]) != 0;
+    sf.aoOn = !fromEdge && p.aoSamples > 0;
+    sf.shOn = !fromEdge && shadowsActive;
+    sf.opacity = fc.w;
+    if (sf.kind != kSphere) {
+      const float op1 = __ldg(&s.primOpacity1[sf.kind][sf.prim]);
+      if (op1 >= 0.0f) {
+        float uu = u;
+        if (uu < 0.0f) uu = 0.0f;
+        if (uu > 1.0f) uu = 1.0f;
+        sf.opacity = fc.w * (1.0f - uu) + op1 * uu;
+      }
+    }
+  }
+  return sf;
+}
+
+// secondary_rays.hpp:51-61
+UBR_D void tea2(uint32_t& v0, uint32_t& v1) {
+  uint32_t sum = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    sum += 0x9E3779B9u;
+    v0 += ((v1 << 4) + 0xA341316Cu) ^ (v1 + sum) ^ ((v1 >> 5) + 0xC8013EA4u);
+    v1 += ((v0 << 4) + 0xAD90777Du) ^ (v0 + sum) ^ ((v0 >> 5) + 0x7E95761Eu);
+  }
+}
+UBR_D float u32ToUnorm(uint32_t u) { return float(u >> 8) * 0x1.0p-24f; }
+// secondary_rays.hpp:66-73
+UBR_D f3 cosineSampleHemisphere(float u1, float u2, const Frame3& f) {
+  const float phi = 6.2831853072f * u1;
+  const float r = sqrtf(u2);
+  const float z = sqrtf(fmaxf(0.0f, 1.0f - u2));
+  const float x = cosf(phi) * r;
+  const float y = sinf(phi) * r;
+  return f.t * x + f.b * y + f.n * z;
+}
+// ambient_occlusion.hpp:98-105
+UBR_D float radicalInverse2(uint32_t bits) { return float(__brev(bits)) * 0x1.0p-32f; }
+// ambient_occlusion.hpp:112-127
+UBR_D void aoSample2d(const Params& p, uint32_t base, int i, float cpx, float cpy, float& u1, float& u2) {
+  if (p.aoLowDiscrepancy) {
+    u1 = float(i) / float(p.aoSamples) + cpx;
+    u2 = radicalInverse2(uint32_t(i)) + cpy;
+    if (u1 >= 1.0f) u1 -= 1.0f;
+    if (u2 >= 1.0f) u2 -= 1.0f;
+  } else {
+    uint32_t s0 = base, s1 = uint32_t(i);
+    tea2(s0, s1);
+    u1 = u32ToUnorm(s0);
+    u2 = u32ToUnorm(s1);
+  }
+}
+UBR_D void cpShift(int px, int py, float& cpx, float& cpy) {
+  uint32_t c0 = uint32_t(px) + 1u, c1 = uint32_t(py) + 1u;
+  tea2(c0, c1);
+  cpx = u32ToUnorm(c0);
+  cpy = u32ToUnorm(c1);
+}
+// AO direction of sample i (legacy: tea2 stream; enhanced: also LD)
+UBR_D f3 aoDir(const Params& p, const Frame3& f, int px, int py, int i) {
+  const uint32_t base = uint32_t(px) + uint32_t(py) * uint32_t(p.W);
+  float u1, u2;
+  if (p.aoEnhanced) {
+    float cpx = 0.0f, cpy = 0.0f;
+    if (p.aoLowDiscrepancy) cpShift(px, py, cpx, cpy);
+    aoSample2d(p, base, i, cpx, cpy, u1, u2);
+  } else {
+    uint32_t s0 = base, s1 = uint32_t(i);
+    tea2(s0, s1);
+    u1 = u32ToUnorm(s0);
+    u2 = u32ToUnorm(s1);
+  }
+  return cosineSampleHemisphere(u1, u2, f);
+}
+// secondary_rays.hpp:102-109
+UBR_D f3 sampleLightDir(const LightD& l, float u1, float u2) {
+  if (l.radius <= 0.0f) return l.L;
+  const Frame3 f = frameFromNormal(l.L);
+  const float phi = 6.2831853072f * u1;
+  const float rr = tanf(l.radius) * sqrtf(u2);
+  const f3 d = f.n + f.t * (rr * cosf(phi)) + f.b * (rr * sinf(phi));
+  return safeNormalize(d, l.L);
+}
+
+UBR_D int warpPushBase(bool push, uint32_t* counter, int& offset) {
+  const unsigned mask = __ballot_sync(0xFFFFFFFFu, push);
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    if (lane == leader) base = int(atomicAdd(counter, uint32_t(__popc(mask))));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+  }
+  offset = __popc(mask & ((1u << lane) - 1u));
+  return base;
+}
+
+UBR_D void warpCount(unsigned long long* ctr, uint32_t v) {
+  uint32_t s = __reduce_add_sync(0xFFFFFFFFu, v);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(ctr, (unsigned long long)s);
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_closest(Params p, DScene s, Bufs b, int layer, uint32_t n,
+                                                       const uint32_t* queue) {
+  Count cnt;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t traced = 0, ovf = 0;
+  if (i < n) {
+    const uint32_t pix = layer == 0 ? i : queue[i];
+    const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
+    f3 org, rd;
+    primaryRay(p, px, py, org, rd);
+    float ctn, ctf;
+    clipRange(p, rd, ctn, ctf);
+    Ray r{org, rd, layer == 0 ? ctn : b.tnear[pix], ctf};
+    Hit h;
+    traverse<false, COUNT>(s, r, h, ovf, &cnt);
+    traced = 1;
+    b.hitA[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.ref));
+    b.hitB[i] = make_float4(h.Ng.x, h.Ng.y, h.Ng.z, 0.0f);
+  }
+  warpCount(&b.stats[0], traced);
+  warpCount(&b.stats[3], ovf);
+  if (COUNT) {
+    warpCount(&b.stats[4], cnt.nodes);
+    warpCount(&b.stats[5], cnt.primBytes);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_surface(Params p, DScene s, Bufs b, int layer, uint32_t n,
+                                                 const uint32_t* queue) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t pix = layer == 0 ? i : queue[i];
+  const float4 ha = b.hitA[i];
+  const uint32_t ref = __float_as_uint(ha.w);
+  if (ref == kInvalid) {
+    b.surfC[i] = make_uint2(pix, 0u);
+    return;
+  }
+  const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
+  f3 org, rd;
+  primaryRay(p, px, py, org, rd);
+  const float4 hb = b.hitB[i];
+  const Surf sf = surfaceAt(p, s, org, rd, ha.x, ref, ha.y, ha.z, f3{hb.x, hb.y, hb.z});
+  // computeAO / computeShadow origin: P + safeNormalize(faceForward-to-N(Ng)) * eps
+  f3 ng = dot(sf.Ng, sf.N) < 0.0f ? neg(sf.Ng) : sf.Ng;
+  ng = safeNormalize(ng, sf.N);
+  const f3 O = sf.P + ng * sf.secEps;
+  b.surfA[i] = make_float4(O.x, O.y, O.z, sf.secEps);
+  b.surfB[i] = make_float4(sf.N.x, sf.N.y, sf.N.z, 0.0f);
+  b.surfC[i] = make_uint2(pix, 1u | (sf.aoOn ? 2u : 0u) | (sf.shOn ? 4u : 0u));
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_occlusion(Params p, DScene s, Bufs b, uint32_t n) {
+  Count cnt;
+  const uint64_t tid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t R = uint64_t(p.raysPerHit);
+  uint32_t traced = 0, ovf = 0;
+  if (tid < uint64_t(n) * R) {
+    const uint32_t slot = uint32_t(tid / R);
+    const int j = int(tid % R);
+    const uint2 sc = b.surfC[slot];
+    const uint32_t flags = sc.y;
+    uint8_t res = 0;
+    const int px = int(sc.x % uint32_t(p.W)), py = int(sc.x / uint32_t(p.W));
+    if (j < p.aoSamples) {
+      if ((flags & 2u)) {
+        const float4 sa = b.surfA[slot], sb = b.surfB[slot];
+        const f3 N = ld3(sb);
+        const Frame3 f = frameFromNormal(N);
+        const f3 dir = aoDir(p, f, px, py, j);
+        float tnear = sa.w;
+        if (dot(dir, N) < 0.01f) {
+          res = 1;
+          if (p.aoEnhanced) b.aoT[uint64_t(slot) * p.aoSamples + j] = -1.0f;
+        } else {
+          Ray r{ld3(sa), dir, tnear, p.aoDistance};
+          Hit h;
+          if (p.aoEnhanced) {
+            const bool hit = traverse<false, COUNT>(s, r, h, ovf, &cnt);
+            b.aoT[uint64_t(slot) * p.aoSamples + j] = hit ? h.t : kInfF;
+            res = hit ? 1 : 0;
+          } else {
+            res = traverse<true, COUNT>(s, r, h, ovf, &cnt) ? 1 : 0;
+          }
+          traced = 1;
+        }
+      }
+    } else if (flags & 4u) {
+      const int k = j - p.aoSamples;
+      int l = 0;
+      while (l + 1 < p.nLights && b.lights[l + 1].rayOffset <= k) ++l;
+      const LightD L = b.lights[l];
+      const float4 sa = b.surfA[slot], sb = b.surfB[slot];
+      const f3 N = ld3(sb);
+      const float ndl = dot(N, L.L);
+      if (ndl > 0.0f) {
+        f3 dir = L.L;
+        if (L.soft) {
+          // the (px, py) stream is advanced by every earlier lit soft light
+          // (shading.hpp:100, secondary_rays.hpp:128-131)
+          int consumed = 0;
+          for (int q = 0; q < l; ++q) {
+            const LightD Q = b.lights[q];
+            if (Q.soft && dot(N, Q.L) > 0.0f) consumed += Q.samples;
+          }
+          uint32_t s0 = uint32_t(px), s1 = uint32_t(py);
+          const int steps = consumed + (k - L.rayOffset) + 1;
+          for (int q = 0; q < steps; ++q) tea2(s0, s1);
+          dir = sampleLightDir(L, u32ToUnorm(s0), u32ToUnorm(s1));
+        }
+        Ray r{ld3(sa), dir, sa.w, kInfF};
+        Hit h;
+        res = traverse<true, COUNT>(s, r, h, ovf, &cnt) ? 1 : 0;
+        traced = 1;
+      }
+    }
+    b.occ[tid] = res;
+  }
+  warpCount(&b.stats[1], traced);
+  warpCount(&b.stats[3], ovf);
+  if (COUNT) {
+    warpCount(&b.stats[6], cnt.nodes);
+    warpCount(&b.stats[7], cnt.primBytes);
+  }
+}
+
+UBR_D float blinnExp(float roughness) {
+  float r = roughness;
+  if (r < 1e-6f) r = 1e-6f;
+  float e = 1.0f / r;
+  if (e < 1.0f) e = 1.0f;
+  if (e > 1.0e6f) e = 1.0e6f;
+  return e;
+}
+UBR_D float aoMultibounce(float ao, float albedo) {
+  const float a = 2.0404f * albedo - 0.3324f;
+  const float bb = -4.7951f * albedo + 0.6417f;
+  const float c = 2.7552f * albedo + 0.6903f;
+  return fmaxf(ao, ((ao * a + bb) * ao + c) * ao);
+}
+
+__global__ void __launch_bounds__(128) k_shade(Params p, DScene s, Bufs b, int layer, uint32_t n,
+                                               const uint32_t* queue, uint32_t* outQueue) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool push = false;
+  uint32_t pix = 0, capped = 0;
+  if (i < n) {
+    pix = layer == 0 ? i : queue[i];
+    const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
+    float4 acc = layer == 0 ? make_float4(0, 0, 0, 0) : b.accum[pix];
+    f3 base = p.bg;
+    float baseCov = p.transparentBg ? 0.0f : 1.0f;
+    bool done = true;
+    const float4 ha = b.hitA[i];
+    const uint32_t ref = __float_as_uint(ha.w);
+    if (ref != kInvalid) {
+      f3 org, rd;
+      primaryRay(p, px, py, org, rd);
+      const float4 hb = b.hitB[i];
+      const float t = ha.x;
+      const Surf sf = surfaceAt(p, s, org, rd, t, ref, ha.y, ha.z, f3{hb.x, hb.y, hb.z});
+      const ubr_material m = s.mats[sf.mat];
+      // --- ambient occlusion factors (ao_shade.hpp:44-141) ---
+      f3 aoFactor{1.0f, 1.0f, 1.0f};
+      f3 ambLight = p.ambLight;
+      float diffuseAo = 1.0f;
+      const uint64_t rb = uint64_t(i) * uint64_t(p.raysPerHit);
+      if (sf.aoOn) {
+        float openness;
+        f3 bent = sf.N;
+        if (!p.aoEnhanced) {
+          int hits = 0;
+          for (int k = 0; k < p.aoSamples; ++k) hits += b.occ[rb + k];
+          openness = 1.0f - float(hits) / float(p.aoSamples);
+        } else {
+          // computeAOQuality accumulation, sample order preserved
+          const float R = p.aoDistance;
+          float radius[3], weight[3];
+          int K;
+          if (p.aoMultiScale) {
+            K = 3;
+            radius[0] = 0.08f * R; radius[1] = 0.30f * R; radius[2] = 1.00f * R;
+            weight[0] = 0.55f; weight[1] = 0.35f; weight[2] = 0.10f;
+          } else {
+            K = 1;
+            radius[0] = radius[1] = radius[2] = R;
+            weight[0] = 1.0f; weight[1] = weight[2] = 0.0f;
+          }
+          const Frame3 f = frameFromNormal(sf.N);
+          float obsScale[3] = {0.0f, 0.0f, 0.0f};
+          float weightedObs = 0.0f;
+          f3 bentAccum{0.0f, 0.0f, 0.0f};
+          for (int k = 0; k < p.aoSamples; ++k) {
+            const f3 dir = aoDir(p, f, px, py, k);
+            if (dot(dir, sf.N) < 0.01f) {
+              obsScale[0] += 1.0f; obsScale[1] += 1.0f; obsScale[2] += 1.0f;
+              weightedObs += 1.0f;
+              continue;
+            }
+            const float th = b.aoT[uint64_t(i) * p.aoSamples + k];
+            float perSample = 0.0f;
+            for (int q = 0; q < K; ++q) {
+              if (th < radius[q]) {
+                float fk = 1.0f;
+                if (p.aoFalloffPower > 0.0f) {
+                  float a = 1.0f - th / radius[q];
+                  if (a < 0.0f) a = 0.0f;
+                  fk = powf(a, p.aoFalloffPower);
+                }
+                obsScale[q] += fk;
+                perSample += weight[q] * fk;
+              }
+            }
+            weightedObs += perSample;
+            bentAccum = bentAccum + dir * (1.0f - perSample);
+          }
+          const float invN = 1.0f / float(p.aoSamples);
+          openness = 1.0f - weightedObs * invN;
+          bent = safeNormalize(bentAccum, sf.N);
+        }
+        if (p.aoEnhanced && p.aoBentNormal) {
+          const float w = 0.5f * (dot(bent, p.aoUp) + 1.0f);
+          ambLight = f3{p.ambLight.x * (p.aoGround.x + (p.aoSky.x - p.aoGround.x) * w),
+                        p.ambLight.y * (p.aoGround.y + (p.aoSky.y - p.aoGround.y) * w),
+                        p.ambLight.z * (p.aoGround.z + (p.aoSky.z - p.aoGround.z) * w)};
+        }
+        if (p.aoMultibounce) {
+          const float ox = aoMultibounce(openness, sf.C.x);
+          const float oy = aoMultibounce(openness, sf.C.y);
+          const float oz = aoMultibounce(openness, sf.C.z);
+          aoFactor = f3{1.0f - p.aoIntensity * (1.0f - ox), 1.0f - p.aoIntensity * (1.0f - oy),
+                        1.0f - p.aoIntensity * (1.0f - oz)};
+        } else {
+          const float sv = 1.0f - p.aoIntensity * (1.0f - openness);
+          aoFactor = f3{sv, sv, sv};
+        }
+        if (p.aoDiffuseFactor > 0.0f) diffuseAo = 1.0f - p.aoDiffuseFactor * (1.0f - openness);
+      }
+      // --- shadeLocal, POV branch (shading.hpp:96-191) ---
+      const f3 C = sf.C, N = sf.N, V = sf.V;
+      f3 out{m.emission * C.x + aoFactor.x * m.ambient * C.x * ambLight.x,
+             m.emission * C.y + aoFactor.y * m.ambient * C.y * ambLight.y,
+             m.emission * C.z + aoFactor.z * m.ambient * C.z * ambLight.z};
+      const float ex = blinnExp(m.roughness);
+      for (int l = 0; l < p.nLights; ++l) {
+        const LightD L = b.lights[l];
+        const float ndl = dot(N, L.L);
+        if (ndl <= 0.0f) continue;
+        float shadowFactor = 1.0f;
+        if (sf.shOn) {
+          const uint8_t* o = b.occ + rb + p.aoSamples + L.rayOffset;
+          if (!L.soft) {
+            shadowFactor = o[0] ? 0.0f : 1.0f;
+          } else {
+            int hits = 0;
+            for (int q = 0; q < L.samples; ++q) hits += o[q];
+            shadowFactor = 1.0f - float(hits) / float(L.samples);
+          }
+        }
+        const f3 Lc{L.color.x * shadowFactor, L.color.y * shadowFactor, L.color.z * shadowFactor};
+        float d;
+        if (m.brilliance == 1.0f) d = ndl;
+        else if (m.brilliance == 0.0f) d = 1.0f;
+        else d = powf(ndl, m.brilliance);
+        const float dk = m.diffuse * d * diffuseAo;
+        out.x += dk * C.x * Lc.x;
+        out.y += dk * C.y * Lc.y;
+        out.z += dk * C.z * Lc.z;
+        if (!L.highlight) continue;
+        f3 hl;
+        if (m.metallic) {
+          float c = ndl;
+          if (c > 1.0f) c = 1.0f;
+          const float x = acosf(c) * 0.63661977f;
+          float fr = 0.014567225f / ((x - 1.12f) * (x - 1.12f)) - 0.011612903f;
+          if (fr < 0.0f) fr = 0.0f;
+          if (fr > 1.0f) fr = 1.0f;
+          hl = f3{Lc.x * (fr + (1.0f - fr) * C.x), Lc.y * (fr + (1.0f - fr) * C.y),
+                  Lc.z * (fr + (1.0f - fr) * C.z)};
+        } else {
+          hl = Lc;
+        }
+        float specW = 0.0f;
+        if (m.specular > 0.0f) {
+          const f3 H = normalize(f3{L.L.x + V.x, L.L.y + V.y, L.L.z + V.z});
+          const float nh = dot(N, H);
+          if (nh > 0.0f) specW += m.specular * powf(nh, ex);
+        }
+        if (m.phong > 0.0f) {
+          const f3 Rr = 2.0f * ndl * N - L.L;
+          const float rv = dot(Rr, V);
+          if (rv > 0.0f && (m.phong_size < 60.0f || rv > 0.0008f)) specW += m.phong * powf(rv, m.phong_size);
+        }
+        if (specW > 0.0f) {
+          const float sc = specW * p.specularScale;
+          out.x += sc * hl.x;
+          out.y += sc * hl.y;
+          out.z += sc * hl.z;
+        }
+      }
+      if (m.reflection > 0.0f) {
+        out.x += m.reflection * p.bg.x;
+        out.y += m.reflection * p.bg.y;
+        out.z += m.reflection * p.bg.z;
+      }
+      // --- first-hit capture + compositing (transparency.hpp:394-467) ---
+      if (b.depth[pix] == 0.0f) {
+        b.depth[pix] = t;
+        b.viewZ[pix] = t * dot(rd, p.camDir);
+        b.hitGeom[pix] = s.geomID[sf.kind];
+        b.hitPrim[pix] = sf.prim;
+      }
+      const float kOpaque = 1.0f - 1e-4f;
+      if (!p.transparency || sf.opacity >= kOpaque) {
+        base = out;
+        baseCov = 1.0f;
+      } else {
+        const float w = (1.0f - acc.w) * sf.opacity;
+        acc.x += w * out.x;
+        acc.y += w * out.y;
+        acc.z += w * out.z;
+        acc.w += w;
+        if (!(acc.w >= kOpaque)) {
+          const f3 hitP{org.x + rd.x * t, org.y + rd.y * t, org.z + rd.z * t};
+          const float dirMax = fmaxf(fabsf(rd.x), fmaxf(fabsf(rd.y), fabsf(rd.z)));
+          const float epsScale =
+              fmaxf(fmaxf(fabsf(hitP.x), fabsf(hitP.y)), fmaxf(fabsf(hitP.z), dirMax * t));
+          const float tn = t + epsScale * 0x1.0fp-21f;
+          if (layer == p.maxIters - 1) {
+            capped = 1;
+          } else {
+            b.tnear[pix] = tn;
+            b.accum[pix] = acc;
+            done = false;
+            push = true;
+          }
+        }
+      }
+    }
+    if (done) {
+      const float floorW = (1.0f - acc.w) * baseCov;
+      float outA = acc.w + floorW;
+      outA = fminf(1.0f, fmaxf(0.0f, outA));
+      b.colorHi[pix] = make_float4(acc.x + floorW * base.x, acc.y + floorW * base.y,
+                                   acc.z + floorW * base.z, outA);
+    }
+  }
+  int off;
+  const int qb = warpPushBase(push, b.counter, off);
+  if (push) outQueue[qb + off] = pix;
+  warpCount(&b.stats[2], capped);
+}
+
+// Fused finishing pass: fog (fog.cpp:7-36) on each hi-res sample, ss x ss box
+// average with the non-finite guard (image_ops.cpp:9-35; only when ss > 1,
+// as renderFrame skips the downsample at ss == 1), assumed gamma
+// (image_ops.cpp:37-46).
+__global__ void k_post(Params p, const float4* colorHi, const float* viewZ, float4* out) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= p.outW * p.outH) return;
+  const int ox = o % p.outW, oy = o / p.outW;
+  const int ss = p.ss;
+  auto fogged = [&](int hx, int hy) {
+    const size_t hp = size_t(hy) * p.W + hx;
+    float4 c = colorHi[hp];
+    if (p.fogOn) {
+      const float z = viewZ[hp];
+      if (z > 0.0f) {
+        float f;
+        const float denom = p.fogEnd - p.fogStart;
+        if (denom <= 0.0f) {
+          f = z < p.fogEnd ? 1.0f : 0.0f;
+        } else {
+          f = (p.fogEnd - z) / denom;
+          if (f < 0.0f) f = 0.0f;
+          if (f > 1.0f) f = 1.0f;
+        }
+        if (p.transparentBg) {
+          c.w *= f;
+        } else {
+          c.x = p.fogColor.x * (1.0f - f) + c.x * f;
+          c.y = p.fogColor.y * (1.0f - f) + c.y * f;
+          c.z = p.fogColor.z * (1.0f - f) + c.z * f;
+        }
+      }
+    }
+    return c;
+  };
+  float4 r;
+  if (ss == 1) {
+    r = fogged(ox, oy);
+  } else {
+    float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int dy = 0; dy < ss; ++dy)
+      for (int dx = 0; dx < ss; ++dx) {
+        const float4 c = fogged(ox * ss + dx, oy * ss + dy);
+        a[0] += isfinite(c.x) ? c.x : 0.0f;
+        a[1] += isfinite(c.y) ? c.y : 0.0f;
+        a[2] += isfinite(c.z) ? c.z : 0.0f;
+        a[3] += isfinite(c.w) ? c.w : 0.0f;
+      }
+    const float inv = 1.0f / float(ss * ss);
+    r = make_float4(a[0] * inv, a[1] * inv, a[2] * inv, a[3] * inv);
+  }
+  const float g = p.gamma;
+  if (!(fabsf(g - 1.0f) <= 1.0e-4f)) {
+    r.x = r.x > 0.0f ? powf(r.x, g) : 0.0f;
+    r.y = r.y > 0.0f ? powf(r.y, g) : 0.0f;
+    r.z = r.z > 0.0f ? powf(r.z, g) : 0.0f;
+  }
+  out[o] = r;
+}
+
+__global__ void k_init_pixels(uint32_t npix, float* depth, float* viewZ, uint32_t* hg, uint32_t* hp) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  depth[i] = 0.0f;
+  viewZ[i] = 0.0f;
+  hg[i] = kInvalid;
+  hp[i] = kInvalid;
+}
+
+// Host-side parameter setup: computeCameraBasis (embree_renderer.cpp:375-386),
+// buildSceneLights (:436-458) and buildEnvDomeLights (ao/env_dome.hpp:33-64),
+// evaluated in float on the host exactly as the reference does.
+ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vector<LightD>& lights) {
+  if (d.abi_version != UBR_ABI_VERSION) return setError(c, UBR_INVALID_ARGUMENT, "render desc: abi_version mismatch");
+  if (d.width <= 0 || d.height <= 0) return setError(c, UBR_INVALID_ARGUMENT, "render desc: width/height must be > 0");
+  const int ss = d.supersample < 1 ? 1 : d.supersample;
+  if (int64_t(d.width) * ss * int64_t(d.height) * ss >= (1ll << 31))
+    return setError(c, UBR_INVALID_ARGUMENT, "render desc: supersampled frame too large");
+  if (d.light_count && !d.lights) return setError(c, UBR_INVALID_ARGUMENT, "render desc: lights is NULL");
+  if (d.ao_samples < 0) return setError(c, UBR_INVALID_ARGUMENT, "render desc: ao_samples < 0");
+  std::memset(&p, 0, sizeof(p));
+  p.ss = ss;
+  p.outW = d.width;
+  p.outH = d.height;
+  p.W = d.width * ss;
+  p.H = d.height * ss;
+  const float aspect = float(p.W) / float(p.H);
+  p.camPos = f3{d.cam_position[0], d.cam_position[1], d.cam_position[2]};
+  p.camDir = normalize(f3{d.cam_direction[0], d.cam_direction[1], d.cam_direction[2]});
+  p.right = normalize(cross(p.camDir, f3{d.cam_up[0], d.cam_up[1], d.cam_up[2]}));
+  p.up = normalize(cross(p.right, p.camDir));
+  p.halfH = d.cam_height * 0.5f;
+  p.halfW = p.halfH * aspect;
+  p.persHalfH = std::tan(radiansf(d.cam_fovy) * 0.5f);
+  p.persHalfW = p.persHalfH * aspect;
+  p.ortho = d.cam_orthographic ? 1 : 0;
+  p.clipNear = d.clip_near;
+  p.clipFar = d.clip_far;
+  p.ambLight = f3{d.ambient_color[0], d.ambient_color[1], d.ambient_color[2]};
+  p.bg = f3{d.background[0], d.background[1], d.background[2]};
+  p.aoUp = d.ao_use_camera_up ? p.up : safeNormalize(f3{d.ao_up[0], d.ao_up[1], d.ao_up[2]}, p.up);
+  p.aoSamples = d.ao_samples;
+  p.aoDistance = d.ao_distance;
+  p.aoIntensity = d.ao_intensity;
+  p.aoFalloffPower = d.ao_falloff_power;
+  p.aoMultiScale = d.ao_multiscale != 0;
+  p.aoBentNormal = d.ao_bent_normal != 0;
+  p.aoMultibounce = d.ao_multibounce != 0;
+  p.aoLowDiscrepancy = d.ao_low_discrepancy != 0;
+  p.aoSky = f3{d.ao_sky_color[0], d.ao_sky_color[1], d.ao_sky_color[2]};
+  p.aoGround = f3{d.ao_ground_color[0], d.ao_ground_color[1], d.ao_ground_color[2]};
+  p.aoDiffuseFactor = d.ao_diffuse_factor;
+  p.aoEnhanced = (d.ao_falloff_power > 0.0f || d.ao_multiscale || d.ao_bent_normal || d.ao_multibounce ||
+                  d.ao_low_discrepancy || d.ao_diffuse_factor > 0.0f)
+                     ? 1
+                     : 0;
+  p.shadowsActive = (d.shadows || d.env_lights > 0) ? 1 : 0;
+  p.shadowSamples = d.shadow_samples;
+  p.specularScale = d.specular_scale;
+  p.transparency = d.transparency ? 1 : 0;
+  p.transparentBg = d.transparent_background ? 1 : 0;
+  p.maxIters = d.transparency ? (d.max_transparent_layers + 1) : 1;
+  if (p.maxIters < 1) p.maxIters = 1;
+  p.fogOn = d.fog_enabled ? 1 : 0;
+  p.fogColor = f3{d.fog_color[0], d.fog_color[1], d.fog_color[2]};
+  p.fogStart = d.fog_start;
+  p.fogEnd = d.fog_end;
+  p.gamma = d.assumed_gamma;
+  // lights
+  lights.clear();
+  for (uint32_t i = 0; i < d.light_count; ++i) {
+    const ubr_light& dl = d.lights[i];
+    LightD l{};
+    l.L = normalize(f3{-dl.direction[0], -dl.direction[1], -dl.direction[2]});
+    l.color = f3{dl.color[0] * dl.intensity, dl.color[1] * dl.intensity, dl.color[2] * dl.intensity};
+    l.highlight = dl.casts_highlight ? 1u : 0u;
+    l.radius = (d.gi_integrator == 2 && dl.angular_radius > 0.0f) ? dl.angular_radius : radiansf(d.light_radius_deg);
+    lights.push_back(l);
+  }
+  if (d.env_lights > 0) {
+    for (LightD& l : lights) l.color = l.color * d.env_key_scale;
+    const int n = d.env_lights;
+    const float cosMax = std::cos(radiansf(d.env_angle));
+    const float ga = 3.14159265f * (3.0f - std::sqrt(5.0f));
+    float cosSum = 0.0f;
+    std::vector<f3> dirs;
+    for (int i = 0; i < n; ++i) {
+      const float z = 1.0f - (1.0f - cosMax) * ((i + 0.5f) / n);
+      const float r = std::sqrt(std::max(0.0f, 1.0f - z * z));
+      const float t = ga * i;
+      dirs.push_back(normalize(p.camDir * z + p.right * (r * std::cos(t)) + p.up * (r * std::sin(t))));
+      cosSum += z;
+    }
+    const float perLight = cosSum > 0.0f ? d.env_intensity / cosSum : 0.0f;
+    for (const f3& dd : dirs) {
+      LightD l{};
+      l.L = f3{-dd.x, -dd.y, -dd.z};
+      l.color = f3{perLight, perLight, perLight};
+      l.highlight = 0u;
+      l.radius = radiansf(d.light_radius_deg);
+      lights.push_back(l);
+    }
+  }
+  if (lights.size() > size_t(kMaxLights)) return setError(c, UBR_INVALID_ARGUMENT, "too many lights (max 64)");
+  int off = 0;
+  for (LightD& l : lights) {
+    l.soft = (d.shadow_samples > 1 && l.radius > 0.0f) ? 1u : 0u;
+    l.samples = l.soft ? d.shadow_samples : 1;
+    l.rayOffset = off;
+    off += l.samples;
+  }
+  p.nLights = int(lights.size());
+  p.shadowRays = p.shadowsActive ? off : 0;
+  p.raysPerHit = p.aoSamples + p.shadowRays;
+  return UBR_OK;
+}
+
+// EmbreeRenderer::occluded plain any-hit branch (embree_renderer.cpp:294-315):
+// the open segment (p, q) trimmed by max(eps*len, eps) and len*(1-eps).
+__global__ void k_occluded_segments(DScene s, const float* segs, uint64_t n, float eps, uint8_t* out,
+                                    unsigned long long* stats) {
+  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  uint32_t ovf = 0;
+  if (i < n) {
+    const float* q = segs + 6 * i;
+    const f3 a{q[0], q[1], q[2]}, bq{q[3], q[4], q[5]};
+    const f3 d = bq - a;
+    const float len = length(d);
+    uint8_t res = 0;
+    if (len > 0.0f) {
+      const f3 dir{d.x / len, d.y / len, d.z / len};
+      const float tnear = fmaxf(eps * len, eps);
+      const float tfar = len * (1.0f - eps);
+      if (tnear < tfar) {
+        Ray r{a, dir, tnear, tfar};
+        Hit h;
+        res = traverse<true>(s, r, h, ovf) ? 1 : 0;
+      }
+    }
+    out[i] = res;
+  }
+  warpCount(&stats[3], ovf);
+}
+
+template <class T>
+T* scratchT(Context* c, int slot, size_t count, ubr_status& st) {
+  void* ptr = nullptr;
+  if (st == UBR_OK) st = scratchGet(c, slot, count * sizeof(T) + 16, &ptr);
+  return static_cast<T*>(ptr);
+}
+
+}  // namespace
+
+ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ubr_frame& fr,
+                       const volatile int32_t* cancel, uint64_t* progress) {
+  Params p;
+  std::vector<LightD> lights;
+  ubr_status st = makeParams(c, d, p, lights);
+  if (st != UBR_OK) return st;
+  const uint32_t npix = uint32_t(p.W) * uint32_t(p.H);
+  const uint32_t nout = uint32_t(p.outW) * uint32_t(p.outH);
+  Bufs b{};
+  // frame scratch slots 16..
+  b.accum = scratchT<float4>(c, 16, npix, st);
+  b.tnear = scratchT<float>(c, 17, npix, st);
+  b.colorHi = scratchT<float4>(c, 18, npix, st);
+  b.depth = scratchT<float>(c, 19, npix, st);
+  b.viewZ = scratchT<float>(c, 20, npix, st);
+  b.hitGeom = scratchT<uint32_t>(c, 21, npix, st);
+  b.hitPrim = scratchT<uint32_t>(c, 22, npix, st);
+  b.hitA = scratchT<float4>(c, 23, npix, st);
+  b.hitB = scratchT<float4>(c, 24, npix, st);
+  uint32_t* q0 = scratchT<uint32_t>(c, 25, npix, st);
+  uint32_t* q1 = scratchT<uint32_t>(c, 26, npix, st);
+  const bool secondary = p.raysPerHit > 0;
+  if (secondary) {
+    b.surfA = scratchT<float4>(c, 27, npix, st);
+    b.surfB = scratchT<float4>(c, 28, npix, st);
+    b.surfC = scratchT<uint2>(c, 29, npix, st);
+    b.occ = scratchT<uint8_t>(c, 30, size_t(npix) * p.raysPerHit, st);
+    if (p.aoEnhanced && p.aoSamples > 0) b.aoT = scratchT<float>(c, 31, size_t(npix) * p.aoSamples, st);
+  }
+  LightD* dl = scratchT<LightD>(c, 32, lights.size() + 1, st);
+  b.stats = scratchT<unsigned long long>(c, 33, 8, st);
+  b.counter = scratchT<uint32_t>(c, 34, 4, st);
+  float4* outColor = scratchT<float4>(c, 35, nout, st);
+  if (st != UBR_OK) return st;
+  b.lights = dl;
+  cudaStream_t s = c->stream;
+  uint32_t kernels = 0;
+  const bool prof = (fr.flags & UBR_FRAME_PROFILE) != 0;
+  const bool count = (fr.flags & UBR_FRAME_COUNT) != 0;
+  // phase timing: pairs of events per launch, summed per phase after the sync
+  std::vector<std::pair<int, int>> marks;  // (phase, event index of the start)
+  auto mark = [&](int phase, bool start) -> ubr_status {
+    if (!prof) return UBR_OK;
+    if (start) {
+      const int e = int(marks.size()) * 2;
+      if (size_t(e + 2) > c->pev.size()) {
+        const size_t old = c->pev.size();
+        c->pev.resize(old + 64);
+        for (size_t i = old; i < c->pev.size(); ++i) cudaEventCreate(&c->pev[i]);
+      }
+      marks.push_back({phase, e});
+      cudaEventRecord(c->pev[size_t(e)], s);
+    } else {
+      cudaEventRecord(c->pev[size_t(marks.back().second + 1)], s);
+    }
+    return UBR_OK;
+  };
+  cudaEventRecord(c->ev[0], s);
+  if (!lights.empty())
+    UBR_CUDA(c, cudaMemcpyAsync(dl, lights.data(), lights.size() * sizeof(LightD), cudaMemcpyHostToDevice, s));
+  UBR_CUDA(c, cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s));
+  const int TB = 128;
+  k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim);
+  ++kernels;
+  cudaEventRecord(c->ev[2], s);
+  uint32_t n = npix;
+  const uint32_t* queue = nullptr;
+  uint32_t* qs[2] = {q0, q1};
+  uint32_t* hostCount = static_cast<uint32_t*>(c->pinned);
+  int layer = 0;
+  bool cancelled = false;
+  for (; layer < p.maxIters && n > 0; ++layer) {
+    uint32_t* outQ = qs[layer & 1];
+    UBR_CUDA(c, cudaMemsetAsync(b.counter, 0, sizeof(uint32_t), s));
+    const uint32_t grid = (n + TB - 1) / TB;
+    mark(0, true);
+    if (count) k_trace_closest<true><<<grid, TB, 0, s>>>(p, sc->view, b, layer, n, queue);
+    else k_trace_closest<false><<<grid, TB, 0, s>>>(p, sc->view, b, layer, n, queue);
+    mark(0, false);
+    ++kernels;
+    if (secondary) {
+      mark(1, true);
+      k_surface<<<grid, TB, 0, s>>>(p, sc->view, b, layer, n, queue);
+      mark(1, false);
+      const uint64_t nr = uint64_t(n) * uint64_t(p.raysPerHit);
+      const uint32_t og = uint32_t((nr + TB - 1) / TB);
+      mark(2, true);
+      if (count) k_trace_occlusion<true><<<og, TB, 0, s>>>(p, sc->view, b, n);
+      else k_trace_occlusion<false><<<og, TB, 0, s>>>(p, sc->view, b, n);
+      mark(2, false);
+      kernels += 2;
+    }
+    mark(3, true);
+    k_shade<<<grid, TB, 0, s>>>(p, sc->view, b, layer, n, queue, outQ);
+    mark(3, false);
+    ++kernels;
+    UBR_CUDA(c, cudaGetLastError());
+    if (layer + 1 >= p.maxIters) { ++layer; break; }
+    UBR_CUDA(c, cudaMemcpyAsync(hostCount, b.counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    UBR_CUDA(c, cudaStreamSynchronize(s));
+    n = *hostCount;
+    queue = outQ;
+    if (progress) *progress = uint64_t(layer + 1);
+    if (cancel && *cancel) {
+      cancelled = true;
+      ++layer;
+      break;
+    }
+  }
+  cudaEventRecord(c->ev[3], s);
+  mark(4, true);
+  k_post<<<(nout + 255) / 256, 256, 0, s>>>(p, b.colorHi, b.viewZ, outColor);
+  mark(4, false);
+  ++kernels;
+  UBR_CUDA(c, cudaGetLastError());
+  // outputs
+  const cudaMemcpyKind kind = fr.memory == UBR_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (fr.color) UBR_CUDA(c, cudaMemcpyAsync(fr.color, outColor, size_t(nout) * 16, kind, s));
+  if (fr.depth) UBR_CUDA(c, cudaMemcpyAsync(fr.depth, b.depth, size_t(npix) * 4, kind, s));
+  if (fr.view_z) UBR_CUDA(c, cudaMemcpyAsync(fr.view_z, b.viewZ, size_t(npix) * 4, kind, s));
+  if (fr.hit_geom) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_geom, b.hitGeom, size_t(npix) * 4, kind, s));
+  if (fr.hit_prim) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_prim, b.hitPrim, size_t(npix) * 4, kind, s));
+  unsigned long long* hs = reinterpret_cast<unsigned long long*>(static_cast<char*>(c->pinned) + 64);
+  UBR_CUDA(c, cudaMemcpyAsync(hs, b.stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  cudaEventRecord(c->ev[1], s);
+  UBR_CUDA(c, cudaStreamSynchronize(s));
+  float msTotal = 0.0f, msLoop = 0.0f;
+  cudaEventElapsedTime(&msTotal, c->ev[0], c->ev[1]);
+  cudaEventElapsedTime(&msLoop, c->ev[2], c->ev[3]);
+  fr.total_ms = msTotal;
+  fr.render_ms = msLoop;
+  fr.rays_primary = hs[0];
+  fr.rays_occlusion = hs[1];
+  fr.capped_rays = hs[2];
+  fr.stack_overflows = hs[3];
+  fr.layers = uint32_t(layer);
+  fr.kernels = kernels;
+  for (int k = 0; k < 5; ++k) fr.phase_ms[k] = 0.0;
+  for (const auto& m : marks) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, c->pev[size_t(m.second)], c->pev[size_t(m.second + 1)]);
+    fr.phase_ms[m.first] += ms;
+  }
+  fr.nodes_visited[0] = hs[4];
+  fr.nodes_visited[1] = hs[6];
+  fr.node_bytes[0] = hs[4] * uint64_t(kNodeF4 * 16);
+  fr.node_bytes[1] = hs[6] * uint64_t(kNodeF4 * 16);
+  fr.prim_bytes[0] = hs[5];
+  fr.prim_bytes[1] = hs[7];
+  if (cancelled) return setError(c, UBR_CANCELLED, "render cancelled");
+  if (hs[3] > 0) return setError(c, UBR_TRAVERSAL_LIMIT, "traversal stack overflow");
+  return UBR_OK;
+}
+
+ubr_status occludedBatch(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps, uint8_t* out,
+                         int32_t memory) {
+  if (n == 0) return UBR_OK;
+  if (!segs || !out) return setError(c, UBR_INVALID_ARGUMENT, "occluded_batch: NULL buffer");
+  ubr_status st = UBR_OK;
+  const float* dsegs = segs;
+  uint8_t* dout = out;
+  cudaStream_t s = c->stream;
+  if (memory != UBR_MEMORY_DEVICE) {
+    float* ts = scratchT<float>(c, 40, size_t(n) * 6, st);
+    dout = scratchT<uint8_t>(c, 41, size_t(n), st);
+    if (st != UBR_OK) return st;
+    UBR_CUDA(c, cudaMemcpyAsync(ts, segs, size_t(n) * 6 * sizeof(float), cudaMemcpyHostToDevice, s));
+    dsegs = ts;
+  }
+  unsigned long long* stats = scratchT<unsigned long long>(c, 42, 8, st);
+  if (st != UBR_OK) return st;
+  UBR_CUDA(c, cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), s));
+  k_occluded_segments<<<uint32_t((n + 127) / 128), 128, 0, s>>>(sc->view, dsegs, n, eps, dout, stats);
+  UBR_CUDA(c, cudaGetLastError());
+  if (memory != UBR_MEMORY_DEVICE) UBR_CUDA(c, cudaMemcpyAsync(out, dout, size_t(n), cudaMemcpyDeviceToHost, s));
+  UBR_CUDA(c, cudaStreamSynchronize(s));
+  return UBR_OK;
+}
+
+}  // namespace ubr

@@ -1,0 +1,680 @@
+// scene_build.cu -- ubr_scene_build: scene flattening + GPU LBVH.
+//
+// Host side: flatten ubr_scene_desc into per-kind primitive arrays in the
+// reference's primID order (render/scene_build.cpp:16-129 for the mesh and
+// spheres, render/curve_build.cpp:41-267 for open-cylinder chains and capped
+// cylinders), deduplicate materials into one table, upload.
+// Device side: a linear BVH (Karras, "Maximizing Parallelism in the
+// Construction of BVHs, Octrees, and k-d Trees", HPG 2012):
+//   k_prim_bounds  per-primitive AABB + centroid, centroid-bounds reduction
+//   k_morton       30-bit Morton code << idxBits | primitive index (unique)
+//   radix sort     CUB DeviceRadixSort over the used key bits only
+//   k_hierarchy    binary radix tree from longest common prefixes
+//   k_refit        leaves write their box into the parent, the second
+//                  arrival at each node (atomic counter) unions and climbs
+// The result replaces the Embree HIGH-quality BVH the reference commits
+// (scene_build.cpp:138-163); hits do not depend on the tree, only on the
+// intersectors, except for exact-t ties which resolve to the lowest
+// (geomID, primID).
+#include <cub/cub.cuh>
+
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <unordered_map>
+#include <vector>
+
+#include "ubr_context.h"
+
+namespace ubr {
+
+namespace {
+
+struct HostScene {
+  std::vector<float> pos, nrm;        // 3 per baked vertex
+  std::vector<float4> col;            // per baked vertex
+  std::vector<uint32_t> idx;          // 3 per triangle (baked)
+  std::vector<uint32_t> triMat;       // per base triangle (material index)
+  uint32_t meshMat = 0;
+  uint32_t baseTri = 0;
+  std::vector<float4> sph;            // (c, r)
+  std::vector<float4> rcV;            // round curve vertices (xyz, r)
+  std::vector<uint32_t> rcIdx;
+  std::vector<uint8_t> rcFlags;
+  std::vector<float4> rcClip;         // 2 per segment
+  std::vector<float4> ccV;
+  std::vector<uint32_t> ccIdx;
+  std::vector<float4> color[4];
+  std::vector<uint32_t> mat[4];
+  std::vector<uint8_t> fromEdge[4];
+  std::vector<float> opacity1[4];
+  std::vector<ubr_material> mats;
+  uint32_t geomID[4] = {kInvalid, kInvalid, kInvalid, kInvalid};
+  bool principled = false;
+};
+
+struct MatKey {
+  ubr_material m;
+  bool operator==(const MatKey& o) const { return std::memcmp(&m, &o.m, sizeof(m)) == 0; }
+};
+struct MatHash {
+  size_t operator()(const MatKey& k) const {
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(&k.m);
+    size_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < sizeof(k.m); ++i) h = (h ^ p[i]) * 1099511628211ull;
+    return h;
+  }
+};
+
+struct MatTable {
+  std::unordered_map<MatKey, uint32_t, MatHash> map;
+  std::vector<ubr_material>* out;
+  uint32_t get(const ubr_material& m) {
+    MatKey k{m};
+    auto it = map.find(k);
+    if (it != map.end()) return it->second;
+    const uint32_t id = static_cast<uint32_t>(out->size());
+    out->push_back(m);
+    map.emplace(k, id);
+    return id;
+  }
+};
+
+f3 ld3(const float* p, size_t i) { return f3{p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
+
+// curve_build.cpp:41-267, restated: open cylinders are chained into polylines
+// through endpoints quantised at 1e-4 (a vertex of degree 2 continues a chain
+// when group and opacity-gradient kind agree); each chain emits chainLen + 1
+// vertices whose radius is that of the segment ending there; segments carry
+// neighbour flags (bit0 left, bit1 right).  Capped cylinders become single
+// cone segments.  Both in instance-major order.
+void flattenCylinders(const ubr_scene_desc& d, const std::vector<f3>& offs, HostScene& s,
+                      MatTable& mt) {
+  const size_t n = d.cylinder_count;
+  if (n == 0) return;
+  std::vector<int> openIdx, capIdx;
+  for (size_t i = 0; i < n; ++i) {
+    if (d.cyl_open && d.cyl_open[i]) openIdx.push_back(int(i));
+    else capIdx.push_back(int(i));
+  }
+  auto op1 = [&](int i) { return d.cyl_opacity1 ? d.cyl_opacity1[i] : -1.0f; };
+  auto grp = [&](int i) { return d.cyl_group ? d.cyl_group[i] : uint16_t(0); };
+  auto side = [&](int kind, int i) {
+    s.color[kind].push_back(make_float4(d.cyl_color[4 * i], d.cyl_color[4 * i + 1],
+                                        d.cyl_color[4 * i + 2], d.cyl_color[4 * i + 3]));
+    s.mat[kind].push_back(mt.get(d.cyl_material[i]));
+    s.fromEdge[kind].push_back(d.cyl_from_edge && d.cyl_from_edge[i] ? 1 : 0);
+    s.opacity1[kind].push_back(op1(i));
+  };
+  if (!openIdx.empty()) {
+    const size_t no = openIdx.size();
+    const float eps = 1.0e-4f;
+    using Key = std::array<long long, 3>;
+    auto keyOf = [&](const f3& p) {
+      return Key{std::llround(p.x / eps), std::llround(p.y / eps), std::llround(p.z / eps)};
+    };
+    for (const f3& off : offs) {
+      std::vector<f3> a0(no), a1(no);
+      for (size_t i = 0; i < no; ++i) {
+        a0[i] = ld3(d.cyl_p0, openIdx[i]) + off;
+        a1[i] = ld3(d.cyl_p1, openIdx[i]) + off;
+      }
+      std::map<Key, std::vector<std::pair<int, int>>> inc;
+      for (int i = 0; i < int(no); ++i) {
+        inc[keyOf(a0[i])].push_back({i, 0});
+        inc[keyOf(a1[i])].push_back({i, 1});
+      }
+      std::vector<int> next(no, -1), prev(no, -1);
+      for (int sg = 0; sg < int(no); ++sg) {
+        const auto& ends = inc[keyOf(a1[sg])];
+        if (ends.size() != 2) continue;
+        int t = -1;
+        for (const auto& e : ends)
+          if (e.first != sg) t = (e.second == 0) ? e.first : -1;
+        if (t >= 0 && t != sg && grp(openIdx[sg]) == grp(openIdx[t]) &&
+            (op1(openIdx[sg]) < 0.0f) == (op1(openIdx[t]) < 0.0f))
+          next[sg] = t;
+      }
+      for (int sg = 0; sg < int(no); ++sg)
+        if (next[sg] >= 0) prev[next[sg]] = sg;
+      std::vector<char> visited(no, 0);
+      auto emit = [&](int start) {
+        std::vector<int> chain;
+        for (int sg = start; sg >= 0 && !visited[sg]; sg = next[sg]) {
+          visited[sg] = 1;
+          chain.push_back(sg);
+        }
+        const uint32_t base = uint32_t(s.rcV.size());
+        const f3 q = a0[chain[0]];
+        s.rcV.push_back(make_float4(q.x, q.y, q.z, d.cyl_radius[openIdx[chain[0]]]));
+        for (int cs : chain)
+          s.rcV.push_back(make_float4(a1[cs].x, a1[cs].y, a1[cs].z, d.cyl_radius[openIdx[cs]]));
+        const int nc = int(chain.size());
+        for (int j = 0; j < nc; ++j) {
+          s.rcIdx.push_back(base + uint32_t(j));
+          uint8_t fl = 0;
+          if (j > 0) fl |= 1u;
+          if (j < nc - 1) fl |= 2u;
+          s.rcFlags.push_back(fl);
+          side(kRound, openIdx[chain[j]]);
+        }
+      };
+      for (int sg = 0; sg < int(no); ++sg)
+        if (prev[sg] < 0 && !visited[sg]) emit(sg);
+      for (int sg = 0; sg < int(no); ++sg)
+        if (!visited[sg]) emit(sg);
+    }
+    // bisector clip planes at chain joints
+    auto vtx = [&](uint32_t i) { return f3{s.rcV[i].x, s.rcV[i].y, s.rcV[i].z}; };
+    for (size_t sg = 0; sg < s.rcIdx.size(); ++sg) {
+      const uint32_t v = s.rcIdx[sg];
+      const f3 p0 = vtx(v), p1 = vtx(v + 1);
+      const f3 dir = normalize(p1 - p0);
+      f3 cl{0, 0, 0}, cr{0, 0, 0};
+      if (s.rcFlags[sg] & 1u) cl = normalize(dir + normalize(p0 - vtx(v - 1)));
+      if (s.rcFlags[sg] & 2u) cr = normalize(dir + normalize(vtx(v + 2) - p1));
+      s.rcClip.push_back(make_float4(cl.x, cl.y, cl.z, 0.0f));
+      s.rcClip.push_back(make_float4(cr.x, cr.y, cr.z, 0.0f));
+    }
+  }
+  for (const f3& off : offs) {
+    for (int i : capIdx) {
+      const uint32_t base = uint32_t(s.ccV.size());
+      const f3 a = ld3(d.cyl_p0, i) + off, b = ld3(d.cyl_p1, i) + off;
+      const float r = d.cyl_radius[i];
+      s.ccV.push_back(make_float4(a.x, a.y, a.z, r));
+      s.ccV.push_back(make_float4(b.x, b.y, b.z, r));
+      s.ccIdx.push_back(base);
+      side(kCone, i);
+    }
+  }
+}
+
+ubr_status validate(Context* c, const ubr_scene_desc& d) {
+  if (d.abi_version != UBR_ABI_VERSION) return setError(c, UBR_INVALID_ARGUMENT, "scene desc: abi_version mismatch");
+  if (d.mesh_triangle_count > 0 && d.mesh_vertex_count >= 3 && !d.mesh_positions)
+    return setError(c, UBR_INVALID_ARGUMENT, "scene desc: mesh_positions is NULL");
+  if (d.mesh_index) {
+    for (uint64_t i = 0; i < 3 * d.mesh_triangle_count; ++i)
+      if (d.mesh_index[i] >= d.mesh_vertex_count)
+        return setError(c, UBR_INVALID_ARGUMENT, "scene desc: mesh_index out of range");
+  } else if (d.mesh_triangle_count * 3 > d.mesh_vertex_count) {
+    return setError(c, UBR_INVALID_ARGUMENT, "scene desc: de-indexed mesh needs 3 vertices per triangle");
+  }
+  if (d.mesh_tri_material) {
+    for (uint64_t i = 0; i < d.mesh_triangle_count; ++i)
+      if (d.mesh_tri_material[i] >= d.mesh_material_count)
+        return setError(c, UBR_INVALID_ARGUMENT, "scene desc: mesh_tri_material out of range");
+  }
+  if (d.sphere_count && (!d.sphere_center_radius || !d.sphere_color || !d.sphere_material))
+    return setError(c, UBR_INVALID_ARGUMENT, "scene desc: sphere arrays missing");
+  if (d.cylinder_count && (!d.cyl_p0 || !d.cyl_p1 || !d.cyl_radius || !d.cyl_color || !d.cyl_material))
+    return setError(c, UBR_INVALID_ARGUMENT, "scene desc: cylinder arrays missing");
+  if (d.instance_count && !d.instance_offsets)
+    return setError(c, UBR_INVALID_ARGUMENT, "scene desc: instance_offsets missing");
+  return UBR_OK;
+}
+
+ubr_status flatten(Context* c, const ubr_scene_desc& d, HostScene& s) {
+  std::vector<f3> offs;
+  for (uint64_t i = 0; i < d.instance_count; ++i) offs.push_back(ld3(d.instance_offsets, i));
+  if (offs.empty()) offs.push_back(f3{0, 0, 0});
+  const uint64_t total = (d.mesh_triangle_count + d.sphere_count + d.cylinder_count) * offs.size();
+  if (total >= (1ull << 30)) return setError(c, UBR_INVALID_ARGUMENT, "scene too large (>= 2^30 primitives)");
+  MatTable mt;
+  mt.out = &s.mats;
+  uint32_t nextGeom = 0;
+  const uint64_t baseV = d.mesh_vertex_count, baseT = d.mesh_triangle_count;
+  if (baseV >= 3 && baseT > 0) {
+    s.geomID[kMesh] = nextGeom++;
+    for (const f3& off : offs)
+      for (uint64_t v = 0; v < baseV; ++v) {
+        const f3 p = ld3(d.mesh_positions, v) + off;
+        s.pos.push_back(p.x);
+        s.pos.push_back(p.y);
+        s.pos.push_back(p.z);
+        for (int k = 0; k < 3; ++k) s.nrm.push_back(d.mesh_normals ? d.mesh_normals[3 * v + k] : 0.0f);
+        if (d.mesh_colors)
+          s.col.push_back(make_float4(d.mesh_colors[4 * v], d.mesh_colors[4 * v + 1], d.mesh_colors[4 * v + 2],
+                                      d.mesh_colors[4 * v + 3]));
+        else
+          s.col.push_back(make_float4(0, 0, 0, 1));
+      }
+    for (size_t ci = 0; ci < offs.size(); ++ci)
+      for (uint64_t t = 0; t < baseT; ++t)
+        for (int k = 0; k < 3; ++k) {
+          const uint64_t corner = 3 * t + k;
+          const uint32_t cv = d.mesh_index ? d.mesh_index[corner] : uint32_t(corner);
+          s.idx.push_back(uint32_t(ci * baseV + cv));
+        }
+    s.baseTri = uint32_t(baseT);
+    s.meshMat = mt.get(d.mesh_material);
+    if (d.mesh_tri_material) {
+      std::vector<uint32_t> remap(d.mesh_material_count);
+      for (uint32_t i = 0; i < d.mesh_material_count; ++i) remap[i] = mt.get(d.mesh_materials[i]);
+      s.triMat.resize(baseT);
+      for (uint64_t t = 0; t < baseT; ++t) s.triMat[t] = remap[d.mesh_tri_material[t]];
+    }
+  }
+  if (d.sphere_count > 0) {
+    s.geomID[kSphere] = nextGeom++;
+    for (const f3& off : offs)
+      for (uint64_t i = 0; i < d.sphere_count; ++i) {
+        const float* q = d.sphere_center_radius + 4 * i;
+        s.sph.push_back(make_float4(q[0] + off.x, q[1] + off.y, q[2] + off.z, q[3]));
+        s.color[kSphere].push_back(make_float4(d.sphere_color[4 * i], d.sphere_color[4 * i + 1],
+                                               d.sphere_color[4 * i + 2], d.sphere_color[4 * i + 3]));
+        s.mat[kSphere].push_back(mt.get(d.sphere_material[i]));
+        s.fromEdge[kSphere].push_back(d.sphere_from_edge && d.sphere_from_edge[i] ? 1 : 0);
+      }
+  }
+  flattenCylinders(d, offs, s, mt);
+  if (!s.rcIdx.empty()) s.geomID[kRound] = nextGeom++;
+  if (!s.ccIdx.empty()) s.geomID[kCone] = nextGeom++;
+  for (const ubr_material& m : s.mats)
+    if (m.model == 1) s.principled = true;
+  return UBR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// device build
+
+struct BuildIn {
+  const float* pos;
+  const uint32_t* idx;
+  const float4* sph;
+  const float4* rcV;
+  const uint32_t* rcIdx;
+  const uint8_t* rcFlags;
+  const float4* ccV;
+  const uint32_t* ccIdx;
+  uint32_t nTri, nSph, nRc, nCc;
+};
+
+__device__ __forceinline__ void globalToRef(const BuildIn& in, uint32_t g, int& kind, uint32_t& prim) {
+  if (g < in.nTri) { kind = kMesh; prim = g; return; }
+  g -= in.nTri;
+  if (g < in.nSph) { kind = kSphere; prim = g; return; }
+  g -= in.nSph;
+  if (g < in.nRc) { kind = kRound; prim = g; return; }
+  kind = kCone;
+  prim = g - in.nRc;
+}
+
+__device__ __forceinline__ int orderedInt(float f) {
+  int i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float orderedFloat(int i) {
+  return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF);
+}
+
+__global__ void k_prim_bounds(BuildIn in, uint32_t n, float4* boxLo, float4* boxHi, int* cbounds) {
+  __shared__ int sm[6][32];
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  float3 lo = make_float3(1e30f, 1e30f, 1e30f), hi = make_float3(-1e30f, -1e30f, -1e30f);
+  float3 cen = make_float3(0, 0, 0);
+  const bool valid = g < n;
+  if (valid) {
+    int kind;
+    uint32_t prim;
+    globalToRef(in, g, kind, prim);
+    auto grow = [&](float x, float y, float z, float r) {
+      lo.x = fminf(lo.x, x - r); lo.y = fminf(lo.y, y - r); lo.z = fminf(lo.z, z - r);
+      hi.x = fmaxf(hi.x, x + r); hi.y = fmaxf(hi.y, y + r); hi.z = fmaxf(hi.z, z + r);
+    };
+    if (kind == kMesh) {
+      for (int k = 0; k < 3; ++k) {
+        const uint32_t v = in.idx[3 * prim + k];
+        grow(in.pos[3 * v], in.pos[3 * v + 1], in.pos[3 * v + 2], 0.0f);
+      }
+    } else if (kind == kSphere) {
+      const float4 q = in.sph[prim];
+      grow(q.x, q.y, q.z, q.w);
+    } else {
+      const float4* V = kind == kRound ? in.rcV : in.ccV;
+      const uint32_t v = kind == kRound ? in.rcIdx[prim] : in.ccIdx[prim];
+      const float4 a = V[v], b = V[v + 1];
+      grow(a.x, a.y, a.z, a.w);
+      grow(b.x, b.y, b.z, b.w);
+    }
+    // conservative padding: relative to the extent and the magnitude
+    const float m = 1e-6f * fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(lo.y)), fmaxf(fabsf(lo.z), fabsf(hi.x))),
+                                  fmaxf(fmaxf(fabsf(hi.y), fabsf(hi.z)), 1.0f));
+    const float ex = (hi.x - lo.x) * 1e-6f + m, ey = (hi.y - lo.y) * 1e-6f + m, ez = (hi.z - lo.z) * 1e-6f + m;
+    lo.x -= ex; lo.y -= ey; lo.z -= ez;
+    hi.x += ex; hi.y += ey; hi.z += ez;
+    boxLo[g] = make_float4(lo.x, lo.y, lo.z, 0.0f);
+    boxHi[g] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+    cen = make_float3(0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z));
+  }
+  // block reduction of centroid bounds
+  int v[6];
+  v[0] = valid ? orderedInt(cen.x) : 0x7FFFFFFF;
+  v[1] = valid ? orderedInt(cen.y) : 0x7FFFFFFF;
+  v[2] = valid ? orderedInt(cen.z) : 0x7FFFFFFF;
+  v[3] = valid ? orderedInt(cen.x) : int(0x80000000);
+  v[4] = valid ? orderedInt(cen.y) : int(0x80000000);
+  v[5] = valid ? orderedInt(cen.z) : int(0x80000000);
+  for (int o = 16; o > 0; o >>= 1) {
+    for (int k = 0; k < 3; ++k) v[k] = min(v[k], __shfl_xor_sync(0xFFFFFFFFu, v[k], o));
+    for (int k = 3; k < 6; ++k) v[k] = max(v[k], __shfl_xor_sync(0xFFFFFFFFu, v[k], o));
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    for (int k = 0; k < 6; ++k) sm[k][warp] = v[k];
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int k = 0; k < 6; ++k) v[k] = lane < nw ? sm[k][lane] : (k < 3 ? 0x7FFFFFFF : int(0x80000000));
+    for (int o = 16; o > 0; o >>= 1) {
+      for (int k = 0; k < 3; ++k) v[k] = min(v[k], __shfl_xor_sync(0xFFFFFFFFu, v[k], o));
+      for (int k = 3; k < 6; ++k) v[k] = max(v[k], __shfl_xor_sync(0xFFFFFFFFu, v[k], o));
+    }
+    if (lane == 0) {
+      for (int k = 0; k < 3; ++k) atomicMin(&cbounds[k], v[k]);
+      for (int k = 3; k < 6; ++k) atomicMax(&cbounds[k], v[k]);
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t expandBits10(uint32_t v) {
+  v = (v * 0x00010001u) & 0xFF0000FFu;
+  v = (v * 0x00000101u) & 0x0F00F00Fu;
+  v = (v * 0x00000011u) & 0xC30C30C3u;
+  v = (v * 0x00000005u) & 0x49249249u;
+  return v;
+}
+
+__global__ void k_morton(uint32_t n, int idxBits, const float4* boxLo, const float4* boxHi,
+                         const int* cbounds, unsigned long long* keys) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const float4 lo = boxLo[g], hi = boxHi[g];
+  const float c[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
+  uint32_t q[3];
+  for (int k = 0; k < 3; ++k) {
+    const float bl = orderedFloat(cbounds[k]), bh = orderedFloat(cbounds[3 + k]);
+    const float ext = bh - bl;
+    float f = ext > 0.0f ? (c[k] - bl) / ext : 0.0f;
+    f = fminf(fmaxf(f, 0.0f), 1.0f);
+    q[k] = min(uint32_t(f * 1024.0f), 1023u);
+  }
+  const uint32_t m = (expandBits10(q[0]) << 2) | (expandBits10(q[1]) << 1) | expandBits10(q[2]);
+  keys[g] = (static_cast<unsigned long long>(m) << idxBits) | g;
+}
+
+__device__ __forceinline__ int deltaKey(const unsigned long long* keys, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  return __clzll(keys[i] ^ keys[j]);
+}
+
+// Karras 2012, Fig. 4: internal node i covers [min(i,j), max(i,j)], split at gamma.
+__global__ void k_hierarchy(int n, const unsigned long long* keys, float4* nodes, int* leafParent,
+                            int* nodeParent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (deltaKey(keys, n, i, i + 1) - deltaKey(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = deltaKey(keys, n, i, i - d);
+  int lmax = 2;
+  while (deltaKey(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (deltaKey(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = deltaKey(keys, n, i, j);
+  int s = 0, t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (deltaKey(keys, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  const int gamma = i + s * d + min(d, 0);
+  const int lo = min(i, j), hi = max(i, j);
+  int left, right;
+  if (lo == gamma) {
+    left = ~gamma;
+    leafParent[gamma] = (i << 1) | 0;
+  } else {
+    left = gamma;
+    nodeParent[gamma] = (i << 1) | 0;
+  }
+  if (hi == gamma + 1) {
+    right = ~(gamma + 1);
+    leafParent[gamma + 1] = (i << 1) | 1;
+  } else {
+    right = gamma + 1;
+    nodeParent[gamma + 1] = (i << 1) | 1;
+  }
+  nodes[kNodeF4 * i + 3] = make_float4(__int_as_float(left), __int_as_float(right), 0.0f, 0.0f);
+  if (i == 0) nodeParent[0] = -1;
+}
+
+__device__ __forceinline__ void writeChildBox(float4* nodes, int p, int side, float3 lo, float3 hi) {
+  float4* nd = nodes + kNodeF4 * p;
+  if (side == 0) {
+    nd[0] = make_float4(lo.x, hi.x, lo.y, hi.y);
+    float* z = reinterpret_cast<float*>(&nd[2]);
+    z[0] = lo.z;
+    z[1] = hi.z;
+  } else {
+    nd[1] = make_float4(lo.x, hi.x, lo.y, hi.y);
+    float* z = reinterpret_cast<float*>(&nd[2]);
+    z[2] = lo.z;
+    z[3] = hi.z;
+  }
+}
+
+// Leaf packing + bottom-up refit.  One thread per sorted slot.
+__global__ void k_refit(BuildIn in, int n, int idxBits, const unsigned long long* keys,
+                        const float4* boxLo, const float4* boxHi, const float4* rcClip,
+                        float4* nodes, const int* leafParent, const int* nodeParent, int* counters,
+                        uint32_t* leafRef, float4* leafGeo) {
+  const int sIdx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sIdx >= n) return;
+  const uint32_t g = uint32_t(keys[sIdx] & ((1ull << idxBits) - 1ull));
+  int kind;
+  uint32_t prim;
+  globalToRef(in, g, kind, prim);
+  leafRef[sIdx] = packRef(kind, prim);
+  float4* lg = leafGeo + kLeafF4 * sIdx;
+  if (kind == kMesh) {
+    for (int k = 0; k < 3; ++k) {
+      const uint32_t v = in.idx[3 * prim + k];
+      lg[k] = make_float4(in.pos[3 * v], in.pos[3 * v + 1], in.pos[3 * v + 2], 0.0f);
+    }
+  } else if (kind == kSphere) {
+    lg[0] = in.sph[prim];
+  } else {
+    const float4* V = kind == kRound ? in.rcV : in.ccV;
+    const uint32_t v = kind == kRound ? in.rcIdx[prim] : in.ccIdx[prim];
+    lg[0] = V[v];
+    lg[1] = V[v + 1];
+    lg[2] = make_float4(__uint_as_float(kind == kRound ? uint32_t(in.rcFlags[prim]) : 0u), 0, 0, 0);
+  }
+  if (n == 1) return;
+  const float4 bl = boxLo[g], bh = boxHi[g];
+  float3 lo = make_float3(bl.x, bl.y, bl.z), hi = make_float3(bh.x, bh.y, bh.z);
+  int pinfo = leafParent[sIdx];
+  while (pinfo >= 0) {
+    const int p = pinfo >> 1, side = pinfo & 1;
+    writeChildBox(nodes, p, side, lo, hi);
+    __threadfence();
+    if (atomicAdd(&counters[p], 1) == 0) return;
+    __threadfence();
+    const float4 a = __ldcg(&nodes[kNodeF4 * p + 0]);
+    const float4 b = __ldcg(&nodes[kNodeF4 * p + 1]);
+    const float4 z = __ldcg(&nodes[kNodeF4 * p + 2]);
+    lo = make_float3(fminf(a.x, b.x), fminf(a.z, b.z), fminf(z.x, z.z));
+    hi = make_float3(fmaxf(a.y, b.y), fmaxf(a.w, b.w), fmaxf(z.y, z.w));
+    pinfo = nodeParent[p];
+  }
+}
+
+template <class T>
+ubr_status upload(Context* c, Scene* sc, const std::vector<T>& v, const T** out) {
+  *out = nullptr;
+  if (v.empty()) return UBR_OK;
+  sc->bufs.emplace_back();
+  DevBuf& b = sc->bufs.back();
+  ubr_status st = devAlloc(c, b, v.size() * sizeof(T));
+  if (st != UBR_OK) return st;
+  UBR_CUDA(c, cudaMemcpyAsync(b.ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+  *out = static_cast<const T*>(b.ptr);
+  return UBR_OK;
+}
+
+ubr_status allocOwned(Context* c, Scene* sc, size_t bytes, void** out) {
+  sc->bufs.emplace_back();
+  DevBuf& b = sc->bufs.back();
+  ubr_status st = devAlloc(c, b, bytes);
+  *out = b.ptr;
+  return st;
+}
+
+int bitsFor(uint32_t n) {
+  int b = 1;
+  while ((1ull << b) < n) ++b;
+  return b;
+}
+
+}  // namespace
+
+ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
+  const auto t0 = std::chrono::steady_clock::now();
+  ubr_status st = validate(c, d);
+  if (st != UBR_OK) return st;
+  HostScene hs;
+  st = flatten(c, d, hs);
+  if (st != UBR_OK) return st;
+  if (hs.principled)
+    return setError(c, UBR_INVALID_ARGUMENT,
+                    "Principled materials are not supported by this library (POV finish only)");
+  Scene* sc = new Scene();
+  sc->ctx = c;
+  auto fail = [&](ubr_status s) {
+    for (DevBuf& b : sc->bufs) devFree(c, b);
+    delete sc;
+    return s;
+  };
+  DScene& v = sc->view;
+  const uint32_t nTri = uint32_t(hs.idx.size() / 3), nSph = uint32_t(hs.sph.size()),
+                 nRc = uint32_t(hs.rcIdx.size()), nCc = uint32_t(hs.ccIdx.size());
+  const uint32_t n = nTri + nSph + nRc + nCc;
+  sc->primCount[kMesh] = nTri;
+  sc->primCount[kSphere] = nSph;
+  sc->primCount[kRound] = nRc;
+  sc->primCount[kCone] = nCc;
+  for (int k = 0; k < 4; ++k) v.geomID[k] = hs.geomID[k];
+  v.primCount = n;
+  v.baseTri = hs.baseTri;
+  v.meshMat = hs.meshMat;
+  cudaEventRecord(c->ev[0], c->stream);
+  const float* dpos = nullptr;
+  const float4* dsph = nullptr;
+  const float4* drcV = nullptr;
+  const uint32_t* drcIdx = nullptr;
+  const uint8_t* drcFl = nullptr;
+  const float4* dccV = nullptr;
+  const uint32_t* dccIdx = nullptr;
+  if ((st = upload(c, sc, hs.pos, &dpos)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.nrm, &v.meshNrm)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.col, &v.meshCol)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.idx, &v.meshIdx)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.triMat, &v.meshTriMat)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.sph, &dsph)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.rcV, &drcV)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.rcIdx, &drcIdx)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.rcFlags, &drcFl)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.rcClip, &v.rcClip)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.ccV, &dccV)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.ccIdx, &dccIdx)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.mats, &v.mats)) != UBR_OK) return fail(st);
+  for (int k = 1; k < 4; ++k) {
+    if ((st = upload(c, sc, hs.color[k], &v.primColor[k])) != UBR_OK) return fail(st);
+    if ((st = upload(c, sc, hs.mat[k], &v.primMat[k])) != UBR_OK) return fail(st);
+    if ((st = upload(c, sc, hs.fromEdge[k], &v.primFromEdge[k])) != UBR_OK) return fail(st);
+    if ((st = upload(c, sc, hs.opacity1[k], &v.primOpacity1[k])) != UBR_OK) return fail(st);
+  }
+  if (n > 0) {
+    BuildIn in{dpos, v.meshIdx, dsph, drcV, drcIdx, drcFl, dccV, dccIdx, nTri, nSph, nRc, nCc};
+    void *pLo, *pHi, *pKeys, *pKeys2, *pCb, *pLeafP, *pNodeP, *pCnt, *pNodes, *pRef, *pGeo;
+    const size_t nn = n > 1 ? n - 1 : 1;
+    if ((st = allocOwned(c, sc, sizeof(float4) * kNodeF4 * nn, &pNodes)) != UBR_OK) return fail(st);
+    if ((st = allocOwned(c, sc, sizeof(uint32_t) * n, &pRef)) != UBR_OK) return fail(st);
+    if ((st = allocOwned(c, sc, sizeof(float4) * kLeafF4 * n, &pGeo)) != UBR_OK) return fail(st);
+    // build temporaries live in context scratch slots 0..7
+    if ((st = scratchGet(c, 0, sizeof(float4) * n, &pLo)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 1, sizeof(float4) * n, &pHi)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 2, sizeof(unsigned long long) * n, &pKeys)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 3, sizeof(unsigned long long) * n, &pKeys2)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 4, 64, &pCb)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 5, sizeof(int) * n, &pLeafP)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 6, sizeof(int) * nn, &pNodeP)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 7, sizeof(int) * nn, &pCnt)) != UBR_OK) return fail(st);
+    const int initB[6] = {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, int(0x80000000), int(0x80000000), int(0x80000000)};
+    UBR_CUDA(c, cudaMemcpyAsync(pCb, initB, sizeof(initB), cudaMemcpyHostToDevice, c->stream));
+    UBR_CUDA(c, cudaMemsetAsync(pCnt, 0, sizeof(int) * nn, c->stream));
+    // parents start at -1 so a refit walk always terminates
+    UBR_CUDA(c, cudaMemsetAsync(pLeafP, 0xFF, sizeof(int) * n, c->stream));
+    UBR_CUDA(c, cudaMemsetAsync(pNodeP, 0xFF, sizeof(int) * nn, c->stream));
+    UBR_CUDA(c, cudaMemsetAsync(pNodes, 0, sizeof(float4) * kNodeF4 * nn, c->stream));
+    const int TB = 256;
+    const int grid = int((n + TB - 1) / TB);
+    k_prim_bounds<<<grid, TB, 0, c->stream>>>(in, n, (float4*)pLo, (float4*)pHi, (int*)pCb);
+    const int idxBits = bitsFor(n);
+    k_morton<<<grid, TB, 0, c->stream>>>(n, idxBits, (const float4*)pLo, (const float4*)pHi, (const int*)pCb,
+                                         (unsigned long long*)pKeys);
+    size_t tmpBytes = 0;
+    cub::DeviceRadixSort::SortKeys(nullptr, tmpBytes, (unsigned long long*)pKeys, (unsigned long long*)pKeys2,
+                                   int(n), 0, 30 + idxBits, c->stream);
+    void* pTmp;
+    if ((st = scratchGet(c, 8, tmpBytes, &pTmp)) != UBR_OK) return fail(st);
+    UBR_CUDA(c, cub::DeviceRadixSort::SortKeys(pTmp, tmpBytes, (unsigned long long*)pKeys,
+                                               (unsigned long long*)pKeys2, int(n), 0, 30 + idxBits, c->stream));
+    if (n > 1)
+      k_hierarchy<<<int((n - 1 + TB - 1) / TB), TB, 0, c->stream>>>(int(n), (const unsigned long long*)pKeys2,
+                                                                   (float4*)pNodes, (int*)pLeafP, (int*)pNodeP);
+    k_refit<<<grid, TB, 0, c->stream>>>(in, int(n), idxBits, (const unsigned long long*)pKeys2,
+                                        (const float4*)pLo, (const float4*)pHi, v.rcClip, (float4*)pNodes,
+                                        (const int*)pLeafP, (const int*)pNodeP, (int*)pCnt, (uint32_t*)pRef,
+                                        (float4*)pGeo);
+    UBR_CUDA(c, cudaGetLastError());
+    v.nodes = (const float4*)pNodes;
+    v.leafRef = (const uint32_t*)pRef;
+    v.leafGeo = (const float4*)pGeo;
+    v.root = n > 1 ? 0 : ~0;
+    sc->nodes = n > 1 ? n - 1 : 0;
+    int cb[6];
+    UBR_CUDA(c, cudaMemcpyAsync(cb, pCb, sizeof(cb), cudaMemcpyDeviceToHost, c->stream));
+    cudaEventRecord(c->ev[1], c->stream);
+    UBR_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < 3; ++k) {
+      auto of = [](int i) {
+        int b = i >= 0 ? i : i ^ 0x7FFFFFFF;
+        float f;
+        std::memcpy(&f, &b, 4);
+        return f;
+      };
+      sc->lo[k] = of(cb[k]);
+      sc->hi[k] = of(cb[3 + k]);
+    }
+  } else {
+    cudaEventRecord(c->ev[1], c->stream);
+    UBR_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  for (const DevBuf& b : sc->bufs) sc->deviceBytes += b.bytes;
+  const auto t1 = std::chrono::steady_clock::now();
+  sc->buildMs = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  *out = sc;
+  return UBR_OK;
+}
+
+void releaseScene(Scene* sc) {
+  if (!sc) return;
+  for (DevBuf& b : sc->bufs) devFree(sc->ctx, b);
+  delete sc;
+}
+
+}  // namespace ubr

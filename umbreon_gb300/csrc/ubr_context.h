@@ -1,0 +1,61 @@
+// ubr_context.h -- context, device buffers and scene object of libubr.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "ubr_internal.h"
+
+namespace ubr {
+
+// A device allocation owned by the context or a scene.  Grows on demand;
+// contents are not preserved across growth.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct Context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool ownStream = false;
+  uint64_t arenaCap = 0;     // 0 = unlimited
+  uint64_t arenaUsed = 0;
+  std::string lastError;
+  // frame scratch, reused across frames
+  std::vector<DevBuf> scratch;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> pev;  // profiling events, created on first use
+  void* pinned = nullptr;    // small pinned host block for counters
+};
+
+struct Scene {
+  Context* ctx = nullptr;
+  DScene view;
+  std::vector<DevBuf> bufs;  // owned allocations
+  uint64_t primCount[4] = {0, 0, 0, 0};
+  uint64_t nodes = 0;
+  uint64_t deviceBytes = 0;
+  double buildMs = 0.0;
+  float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+
+// error helpers
+ubr_status setError(Context* c, ubr_status s, const std::string& msg);
+ubr_status cudaFail(Context* c, cudaError_t e, const char* what);
+// allocate `bytes` on the context's device, honouring the arena cap
+ubr_status devAlloc(Context* c, DevBuf& b, size_t bytes);
+void devFree(Context* c, DevBuf& b);
+// scratch slot `i` of at least `bytes`
+ubr_status scratchGet(Context* c, int i, size_t bytes, void** out);
+
+#define UBR_CUDA(ctx, call)                                  \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cudaFail((ctx), e_, #call); \
+  } while (0)
+
+}  // namespace ubr
