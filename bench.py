@@ -179,6 +179,10 @@ def run_ours(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     sc, opt = scenes.ball_and_stick()
+    if args.frame:
+        opt.width, opt.height = (int(x) for x in args.frame.lower().split("x"))
+    if args.ss:
+        opt.supersample = args.ss
     ctx = Context(local)
     built = ctx.build(sc)
     info = built.info()
@@ -258,7 +262,7 @@ def run_ours(args):
     host_color = np.zeros((opt.height, opt.width, 4), np.float32)
     desc, keepd = sc.to_desc()
     h2d = sum(a.nbytes for a in keepd)
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 5))
     e2e_rays = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -271,9 +275,9 @@ def run_ours(args):
         ctx._check(ctx._L.ubr_render(ctx.handle, h, C.byref(rd), C.byref(fr), None, None))
         e2e_rays += fr.rays_primary + fr.rays_occlusion
         ctx._L.ubr_scene_release(h)
-    e2e_s = time.perf_counter() - t0
-    e2e = {"value": round(e2e_rays * ws / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(host_color.nbytes), "ms_per_step": round(e2e_s / e2e_steps * 1e3, 2),
+    e2e_s = max(time.perf_counter() - t0, 1e-9)
+    e2e = None if args.no_e2e else {"value": round(e2e_rays * ws / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(host_color.nbytes), "ms_per_step": round(e2e_s / max(1, e2e_steps) * 1e3, 2),
            "steps": e2e_steps}
 
     cpu = None
@@ -290,7 +294,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms_frame, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded PCG32 random-walk chain)",
-            "config": {"workload": WORKLOAD, "frame": f"{opt.width}x{opt.height} ss{ss}",
+            "config": {"workload": WORKLOAD if not (args.frame or args.ss) else WORKLOAD + "_resized",
+                       "frame": f"{opt.width}x{opt.height} ss{opt.supersample}",
                        "primitives": info["prim_count"], "bvh_nodes": info["bvh_nodes"],
                        "l2": "flushed (256 MB write) before every timed frame",
                        "parallelism": f"replicas x{ws}"},
@@ -316,6 +321,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--frame", default=None, help="override the frame size WxH (profiling runs)")
+    ap.add_argument("--ss", type=int, default=0, help="override the supersample factor (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -179,38 +179,45 @@ inline bool intersectSphere(const Ray& r, V3 c, float rad, float tnear,
 
 // Ray vs. the lateral surface of a frustum on axis (base b, unit axis a):
 // radial distance rho(hax) = k0 + k1*hax for axial coordinate hax in [h0, h1].
-// Appends up to two roots (t, hax).
+// Float quadratic after moving the ray origin to the ray point closest to the
+// frustum's mid-axis point (parameter ts0); roots in the original parameter.
 inline int frustumRoots(const Ray& r, V3 b, V3 a, float h0, float h1, float k0,
                         float k1, float* ts, float* hs) {
-  const V3 w = r.org - b;
+  const V3 mid = b + a * (0.5f * (h0 + h1));
+  const float dd = dot(r.dir, r.dir);
+  const float ts0 = dot(mid - r.org, r.dir) / dd;
+  const V3 o = r.org + r.dir * ts0;
+  const V3 w = o - b;
   const float wa = dot(w, a), da = dot(r.dir, a);
-  const V3 wp = w - a * wa;          // radial part of the origin
-  const V3 dp = r.dir - a * da;      // radial part of the direction
-  // |wp + t dp|^2 = (k0 + k1 (wa + t da))^2
+  const V3 wp = w - a * wa;
+  const V3 dp = r.dir - a * da;
   const float g0 = k0 + k1 * wa, g1 = k1 * da;
-  const double qa = static_cast<double>(dot(dp, dp)) - static_cast<double>(g1) * g1;
-  const double qb = 2.0 * (static_cast<double>(dot(wp, dp)) - static_cast<double>(g0) * g1);
-  const double qc = static_cast<double>(dot(wp, wp)) - static_cast<double>(g0) * g0;
-  int n = 0;
-  if (std::fabs(qa) < 1e-30) {
-    if (std::fabs(qb) < 1e-30) return 0;
-    const float t = static_cast<float>(-qc / qb);
-    const float hh = wa + t * da;
-    if (hh >= h0 && hh <= h1 && k0 + k1 * hh >= 0.0f) { ts[n] = t; hs[n] = hh; ++n; }
-    return n;
+  const float A = dot(dp, dp) - g1 * g1;
+  const float B = dot(wp, dp) - g0 * g1;
+  const float Cc = dot(wp, wp) - g0 * g0;
+  float rr[2];
+  int m = 0;
+  if (std::fabs(A) <= 1e-12f * dd) {
+    if (B == 0.0f) return 0;
+    rr[m++] = -Cc / (2.0f * B);
+  } else {
+    const float disc = B * B - A * Cc;
+    if (disc < 0.0f) return 0;
+    const float sq = std::sqrt(disc);
+    const float q = -(B + std::copysign(sq, B));
+    float r0 = q / A, r1 = q != 0.0f ? Cc / q : r0;
+    if (r0 > r1) std::swap(r0, r1);
+    rr[m++] = r0;
+    rr[m++] = r1;
   }
-  const double disc = qb * qb - 4.0 * qa * qc;
-  if (disc < 0.0) return 0;
-  const double sq = std::sqrt(disc);
-  // numerically stable pair
-  const double q = (qb < 0.0) ? -0.5 * (qb - sq) : -0.5 * (qb + sq);
-  double r0 = q / qa, r1 = (q != 0.0) ? qc / q : r0;
-  if (r0 > r1) std::swap(r0, r1);
-  const double rr[2] = {r0, r1};
-  for (int i = 0; i < 2; ++i) {
-    const float t = static_cast<float>(rr[i]);
-    const float hh = wa + t * da;
-    if (hh >= h0 && hh <= h1 && k0 + k1 * hh >= 0.0f) { ts[n] = t; hs[n] = hh; ++n; }
+  int n = 0;
+  for (int i = 0; i < m; ++i) {
+    const float hh = wa + rr[i] * da;
+    if (hh >= h0 && hh <= h1 && k0 + k1 * hh >= 0.0f) {
+      ts[n] = ts0 + rr[i];
+      hs[n] = hh;
+      ++n;
+    }
   }
   return n;
 }

@@ -99,21 +99,31 @@ UBR_D bool slabHit(float lox, float hix, float loy, float hiy, float loz, float 
   return tmin <= tmx;
 }
 
+// Kind masks: bit k set when primitives of kind k exist.  Kernels are
+// instantiated per mask so a scene only carries the intersectors it needs.
+constexpr int kMaskMesh = 1 << kMesh, kMaskSphere = 1 << kSphere, kMaskRound = 1 << kRound,
+              kMaskCone = 1 << kCone, kMaskAll = 15;
+
+template <int KM>
 UBR_D bool testLeaf(const DScene& s, int slot, const Ray& r, const TriPre& pre, float tnear,
                     float tmax, Hit& h, uint32_t& ref) {
   ref = __ldg(&s.leafRef[slot]);
   const int kind = refKind(ref);
   const float4* g = s.leafGeo + kLeafF4 * slot;
-  if (kind == kSphere) {
+  constexpr bool single = (KM & (KM - 1)) == 0;
+  if ((KM & kMaskSphere) && (single || kind == kSphere)) {
     const float4 q = __ldg(g);
     return isectSphere(r, f3{q.x, q.y, q.z}, q.w, tnear, tmax, h);
   }
-  if (kind == kMesh) {
+  if ((KM & kMaskMesh) && (single || kind == kMesh)) {
     const float4 a = __ldg(g), b = __ldg(g + 1), c = __ldg(g + 2);
     return isectTriangle(r, pre, ld3(a), ld3(b), ld3(c), tnear, tmax, h);
   }
+  if (!(KM & (kMaskCone | kMaskRound))) return false;
   const float4 a = __ldg(g), b = __ldg(g + 1);
-  if (kind == kCone) return isectConeCurve(r, ld3(a), a.w, ld3(b), b.w, tnear, tmax, h);
+  if ((KM & kMaskCone) && (!(KM & kMaskRound) || kind == kCone))
+    return isectConeCurve(r, ld3(a), a.w, ld3(b), b.w, tnear, tmax, h);
+  if (!(KM & kMaskRound)) return false;
   const uint32_t prim = refPrim(ref);
   const uint32_t flags = __float_as_uint(__ldg(g + 2).x);
   const float4 cl = __ldg(&s.rcClip[2 * prim]), cr = __ldg(&s.rcClip[2 * prim + 1]);
@@ -133,12 +143,13 @@ struct Count {
   uint32_t nodes = 0, primBytes = 0;
 };
 
-template <bool ANY, bool COUNT = false>
+template <bool ANY, bool COUNT = false, int KM = kMaskAll>
 __device__ bool traverse(const DScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt = nullptr) {
   best.ref = kInvalid;
   if (s.primCount == 0) return false;
   const f3 inv = safeInv(r.dir);
-  const TriPre pre = triPre(r.dir);
+  TriPre pre;
+  if (KM & kMaskMesh) pre = triPre(r.dir);
   float tmax = r.tfar;
   int stack[kStackDepth];
   int sp = 0;
@@ -173,7 +184,7 @@ __device__ bool traverse(const DScene& s, const Ray& r, Hit& best, uint32_t& ove
     } else {
       Hit h;
       uint32_t ref;
-      const bool hitLeaf = testLeaf(s, ~code, r, pre, r.tnear, tmax, h, ref);
+      const bool hitLeaf = testLeaf<KM>(s, ~code, r, pre, r.tnear, tmax, h, ref);
       if (COUNT) cnt->primBytes += leafBytes(refKind(ref));
       if (hitLeaf) {
         if (ANY) {
@@ -361,7 +372,7 @@ UBR_D void warpCount(unsigned long long* ctr, uint32_t v) {
 // ---------------------------------------------------------------------------
 // kernels
 
-template <bool COUNT>
+template <bool COUNT, int KM>
 __global__ void __launch_bounds__(128) k_trace_closest(Params p, DScene s, Bufs b, int layer, uint32_t n,
                                                        const uint32_t* queue) {
   Count cnt;
@@ -376,7 +387,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(Params p, DScene s, Bufs 
     clipRange(p, rd, ctn, ctf);
     Ray r{org, rd, layer == 0 ? ctn : b.tnear[pix], ctf};
     Hit h;
-    traverse<false, COUNT>(s, r, h, ovf, &cnt);
+    traverse<false, COUNT, KM>(s, r, h, ovf, &cnt);
     traced = 1;
     b.hitA[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.ref));
     b.hitB[i] = make_float4(h.Ng.x, h.Ng.y, h.Ng.z, 0.0f);
@@ -414,7 +425,7 @@ __global__ void __launch_bounds__(128) k_surface(Params p, DScene s, Bufs b, int
   b.surfC[i] = make_uint2(pix, 1u | (sf.aoOn ? 2u : 0u) | (sf.shOn ? 4u : 0u));
 }
 
-template <bool COUNT>
+template <bool COUNT, int KM>
 __global__ void __launch_bounds__(128) k_trace_occlusion(Params p, DScene s, Bufs b, uint32_t n) {
   Count cnt;
   const uint64_t tid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -441,11 +452,11 @@ __global__ void __launch_bounds__(128) k_trace_occlusion(Params p, DScene s, Buf
           Ray r{ld3(sa), dir, tnear, p.aoDistance};
           Hit h;
           if (p.aoEnhanced) {
-            const bool hit = traverse<false, COUNT>(s, r, h, ovf, &cnt);
+            const bool hit = traverse<false, COUNT, KM>(s, r, h, ovf, &cnt);
             b.aoT[uint64_t(slot) * p.aoSamples + j] = hit ? h.t : kInfF;
             res = hit ? 1 : 0;
           } else {
-            res = traverse<true, COUNT>(s, r, h, ovf, &cnt) ? 1 : 0;
+            res = traverse<true, COUNT, KM>(s, r, h, ovf, &cnt) ? 1 : 0;
           }
           traced = 1;
         }
@@ -475,7 +486,7 @@ __global__ void __launch_bounds__(128) k_trace_occlusion(Params p, DScene s, Buf
         }
         Ray r{ld3(sa), dir, sa.w, kInfF};
         Hit h;
-        res = traverse<true, COUNT>(s, r, h, ovf, &cnt) ? 1 : 0;
+        res = traverse<true, COUNT, KM>(s, r, h, ovf, &cnt) ? 1 : 0;
         traced = 1;
       }
     }
@@ -920,6 +931,57 @@ __global__ void k_occluded_segments(DScene s, const float* segs, uint64_t n, flo
   warpCount(&stats[3], ovf);
 }
 
+// Kind mask of a scene, rounded to one of the instantiated variants.
+int kindMask(const Scene& sc) {
+  int m = 0;
+  for (int k = 0; k < 4; ++k)
+    if (sc.primCount[k]) m |= 1 << k;
+  switch (m) {
+    case kMaskMesh:
+    case kMaskSphere:
+    case kMaskMesh | kMaskSphere:
+    case kMaskSphere | kMaskCone:
+      return m;
+    default:
+      return kMaskAll;
+  }
+}
+
+#define UBR_KM_DISPATCH(KERNEL, km, count, grid, tb, stream, ...)                                \
+  do {                                                                                           \
+    switch (km) {                                                                                \
+      case kMaskMesh:                                                                            \
+        if (count) KERNEL<true, kMaskMesh><<<grid, tb, 0, stream>>>(__VA_ARGS__);               \
+        else KERNEL<false, kMaskMesh><<<grid, tb, 0, stream>>>(__VA_ARGS__);                    \
+        break;                                                                                   \
+      case kMaskSphere:                                                                          \
+        if (count) KERNEL<true, kMaskSphere><<<grid, tb, 0, stream>>>(__VA_ARGS__);             \
+        else KERNEL<false, kMaskSphere><<<grid, tb, 0, stream>>>(__VA_ARGS__);                  \
+        break;                                                                                   \
+      case kMaskMesh | kMaskSphere:                                                              \
+        if (count) KERNEL<true, kMaskMesh | kMaskSphere><<<grid, tb, 0, stream>>>(__VA_ARGS__); \
+        else KERNEL<false, kMaskMesh | kMaskSphere><<<grid, tb, 0, stream>>>(__VA_ARGS__);      \
+        break;                                                                                   \
+      case kMaskSphere | kMaskCone:                                                              \
+        if (count) KERNEL<true, kMaskSphere | kMaskCone><<<grid, tb, 0, stream>>>(__VA_ARGS__); \
+        else KERNEL<false, kMaskSphere | kMaskCone><<<grid, tb, 0, stream>>>(__VA_ARGS__);      \
+        break;                                                                                   \
+      default:                                                                                   \
+        if (count) KERNEL<true, kMaskAll><<<grid, tb, 0, stream>>>(__VA_ARGS__);                \
+        else KERNEL<false, kMaskAll><<<grid, tb, 0, stream>>>(__VA_ARGS__);                     \
+    }                                                                                            \
+  } while (0)
+
+void launchClosest(int km, bool count, uint32_t grid, int tb, cudaStream_t st, const Params& p, const DScene& s,
+                   const Bufs& b, int layer, uint32_t n, const uint32_t* queue) {
+  UBR_KM_DISPATCH(k_trace_closest, km, count, grid, tb, st, p, s, b, layer, n, queue);
+}
+
+void launchOcclusion(int km, bool count, uint32_t grid, int tb, cudaStream_t st, const Params& p, const DScene& s,
+                     const Bufs& b, uint32_t n) {
+  UBR_KM_DISPATCH(k_trace_occlusion, km, count, grid, tb, st, p, s, b, n);
+}
+
 template <class T>
 T* scratchT(Context* c, int slot, size_t count, ubr_status& st) {
   void* ptr = nullptr;
@@ -967,6 +1029,7 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
   cudaStream_t s = c->stream;
   uint32_t kernels = 0;
   const bool prof = (fr.flags & UBR_FRAME_PROFILE) != 0;
+  const int km = kindMask(*sc);
   const bool count = (fr.flags & UBR_FRAME_COUNT) != 0;
   // phase timing: pairs of events per launch, summed per phase after the sync
   std::vector<std::pair<int, int>> marks;  // (phase, event index of the start)
@@ -1005,8 +1068,7 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
     UBR_CUDA(c, cudaMemsetAsync(b.counter, 0, sizeof(uint32_t), s));
     const uint32_t grid = (n + TB - 1) / TB;
     mark(0, true);
-    if (count) k_trace_closest<true><<<grid, TB, 0, s>>>(p, sc->view, b, layer, n, queue);
-    else k_trace_closest<false><<<grid, TB, 0, s>>>(p, sc->view, b, layer, n, queue);
+    launchClosest(km, count, grid, TB, s, p, sc->view, b, layer, n, queue);
     mark(0, false);
     ++kernels;
     if (secondary) {
@@ -1016,8 +1078,7 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
       const uint64_t nr = uint64_t(n) * uint64_t(p.raysPerHit);
       const uint32_t og = uint32_t((nr + TB - 1) / TB);
       mark(2, true);
-      if (count) k_trace_occlusion<true><<<og, TB, 0, s>>>(p, sc->view, b, n);
-      else k_trace_occlusion<false><<<og, TB, 0, s>>>(p, sc->view, b, n);
+      launchOcclusion(km, count, og, TB, s, p, sc->view, b, n);
       mark(2, false);
       kernels += 2;
     }

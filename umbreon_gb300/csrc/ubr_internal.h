@@ -200,45 +200,48 @@ UBR_HD bool isectSphere(const Ray& r, f3 c, float rad, float tnear, float tmax, 
 }
 
 // Lateral surface of a frustum on axis (b, unit a), radius k0 + k1*hax over
-// axial range [h0, h1]; quadratic solved in double.  Up to two roots.
+// axial range [h0, h1].  Solved in float: the ray origin is first moved to
+// the point of the ray closest to the frustum's mid-axis point (parameter
+// ts0), so the quadratic's coefficients stay small and well conditioned;
+// roots are returned in the original ray parameter.  Up to two roots.
 UBR_HD int frustumRoots(const Ray& r, f3 b, f3 a, float h0, float h1, float k0, float k1,
                         float* ts, float* hs) {
-  const f3 w = r.org - b;
+  const f3 mid = b + a * (0.5f * (h0 + h1));
+  const float dd = dot(r.dir, r.dir);
+  const float ts0 = dot(mid - r.org, r.dir) / dd;
+  const f3 o = r.org + r.dir * ts0;
+  const f3 w = o - b;
   const float wa = dot(w, a), da = dot(r.dir, a);
   const f3 wp = w - a * wa;
   const f3 dp = r.dir - a * da;
   const float g0 = k0 + k1 * wa, g1 = k1 * da;
-  const double qa = double(dot(dp, dp)) - double(g1) * g1;
-  const double qb = 2.0 * (double(dot(wp, dp)) - double(g0) * g1);
-  const double qc = double(dot(wp, wp)) - double(g0) * g0;
-  int n = 0;
-  if (fabs(qa) < 1e-30) {
-    if (fabs(qb) < 1e-30) return 0;
-    const float t = float(-qc / qb);
-    const float hh = wa + t * da;
-    if (hh >= h0 && hh <= h1 && k0 + k1 * hh >= 0.0f) {
-      ts[n] = t;
-      hs[n] = hh;
-      ++n;
+  const float A = dot(dp, dp) - g1 * g1;
+  const float B = dot(wp, dp) - g0 * g1;  // half of the linear coefficient
+  const float Cc = dot(wp, wp) - g0 * g0;
+  float rr[2];
+  int m = 0;
+  if (fabsf(A) <= 1e-12f * dd) {
+    if (B == 0.0f) return 0;
+    rr[m++] = -Cc / (2.0f * B);
+  } else {
+    const float disc = B * B - A * Cc;
+    if (disc < 0.0f) return 0;
+    const float sq = sqrtf(disc);
+    const float q = -(B + copysignf(sq, B));
+    float r0 = q / A, r1 = q != 0.0f ? Cc / q : r0;
+    if (r0 > r1) {
+      const float t = r0;
+      r0 = r1;
+      r1 = t;
     }
-    return n;
+    rr[m++] = r0;
+    rr[m++] = r1;
   }
-  const double disc = qb * qb - 4.0 * qa * qc;
-  if (disc < 0.0) return 0;
-  const double sq = sqrt(disc);
-  const double q = (qb < 0.0) ? -0.5 * (qb - sq) : -0.5 * (qb + sq);
-  double r0 = q / qa, r1 = (q != 0.0) ? qc / q : r0;
-  if (r0 > r1) {
-    double t = r0;
-    r0 = r1;
-    r1 = t;
-  }
-  const double rr[2] = {r0, r1};
-  for (int i = 0; i < 2; ++i) {
-    const float t = float(rr[i]);
-    const float hh = wa + t * da;
+  int n = 0;
+  for (int i = 0; i < m; ++i) {
+    const float hh = wa + rr[i] * da;
     if (hh >= h0 && hh <= h1 && k0 + k1 * hh >= 0.0f) {
-      ts[n] = t;
+      ts[n] = ts0 + rr[i];
       hs[n] = hh;
       ++n;
     }
