@@ -1,0 +1,163 @@
+// umbreon::render through the GB300 library: the reference's own render
+// known answers (tests/test_render_shading.cpp, test_render_transparency.cpp,
+// test_render_shadows_gi.cpp), group-alpha blending and async/cancel, written
+// against the unchanged public API.
+#include <chrono>
+#include <stdexcept>
+#include <vector>
+
+#include "check.hpp"
+#include "postprocess/image_ops.hpp"
+#include "umbreon.hpp"
+
+using umbreon::Vec3;
+using umbreon::Vec4;
+
+namespace {
+constexpr std::size_t kC = (2 * 5 + 2) * 4;
+
+umbreon::Mesh quad(Vec4 col, float z = 0.0f) {
+  umbreon::Mesh m;
+  const Vec3 p[6] = {{-2, -2, z}, {2, -2, z}, {2, 2, z}, {-2, -2, z}, {2, 2, z}, {-2, 2, z}};
+  for (const Vec3& v : p) {
+    m.positions.push_back(v);
+    m.normals.push_back({0, 0, 1});
+    m.colors.push_back(col);
+  }
+  m.material.ambient = 0.2f;
+  m.material.diffuse = 0.8f;
+  return m;
+}
+umbreon::Camera cam() {
+  umbreon::Camera c;
+  c.position = {0, 0, 10};
+  c.direction = {0, 0, -1};
+  c.orthographic = true;
+  c.height = 4.0f;
+  return c;
+}
+umbreon::DistantLight key() {
+  umbreon::DistantLight l;
+  l.direction = {0, 0, -1};
+  l.intensity = 0.5f;
+  return l;
+}
+umbreon::RenderOptions o5() {
+  umbreon::RenderOptions o;
+  o.width = 5;
+  o.height = 5;
+  return o;
+}
+void addQuad(umbreon::Mesh& m, Vec4 col, float z, uint16_t g) {
+  const umbreon::Mesh q = quad(col, z);
+  m.positions.insert(m.positions.end(), q.positions.begin(), q.positions.end());
+  m.normals.insert(m.normals.end(), q.normals.begin(), q.normals.end());
+  m.colors.insert(m.colors.end(), q.colors.begin(), q.colors.end());
+  m.triGroupId.push_back(g);
+  m.triGroupId.push_back(g);
+}
+}  // namespace
+
+int main() {
+  Checks c;
+  {  // mesh direct shading: C * (0.2 + 0.8 * 0.5)
+    umbreon::Scene sc;
+    sc.mesh = quad({0.5f, 0.6f, 0.7f, 1.0f});
+    sc.camera = cam();
+    sc.lights.push_back(key());
+    umbreon::FrameResult f = umbreon::render(sc, o5());
+    c("mesh centre = C*0.6", near(f.color[kC], 0.30f, 1e-4f) && near(f.color[kC + 1], 0.36f, 1e-4f) &&
+                                 near(f.color[kC + 2], 0.42f, 1e-4f));
+    c("mesh depth = 10", near(f.depth[12], 10.0f, 1e-3f));
+    c("frame size", f.width == 5 && f.height == 5 && f.color.size() == 100);
+  }
+  {  // supersample keeps the final size and the uniform value
+    umbreon::Scene sc;
+    sc.mesh = quad({0.5f, 0.6f, 0.7f, 1.0f});
+    sc.camera = cam();
+    sc.lights.push_back(key());
+    umbreon::RenderOptions o = o5();
+    o.supersample = 2;
+    umbreon::FrameResult f = umbreon::render(sc, o);
+    c("ss2 final 5x5, depth on the 10x10 grid", f.width == 5 && f.depth.size() == 100);
+    c("ss2 value", near(f.color[kC], 0.30f, 1e-4f));
+  }
+  {  // fragment over, F2 order dependence
+    umbreon::Mesh m;
+    addQuad(m, {1, 0, 0, 1.0f}, 0.0f, 0);
+    addQuad(m, {0, 0, 1, 0.5f}, 0.5f, 2);
+    addQuad(m, {0, 1, 0, 0.5f}, 1.0f, 1);
+    m.material = umbreon::Material::flatOutline();
+    umbreon::Scene sc;
+    sc.mesh = m;
+    sc.camera = cam();
+    umbreon::FrameResult f = umbreon::render(sc, o5());
+    c("F2 green front G=0.5 B=0.25", near(f.color[kC + 1], 0.5f, 1e-4f) && near(f.color[kC + 2], 0.25f, 1e-4f));
+  }
+  {  // group-alpha T1: 0.6 * blue + 0.4 * red in the display domain
+    umbreon::Mesh m;
+    addQuad(m, {1, 0, 0, 1.0f}, 0.0f, 0);
+    addQuad(m, {0, 0, 1, 1.0f}, 1.0f, 1);
+    m.material = umbreon::Material::flatOutline();
+    umbreon::Scene sc;
+    sc.mesh = m;
+    sc.camera = cam();
+    sc.groupBlend.push_back({1, 0.6f});
+    umbreon::FrameResult f = umbreon::render(sc, o5());
+    c("T1 blend R=0.4 B=0.6 (sRGB domain)", near(umbreon::srgbEncodeF(f.color[kC]), 0.4f, 1e-4f) &&
+                                                near(umbreon::srgbEncodeF(f.color[kC + 2]), 0.6f, 1e-4f));
+  }
+  {  // hard shadow from a slab
+    umbreon::Scene sc;
+    sc.mesh = quad({1, 1, 1, 1});
+    const umbreon::Mesh slab = quad({0, 0, 0, 1}, 0.4f);
+    for (int i = 0; i < 6; ++i) {
+      Vec3 p = slab.positions[i];
+      p.x = p.x < 0 ? 0.1f : 4.0f;
+      sc.mesh.positions.push_back(p);
+      sc.mesh.normals.push_back({0, 0, -1});
+      sc.mesh.colors.push_back({0, 0, 0, 1});
+    }
+    sc.camera = cam();
+    umbreon::DistantLight l;
+    l.direction = {-0.6f, 0.0f, -0.8f};
+    sc.lights.push_back(l);
+    umbreon::RenderOptions off = o5(), on = o5();
+    on.shadows = true;
+    const float a = umbreon::render(sc, off).color[kC], b = umbreon::render(sc, on).color[kC];
+    c("shadow off ~0.84, on ~0.2", near(a, 0.84f, 0.03f) && near(b, 0.2f, 0.03f));
+  }
+  {  // unsupported requests throw like the reference's failures
+    umbreon::Scene sc;
+    sc.mesh = quad({1, 1, 1, 1});
+    sc.camera = cam();
+    umbreon::RenderOptions o = o5();
+    o.gi = true;
+    bool threw = false;
+    try {
+      umbreon::render(sc, o);
+    } catch (const std::runtime_error&) {
+      threw = true;
+    }
+    c("gi request throws std::runtime_error", threw);
+  }
+  {  // async == blocking; cancel before start yields a cancelled frame
+    umbreon::Scene sc;
+    sc.mesh = quad({0.5f, 0.6f, 0.7f, 1.0f});
+    sc.camera = cam();
+    sc.lights.push_back(key());
+    umbreon::RenderOptions o = o5();
+    o.aoSamples = 8;
+    o.aoDistance = 10.0f;
+    const umbreon::FrameResult blocking = umbreon::render(sc, o);
+    umbreon::RenderTask t = umbreon::renderAsync(sc, o);
+    t.wait();
+    const umbreon::FrameResult async = t.get();
+    c("async result == blocking result", async.color == blocking.color);
+    umbreon::RenderProgress p;
+    p.requestCancel();
+    const umbreon::FrameResult cf = umbreon::render(sc, o, p);
+    c("pre-cancelled render reports cancelled", cf.cancelled);
+  }
+  return c.report("host_render");
+}

@@ -51,7 +51,8 @@ struct Bufs {
   float* aoT;         // per slot * aoSamples (enhanced AO nearest t)
   const LightD* lights;
   unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
-  uint32_t* counter;  // next-queue size
+  uint32_t* counter;  // [0] next-queue size, [1] occlusion work-queue size
+  uint32_t* occQueue; // queue slots of hits that cast AO / shadow rays
 };
 
 UBR_D f3 ld3(const float4 v) { return f3{v.x, v.y, v.z}; }
@@ -403,26 +404,34 @@ __global__ void __launch_bounds__(128) k_trace_closest(Params p, DScene s, Bufs 
 __global__ void __launch_bounds__(128) k_surface(Params p, DScene s, Bufs b, int layer, uint32_t n,
                                                  const uint32_t* queue) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t pix = layer == 0 ? i : queue[i];
-  const float4 ha = b.hitA[i];
-  const uint32_t ref = __float_as_uint(ha.w);
-  if (ref == kInvalid) {
-    b.surfC[i] = make_uint2(pix, 0u);
-    return;
+  bool cast = false;
+  if (i < n) {
+    const uint32_t pix = layer == 0 ? i : queue[i];
+    const float4 ha = b.hitA[i];
+    const uint32_t ref = __float_as_uint(ha.w);
+    if (ref == kInvalid) {
+      b.surfC[i] = make_uint2(pix, 0u);
+    } else {
+      const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
+      f3 org, rd;
+      primaryRay(p, px, py, org, rd);
+      const float4 hb = b.hitB[i];
+      const Surf sf = surfaceAt(p, s, org, rd, ha.x, ref, ha.y, ha.z, f3{hb.x, hb.y, hb.z});
+      // computeAO / computeShadow origin: P + safeNormalize(faceForward-to-N(Ng)) * eps
+      f3 ng = dot(sf.Ng, sf.N) < 0.0f ? neg(sf.Ng) : sf.Ng;
+      ng = safeNormalize(ng, sf.N);
+      const f3 O = sf.P + ng * sf.secEps;
+      b.surfA[i] = make_float4(O.x, O.y, O.z, sf.secEps);
+      b.surfB[i] = make_float4(sf.N.x, sf.N.y, sf.N.z, 0.0f);
+      const uint32_t flags = 1u | (sf.aoOn ? 2u : 0u) | (sf.shOn ? 4u : 0u);
+      b.surfC[i] = make_uint2(pix, flags);
+      cast = (flags & 6u) != 0u;
+    }
   }
-  const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
-  f3 org, rd;
-  primaryRay(p, px, py, org, rd);
-  const float4 hb = b.hitB[i];
-  const Surf sf = surfaceAt(p, s, org, rd, ha.x, ref, ha.y, ha.z, f3{hb.x, hb.y, hb.z});
-  // computeAO / computeShadow origin: P + safeNormalize(faceForward-to-N(Ng)) * eps
-  f3 ng = dot(sf.Ng, sf.N) < 0.0f ? neg(sf.Ng) : sf.Ng;
-  ng = safeNormalize(ng, sf.N);
-  const f3 O = sf.P + ng * sf.secEps;
-  b.surfA[i] = make_float4(O.x, O.y, O.z, sf.secEps);
-  b.surfB[i] = make_float4(sf.N.x, sf.N.y, sf.N.z, 0.0f);
-  b.surfC[i] = make_uint2(pix, 1u | (sf.aoOn ? 2u : 0u) | (sf.shOn ? 4u : 0u));
+  // compact the hits that cast secondary rays so occlusion warps hold only live rays
+  int off;
+  const int qb = warpPushBase(cast, b.counter + 1, off);
+  if (cast) b.occQueue[qb + off] = i;
 }
 
 template <bool COUNT, int KM>
@@ -431,8 +440,9 @@ __global__ void __launch_bounds__(128) k_trace_occlusion(Params p, DScene s, Buf
   const uint64_t tid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t R = uint64_t(p.raysPerHit);
   uint32_t traced = 0, ovf = 0;
-  if (tid < uint64_t(n) * R) {
-    const uint32_t slot = uint32_t(tid / R);
+  const uint32_t nq = *(volatile const uint32_t*)(b.counter + 1);
+  if (tid < uint64_t(nq) * R) {
+    const uint32_t slot = b.occQueue[uint32_t(tid / R)];
     const int j = int(tid % R);
     const uint2 sc = b.surfC[slot];
     const uint32_t flags = sc.y;
@@ -490,7 +500,7 @@ __global__ void __launch_bounds__(128) k_trace_occlusion(Params p, DScene s, Buf
         traced = 1;
       }
     }
-    b.occ[tid] = res;
+    b.occ[uint64_t(slot) * R + j] = res;
   }
   warpCount(&b.stats[1], traced);
   warpCount(&b.stats[3], ovf);
@@ -1017,6 +1027,7 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
     b.surfA = scratchT<float4>(c, 27, npix, st);
     b.surfB = scratchT<float4>(c, 28, npix, st);
     b.surfC = scratchT<uint2>(c, 29, npix, st);
+    b.occQueue = scratchT<uint32_t>(c, 36, npix, st);
     b.occ = scratchT<uint8_t>(c, 30, size_t(npix) * p.raysPerHit, st);
     if (p.aoEnhanced && p.aoSamples > 0) b.aoT = scratchT<float>(c, 31, size_t(npix) * p.aoSamples, st);
   }
@@ -1065,7 +1076,7 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
   bool cancelled = false;
   for (; layer < p.maxIters && n > 0; ++layer) {
     uint32_t* outQ = qs[layer & 1];
-    UBR_CUDA(c, cudaMemsetAsync(b.counter, 0, sizeof(uint32_t), s));
+    UBR_CUDA(c, cudaMemsetAsync(b.counter, 0, 2 * sizeof(uint32_t), s));
     const uint32_t grid = (n + TB - 1) / TB;
     mark(0, true);
     launchClosest(km, count, grid, TB, s, p, sc->view, b, layer, n, queue);
