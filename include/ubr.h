@@ -245,6 +245,10 @@ typedef struct ubr_context_desc {
   int32_t device;              /* CUDA ordinal */
   uint64_t arena_bytes;        /* 0 = grow on demand; >0 = hard cap */
   void* stream;                /* cudaStream_t to run on, NULL = own stream */
+  /* BVH tuning (0 = library default): the most primitives a wide-BVH leaf
+   * holds (1..3); smaller leaves mean more nodes and fewer primitive tests */
+  uint32_t bvh_leaf_max;
+  uint32_t reserved[7];
 } ubr_context_desc;
 
 const char* ubr_status_string(ubr_status s);

@@ -124,7 +124,7 @@ FRAME_COUNT = 2
 
 class ContextDesc(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("device", C.c_int32), ("arena_bytes", C.c_uint64),
-                ("stream", C.c_void_p)]
+                ("stream", C.c_void_p), ("bvh_leaf_max", C.c_uint32), ("reserved", C.c_uint32 * 7)]
 
 
 class SceneInfo(C.Structure):

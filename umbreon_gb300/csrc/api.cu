@@ -110,6 +110,13 @@ ubr_status ubr_context_create(ubr_context** out, const ubr_context_desc* desc) {
   Context& x = c->impl;
   x.device = dev;
   x.arenaCap = desc ? desc->arena_bytes : 0;
+  if (desc && desc->bvh_leaf_max) {
+    if (desc->bvh_leaf_max > uint32_t(kWideLeafMax)) {
+      delete c;
+      return UBR_INVALID_ARGUMENT;
+    }
+    x.leafMax = int(desc->bvh_leaf_max);
+  }
   if (cudaSetDevice(dev) != cudaSuccess) {
     delete c;
     return UBR_CUDA_ERROR;

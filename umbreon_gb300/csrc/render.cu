@@ -31,7 +31,7 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out);
 
 namespace {
 
-constexpr int kStackDepth = 64;
+constexpr int kStackDepth = 32;  // group entries: one per tree level
 constexpr float kInfF = __builtin_huge_valf();
 
 struct Bufs {
@@ -144,70 +144,135 @@ struct Count {
   uint32_t nodes = 0, primBytes = 0;
 };
 
-template <bool ANY, bool COUNT = false, int KM = kMaskAll>
-__device__ bool traverse(const DScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt = nullptr) {
+// Stack traversal of the 8-wide BVH (node/primitive groups after Ylitie,
+// Karras and Laine, HPG 2017).  Visiting a node is branch-free: each child's
+// slab planes are one fmaf each from the 8-bit bounds, giving a hit mask;
+// the nearest hit internal child is visited next and the other hit internal
+// children are pushed as ONE group entry (childBase << 8 | slot mask), so the
+// stack depth is the tree depth; hit leaves expand into a mask over the
+// node's contiguous primitive block, tested in one loop.  The slab interval
+// is widened by a relative 2^-19 so quantised boxes stay conservative under
+// float rounding at any camera distance.  any: return at the first hit in
+// [tnear, tfar]; otherwise the closest hit, ties to the lowest
+// (geomID, primID).
+constexpr float kSlabGrow = 1.0f + 0x1.0p-19f;
+
+// Byte b of word q as a float, without an integer->float conversion: place
+// the byte in the mantissa of 2^23 (byte permute) and subtract 2^23 (exact).
+UBR_D float byteToFloat(uint32_t q, int b) {
+  return __uint_as_float(__byte_perm(q, 0x4B000000u, 0x7540u + uint32_t(b))) - 8388608.0f;
+}
+
+template <bool COUNT = false, int KM = kMaskAll>
+__device__ bool traverse(const DScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt, const bool any) {
   best.ref = kInvalid;
   if (s.primCount == 0) return false;
   const f3 inv = safeInv(r.dir);
   TriPre pre;
   if (KM & kMaskMesh) pre = triPre(r.dir);
   float tmax = r.tfar;
-  int stack[kStackDepth];
+  uint32_t stack[kStackDepth];
   int sp = 0;
-  int code = s.root;
+  int node = 0;
   uint32_t bestGeom = kInvalid, bestPrim = kInvalid;
-  // A valid tree visits each of its 2n-1 nodes at most once per ray; the
-  // bound turns a malformed tree into a reported overflow instead of a hang.
   uint32_t steps = 0;
-  const uint32_t maxSteps = 2u * s.primCount + 16u;
+  const uint32_t maxSteps = s.primCount + 16u;  // each node at most once per ray
   for (;;) {
     if (++steps > maxSteps) {
       ++overflow;
       break;
     }
-    if (code >= 0) {
-      const float4* nd = s.nodes + kNodeF4 * code;
-      if (COUNT) ++cnt->nodes;
-      const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
-      float tl, tr;
-      const bool hl = slabHit(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, r.org, inv, r.tnear, tmax, tl);
-      const bool hr = slabHit(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, r.org, inv, r.tnear, tmax, tr);
-      const int cl = __float_as_int(n3.x), cr = __float_as_int(n3.y);
-      if (hl && hr) {
-        const bool leftFirst = tl <= tr;
-        if (sp < kStackDepth) stack[sp++] = leftFirst ? cr : cl;
-        else ++overflow;
-        code = leftFirst ? cl : cr;
-        continue;
-      }
-      if (hl) { code = cl; continue; }
-      if (hr) { code = cr; continue; }
-    } else {
-      Hit h;
-      uint32_t ref;
-      const bool hitLeaf = testLeaf<KM>(s, ~code, r, pre, r.tnear, tmax, h, ref);
-      if (COUNT) cnt->primBytes += leafBytes(refKind(ref));
-      if (hitLeaf) {
-        if (ANY) {
-          best = h;
-          best.ref = ref;
-          return true;
-        }
-        const int kind = refKind(ref);
-        const uint32_t gid = s.geomID[kind], prim = refPrim(ref);
-        const bool better = best.ref == kInvalid || h.t < best.t ||
-                            (h.t == best.t && (gid < bestGeom || (gid == bestGeom && prim < bestPrim)));
-        if (better) {
-          best = h;
-          best.ref = ref;
-          bestGeom = gid;
-          bestPrim = prim;
-          tmax = h.t;
-        }
+    if (COUNT) ++cnt->nodes;
+    const float4* nd = s.wnodes + kWideF4 * node;
+    const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3), n4 = __ldg(nd + 4);
+    const uint32_t hdr = __float_as_uint(n0.w);
+    const float sx = __uint_as_float((hdr & 0xFFu) << 23) * inv.x;
+    const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * inv.y;
+    const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23) * inv.z;
+    const int nInt = int((hdr >> 24) & 0xFu), nCh = int(hdr >> 28);
+    const float ox = (n0.x - r.org.x) * inv.x, oy = (n0.y - r.org.y) * inv.y, oz = (n0.z - r.org.z) * inv.z;
+    const uint32_t childBase = __float_as_uint(n1.x);
+    const int primBase = __float_as_int(n1.y);
+    const uint32_t meta0 = __float_as_uint(n1.z), meta1 = __float_as_uint(n1.w);
+    // near/far planes per axis by the sign of the direction (swap lo/hi words)
+    const bool nx = inv.x < 0.0f, ny = inv.y < 0.0f, nz = inv.z < 0.0f;
+    const uint32_t qnx[2] = {nx ? __float_as_uint(n3.z) : __float_as_uint(n2.x),
+                             nx ? __float_as_uint(n3.w) : __float_as_uint(n2.y)};
+    const uint32_t qfx[2] = {nx ? __float_as_uint(n2.x) : __float_as_uint(n3.z),
+                             nx ? __float_as_uint(n2.y) : __float_as_uint(n3.w)};
+    const uint32_t qny[2] = {ny ? __float_as_uint(n4.x) : __float_as_uint(n2.z),
+                             ny ? __float_as_uint(n4.y) : __float_as_uint(n2.w)};
+    const uint32_t qfy[2] = {ny ? __float_as_uint(n2.z) : __float_as_uint(n4.x),
+                             ny ? __float_as_uint(n2.w) : __float_as_uint(n4.y)};
+    const uint32_t qnz[2] = {nz ? __float_as_uint(n4.z) : __float_as_uint(n3.x),
+                             nz ? __float_as_uint(n4.w) : __float_as_uint(n3.y)};
+    const uint32_t qfz[2] = {nz ? __float_as_uint(n3.x) : __float_as_uint(n4.z),
+                             nz ? __float_as_uint(n3.y) : __float_as_uint(n4.w)};
+    uint32_t hitInt = 0, primMask = 0;
+    float nearT = kInfF;
+    int nearK = -1;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int w = k >> 2;
+      const float tnx = fmaf(byteToFloat(qnx[w], k & 3), sx, ox), tfx = fmaf(byteToFloat(qfx[w], k & 3), sx, ox);
+      const float tny = fmaf(byteToFloat(qny[w], k & 3), sy, oy), tfy = fmaf(byteToFloat(qfy[w], k & 3), sy, oy);
+      const float tnz = fmaf(byteToFloat(qnz[w], k & 3), sz, oz), tfz = fmaf(byteToFloat(qfz[w], k & 3), sz, oz);
+      const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tnear));
+      const float tmx = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+      const bool hit = k < nCh && tmin <= tmx * kSlabGrow;
+      if (k < nInt) {
+        hitInt |= hit ? (1u << k) : 0u;
+        const bool nearer = hit && tmin < nearT;
+        nearT = nearer ? tmin : nearT;
+        nearK = nearer ? k : nearK;
+      } else {
+        const uint32_t m = ((w == 0 ? meta0 : meta1) >> ((k & 3) * 8)) & 0xFFu;
+        primMask |= hit ? (((1u << (m >> 5)) - 1u) << (m & 31u)) : 0u;
       }
     }
+    // primitives of the hit leaves
+    while (primMask) {
+      const int q = __ffs(primMask) - 1;
+      primMask &= primMask - 1u;
+      Hit h;
+      uint32_t ref;
+      const bool hitLeaf = testLeaf<KM>(s, primBase + q, r, pre, r.tnear, tmax, h, ref);
+      if (COUNT) cnt->primBytes += leafBytes(refKind(ref));
+      if (!hitLeaf) continue;
+      if (any) {
+        best = h;
+        best.ref = ref;
+        return true;
+      }
+      const int kind = refKind(ref);
+      const uint32_t gid = s.geomID[kind], prim = refPrim(ref);
+      const bool better = best.ref == kInvalid || h.t < best.t ||
+                          (h.t == best.t && (gid < bestGeom || (gid == bestGeom && prim < bestPrim)));
+      if (better) {
+        best = h;
+        best.ref = ref;
+        bestGeom = gid;
+        bestPrim = prim;
+        tmax = h.t;
+      }
+    }
+    if (nearK >= 0) {
+      const uint32_t rest = hitInt & ~(1u << nearK);
+      if (rest) {
+        if (sp < kStackDepth) stack[sp++] = (childBase << 8) | rest;
+        else ++overflow;
+      }
+      node = int(childBase) + nearK;
+      continue;
+    }
     if (sp == 0) break;
-    code = stack[--sp];
+    const uint32_t g = stack[sp - 1];
+    const uint32_t mask = g & 0xFFu;
+    const int k = __ffs(mask) - 1;
+    const uint32_t left = mask & (mask - 1u);
+    if (left) stack[sp - 1] = (g & ~0xFFu) | left;
+    else --sp;
+    node = int(g >> 8) + k;
   }
   return best.ref != kInvalid;
 }
@@ -374,7 +439,7 @@ UBR_D void warpCount(unsigned long long* ctr, uint32_t v) {
 // kernels
 
 template <bool COUNT, int KM>
-__global__ void __launch_bounds__(128) k_trace_closest(Params p, DScene s, Bufs b, int layer, uint32_t n,
+__global__ void __launch_bounds__(128, 8) k_trace_closest(Params p, DScene s, Bufs b, int layer, uint32_t n,
                                                        const uint32_t* queue) {
   Count cnt;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -388,7 +453,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(Params p, DScene s, Bufs 
     clipRange(p, rd, ctn, ctf);
     Ray r{org, rd, layer == 0 ? ctn : b.tnear[pix], ctf};
     Hit h;
-    traverse<false, COUNT, KM>(s, r, h, ovf, &cnt);
+    traverse<COUNT, KM>(s, r, h, ovf, &cnt, false);
     traced = 1;
     b.hitA[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.ref));
     b.hitB[i] = make_float4(h.Ng.x, h.Ng.y, h.Ng.z, 0.0f);
@@ -435,7 +500,7 @@ __global__ void __launch_bounds__(128) k_surface(Params p, DScene s, Bufs b, int
 }
 
 template <bool COUNT, int KM>
-__global__ void __launch_bounds__(128) k_trace_occlusion(Params p, DScene s, Bufs b, uint32_t n) {
+__global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p, DScene s, Bufs b, uint32_t n) {
   Count cnt;
   const uint64_t tid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t R = uint64_t(p.raysPerHit);
@@ -446,41 +511,29 @@ __global__ void __launch_bounds__(128) k_trace_occlusion(Params p, DScene s, Buf
     const int j = int(tid % R);
     const uint2 sc = b.surfC[slot];
     const uint32_t flags = sc.y;
-    uint8_t res = 0;
     const int px = int(sc.x % uint32_t(p.W)), py = int(sc.x / uint32_t(p.W));
+    // the ray of this thread: AO sample j, or a shadow ray of light l
+    bool trace = false, anyHit = true, grazing = false;
+    f3 dir{0.0f, 0.0f, 0.0f};
+    float tfar = kInfF;
+    const float4 sa = b.surfA[slot], sb = b.surfB[slot];
+    const f3 N = ld3(sb);
     if (j < p.aoSamples) {
-      if ((flags & 2u)) {
-        const float4 sa = b.surfA[slot], sb = b.surfB[slot];
-        const f3 N = ld3(sb);
+      if (flags & 2u) {
         const Frame3 f = frameFromNormal(N);
-        const f3 dir = aoDir(p, f, px, py, j);
-        float tnear = sa.w;
-        if (dot(dir, N) < 0.01f) {
-          res = 1;
-          if (p.aoEnhanced) b.aoT[uint64_t(slot) * p.aoSamples + j] = -1.0f;
-        } else {
-          Ray r{ld3(sa), dir, tnear, p.aoDistance};
-          Hit h;
-          if (p.aoEnhanced) {
-            const bool hit = traverse<false, COUNT, KM>(s, r, h, ovf, &cnt);
-            b.aoT[uint64_t(slot) * p.aoSamples + j] = hit ? h.t : kInfF;
-            res = hit ? 1 : 0;
-          } else {
-            res = traverse<true, COUNT, KM>(s, r, h, ovf, &cnt) ? 1 : 0;
-          }
-          traced = 1;
-        }
+        dir = aoDir(p, f, px, py, j);
+        grazing = dot(dir, N) < 0.01f;
+        trace = !grazing;
+        anyHit = !p.aoEnhanced;
+        tfar = p.aoDistance;
       }
     } else if (flags & 4u) {
       const int k = j - p.aoSamples;
       int l = 0;
       while (l + 1 < p.nLights && b.lights[l + 1].rayOffset <= k) ++l;
       const LightD L = b.lights[l];
-      const float4 sa = b.surfA[slot], sb = b.surfB[slot];
-      const f3 N = ld3(sb);
-      const float ndl = dot(N, L.L);
-      if (ndl > 0.0f) {
-        f3 dir = L.L;
+      if (dot(N, L.L) > 0.0f) {
+        dir = L.L;
         if (L.soft) {
           // the (px, py) stream is advanced by every earlier lit soft light
           // (shading.hpp:100, secondary_rays.hpp:128-131)
@@ -490,16 +543,24 @@ __global__ void __launch_bounds__(128) k_trace_occlusion(Params p, DScene s, Buf
             if (Q.soft && dot(N, Q.L) > 0.0f) consumed += Q.samples;
           }
           uint32_t s0 = uint32_t(px), s1 = uint32_t(py);
-          const int steps = consumed + (k - L.rayOffset) + 1;
-          for (int q = 0; q < steps; ++q) tea2(s0, s1);
+          const int stepsRng = consumed + (k - L.rayOffset) + 1;
+          for (int q = 0; q < stepsRng; ++q) tea2(s0, s1);
           dir = sampleLightDir(L, u32ToUnorm(s0), u32ToUnorm(s1));
         }
-        Ray r{ld3(sa), dir, sa.w, kInfF};
-        Hit h;
-        res = traverse<true, COUNT, KM>(s, r, h, ovf, &cnt) ? 1 : 0;
-        traced = 1;
+        trace = true;
       }
     }
+    uint8_t res = grazing ? 1 : 0;
+    float th = grazing ? -1.0f : kInfF;
+    if (trace) {
+      Ray r{ld3(sa), dir, sa.w, tfar};
+      Hit h;
+      const bool hit = traverse<COUNT, KM>(s, r, h, ovf, &cnt, anyHit);
+      res = hit ? 1 : 0;
+      if (hit) th = h.t;
+      traced = 1;
+    }
+    if (j < p.aoSamples && p.aoEnhanced && (flags & 2u)) b.aoT[uint64_t(slot) * p.aoSamples + j] = th;
     b.occ[uint64_t(slot) * R + j] = res;
   }
   warpCount(&b.stats[1], traced);
@@ -933,7 +994,7 @@ __global__ void k_occluded_segments(DScene s, const float* segs, uint64_t n, flo
       if (tnear < tfar) {
         Ray r{a, dir, tnear, tfar};
         Hit h;
-        res = traverse<true>(s, r, h, ovf) ? 1 : 0;
+        res = traverse<false, kMaskAll>(s, r, h, ovf, nullptr, true) ? 1 : 0;
       }
     }
     out[i] = res;
@@ -1146,8 +1207,8 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
   }
   fr.nodes_visited[0] = hs[4];
   fr.nodes_visited[1] = hs[6];
-  fr.node_bytes[0] = hs[4] * uint64_t(kNodeF4 * 16);
-  fr.node_bytes[1] = hs[6] * uint64_t(kNodeF4 * 16);
+  fr.node_bytes[0] = hs[4] * uint64_t(kWideF4 * 16);
+  fr.node_bytes[1] = hs[6] * uint64_t(kWideF4 * 16);
   fr.prim_bytes[0] = hs[5];
   fr.prim_bytes[1] = hs[7];
   if (cancelled) return setError(c, UBR_CANCELLED, "render cancelled");

@@ -413,7 +413,7 @@ __device__ __forceinline__ int deltaKey(const unsigned long long* keys, int n, i
 
 // Karras 2012, Fig. 4: internal node i covers [min(i,j), max(i,j)], split at gamma.
 __global__ void k_hierarchy(int n, const unsigned long long* keys, float4* nodes, int* leafParent,
-                            int* nodeParent) {
+                            int* nodeParent, int2* ranges) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
   const int d = (deltaKey(keys, n, i, i + 1) - deltaKey(keys, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -432,6 +432,7 @@ __global__ void k_hierarchy(int n, const unsigned long long* keys, float4* nodes
   } while (t > 1);
   const int gamma = i + s * d + min(d, 0);
   const int lo = min(i, j), hi = max(i, j);
+  ranges[i] = make_int2(lo, hi);
   int left, right;
   if (lo == gamma) {
     left = ~gamma;
@@ -510,6 +511,166 @@ __global__ void k_refit(BuildIn in, int n, int idxBits, const unsigned long long
     hi = make_float3(fmaxf(a.y, b.y), fmaxf(a.w, b.w), fmaxf(z.y, z.w));
     pinfo = nodeParent[p];
   }
+}
+
+__device__ __forceinline__ void binChild(const float4* nodes, int node, int side, int& code, float3& lo, float3& hi) {
+  const float4* nd = nodes + kNodeF4 * node;
+  const float4 a = nd[side], z = nd[2], c = nd[3];
+  lo = make_float3(a.x, a.z, side == 0 ? z.x : z.z);
+  hi = make_float3(a.y, a.w, side == 0 ? z.y : z.w);
+  code = __float_as_int(side == 0 ? c.x : c.y);
+}
+
+__device__ __forceinline__ float halfArea(float3 lo, float3 hi) {
+  const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = hi.z - lo.z;
+  return ex * ey + ey * ez + ez * ex;
+}
+
+// Power-of-two scale s >= ext/255 (with slack) as its biased exponent.
+__device__ __forceinline__ uint32_t scaleExp(float ext) {
+  float x = ext * (1.0f / 255.0f) * (1.0f + 0x1.0p-20f);
+  if (!(x > 0x1.0p-126f)) x = 0x1.0p-126f;
+  const uint32_t bits = __float_as_uint(x);
+  uint32_t ex = bits >> 23;
+  if (bits & 0x7FFFFFu) ++ex;
+  return ex;
+}
+
+__device__ __forceinline__ void quantize(float lo, float hi, float p, float sc, uint32_t& qlo, uint32_t& qhi) {
+  int a = int(floorf((lo - p) / sc)), b = int(ceilf((hi - p) / sc));
+  a = max(0, min(255, a));
+  b = max(0, min(255, b));
+  while (a > 0 && fmaf(float(a), sc, p) > lo) --a;
+  while (b < 255 && fmaf(float(b), sc, p) < hi) ++b;
+  qlo = uint32_t(a);
+  qhi = uint32_t(b);
+}
+
+// Top-down collapse of the binary LBVH into 8-wide nodes, one level of wide
+// nodes per launch.  A wide node starts from its binary node's two children
+// and repeatedly opens the child with the largest surface area until it has
+// 8 children or none is worth opening (subtrees of <= 3 primitives become
+// leaves: their primitives are a contiguous run of Morton-sorted slots).
+// Leaf primitives of a node are copied into one contiguous block so a wide
+// node addresses them with an 8-bit offset.
+__global__ void k_collapse(const float4* bnodes, const int2* brange, const float4* rootLo, const float4* rootHi,
+                           const int* workCode, const int* workWide, int workCount, int leafMax, int* nextCode,
+                           int* nextWide,
+                           int* cursors, float4* wnodes, const uint32_t* srcRef, const float4* srcGeo,
+                           uint32_t* dstRef, float4* dstGeo) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= workCount) return;
+  const int code = workCode[i];
+  const int w = workWide[i];
+  int ec[8];
+  float3 elo[8], ehi[8];
+  int en;
+  if (code < 0) {  // single-primitive scene
+    ec[0] = code;
+    elo[0] = make_float3(rootLo->x, rootLo->y, rootLo->z);
+    ehi[0] = make_float3(rootHi->x, rootHi->y, rootHi->z);
+    en = 1;
+  } else {
+    binChild(bnodes, code, 0, ec[0], elo[0], ehi[0]);
+    binChild(bnodes, code, 1, ec[1], elo[1], ehi[1]);
+    en = 2;
+  }
+  auto countOf = [&](int c) { return c < 0 ? 1 : brange[c].y - brange[c].x + 1; };
+  while (en < 8) {
+    int best = -1;
+    float bestA = -1.0f;
+    for (int k = 0; k < en; ++k) {
+      if (ec[k] >= 0 && countOf(ec[k]) > leafMax) {
+        const float a = halfArea(elo[k], ehi[k]);
+        if (a > bestA) {
+          bestA = a;
+          best = k;
+        }
+      }
+    }
+    if (best < 0) break;
+    const int c = ec[best];
+    binChild(bnodes, c, 0, ec[best], elo[best], ehi[best]);
+    binChild(bnodes, c, 1, ec[en], elo[en], ehi[en]);
+    ++en;
+  }
+  int nInt = 0, nLeaf = 0;
+  for (int k = 0; k < en; ++k) {
+    if (ec[k] >= 0 && countOf(ec[k]) > leafMax) ++nInt;
+    else nLeaf += countOf(ec[k]);
+  }
+  const int childBase = nInt ? atomicAdd(&cursors[0], nInt) : 0;
+  const int primBase = nLeaf ? atomicAdd(&cursors[1], nLeaf) : 0;
+  const int pushBase = nInt ? atomicAdd(&cursors[2], nInt) : 0;
+  float3 p = elo[0], hmax = ehi[0];
+  for (int k = 1; k < en; ++k) {
+    p = make_float3(fminf(p.x, elo[k].x), fminf(p.y, elo[k].y), fminf(p.z, elo[k].z));
+    hmax = make_float3(fmaxf(hmax.x, ehi[k].x), fmaxf(hmax.y, ehi[k].y), fmaxf(hmax.z, ehi[k].z));
+  }
+  const uint32_t exX = scaleExp(hmax.x - p.x), exY = scaleExp(hmax.y - p.y), exZ = scaleExp(hmax.z - p.z);
+  const float scX = __uint_as_float(exX << 23), scY = __uint_as_float(exY << 23), scZ = __uint_as_float(exZ << 23);
+  uint32_t meta[2] = {0u, 0u}, qlx[2] = {0u, 0u}, qly[2] = {0u, 0u}, qlz[2] = {0u, 0u};
+  uint32_t qhx[2] = {0u, 0u}, qhy[2] = {0u, 0u}, qhz[2] = {0u, 0u};
+  // slot order: internal children first (slot k -> node childBase + k), then leaves
+  int order[8];
+  {
+    int o = 0;
+    for (int k = 0; k < en; ++k)
+      if (ec[k] >= 0 && countOf(ec[k]) > leafMax) order[o++] = k;
+    for (int k = 0; k < en; ++k)
+      if (!(ec[k] >= 0 && countOf(ec[k]) > leafMax)) order[o++] = k;
+  }
+  int kInt = 0, off = 0;
+  for (int slot = 0; slot < en; ++slot) {
+    const int k = order[slot];
+    uint32_t a, b;
+    const int wd = slot >> 2, sh = (slot & 3) * 8;
+    quantize(elo[k].x, ehi[k].x, p.x, scX, a, b);
+    qlx[wd] |= a << sh;
+    qhx[wd] |= b << sh;
+    quantize(elo[k].y, ehi[k].y, p.y, scY, a, b);
+    qly[wd] |= a << sh;
+    qhy[wd] |= b << sh;
+    quantize(elo[k].z, ehi[k].z, p.z, scZ, a, b);
+    qlz[wd] |= a << sh;
+    qhz[wd] |= b << sh;
+    uint32_t m;
+    if (ec[k] >= 0 && countOf(ec[k]) > leafMax) {
+      m = 0x80u | uint32_t(kInt);
+      nextCode[pushBase + kInt] = ec[k];
+      nextWide[pushBase + kInt] = childBase + kInt;
+      ++kInt;
+    } else {
+      const int cnt = countOf(ec[k]);
+      const int first = ec[k] < 0 ? ~ec[k] : brange[ec[k]].x;
+      m = (uint32_t(cnt) << 5) | uint32_t(off);
+      for (int q = 0; q < cnt; ++q) {
+        const int d = primBase + off + q, sidx = first + q;
+        dstRef[d] = srcRef[sidx];
+        for (int f = 0; f < kLeafF4; ++f) dstGeo[kLeafF4 * d + f] = srcGeo[kLeafF4 * sidx + f];
+      }
+      off += cnt;
+    }
+    meta[wd] |= m << sh;
+  }
+  // empty slots: qlo = 255 > qhi = 0 and meta 0 (never tested)
+  for (int k = en; k < 8; ++k) {
+    const int wd = k >> 2, sh = (k & 3) * 8;
+    qlx[wd] |= 255u << sh;
+    qly[wd] |= 255u << sh;
+    qlz[wd] |= 255u << sh;
+  }
+  float4* o = wnodes + kWideF4 * w;
+  o[0] = make_float4(p.x, p.y, p.z,
+                     __uint_as_float(exX | (exY << 8) | (exZ << 16) | (uint32_t(nInt) << 24) | (uint32_t(en) << 28)));
+  o[1] = make_float4(__int_as_float(childBase), __int_as_float(primBase), __uint_as_float(meta[0]),
+                     __uint_as_float(meta[1]));
+  o[2] = make_float4(__uint_as_float(qlx[0]), __uint_as_float(qlx[1]), __uint_as_float(qly[0]),
+                     __uint_as_float(qly[1]));
+  o[3] = make_float4(__uint_as_float(qlz[0]), __uint_as_float(qlz[1]), __uint_as_float(qhx[0]),
+                     __uint_as_float(qhx[1]));
+  o[4] = make_float4(__uint_as_float(qhy[0]), __uint_as_float(qhy[1]), __uint_as_float(qhz[0]),
+                     __uint_as_float(qhz[1]));
 }
 
 template <class T>
@@ -600,10 +761,22 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   if (n > 0) {
     BuildIn in{dpos, v.meshIdx, dsph, drcV, drcIdx, drcFl, dccV, dccIdx, nTri, nSph, nRc, nCc};
     void *pLo, *pHi, *pKeys, *pKeys2, *pCb, *pLeafP, *pNodeP, *pCnt, *pNodes, *pRef, *pGeo;
+    void *pWide, *pRef2, *pGeo2, *pRange, *pWc[2], *pWw[2], *pCur;
     const size_t nn = n > 1 ? n - 1 : 1;
-    if ((st = allocOwned(c, sc, sizeof(float4) * kNodeF4 * nn, &pNodes)) != UBR_OK) return fail(st);
-    if ((st = allocOwned(c, sc, sizeof(uint32_t) * n, &pRef)) != UBR_OK) return fail(st);
-    if ((st = allocOwned(c, sc, sizeof(float4) * kLeafF4 * n, &pGeo)) != UBR_OK) return fail(st);
+    // the scene keeps the 8-wide nodes and the leaf records in wide order;
+    // the binary tree and the Morton-ordered leaves are build temporaries
+    if ((st = allocOwned(c, sc, sizeof(float4) * kWideF4 * nn, &pWide)) != UBR_OK) return fail(st);
+    if ((st = allocOwned(c, sc, sizeof(uint32_t) * n, &pRef2)) != UBR_OK) return fail(st);
+    if ((st = allocOwned(c, sc, sizeof(float4) * kLeafF4 * n, &pGeo2)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 50, sizeof(float4) * kNodeF4 * nn, &pNodes)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 51, sizeof(uint32_t) * n, &pRef)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 52, sizeof(float4) * kLeafF4 * n, &pGeo)) != UBR_OK) return fail(st);
+    if ((st = scratchGet(c, 53, sizeof(int2) * nn, &pRange)) != UBR_OK) return fail(st);
+    for (int k = 0; k < 2; ++k) {
+      if ((st = scratchGet(c, 54 + 2 * k, sizeof(int) * nn, &pWc[k])) != UBR_OK) return fail(st);
+      if ((st = scratchGet(c, 55 + 2 * k, sizeof(int) * nn, &pWw[k])) != UBR_OK) return fail(st);
+    }
+    if ((st = scratchGet(c, 58, 64, &pCur)) != UBR_OK) return fail(st);
     // build temporaries live in context scratch slots 0..7
     if ((st = scratchGet(c, 0, sizeof(float4) * n, &pLo)) != UBR_OK) return fail(st);
     if ((st = scratchGet(c, 1, sizeof(float4) * n, &pHi)) != UBR_OK) return fail(st);
@@ -635,17 +808,47 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
                                                (unsigned long long*)pKeys2, int(n), 0, 30 + idxBits, c->stream));
     if (n > 1)
       k_hierarchy<<<int((n - 1 + TB - 1) / TB), TB, 0, c->stream>>>(int(n), (const unsigned long long*)pKeys2,
-                                                                   (float4*)pNodes, (int*)pLeafP, (int*)pNodeP);
+                                                                   (float4*)pNodes, (int*)pLeafP, (int*)pNodeP,
+                                                                   (int2*)pRange);
     k_refit<<<grid, TB, 0, c->stream>>>(in, int(n), idxBits, (const unsigned long long*)pKeys2,
                                         (const float4*)pLo, (const float4*)pHi, v.rcClip, (float4*)pNodes,
                                         (const int*)pLeafP, (const int*)pNodeP, (int*)pCnt, (uint32_t*)pRef,
                                         (float4*)pGeo);
     UBR_CUDA(c, cudaGetLastError());
-    v.nodes = (const float4*)pNodes;
-    v.leafRef = (const uint32_t*)pRef;
-    v.leafGeo = (const float4*)pGeo;
-    v.root = n > 1 ? 0 : ~0;
-    sc->nodes = n > 1 ? n - 1 : 0;
+    // collapse to 8-wide, level by level: cursors = {wide nodes, leaf prims, next work}
+    {
+      const int rootCode = n > 1 ? 0 : ~0;
+      const int zero = 0;
+      const int cur0[3] = {1, 0, 0};
+      UBR_CUDA(c, cudaMemcpyAsync(pCur, cur0, sizeof(cur0), cudaMemcpyHostToDevice, c->stream));
+      UBR_CUDA(c, cudaMemcpyAsync(pWc[0], &rootCode, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+      UBR_CUDA(c, cudaMemcpyAsync(pWw[0], &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+      int count = 1, cur = 0, levels = 0;
+      int* hostCur = static_cast<int*>(c->pinned);
+      while (count > 0) {
+        UBR_CUDA(c, cudaMemsetAsync(static_cast<int*>(pCur) + 2, 0, sizeof(int), c->stream));
+        k_collapse<<<(count + 127) / 128, 128, 0, c->stream>>>(
+            (const float4*)pNodes, (const int2*)pRange, (const float4*)pLo, (const float4*)pHi,
+            (const int*)pWc[cur], (const int*)pWw[cur], count, c->leafMax, (int*)pWc[cur ^ 1], (int*)pWw[cur ^ 1],
+            (int*)pCur,
+            (float4*)pWide, (const uint32_t*)pRef, (const float4*)pGeo, (uint32_t*)pRef2, (float4*)pGeo2);
+        UBR_CUDA(c, cudaGetLastError());
+        UBR_CUDA(c, cudaMemcpyAsync(hostCur, pCur, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        UBR_CUDA(c, cudaStreamSynchronize(c->stream));
+        count = hostCur[2];
+        cur ^= 1;
+        if (++levels > 64) return fail(setError(c, UBR_INTERNAL, "wide BVH collapse did not converge"));
+      }
+      sc->nodes = uint64_t(hostCur[0]);
+      // traversal stack entries pack a node index into 24 bits
+      if (sc->nodes >= (1ull << 24))
+        return fail(setError(c, UBR_INVALID_ARGUMENT, "scene too large: more than 2^24 wide BVH nodes"));
+    }
+    v.wnodes = (const float4*)pWide;
+    v.nodes = nullptr;
+    v.leafRef = (const uint32_t*)pRef2;
+    v.leafGeo = (const float4*)pGeo2;
+    v.root = 0;
     int cb[6];
     UBR_CUDA(c, cudaMemcpyAsync(cb, pCb, sizeof(cb), cudaMemcpyDeviceToHost, c->stream));
     cudaEventRecord(c->ev[1], c->stream);

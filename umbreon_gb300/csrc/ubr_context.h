@@ -23,6 +23,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   bool ownStream = false;
   uint64_t arenaCap = 0;     // 0 = unlimited
+  int leafMax = 1;           // wide-BVH leaf size (1..kWideLeafMax); 1 measured fastest
   uint64_t arenaUsed = 0;
   std::string lastError;
   // frame scratch, reused across frames

@@ -81,7 +81,27 @@ constexpr int kNodeF4 = 4;
 //   round  : (p0, r0) | (p1, r1) | (flags bits, -, -, -)
 constexpr int kLeafF4 = 3;
 
+// 8-wide BVH node, 80 B = 5 float4 (compressed child bounds after Ylitie,
+// Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs Through
+// Compressed Wide BVHs", HPG 2017):
+//   [0] origin p.xyz, (ex | ey<<8 | ez<<16 | nInternal<<24 | nChildren<<28):
+//       biased exponents of the per-axis power-of-two scale, then the number
+//       of internal children (slots 0..nInternal-1, node = childBase + slot)
+//       and of all children (leaf slots follow the internal ones)
+//   [1] childBase, primBase, meta[0..3], meta[4..7]
+//   [2] qlo.x[0..7], qlo.y[0..7]      (8-bit quantised child bounds)
+//   [3] qlo.z[0..7], qhi.x[0..7]
+//   [4] qhi.y[0..7], qhi.z[0..7]
+// meta byte: 0 empty; 0x80|k internal child = node childBase+k;
+//            (count<<5)|offset leaf = count (1..3) primitives at primBase+offset.
+// Child bound = p + q * scale, evaluated with fmaf in both build and
+// traversal so the quantised box is exactly the one the build made
+// conservative.
+constexpr int kWideF4 = 5;
+constexpr int kWideLeafMax = 3;
+
 struct DScene {
+  const float4* wnodes = nullptr;  // 8-wide nodes (root = 0)
   const float4* nodes = nullptr;
   int32_t root = 0;             // child code of the root (when prims > 0)
   uint32_t primCount = 0;       // total primitives
