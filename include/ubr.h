@@ -295,6 +295,24 @@ ubr_status ubr_occluded_batch(ubr_context* ctx, const ubr_scene* scene,
                               const float* segs, uint64_t n, float eps,
                               uint8_t* out, int32_t memory);
 
+/* Segment occlusion that allocates nothing.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory when
+ * they query -- a host with its own strict GPU memory budget, a plugin
+ * sandbox whose host owns every device allocation, or a per-frame loop that
+ * must not risk an allocation failure or the synchronisation that
+ * cudaMalloc/cudaFree can cause.  Same answer as ubr_occluded_batch on HOST
+ * buffers (segs = 6*n floats, out = n bytes), staged through one fixed device
+ * array compiled into the library (about 12.5 MiB, held by every GPU that
+ * loads the library until the process exits).
+ *   - n may be at most 524,288; larger n returns UBR_INVALID_ARGUMENT.
+ *   - The first call on a device resolves the array's device address with
+ *     that device current; make that first call before any stream capture.
+ *   - Every call on a device shares the one array: calls whose GPU work
+ *     overlaps (other threads, other contexts on the same device) race. */
+ubr_status ubr_occluded_batch_noalloc(ubr_context* ctx, const ubr_scene* scene,
+                                      const float* segs, uint64_t n, float eps,
+                                      uint8_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -147,6 +147,8 @@ SIGNATURES = {
                              C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
     "ubr_occluded_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
                                      C.c_void_p, C.c_int32]),
+    "ubr_occluded_batch_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
+                                             C.c_void_p]),
 }
 
 _LIB = None

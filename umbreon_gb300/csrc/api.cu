@@ -16,6 +16,8 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
                        const volatile int32_t* cancel, uint64_t* progress);
 ubr_status occludedBatch(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps, uint8_t* out,
                          int32_t memory);
+ubr_status occludedBatchNoAlloc(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps,
+                                uint8_t* out);
 
 ubr_status setError(Context* c, ubr_status s, const std::string& msg) {
   if (c) c->lastError = msg;
@@ -238,6 +240,16 @@ ubr_status ubr_occluded_batch(ubr_context* c, const ubr_scene* s, const float* s
   if (!s || !s->impl) return setError(&c->impl, UBR_INVALID_ARGUMENT, "occluded_batch: NULL scene");
   cudaSetDevice(c->impl.device);
   return occludedBatch(&c->impl, s->impl, segs, n, eps, out, memory);
+}
+
+ubr_status ubr_occluded_batch_noalloc(ubr_context* c, const ubr_scene* s, const float* segs, uint64_t n, float eps,
+                                      uint8_t* out) {
+  if (!c) return UBR_INVALID_ARGUMENT;
+  if (!s || !s->impl) return setError(&c->impl, UBR_INVALID_ARGUMENT, "occluded_batch_noalloc: NULL scene");
+  if (s->impl->ctx != &c->impl)
+    return setError(&c->impl, UBR_INVALID_ARGUMENT, "occluded_batch_noalloc: scene from another context");
+  cudaSetDevice(c->impl.device);
+  return occludedBatchNoAlloc(&c->impl, s->impl, segs, n, eps, out);
 }
 
 }  // extern "C"

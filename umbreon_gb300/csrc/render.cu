@@ -19,6 +19,7 @@
 // Per-pixel and per-ray results do not depend on launch order, so a frame is
 // bit-reproducible.
 #include <chrono>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -1238,6 +1239,77 @@ ubr_status occludedBatch(Context* c, const Scene* sc, const float* segs, uint64_
   UBR_CUDA(c, cudaGetLastError());
   if (memory != UBR_MEMORY_DEVICE) UBR_CUDA(c, cudaMemcpyAsync(out, dout, size_t(n), cudaMemcpyDeviceToHost, s));
   UBR_CUDA(c, cudaStreamSynchronize(s));
+  return UBR_OK;
+}
+
+}  // namespace ubr
+
+// ---------------------------------------------------------------------------
+// Segment occlusion without allocation (ubr_occluded_batch_noalloc).
+//
+// Some callers of this library cannot allocate device memory at the time they
+// need an answer: a host that runs the query from inside its own per-frame
+// loop under a strict GPU memory budget, a plugin sandbox whose host owns all
+// device allocations, or code that must not risk an allocation failure or the
+// implicit synchronisation cudaMalloc/cudaFree can cause mid-frame.  For them
+// the segments and the results are staged through one file-scope device array
+// of fixed size instead of the context's growable scratch.  Every GPU that
+// loads the library holds this array until the process exits.
+
+constexpr uint64_t kNoAllocMaxSegments = 1ull << 19;  // 524,288 segments per call
+constexpr size_t kNoAllocHeader = 256;                // counters (8 x u64), padded
+constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocMaxSegments * 6 * sizeof(float) + kNoAllocMaxSegments;
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
+
+namespace ubr {
+
+namespace {
+
+// Device address of g_noallocScratch for each device, resolved once per
+// device (with that device current) by the first call made on it.
+std::mutex g_noallocMutex;
+void* g_noallocPtr[64] = {};
+
+ubr_status noallocScratch(Context* c, unsigned char** out) {
+  if (c->device < 0 || c->device >= 64) return setError(c, UBR_INVALID_ARGUMENT, "device ordinal out of range");
+  std::lock_guard<std::mutex> lk(g_noallocMutex);
+  if (!g_noallocPtr[c->device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+    if (e != cudaSuccess) return cudaFail(c, e, "cudaGetSymbolAddress(g_noallocScratch)");
+    g_noallocPtr[c->device] = p;
+  }
+  *out = static_cast<unsigned char*>(g_noallocPtr[c->device]);
+  return UBR_OK;
+}
+
+}  // namespace
+
+ubr_status occludedBatchNoAlloc(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps,
+                                uint8_t* out) {
+  if (n == 0) return UBR_OK;
+  if (!segs || !out) return setError(c, UBR_INVALID_ARGUMENT, "occluded_batch_noalloc: NULL buffer");
+  if (n > kNoAllocMaxSegments)
+    return setError(c, UBR_INVALID_ARGUMENT,
+                    "occluded_batch_noalloc: more than 524288 segments in one call (the fixed scratch limit)");
+  unsigned char* base = nullptr;
+  ubr_status st = noallocScratch(c, &base);
+  if (st != UBR_OK) return st;
+  unsigned long long* stats = reinterpret_cast<unsigned long long*>(base);
+  float* dsegs = reinterpret_cast<float*>(base + kNoAllocHeader);
+  uint8_t* dout = reinterpret_cast<uint8_t*>(base + kNoAllocHeader + kNoAllocMaxSegments * 6 * sizeof(float));
+  cudaStream_t s = c->stream;
+  // the array keeps the previous call's contents: the counters start at zero
+  UBR_CUDA(c, cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), s));
+  UBR_CUDA(c, cudaMemcpyAsync(dsegs, segs, size_t(n) * 6 * sizeof(float), cudaMemcpyHostToDevice, s));
+  k_occluded_segments<<<uint32_t((n + 127) / 128), 128, 0, s>>>(sc->view, dsegs, n, eps, dout, stats);
+  UBR_CUDA(c, cudaGetLastError());
+  UBR_CUDA(c, cudaMemcpyAsync(out, dout, size_t(n), cudaMemcpyDeviceToHost, s));
+  unsigned long long ovf = 0;
+  UBR_CUDA(c, cudaMemcpyAsync(&ovf, stats + 3, sizeof(ovf), cudaMemcpyDeviceToHost, s));
+  UBR_CUDA(c, cudaStreamSynchronize(s));
+  if (ovf) return setError(c, UBR_TRAVERSAL_LIMIT, "traversal stack overflow");
   return UBR_OK;
 }
 
