@@ -183,7 +183,7 @@ def run_ours(args):
         opt.width, opt.height = (int(x) for x in args.frame.lower().split("x"))
     if args.ss:
         opt.supersample = args.ss
-    ctx = Context(local, bvh_leaf_max=args.leaf_max)
+    ctx = Context(local, bvh_leaf_max=args.leaf_max, trace_mode=args.trace_mode)
     built = ctx.build(sc)
     info = built.info()
     import ctypes as C
@@ -323,6 +323,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--leaf-max", type=int, default=0, help="wide-BVH leaf size 1..3 (0 = library default)")
+    ap.add_argument("--trace-mode", type=int, default=0, help="occlusion kernel: 1 per-ray, 2 persistent (0 = default)")
     ap.add_argument("--frame", default=None, help="override the frame size WxH (profiling runs)")
     ap.add_argument("--ss", type=int, default=0, help="override the supersample factor (profiling runs)")
     args = ap.parse_args()

@@ -248,7 +248,10 @@ typedef struct ubr_context_desc {
   /* BVH tuning (0 = library default): the most primitives a wide-BVH leaf
    * holds (1..3); smaller leaves mean more nodes and fewer primitive tests */
   uint32_t bvh_leaf_max;
-  uint32_t reserved[7];
+  /* occlusion-ray kernel (0 = library default): 1 = one thread per ray,
+   * 2 = persistent warps that refill idle lanes with new rays */
+  uint32_t trace_mode;
+  uint32_t reserved[6];
 } ubr_context_desc;
 
 const char* ubr_status_string(ubr_status s);

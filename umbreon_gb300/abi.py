@@ -124,7 +124,8 @@ FRAME_COUNT = 2
 
 class ContextDesc(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("device", C.c_int32), ("arena_bytes", C.c_uint64),
-                ("stream", C.c_void_p), ("bvh_leaf_max", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+                ("stream", C.c_void_p), ("bvh_leaf_max", C.c_uint32), ("trace_mode", C.c_uint32),
+                ("reserved", C.c_uint32 * 6)]
 
 
 class SceneInfo(C.Structure):
@@ -155,7 +156,9 @@ _LIB = None
 
 
 def lib_path() -> Path:
-    return LIBDIR / "libubr.so"
+    """libubr.so of this package, or the file named by UBR_LIBRARY."""
+    import os
+    return Path(os.environ.get("UBR_LIBRARY") or (LIBDIR / "libubr.so"))
 
 
 def lib():

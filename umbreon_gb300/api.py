@@ -291,11 +291,12 @@ class FrameResult:
 class Context:
     """One GPU, one stream (ubr_context)."""
 
-    def __init__(self, device: int = 0, arena_bytes: int = 0, stream: int | None = None, bvh_leaf_max: int = 0):
+    def __init__(self, device: int = 0, arena_bytes: int = 0, stream: int | None = None, bvh_leaf_max: int = 0,
+                 trace_mode: int = 0):
         L = abi.lib()
         self._L = L
         h = C.c_void_p()
-        cd = abi.ContextDesc(abi.ABI_VERSION, device, arena_bytes, stream, bvh_leaf_max)
+        cd = abi.ContextDesc(abi.ABI_VERSION, device, arena_bytes, stream, bvh_leaf_max, trace_mode)
         st = L.ubr_context_create(C.byref(h), C.byref(cd))
         if st != abi.UBR_OK:
             raise abi.UbrError(st, "ubr_context_create failed")

@@ -18,6 +18,7 @@
 // (image_ops.cpp:9-35) and assumed gamma (image_ops.cpp:37-46).
 // Per-pixel and per-ray results do not depend on launch order, so a frame is
 // bit-reproducible.
+#include <algorithm>
 #include <chrono>
 #include <mutex>
 #include <cmath>
@@ -54,6 +55,7 @@ struct Bufs {
   unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
   uint32_t* counter;  // [0] next-queue size, [1] occlusion work-queue size
   uint32_t* occQueue; // queue slots of hits that cast AO / shadow rays
+  unsigned long long* cursor;  // next ray of the persistent occlusion kernel
 };
 
 UBR_D f3 ld3(const float4 v) { return f3{v.x, v.y, v.z}; }
@@ -106,7 +108,7 @@ UBR_D bool slabHit(float lox, float hix, float loy, float hiy, float loz, float 
 constexpr int kMaskMesh = 1 << kMesh, kMaskSphere = 1 << kSphere, kMaskRound = 1 << kRound,
               kMaskCone = 1 << kCone, kMaskAll = 15;
 
-template <int KM>
+template <int KM, bool ATTR = true>
 UBR_D bool testLeaf(const DScene& s, int slot, const Ray& r, const TriPre& pre, float tnear,
                     float tmax, Hit& h, uint32_t& ref) {
   ref = __ldg(&s.leafRef[slot]);
@@ -115,7 +117,7 @@ UBR_D bool testLeaf(const DScene& s, int slot, const Ray& r, const TriPre& pre, 
   constexpr bool single = (KM & (KM - 1)) == 0;
   if ((KM & kMaskSphere) && (single || kind == kSphere)) {
     const float4 q = __ldg(g);
-    return isectSphere(r, f3{q.x, q.y, q.z}, q.w, tnear, tmax, h);
+    return isectSphere<ATTR>(r, f3{q.x, q.y, q.z}, q.w, tnear, tmax, h);
   }
   if ((KM & kMaskMesh) && (single || kind == kMesh)) {
     const float4 a = __ldg(g), b = __ldg(g + 1), c = __ldg(g + 2);
@@ -123,8 +125,10 @@ UBR_D bool testLeaf(const DScene& s, int slot, const Ray& r, const TriPre& pre, 
   }
   if (!(KM & (kMaskCone | kMaskRound))) return false;
   const float4 a = __ldg(g), b = __ldg(g + 1);
-  if ((KM & kMaskCone) && (!(KM & kMaskRound) || kind == kCone))
-    return isectConeCurve(r, ld3(a), a.w, ld3(b), b.w, tnear, tmax, h);
+  if ((KM & kMaskCone) && (!(KM & kMaskRound) || kind == kCone)) {
+    const float4 ax = __ldg(g + 2);
+    return isectConeCurveAxis<ATTR>(r, ld3(a), a.w, ld3(b), b.w, ld3(ax), ax.w, tnear, tmax, h);
+  }
   if (!(KM & kMaskRound)) return false;
   const uint32_t prim = refPrim(ref);
   const uint32_t flags = __float_as_uint(__ldg(g + 2).x);
@@ -164,116 +168,143 @@ UBR_D float byteToFloat(uint32_t q, int b) {
   return __uint_as_float(__byte_perm(q, 0x4B000000u, 0x7540u + uint32_t(b))) - 8388608.0f;
 }
 
-template <bool COUNT = false, int KM = kMaskAll>
+// Traversal state of one ray, resumable one node at a time (the persistent
+// occlusion kernel interleaves rays at node granularity).
+struct TravState {
+  int node;                      // node to visit next
+  int sp;
+  uint32_t steps;
+  float tmax;
+  uint32_t bestGeom, bestPrim;
+  uint32_t stack[kStackDepth];   // group entries: (childBase << 8) | slot mask
+};
+
+UBR_D void travInit(const Ray& r, TravState& st, Hit& best) {
+  st.node = 0;
+  st.sp = 0;
+  st.steps = 0;
+  st.tmax = r.tfar;
+  st.bestGeom = kInvalid;
+  st.bestPrim = kInvalid;
+  best.ref = kInvalid;
+}
+
+// Visit st.node: test its 8 children, its hit leaves' primitives, choose the
+// next node.  Returns true when the ray is finished (any-hit found, stack
+// empty, or the step bound reached).
+template <bool COUNT, int KM, bool ALWAYS_ANY = false>
+UBR_D bool travStep(const DScene& s, const Ray& r, const f3& inv, const TriPre& pre, TravState& st, Hit& best,
+                    uint32_t& overflow, Count* cnt, bool any) {
+  if (ALWAYS_ANY) any = true;
+  if (++st.steps > s.primCount + 16u) {  // each node at most once per ray in a valid tree
+    ++overflow;
+    return true;
+  }
+  if (COUNT) ++cnt->nodes;
+  const float4* nd = s.wnodes + kWideF4 * st.node;
+  const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3), n4 = __ldg(nd + 4);
+  const uint32_t hdr = __float_as_uint(n0.w);
+  const float sx = __uint_as_float((hdr & 0xFFu) << 23) * inv.x;
+  const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * inv.y;
+  const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23) * inv.z;
+  const int nInt = int((hdr >> 24) & 0xFu), nCh = int(hdr >> 28);
+  const float ox = (n0.x - r.org.x) * inv.x, oy = (n0.y - r.org.y) * inv.y, oz = (n0.z - r.org.z) * inv.z;
+  const uint32_t childBase = __float_as_uint(n1.x);
+  const int primBase = __float_as_int(n1.y);
+  const uint32_t meta0 = __float_as_uint(n1.z), meta1 = __float_as_uint(n1.w);
+  // near/far planes per axis by the sign of the direction (swap lo/hi words)
+  const bool nx = inv.x < 0.0f, ny = inv.y < 0.0f, nz = inv.z < 0.0f;
+  const uint32_t qnx[2] = {nx ? __float_as_uint(n3.z) : __float_as_uint(n2.x),
+                           nx ? __float_as_uint(n3.w) : __float_as_uint(n2.y)};
+  const uint32_t qfx[2] = {nx ? __float_as_uint(n2.x) : __float_as_uint(n3.z),
+                           nx ? __float_as_uint(n2.y) : __float_as_uint(n3.w)};
+  const uint32_t qny[2] = {ny ? __float_as_uint(n4.x) : __float_as_uint(n2.z),
+                           ny ? __float_as_uint(n4.y) : __float_as_uint(n2.w)};
+  const uint32_t qfy[2] = {ny ? __float_as_uint(n2.z) : __float_as_uint(n4.x),
+                           ny ? __float_as_uint(n2.w) : __float_as_uint(n4.y)};
+  const uint32_t qnz[2] = {nz ? __float_as_uint(n4.z) : __float_as_uint(n3.x),
+                           nz ? __float_as_uint(n4.w) : __float_as_uint(n3.y)};
+  const uint32_t qfz[2] = {nz ? __float_as_uint(n3.x) : __float_as_uint(n4.z),
+                           nz ? __float_as_uint(n3.y) : __float_as_uint(n4.w)};
+  uint32_t hitInt = 0, primMask = 0;
+  float nearT = kInfF;
+  int nearK = -1;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int w = k >> 2;
+    const float tnx = fmaf(byteToFloat(qnx[w], k & 3), sx, ox), tfx = fmaf(byteToFloat(qfx[w], k & 3), sx, ox);
+    const float tny = fmaf(byteToFloat(qny[w], k & 3), sy, oy), tfy = fmaf(byteToFloat(qfy[w], k & 3), sy, oy);
+    const float tnz = fmaf(byteToFloat(qnz[w], k & 3), sz, oz), tfz = fmaf(byteToFloat(qfz[w], k & 3), sz, oz);
+    const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tnear));
+    const float tmx = fminf(fminf(tfx, tfy), fminf(tfz, st.tmax));
+    const bool hit = k < nCh && tmin <= tmx * kSlabGrow;
+    if (k < nInt) {
+      hitInt |= hit ? (1u << k) : 0u;
+      const bool nearer = hit && tmin < nearT;
+      nearT = nearer ? tmin : nearT;
+      nearK = nearer ? k : nearK;
+    } else if (hit) {
+      const uint32_t m = ((w == 0 ? meta0 : meta1) >> ((k & 3) * 8)) & 0xFFu;
+      primMask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+    }
+  }
+  // primitives of the hit leaves
+  while (primMask) {
+    const int q = __ffs(primMask) - 1;
+    primMask &= primMask - 1u;
+    Hit h;
+    uint32_t ref;
+    const bool hitLeaf = testLeaf<KM, !ALWAYS_ANY>(s, primBase + q, r, pre, r.tnear, st.tmax, h, ref);
+    if (COUNT) cnt->primBytes += leafBytes(refKind(ref));
+    if (!hitLeaf) continue;
+    if (any) {
+      best = h;
+      best.ref = ref;
+      return true;
+    }
+    const int kind = refKind(ref);
+    const uint32_t gid = s.geomID[kind], prim = refPrim(ref);
+    const bool better = best.ref == kInvalid || h.t < best.t ||
+                        (h.t == best.t && (gid < st.bestGeom || (gid == st.bestGeom && prim < st.bestPrim)));
+    if (better) {
+      best = h;
+      best.ref = ref;
+      st.bestGeom = gid;
+      st.bestPrim = prim;
+      st.tmax = h.t;
+    }
+  }
+  if (nearK >= 0) {
+    const uint32_t rest = hitInt & ~(1u << nearK);
+    if (rest) {
+      if (st.sp < kStackDepth) st.stack[st.sp++] = (childBase << 8) | rest;
+      else ++overflow;
+    }
+    st.node = int(childBase) + nearK;
+    return false;
+  }
+  if (st.sp == 0) return true;
+  const uint32_t g = st.stack[st.sp - 1];
+  const uint32_t mask = g & 0xFFu;
+  const int k = __ffs(mask) - 1;
+  const uint32_t left = mask & (mask - 1u);
+  if (left) st.stack[st.sp - 1] = (g & ~0xFFu) | left;
+  else --st.sp;
+  st.node = int(g >> 8) + k;
+  return false;
+}
+
+// Whole traversal of one ray (one thread per ray).
+template <bool COUNT = false, int KM = kMaskAll, bool ALWAYS_ANY = false>
 __device__ bool traverse(const DScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt, const bool any) {
   best.ref = kInvalid;
   if (s.primCount == 0) return false;
   const f3 inv = safeInv(r.dir);
   TriPre pre;
   if (KM & kMaskMesh) pre = triPre(r.dir);
-  float tmax = r.tfar;
-  uint32_t stack[kStackDepth];
-  int sp = 0;
-  int node = 0;
-  uint32_t bestGeom = kInvalid, bestPrim = kInvalid;
-  uint32_t steps = 0;
-  const uint32_t maxSteps = s.primCount + 16u;  // each node at most once per ray
-  for (;;) {
-    if (++steps > maxSteps) {
-      ++overflow;
-      break;
-    }
-    if (COUNT) ++cnt->nodes;
-    const float4* nd = s.wnodes + kWideF4 * node;
-    const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3), n4 = __ldg(nd + 4);
-    const uint32_t hdr = __float_as_uint(n0.w);
-    const float sx = __uint_as_float((hdr & 0xFFu) << 23) * inv.x;
-    const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * inv.y;
-    const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23) * inv.z;
-    const int nInt = int((hdr >> 24) & 0xFu), nCh = int(hdr >> 28);
-    const float ox = (n0.x - r.org.x) * inv.x, oy = (n0.y - r.org.y) * inv.y, oz = (n0.z - r.org.z) * inv.z;
-    const uint32_t childBase = __float_as_uint(n1.x);
-    const int primBase = __float_as_int(n1.y);
-    const uint32_t meta0 = __float_as_uint(n1.z), meta1 = __float_as_uint(n1.w);
-    // near/far planes per axis by the sign of the direction (swap lo/hi words)
-    const bool nx = inv.x < 0.0f, ny = inv.y < 0.0f, nz = inv.z < 0.0f;
-    const uint32_t qnx[2] = {nx ? __float_as_uint(n3.z) : __float_as_uint(n2.x),
-                             nx ? __float_as_uint(n3.w) : __float_as_uint(n2.y)};
-    const uint32_t qfx[2] = {nx ? __float_as_uint(n2.x) : __float_as_uint(n3.z),
-                             nx ? __float_as_uint(n2.y) : __float_as_uint(n3.w)};
-    const uint32_t qny[2] = {ny ? __float_as_uint(n4.x) : __float_as_uint(n2.z),
-                             ny ? __float_as_uint(n4.y) : __float_as_uint(n2.w)};
-    const uint32_t qfy[2] = {ny ? __float_as_uint(n2.z) : __float_as_uint(n4.x),
-                             ny ? __float_as_uint(n2.w) : __float_as_uint(n4.y)};
-    const uint32_t qnz[2] = {nz ? __float_as_uint(n4.z) : __float_as_uint(n3.x),
-                             nz ? __float_as_uint(n4.w) : __float_as_uint(n3.y)};
-    const uint32_t qfz[2] = {nz ? __float_as_uint(n3.x) : __float_as_uint(n4.z),
-                             nz ? __float_as_uint(n3.y) : __float_as_uint(n4.w)};
-    uint32_t hitInt = 0, primMask = 0;
-    float nearT = kInfF;
-    int nearK = -1;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int w = k >> 2;
-      const float tnx = fmaf(byteToFloat(qnx[w], k & 3), sx, ox), tfx = fmaf(byteToFloat(qfx[w], k & 3), sx, ox);
-      const float tny = fmaf(byteToFloat(qny[w], k & 3), sy, oy), tfy = fmaf(byteToFloat(qfy[w], k & 3), sy, oy);
-      const float tnz = fmaf(byteToFloat(qnz[w], k & 3), sz, oz), tfz = fmaf(byteToFloat(qfz[w], k & 3), sz, oz);
-      const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tnear));
-      const float tmx = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
-      const bool hit = k < nCh && tmin <= tmx * kSlabGrow;
-      if (k < nInt) {
-        hitInt |= hit ? (1u << k) : 0u;
-        const bool nearer = hit && tmin < nearT;
-        nearT = nearer ? tmin : nearT;
-        nearK = nearer ? k : nearK;
-      } else {
-        const uint32_t m = ((w == 0 ? meta0 : meta1) >> ((k & 3) * 8)) & 0xFFu;
-        primMask |= hit ? (((1u << (m >> 5)) - 1u) << (m & 31u)) : 0u;
-      }
-    }
-    // primitives of the hit leaves
-    while (primMask) {
-      const int q = __ffs(primMask) - 1;
-      primMask &= primMask - 1u;
-      Hit h;
-      uint32_t ref;
-      const bool hitLeaf = testLeaf<KM>(s, primBase + q, r, pre, r.tnear, tmax, h, ref);
-      if (COUNT) cnt->primBytes += leafBytes(refKind(ref));
-      if (!hitLeaf) continue;
-      if (any) {
-        best = h;
-        best.ref = ref;
-        return true;
-      }
-      const int kind = refKind(ref);
-      const uint32_t gid = s.geomID[kind], prim = refPrim(ref);
-      const bool better = best.ref == kInvalid || h.t < best.t ||
-                          (h.t == best.t && (gid < bestGeom || (gid == bestGeom && prim < bestPrim)));
-      if (better) {
-        best = h;
-        best.ref = ref;
-        bestGeom = gid;
-        bestPrim = prim;
-        tmax = h.t;
-      }
-    }
-    if (nearK >= 0) {
-      const uint32_t rest = hitInt & ~(1u << nearK);
-      if (rest) {
-        if (sp < kStackDepth) stack[sp++] = (childBase << 8) | rest;
-        else ++overflow;
-      }
-      node = int(childBase) + nearK;
-      continue;
-    }
-    if (sp == 0) break;
-    const uint32_t g = stack[sp - 1];
-    const uint32_t mask = g & 0xFFu;
-    const int k = __ffs(mask) - 1;
-    const uint32_t left = mask & (mask - 1u);
-    if (left) stack[sp - 1] = (g & ~0xFFu) | left;
-    else --sp;
-    node = int(g >> 8) + k;
+  TravState st;
+  travInit(r, st, best);
+  while (!travStep<COUNT, KM, ALWAYS_ANY>(s, r, inv, pre, st, best, overflow, cnt, any)) {
   }
   return best.ref != kInvalid;
 }
@@ -500,6 +531,74 @@ __global__ void __launch_bounds__(128) k_surface(Params p, DScene s, Bufs b, int
   if (cast) b.occQueue[qb + off] = i;
 }
 
+// The AO / shadow ray j of the hit in queue slot `slot` (rays of a hit: AO
+// sample j < aoSamples, then each light's shadow samples in light order).
+struct OccRay {
+  Ray r;
+  bool trace;    // needs a traversal
+  bool anyHit;   // binary visibility (false: nearest t, enhanced AO)
+  bool grazing;  // AO sample below the 0.01 cosine: counts as occluded
+  bool ao;       // this is an AO ray of an AO-receiving hit
+};
+
+UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, int j) {
+  OccRay o;
+  o.trace = false;
+  o.anyHit = true;
+  o.grazing = false;
+  o.ao = false;
+  const uint2 sc = b.surfC[slot];
+  const uint32_t flags = sc.y;
+  const int px = int(sc.x % uint32_t(p.W)), py = int(sc.x / uint32_t(p.W));
+  const float4 sa = b.surfA[slot], sb = b.surfB[slot];
+  const f3 N = ld3(sb);
+  f3 dir{0.0f, 0.0f, 0.0f};
+  float tfar = kInfF;
+  if (j < p.aoSamples) {
+    if (flags & 2u) {
+      o.ao = true;
+      const Frame3 f = frameFromNormal(N);
+      dir = aoDir(p, f, px, py, j);
+      o.grazing = dot(dir, N) < 0.01f;
+      o.trace = !o.grazing;
+      o.anyHit = !p.aoEnhanced;
+      tfar = p.aoDistance;
+    }
+  } else if (flags & 4u) {
+    const int k = j - p.aoSamples;
+    int l = 0;
+    while (l + 1 < p.nLights && b.lights[l + 1].rayOffset <= k) ++l;
+    const LightD L = b.lights[l];
+    if (dot(N, L.L) > 0.0f) {
+      dir = L.L;
+      if (L.soft) {
+        // the (px, py) stream is advanced by every earlier lit soft light
+        // (shading.hpp:100, secondary_rays.hpp:128-131)
+        int consumed = 0;
+        for (int q = 0; q < l; ++q) {
+          const LightD Q = b.lights[q];
+          if (Q.soft && dot(N, Q.L) > 0.0f) consumed += Q.samples;
+        }
+        uint32_t s0 = uint32_t(px), s1 = uint32_t(py);
+        const int stepsRng = consumed + (k - L.rayOffset) + 1;
+        for (int q = 0; q < stepsRng; ++q) tea2(s0, s1);
+        dir = sampleLightDir(L, u32ToUnorm(s0), u32ToUnorm(s1));
+      }
+      o.trace = true;
+    }
+  }
+  o.r = Ray{ld3(sa), dir, sa.w, tfar};
+  return o;
+}
+
+UBR_D void occlusionWrite(const Params& p, const Bufs& b, uint32_t slot, int j, const OccRay& o, bool hit,
+                          float t) {
+  const uint8_t res = o.grazing ? 1 : (hit ? 1 : 0);
+  if (o.ao && p.aoEnhanced) b.aoT[uint64_t(slot) * p.aoSamples + j] = o.grazing ? -1.0f : (hit ? t : kInfF);
+  b.occ[uint64_t(slot) * uint64_t(p.raysPerHit) + j] = res;
+}
+
+// One thread per AO / shadow ray.
 template <bool COUNT, int KM>
 __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p, DScene s, Bufs b, uint32_t n) {
   Count cnt;
@@ -510,59 +609,82 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p, DScene s, 
   if (tid < uint64_t(nq) * R) {
     const uint32_t slot = b.occQueue[uint32_t(tid / R)];
     const int j = int(tid % R);
-    const uint2 sc = b.surfC[slot];
-    const uint32_t flags = sc.y;
-    const int px = int(sc.x % uint32_t(p.W)), py = int(sc.x / uint32_t(p.W));
-    // the ray of this thread: AO sample j, or a shadow ray of light l
-    bool trace = false, anyHit = true, grazing = false;
-    f3 dir{0.0f, 0.0f, 0.0f};
-    float tfar = kInfF;
-    const float4 sa = b.surfA[slot], sb = b.surfB[slot];
-    const f3 N = ld3(sb);
-    if (j < p.aoSamples) {
-      if (flags & 2u) {
-        const Frame3 f = frameFromNormal(N);
-        dir = aoDir(p, f, px, py, j);
-        grazing = dot(dir, N) < 0.01f;
-        trace = !grazing;
-        anyHit = !p.aoEnhanced;
-        tfar = p.aoDistance;
-      }
-    } else if (flags & 4u) {
-      const int k = j - p.aoSamples;
-      int l = 0;
-      while (l + 1 < p.nLights && b.lights[l + 1].rayOffset <= k) ++l;
-      const LightD L = b.lights[l];
-      if (dot(N, L.L) > 0.0f) {
-        dir = L.L;
-        if (L.soft) {
-          // the (px, py) stream is advanced by every earlier lit soft light
-          // (shading.hpp:100, secondary_rays.hpp:128-131)
-          int consumed = 0;
-          for (int q = 0; q < l; ++q) {
-            const LightD Q = b.lights[q];
-            if (Q.soft && dot(N, Q.L) > 0.0f) consumed += Q.samples;
-          }
-          uint32_t s0 = uint32_t(px), s1 = uint32_t(py);
-          const int stepsRng = consumed + (k - L.rayOffset) + 1;
-          for (int q = 0; q < stepsRng; ++q) tea2(s0, s1);
-          dir = sampleLightDir(L, u32ToUnorm(s0), u32ToUnorm(s1));
-        }
-        trace = true;
-      }
-    }
-    uint8_t res = grazing ? 1 : 0;
-    float th = grazing ? -1.0f : kInfF;
-    if (trace) {
-      Ray r{ld3(sa), dir, sa.w, tfar};
-      Hit h;
-      const bool hit = traverse<COUNT, KM>(s, r, h, ovf, &cnt, anyHit);
-      res = hit ? 1 : 0;
-      if (hit) th = h.t;
+    const OccRay o = occlusionRay(p, b, slot, j);
+    bool hit = false;
+    Hit h;
+    h.t = kInfF;
+    if (o.trace) {
+      hit = p.aoEnhanced ? traverse<COUNT, KM, false>(s, o.r, h, ovf, &cnt, o.anyHit)
+                         : traverse<COUNT, KM, true>(s, o.r, h, ovf, &cnt, true);
       traced = 1;
     }
-    if (j < p.aoSamples && p.aoEnhanced && (flags & 2u)) b.aoT[uint64_t(slot) * p.aoSamples + j] = th;
-    b.occ[uint64_t(slot) * R + j] = res;
+    occlusionWrite(p, b, slot, j, o, hit, h.t);
+  }
+  warpCount(&b.stats[1], traced);
+  warpCount(&b.stats[3], ovf);
+  if (COUNT) {
+    warpCount(&b.stats[6], cnt.nodes);
+    warpCount(&b.stats[7], cnt.primBytes);
+  }
+}
+
+// Persistent variant: a resident grid whose warps keep their lanes busy.
+// Each lane advances its ray one BVH node per iteration; when at least
+// kRefill lanes of a warp are idle they fetch the next rays of the global
+// list with one atomic per warp (dynamic fetch after Aila and Laine,
+// "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009), so
+// lanes whose rays end early do not wait for the warp's longest ray.
+constexpr int kRefill = 8;
+
+template <bool COUNT, int KM>
+__global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p, DScene s, Bufs b) {
+  Count cnt;
+  uint32_t traced = 0, ovf = 0;
+  const uint64_t R = uint64_t(p.raysPerHit);
+  const uint64_t total = uint64_t(*(volatile const uint32_t*)(b.counter + 1)) * R;
+  const int lane = threadIdx.x & 31;
+  bool active = false, exhausted = total == 0;
+  uint32_t slot = 0;
+  int j = 0;
+  OccRay o;
+  f3 inv{0.0f, 0.0f, 0.0f};
+  TriPre pre;
+  TravState st;
+  Hit best;
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active);
+    if (!exhausted && (__popc(idle) >= kRefill || idle == 0xFFFFFFFFu)) {
+      const int leader = __ffs(idle) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(b.cursor, (unsigned long long)__popc(idle));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (!active) {
+        const uint64_t rid = base + uint64_t(__popc(idle & ((1u << lane) - 1u)));
+        if (rid < total) {
+          slot = b.occQueue[uint32_t(rid / R)];
+          j = int(rid % R);
+          o = occlusionRay(p, b, slot, j);
+          if (o.trace && s.primCount > 0) {
+            inv = safeInv(o.r.dir);
+            if (KM & kMaskMesh) pre = triPre(o.r.dir);
+            travInit(o.r, st, best);
+            active = true;
+            ++traced;
+          } else {
+            occlusionWrite(p, b, slot, j, o, false, kInfF);
+          }
+        }
+      }
+      if (base + uint64_t(__popc(idle)) >= total) exhausted = true;
+    }
+    if (!__any_sync(0xFFFFFFFFu, active)) {
+      if (exhausted) break;
+      continue;
+    }
+    if (active && travStep<COUNT, KM>(s, o.r, inv, pre, st, best, ovf, &cnt, o.anyHit)) {
+      occlusionWrite(p, b, slot, j, o, best.ref != kInvalid, best.t);
+      active = false;
+    }
   }
   warpCount(&b.stats[1], traced);
   warpCount(&b.stats[3], ovf);
@@ -995,7 +1117,7 @@ __global__ void k_occluded_segments(DScene s, const float* segs, uint64_t n, flo
       if (tnear < tfar) {
         Ray r{a, dir, tnear, tfar};
         Hit h;
-        res = traverse<false, kMaskAll>(s, r, h, ovf, nullptr, true) ? 1 : 0;
+        res = traverse<false, kMaskAll, true>(s, r, h, ovf, nullptr, true) ? 1 : 0;
       }
     }
     out[i] = res;
@@ -1054,6 +1176,23 @@ void launchOcclusion(int km, bool count, uint32_t grid, int tb, cudaStream_t st,
   UBR_KM_DISPATCH(k_trace_occlusion, km, count, grid, tb, st, p, s, b, n);
 }
 
+// Resident grid of the persistent occlusion kernel: SMs x resident blocks.
+uint32_t persistentGrid(int device) {
+  static int cached[64] = {};
+  if (device >= 0 && device < 64 && cached[device]) return uint32_t(cached[device]);
+  int sms = 0, perSm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_trace_occlusion_persistent<false, kMaskAll>, 128, 0);
+  const int g = std::max(1, sms) * std::max(1, perSm);
+  if (device >= 0 && device < 64) cached[device] = g;
+  return uint32_t(g);
+}
+
+void launchOcclusionPersistent(int km, bool count, uint32_t grid, int tb, cudaStream_t st, const Params& p,
+                               const DScene& s, const Bufs& b) {
+  UBR_KM_DISPATCH(k_trace_occlusion_persistent, km, count, grid, tb, st, p, s, b);
+}
+
 template <class T>
 T* scratchT(Context* c, int slot, size_t count, ubr_status& st) {
   void* ptr = nullptr;
@@ -1090,6 +1229,7 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
     b.surfB = scratchT<float4>(c, 28, npix, st);
     b.surfC = scratchT<uint2>(c, 29, npix, st);
     b.occQueue = scratchT<uint32_t>(c, 36, npix, st);
+    b.cursor = scratchT<unsigned long long>(c, 37, 1, st);
     b.occ = scratchT<uint8_t>(c, 30, size_t(npix) * p.raysPerHit, st);
     if (p.aoEnhanced && p.aoSamples > 0) b.aoT = scratchT<float>(c, 31, size_t(npix) * p.aoSamples, st);
   }
@@ -1149,9 +1289,13 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
       k_surface<<<grid, TB, 0, s>>>(p, sc->view, b, layer, n, queue);
       mark(1, false);
       const uint64_t nr = uint64_t(n) * uint64_t(p.raysPerHit);
-      const uint32_t og = uint32_t((nr + TB - 1) / TB);
       mark(2, true);
-      launchOcclusion(km, count, og, TB, s, p, sc->view, b, n);
+      if (c->traceMode == 1) {
+        launchOcclusion(km, count, uint32_t((nr + TB - 1) / TB), TB, s, p, sc->view, b, n);
+      } else {
+        UBR_CUDA(c, cudaMemsetAsync(b.cursor, 0, sizeof(unsigned long long), s));
+        launchOcclusionPersistent(km, count, persistentGrid(c->device), TB, s, p, sc->view, b);
+      }
       mark(2, false);
       kernels += 2;
     }

@@ -492,7 +492,14 @@ __global__ void k_refit(BuildIn in, int n, int idxBits, const unsigned long long
     const uint32_t v = kind == kRound ? in.rcIdx[prim] : in.ccIdx[prim];
     lg[0] = V[v];
     lg[1] = V[v + 1];
-    lg[2] = make_float4(__uint_as_float(kind == kRound ? uint32_t(in.rcFlags[prim]) : 0u), 0, 0, 0);
+    if (kind == kRound) {
+      lg[2] = make_float4(__uint_as_float(uint32_t(in.rcFlags[prim])), 0, 0, 0);
+    } else {
+      f3 a;
+      float L;
+      segmentAxis(f3{V[v].x, V[v].y, V[v].z}, f3{V[v + 1].x, V[v + 1].y, V[v + 1].z}, a, L);
+      lg[2] = make_float4(a.x, a.y, a.z, L);
+    }
   }
   if (n == 1) return;
   const float4 bl = boxLo[g], bh = boxHi[g];

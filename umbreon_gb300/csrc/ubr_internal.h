@@ -77,7 +77,7 @@ constexpr int kNodeF4 = 4;
 // Leaf slot geometry = 3 float4, by kind:
 //   mesh   : v0 | v1 | v2          (xyz, w unused)
 //   sphere : (c, r)
-//   cone   : (p0, r0) | (p1, r1)
+//   cone   : (p0, r0) | (p1, r1) | (unit axis, length) from segmentAxis
 //   round  : (p0, r0) | (p1, r1) | (flags bits, -, -, -)
 constexpr int kLeafF4 = 3;
 
@@ -197,6 +197,8 @@ UBR_HD bool isectTriangle(const Ray& r, const TriPre& pre, f3 v0, f3 v1, f3 v2, 
 }
 
 // Sphere, perpendicular-distance form; front root first, back root second.
+// ATTR = false (any-hit queries) skips the hit attributes.
+template <bool ATTR = true>
 UBR_HD bool isectSphere(const Ray& r, f3 c, float rad, float tnear, float tmax, Hit& h) {
   const f3 c0 = c - r.org;
   const float rd2 = 1.0f / dot(r.dir, r.dir);
@@ -213,9 +215,11 @@ UBR_HD bool isectSphere(const Ray& r, f3 c, float rad, float tnear, float tmax, 
   else if (tb >= tnear && tb <= tmax) t = tb;
   else return false;
   h.t = t;
-  h.u = 0.0f;
-  h.v = 0.0f;
-  h.Ng = r.dir * t - c0;
+  if (ATTR) {
+    h.u = 0.0f;
+    h.v = 0.0f;
+    h.Ng = r.dir * t - c0;
+  }
   return true;
 }
 
@@ -269,13 +273,21 @@ UBR_HD int frustumRoots(const Ray& r, f3 b, f3 a, float h0, float h1, float k0, 
   return n;
 }
 
-// Capped cone segment (CONE_LINEAR_CURVE): frustum + flat disks at p0, p1.
-UBR_HD bool isectConeCurve(const Ray& r, f3 p0, float r0, f3 p1, float r1, float tnear,
-                           float tmax, Hit& h) {
+// Unit axis and length of a segment, as the cone intersector derives them
+// (the BVH build stores them in the leaf record with these same operations).
+UBR_HD void segmentAxis(f3 p0, f3 p1, f3& a, float& L) {
   const f3 ax = p1 - p0;
-  const float L = length(ax);
+  L = length(ax);
+  a = ax * (1.0f / L);
+}
+
+// Capped cone segment (CONE_LINEAR_CURVE): frustum + flat disks at p0, p1,
+// with its unit axis `a` and length L precomputed by segmentAxis.
+// ATTR = false (any-hit queries) returns at the first valid hit.
+template <bool ATTR = true>
+UBR_HD bool isectConeCurveAxis(const Ray& r, f3 p0, float r0, f3 p1, float r1, f3 a, float L, float tnear,
+                               float tmax, Hit& h) {
   if (!(L > 0.0f)) return false;
-  const f3 a = ax * (1.0f / L);
   const float k1 = (r1 - r0) / L;
   float ts[2], hs[2];
   const int n = frustumRoots(r, p0, a, 0.0f, L, r0, k1, ts, hs);
@@ -284,9 +296,10 @@ UBR_HD bool isectConeCurve(const Ray& r, f3 p0, float r0, f3 p1, float r1, float
   for (int i = 0; i < n; ++i) {
     if (ts[i] >= tnear && ts[i] <= best) {
       best = ts[i];
+      h.t = ts[i];
+      if (!ATTR) return true;
       const f3 P = r.org + r.dir * ts[i];
       const f3 rad = (P - p0) - a * hs[i];
-      h.t = ts[i];
       h.u = hs[i] / L;
       h.v = 0.0f;
       h.Ng = rad - a * (k1 * length(rad));
@@ -305,6 +318,7 @@ UBR_HD bool isectConeCurve(const Ray& r, f3 p0, float r0, f3 p1, float r1, float
       if (dot(d, d) > rc * rc) continue;
       best = t;
       h.t = t;
+      if (!ATTR) return true;
       h.u = float(e);
       h.v = 0.0f;
       h.Ng = e == 0 ? a * -1.0f : a;
@@ -312,6 +326,13 @@ UBR_HD bool isectConeCurve(const Ray& r, f3 p0, float r0, f3 p1, float r1, float
     }
   }
   return found;
+}
+
+UBR_HD bool isectConeCurve(const Ray& r, f3 p0, float r0, f3 p1, float r1, float tnear, float tmax, Hit& h) {
+  f3 a;
+  float L;
+  segmentAxis(p0, p1, a, L);
+  return isectConeCurveAxis<true>(r, p0, r0, p1, r1, a, L, tnear, tmax, h);
 }
 
 // Round segment (ROUND_LINEAR_CURVE): end spheres + tangent cone, hits kept
