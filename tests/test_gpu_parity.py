@@ -15,7 +15,8 @@ from umbreon_gb300 import scenes
 pytestmark = pytest.mark.gpu
 
 
-def _compare(gpu_ctx, oracle_lib, sc, opt, max_err=1e-3, min_agree=0.999, min_psnr=45.0):
+def _compare(gpu_ctx, oracle_lib, sc, opt, max_err=1e-3, min_agree=0.999, min_psnr=45.0, err_quantile=1.0,
+             hard_max=None):
     b = gpu_ctx.build(sc)
     try:
         g = gpu_ctx.render(b, sc, opt)
@@ -25,12 +26,16 @@ def _compare(gpu_ctx, oracle_lib, sc, opt, max_err=1e-3, min_agree=0.999, min_ps
     agree = id_agreement(g.hit_geom, g.hit_prim, o.hit_geom, o.hit_prim)
     ss = max(1, opt.supersample)
     m = agree_mask_final(g.hit_geom, g.hit_prim, o.hit_geom, o.hit_prim, ss)
-    err = float(np.abs(g.color - o.color)[m].max()) if m.any() else 0.0
+    diff = np.abs(g.color - o.color)[m]
+    err = float(np.quantile(diff, err_quantile)) if diff.size else 0.0
+    worst = float(diff.max()) if diff.size else 0.0
     pl, ps = psnr_linear(g.color, o.color), psnr_srgb(g.color, o.color)
-    info = dict(agree=agree, max_err=err, psnr_linear=pl, psnr_srgb=ps, stats=g.stats)
+    info = dict(agree=agree, err_at_quantile=err, worst=worst, psnr_linear=pl, psnr_srgb=ps, stats=g.stats)
     assert agree >= min_agree, info
     assert pl >= min_psnr and ps >= min_psnr, info
     assert err <= max_err, info
+    if hard_max is not None:
+        assert worst <= hard_max, info
     return g, o, info
 
 
@@ -69,3 +74,58 @@ def test_gpu_determinism(gpu_ctx):
         b.release()
     assert np.array_equal(a.color, c.color)
     assert np.array_equal(a.hit_prim, c.hit_prim)
+
+
+# Scenes with AO / soft shadows: GPU and oracle trace the same per-pixel
+# sample directions, but cos/sin differ in the last ulp between CUDA and
+# libm, so a sample grazing an occluder's silhouette can land on the other
+# side.  Bar: 99.9 % of agreeing pixels within 1e-3 and every pixel within
+# the colour change of two flipped samples.
+AO_QUANTILE = 0.999
+
+
+def test_molecular_surface_small(gpu_ctx, oracle_lib):
+    sc, opt = scenes.molecular_surface(n_atoms=600, box=16.0, n_spheres=300, width=192, height=192,
+                                       ao_samples=8, layers=4)
+    assert sc.triangle_count() > 5000
+    _compare(gpu_ctx, oracle_lib, sc, opt, err_quantile=AO_QUANTILE, hard_max=2 * 0.2 * 2 / 8 + 0.05)
+
+
+def test_enhanced_ao(gpu_ctx, oracle_lib):
+    sc, opt = scenes.space_filling(n=800, width=160, height=120)
+    opt.aoSamples, opt.aoDistance = 12, 5.0
+    opt.aoFalloffPower, opt.aoMultiScale, opt.aoBentNormal = 1.0, True, True
+    opt.aoMultibounce, opt.aoLowDiscrepancy, opt.aoDiffuseFactor = True, True, 0.3
+    opt.aoSkyColor, opt.aoGroundColor = (1.0, 0.95, 0.9), (0.6, 0.6, 0.7)
+    _compare(gpu_ctx, oracle_lib, sc, opt, err_quantile=AO_QUANTILE, hard_max=0.2)
+
+
+def test_env_dome_soft_shadows(gpu_ctx, oracle_lib):
+    sc, opt = scenes.space_filling(n=600, width=128, height=96)
+    opt.envLights, opt.envIntensity, opt.envKeyScale = 6, 0.8, 0.5
+    opt.shadows, opt.lightRadius, opt.shadowSamples = True, 4.0, 3
+    _compare(gpu_ctx, oracle_lib, sc, opt, err_quantile=AO_QUANTILE, hard_max=0.3)
+
+
+def test_clip_planes(gpu_ctx, oracle_lib):
+    sc, opt = scenes.space_filling(n=800, width=160, height=120)
+    sc.clipNear, sc.clipFar = 95.0, 110.0
+    g, o, info = _compare(gpu_ctx, oracle_lib, sc, opt)
+    assert info["stats"]["rays_primary"] > 0
+
+
+def test_open_cylinder_chains(gpu_ctx, oracle_lib):
+    sc, opt = scenes.ball_and_stick(n=1500, width=160, height=96, supersample=2, ao_samples=4)
+    n = len(sc.cyl_p0)
+    sc.cyl_open = (np.arange(n) % 7 != 0).astype(np.uint8)       # open chains broken by capped bonds
+    sc.cyl_radius = np.where(np.arange(n) % 3 == 0, 0.25, 0.2).astype(np.float32)
+    sc.cyl_opacity1 = np.where(np.arange(n) % 5 == 0, 0.3, -1.0).astype(np.float32)
+    sc.cyl_from_edge = (np.arange(n) % 11 == 0).astype(np.uint8)
+    sc.cyl_color[:, 3] = np.where(np.arange(n) % 4 == 0, 0.6, 1.0)
+    _compare(gpu_ctx, oracle_lib, sc, opt, err_quantile=AO_QUANTILE, hard_max=0.3)
+
+
+def test_instances(gpu_ctx, oracle_lib):
+    sc, opt = scenes.space_filling(n=300, width=160, height=120)
+    sc.instance_offsets = np.array([[0, 0, 0], [12.0, 3.0, -5.0], [-9.0, -6.0, 4.0]], np.float32)
+    _compare(gpu_ctx, oracle_lib, sc, opt)

@@ -186,3 +186,138 @@ def material_sphere_scene(color, mat, bg):
     sc.lights = [key_light()]
     sc.background = bg
     return sc
+
+
+# --- molecular surface: iso-surface of a sum of Gaussians -------------------
+
+# Freudenthal split of a cube into 6 tetrahedra around the (0,0,0)-(1,1,1)
+# diagonal; neighbouring cubes split shared faces along the same diagonal, so
+# the extracted surface is crack-free.  Corner c has offset (c&1, c>>1&1, c>>2&1).
+_TETS = np.array([[0, 7, 1, 3], [0, 7, 3, 2], [0, 7, 2, 6], [0, 7, 6, 4], [0, 7, 4, 5], [0, 7, 5, 1]])
+_TET_EDGES = np.array([[0, 1], [0, 2], [0, 3], [1, 2], [1, 3], [2, 3]])
+
+
+def gaussian_density(atoms: np.ndarray, sigma: float, h: float, lo: np.ndarray, shape, cutoff: float = 3.0):
+    """sum_i exp(-|x - a_i|^2 / sigma^2) on a grid (origin lo, spacing h),
+    each atom splatted within cutoff*sigma."""
+    nx, ny, nz = shape
+    field = np.zeros(nx * ny * nz, np.float64)
+    r = int(math.ceil(cutoff * sigma / h))
+    base = np.floor((atoms - lo) / h).astype(np.int64)
+    offs = np.stack(np.meshgrid(*(np.arange(-r, r + 2),) * 3, indexing="ij"), -1).reshape(-1, 3)
+    inv2 = 1.0 / (sigma * sigma)
+    for chunk in np.array_split(offs, max(1, len(offs) // 256)):
+        g = base[None, :, :] + chunk[:, None, :]                  # (c, n, 3)
+        ok = np.all((g >= 0) & (g < np.array(shape)), axis=-1)
+        p = lo + g * h
+        d2 = np.sum((p - atoms[None]) ** 2, axis=-1)
+        w = np.exp(-d2 * inv2) * ok * (d2 <= (cutoff * sigma) ** 2)
+        flat = (g[..., 0] * ny + g[..., 1]) * nz + g[..., 2]
+        field += np.bincount(np.where(ok, flat, 0).ravel(), weights=w.ravel(), minlength=field.size)
+    return field.reshape(shape)
+
+
+def marching_tetrahedra(field: np.ndarray, iso: float, lo: np.ndarray, h: float):
+    """Indexed iso-surface of `field` at `iso`: (positions, normals, index).
+    Triangles wind counter-clockwise seen from the low-field side, and vertex
+    normals point down the gradient (outward for a density)."""
+    nx, ny, nz = field.shape
+    f = field.ravel()
+    gx, gy, gz = np.gradient(field, h)
+    grad = np.stack([gx.ravel(), gy.ravel(), gz.ravel()], 1)
+    ci, cj, ck = np.meshgrid(np.arange(nx - 1), np.arange(ny - 1), np.arange(nz - 1), indexing="ij")
+    cube0 = ((ci * ny + cj) * nz + ck).ravel()
+    corner = np.array([((c & 1) * ny + ((c >> 1) & 1)) * nz + ((c >> 2) & 1) for c in range(8)])
+    inside_c = f[cube0[:, None] + corner[None, :]] > iso
+    keep = inside_c.any(1) & ~inside_c.all(1)
+    cube0 = cube0[keep]
+    tris = []
+    for t in _TETS:
+        vid = cube0[:, None] + corner[t][None, :]                 # (m, 4) grid ids
+        ins = f[vid] > iso
+        case = ins[:, 0] * 1 + ins[:, 1] * 2 + ins[:, 2] * 4 + ins[:, 3] * 8
+        for cs in range(1, 15):
+            sel = case == cs
+            if not sel.any():
+                continue
+            v = vid[sel]
+            inside = [(cs >> q) & 1 for q in range(4)]
+            n_in = sum(inside)
+            # edges crossing the surface, in a cyclic order around the tet
+            if n_in == 1 or n_in == 3:
+                a = inside.index(1) if n_in == 1 else inside.index(0)
+                others = [q for q in range(4) if q != a]
+                polys = [[(a, others[0]), (a, others[1]), (a, others[2])]]
+            else:
+                ia = [q for q in range(4) if inside[q]]
+                oa = [q for q in range(4) if not inside[q]]
+                polys = [[(ia[0], oa[0]), (ia[0], oa[1]), (ia[1], oa[1]), (ia[1], oa[0])]]
+            for poly in polys:
+                ge = np.stack([np.stack([np.minimum(v[:, p], v[:, q]), np.maximum(v[:, p], v[:, q])], 1)
+                               for (p, q) in poly], 1)           # (m, k, 2) sorted edge keys
+                tris.append(ge[:, [0, 1, 2]])
+                if len(poly) == 4:
+                    tris.append(ge[:, [0, 2, 3]])
+    E = np.concatenate(tris, 0)                                   # (T, 3, 2)
+    keys = E[..., 0].astype(np.int64) * f.size + E[..., 1]
+    uk, inv = np.unique(keys.ravel(), return_inverse=True)
+    a_id, b_id = uk // f.size, uk % f.size
+    fa, fb = f[a_id], f[b_id]
+    w = np.clip((iso - fa) / np.where(fb != fa, fb - fa, 1.0), 0.0, 1.0)[:, None]
+
+    def gpos(g):
+        k = g % nz
+        j = (g // nz) % ny
+        i = g // (ny * nz)
+        return lo + np.stack([i, j, k], 1) * h
+
+    pos = gpos(a_id) * (1 - w) + gpos(b_id) * w
+    gv = grad[a_id] * (1 - w) + grad[b_id] * w
+    nrm = -gv / np.maximum(np.linalg.norm(gv, axis=1, keepdims=True), 1e-12)
+    idx = inv.reshape(-1, 3)
+    # orient: geometric normal along the outward (down-gradient) normal
+    p0, p1, p2 = pos[idx[:, 0]], pos[idx[:, 1]], pos[idx[:, 2]]
+    ng = np.cross(p1 - p0, p2 - p0)
+    flip = np.sum(ng * (nrm[idx[:, 0]] + nrm[idx[:, 1]] + nrm[idx[:, 2]]), 1) < 0
+    idx[flip] = idx[flip][:, [0, 2, 1]]
+    area2 = np.linalg.norm(ng, axis=1)
+    idx = idx[area2 > 1e-12]
+    return pos.astype(np.float32), nrm.astype(np.float32), idx.astype(np.uint32)
+
+
+def molecular_surface(seed: int = BASE_SEED + 2, n_atoms: int = 10000, box: float = 60.0, grid: float = 0.5,
+                      sigma: float = 1.5, iso: float = 1.35, n_spheres: int = 5000, width: int = 2048,
+                      height: int = 2048, ao_samples: int = 32, layers: int = 4):
+    """Workload 2: iso-surface (0.5 A grid) of a sum of Gaussians over 10,000
+    random atoms in a 60 A box, vertex alpha 0.5, plus 5,000 opaque sphere
+    atoms; up to 4 transparent layers, 32 AO rays, 2 shadowed lights, 2048^2."""
+    u = uniform(seed, n_atoms, 6)
+    atoms = u[:, :3] * box
+    margin = 3.0 * sigma
+    lo = np.full(3, -margin)
+    shape = tuple([int(math.ceil((box + 2 * margin) / grid)) + 1] * 3)
+    field = gaussian_density(atoms, sigma, grid, lo, shape)
+    pos, nrm, idx = marching_tetrahedra(field, iso, lo, grid)
+    col = np.empty((len(pos), 4), np.float32)
+    col[:, 0] = 0.35 + 0.5 * (pos[:, 0] / box).clip(0, 1)
+    col[:, 1] = 0.55
+    col[:, 2] = 0.85 - 0.5 * (pos[:, 2] / box).clip(0, 1)
+    col[:, 3] = 0.5
+    sc = Scene(mesh_positions=pos, mesh_normals=nrm, mesh_colors=col, mesh_index=idx, mesh_material=pov_material())
+    ns = min(n_spheres, n_atoms)
+    cr = np.empty((ns, 4), np.float32)
+    cr[:, :3] = atoms[:ns]
+    cr[:, 3] = 0.6
+    sc.sphere_center_radius = cr
+    scol = np.ones((ns, 4), np.float32)
+    scol[:, :3] = (0.3 + 0.7 * u[:ns, 3:6]).astype(np.float32)
+    sc.sphere_color = scol
+    sc.sphere_material = np.full(ns, pov_material(), abi.MATERIAL_DTYPE)
+    blo, bhi = pos.min(0), pos.max(0)
+    _frame_ortho(sc, blo, bhi, width, height, margin=1.02)
+    sc.lights = [DistantLight(direction=(-0.4, -0.5, -1.0), intensity=0.8),
+                 DistantLight(direction=(0.6, 0.3, -1.0), intensity=0.4)]
+    sc.background = (1.0, 1.0, 1.0)
+    opt = RenderOptions(width=width, height=height, supersample=1, aoSamples=ao_samples, aoDistance=4.0,
+                        shadows=True, maxTransparentLayers=layers)
+    return sc, opt
