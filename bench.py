@@ -167,6 +167,151 @@ def _cpu_band(sc, opt, threads, target_s):
 _cpu_band.cache = {}
 
 
+def _device_frames(ctx, built, sc, opt, steps, warmup, flush):
+    """Device-resident timing of `steps` frames (outputs in device memory,
+    L2 flushed before each frame); returns ms/frame, traced rays/frame and
+    one profiled frame's phase split."""
+    import ctypes as C
+    import torch
+    from umbreon_gb300 import abi
+    from umbreon_gb300.api import make_render_desc
+    rd, keep = make_render_desc(sc, opt)
+    col = torch.empty((opt.height, opt.width, 4), dtype=torch.float32, device="cuda")
+
+    def one(flags=0):
+        fr = abi.Frame()
+        fr.memory = abi.MEMORY_DEVICE
+        fr.flags = flags
+        fr.color = C.cast(C.c_void_p(col.data_ptr()), abi.f32p)
+        ctx._check(ctx._L.ubr_render(ctx.handle, built.handle, C.byref(rd), C.byref(fr), None, None))
+        return fr
+
+    for _ in range(warmup):
+        one()
+    ms, rays = [], 0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        fr = one()
+        ms.append(fr.total_ms)
+        rays += fr.rays_primary + fr.rays_occlusion
+    pf = one(abi.FRAME_PROFILE)
+    names = ["trace_closest", "surface", "trace_occlusion", "shade", "post"]
+    return (sum(ms) / len(ms), rays / steps, {n: round(v, 3) for n, v in zip(names, pf.phase_ms)},
+            pf.layers)
+
+
+def _cpu_full_or_band(sc, opt, threads, target_s):
+    """CPU restatement timed on a band of rows sized to about target_s."""
+    _cpu_band.cache.clear()
+    _cpu_band.__dict__.pop("rate", None)
+    r = _cpu_band(sc, opt, threads, target_s)
+    return {"Mrays_s": round(r["rays"] / r["secs"] / 1e6, 3),
+            "ms_per_frame": round(r["secs"] * r["frame_rays"] / r["rays"] * 1e3, 1),
+            "sample": f"{r['rows']} of {r['H']} hi-res rows", "cores": threads}
+
+
+def secondary_workloads(args, flush):
+    """Workloads 0, 2 and 3 (space filling, molecular surface, batched
+    turntable), GPU device-resident, with the CPU restatement beside them."""
+    import ctypes as C
+    import torch
+    from umbreon_gb300 import abi, scenes
+    from umbreon_gb300.api import Context, make_render_desc
+    from umbreon_gb300.autotune import autotune
+    out = {}
+    threads = os.cpu_count() or 1
+    ctx = Context(0)
+    # workload 0
+    sc, opt = scenes.space_filling()
+    b = ctx.build(sc)
+    ms, rays, ph, layers = _device_frames(ctx, b, sc, opt, 10, 3, flush)
+    b.release()
+    cpu = _cpu_full_or_band(sc, opt, threads, 2.0) if not args.no_cpu else None
+    out["space_filling_2k_640x480"] = {"ms_per_frame": round(ms, 4), "Mrays_s": round(rays / ms / 1e3, 1),
+                                       "phase_ms": ph, "cpu": cpu}
+    # workload 2
+    t0 = time.perf_counter()
+    sc, opt = scenes.molecular_surface()
+    gen_s = time.perf_counter() - t0
+    b = ctx.build(sc)
+    info = b.info()
+    ms, rays, ph, layers = _device_frames(ctx, b, sc, opt, 3, 3, flush)
+    b.release()
+    cpu = _cpu_full_or_band(sc, opt, threads, 4.0) if not args.no_cpu else None
+    out["molecular_surface_2048"] = {"triangles": int(info["prim_count"][0]), "spheres": int(info["prim_count"][1]),
+                                     "bvh_build_ms": round(info["build_ms"], 1), "generate_s": round(gen_s, 1),
+                                     "ms_per_frame": round(ms, 3), "Mrays_s": round(rays / ms / 1e3, 1),
+                                     "rays_per_frame": int(rays), "layers": int(layers), "phase_ms": ph,
+                                     "cpu": cpu}
+    ctx.close()
+    # workload 3: batched vs one frame per call
+    bases, items = scenes.turntable_batch()
+    tune = autotune(items[0][1], items[0][2])
+    res = {"autotune": tune}
+    for label, its in (("turntable_64_mixed", items),
+                       ("turntable_64_small_256", [(si, sc2, _resized(o, 256)) for si, sc2, o in items])):
+        entry = {}
+        for mode, graphs in (("batched", True), ("per_frame_graph", True), ("per_frame_no_graph", False)):
+            cx = Context(0, bvh_leaf_max=tune["bvh_leaf_max"], trace_mode=tune["trace_mode"], graphs=graphs)
+            built = [cx.build(bs) for bs in bases]
+            descs, outs, frames = [], [], []
+            for si, sc2, o in its:
+                rd, k = make_render_desc(sc2, o)
+                descs.append((rd, k))
+                t = torch.empty((o.height, o.width, 4), dtype=torch.float32, device="cuda")
+                outs.append(t)
+                fr = abi.Frame()
+                fr.memory = abi.MEMORY_DEVICE
+                fr.color = C.cast(C.c_void_p(t.data_ptr()), abi.f32p)
+                frames.append(fr)
+            arr = (abi.BatchItem * len(its))()
+            for i, (si, sc2, o) in enumerate(its):
+                arr[i].scene = built[si].handle
+                arr[i].desc = C.pointer(descs[i][0])
+                arr[i].frame = C.pointer(frames[i])
+
+            def run():
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                if mode == "batched":
+                    tot = abi.Frame()
+                    cx._check(cx._L.ubr_render_batch(cx.handle, len(its), arr, C.byref(tot)))
+                    rays_ = tot.rays_primary + tot.rays_occlusion
+                else:
+                    rays_ = 0
+                    for i, (si, sc2, o) in enumerate(its):
+                        cx._check(cx._L.ubr_render(cx.handle, built[si].handle, C.byref(descs[i][0]),
+                                                   C.byref(frames[i]), None, None))
+                        rays_ += frames[i].rays_primary + frames[i].rays_occlusion
+                torch.cuda.synchronize()
+                return time.perf_counter() - t1, rays_
+            for _ in range(3):
+                run()
+            runs = [run() for _ in range(5)]
+            wall = min(r[0] for r in runs)
+            entry[mode] = {"ms_per_batch": round(wall * 1e3, 3), "frames_per_s": round(len(its) / wall, 1),
+                           "Mrays_s": round(runs[0][1] / wall / 1e6, 1)}
+            for bb in built:
+                bb.release()
+            cx.close()
+        entry["batched_over_per_frame_graph"] = round(entry["batched"]["frames_per_s"] /
+                                                      entry["per_frame_graph"]["frames_per_s"], 3)
+        entry["batched_over_per_frame_no_graph"] = round(entry["batched"]["frames_per_s"] /
+                                                         entry["per_frame_no_graph"]["frames_per_s"], 3)
+        entry["pixels"] = int(sum(o.width * o.height for _, _, o in its))
+        res[label] = entry
+    out["turntable_batch"] = res
+    return out
+
+
+def _resized(opt, res):
+    import copy
+    o = copy.copy(opt)
+    o.width = o.height = res
+    return o
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -288,6 +433,10 @@ def run_ours(args):
                "kind": "port", "sample": f"{r['rows']} of {r['H']} hi-res rows of the same frame",
                "ms_per_frame_est": round(r["secs"] * r["frame_rays"] / r["rays"] * 1e3, 1)}
 
+    secondary = None
+    if rank == 0 and ws == 1 and not args.no_secondary:
+        secondary = secondary_workloads(args, flush)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
@@ -305,6 +454,7 @@ def run_ours(args):
             "wall_s": round(wall, 3),
             "roofline": roof, "counting_frame": ctr, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(kernels), "clocks": clk.summary(),
+            "workloads": secondary,
         }
         print(json.dumps(line), flush=True)
     built.release()
@@ -322,6 +472,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the other workloads (space filling, "
+                    "molecular surface, batched turntable)")
     ap.add_argument("--leaf-max", type=int, default=0, help="wide-BVH leaf size 1..3 (0 = library default)")
     ap.add_argument("--trace-mode", type=int, default=0, help="occlusion kernel: 1 per-ray, 2 persistent (0 = default)")
     ap.add_argument("--frame", default=None, help="override the frame size WxH (profiling runs)")

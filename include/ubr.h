@@ -251,7 +251,10 @@ typedef struct ubr_context_desc {
   /* occlusion-ray kernel (0 = library default): 1 = one thread per ray,
    * 2 = persistent warps that refill idle lanes with new rays */
   uint32_t trace_mode;
-  uint32_t reserved[6];
+  /* 1 = launch every kernel on its own instead of replaying single-layer
+   * frames from a captured CUDA graph (0 = graphs, the default) */
+  uint32_t disable_graphs;
+  uint32_t reserved[5];
 } ubr_context_desc;
 
 const char* ubr_status_string(ubr_status s);
@@ -289,6 +292,22 @@ ubr_status ubr_render(ubr_context* ctx, const ubr_scene* scene,
                       const ubr_render_desc* desc, ubr_frame* frame,
                       const volatile int32_t* cancel_flag,
                       uint64_t* progress_units);
+
+/* Many frames in one launch sequence: every stage runs once over the pixels
+ * and rays of all items (a global ray queue), and single-layer batches are
+ * replayed from a CUDA graph.  Items may use different scenes, cameras,
+ * resolutions and options; each item's outputs go to its own frame buffers.
+ * `total` (may be NULL) receives the batch's statistics; its `flags` select
+ * profiling as for ubr_render.  No reference counterpart (the reference
+ * renders one frame per call). */
+typedef struct ubr_batch_item {
+  const ubr_scene* scene;
+  const ubr_render_desc* desc;
+  ubr_frame* frame;
+} ubr_batch_item;
+
+ubr_status ubr_render_batch(ubr_context* ctx, uint32_t n, const ubr_batch_item* items,
+                            ubr_frame* total);
 
 /* Segment occlusion for the stroke-edge pass: out[i] = 1 when any geometry
  * lies strictly inside segment (p[i], q[i]) trimmed by eps

@@ -125,13 +125,17 @@ FRAME_COUNT = 2
 class ContextDesc(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("device", C.c_int32), ("arena_bytes", C.c_uint64),
                 ("stream", C.c_void_p), ("bvh_leaf_max", C.c_uint32), ("trace_mode", C.c_uint32),
-                ("reserved", C.c_uint32 * 6)]
+                ("disable_graphs", C.c_uint32), ("reserved", C.c_uint32 * 5)]
 
 
 class SceneInfo(C.Structure):
     _fields_ = [("prim_count", C.c_uint64 * 4), ("geom_id", C.c_uint32 * 4), ("bvh_nodes", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("build_ms", C.c_double), ("bounds_lo", C.c_float * 3),
                 ("bounds_hi", C.c_float * 3)]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("desc", C.POINTER(RenderDesc)), ("frame", C.POINTER(Frame))]
 
 
 # Every symbol include/ubr.h declares, with its ctypes signature.
@@ -146,6 +150,7 @@ SIGNATURES = {
     "ubr_scene_get_info": (C.c_int, [C.c_void_p, C.POINTER(SceneInfo)]),
     "ubr_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderDesc), C.POINTER(Frame),
                              C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
+    "ubr_render_batch": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(BatchItem), C.POINTER(Frame)]),
     "ubr_occluded_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
                                      C.c_void_p, C.c_int32]),
     "ubr_occluded_batch_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,

@@ -292,11 +292,12 @@ class Context:
     """One GPU, one stream (ubr_context)."""
 
     def __init__(self, device: int = 0, arena_bytes: int = 0, stream: int | None = None, bvh_leaf_max: int = 0,
-                 trace_mode: int = 0):
+                 trace_mode: int = 0, graphs: bool = True):
         L = abi.lib()
         self._L = L
         h = C.c_void_p()
-        cd = abi.ContextDesc(abi.ABI_VERSION, device, arena_bytes, stream, bvh_leaf_max, trace_mode)
+        cd = abi.ContextDesc(abi.ABI_VERSION, device, arena_bytes, stream, bvh_leaf_max, trace_mode,
+                             0 if graphs else 1)
         st = L.ubr_context_create(C.byref(h), C.byref(cd))
         if st != abi.UBR_OK:
             raise abi.UbrError(st, "ubr_context_create failed")
@@ -337,6 +338,42 @@ class Context:
         if st not in (abi.UBR_OK,):
             self._check(st)
         return FrameResult(opt.width, opt.height, color, depth, vz, hg, hp, fr.render_ms / 1e3, stats)
+
+    def render_batch(self, items, want_ids: bool = True, flags: int = 0):
+        """Render [(built, scene, opt), ...] in one launch sequence
+        (ubr_render_batch); returns ([FrameResult], batch stats)."""
+        n = len(items)
+        keep, results = [], []
+        arr = (abi.BatchItem * n)()
+        frames = []
+        for i, (built, scene, opt) in enumerate(items):
+            rd, k = make_render_desc(scene, opt)
+            keep += [rd, k]
+            ss = max(1, opt.supersample)
+            W, H = opt.width * ss, opt.height * ss
+            res = FrameResult(opt.width, opt.height, np.zeros((opt.height, opt.width, 4), np.float32),
+                              np.zeros((H, W), np.float32), np.zeros((H, W), np.float32),
+                              np.zeros((H, W), np.uint32) if want_ids else None,
+                              np.zeros((H, W), np.uint32) if want_ids else None)
+            fr = abi.Frame()
+            fr.memory = abi.MEMORY_HOST
+            fr.color = abi.ptr(res.color)
+            fr.depth = abi.ptr(res.depth)
+            fr.view_z = abi.ptr(res.viewZ)
+            fr.hit_geom = abi.ptr(res.hit_geom, C.c_uint32)
+            fr.hit_prim = abi.ptr(res.hit_prim, C.c_uint32)
+            frames.append(fr)
+            results.append(res)
+            arr[i].scene = built.handle
+            arr[i].desc = C.pointer(rd)
+            arr[i].frame = C.pointer(fr)
+        total = abi.Frame()
+        total.flags = flags
+        self._check(self._L.ubr_render_batch(self.handle, n, arr, C.byref(total)))
+        stats = dict(render_ms=total.render_ms, total_ms=total.total_ms, rays_primary=total.rays_primary,
+                     rays_occlusion=total.rays_occlusion, kernels=total.kernels, layers=total.layers,
+                     phase_ms=list(total.phase_ms))
+        return results, stats
 
     def occluded(self, built: "BuiltScene", segs: np.ndarray, eps: float) -> np.ndarray:
         segs = np.ascontiguousarray(segs, np.float32).reshape(-1, 6)

@@ -82,7 +82,8 @@ def build_ubr(verbose: bool = False) -> Path:
             f.result()
     out = LIB / "libubr.so"
     if jobs or _stale(out, objs):
-        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", str(out)] + [str(o) for o in objs])
+        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-Xlinker", "--no-undefined", "-o", str(out)]
+             + [str(o) for o in objs])
     if verbose:
         print("built", out)
     return out

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "ubr_context.h"
 
@@ -16,6 +17,12 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
                        const volatile int32_t* cancel, uint64_t* progress);
 ubr_status occludedBatch(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps, uint8_t* out,
                          int32_t memory);
+struct Job {
+  const Scene* scene;
+  const ubr_render_desc* desc;
+  ubr_frame* frame;
+};
+ubr_status renderBatch(Context* c, const std::vector<Job>& jobs, ubr_frame* total);
 ubr_status occludedBatchNoAlloc(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps,
                                 uint8_t* out);
 
@@ -126,6 +133,7 @@ ubr_status ubr_context_create(ubr_context** out, const ubr_context_desc* desc) {
     }
     x.traceMode = int(desc->trace_mode);
   }
+  if (desc && desc->disable_graphs) x.useGraphs = false;
   if (cudaSetDevice(dev) != cudaSuccess) {
     delete c;
     return UBR_CUDA_ERROR;
@@ -160,6 +168,7 @@ ubr_status ubr_context_destroy(ubr_context* c) {
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t& e : x.pev)
     if (e) cudaEventDestroy(e);
+  if (x.graphExec) cudaGraphExecDestroy(x.graphExec);
   if (x.pinned) cudaFreeHost(x.pinned);
   if (x.ownStream && x.stream) cudaStreamDestroy(x.stream);
   delete c;
@@ -234,6 +243,30 @@ ubr_status ubr_render(ubr_context* c, const ubr_scene* s, const ubr_render_desc*
   if (cancel_flag && *cancel_flag) return setError(&c->impl, UBR_CANCELLED, "render cancelled before launch");
   try {
     return renderFrame(&c->impl, s->impl, *desc, *frame, cancel_flag, progress_units);
+  } catch (const std::bad_alloc&) {
+    return setError(&c->impl, UBR_OUT_OF_MEMORY, "host allocation failed");
+  } catch (...) {
+    return setError(&c->impl, UBR_INTERNAL, "render failed");
+  }
+}
+
+ubr_status ubr_render_batch(ubr_context* c, uint32_t n, const ubr_batch_item* items, ubr_frame* total) {
+  if (!c) return UBR_INVALID_ARGUMENT;
+  if (n == 0) return UBR_OK;
+  if (!items) return setError(&c->impl, UBR_INVALID_ARGUMENT, "render_batch: NULL items");
+  std::vector<Job> jobs;
+  jobs.reserve(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    const ubr_batch_item& it = items[i];
+    if (!it.scene || !it.scene->impl || !it.desc || !it.frame)
+      return setError(&c->impl, UBR_INVALID_ARGUMENT, "render_batch: NULL scene, desc or frame in an item");
+    if (it.scene->impl->ctx != &c->impl)
+      return setError(&c->impl, UBR_INVALID_ARGUMENT, "render_batch: scene from another context");
+    jobs.push_back(Job{it.scene->impl, it.desc, it.frame});
+  }
+  cudaSetDevice(c->impl.device);
+  try {
+    return renderBatch(&c->impl, jobs, total);
   } catch (const std::bad_alloc&) {
     return setError(&c->impl, UBR_OUT_OF_MEMORY, "host allocation failed");
   } catch (...) {

@@ -58,6 +58,36 @@ struct Bufs {
   unsigned long long* cursor;  // next ray of the persistent occlusion kernel
 };
 
+// Per-frame record of a batched launch (device array): the frame's
+// parameters and scene, and where its pixels start in the batch's global
+// hi-res pixel and output pixel spaces.
+struct FrameDesc {
+  Params p;
+  DScene s;
+  uint32_t pixOff;
+  uint32_t outOff;
+};
+
+struct Batch {
+  const FrameDesc* frames = nullptr;
+  const uint32_t* pixOffs = nullptr;  // frames' pixOff, ascending
+  const uint32_t* outOffs = nullptr;  // frames' outOff, ascending
+  int nFrames = 0;
+  uint32_t R = 0;         // AO/shadow-ray stride per hit (max over frames)
+  uint32_t aoStride = 0;  // enhanced-AO t stride per hit (max over frames)
+};
+
+// Frame owning global index g in an ascending offset table.
+UBR_D int frameOf(const uint32_t* offs, int n, uint32_t g) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&offs[mid]) <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 UBR_D f3 ld3(const float4 v) { return f3{v.x, v.y, v.z}; }
 
 UBR_D f3 safeInv(f3 d) {
@@ -109,7 +139,7 @@ constexpr int kMaskMesh = 1 << kMesh, kMaskSphere = 1 << kSphere, kMaskRound = 1
               kMaskCone = 1 << kCone, kMaskAll = 15;
 
 template <int KM, bool ATTR = true>
-UBR_D bool testLeaf(const DScene& s, int slot, const Ray& r, const TriPre& pre, float tnear,
+UBR_D bool testLeaf(const TravScene& s, int slot, const Ray& r, const TriPre& pre, float tnear,
                     float tmax, Hit& h, uint32_t& ref) {
   ref = __ldg(&s.leafRef[slot]);
   const int kind = refKind(ref);
@@ -193,7 +223,7 @@ UBR_D void travInit(const Ray& r, TravState& st, Hit& best) {
 // next node.  Returns true when the ray is finished (any-hit found, stack
 // empty, or the step bound reached).
 template <bool COUNT, int KM, bool ALWAYS_ANY = false>
-UBR_D bool travStep(const DScene& s, const Ray& r, const f3& inv, const TriPre& pre, TravState& st, Hit& best,
+UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPre& pre, TravState& st, Hit& best,
                     uint32_t& overflow, Count* cnt, bool any) {
   if (ALWAYS_ANY) any = true;
   if (++st.steps > s.primCount + 16u) {  // each node at most once per ray in a valid tree
@@ -296,7 +326,8 @@ UBR_D bool travStep(const DScene& s, const Ray& r, const f3& inv, const TriPre& 
 
 // Whole traversal of one ray (one thread per ray).
 template <bool COUNT = false, int KM = kMaskAll, bool ALWAYS_ANY = false>
-__device__ bool traverse(const DScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt, const bool any) {
+__device__ bool traverse(const TravScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt,
+                         const bool any) {
   best.ref = kInvalid;
   if (s.primCount == 0) return false;
   const f3 inv = safeInv(r.dir);
@@ -470,22 +501,27 @@ UBR_D void warpCount(unsigned long long* ctr, uint32_t v) {
 // ---------------------------------------------------------------------------
 // kernels
 
-template <bool COUNT, int KM>
-__global__ void __launch_bounds__(128, 8) k_trace_closest(Params p, DScene s, Bufs b, int layer, uint32_t n,
-                                                       const uint32_t* queue) {
+template <bool COUNT, int KM, bool BATCH>
+__global__ void __launch_bounds__(128, 8) k_trace_closest(Params p1, DScene s1, Batch bt, Bufs b, int layer,
+                                                       uint32_t n, const uint32_t* queue) {
   Count cnt;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t traced = 0, ovf = 0;
   if (i < n) {
-    const uint32_t pix = layer == 0 ? i : queue[i];
+    const uint32_t gpix = layer == 0 ? i : queue[i];
+    const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
+    const Params& p = BATCH ? bt.frames[f].p : p1;
+    const DScene& s = BATCH ? bt.frames[f].s : s1;
+    const uint32_t pix = gpix - (BATCH ? bt.frames[f].pixOff : 0u);
     const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
     f3 org, rd;
     primaryRay(p, px, py, org, rd);
     float ctn, ctf;
     clipRange(p, rd, ctn, ctf);
-    Ray r{org, rd, layer == 0 ? ctn : b.tnear[pix], ctf};
+    Ray r{org, rd, layer == 0 ? ctn : b.tnear[gpix], ctf};
     Hit h;
-    traverse<COUNT, KM>(s, r, h, ovf, &cnt, false);
+    const TravScene ts = travOf(s);
+    traverse<COUNT, KM>(ts, r, h, ovf, &cnt, false);
     traced = 1;
     b.hitA[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.ref));
     b.hitB[i] = make_float4(h.Ng.x, h.Ng.y, h.Ng.z, 0.0f);
@@ -498,16 +534,21 @@ __global__ void __launch_bounds__(128, 8) k_trace_closest(Params p, DScene s, Bu
   }
 }
 
-__global__ void __launch_bounds__(128) k_surface(Params p, DScene s, Bufs b, int layer, uint32_t n,
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_surface(Params p1, DScene s1, Batch bt, Bufs b, int layer, uint32_t n,
                                                  const uint32_t* queue) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool cast = false;
   if (i < n) {
-    const uint32_t pix = layer == 0 ? i : queue[i];
+    const uint32_t gpix = layer == 0 ? i : queue[i];
+    const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
+    const Params& p = BATCH ? bt.frames[f].p : p1;
+    const DScene& s = BATCH ? bt.frames[f].s : s1;
+    const uint32_t pix = gpix - (BATCH ? bt.frames[f].pixOff : 0u);
     const float4 ha = b.hitA[i];
     const uint32_t ref = __float_as_uint(ha.w);
     if (ref == kInvalid) {
-      b.surfC[i] = make_uint2(pix, 0u);
+      b.surfC[i] = make_uint2(gpix, 0u);
     } else {
       const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
       f3 org, rd;
@@ -520,8 +561,9 @@ __global__ void __launch_bounds__(128) k_surface(Params p, DScene s, Bufs b, int
       const f3 O = sf.P + ng * sf.secEps;
       b.surfA[i] = make_float4(O.x, O.y, O.z, sf.secEps);
       b.surfB[i] = make_float4(sf.N.x, sf.N.y, sf.N.z, 0.0f);
-      const uint32_t flags = 1u | (sf.aoOn ? 2u : 0u) | (sf.shOn ? 4u : 0u);
-      b.surfC[i] = make_uint2(pix, flags);
+      // flags: 1 hit, 2 casts AO, 4 casts shadows; bits 8.. the frame index
+      const uint32_t flags = 1u | (sf.aoOn ? 2u : 0u) | (sf.shOn ? 4u : 0u) | (uint32_t(f) << 8);
+      b.surfC[i] = make_uint2(gpix, flags);
       cast = (flags & 6u) != 0u;
     }
   }
@@ -541,15 +583,14 @@ struct OccRay {
   bool ao;       // this is an AO ray of an AO-receiving hit
 };
 
-UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, int j) {
+UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, uint32_t pix, uint32_t flags, int j) {
   OccRay o;
   o.trace = false;
   o.anyHit = true;
   o.grazing = false;
   o.ao = false;
-  const uint2 sc = b.surfC[slot];
-  const uint32_t flags = sc.y;
-  const int px = int(sc.x % uint32_t(p.W)), py = int(sc.x / uint32_t(p.W));
+  const LightD* lights = b.lights + p.lightOff;
+  const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
   const float4 sa = b.surfA[slot], sb = b.surfB[slot];
   const f3 N = ld3(sb);
   f3 dir{0.0f, 0.0f, 0.0f};
@@ -567,8 +608,8 @@ UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, int j) 
   } else if (flags & 4u) {
     const int k = j - p.aoSamples;
     int l = 0;
-    while (l + 1 < p.nLights && b.lights[l + 1].rayOffset <= k) ++l;
-    const LightD L = b.lights[l];
+    while (l + 1 < p.nLights && lights[l + 1].rayOffset <= k) ++l;
+    const LightD L = lights[l];
     if (dot(N, L.L) > 0.0f) {
       dir = L.L;
       if (L.soft) {
@@ -576,7 +617,7 @@ UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, int j) 
         // (shading.hpp:100, secondary_rays.hpp:128-131)
         int consumed = 0;
         for (int q = 0; q < l; ++q) {
-          const LightD Q = b.lights[q];
+          const LightD Q = lights[q];
           if (Q.soft && dot(N, Q.L) > 0.0f) consumed += Q.samples;
         }
         uint32_t s0 = uint32_t(px), s1 = uint32_t(py);
@@ -591,34 +632,42 @@ UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, int j) 
   return o;
 }
 
-UBR_D void occlusionWrite(const Params& p, const Bufs& b, uint32_t slot, int j, const OccRay& o, bool hit,
-                          float t) {
+UBR_D void occlusionWrite(const Params& p, const Bufs& b, uint64_t R, uint64_t aoStride, uint32_t slot, int j,
+                          const OccRay& o, bool hit, float t) {
   const uint8_t res = o.grazing ? 1 : (hit ? 1 : 0);
-  if (o.ao && p.aoEnhanced) b.aoT[uint64_t(slot) * p.aoSamples + j] = o.grazing ? -1.0f : (hit ? t : kInfF);
-  b.occ[uint64_t(slot) * uint64_t(p.raysPerHit) + j] = res;
+  if (o.ao && p.aoEnhanced) b.aoT[uint64_t(slot) * aoStride + j] = o.grazing ? -1.0f : (hit ? t : kInfF);
+  b.occ[uint64_t(slot) * R + j] = res;
 }
 
 // One thread per AO / shadow ray.
-template <bool COUNT, int KM>
-__global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p, DScene s, Bufs b, uint32_t n) {
+template <bool COUNT, int KM, bool BATCH>
+__global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p1, DScene s1, Batch bt, Bufs b, uint32_t n) {
   Count cnt;
   const uint64_t tid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const uint64_t R = uint64_t(p.raysPerHit);
+  const uint64_t R = BATCH ? uint64_t(bt.R) : uint64_t(p1.raysPerHit);
+  const uint64_t aoStride = BATCH ? uint64_t(bt.aoStride) : uint64_t(p1.aoSamples);
   uint32_t traced = 0, ovf = 0;
   const uint32_t nq = *(volatile const uint32_t*)(b.counter + 1);
   if (tid < uint64_t(nq) * R) {
     const uint32_t slot = b.occQueue[uint32_t(tid / R)];
     const int j = int(tid % R);
-    const OccRay o = occlusionRay(p, b, slot, j);
-    bool hit = false;
-    Hit h;
-    h.t = kInfF;
-    if (o.trace) {
-      hit = p.aoEnhanced ? traverse<COUNT, KM, false>(s, o.r, h, ovf, &cnt, o.anyHit)
-                         : traverse<COUNT, KM, true>(s, o.r, h, ovf, &cnt, true);
-      traced = 1;
+    const uint2 sc = b.surfC[slot];
+    const int f = BATCH ? int(sc.y >> 8) : 0;
+    const Params& p = BATCH ? bt.frames[f].p : p1;
+    const DScene& s = BATCH ? bt.frames[f].s : s1;
+    if (j < p.raysPerHit) {
+      const OccRay o = occlusionRay(p, b, slot, sc.x - (BATCH ? bt.frames[f].pixOff : 0u), sc.y, j);
+      bool hit = false;
+      Hit h;
+      h.t = kInfF;
+      if (o.trace) {
+        const TravScene ts = travOf(s);
+        hit = p.aoEnhanced ? traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit)
+                           : traverse<COUNT, KM, true>(ts, o.r, h, ovf, &cnt, true);
+        traced = 1;
+      }
+      occlusionWrite(p, b, R, aoStride, slot, j, o, hit, h.t);
     }
-    occlusionWrite(p, b, slot, j, o, hit, h.t);
   }
   warpCount(&b.stats[1], traced);
   warpCount(&b.stats[3], ovf);
@@ -636,11 +685,13 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p, DScene s, 
 // lanes whose rays end early do not wait for the warp's longest ray.
 constexpr int kRefill = 8;
 
-template <bool COUNT, int KM>
-__global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p, DScene s, Bufs b) {
+template <bool COUNT, int KM, bool BATCH>
+__global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p1, DScene s1, Batch bt, Bufs b) {
   Count cnt;
   uint32_t traced = 0, ovf = 0;
-  const uint64_t R = uint64_t(p.raysPerHit);
+  const uint64_t R = BATCH ? uint64_t(bt.R) : uint64_t(p1.raysPerHit);
+  const uint64_t aoStride = BATCH ? uint64_t(bt.aoStride) : uint64_t(p1.aoSamples);
+  int f = 0;
   const uint64_t total = uint64_t(*(volatile const uint32_t*)(b.counter + 1)) * R;
   const int lane = threadIdx.x & 31;
   bool active = false, exhausted = total == 0;
@@ -651,6 +702,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p,
   TriPre pre;
   TravState st;
   Hit best;
+  TravScene ts = travOf(s1);
   for (;;) {
     const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active);
     if (!exhausted && (__popc(idle) >= kRefill || idle == 0xFFFFFFFFu)) {
@@ -663,15 +715,23 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p,
         if (rid < total) {
           slot = b.occQueue[uint32_t(rid / R)];
           j = int(rid % R);
-          o = occlusionRay(p, b, slot, j);
-          if (o.trace && s.primCount > 0) {
+          const uint2 sc = b.surfC[slot];
+          f = BATCH ? int(sc.y >> 8) : 0;
+          const Params& p = BATCH ? bt.frames[f].p : p1;
+          const DScene& s = BATCH ? bt.frames[f].s : s1;
+          if (j < p.raysPerHit) o = occlusionRay(p, b, slot, sc.x - (BATCH ? bt.frames[f].pixOff : 0u), sc.y, j);
+          else o.trace = o.grazing = o.ao = false;
+          if (j >= p.raysPerHit) {
+            // stride padding of a frame with fewer rays per hit: nothing to do
+          } else if (o.trace && s.primCount > 0) {
+            ts = travOf(s);
             inv = safeInv(o.r.dir);
             if (KM & kMaskMesh) pre = triPre(o.r.dir);
             travInit(o.r, st, best);
             active = true;
             ++traced;
           } else {
-            occlusionWrite(p, b, slot, j, o, false, kInfF);
+            occlusionWrite(p, b, R, aoStride, slot, j, o, false, kInfF);
           }
         }
       }
@@ -681,9 +741,12 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p,
       if (exhausted) break;
       continue;
     }
-    if (active && travStep<COUNT, KM>(s, o.r, inv, pre, st, best, ovf, &cnt, o.anyHit)) {
-      occlusionWrite(p, b, slot, j, o, best.ref != kInvalid, best.t);
-      active = false;
+    if (active) {
+      const Params& p = BATCH ? bt.frames[f].p : p1;
+      if (travStep<COUNT, KM>(ts, o.r, inv, pre, st, best, ovf, &cnt, o.anyHit)) {
+        occlusionWrite(p, b, R, aoStride, slot, j, o, best.ref != kInvalid, best.t);
+        active = false;
+      }
     }
   }
   warpCount(&b.stats[1], traced);
@@ -709,15 +772,23 @@ UBR_D float aoMultibounce(float ao, float albedo) {
   return fmaxf(ao, ((ao * a + bb) * ao + c) * ao);
 }
 
-__global__ void __launch_bounds__(128) k_shade(Params p, DScene s, Bufs b, int layer, uint32_t n,
+template <bool BATCH>
+__global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, Bufs b, int layer, uint32_t n,
                                                const uint32_t* queue, uint32_t* outQueue) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool push = false;
-  uint32_t pix = 0, capped = 0;
+  uint32_t gpix = 0, capped = 0;
   if (i < n) {
-    pix = layer == 0 ? i : queue[i];
+    gpix = layer == 0 ? i : queue[i];
+    const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
+    const Params& p = BATCH ? bt.frames[f].p : p1;
+    const DScene& s = BATCH ? bt.frames[f].s : s1;
+    const LightD* lights = b.lights + p.lightOff;
+    const uint64_t R = BATCH ? uint64_t(bt.R) : uint64_t(p.raysPerHit);
+    const uint64_t aoStride = BATCH ? uint64_t(bt.aoStride) : uint64_t(p.aoSamples);
+    const uint32_t pix = gpix - (BATCH ? bt.frames[f].pixOff : 0u);
     const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
-    float4 acc = layer == 0 ? make_float4(0, 0, 0, 0) : b.accum[pix];
+    float4 acc = layer == 0 ? make_float4(0, 0, 0, 0) : b.accum[gpix];
     f3 base = p.bg;
     float baseCov = p.transparentBg ? 0.0f : 1.0f;
     bool done = true;
@@ -734,7 +805,7 @@ __global__ void __launch_bounds__(128) k_shade(Params p, DScene s, Bufs b, int l
       f3 aoFactor{1.0f, 1.0f, 1.0f};
       f3 ambLight = p.ambLight;
       float diffuseAo = 1.0f;
-      const uint64_t rb = uint64_t(i) * uint64_t(p.raysPerHit);
+      const uint64_t rb = uint64_t(i) * R;
       if (sf.aoOn) {
         float openness;
         f3 bent = sf.N;
@@ -767,7 +838,7 @@ __global__ void __launch_bounds__(128) k_shade(Params p, DScene s, Bufs b, int l
               weightedObs += 1.0f;
               continue;
             }
-            const float th = b.aoT[uint64_t(i) * p.aoSamples + k];
+            const float th = b.aoT[uint64_t(i) * aoStride + k];
             float perSample = 0.0f;
             for (int q = 0; q < K; ++q) {
               if (th < radius[q]) {
@@ -813,7 +884,7 @@ __global__ void __launch_bounds__(128) k_shade(Params p, DScene s, Bufs b, int l
              m.emission * C.z + aoFactor.z * m.ambient * C.z * ambLight.z};
       const float ex = blinnExp(m.roughness);
       for (int l = 0; l < p.nLights; ++l) {
-        const LightD L = b.lights[l];
+        const LightD L = lights[l];
         const float ndl = dot(N, L.L);
         if (ndl <= 0.0f) continue;
         float shadowFactor = 1.0f;
@@ -874,11 +945,11 @@ __global__ void __launch_bounds__(128) k_shade(Params p, DScene s, Bufs b, int l
         out.z += m.reflection * p.bg.z;
       }
       // --- first-hit capture + compositing (transparency.hpp:394-467) ---
-      if (b.depth[pix] == 0.0f) {
-        b.depth[pix] = t;
-        b.viewZ[pix] = t * dot(rd, p.camDir);
-        b.hitGeom[pix] = s.geomID[sf.kind];
-        b.hitPrim[pix] = sf.prim;
+      if (b.depth[gpix] == 0.0f) {
+        b.depth[gpix] = t;
+        b.viewZ[gpix] = t * dot(rd, p.camDir);
+        b.hitGeom[gpix] = s.geomID[sf.kind];
+        b.hitPrim[gpix] = sf.prim;
       }
       const float kOpaque = 1.0f - 1e-4f;
       if (!p.transparency || sf.opacity >= kOpaque) {
@@ -899,8 +970,8 @@ __global__ void __launch_bounds__(128) k_shade(Params p, DScene s, Bufs b, int l
           if (layer == p.maxIters - 1) {
             capped = 1;
           } else {
-            b.tnear[pix] = tn;
-            b.accum[pix] = acc;
+            b.tnear[gpix] = tn;
+            b.accum[gpix] = acc;
             done = false;
             push = true;
           }
@@ -911,13 +982,13 @@ __global__ void __launch_bounds__(128) k_shade(Params p, DScene s, Bufs b, int l
       const float floorW = (1.0f - acc.w) * baseCov;
       float outA = acc.w + floorW;
       outA = fminf(1.0f, fmaxf(0.0f, outA));
-      b.colorHi[pix] = make_float4(acc.x + floorW * base.x, acc.y + floorW * base.y,
-                                   acc.z + floorW * base.z, outA);
+      b.colorHi[gpix] = make_float4(acc.x + floorW * base.x, acc.y + floorW * base.y,
+                                    acc.z + floorW * base.z, outA);
     }
   }
   int off;
   const int qb = warpPushBase(push, b.counter, off);
-  if (push) outQueue[qb + off] = pix;
+  if (push) outQueue[qb + off] = gpix;
   warpCount(&b.stats[2], capped);
 }
 
@@ -925,13 +996,19 @@ __global__ void __launch_bounds__(128) k_shade(Params p, DScene s, Bufs b, int l
 // average with the non-finite guard (image_ops.cpp:9-35; only when ss > 1,
 // as renderFrame skips the downsample at ss == 1), assumed gamma
 // (image_ops.cpp:37-46).
-__global__ void k_post(Params p, const float4* colorHi, const float* viewZ, float4* out) {
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= p.outW * p.outH) return;
+template <bool BATCH>
+__global__ void k_post(Params p1, Batch bt, uint32_t nOut, const float4* colorHi, const float* viewZ,
+                       float4* out) {
+  const uint32_t go = blockIdx.x * blockDim.x + threadIdx.x;
+  if (go >= nOut) return;
+  const int f = BATCH ? frameOf(bt.outOffs, bt.nFrames, go) : 0;
+  const Params& p = BATCH ? bt.frames[f].p : p1;
+  const size_t pixOff = BATCH ? bt.frames[f].pixOff : 0u;
+  const int o = int(go - (BATCH ? bt.frames[f].outOff : 0u));
   const int ox = o % p.outW, oy = o / p.outW;
   const int ss = p.ss;
   auto fogged = [&](int hx, int hy) {
-    const size_t hp = size_t(hy) * p.W + hx;
+    const size_t hp = pixOff + size_t(hy) * p.W + hx;
     float4 c = colorHi[hp];
     if (p.fogOn) {
       const float z = viewZ[hp];
@@ -978,7 +1055,7 @@ __global__ void k_post(Params p, const float4* colorHi, const float* viewZ, floa
     r.y = r.y > 0.0f ? powf(r.y, g) : 0.0f;
     r.z = r.z > 0.0f ? powf(r.z, g) : 0.0f;
   }
-  out[o] = r;
+  out[go] = r;
 }
 
 __global__ void k_init_pixels(uint32_t npix, float* depth, float* viewZ, uint32_t* hg, uint32_t* hp) {
@@ -1117,7 +1194,7 @@ __global__ void k_occluded_segments(DScene s, const float* segs, uint64_t n, flo
       if (tnear < tfar) {
         Ray r{a, dir, tnear, tfar};
         Hit h;
-        res = traverse<false, kMaskAll, true>(s, r, h, ovf, nullptr, true) ? 1 : 0;
+        res = traverse<false, kMaskAll, true>(travOf(s), r, h, ovf, nullptr, true) ? 1 : 0;
       }
     }
     out[i] = res;
@@ -1125,11 +1202,15 @@ __global__ void k_occluded_segments(DScene s, const float* segs, uint64_t n, flo
   warpCount(&stats[3], ovf);
 }
 
-// Kind mask of a scene, rounded to one of the instantiated variants.
-int kindMask(const Scene& sc) {
+// Kind bits of a scene, and the instantiated variant that covers a set of kinds.
+int kindMaskBits(const Scene& sc) {
   int m = 0;
   for (int k = 0; k < 4; ++k)
     if (sc.primCount[k]) m |= 1 << k;
+  return m;
+}
+
+int roundKindMask(int m) {
   switch (m) {
     case kMaskMesh:
     case kMaskSphere:
@@ -1141,39 +1222,42 @@ int kindMask(const Scene& sc) {
   }
 }
 
-#define UBR_KM_DISPATCH(KERNEL, km, count, grid, tb, stream, ...)                                \
-  do {                                                                                           \
-    switch (km) {                                                                                \
-      case kMaskMesh:                                                                            \
-        if (count) KERNEL<true, kMaskMesh><<<grid, tb, 0, stream>>>(__VA_ARGS__);               \
-        else KERNEL<false, kMaskMesh><<<grid, tb, 0, stream>>>(__VA_ARGS__);                    \
-        break;                                                                                   \
-      case kMaskSphere:                                                                          \
-        if (count) KERNEL<true, kMaskSphere><<<grid, tb, 0, stream>>>(__VA_ARGS__);             \
-        else KERNEL<false, kMaskSphere><<<grid, tb, 0, stream>>>(__VA_ARGS__);                  \
-        break;                                                                                   \
-      case kMaskMesh | kMaskSphere:                                                              \
-        if (count) KERNEL<true, kMaskMesh | kMaskSphere><<<grid, tb, 0, stream>>>(__VA_ARGS__); \
-        else KERNEL<false, kMaskMesh | kMaskSphere><<<grid, tb, 0, stream>>>(__VA_ARGS__);      \
-        break;                                                                                   \
-      case kMaskSphere | kMaskCone:                                                              \
-        if (count) KERNEL<true, kMaskSphere | kMaskCone><<<grid, tb, 0, stream>>>(__VA_ARGS__); \
-        else KERNEL<false, kMaskSphere | kMaskCone><<<grid, tb, 0, stream>>>(__VA_ARGS__);      \
-        break;                                                                                   \
-      default:                                                                                   \
-        if (count) KERNEL<true, kMaskAll><<<grid, tb, 0, stream>>>(__VA_ARGS__);                \
-        else KERNEL<false, kMaskAll><<<grid, tb, 0, stream>>>(__VA_ARGS__);                     \
-    }                                                                                            \
+int kindMask(const Scene& sc) { return roundKindMask(kindMaskBits(sc)); }
+
+#define UBR_LAUNCH3(KERNEL, KM, count, batch, grid, tb, stream, ...)                  \
+  do {                                                                                \
+    if (count) {                                                                      \
+      if (batch) KERNEL<true, KM, true><<<grid, tb, 0, stream>>>(__VA_ARGS__);        \
+      else KERNEL<true, KM, false><<<grid, tb, 0, stream>>>(__VA_ARGS__);             \
+    } else {                                                                          \
+      if (batch) KERNEL<false, KM, true><<<grid, tb, 0, stream>>>(__VA_ARGS__);       \
+      else KERNEL<false, KM, false><<<grid, tb, 0, stream>>>(__VA_ARGS__);            \
+    }                                                                                 \
   } while (0)
 
-void launchClosest(int km, bool count, uint32_t grid, int tb, cudaStream_t st, const Params& p, const DScene& s,
-                   const Bufs& b, int layer, uint32_t n, const uint32_t* queue) {
-  UBR_KM_DISPATCH(k_trace_closest, km, count, grid, tb, st, p, s, b, layer, n, queue);
+#define UBR_KM_DISPATCH(KERNEL, km, count, batch, grid, tb, stream, ...)                                     \
+  do {                                                                                                       \
+    switch (km) {                                                                                            \
+      case kMaskMesh: UBR_LAUNCH3(KERNEL, kMaskMesh, count, batch, grid, tb, stream, __VA_ARGS__); break;  \
+      case kMaskSphere: UBR_LAUNCH3(KERNEL, kMaskSphere, count, batch, grid, tb, stream, __VA_ARGS__); break; \
+      case kMaskMesh | kMaskSphere:                                                                          \
+        UBR_LAUNCH3(KERNEL, kMaskMesh | kMaskSphere, count, batch, grid, tb, stream, __VA_ARGS__);           \
+        break;                                                                                               \
+      case kMaskSphere | kMaskCone:                                                                          \
+        UBR_LAUNCH3(KERNEL, kMaskSphere | kMaskCone, count, batch, grid, tb, stream, __VA_ARGS__);           \
+        break;                                                                                               \
+      default: UBR_LAUNCH3(KERNEL, kMaskAll, count, batch, grid, tb, stream, __VA_ARGS__);                   \
+    }                                                                                                        \
+  } while (0)
+
+void launchClosest(int km, bool count, bool batch, uint32_t grid, int tb, cudaStream_t st, const Params& p,
+                   const DScene& s, const Batch& bt, const Bufs& b, int layer, uint32_t n, const uint32_t* queue) {
+  UBR_KM_DISPATCH(k_trace_closest, km, count, batch, grid, tb, st, p, s, bt, b, layer, n, queue);
 }
 
-void launchOcclusion(int km, bool count, uint32_t grid, int tb, cudaStream_t st, const Params& p, const DScene& s,
-                     const Bufs& b, uint32_t n) {
-  UBR_KM_DISPATCH(k_trace_occlusion, km, count, grid, tb, st, p, s, b, n);
+void launchOcclusion(int km, bool count, bool batch, uint32_t grid, int tb, cudaStream_t st, const Params& p,
+                     const DScene& s, const Batch& bt, const Bufs& b, uint32_t n) {
+  UBR_KM_DISPATCH(k_trace_occlusion, km, count, batch, grid, tb, st, p, s, bt, b, n);
 }
 
 // Resident grid of the persistent occlusion kernel: SMs x resident blocks.
@@ -1182,15 +1266,16 @@ uint32_t persistentGrid(int device) {
   if (device >= 0 && device < 64 && cached[device]) return uint32_t(cached[device]);
   int sms = 0, perSm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_trace_occlusion_persistent<false, kMaskAll>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_trace_occlusion_persistent<false, kMaskAll, false>, 128,
+                                                0);
   const int g = std::max(1, sms) * std::max(1, perSm);
   if (device >= 0 && device < 64) cached[device] = g;
   return uint32_t(g);
 }
 
-void launchOcclusionPersistent(int km, bool count, uint32_t grid, int tb, cudaStream_t st, const Params& p,
-                               const DScene& s, const Bufs& b) {
-  UBR_KM_DISPATCH(k_trace_occlusion_persistent, km, count, grid, tb, st, p, s, b);
+void launchOcclusionPersistent(int km, bool count, bool batch, uint32_t grid, int tb, cudaStream_t st,
+                               const Params& p, const DScene& s, const Batch& bt, const Bufs& b) {
+  UBR_KM_DISPATCH(k_trace_occlusion_persistent, km, count, batch, grid, tb, st, p, s, bt, b);
 }
 
 template <class T>
@@ -1202,16 +1287,64 @@ T* scratchT(Context* c, int slot, size_t count, ubr_status& st) {
 
 }  // namespace
 
-ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ubr_frame& fr,
-                       const volatile int32_t* cancel, uint64_t* progress) {
-  Params p;
+// One frame of a (possibly single-frame) launch.
+struct Job {
+  const Scene* scene;
+  const ubr_render_desc* desc;
+  ubr_frame* frame;
+};
+
+// Run N frames through one set of launches over a global pixel / ray space
+// (N = 1 is the per-frame path, BATCH = false, parameters in the constant
+// bank).  When every frame is one layer deep (opaque scene or transparency
+// off) and nothing is profiled, the device work is a fixed sequence: it is
+// captured once into a CUDA graph and replayed (re-captured and updated in
+// place when the parameters change).
+ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total, const volatile int32_t* cancel,
+                     uint64_t* progress) {
+  const size_t nf = jobs.size();
+  if (nf == 0) return UBR_OK;
+  const bool batch = nf > 1;
+  std::vector<FrameDesc> fds(nf);
   std::vector<LightD> lights;
-  ubr_status st = makeParams(c, d, p, lights);
-  if (st != UBR_OK) return st;
-  const uint32_t npix = uint32_t(p.W) * uint32_t(p.H);
-  const uint32_t nout = uint32_t(p.outW) * uint32_t(p.outH);
+  std::vector<uint32_t> pixOffs(nf), outOffs(nf);
+  uint64_t npix64 = 0, nout64 = 0;
+  uint32_t R = 0, aoStride = 0;
+  int km = 0, maxIters = 1;
+  bool secondary = false, enhanced = false, singleLayer = true;
+  for (size_t f = 0; f < nf; ++f) {
+    std::vector<LightD> fl;
+    Params& p = fds[f].p;
+    ubr_status st = makeParams(c, *jobs[f].desc, p, fl);
+    if (st != UBR_OK) return st;
+    p.lightOff = int(lights.size());
+    lights.insert(lights.end(), fl.begin(), fl.end());
+    fds[f].s = jobs[f].scene->view;
+    fds[f].pixOff = uint32_t(npix64);
+    fds[f].outOff = uint32_t(nout64);
+    pixOffs[f] = fds[f].pixOff;
+    outOffs[f] = fds[f].outOff;
+    npix64 += uint64_t(p.W) * uint64_t(p.H);
+    nout64 += uint64_t(p.outW) * uint64_t(p.outH);
+    R = std::max(R, uint32_t(p.raysPerHit));
+    if (p.aoEnhanced && p.aoSamples > 0) {
+      enhanced = true;
+      aoStride = std::max(aoStride, uint32_t(p.aoSamples));
+    }
+    secondary = secondary || p.raysPerHit > 0;
+    if (!(p.maxIters == 1 || jobs[f].scene->opaque)) singleLayer = false;
+    maxIters = std::max(maxIters, jobs[f].scene->opaque ? 1 : p.maxIters);
+    km |= kindMaskBits(*jobs[f].scene);
+  }
+  if (npix64 >= (1ull << 31) || nout64 >= (1ull << 31))
+    return setError(c, UBR_INVALID_ARGUMENT, "render: more than 2^31 pixels in one launch");
+  if (lights.size() > size_t(kMaxLights) * nf) return setError(c, UBR_INVALID_ARGUMENT, "too many lights");
+  km = roundKindMask(km);
+  const uint32_t npix = uint32_t(npix64), nout = uint32_t(nout64);
+  const Params& p1 = fds[0].p;
+  const DScene& s1 = fds[0].s;
+  ubr_status st = UBR_OK;
   Bufs b{};
-  // frame scratch slots 16..
   b.accum = scratchT<float4>(c, 16, npix, st);
   b.tnear = scratchT<float>(c, 17, npix, st);
   b.colorHi = scratchT<float4>(c, 18, npix, st);
@@ -1223,31 +1356,45 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
   b.hitB = scratchT<float4>(c, 24, npix, st);
   uint32_t* q0 = scratchT<uint32_t>(c, 25, npix, st);
   uint32_t* q1 = scratchT<uint32_t>(c, 26, npix, st);
-  const bool secondary = p.raysPerHit > 0;
   if (secondary) {
     b.surfA = scratchT<float4>(c, 27, npix, st);
     b.surfB = scratchT<float4>(c, 28, npix, st);
     b.surfC = scratchT<uint2>(c, 29, npix, st);
     b.occQueue = scratchT<uint32_t>(c, 36, npix, st);
     b.cursor = scratchT<unsigned long long>(c, 37, 1, st);
-    b.occ = scratchT<uint8_t>(c, 30, size_t(npix) * p.raysPerHit, st);
-    if (p.aoEnhanced && p.aoSamples > 0) b.aoT = scratchT<float>(c, 31, size_t(npix) * p.aoSamples, st);
+    b.occ = scratchT<uint8_t>(c, 30, size_t(npix) * R, st);
+    if (enhanced) b.aoT = scratchT<float>(c, 31, size_t(npix) * aoStride, st);
   }
   LightD* dl = scratchT<LightD>(c, 32, lights.size() + 1, st);
   b.stats = scratchT<unsigned long long>(c, 33, 8, st);
   b.counter = scratchT<uint32_t>(c, 34, 4, st);
   float4* outColor = scratchT<float4>(c, 35, nout, st);
+  Batch bt{};
+  if (batch) {
+    FrameDesc* dfd = scratchT<FrameDesc>(c, 38, nf, st);
+    uint32_t* doffs = scratchT<uint32_t>(c, 39, 2 * nf, st);
+    if (st != UBR_OK) return st;
+    UBR_CUDA(c, cudaMemcpyAsync(dfd, fds.data(), nf * sizeof(FrameDesc), cudaMemcpyHostToDevice, c->stream));
+    UBR_CUDA(c, cudaMemcpyAsync(doffs, pixOffs.data(), nf * 4, cudaMemcpyHostToDevice, c->stream));
+    UBR_CUDA(c, cudaMemcpyAsync(doffs + nf, outOffs.data(), nf * 4, cudaMemcpyHostToDevice, c->stream));
+    bt.frames = dfd;
+    bt.pixOffs = doffs;
+    bt.outOffs = doffs + nf;
+    bt.nFrames = int(nf);
+    bt.R = R;
+    bt.aoStride = aoStride;
+  }
   if (st != UBR_OK) return st;
   b.lights = dl;
   cudaStream_t s = c->stream;
   uint32_t kernels = 0;
-  const bool prof = (fr.flags & UBR_FRAME_PROFILE) != 0;
-  const int km = kindMask(*sc);
-  const bool count = (fr.flags & UBR_FRAME_COUNT) != 0;
+  const uint32_t flags = total ? total->flags : 0u;
+  const bool prof = (flags & UBR_FRAME_PROFILE) != 0;
+  const bool count = (flags & UBR_FRAME_COUNT) != 0;
   // phase timing: pairs of events per launch, summed per phase after the sync
   std::vector<std::pair<int, int>> marks;  // (phase, event index of the start)
-  auto mark = [&](int phase, bool start) -> ubr_status {
-    if (!prof) return UBR_OK;
+  auto mark = [&](int phase, bool start) {
+    if (!prof) return;
     if (start) {
       const int e = int(marks.size()) * 2;
       if (size_t(e + 2) > c->pev.size()) {
@@ -1260,75 +1407,155 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
     } else {
       cudaEventRecord(c->pev[size_t(marks.back().second + 1)], s);
     }
-    return UBR_OK;
   };
-  cudaEventRecord(c->ev[0], s);
-  if (!lights.empty())
-    UBR_CUDA(c, cudaMemcpyAsync(dl, lights.data(), lights.size() * sizeof(LightD), cudaMemcpyHostToDevice, s));
-  UBR_CUDA(c, cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s));
   const int TB = 128;
-  k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim);
-  ++kernels;
-  cudaEventRecord(c->ev[2], s);
-  uint32_t n = npix;
-  const uint32_t* queue = nullptr;
-  uint32_t* qs[2] = {q0, q1};
-  uint32_t* hostCount = static_cast<uint32_t*>(c->pinned);
-  int layer = 0;
-  bool cancelled = false;
-  for (; layer < p.maxIters && n > 0; ++layer) {
-    uint32_t* outQ = qs[layer & 1];
+  // one transparency round of device work
+  auto round = [&](int layer, uint32_t n, const uint32_t* queue, uint32_t* outQ) -> ubr_status {
     UBR_CUDA(c, cudaMemsetAsync(b.counter, 0, 2 * sizeof(uint32_t), s));
     const uint32_t grid = (n + TB - 1) / TB;
     mark(0, true);
-    launchClosest(km, count, grid, TB, s, p, sc->view, b, layer, n, queue);
+    launchClosest(km, count, batch, grid, TB, s, p1, s1, bt, b, layer, n, queue);
     mark(0, false);
     ++kernels;
     if (secondary) {
       mark(1, true);
-      k_surface<<<grid, TB, 0, s>>>(p, sc->view, b, layer, n, queue);
+      if (batch) k_surface<true><<<grid, TB, 0, s>>>(p1, s1, bt, b, layer, n, queue);
+      else k_surface<false><<<grid, TB, 0, s>>>(p1, s1, bt, b, layer, n, queue);
       mark(1, false);
-      const uint64_t nr = uint64_t(n) * uint64_t(p.raysPerHit);
+      const uint64_t nr = uint64_t(n) * uint64_t(R);
       mark(2, true);
       if (c->traceMode == 1) {
-        launchOcclusion(km, count, uint32_t((nr + TB - 1) / TB), TB, s, p, sc->view, b, n);
+        launchOcclusion(km, count, batch, uint32_t((nr + TB - 1) / TB), TB, s, p1, s1, bt, b, n);
       } else {
         UBR_CUDA(c, cudaMemsetAsync(b.cursor, 0, sizeof(unsigned long long), s));
-        launchOcclusionPersistent(km, count, persistentGrid(c->device), TB, s, p, sc->view, b);
+        launchOcclusionPersistent(km, count, batch, persistentGrid(c->device), TB, s, p1, s1, bt, b);
       }
       mark(2, false);
       kernels += 2;
     }
     mark(3, true);
-    k_shade<<<grid, TB, 0, s>>>(p, sc->view, b, layer, n, queue, outQ);
+    if (batch) k_shade<true><<<grid, TB, 0, s>>>(p1, s1, bt, b, layer, n, queue, outQ);
+    else k_shade<false><<<grid, TB, 0, s>>>(p1, s1, bt, b, layer, n, queue, outQ);
     mark(3, false);
     ++kernels;
     UBR_CUDA(c, cudaGetLastError());
-    if (layer + 1 >= p.maxIters) { ++layer; break; }
-    UBR_CUDA(c, cudaMemcpyAsync(hostCount, b.counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    UBR_CUDA(c, cudaStreamSynchronize(s));
-    n = *hostCount;
-    queue = outQ;
-    if (progress) *progress = uint64_t(layer + 1);
-    if (cancel && *cancel) {
-      cancelled = true;
-      ++layer;
-      break;
+    return UBR_OK;
+  };
+  auto post = [&]() -> ubr_status {
+    mark(4, true);
+    if (batch) k_post<true><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.colorHi, b.viewZ, outColor);
+    else k_post<false><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.colorHi, b.viewZ, outColor);
+    mark(4, false);
+    ++kernels;
+    UBR_CUDA(c, cudaGetLastError());
+    return UBR_OK;
+  };
+  cudaEventRecord(c->ev[0], s);
+  if (!lights.empty())
+    UBR_CUDA(c, cudaMemcpyAsync(dl, lights.data(), lights.size() * sizeof(LightD), cudaMemcpyHostToDevice, s));
+  int layer = 0;
+  bool cancelled = false;
+  const bool useGraph = singleLayer && !prof && !count && c->useGraphs;
+  if (useGraph) {
+    // key: everything the captured launches depend on
+    std::vector<unsigned char> key(sizeof(Params) + sizeof(DScene) + sizeof(Batch) + sizeof(Bufs) + 64);
+    size_t o = 0;
+    auto put = [&](const void* src, size_t n) {
+      std::memcpy(key.data() + o, src, n);
+      o += n;
+    };
+    put(&p1, sizeof(Params));
+    put(&s1, sizeof(DScene));
+    put(&bt, sizeof(Batch));
+    put(&b, sizeof(Bufs));
+    const uint64_t misc[6] = {npix, nout, uint64_t(km), uint64_t(c->traceMode), uint64_t(outColor), R};
+    put(misc, sizeof(misc));
+    key.resize(o);
+    if (!c->graphExec || key != c->graphKey) {
+      UBR_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s);
+      k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim);
+      ubr_status rs = round(0, npix, nullptr, q0);
+      if (rs == UBR_OK) rs = post();
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+      if (rs != UBR_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rs;
+      }
+      if (ce != cudaSuccess) return cudaFail(c, ce, "cudaStreamEndCapture");
+      bool updated = false;
+      if (c->graphExec) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(c->graphExec, graph, &info) == cudaSuccess;
+        if (!updated) {
+          cudaGetLastError();
+          cudaGraphExecDestroy(c->graphExec);
+          c->graphExec = nullptr;
+        }
+      }
+      if (!updated) {
+        const cudaError_t ie = cudaGraphInstantiate(&c->graphExec, graph, 0);
+        if (ie != cudaSuccess) {
+          cudaGraphDestroy(graph);
+          return cudaFail(c, ie, "cudaGraphInstantiate");
+        }
+      }
+      cudaGraphDestroy(graph);
+      c->graphKey = key;
+    } else {
+      kernels = (secondary ? 4u : 2u) + 1u;
     }
+    cudaEventRecord(c->ev[2], s);
+    UBR_CUDA(c, cudaGraphLaunch(c->graphExec, s));
+    cudaEventRecord(c->ev[3], s);
+    layer = 1;
+    ++kernels;  // k_init_pixels
+  } else {
+    UBR_CUDA(c, cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s));
+    k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim);
+    ++kernels;
+    cudaEventRecord(c->ev[2], s);
+    uint32_t n = npix;
+    const uint32_t* queue = nullptr;
+    uint32_t* qs[2] = {q0, q1};
+    uint32_t* hostCount = static_cast<uint32_t*>(c->pinned);
+    for (; layer < maxIters && n > 0; ++layer) {
+      uint32_t* outQ = qs[layer & 1];
+      st = round(layer, n, queue, outQ);
+      if (st != UBR_OK) return st;
+      if (layer + 1 >= maxIters) {
+        ++layer;
+        break;
+      }
+      UBR_CUDA(c, cudaMemcpyAsync(hostCount, b.counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      UBR_CUDA(c, cudaStreamSynchronize(s));
+      n = *hostCount;
+      queue = outQ;
+      if (progress) *progress = uint64_t(layer + 1);
+      if (cancel && *cancel) {
+        cancelled = true;
+        ++layer;
+        break;
+      }
+    }
+    cudaEventRecord(c->ev[3], s);
+    st = post();
+    if (st != UBR_OK) return st;
   }
-  cudaEventRecord(c->ev[3], s);
-  mark(4, true);
-  k_post<<<(nout + 255) / 256, 256, 0, s>>>(p, b.colorHi, b.viewZ, outColor);
-  mark(4, false);
-  ++kernels;
-  UBR_CUDA(c, cudaGetLastError());
   // outputs
-  const cudaMemcpyKind kind = fr.memory == UBR_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  if (fr.color) UBR_CUDA(c, cudaMemcpyAsync(fr.color, outColor, size_t(nout) * 16, kind, s));
-  if (fr.depth) UBR_CUDA(c, cudaMemcpyAsync(fr.depth, b.depth, size_t(npix) * 4, kind, s));
-  if (fr.view_z) UBR_CUDA(c, cudaMemcpyAsync(fr.view_z, b.viewZ, size_t(npix) * 4, kind, s));
-  if (fr.hit_geom) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_geom, b.hitGeom, size_t(npix) * 4, kind, s));
-  if (fr.hit_prim) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_prim, b.hitPrim, size_t(npix) * 4, kind, s));
+  for (size_t f = 0; f < nf; ++f) {
+    ubr_frame& fr = *jobs[f].frame;
+    const Params& p = fds[f].p;
+    const size_t fpix = size_t(p.W) * p.H, fout = size_t(p.outW) * p.outH;
+    const cudaMemcpyKind kind = fr.memory == UBR_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const size_t po = fds[f].pixOff, oo = fds[f].outOff;
+    if (fr.color) UBR_CUDA(c, cudaMemcpyAsync(fr.color, outColor + oo, fout * 16, kind, s));
+    if (fr.depth) UBR_CUDA(c, cudaMemcpyAsync(fr.depth, b.depth + po, fpix * 4, kind, s));
+    if (fr.view_z) UBR_CUDA(c, cudaMemcpyAsync(fr.view_z, b.viewZ + po, fpix * 4, kind, s));
+    if (fr.hit_geom) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_geom, b.hitGeom + po, fpix * 4, kind, s));
+    if (fr.hit_prim) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_prim, b.hitPrim + po, fpix * 4, kind, s));
+  }
   unsigned long long* hs = reinterpret_cast<unsigned long long*>(static_cast<char*>(c->pinned) + 64);
   UBR_CUDA(c, cudaMemcpyAsync(hs, b.stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
   cudaEventRecord(c->ev[1], s);
@@ -1336,29 +1563,42 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
   float msTotal = 0.0f, msLoop = 0.0f;
   cudaEventElapsedTime(&msTotal, c->ev[0], c->ev[1]);
   cudaEventElapsedTime(&msLoop, c->ev[2], c->ev[3]);
-  fr.total_ms = msTotal;
-  fr.render_ms = msLoop;
-  fr.rays_primary = hs[0];
-  fr.rays_occlusion = hs[1];
-  fr.capped_rays = hs[2];
-  fr.stack_overflows = hs[3];
-  fr.layers = uint32_t(layer);
-  fr.kernels = kernels;
-  for (int k = 0; k < 5; ++k) fr.phase_ms[k] = 0.0;
-  for (const auto& m : marks) {
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, c->pev[size_t(m.second)], c->pev[size_t(m.second + 1)]);
-    fr.phase_ms[m.first] += ms;
+  if (total) {
+    ubr_frame& fr = *total;
+    fr.total_ms = msTotal;
+    fr.render_ms = msLoop;
+    fr.rays_primary = hs[0];
+    fr.rays_occlusion = hs[1];
+    fr.capped_rays = hs[2];
+    fr.stack_overflows = hs[3];
+    fr.layers = uint32_t(layer);
+    fr.kernels = kernels;
+    for (int k = 0; k < 5; ++k) fr.phase_ms[k] = 0.0;
+    for (const auto& m : marks) {
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, c->pev[size_t(m.second)], c->pev[size_t(m.second + 1)]);
+      fr.phase_ms[m.first] += ms;
+    }
+    fr.nodes_visited[0] = hs[4];
+    fr.nodes_visited[1] = hs[6];
+    fr.node_bytes[0] = hs[4] * uint64_t(kWideF4 * 16);
+    fr.node_bytes[1] = hs[6] * uint64_t(kWideF4 * 16);
+    fr.prim_bytes[0] = hs[5];
+    fr.prim_bytes[1] = hs[7];
   }
-  fr.nodes_visited[0] = hs[4];
-  fr.nodes_visited[1] = hs[6];
-  fr.node_bytes[0] = hs[4] * uint64_t(kWideF4 * 16);
-  fr.node_bytes[1] = hs[6] * uint64_t(kWideF4 * 16);
-  fr.prim_bytes[0] = hs[5];
-  fr.prim_bytes[1] = hs[7];
   if (cancelled) return setError(c, UBR_CANCELLED, "render cancelled");
   if (hs[3] > 0) return setError(c, UBR_TRAVERSAL_LIMIT, "traversal stack overflow");
   return UBR_OK;
+}
+
+ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ubr_frame& fr,
+                       const volatile int32_t* cancel, uint64_t* progress) {
+  std::vector<Job> jobs{Job{sc, &d, &fr}};
+  return runFrames(c, jobs, &fr, cancel, progress);
+}
+
+ubr_status renderBatch(Context* c, const std::vector<Job>& jobs, ubr_frame* total) {
+  return runFrames(c, jobs, total, nullptr, nullptr);
 }
 
 ubr_status occludedBatch(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps, uint8_t* out,

@@ -53,6 +53,7 @@ struct HostScene {
   std::vector<ubr_material> mats;
   uint32_t geomID[4] = {kInvalid, kInvalid, kInvalid, kInvalid};
   bool principled = false;
+  bool opaque = true;
 };
 
 struct MatKey {
@@ -275,6 +276,16 @@ ubr_status flatten(Context* c, const ubr_scene_desc& d, HostScene& s) {
   if (!s.ccIdx.empty()) s.geomID[kCone] = nextGeom++;
   for (const ubr_material& m : s.mats)
     if (m.model == 1) s.principled = true;
+  // a scene whose every surface is opaque renders in one transparency round
+  const float kOpaque = 1.0f - 1e-4f;
+  for (const float4& c : s.col)
+    if (!(c.w >= kOpaque)) s.opaque = false;
+  for (int k = 1; k < 4; ++k) {
+    for (const float4& c : s.color[k])
+      if (!(c.w >= kOpaque)) s.opaque = false;
+    for (float o1 : s.opacity1[k])
+      if (o1 >= 0.0f && !(o1 >= kOpaque)) s.opaque = false;
+  }
   return UBR_OK;
 }
 
@@ -736,6 +747,7 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   sc->primCount[kCone] = nCc;
   for (int k = 0; k < 4; ++k) v.geomID[k] = hs.geomID[k];
   v.primCount = n;
+  sc->opaque = hs.opaque;
   v.baseTri = hs.baseTri;
   v.meshMat = hs.meshMat;
   cudaEventRecord(c->ev[0], c->stream);

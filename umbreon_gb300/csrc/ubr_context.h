@@ -32,6 +32,9 @@ struct Context {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::vector<cudaEvent_t> pev;  // profiling events, created on first use
   void* pinned = nullptr;    // small pinned host block for counters
+  bool useGraphs = true;     // replay single-layer frames from a CUDA graph
+  cudaGraphExec_t graphExec = nullptr;
+  std::vector<unsigned char> graphKey;  // launch parameters the graph was captured with
 };
 
 struct Scene {
@@ -40,6 +43,7 @@ struct Scene {
   std::vector<DevBuf> bufs;  // owned allocations
   uint64_t primCount[4] = {0, 0, 0, 0};
   uint64_t nodes = 0;
+  bool opaque = true;        // every primitive fully opaque: frames are one layer deep
   uint64_t deviceBytes = 0;
   double buildMs = 0.0;
   float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};

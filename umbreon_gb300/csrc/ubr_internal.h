@@ -124,6 +124,23 @@ struct DScene {
   uint32_t geomID[4] = {kInvalid, kInvalid, kInvalid, kInvalid};
 };
 
+// What traversal reads of a scene, compact enough to live in registers (a
+// batched kernel loads it once per ray instead of re-reading the frame's
+// DScene through global memory inside the traversal loop).
+struct TravScene {
+  const float4* wnodes;
+  const uint32_t* leafRef;
+  const float4* leafGeo;
+  const float4* rcClip;
+  uint32_t primCount;
+  uint32_t geomID[4];
+};
+
+UBR_HD TravScene travOf(const DScene& s) {
+  return TravScene{s.wnodes, s.leafRef, s.leafGeo, s.rcClip, s.primCount,
+                   {s.geomID[0], s.geomID[1], s.geomID[2], s.geomID[3]}};
+}
+
 struct Hit {
   float t;
   uint32_t ref;  // kInvalid on a miss
@@ -440,6 +457,7 @@ struct Params {
   float gamma;
   int raysPerHit;       // AO rays + all lights' shadow rays
   int shadowRays;       // sum of LightD::samples (0 when shadows inactive)
+  int lightOff;         // first light of this frame in the lights array
 };
 
 }  // namespace ubr

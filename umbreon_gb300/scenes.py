@@ -321,3 +321,46 @@ def molecular_surface(seed: int = BASE_SEED + 2, n_atoms: int = 10000, box: floa
     opt = RenderOptions(width=width, height=height, supersample=1, aoSamples=ao_samples, aoDistance=4.0,
                         shadows=True, maxTransparentLayers=layers)
     return sc, opt
+
+
+# --- batched turntable workload ---------------------------------------------
+
+def turntable_batch(seed: int = BASE_SEED + 3, n_items: int = 64, n_scenes: int = 8, ao_samples: int = 8,
+                    resolutions=(256, 512, 1024, 2048), max_spheres: int = 200000, min_spheres: int = 5000):
+    """Workload 3: n_items (scene, turntable angle, resolution) frames.  Scenes
+    hold log-uniform 5k..200k spheres with workload 0's radius distribution in
+    a cube sized to keep workload 0's density (40 A for 2,000 spheres); each
+    item picks one of 36 turntable angles (10 degree steps, perspective
+    fovy 40) and a square resolution from `resolutions`; 8 AO rays, two
+    shadowed lights.  Returns (scenes, items) with items = [(scene index,
+    Scene, RenderOptions)] sharing the geometry of their scene."""
+    us = uniform(seed, n_scenes, 1)[:, 0]
+    counts = np.exp(np.log(min_spheres) + us * (np.log(max_spheres) - np.log(min_spheres))).astype(int)
+    bases = []
+    for i, n in enumerate(counts):
+        box = 40.0 * (n / 2000.0) ** (1.0 / 3.0)
+        cr, col, mats = random_spheres(int(n), box, seed * 131 + i)
+        bases.append((Scene(sphere_center_radius=cr, sphere_color=col, sphere_material=mats), box))
+    ui = uniform(seed + 7, n_items, 3)
+    items = []
+    for k in range(n_items):
+        si = min(int(ui[k, 0] * n_scenes), n_scenes - 1)
+        angle = 10.0 * min(int(ui[k, 1] * 36), 35)
+        res = resolutions[min(int(ui[k, 2] * len(resolutions)), len(resolutions) - 1)]
+        base, box = bases[si]
+        c = np.full(3, 0.5 * box)
+        radius = 0.5 * np.sqrt(3.0) * box
+        dist = radius / math.sin(math.radians(20.0)) * 1.05
+        a = math.radians(angle)
+        pos = c + dist * np.array([math.sin(a), 0.0, math.cos(a)])
+        sc = Scene(sphere_center_radius=base.sphere_center_radius, sphere_color=base.sphere_color,
+                   sphere_material=base.sphere_material)
+        sc.camera = Camera(position=tuple(float(x) for x in pos), direction=tuple(float(x) for x in (c - pos)),
+                           up=(0.0, 1.0, 0.0), fovy=40.0, orthographic=False)
+        sc.lights = [DistantLight(direction=(-0.4, -0.6, -0.7), intensity=0.8),
+                     DistantLight(direction=(0.6, -0.2, -0.8), intensity=0.4)]
+        sc.background = (0.0, 0.0, 0.0)
+        opt = RenderOptions(width=res, height=res, supersample=1, aoSamples=ao_samples,
+                            aoDistance=0.1 * box, shadows=True)
+        items.append((si, sc, opt))
+    return [b for b, _ in bases], items
