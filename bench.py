@@ -188,17 +188,65 @@ def _device_frames(ctx, built, sc, opt, steps, warmup, flush):
 
     for _ in range(warmup):
         one()
-    ms, rays = [], 0
+    ms, msr, rays = [], [], 0
     for _ in range(steps):
         flush.zero_()
         torch.cuda.synchronize()
         fr = one()
         ms.append(fr.total_ms)
+        msr.append(fr.render_ms)
         rays += fr.rays_primary + fr.rays_occlusion
     pf = one(abi.FRAME_PROFILE)
     names = ["trace_closest", "surface", "trace_occlusion", "shade", "post"]
+    _device_frames.render_ms = sum(msr) / len(msr)
     return (sum(ms) / len(ms), rays / steps, {n: round(v, 3) for n, v in zip(names, pf.phase_ms)},
             pf.layers)
+
+
+def _adjoint_timing(ctx, built, sc, opt, flush, ms_forward, rays_forward, steps=5, warmup=3):
+    """ubr_adjoint with device buffers: dL/dcolour = 2 (frame - 0.5), every
+    gradient group returned, interior samples only."""
+    import ctypes as C
+    import torch
+    from umbreon_gb300 import abi
+    from umbreon_gb300.api import make_render_desc
+    rd, keep = make_render_desc(sc, opt)
+    n = sc.sphere_count()
+    dcol = torch.full((opt.height, opt.width, 4), 0.1, dtype=torch.float32, device="cuda")
+    dcol[..., 3] = 0.0
+    gcol = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    gcen = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    grad = torch.empty(n, dtype=torch.float32, device="cuda")
+
+    def one():
+        g = abi.Grads()
+        g.memory = abi.MEMORY_DEVICE
+        g.flags = abi.ADJOINT_INTERIOR_ONLY
+        g.sphere_color = C.cast(C.c_void_p(gcol.data_ptr()), abi.f32p)
+        g.sphere_center = C.cast(C.c_void_p(gcen.data_ptr()), abi.f32p)
+        g.sphere_radius = C.cast(C.c_void_p(grad.data_ptr()), abi.f32p)
+        ctx._check(ctx._L.ubr_adjoint(ctx.handle, built.handle, C.byref(rd), C.c_void_p(dcol.data_ptr()),
+                                      C.byref(g)))
+        return g
+
+    for _ in range(warmup):
+        one()
+    ms, rays, samples = [], 0, 0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        g = one()
+        ms.append(g.adjoint_ms)
+        rays += g.rays
+        samples = g.samples
+    ms_a = sum(ms) / len(ms)
+    return {"spheres": n, "frame": f"{opt.width}x{opt.height}", "forward_kernels_ms": round(ms_forward, 3),
+            "forward_Mrays_s": round(rays_forward / ms_forward / 1e3, 1), "adjoint_ms": round(ms_a, 3),
+            "adjoint_over_forward": round(ms_a / ms_forward, 3), "adjoint_rays": int(rays / steps),
+            "timing": "device kernels of one call each (CUDA events), L2 flushed before each call",
+            "adjoint_samples": int(samples),
+            "gradients": "sphere colour/centre/radius (device arrays) + material, light, ambient, "
+                         "background, fog, AO globals"}
 
 
 def _cpu_full_or_band(sc, opt, threads, target_s):
@@ -244,6 +292,13 @@ def secondary_workloads(args, flush):
                                      "ms_per_frame": round(ms, 3), "Mrays_s": round(rays / ms / 1e3, 1),
                                      "rays_per_frame": int(rays), "layers": int(layers), "phase_ms": ph,
                                      "cpu": cpu}
+    # workload 4: forward frame vs adjoint (device buffers, L2 flushed)
+    sc, opt = scenes.differentiable()
+    b = ctx.build(sc)
+    ms_f, rays_f, ph, _ = _device_frames(ctx, b, sc, opt, 5, 3, flush)
+    out["differentiable_100k_1024"] = _adjoint_timing(ctx, b, sc, opt, flush, _device_frames.render_ms, rays_f)
+    out["differentiable_100k_1024"]["forward_phase_ms"] = ph
+    b.release()
     ctx.close()
     # workload 3: batched vs one frame per call
     bases, items = scenes.turntable_batch()

@@ -270,6 +270,9 @@ const char* ubr_context_last_error(const ubr_context* ctx);
  * curve_build.cpp:95-175,221-247) so (geomID, primID) can be compared. */
 ubr_status ubr_scene_build(ubr_context* ctx, const ubr_scene_desc* desc,
                            ubr_scene** out);
+/* Frees the scene's device memory.  Destroying a context releases the device
+ * memory of the scenes still alive on it; their handles then stay valid for
+ * ubr_scene_release only. */
 ubr_status ubr_scene_release(ubr_scene* scene);
 /* Scene facts: primitive counts per kind, BVH node count, build time. */
 typedef struct ubr_scene_info {
@@ -308,6 +311,60 @@ typedef struct ubr_batch_item {
 
 ubr_status ubr_render_batch(ubr_context* ctx, uint32_t n, const ubr_batch_item* items,
                             ubr_frame* total);
+
+/* Adjoint of ubr_render: gradients of a scalar image loss L with respect to
+ * scene and render parameters, given dL/d(colour) of the frame.  No
+ * reference counterpart (the reference renders forward only).
+ *
+ * Scope: sphere scenes rendered in one opaque layer (every sphere opaque, or
+ * transparency off); distant lights with hard shadows (at most
+ * UBR_ADJOINT_MAX_LIGHTS, no env dome, no soft shadows); legacy or enhanced AO
+ * without bent normal or multibounce; POV shading; fog; box downsample;
+ * assumed gamma.  Other descriptions return UBR_INVALID_ARGUMENT.
+ *
+ * Visibility is held fixed: the primary hit, each AO sample's occluder and
+ * each shadow bit are recomputed by re-traversal and enter as constants.
+ * Gradients flow through hit distances, normals, AO sample directions and
+ * occluder distances, and every shading, fog, downsample and gamma term, but
+ * not through visibility changes (silhouette / edge terms are excluded).  With
+ * UBR_ADJOINT_INTERIOR_ONLY only hi-res samples whose 3x3 neighbourhood shows
+ * one primitive (or only background) contribute. */
+#define UBR_ADJOINT_MAX_LIGHTS 4
+#define UBR_ADJOINT_INTERIOR_ONLY 1u
+
+typedef struct ubr_grads {
+  int32_t memory;             /* UBR_MEMORY_*: d_color and the per-sphere arrays */
+  uint32_t flags;             /* UBR_ADJOINT_INTERIOR_ONLY */
+  /* per input sphere (n = sphere_count of the scene desc, instances summed);
+   * each may be NULL */
+  float* sphere_color;        /* 3n: d/d(r, g, b) */
+  float* sphere_center;       /* 3n */
+  float* sphere_radius;       /* n */
+  /* global parameters (written) */
+  float material[9];          /* d/d ambient, diffuse, specular, roughness, brilliance,
+                                 phong, phong_size, reflection, emission, each moved
+                                 together in every sphere's material */
+  float light_direction[UBR_ADJOINT_MAX_LIGHTS][3];  /* d/d ubr_light.direction */
+  float light_color[UBR_ADJOINT_MAX_LIGHTS][3];
+  float light_intensity[UBR_ADJOINT_MAX_LIGHTS];
+  float ambient_color[3];
+  float background[3];
+  float fog_start, fog_end;
+  float fog_color[3];
+  float ao_distance, ao_intensity;
+  float specular_scale;
+  /* statistics (written) */
+  uint64_t samples;           /* hi-res samples that contributed */
+  uint64_t rays;              /* rays re-traced */
+  float adjoint_ms;           /* device time of the adjoint launches */
+  float reserved_f[3];
+  uint64_t reserved[4];
+} ubr_grads;
+
+/* d_color: dL/d(frame colour), width x height x 4 floats (r g b a) in
+ * grads->memory.  Per-sphere arrays are overwritten (not accumulated). */
+ubr_status ubr_adjoint(ubr_context* ctx, const ubr_scene* scene, const ubr_render_desc* desc,
+                       const float* d_color, ubr_grads* grads);
 
 /* Segment occlusion for the stroke-edge pass: out[i] = 1 when any geometry
  * lies strictly inside segment (p[i], q[i]) trimmed by eps

@@ -139,6 +139,30 @@ class BatchItem(C.Structure):
 
 
 # Every symbol include/ubr.h declares, with its ctypes signature.
+ADJOINT_MAX_LIGHTS = 4
+ADJOINT_INTERIOR_ONLY = 1
+
+
+class Grads(C.Structure):
+    """ubr_grads (include/ubr.h)."""
+    _fields_ = [
+        ("memory", C.c_int32), ("flags", C.c_uint32),
+        ("sphere_color", f32p), ("sphere_center", f32p), ("sphere_radius", f32p),
+        ("material", C.c_float * 9),
+        ("light_direction", (C.c_float * 3) * ADJOINT_MAX_LIGHTS),
+        ("light_color", (C.c_float * 3) * ADJOINT_MAX_LIGHTS),
+        ("light_intensity", C.c_float * ADJOINT_MAX_LIGHTS),
+        ("ambient_color", C.c_float * 3), ("background", C.c_float * 3),
+        ("fog_start", C.c_float), ("fog_end", C.c_float), ("fog_color", C.c_float * 3),
+        ("ao_distance", C.c_float), ("ao_intensity", C.c_float), ("specular_scale", C.c_float),
+        ("samples", C.c_uint64), ("rays", C.c_uint64), ("adjoint_ms", C.c_float),
+        ("reserved_f", C.c_float * 3), ("reserved", C.c_uint64 * 4),
+    ]
+
+
+MATERIAL_GRAD_FIELDS = ("ambient", "diffuse", "specular", "roughness", "brilliance", "phong", "phong_size",
+                        "reflection", "emission")
+
 SIGNATURES = {
     "ubr_status_string": (C.c_char_p, [C.c_int]),
     "ubr_abi_version": (C.c_uint32, []),
@@ -151,6 +175,7 @@ SIGNATURES = {
     "ubr_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderDesc), C.POINTER(Frame),
                              C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
     "ubr_render_batch": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(BatchItem), C.POINTER(Frame)]),
+    "ubr_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderDesc), C.c_void_p, C.POINTER(Grads)]),
     "ubr_occluded_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
                                      C.c_void_p, C.c_int32]),
     "ubr_occluded_batch_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,

@@ -375,6 +375,40 @@ class Context:
                      phase_ms=list(total.phase_ms))
         return results, stats
 
+    def adjoint(self, built: "BuiltScene", scene: Scene, opt: RenderOptions, d_color: np.ndarray,
+                interior_only: bool = False, spheres: bool = True) -> dict:
+        """Gradients of a loss L given dL/d(colour) (H, W, 4) (ubr_adjoint):
+        per-sphere colour / centre / radius arrays and the global parameters."""
+        rd, keep = make_render_desc(scene, opt)
+        dc = np.ascontiguousarray(d_color, np.float32).reshape(opt.height, opt.width, 4)
+        n = scene.sphere_count()
+        g = abi.Grads()
+        g.memory = abi.MEMORY_HOST
+        g.flags = abi.ADJOINT_INTERIOR_ONLY if interior_only else 0
+        out = {}
+        if spheres:
+            out["sphere_color"] = np.zeros((n, 3), np.float32)
+            out["sphere_center"] = np.zeros((n, 3), np.float32)
+            out["sphere_radius"] = np.zeros(n, np.float32)
+            g.sphere_color = abi.ptr(out["sphere_color"])
+            g.sphere_center = abi.ptr(out["sphere_center"])
+            g.sphere_radius = abi.ptr(out["sphere_radius"])
+        self._check(self._L.ubr_adjoint(self.handle, built.handle, C.byref(rd), dc.ctypes.data, C.byref(g)))
+        for k, name in enumerate(abi.MATERIAL_GRAD_FIELDS):
+            out[name] = float(g.material[k])
+        nl = min(len(scene.lights), abi.ADJOINT_MAX_LIGHTS)
+        out["light_direction"] = np.array([list(g.light_direction[l]) for l in range(nl)], np.float64).reshape(nl, 3)
+        out["light_color"] = np.array([list(g.light_color[l]) for l in range(nl)], np.float64).reshape(nl, 3)
+        out["light_intensity"] = np.array([g.light_intensity[l] for l in range(nl)], np.float64)
+        out["ambient_color"] = np.array(list(g.ambient_color))
+        out["background"] = np.array(list(g.background))
+        out["fog_start"], out["fog_end"] = float(g.fog_start), float(g.fog_end)
+        out["fog_color"] = np.array(list(g.fog_color))
+        out["ao_distance"], out["ao_intensity"] = float(g.ao_distance), float(g.ao_intensity)
+        out["specular_scale"] = float(g.specular_scale)
+        out["stats"] = dict(samples=int(g.samples), rays=int(g.rays), adjoint_ms=float(g.adjoint_ms))
+        return out
+
     def occluded(self, built: "BuiltScene", segs: np.ndarray, eps: float) -> np.ndarray:
         segs = np.ascontiguousarray(segs, np.float32).reshape(-1, 6)
         out = np.zeros(len(segs), np.uint8)

@@ -29,7 +29,7 @@ INCLUDE = ROOT / "include"
 ORACLE = ROOT / "oracle"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["api.cu", "scene_build.cu", "render.cu"]
+CU_SOURCES = ["api.cu", "scene_build.cu", "render.cu", "adjoint.cu"]
 HOST_SOURCES = ["umbreon.cpp"]
 
 
@@ -54,7 +54,7 @@ def _stale(out: Path, deps: list[Path]) -> bool:
 
 
 def _headers() -> list[Path]:
-    return sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
+    return sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 
 
 def build_ubr(verbose: bool = False) -> Path:
@@ -109,7 +109,7 @@ def build_host(verbose: bool = False) -> Path:
 def build_oracle(verbose: bool = False) -> Path:
     """Compile the CPU oracle (test infrastructure)."""
     out = ORACLE / "liboracle.so"
-    srcs = [ORACLE / "src" / "oracle_render.cpp"]
+    srcs = [ORACLE / "src" / "oracle_render.cpp", ORACLE / "src" / "oracle_fd64.cpp"]
     deps = srcs + sorted((ORACLE / "src").glob("*.hpp")) + sorted(INCLUDE.glob("*.h"))
     if _stale(out, deps):
         _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",

@@ -2,6 +2,7 @@
 // The C-ABI never throws: every failure is a ubr_status plus a message kept
 // on the context (ubr_context_last_error).
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -23,6 +24,7 @@ struct Job {
   ubr_frame* frame;
 };
 ubr_status renderBatch(Context* c, const std::vector<Job>& jobs, ubr_frame* total);
+ubr_status adjoint(Context* c, const Scene* sc, const ubr_render_desc& d, const float* dColor, ubr_grads& g);
 ubr_status occludedBatchNoAlloc(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps,
                                 uint8_t* out);
 
@@ -163,6 +165,14 @@ ubr_status ubr_context_destroy(ubr_context* c) {
   Context& x = c->impl;
   cudaSetDevice(x.device);
   if (x.stream) cudaStreamSynchronize(x.stream);
+  // scenes still alive lose their device memory now; their handles stay
+  // valid for ubr_scene_release only
+  for (void* h : x.sceneHandles) {
+    ubr_scene* s = static_cast<ubr_scene*>(h);
+    if (s->impl) releaseScene(s->impl);
+    s->impl = nullptr;
+  }
+  x.sceneHandles.clear();
   for (DevBuf& b : x.scratch) devFree(&x, b);
   for (cudaEvent_t& e : x.ev)
     if (e) cudaEventDestroy(e);
@@ -200,6 +210,7 @@ ubr_status ubr_scene_build(ubr_context* c, const ubr_scene_desc* desc, ubr_scene
     releaseScene(sc);
     return setError(&c->impl, UBR_OUT_OF_MEMORY, "host allocation failed");
   }
+  c->impl.sceneHandles.push_back(s);
   *out = s;
   return UBR_OK;
 }
@@ -207,9 +218,12 @@ ubr_status ubr_scene_build(ubr_context* c, const ubr_scene_desc* desc, ubr_scene
 ubr_status ubr_scene_release(ubr_scene* s) {
   if (!s) return UBR_OK;
   if (s->impl) {
-    cudaSetDevice(s->impl->ctx->device);
-    cudaStreamSynchronize(s->impl->ctx->stream);
+    Context* x = s->impl->ctx;
+    cudaSetDevice(x->device);
+    cudaStreamSynchronize(x->stream);
     releaseScene(s->impl);
+    auto& v = x->sceneHandles;
+    v.erase(std::remove(v.begin(), v.end(), static_cast<void*>(s)), v.end());
   }
   delete s;
   return UBR_OK;
@@ -272,6 +286,16 @@ ubr_status ubr_render_batch(ubr_context* c, uint32_t n, const ubr_batch_item* it
   } catch (...) {
     return setError(&c->impl, UBR_INTERNAL, "render failed");
   }
+}
+
+ubr_status ubr_adjoint(ubr_context* c, const ubr_scene* s, const ubr_render_desc* desc, const float* d_color,
+                       ubr_grads* grads) {
+  if (!c) return UBR_INVALID_ARGUMENT;
+  if (!s || !s->impl) return setError(&c->impl, UBR_INVALID_ARGUMENT, "adjoint: NULL scene");
+  if (!desc || !grads) return setError(&c->impl, UBR_INVALID_ARGUMENT, "adjoint: NULL desc or grads");
+  if (s->impl->ctx != &c->impl) return setError(&c->impl, UBR_INVALID_ARGUMENT, "adjoint: scene from another context");
+  cudaSetDevice(c->impl.device);
+  return adjoint(&c->impl, s->impl, *desc, d_color, *grads);
 }
 
 ubr_status ubr_occluded_batch(ubr_context* c, const ubr_scene* s, const float* segs, uint64_t n, float eps,

@@ -25,7 +25,7 @@
 #include <cstring>
 #include <vector>
 
-#include "ubr_context.h"
+#include "trace.cuh"
 
 namespace ubr {
 
@@ -33,8 +33,6 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out);
 
 namespace {
 
-constexpr int kStackDepth = 32;  // group entries: one per tree level
-constexpr float kInfF = __builtin_huge_valf();
 
 struct Bufs {
   float4* accum;      // per hi-res pixel: Cf.rgb, Af
@@ -86,416 +84,6 @@ UBR_D int frameOf(const uint32_t* offs, int n, uint32_t g) {
     else hi = mid - 1;
   }
   return lo;
-}
-
-UBR_D f3 ld3(const float4 v) { return f3{v.x, v.y, v.z}; }
-
-UBR_D f3 safeInv(f3 d) {
-  auto f = [](float x) {
-    if (fabsf(x) < 1e-30f) x = copysignf(1e-30f, x);
-    return 1.0f / x;
-  };
-  return f3{f(d.x), f(d.y), f(d.z)};
-}
-
-// Primary ray of hi-res pixel (px, py): embree_renderer.cpp:1399-1414.
-UBR_D void primaryRay(const Params& p, int px, int py, f3& org, f3& rd) {
-  const float v = 1.0f - 2.0f * (float(py) + 0.5f) / float(p.H);
-  const float u = 2.0f * (float(px) + 0.5f) / float(p.W) - 1.0f;
-  if (p.ortho) {
-    org = p.camPos + p.right * (u * p.halfW) + p.up * (v * p.halfH);
-    rd = p.camDir;
-  } else {
-    org = p.camPos;
-    rd = normalize(p.camDir + p.right * (u * p.persHalfW) + p.up * (v * p.persHalfH));
-  }
-}
-
-// clipRangeT (transparency.hpp:118-129)
-UBR_D void clipRange(const Params& p, f3 rd, float& tn, float& tf) {
-  tn = 0.0f;
-  tf = kInfF;
-  if (p.clipNear <= -kInfF && p.clipFar >= kInfF) return;
-  const float cosr = dot(rd, p.camDir);
-  if (cosr <= 1.0e-6f) return;
-  if (p.clipNear > 0.0f) tn = p.clipNear / cosr;
-  if (p.clipFar < kInfF) tf = p.clipFar / cosr;
-}
-
-UBR_D bool slabHit(float lox, float hix, float loy, float hiy, float loz, float hiz, const f3& o,
-                   const f3& inv, float tnear, float tmax, float& tEntry) {
-  const float t0x = (lox - o.x) * inv.x, t1x = (hix - o.x) * inv.x;
-  const float t0y = (loy - o.y) * inv.y, t1y = (hiy - o.y) * inv.y;
-  const float t0z = (loz - o.z) * inv.z, t1z = (hiz - o.z) * inv.z;
-  const float tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tnear));
-  const float tmx = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tmax));
-  tEntry = tmin;
-  return tmin <= tmx;
-}
-
-// Kind masks: bit k set when primitives of kind k exist.  Kernels are
-// instantiated per mask so a scene only carries the intersectors it needs.
-constexpr int kMaskMesh = 1 << kMesh, kMaskSphere = 1 << kSphere, kMaskRound = 1 << kRound,
-              kMaskCone = 1 << kCone, kMaskAll = 15;
-
-template <int KM, bool ATTR = true>
-UBR_D bool testLeaf(const TravScene& s, int slot, const Ray& r, const TriPre& pre, float tnear,
-                    float tmax, Hit& h, uint32_t& ref) {
-  ref = __ldg(&s.leafRef[slot]);
-  const int kind = refKind(ref);
-  const float4* g = s.leafGeo + kLeafF4 * slot;
-  constexpr bool single = (KM & (KM - 1)) == 0;
-  if ((KM & kMaskSphere) && (single || kind == kSphere)) {
-    const float4 q = __ldg(g);
-    return isectSphere<ATTR>(r, f3{q.x, q.y, q.z}, q.w, tnear, tmax, h);
-  }
-  if ((KM & kMaskMesh) && (single || kind == kMesh)) {
-    const float4 a = __ldg(g), b = __ldg(g + 1), c = __ldg(g + 2);
-    return isectTriangle(r, pre, ld3(a), ld3(b), ld3(c), tnear, tmax, h);
-  }
-  if (!(KM & (kMaskCone | kMaskRound))) return false;
-  const float4 a = __ldg(g), b = __ldg(g + 1);
-  if ((KM & kMaskCone) && (!(KM & kMaskRound) || kind == kCone)) {
-    const float4 ax = __ldg(g + 2);
-    return isectConeCurveAxis<ATTR>(r, ld3(a), a.w, ld3(b), b.w, ld3(ax), ax.w, tnear, tmax, h);
-  }
-  if (!(KM & kMaskRound)) return false;
-  const uint32_t prim = refPrim(ref);
-  const uint32_t flags = __float_as_uint(__ldg(g + 2).x);
-  const float4 cl = __ldg(&s.rcClip[2 * prim]), cr = __ldg(&s.rcClip[2 * prim + 1]);
-  return isectRoundCurve(r, ld3(a), a.w, ld3(b), b.w, flags, ld3(cl), ld3(cr), tnear, tmax, h);
-}
-
-// Stack traversal of the binary LBVH, near child first.  ANY: return at the
-// first hit in [tnear, tfar].  Closest: smallest t, ties to lowest
-// (geomID, primID).
-// Bytes of the leaf record fetched for one primitive test, by kind
-// (leafRef 4 B + geometry float4s; round segments add their 32 B clip planes).
-UBR_D uint32_t leafBytes(int kind) {
-  return kind == kSphere ? 20u : kind == kMesh ? 52u : kind == kCone ? 36u : 84u;
-}
-
-struct Count {
-  uint32_t nodes = 0, primBytes = 0;
-};
-
-// Stack traversal of the 8-wide BVH (node/primitive groups after Ylitie,
-// Karras and Laine, HPG 2017).  Visiting a node is branch-free: each child's
-// slab planes are one fmaf each from the 8-bit bounds, giving a hit mask;
-// the nearest hit internal child is visited next and the other hit internal
-// children are pushed as ONE group entry (childBase << 8 | slot mask), so the
-// stack depth is the tree depth; hit leaves expand into a mask over the
-// node's contiguous primitive block, tested in one loop.  The slab interval
-// is widened by a relative 2^-19 so quantised boxes stay conservative under
-// float rounding at any camera distance.  any: return at the first hit in
-// [tnear, tfar]; otherwise the closest hit, ties to the lowest
-// (geomID, primID).
-constexpr float kSlabGrow = 1.0f + 0x1.0p-19f;
-
-// Byte b of word q as a float, without an integer->float conversion: place
-// the byte in the mantissa of 2^23 (byte permute) and subtract 2^23 (exact).
-UBR_D float byteToFloat(uint32_t q, int b) {
-  return __uint_as_float(__byte_perm(q, 0x4B000000u, 0x7540u + uint32_t(b))) - 8388608.0f;
-}
-
-// Traversal state of one ray, resumable one node at a time (the persistent
-// occlusion kernel interleaves rays at node granularity).
-struct TravState {
-  int node;                      // node to visit next
-  int sp;
-  uint32_t steps;
-  float tmax;
-  uint32_t bestGeom, bestPrim;
-  uint32_t stack[kStackDepth];   // group entries: (childBase << 8) | slot mask
-};
-
-UBR_D void travInit(const Ray& r, TravState& st, Hit& best) {
-  st.node = 0;
-  st.sp = 0;
-  st.steps = 0;
-  st.tmax = r.tfar;
-  st.bestGeom = kInvalid;
-  st.bestPrim = kInvalid;
-  best.ref = kInvalid;
-}
-
-// Visit st.node: test its 8 children, its hit leaves' primitives, choose the
-// next node.  Returns true when the ray is finished (any-hit found, stack
-// empty, or the step bound reached).
-template <bool COUNT, int KM, bool ALWAYS_ANY = false>
-UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPre& pre, TravState& st, Hit& best,
-                    uint32_t& overflow, Count* cnt, bool any) {
-  if (ALWAYS_ANY) any = true;
-  if (++st.steps > s.primCount + 16u) {  // each node at most once per ray in a valid tree
-    ++overflow;
-    return true;
-  }
-  if (COUNT) ++cnt->nodes;
-  const float4* nd = s.wnodes + kWideF4 * st.node;
-  const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3), n4 = __ldg(nd + 4);
-  const uint32_t hdr = __float_as_uint(n0.w);
-  const float sx = __uint_as_float((hdr & 0xFFu) << 23) * inv.x;
-  const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * inv.y;
-  const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23) * inv.z;
-  const int nInt = int((hdr >> 24) & 0xFu), nCh = int(hdr >> 28);
-  const float ox = (n0.x - r.org.x) * inv.x, oy = (n0.y - r.org.y) * inv.y, oz = (n0.z - r.org.z) * inv.z;
-  const uint32_t childBase = __float_as_uint(n1.x);
-  const int primBase = __float_as_int(n1.y);
-  const uint32_t meta0 = __float_as_uint(n1.z), meta1 = __float_as_uint(n1.w);
-  // near/far planes per axis by the sign of the direction (swap lo/hi words)
-  const bool nx = inv.x < 0.0f, ny = inv.y < 0.0f, nz = inv.z < 0.0f;
-  const uint32_t qnx[2] = {nx ? __float_as_uint(n3.z) : __float_as_uint(n2.x),
-                           nx ? __float_as_uint(n3.w) : __float_as_uint(n2.y)};
-  const uint32_t qfx[2] = {nx ? __float_as_uint(n2.x) : __float_as_uint(n3.z),
-                           nx ? __float_as_uint(n2.y) : __float_as_uint(n3.w)};
-  const uint32_t qny[2] = {ny ? __float_as_uint(n4.x) : __float_as_uint(n2.z),
-                           ny ? __float_as_uint(n4.y) : __float_as_uint(n2.w)};
-  const uint32_t qfy[2] = {ny ? __float_as_uint(n2.z) : __float_as_uint(n4.x),
-                           ny ? __float_as_uint(n2.w) : __float_as_uint(n4.y)};
-  const uint32_t qnz[2] = {nz ? __float_as_uint(n4.z) : __float_as_uint(n3.x),
-                           nz ? __float_as_uint(n4.w) : __float_as_uint(n3.y)};
-  const uint32_t qfz[2] = {nz ? __float_as_uint(n3.x) : __float_as_uint(n4.z),
-                           nz ? __float_as_uint(n3.y) : __float_as_uint(n4.w)};
-  uint32_t hitInt = 0, primMask = 0;
-  float nearT = kInfF;
-  int nearK = -1;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int w = k >> 2;
-    const float tnx = fmaf(byteToFloat(qnx[w], k & 3), sx, ox), tfx = fmaf(byteToFloat(qfx[w], k & 3), sx, ox);
-    const float tny = fmaf(byteToFloat(qny[w], k & 3), sy, oy), tfy = fmaf(byteToFloat(qfy[w], k & 3), sy, oy);
-    const float tnz = fmaf(byteToFloat(qnz[w], k & 3), sz, oz), tfz = fmaf(byteToFloat(qfz[w], k & 3), sz, oz);
-    const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tnear));
-    const float tmx = fminf(fminf(tfx, tfy), fminf(tfz, st.tmax));
-    const bool hit = k < nCh && tmin <= tmx * kSlabGrow;
-    if (k < nInt) {
-      hitInt |= hit ? (1u << k) : 0u;
-      const bool nearer = hit && tmin < nearT;
-      nearT = nearer ? tmin : nearT;
-      nearK = nearer ? k : nearK;
-    } else if (hit) {
-      const uint32_t m = ((w == 0 ? meta0 : meta1) >> ((k & 3) * 8)) & 0xFFu;
-      primMask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-    }
-  }
-  // primitives of the hit leaves
-  while (primMask) {
-    const int q = __ffs(primMask) - 1;
-    primMask &= primMask - 1u;
-    Hit h;
-    uint32_t ref;
-    const bool hitLeaf = testLeaf<KM, !ALWAYS_ANY>(s, primBase + q, r, pre, r.tnear, st.tmax, h, ref);
-    if (COUNT) cnt->primBytes += leafBytes(refKind(ref));
-    if (!hitLeaf) continue;
-    if (any) {
-      best = h;
-      best.ref = ref;
-      return true;
-    }
-    const int kind = refKind(ref);
-    const uint32_t gid = s.geomID[kind], prim = refPrim(ref);
-    const bool better = best.ref == kInvalid || h.t < best.t ||
-                        (h.t == best.t && (gid < st.bestGeom || (gid == st.bestGeom && prim < st.bestPrim)));
-    if (better) {
-      best = h;
-      best.ref = ref;
-      st.bestGeom = gid;
-      st.bestPrim = prim;
-      st.tmax = h.t;
-    }
-  }
-  if (nearK >= 0) {
-    const uint32_t rest = hitInt & ~(1u << nearK);
-    if (rest) {
-      if (st.sp < kStackDepth) st.stack[st.sp++] = (childBase << 8) | rest;
-      else ++overflow;
-    }
-    st.node = int(childBase) + nearK;
-    return false;
-  }
-  if (st.sp == 0) return true;
-  const uint32_t g = st.stack[st.sp - 1];
-  const uint32_t mask = g & 0xFFu;
-  const int k = __ffs(mask) - 1;
-  const uint32_t left = mask & (mask - 1u);
-  if (left) st.stack[st.sp - 1] = (g & ~0xFFu) | left;
-  else --st.sp;
-  st.node = int(g >> 8) + k;
-  return false;
-}
-
-// Whole traversal of one ray (one thread per ray).
-template <bool COUNT = false, int KM = kMaskAll, bool ALWAYS_ANY = false>
-__device__ bool traverse(const TravScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt,
-                         const bool any) {
-  best.ref = kInvalid;
-  if (s.primCount == 0) return false;
-  const f3 inv = safeInv(r.dir);
-  TriPre pre;
-  if (KM & kMaskMesh) pre = triPre(r.dir);
-  TravState st;
-  travInit(r, st, best);
-  while (!travStep<COUNT, KM, ALWAYS_ANY>(s, r, inv, pre, st, best, overflow, cnt, any)) {
-  }
-  return best.ref != kInvalid;
-}
-
-// Shading surface of a hit (hit_shader.hpp:147-341 attribute + normal logic).
-struct Surf {
-  int kind;
-  uint32_t prim;
-  f3 P, N, Ng, C, V;
-  float opacity;
-  uint32_t mat;
-  float secEps;
-  bool aoOn, shOn;
-};
-
-// secondary_rays.hpp:38-46
-UBR_D float selfIntersectEps(f3 P, f3 dir, float t) {
-  const float dirMax = fmaxf(fabsf(dir.x), fmaxf(fabsf(dir.y), fabsf(dir.z)));
-  const float epsScale = fmaxf(fmaxf(fabsf(P.x), fabsf(P.y)), fmaxf(fabsf(P.z), dirMax * t));
-  return epsScale * 0x1.0fp-21f;
-}
-// shading.hpp:27-30
-UBR_D f3 faceForward(f3 n, f3 rd) { return dot(n, rd) > 0.0f ? neg(n) : n; }
-
-UBR_D Surf surfaceAt(const Params& p, const DScene& s, f3 org, f3 rd, float t, uint32_t ref, float u,
-                     float v, f3 Ng) {
-  Surf sf;
-  sf.kind = refKind(ref);
-  sf.prim = refPrim(ref);
-  sf.V = normalize(f3{-rd.x, -rd.y, -rd.z});
-  sf.Ng = Ng;
-  sf.P = f3{org.x + rd.x * t, org.y + rd.y * t, org.z + rd.z * t};
-  sf.secEps = selfIntersectEps(sf.P, rd, t);
-  const bool shadowsActive = p.shadowsActive != 0;
-  if (sf.kind == kMesh) {
-    const uint32_t i0 = __ldg(&s.meshIdx[3 * sf.prim]), i1 = __ldg(&s.meshIdx[3 * sf.prim + 1]),
-                   i2 = __ldg(&s.meshIdx[3 * sf.prim + 2]);
-    const float w0 = 1.0f - u - v;
-    float nb[3];
-    for (int k = 0; k < 3; ++k)
-      nb[k] = w0 * __ldg(&s.meshNrm[3 * i0 + k]) + u * __ldg(&s.meshNrm[3 * i1 + k]) +
-              v * __ldg(&s.meshNrm[3 * i2 + k]);
-    const float4 c0 = __ldg(&s.meshCol[i0]), c1 = __ldg(&s.meshCol[i1]), c2 = __ldg(&s.meshCol[i2]);
-    const float4 cb = make_float4(w0 * c0.x + u * c1.x + v * c2.x, w0 * c0.y + u * c1.y + v * c2.y,
-                                  w0 * c0.z + u * c1.z + v * c2.z, w0 * c0.w + u * c1.w + v * c2.w);
-    const f3 NgF = faceForward(Ng, rd);
-    f3 N = normalize(f3{nb[0], nb[1], nb[2]});
-    if (dot(N, NgF) < 0.0f) N = neg(N);
-    sf.N = N;
-    sf.C = f3{cb.x, cb.y, cb.z};
-    sf.opacity = cb.w;
-    sf.mat = s.meshTriMat ? __ldg(&s.meshTriMat[s.baseTri ? sf.prim % s.baseTri : 0]) : s.meshMat;
-    sf.aoOn = p.aoSamples > 0;
-    sf.shOn = shadowsActive;
-  } else {
-    const float4 fc = __ldg(&s.primColor[sf.kind][sf.prim]);
-    sf.mat = __ldg(&s.primMat[sf.kind][sf.prim]);
-    sf.N = faceForward(normalize(Ng), rd);
-    sf.C = f3{fc.x, fc.y, fc.z};
-    const bool fromEdge = __ldg(&s.primFromEdge[sf.kind][sf.prim]) != 0;
-    sf.aoOn = !fromEdge && p.aoSamples > 0;
-    sf.shOn = !fromEdge && shadowsActive;
-    sf.opacity = fc.w;
-    if (sf.kind != kSphere) {
-      const float op1 = __ldg(&s.primOpacity1[sf.kind][sf.prim]);
-      if (op1 >= 0.0f) {
-        float uu = u;
-        if (uu < 0.0f) uu = 0.0f;
-        if (uu > 1.0f) uu = 1.0f;
-        sf.opacity = fc.w * (1.0f - uu) + op1 * uu;
-      }
-    }
-  }
-  return sf;
-}
-
-// secondary_rays.hpp:51-61
-UBR_D void tea2(uint32_t& v0, uint32_t& v1) {
-  uint32_t sum = 0;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    sum += 0x9E3779B9u;
-    v0 += ((v1 << 4) + 0xA341316Cu) ^ (v1 + sum) ^ ((v1 >> 5) + 0xC8013EA4u);
-    v1 += ((v0 << 4) + 0xAD90777Du) ^ (v0 + sum) ^ ((v0 >> 5) + 0x7E95761Eu);
-  }
-}
-UBR_D float u32ToUnorm(uint32_t u) { return float(u >> 8) * 0x1.0p-24f; }
-// secondary_rays.hpp:66-73
-UBR_D f3 cosineSampleHemisphere(float u1, float u2, const Frame3& f) {
-  const float phi = 6.2831853072f * u1;
-  const float r = sqrtf(u2);
-  const float z = sqrtf(fmaxf(0.0f, 1.0f - u2));
-  const float x = cosf(phi) * r;
-  const float y = sinf(phi) * r;
-  return f.t * x + f.b * y + f.n * z;
-}
-// ambient_occlusion.hpp:98-105
-UBR_D float radicalInverse2(uint32_t bits) { return float(__brev(bits)) * 0x1.0p-32f; }
-// ambient_occlusion.hpp:112-127
-UBR_D void aoSample2d(const Params& p, uint32_t base, int i, float cpx, float cpy, float& u1, float& u2) {
-  if (p.aoLowDiscrepancy) {
-    u1 = float(i) / float(p.aoSamples) + cpx;
-    u2 = radicalInverse2(uint32_t(i)) + cpy;
-    if (u1 >= 1.0f) u1 -= 1.0f;
-    if (u2 >= 1.0f) u2 -= 1.0f;
-  } else {
-    uint32_t s0 = base, s1 = uint32_t(i);
-    tea2(s0, s1);
-    u1 = u32ToUnorm(s0);
-    u2 = u32ToUnorm(s1);
-  }
-}
-UBR_D void cpShift(int px, int py, float& cpx, float& cpy) {
-  uint32_t c0 = uint32_t(px) + 1u, c1 = uint32_t(py) + 1u;
-  tea2(c0, c1);
-  cpx = u32ToUnorm(c0);
-  cpy = u32ToUnorm(c1);
-}
-// AO direction of sample i (legacy: tea2 stream; enhanced: also LD)
-UBR_D f3 aoDir(const Params& p, const Frame3& f, int px, int py, int i) {
-  const uint32_t base = uint32_t(px) + uint32_t(py) * uint32_t(p.W);
-  float u1, u2;
-  if (p.aoEnhanced) {
-    float cpx = 0.0f, cpy = 0.0f;
-    if (p.aoLowDiscrepancy) cpShift(px, py, cpx, cpy);
-    aoSample2d(p, base, i, cpx, cpy, u1, u2);
-  } else {
-    uint32_t s0 = base, s1 = uint32_t(i);
-    tea2(s0, s1);
-    u1 = u32ToUnorm(s0);
-    u2 = u32ToUnorm(s1);
-  }
-  return cosineSampleHemisphere(u1, u2, f);
-}
-// secondary_rays.hpp:102-109
-UBR_D f3 sampleLightDir(const LightD& l, float u1, float u2) {
-  if (l.radius <= 0.0f) return l.L;
-  const Frame3 f = frameFromNormal(l.L);
-  const float phi = 6.2831853072f * u1;
-  const float rr = tanf(l.radius) * sqrtf(u2);
-  const f3 d = f.n + f.t * (rr * cosf(phi)) + f.b * (rr * sinf(phi));
-  return safeNormalize(d, l.L);
-}
-
-UBR_D int warpPushBase(bool push, uint32_t* counter, int& offset) {
-  const unsigned mask = __ballot_sync(0xFFFFFFFFu, push);
-  const int lane = threadIdx.x & 31;
-  int base = 0;
-  if (mask) {
-    const int leader = __ffs(mask) - 1;
-    if (lane == leader) base = int(atomicAdd(counter, uint32_t(__popc(mask))));
-    base = __shfl_sync(0xFFFFFFFFu, base, leader);
-  }
-  offset = __popc(mask & ((1u << lane) - 1u));
-  return base;
-}
-
-UBR_D void warpCount(unsigned long long* ctr, uint32_t v) {
-  uint32_t s = __reduce_add_sync(0xFFFFFFFFu, v);
-  if ((threadIdx.x & 31) == 0 && s) atomicAdd(ctr, (unsigned long long)s);
 }
 
 // ---------------------------------------------------------------------------
@@ -755,21 +343,6 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p1
     warpCount(&b.stats[6], cnt.nodes);
     warpCount(&b.stats[7], cnt.primBytes);
   }
-}
-
-UBR_D float blinnExp(float roughness) {
-  float r = roughness;
-  if (r < 1e-6f) r = 1e-6f;
-  float e = 1.0f / r;
-  if (e < 1.0f) e = 1.0f;
-  if (e > 1.0e6f) e = 1.0e6f;
-  return e;
-}
-UBR_D float aoMultibounce(float ao, float albedo) {
-  const float a = 2.0404f * albedo - 0.3324f;
-  const float bb = -4.7951f * albedo + 0.6417f;
-  const float c = 2.7552f * albedo + 0.6903f;
-  return fmaxf(ao, ((ao * a + bb) * ao + c) * ao);
 }
 
 template <bool BATCH>
@@ -1067,6 +640,8 @@ __global__ void k_init_pixels(uint32_t npix, float* depth, float* viewZ, uint32_
   hp[i] = kInvalid;
 }
 
+}  // namespace
+
 // Host-side parameter setup: computeCameraBasis (embree_renderer.cpp:375-386),
 // buildSceneLights (:436-458) and buildEnvDomeLights (ao/env_dome.hpp:33-64),
 // evaluated in float on the host exactly as the reference does.
@@ -1175,6 +750,8 @@ ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vect
   return UBR_OK;
 }
 
+namespace {
+
 // EmbreeRenderer::occluded plain any-hit branch (embree_renderer.cpp:294-315):
 // the open segment (p, q) trimmed by max(eps*len, eps) and len*(1-eps).
 __global__ void k_occluded_segments(DScene s, const float* segs, uint64_t n, float eps, uint8_t* out,
@@ -1276,13 +853,6 @@ uint32_t persistentGrid(int device) {
 void launchOcclusionPersistent(int km, bool count, bool batch, uint32_t grid, int tb, cudaStream_t st,
                                const Params& p, const DScene& s, const Batch& bt, const Bufs& b) {
   UBR_KM_DISPATCH(k_trace_occlusion_persistent, km, count, batch, grid, tb, st, p, s, bt, b);
-}
-
-template <class T>
-T* scratchT(Context* c, int slot, size_t count, ubr_status& st) {
-  void* ptr = nullptr;
-  if (st == UBR_OK) st = scratchGet(c, slot, count * sizeof(T) + 16, &ptr);
-  return static_cast<T*>(ptr);
 }
 
 }  // namespace

@@ -40,6 +40,7 @@ struct HostScene {
   uint32_t meshMat = 0;
   uint32_t baseTri = 0;
   std::vector<float4> sph;            // (c, r)
+  uint32_t baseSph = 0;               // spheres per instance
   std::vector<float4> rcV;            // round curve vertices (xyz, r)
   std::vector<uint32_t> rcIdx;
   std::vector<uint8_t> rcFlags;
@@ -261,6 +262,7 @@ ubr_status flatten(Context* c, const ubr_scene_desc& d, HostScene& s) {
   }
   if (d.sphere_count > 0) {
     s.geomID[kSphere] = nextGeom++;
+    s.baseSph = uint32_t(d.sphere_count);
     for (const f3& off : offs)
       for (uint64_t i = 0; i < d.sphere_count; ++i) {
         const float* q = d.sphere_center_radius + 4 * i;
@@ -764,6 +766,8 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   if ((st = upload(c, sc, hs.idx, &v.meshIdx)) != UBR_OK) return fail(st);
   if ((st = upload(c, sc, hs.triMat, &v.meshTriMat)) != UBR_OK) return fail(st);
   if ((st = upload(c, sc, hs.sph, &dsph)) != UBR_OK) return fail(st);
+  v.sph = dsph;
+  v.baseSph = hs.baseSph;
   if ((st = upload(c, sc, hs.rcV, &drcV)) != UBR_OK) return fail(st);
   if ((st = upload(c, sc, hs.rcIdx, &drcIdx)) != UBR_OK) return fail(st);
   if ((st = upload(c, sc, hs.rcFlags, &drcFl)) != UBR_OK) return fail(st);

@@ -35,6 +35,7 @@ struct Context {
   bool useGraphs = true;     // replay single-layer frames from a CUDA graph
   cudaGraphExec_t graphExec = nullptr;
   std::vector<unsigned char> graphKey;  // launch parameters the graph was captured with
+  std::vector<void*> sceneHandles;      // live ubr_scene handles built on this context
 };
 
 struct Scene {
@@ -57,6 +58,18 @@ ubr_status devAlloc(Context* c, DevBuf& b, size_t bytes);
 void devFree(Context* c, DevBuf& b);
 // scratch slot `i` of at least `bytes`
 ubr_status scratchGet(Context* c, int i, size_t bytes, void** out);
+
+// typed view of scratch slot `slot` (count elements); a no-op once st != OK
+template <class T>
+T* scratchT(Context* c, int slot, size_t count, ubr_status& st) {
+  void* ptr = nullptr;
+  if (st == UBR_OK) st = scratchGet(c, slot, count * sizeof(T) + 16, &ptr);
+  return static_cast<T*>(ptr);
+}
+
+// Frame parameters and light table of a render description (camera basis,
+// lights, AO / fog / gamma settings), validated.
+ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vector<LightD>& lights);
 
 #define UBR_CUDA(ctx, call)                                  \
   do {                                                       \

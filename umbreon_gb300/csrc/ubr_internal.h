@@ -120,6 +120,8 @@ struct DScene {
   const uint8_t* primFromEdge[4] = {nullptr, nullptr, nullptr, nullptr};
   const float* primOpacity1[4] = {nullptr, nullptr, nullptr, nullptr};
   const float4* rcClip = nullptr;      // 2 per round segment (clipL, clipR)
+  const float4* sph = nullptr;         // per sphere (centre, radius), primID order
+  uint32_t baseSph = 0;                // spheres per instance (primID % baseSph = input sphere)
   const ubr_material* mats = nullptr;
   uint32_t geomID[4] = {kInvalid, kInvalid, kInvalid, kInvalid};
 };

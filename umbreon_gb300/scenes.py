@@ -364,3 +364,70 @@ def turntable_batch(seed: int = BASE_SEED + 3, n_items: int = 64, n_scenes: int 
                             aoDistance=0.1 * box, shadows=True)
         items.append((si, sc, opt))
     return [b for b, _ in bases], items
+
+
+def differentiable(seed: int = BASE_SEED + 4, n: int = 100000, res: int = 1024, ao_samples: int = 16,
+                   box: float | None = None):
+    """Workload 4: n spheres with workload 0's radius and colour distribution
+    in a cube of 120 A at 100,000 spheres (the side scales with n^(1/3) to
+    keep the density), POV finish with Blinn specular 0.3 (roughness 0.02)
+    and Phong 0.3 (size 40), res x res orthographic view along -z, one
+    shadowed light, enhanced AO (16 rays, linear falloff: power 1) at
+    distance 4 A, linear fog across the cube's depth."""
+    if box is None:
+        box = 120.0 * (n / 100000.0) ** (1.0 / 3.0)
+    mat = abi.material(ambient=0.2, diffuse=0.7, specular=0.3, roughness=0.02, brilliance=1.0,
+                       phong=0.3, phong_size=40.0)
+    cr, col, mats = random_spheres(n, box, seed, mat)
+    sc = Scene(sphere_center_radius=cr, sphere_color=col, sphere_material=mats)
+    c = 0.5 * box
+    dist = 1.5 * box + 10.0
+    sc.camera = Camera(position=(c, c, c + dist), direction=(0.0, 0.0, -1.0), up=(0.0, 1.0, 0.0),
+                       orthographic=True, height=1.02 * box)
+    sc.lights = [DistantLight(direction=(-0.35, -0.45, -0.8), intensity=0.9)]
+    sc.ambientColor = (1.0, 1.0, 1.0)
+    sc.background = (0.05, 0.05, 0.1)
+    # view-z of the cube's front face is dist - box / 2
+    sc.fog = Fog(enabled=True, color=(0.6, 0.65, 0.7), start=dist - 0.5 * box + 0.1 * box,
+                 end=dist - 0.5 * box + 1.4 * box)
+    opt = RenderOptions(width=res, height=res, supersample=1, aoSamples=ao_samples, aoDistance=4.0,
+                        aoFalloffPower=1.0, shadows=True)
+    return sc, opt
+
+
+def differentiable_target(sc: Scene, opt: RenderOptions, seed: int = BASE_SEED + 40):
+    """The target of workload 4's loss: the same scene with perturbed diffuse,
+    specular and phong size, light direction turned by up to 10 degrees and
+    intensity scaled by up to +/-20%, fog range, AO distance, per-sphere
+    colours (+/-0.05) and centres (+/-0.1 A)."""
+    import copy
+    u = uniform(seed, 8, 1)[:, 0]
+    t = copy.deepcopy(sc)
+    o = copy.deepcopy(opt)
+    m = np.array(t.sphere_material, abi.MATERIAL_DTYPE, copy=True)
+    m["diffuse"] *= 1.0 + 0.2 * (u[0] - 0.5)
+    m["specular"] *= 1.0 + 0.2 * (u[1] - 0.5)
+    m["phong_size"] *= 1.0 + 0.2 * (u[2] - 0.5)
+    t.sphere_material = m
+    L = t.lights[0]
+    d = np.asarray(L.direction, np.float64)
+    d = d / np.linalg.norm(d)
+    axis = np.cross(d, [0.0, 1.0, 0.0])
+    axis /= np.linalg.norm(axis)
+    ang = math.radians(10.0 * (2.0 * u[3] - 1.0))
+    d2 = d * math.cos(ang) + np.cross(axis, d) * math.sin(ang) + axis * np.dot(axis, d) * (1 - math.cos(ang))
+    t.lights = [DistantLight(direction=tuple(float(x) for x in d2), intensity=L.intensity * (1.0 + 0.4 * (u[4] - 0.5)),
+                             color=L.color, castsHighlight=L.castsHighlight)]
+    span = t.fog.end - t.fog.start
+    t.fog = Fog(enabled=True, color=t.fog.color, start=t.fog.start + 0.1 * span * (u[5] - 0.5),
+                end=t.fog.end + 0.1 * span * (u[5] - 0.5))
+    o.aoDistance = opt.aoDistance * (1.0 + 0.3 * (u[6] - 0.5))
+    n = sc.sphere_count()
+    up = uniform(seed + 1, n, 6)
+    col = np.array(t.sphere_color, np.float32, copy=True)
+    col[:, :3] = np.clip(col[:, :3] + 0.1 * (up[:, :3] - 0.5), 0.0, 1.0)
+    cr = np.array(t.sphere_center_radius, np.float32, copy=True)
+    cr[:, :3] += (0.2 * (up[:, 3:6] - 0.5)).astype(np.float32)
+    t.sphere_color = col
+    t.sphere_center_radius = cr
+    return t, o
