@@ -289,6 +289,9 @@ __global__ void __launch_bounds__(128) k_adj_shade(Params p, DScene s, AdjBufs b
           weight[0] = 1.0f; weight[1] = weight[2] = 0.0f;
         }
         const float gObs = -gOpen / float(p.aoSamples);
+        f3 blo, bhi;
+        aoBox(O, R, blo, bhi);
+        const int start = boxStartNode(ts, blo, bhi);
         float obsSum = 0.0f;
         f3 gT{0.0f, 0.0f, 0.0f}, gB{0.0f, 0.0f, 0.0f};
         float gR = 0.0f;
@@ -309,11 +312,12 @@ __global__ void __launch_bounds__(128) k_adj_shade(Params p, DScene s, AdjBufs b
           ++traced;
           if (!p.aoEnhanced) {
             Hit h;
-            if (traverse<false, kMaskSphere, true>(ts, Ray{O, dir, eps, R}, h, ovf, nullptr, true)) obsSum += 1.0f;
+            if (traverse<false, kMaskSphere, true>(ts, Ray{O, dir, eps, R}, h, ovf, nullptr, true, start))
+              obsSum += 1.0f;
             continue;
           }
           Hit h;
-          if (!traverse<false, kMaskSphere, false>(ts, Ray{O, dir, eps, R}, h, ovf, nullptr, false)) continue;
+          if (!traverse<false, kMaskSphere, false>(ts, Ray{O, dir, eps, R}, h, ovf, nullptr, false, start)) continue;
           const float th = h.t;
           float per = 0.0f, dPerDt = 0.0f, dPerDR = 0.0f;
           for (int q = 0; q < K; ++q) {

@@ -147,8 +147,15 @@ __global__ void __launch_bounds__(128) k_surface(Params p1, DScene s1, Batch bt,
       f3 ng = dot(sf.Ng, sf.N) < 0.0f ? neg(sf.Ng) : sf.Ng;
       ng = safeNormalize(ng, sf.N);
       const f3 O = sf.P + ng * sf.secEps;
+      // subtree that holds everything the hit's AO rays can meet
+      int start = 0;
+      if (sf.aoOn) {
+        f3 lo, hi;
+        aoBox(O, p.aoDistance, lo, hi);
+        start = boxStartNode(travOf(s), lo, hi);
+      }
       b.surfA[i] = make_float4(O.x, O.y, O.z, sf.secEps);
-      b.surfB[i] = make_float4(sf.N.x, sf.N.y, sf.N.z, 0.0f);
+      b.surfB[i] = make_float4(sf.N.x, sf.N.y, sf.N.z, __int_as_float(start));
       // flags: 1 hit, 2 casts AO, 4 casts shadows; bits 8.. the frame index
       const uint32_t flags = 1u | (sf.aoOn ? 2u : 0u) | (sf.shOn ? 4u : 0u) | (uint32_t(f) << 8);
       b.surfC[i] = make_uint2(gpix, flags);
@@ -169,6 +176,7 @@ struct OccRay {
   bool anyHit;   // binary visibility (false: nearest t, enhanced AO)
   bool grazing;  // AO sample below the 0.01 cosine: counts as occluded
   bool ao;       // this is an AO ray of an AO-receiving hit
+  int start;     // traversal start node (-1: provably no hit)
 };
 
 UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, uint32_t pix, uint32_t flags, int j) {
@@ -177,6 +185,7 @@ UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, uint32_
   o.anyHit = true;
   o.grazing = false;
   o.ao = false;
+  o.start = 0;
   const LightD* lights = b.lights + p.lightOff;
   const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
   const float4 sa = b.surfA[slot], sb = b.surfB[slot];
@@ -191,6 +200,7 @@ UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, uint32_
       o.grazing = dot(dir, N) < 0.01f;
       o.trace = !o.grazing;
       o.anyHit = !p.aoEnhanced;
+      o.start = __float_as_int(sb.w);
       tfar = p.aoDistance;
     }
   } else if (flags & 4u) {
@@ -250,8 +260,8 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p1, DScene s1
       h.t = kInfF;
       if (o.trace) {
         const TravScene ts = travOf(s);
-        hit = p.aoEnhanced ? traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit)
-                           : traverse<COUNT, KM, true>(ts, o.r, h, ovf, &cnt, true);
+        hit = p.aoEnhanced ? traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit, o.start)
+                           : traverse<COUNT, KM, true>(ts, o.r, h, ovf, &cnt, true, o.start);
         traced = 1;
       }
       occlusionWrite(p, b, R, aoStride, slot, j, o, hit, h.t);
@@ -311,14 +321,15 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p1
           else o.trace = o.grazing = o.ao = false;
           if (j >= p.raysPerHit) {
             // stride padding of a frame with fewer rays per hit: nothing to do
-          } else if (o.trace && s.primCount > 0) {
+          } else if (o.trace && s.primCount > 0 && o.start >= 0) {
             ts = travOf(s);
             inv = safeInv(o.r.dir);
             if (KM & kMaskMesh) pre = triPre(o.r.dir);
-            travInit(o.r, st, best);
+            travInit(o.r, st, best, o.start);
             active = true;
             ++traced;
           } else {
+            if (o.trace) ++traced;
             occlusionWrite(p, b, R, aoStride, slot, j, o, false, kInfF);
           }
         }

@@ -132,8 +132,8 @@ struct TravState {
   uint32_t stack[kStackDepth];   // group entries: (childBase << 8) | slot mask
 };
 
-UBR_D void travInit(const Ray& r, TravState& st, Hit& best) {
-  st.node = 0;
+UBR_D void travInit(const Ray& r, TravState& st, Hit& best, int start = 0) {
+  st.node = start;
   st.sp = 0;
   st.steps = 0;
   st.tmax = r.tfar;
@@ -250,17 +250,63 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
 // Whole traversal of one ray (one thread per ray).
 template <bool COUNT = false, int KM = kMaskAll, bool ALWAYS_ANY = false>
 __device__ bool traverse(const TravScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt,
-                         const bool any) {
+                         const bool any, int start = 0) {
   best.ref = kInvalid;
-  if (s.primCount == 0) return false;
+  if (s.primCount == 0 || start < 0) return false;
   const f3 inv = safeInv(r.dir);
   TriPre pre;
   if (KM & kMaskMesh) pre = triPre(r.dir);
   TravState st;
-  travInit(r, st, best);
+  travInit(r, st, best, start);
   while (!travStep<COUNT, KM, ALWAYS_ANY>(s, r, inv, pre, st, best, overflow, cnt, any)) {
   }
   return best.ref != kInvalid;
+}
+
+// Start node for rays that stay inside the box [lo, hi] (AO rays: origin
+// +- the AO distance): descend from the root while exactly one child's
+// quantised box overlaps the box.  Every sibling passed over is disjoint
+// from the box, so no primitive outside the returned subtree can meet such
+// a ray, and its traversal may start there with the same result.  -1: no
+// box overlaps, nothing can be hit.
+UBR_D int boxStartNode(const TravScene& s, f3 lo, f3 hi) {
+  if (s.primCount == 0) return -1;
+  int node = 0;
+  for (int depth = 0; depth < kStackDepth; ++depth) {
+    const float4* nd = s.wnodes + kWideF4 * node;
+    const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3), n4 = __ldg(nd + 4);
+    const uint32_t hdr = __float_as_uint(n0.w);
+    const float sx = __uint_as_float((hdr & 0xFFu) << 23);
+    const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23);
+    const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23);
+    const int nInt = int((hdr >> 24) & 0xFu), nCh = int(hdr >> 28);
+    int count = 0, only = -1;
+    for (int k = 0; k < nCh; ++k) {
+      const int w = k >> 2, b = k & 3;
+      const float lx = fmaf(byteToFloat(__float_as_uint(w ? n2.y : n2.x), b), sx, n0.x);
+      const float ly = fmaf(byteToFloat(__float_as_uint(w ? n2.w : n2.z), b), sy, n0.y);
+      const float lz = fmaf(byteToFloat(__float_as_uint(w ? n3.y : n3.x), b), sz, n0.z);
+      const float hx = fmaf(byteToFloat(__float_as_uint(w ? n3.w : n3.z), b), sx, n0.x);
+      const float hy = fmaf(byteToFloat(__float_as_uint(w ? n4.y : n4.x), b), sy, n0.y);
+      const float hz = fmaf(byteToFloat(__float_as_uint(w ? n4.w : n4.z), b), sz, n0.z);
+      if (lx <= hi.x && hx >= lo.x && ly <= hi.y && hy >= lo.y && lz <= hi.z && hz >= lo.z) {
+        ++count;
+        only = k;
+      }
+    }
+    if (count == 0) return -1;
+    if (count > 1 || only >= nInt) return node;
+    node = int(__float_as_uint(n1.x)) + only;
+  }
+  return node;
+}
+
+// The box holding every AO ray of a hit: origin O, length up to R (unit
+// directions), with a relative margin for rounding.
+UBR_D void aoBox(f3 O, float R, f3& lo, f3& hi) {
+  const float m = R * 1.001f + 1.0e-6f * fmaxf(fmaxf(fabsf(O.x), fabsf(O.y)), fabsf(O.z));
+  lo = f3{O.x - m, O.y - m, O.z - m};
+  hi = f3{O.x + m, O.y + m, O.z + m};
 }
 
 // Shading surface of a hit (hit_shader.hpp:147-341 attribute + normal logic).
