@@ -72,6 +72,7 @@ struct Batch {
   const uint32_t* outOffs = nullptr;  // frames' outOff, ascending
   int nFrames = 0;
   uint32_t R = 0;         // AO/shadow-ray stride per hit (max over frames)
+  uint32_t aoSplit = 0;   // ray index where shadow rays start in the ray order (min AO count)
   uint32_t aoStride = 0;  // enhanced-AO t stride per hit (max over frames)
 };
 
@@ -237,6 +238,23 @@ UBR_D void occlusionWrite(const Params& p, const Bufs& b, uint64_t R, uint64_t a
   b.occ[uint64_t(slot) * R + j] = res;
 }
 
+// Ray (queue position, ray index) of global ray id `rid` among nq hits with
+// R rays each: AO rays first, hit-major (a warp holds whole hits' AO samples,
+// rays from one origin), then the shadow rays, ray-index-major (a warp holds
+// one light's rays of 32 neighbouring hits, one direction).  A bijection onto
+// [0, nq) x [0, R) for any split A.
+UBR_D void occRayOf(uint64_t rid, uint32_t nq, uint64_t R, uint64_t A, uint32_t& q, int& j) {
+  const uint64_t nAo = uint64_t(nq) * A;
+  if (rid < nAo) {
+    q = uint32_t(rid / A);
+    j = int(rid % A);
+  } else {
+    const uint64_t t = rid - nAo;
+    q = uint32_t(t % nq);
+    j = int(A + t / nq);
+  }
+}
+
 // One thread per AO / shadow ray.
 template <bool COUNT, int KM, bool BATCH>
 __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p1, DScene s1, Batch bt, Bufs b, uint32_t n) {
@@ -247,8 +265,10 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p1, DScene s1
   uint32_t traced = 0, ovf = 0;
   const uint32_t nq = *(volatile const uint32_t*)(b.counter + 1);
   if (tid < uint64_t(nq) * R) {
-    const uint32_t slot = b.occQueue[uint32_t(tid / R)];
-    const int j = int(tid % R);
+    uint32_t q;
+    int j;
+    occRayOf(tid, nq, R, BATCH ? uint64_t(bt.aoSplit) : uint64_t(p1.aoSamples), q, j);
+    const uint32_t slot = b.occQueue[q];
     const uint2 sc = b.surfC[slot];
     const int f = BATCH ? int(sc.y >> 8) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
@@ -290,7 +310,8 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p1
   const uint64_t R = BATCH ? uint64_t(bt.R) : uint64_t(p1.raysPerHit);
   const uint64_t aoStride = BATCH ? uint64_t(bt.aoStride) : uint64_t(p1.aoSamples);
   int f = 0;
-  const uint64_t total = uint64_t(*(volatile const uint32_t*)(b.counter + 1)) * R;
+  const uint32_t nqq = *(volatile const uint32_t*)(b.counter + 1);
+  const uint64_t total = uint64_t(nqq) * R;
   const int lane = threadIdx.x & 31;
   bool active = false, exhausted = total == 0;
   uint32_t slot = 0;
@@ -311,8 +332,9 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p1
       if (!active) {
         const uint64_t rid = base + uint64_t(__popc(idle & ((1u << lane) - 1u)));
         if (rid < total) {
-          slot = b.occQueue[uint32_t(rid / R)];
-          j = int(rid % R);
+          uint32_t q;
+          occRayOf(rid, nqq, R, BATCH ? uint64_t(bt.aoSplit) : uint64_t(p1.aoSamples), q, j);
+          slot = b.occQueue[q];
           const uint2 sc = b.surfC[slot];
           f = BATCH ? int(sc.y >> 8) : 0;
           const Params& p = BATCH ? bt.frames[f].p : p1;
@@ -890,7 +912,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   std::vector<LightD> lights;
   std::vector<uint32_t> pixOffs(nf), outOffs(nf);
   uint64_t npix64 = 0, nout64 = 0;
-  uint32_t R = 0, aoStride = 0;
+  uint32_t R = 0, aoStride = 0, aoMin = 0xFFFFFFFFu;
   int km = 0, maxIters = 1;
   bool secondary = false, enhanced = false, singleLayer = true;
   for (size_t f = 0; f < nf; ++f) {
@@ -908,6 +930,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     npix64 += uint64_t(p.W) * uint64_t(p.H);
     nout64 += uint64_t(p.outW) * uint64_t(p.outH);
     R = std::max(R, uint32_t(p.raysPerHit));
+    aoMin = std::min(aoMin, uint32_t(p.aoSamples));
     if (p.aoEnhanced && p.aoSamples > 0) {
       enhanced = true;
       aoStride = std::max(aoStride, uint32_t(p.aoSamples));
@@ -963,6 +986,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     bt.outOffs = doffs + nf;
     bt.nFrames = int(nf);
     bt.R = R;
+    bt.aoSplit = aoMin;
     bt.aoStride = aoStride;
   }
   if (st != UBR_OK) return st;
