@@ -32,15 +32,14 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+from umbreon_gb300 import replicas  # noqa: E402
+
 METRIC = "ms/frame & Mrays/s (batched vs per-frame GPU) at >=45 dB PSNR; adjoint ms/iter"
 WORKLOAD = "ball_and_stick_20k_1920x1080_ss2_ao16_2lights_shadows_fog"
 
 
 def _dist():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return replicas.env_ranks()
 
 
 class ClockSampler:
@@ -428,12 +427,10 @@ def run_ours(args):
             kernels += fr.kernels
         torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
-    if ws > 1:
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    # replicas: the job's time is the slowest rank's, its rays those of all ranks
+    rays_s, total_ms = replicas.job_throughput(rays, total_ms, device=f"cuda:{local}")
     ms_frame = total_ms / args.steps
-    value = rays * ws / (total_ms / 1e3) / 1e6
+    value = rays_s / 1e6
 
     # roofline of the dominant kernel (per launch = per frame here)
     names = ["trace_closest", "surface", "trace_occlusion", "shade", "post"]
