@@ -268,7 +268,7 @@ def secondary_workloads(args, flush):
     from umbreon_gb300.autotune import autotune
     out = {}
     threads = os.cpu_count() or 1
-    ctx = Context(0)
+    ctx = Context(0, bvh_builder=args.builder)
     # workload 0
     sc, opt = scenes.space_filling()
     b = ctx.build(sc)
@@ -301,13 +301,14 @@ def secondary_workloads(args, flush):
     ctx.close()
     # workload 3: batched vs one frame per call
     bases, items = scenes.turntable_batch()
-    tune = autotune(items[0][1], items[0][2])
+    tune = autotune(items[0][1], items[0][2], pixels=512 * 512)
     res = {"autotune": tune}
     for label, its in (("turntable_64_mixed", items),
                        ("turntable_64_small_256", [(si, sc2, _resized(o, 256)) for si, sc2, o in items])):
         entry = {}
         for mode, graphs in (("batched", True), ("per_frame_graph", True), ("per_frame_no_graph", False)):
-            cx = Context(0, bvh_leaf_max=tune["bvh_leaf_max"], trace_mode=tune["trace_mode"], graphs=graphs)
+            cx = Context(0, bvh_leaf_max=tune["bvh_leaf_max"], trace_mode=tune["trace_mode"], graphs=graphs,
+                         bvh_builder=args.builder or tune["bvh_builder"])
             built = [cx.build(bs) for bs in bases]
             descs, outs, frames = [], [], []
             for si, sc2, o in its:
@@ -382,7 +383,7 @@ def run_ours(args):
         opt.width, opt.height = (int(x) for x in args.frame.lower().split("x"))
     if args.ss:
         opt.supersample = args.ss
-    ctx = Context(local, bvh_leaf_max=args.leaf_max, trace_mode=args.trace_mode)
+    ctx = Context(local, bvh_leaf_max=args.leaf_max, trace_mode=args.trace_mode, bvh_builder=args.builder)
     built = ctx.build(sc)
     info = built.info()
     import ctypes as C
@@ -524,6 +525,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--builder", type=int, default=0, help="BVH builder (0 library default, 1 radix tree, 2 PLOC)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the other workloads (space filling, "
                     "molecular surface, batched turntable)")
     ap.add_argument("--leaf-max", type=int, default=0, help="wide-BVH leaf size 1..3 (0 = library default)")

@@ -254,7 +254,11 @@ typedef struct ubr_context_desc {
   /* 1 = launch every kernel on its own instead of replaying single-layer
    * frames from a captured CUDA graph (0 = graphs, the default) */
   uint32_t disable_graphs;
-  uint32_t reserved[5];
+  /* BVH builder (0 = library default): 1 = Karras radix tree over Morton
+   * codes, 2 = locally-ordered clustering (PLOC) over the same Morton order;
+   * leaf sizes above 1 always use the radix tree */
+  uint32_t bvh_builder;
+  uint32_t reserved[4];
 } ubr_context_desc;
 
 const char* ubr_status_string(ubr_status s);

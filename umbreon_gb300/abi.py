@@ -125,7 +125,8 @@ FRAME_COUNT = 2
 class ContextDesc(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("device", C.c_int32), ("arena_bytes", C.c_uint64),
                 ("stream", C.c_void_p), ("bvh_leaf_max", C.c_uint32), ("trace_mode", C.c_uint32),
-                ("disable_graphs", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+                ("disable_graphs", C.c_uint32), ("bvh_builder", C.c_uint32),
+                ("reserved", C.c_uint32 * 4)]
 
 
 class SceneInfo(C.Structure):

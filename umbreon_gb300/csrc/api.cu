@@ -136,6 +136,13 @@ ubr_status ubr_context_create(ubr_context** out, const ubr_context_desc* desc) {
     x.traceMode = int(desc->trace_mode);
   }
   if (desc && desc->disable_graphs) x.useGraphs = false;
+  if (desc && desc->bvh_builder) {
+    if (desc->bvh_builder > 2) {
+      delete c;
+      return UBR_INVALID_ARGUMENT;
+    }
+    x.builder = int(desc->bvh_builder);
+  }
   if (cudaSetDevice(dev) != cudaSuccess) {
     delete c;
     return UBR_CUDA_ERROR;

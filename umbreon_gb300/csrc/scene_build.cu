@@ -484,7 +484,7 @@ __device__ __forceinline__ void writeChildBox(float4* nodes, int p, int side, fl
 __global__ void k_refit(BuildIn in, int n, int idxBits, const unsigned long long* keys,
                         const float4* boxLo, const float4* boxHi, const float4* rcClip,
                         float4* nodes, const int* leafParent, const int* nodeParent, int* counters,
-                        uint32_t* leafRef, float4* leafGeo) {
+                        uint32_t* leafRef, float4* leafGeo, int refit) {
   const int sIdx = blockIdx.x * blockDim.x + threadIdx.x;
   if (sIdx >= n) return;
   const uint32_t g = uint32_t(keys[sIdx] & ((1ull << idxBits) - 1ull));
@@ -514,7 +514,7 @@ __global__ void k_refit(BuildIn in, int n, int idxBits, const unsigned long long
       lg[2] = make_float4(a.x, a.y, a.z, L);
     }
   }
-  if (n == 1) return;
+  if (n == 1 || !refit) return;
   const float4 bl = boxLo[g], bh = boxHi[g];
   float3 lo = make_float3(bl.x, bl.y, bl.z), hi = make_float3(bh.x, bh.y, bh.z);
   int pinfo = leafParent[sIdx];
@@ -531,6 +531,110 @@ __global__ void k_refit(BuildIn in, int n, int idxBits, const unsigned long long
     hi = make_float3(fmaxf(a.y, b.y), fmaxf(a.w, b.w), fmaxf(z.y, z.w));
     pinfo = nodeParent[p];
   }
+}
+
+// Locally-ordered clustering (PLOC: Meister and Bittner, "Parallel
+// Locally-Ordered Clustering for Bounding Volume Hierarchy Construction",
+// IEEE TVCG 2018).  Clusters start as the Morton-sorted leaves; each round
+// every cluster finds its nearest neighbour within kPlocRadius positions by
+// the surface area of the merged box, mutual nearest pairs merge into a new
+// binary node (written in the radix tree's node format, child boxes
+// included, so no refit is needed) and the cluster list is compacted in
+// order.  The pair with the smallest distance (ties to the lowest indices)
+// is always mutual, so every round merges at least once.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocBlock = 256;
+
+__device__ __forceinline__ float unionArea(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+  const float ex = fmaxf(ahi.x, bhi.x) - fminf(alo.x, blo.x);
+  const float ey = fmaxf(ahi.y, bhi.y) - fminf(alo.y, blo.y);
+  const float ez = fmaxf(ahi.z, bhi.z) - fminf(alo.z, blo.z);
+  return ex * ey + ey * ez + ez * ex;
+}
+
+__global__ void k_ploc_init(int n, int idxBits, const unsigned long long* keys, const float4* primLo,
+                            const float4* primHi, int* code, float4* lo, float4* hi, int* cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t g = uint32_t(keys[i] & ((1ull << idxBits) - 1ull));
+  code[i] = ~i;
+  lo[i] = primLo[g];
+  hi[i] = primHi[g];
+  cnt[i] = 1;
+}
+
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(int nc, const float4* lo, const float4* hi, int* nn) {
+  __shared__ float4 sLo[kPlocBlock + 2 * kPlocRadius], sHi[kPlocBlock + 2 * kPlocRadius];
+  const int b0 = blockIdx.x * kPlocBlock - kPlocRadius;
+  for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += kPlocBlock) {
+    const int j = b0 + k;
+    if (j >= 0 && j < nc) {
+      sLo[k] = lo[j];
+      sHi[k] = hi[j];
+    }
+  }
+  __syncthreads();
+  const int i = blockIdx.x * kPlocBlock + threadIdx.x;
+  if (i >= nc) return;
+  const int si = threadIdx.x + kPlocRadius;
+  const float4 ilo = sLo[si], ihi = sHi[si];
+  float best = __int_as_float(0x7F800000);
+  int bestJ = -1;
+  const int j0 = max(0, i - kPlocRadius), j1 = min(nc - 1, i + kPlocRadius);
+  for (int j = j0; j <= j1; ++j) {
+    if (j == i) continue;
+    const float d = unionArea(ilo, ihi, sLo[j - b0], sHi[j - b0]);
+    if (d < best) {
+      best = d;
+      bestJ = j;
+    }
+  }
+  nn[i] = bestJ;
+}
+
+__device__ __forceinline__ void writeBinNode(float4* nodes, int node, int c0, float4 lo0, float4 hi0, int c1,
+                                             float4 lo1, float4 hi1) {
+  float4* nd = nodes + kNodeF4 * node;
+  nd[0] = make_float4(lo0.x, hi0.x, lo0.y, hi0.y);
+  nd[1] = make_float4(lo1.x, hi1.x, lo1.y, hi1.y);
+  nd[2] = make_float4(lo0.z, hi0.z, lo1.z, hi1.z);
+  nd[3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.0f, 0.0f);
+}
+
+__global__ void k_ploc_merge(int nc, const int* nn, int* code, float4* lo, float4* hi, int* cnt, float4* nodes,
+                             int2* ranges, int* nodeCounter, int* valid) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const int j = nn[i];
+  const bool mutual = j >= 0 && nn[j] == i;
+  if (mutual && i < j) {
+    const int node = atomicAdd(nodeCounter, 1);
+    const float4 l0 = lo[i], h0 = hi[i], l1 = lo[j], h1 = hi[j];
+    writeBinNode(nodes, node, code[i], l0, h0, code[j], l1, h1);
+    const int c = cnt[i] + cnt[j];
+    ranges[node] = make_int2(0, c - 1);  // only the primitive count is read
+    code[i] = node;
+    lo[i] = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.0f);
+    hi[i] = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.0f);
+    cnt[i] = c;
+    valid[i] = 1;
+  } else {
+    valid[i] = (mutual && i > j) ? 0 : 1;
+  }
+}
+
+__global__ void k_ploc_compact(int nc, const int* valid, const int* pos, const int* code, const float4* lo,
+                               const float4* hi, const int* cnt, int* code2, float4* lo2, float4* hi2, int* cnt2,
+                               int* newCount) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  if (i == nc - 1) *newCount = pos[i] + valid[i];
+  if (!valid[i]) return;
+  const int o = pos[i];
+  code2[o] = code[i];
+  lo2[o] = lo[i];
+  hi2[o] = hi[i];
+  cnt2[o] = cnt[i];
 }
 
 __device__ __forceinline__ void binChild(const float4* nodes, int node, int side, int& code, float3& lo, float3& hi) {
@@ -829,18 +933,67 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
     if ((st = scratchGet(c, 8, tmpBytes, &pTmp)) != UBR_OK) return fail(st);
     UBR_CUDA(c, cub::DeviceRadixSort::SortKeys(pTmp, tmpBytes, (unsigned long long*)pKeys,
                                                (unsigned long long*)pKeys2, int(n), 0, 30 + idxBits, c->stream));
-    if (n > 1)
+    const bool ploc = n > 1 && c->builder == 2 && c->leafMax == 1;
+    if (n > 1 && !ploc)
       k_hierarchy<<<int((n - 1 + TB - 1) / TB), TB, 0, c->stream>>>(int(n), (const unsigned long long*)pKeys2,
                                                                    (float4*)pNodes, (int*)pLeafP, (int*)pNodeP,
                                                                    (int2*)pRange);
+    // leaf records in Morton order (+ the radix tree's bottom-up refit)
     k_refit<<<grid, TB, 0, c->stream>>>(in, int(n), idxBits, (const unsigned long long*)pKeys2,
                                         (const float4*)pLo, (const float4*)pHi, v.rcClip, (float4*)pNodes,
                                         (const int*)pLeafP, (const int*)pNodeP, (int*)pCnt, (uint32_t*)pRef,
-                                        (float4*)pGeo);
+                                        (float4*)pGeo, ploc ? 0 : 1);
     UBR_CUDA(c, cudaGetLastError());
+    int rootCodeDev = -1;  // root node of the PLOC tree (the radix tree's root is node 0)
+    if (ploc) {
+      void *pCode[2], *pCLo[2], *pCHi[2], *pCCnt[2], *pNn, *pValid, *pPos, *pPc;
+      for (int k = 0; k < 2; ++k) {
+        if ((st = scratchGet(c, 40 + 4 * k, sizeof(int) * n, &pCode[k])) != UBR_OK) return fail(st);
+        if ((st = scratchGet(c, 41 + 4 * k, sizeof(float4) * n, &pCLo[k])) != UBR_OK) return fail(st);
+        if ((st = scratchGet(c, 42 + 4 * k, sizeof(float4) * n, &pCHi[k])) != UBR_OK) return fail(st);
+        if ((st = scratchGet(c, 43 + 4 * k, sizeof(int) * n, &pCCnt[k])) != UBR_OK) return fail(st);
+      }
+      if ((st = scratchGet(c, 48, sizeof(int) * n, &pNn)) != UBR_OK) return fail(st);
+      if ((st = scratchGet(c, 49, sizeof(int) * n, &pValid)) != UBR_OK) return fail(st);
+      if ((st = scratchGet(c, 59, sizeof(int) * n, &pPos)) != UBR_OK) return fail(st);
+      if ((st = scratchGet(c, 9, 64, &pPc)) != UBR_OK) return fail(st);
+      size_t scanBytes = 0;
+      cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, (const int*)pValid, (int*)pPos, int(n), c->stream);
+      void* pScan;
+      if ((st = scratchGet(c, 10, scanBytes, &pScan)) != UBR_OK) return fail(st);
+      UBR_CUDA(c, cudaMemsetAsync(pPc, 0, 64, c->stream));
+      k_ploc_init<<<grid, TB, 0, c->stream>>>(int(n), idxBits, (const unsigned long long*)pKeys2,
+                                              (const float4*)pLo, (const float4*)pHi, (int*)pCode[0],
+                                              (float4*)pCLo[0], (float4*)pCHi[0], (int*)pCCnt[0]);
+      int nc = int(n), cur = 0, rounds = 0;
+      int* hostPc = static_cast<int*>(c->pinned);
+      while (nc > 1) {
+        const int g = (nc + kPlocBlock - 1) / kPlocBlock;
+        k_ploc_nn<<<g, kPlocBlock, 0, c->stream>>>(nc, (const float4*)pCLo[cur], (const float4*)pCHi[cur],
+                                                   (int*)pNn);
+        k_ploc_merge<<<g, kPlocBlock, 0, c->stream>>>(nc, (const int*)pNn, (int*)pCode[cur], (float4*)pCLo[cur],
+                                                      (float4*)pCHi[cur], (int*)pCCnt[cur], (float4*)pNodes,
+                                                      (int2*)pRange, (int*)pPc, (int*)pValid);
+        UBR_CUDA(c, cub::DeviceScan::ExclusiveSum(pScan, scanBytes, (const int*)pValid, (int*)pPos, nc,
+                                                  c->stream));
+        k_ploc_compact<<<g, kPlocBlock, 0, c->stream>>>(
+            nc, (const int*)pValid, (const int*)pPos, (const int*)pCode[cur], (const float4*)pCLo[cur],
+            (const float4*)pCHi[cur], (const int*)pCCnt[cur], (int*)pCode[cur ^ 1], (float4*)pCLo[cur ^ 1],
+            (float4*)pCHi[cur ^ 1], (int*)pCCnt[cur ^ 1], static_cast<int*>(pPc) + 1);
+        UBR_CUDA(c, cudaGetLastError());
+        UBR_CUDA(c, cudaMemcpyAsync(hostPc, pPc, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        UBR_CUDA(c, cudaStreamSynchronize(c->stream));
+        const int next = hostPc[1];
+        if (!(next < nc) || ++rounds > (1 << 20)) return fail(setError(c, UBR_INTERNAL, "PLOC did not converge"));
+        nc = next;
+        cur ^= 1;
+      }
+      if (hostPc[0] != int(n) - 1) return fail(setError(c, UBR_INTERNAL, "PLOC node count mismatch"));
+      rootCodeDev = int(n) - 2;  // the last merge makes the root
+    }
     // collapse to 8-wide, level by level: cursors = {wide nodes, leaf prims, next work}
     {
-      const int rootCode = n > 1 ? 0 : ~0;
+      const int rootCode = n > 1 ? (rootCodeDev >= 0 ? rootCodeDev : 0) : ~0;
       const int zero = 0;
       const int cur0[3] = {1, 0, 0};
       UBR_CUDA(c, cudaMemcpyAsync(pCur, cur0, sizeof(cur0), cudaMemcpyHostToDevice, c->stream));

@@ -24,6 +24,7 @@ struct Context {
   bool ownStream = false;
   uint64_t arenaCap = 0;     // 0 = unlimited
   int leafMax = 1;           // wide-BVH leaf size (1..kWideLeafMax); 1 measured fastest
+  int builder = 1;           // binary tree before the 8-wide collapse: 1 Karras radix tree, 2 PLOC
   int traceMode = 1;         // occlusion kernel: 1 one thread per ray (measured faster), 2 persistent
   uint64_t arenaUsed = 0;
   std::string lastError;
