@@ -268,19 +268,30 @@ def secondary_workloads(args, flush):
     from umbreon_gb300.autotune import autotune
     out = {}
     threads = os.cpu_count() or 1
-    ctx = Context(0, bvh_builder=args.builder)
+
+    def tuned(sc, opt):
+        """Context with the knobs given on the command line, else autotuned."""
+        if args.builder or args.leaf_max or args.trace_mode:
+            return Context(0, bvh_leaf_max=args.leaf_max, trace_mode=args.trace_mode, bvh_builder=args.builder), None
+        t = autotune(sc, opt, pixels=512 * 512)
+        return Context(0, bvh_leaf_max=t["bvh_leaf_max"], trace_mode=t["trace_mode"],
+                       bvh_builder=t["bvh_builder"]), {k: t[k] for k in ("bvh_builder", "bvh_leaf_max", "trace_mode")}
+
     # workload 0
     sc, opt = scenes.space_filling()
+    ctx, tn = tuned(sc, opt)
     b = ctx.build(sc)
     ms, rays, ph, layers = _device_frames(ctx, b, sc, opt, 10, 3, flush)
     b.release()
     cpu = _cpu_full_or_band(sc, opt, threads, 2.0) if not args.no_cpu else None
     out["space_filling_2k_640x480"] = {"ms_per_frame": round(ms, 4), "Mrays_s": round(rays / ms / 1e3, 1),
-                                       "phase_ms": ph, "cpu": cpu}
+                                       "phase_ms": ph, "cpu": cpu, "traversal": tn}
+    ctx.close()
     # workload 2
     t0 = time.perf_counter()
     sc, opt = scenes.molecular_surface()
     gen_s = time.perf_counter() - t0
+    ctx, tn = tuned(sc, opt)
     b = ctx.build(sc)
     info = b.info()
     ms, rays, ph, layers = _device_frames(ctx, b, sc, opt, 3, 3, flush)
@@ -290,13 +301,16 @@ def secondary_workloads(args, flush):
                                      "bvh_build_ms": round(info["build_ms"], 1), "generate_s": round(gen_s, 1),
                                      "ms_per_frame": round(ms, 3), "Mrays_s": round(rays / ms / 1e3, 1),
                                      "rays_per_frame": int(rays), "layers": int(layers), "phase_ms": ph,
-                                     "cpu": cpu}
+                                     "cpu": cpu, "traversal": tn}
+    ctx.close()
     # workload 4: forward frame vs adjoint (device buffers, L2 flushed)
     sc, opt = scenes.differentiable()
+    ctx, tn = tuned(sc, opt)
     b = ctx.build(sc)
     ms_f, rays_f, ph, _ = _device_frames(ctx, b, sc, opt, 5, 3, flush)
     out["differentiable_100k_1024"] = _adjoint_timing(ctx, b, sc, opt, flush, _device_frames.render_ms, rays_f)
     out["differentiable_100k_1024"]["forward_phase_ms"] = ph
+    out["differentiable_100k_1024"]["traversal"] = tn
     b.release()
     ctx.close()
     # workload 3: batched vs one frame per call
@@ -383,7 +397,14 @@ def run_ours(args):
         opt.width, opt.height = (int(x) for x in args.frame.lower().split("x"))
     if args.ss:
         opt.supersample = args.ss
-    ctx = Context(local, bvh_leaf_max=args.leaf_max, trace_mode=args.trace_mode, bvh_builder=args.builder)
+    # traversal knobs: as given, else what the autotuner picks on a downscaled frame
+    tune = None
+    builder, leaf_max, trace_mode = args.builder, args.leaf_max, args.trace_mode
+    if not (builder or leaf_max or trace_mode):
+        from umbreon_gb300.autotune import autotune
+        tune = autotune(sc, opt, device=local, pixels=512 * 512)
+        builder, leaf_max, trace_mode = tune["bvh_builder"], tune["bvh_leaf_max"], tune["trace_mode"]
+    ctx = Context(local, bvh_leaf_max=leaf_max, trace_mode=trace_mode, bvh_builder=builder)
     built = ctx.build(sc)
     info = built.info()
     import ctypes as C
@@ -500,6 +521,8 @@ def run_ours(args):
                        "frame": f"{opt.width}x{opt.height} ss{opt.supersample}",
                        "primitives": info["prim_count"], "bvh_nodes": info["bvh_nodes"],
                        "l2": "flushed (256 MB write) before every timed frame",
+                       "traversal": {"bvh_builder": builder, "bvh_leaf_max": leaf_max, "trace_mode": trace_mode,
+                                     "autotuned": tune["table"] if tune else None},
                        "parallelism": f"replicas x{ws}"},
             "ms_per_frame": round(ms_frame, 3),
             "phase_ms_per_frame": {n: round(v / args.steps, 3) for n, v in zip(names, phase)},
