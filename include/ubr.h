@@ -249,7 +249,8 @@ typedef struct ubr_context_desc {
    * holds (1..3); smaller leaves mean more nodes and fewer primitive tests */
   uint32_t bvh_leaf_max;
   /* occlusion-ray kernel (0 = library default): 1 = one thread per ray,
-   * 2 = persistent warps that refill idle lanes with new rays */
+   * 2 = persistent warps that refill idle lanes with new rays, 3 = resident
+   * grid striding over the rays with the top BVH levels in shared memory */
   uint32_t trace_mode;
   /* 1 = launch every kernel on its own instead of replaying single-layer
    * frames from a captured CUDA graph (0 = graphs, the default) */

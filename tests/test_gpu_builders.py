@@ -30,3 +30,20 @@ def test_builders_render_identically(name):
         ctx.close()
     assert np.array_equal(out[1][1], out[2][1])
     assert np.array_equal(out[1][0], out[2][0])
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_occlusion_kernels_render_identically(name):
+    """The three occlusion kernels (one thread per ray, persistent refill,
+    resident grid with shared-memory top levels) give the same frame."""
+    from umbreon_gb300.api import Context
+    sc, opt = CASES[name]()
+    out = {}
+    for mode in (1, 2, 3):
+        ctx = Context(0, trace_mode=mode)
+        b = ctx.build(sc)
+        out[mode] = ctx.render(b, sc, opt).color.copy()
+        b.release()
+        ctx.close()
+    assert np.array_equal(out[1], out[2])
+    assert np.array_equal(out[1], out[3])

@@ -18,7 +18,7 @@ from .api import Context
 
 
 def autotune(scene, opt, device: int = 0, pixels: int = 256 * 256, repeats: int = 3,
-             leaf_sizes=(1, 2, 3), trace_modes=(1, 2), builders=(1, 2)):
+             leaf_sizes=(1, 2, 3), trace_modes=(1, 2, 3), builders=(1, 2)):
     small = copy.copy(opt)
     ss = max(1, opt.supersample)
     scale = math.sqrt(pixels / float(opt.width * opt.height * ss * ss))

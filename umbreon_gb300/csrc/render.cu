@@ -295,6 +295,54 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p1, DScene s1
   }
 }
 
+// Resident-grid variant: each CTA stages the top wide nodes (root and the two
+// levels below) in shared memory once, then walks the ray list with a grid
+// stride in the same order as k_trace_occlusion.  (Batches mix scenes, so
+// there the nodes are read from global memory.)
+template <bool COUNT, int KM, bool BATCH>
+__global__ void __launch_bounds__(128, 8) k_trace_occlusion_gs(Params p1, DScene s1, Batch bt, Bufs b) {
+  __shared__ float4 sTop[kTopNodes * kWideF4];
+  const int nTop = BATCH ? 0 : min(kTopNodes, int(s1.wideNodes));
+  for (int k = threadIdx.x; k < nTop * kWideF4; k += blockDim.x) sTop[k] = __ldg(&s1.wnodes[k]);
+  __syncthreads();
+  Count cnt;
+  const uint64_t R = BATCH ? uint64_t(bt.R) : uint64_t(p1.raysPerHit);
+  const uint64_t aoStride = BATCH ? uint64_t(bt.aoStride) : uint64_t(p1.aoSamples);
+  uint32_t traced = 0, ovf = 0;
+  const uint32_t nq = *(volatile const uint32_t*)(b.counter + 1);
+  const uint64_t total = uint64_t(nq) * R;
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t tid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; tid < total; tid += stride) {
+    uint32_t q;
+    int j;
+    occRayOf(tid, nq, R, BATCH ? uint64_t(bt.aoSplit) : uint64_t(p1.aoSamples), q, j);
+    const uint32_t slot = b.occQueue[q];
+    const uint2 sc = b.surfC[slot];
+    const int f = BATCH ? int(sc.y >> 8) : 0;
+    const Params& p = BATCH ? bt.frames[f].p : p1;
+    const DScene& s = BATCH ? bt.frames[f].s : s1;
+    if (j < p.raysPerHit) {
+      const OccRay o = occlusionRay(p, b, slot, sc.x - (BATCH ? bt.frames[f].pixOff : 0u), sc.y, j);
+      bool hit = false;
+      Hit h;
+      h.t = kInfF;
+      if (o.trace) {
+        const TravScene ts = travOf(s);
+        hit = p.aoEnhanced ? traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit, o.start, sTop, nTop)
+                           : traverse<COUNT, KM, true>(ts, o.r, h, ovf, &cnt, true, o.start, sTop, nTop);
+        ++traced;
+      }
+      occlusionWrite(p, b, R, aoStride, slot, j, o, hit, h.t);
+    }
+  }
+  warpCount(&b.stats[1], traced);
+  warpCount(&b.stats[3], ovf);
+  if (COUNT) {
+    warpCount(&b.stats[6], cnt.nodes);
+    warpCount(&b.stats[7], cnt.primBytes);
+  }
+}
+
 // Persistent variant: a resident grid whose warps keep their lanes busy.
 // Each lane advances its ray one BVH node per iteration; when at least
 // kRefill lanes of a warp are idle they fetch the next rays of the global
@@ -883,6 +931,22 @@ uint32_t persistentGrid(int device) {
   return uint32_t(g);
 }
 
+uint32_t gridStrideGrid(int device) {
+  static int cached[64] = {};
+  if (device >= 0 && device < 64 && cached[device]) return uint32_t(cached[device]);
+  int sms = 0, perSm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_trace_occlusion_gs<false, kMaskAll, false>, 128, 0);
+  const int g = std::max(1, sms) * std::max(1, perSm);
+  if (device >= 0 && device < 64) cached[device] = g;
+  return uint32_t(g);
+}
+
+void launchOcclusionGridStride(int km, bool count, bool batch, uint32_t grid, int tb, cudaStream_t st,
+                               const Params& p, const DScene& s, const Batch& bt, const Bufs& b) {
+  UBR_KM_DISPATCH(k_trace_occlusion_gs, km, count, batch, grid, tb, st, p, s, bt, b);
+}
+
 void launchOcclusionPersistent(int km, bool count, bool batch, uint32_t grid, int tb, cudaStream_t st,
                                const Params& p, const DScene& s, const Batch& bt, const Bufs& b) {
   UBR_KM_DISPATCH(k_trace_occlusion_persistent, km, count, batch, grid, tb, st, p, s, bt, b);
@@ -1031,6 +1095,8 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       mark(2, true);
       if (c->traceMode == 1) {
         launchOcclusion(km, count, batch, uint32_t((nr + TB - 1) / TB), TB, s, p1, s1, bt, b, n);
+      } else if (c->traceMode == 3) {
+        launchOcclusionGridStride(km, count, batch, gridStrideGrid(c->device), TB, s, p1, s1, bt, b);
       } else {
         UBR_CUDA(c, cudaMemsetAsync(b.cursor, 0, sizeof(unsigned long long), s));
         launchOcclusionPersistent(km, count, batch, persistentGrid(c->device), TB, s, p1, s1, bt, b);

@@ -1016,6 +1016,7 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
         if (++levels > 64) return fail(setError(c, UBR_INTERNAL, "wide BVH collapse did not converge"));
       }
       sc->nodes = uint64_t(hostCur[0]);
+      v.wideNodes = uint32_t(hostCur[0]);
       // traversal stack entries pack a node index into 24 bits
       if (sc->nodes >= (1ull << 24))
         return fail(setError(c, UBR_INVALID_ARGUMENT, "scene too large: more than 2^24 wide BVH nodes"));

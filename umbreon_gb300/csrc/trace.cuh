@@ -145,17 +145,36 @@ UBR_D void travInit(const Ray& r, TravState& st, Hit& best, int start = 0) {
 // Visit st.node: test its 8 children, its hit leaves' primitives, choose the
 // next node.  Returns true when the ray is finished (any-hit found, stack
 // empty, or the step bound reached).
+// Wide nodes 0..kTopNodes-1 are the root and the two levels below it (the
+// collapse numbers nodes level by level); a kernel may stage them in shared
+// memory and pass them as `top` (nTop of them).
+constexpr int kTopNodes = 73;
+
 template <bool COUNT, int KM, bool ALWAYS_ANY = false>
 UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPre& pre, TravState& st, Hit& best,
-                    uint32_t& overflow, Count* cnt, bool any) {
+                    uint32_t& overflow, Count* cnt, bool any, const float4* top = nullptr, int nTop = 0) {
   if (ALWAYS_ANY) any = true;
   if (++st.steps > s.primCount + 16u) {  // each node at most once per ray in a valid tree
     ++overflow;
     return true;
   }
   if (COUNT) ++cnt->nodes;
-  const float4* nd = s.wnodes + kWideF4 * st.node;
-  const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3), n4 = __ldg(nd + 4);
+  float4 n0, n1, n2, n3, n4;
+  if (st.node < nTop) {
+    const float4* nd = top + kWideF4 * st.node;
+    n0 = nd[0];
+    n1 = nd[1];
+    n2 = nd[2];
+    n3 = nd[3];
+    n4 = nd[4];
+  } else {
+    const float4* nd = s.wnodes + kWideF4 * st.node;
+    n0 = __ldg(nd);
+    n1 = __ldg(nd + 1);
+    n2 = __ldg(nd + 2);
+    n3 = __ldg(nd + 3);
+    n4 = __ldg(nd + 4);
+  }
   const uint32_t hdr = __float_as_uint(n0.w);
   const float sx = __uint_as_float((hdr & 0xFFu) << 23) * inv.x;
   const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * inv.y;
@@ -250,7 +269,7 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
 // Whole traversal of one ray (one thread per ray).
 template <bool COUNT = false, int KM = kMaskAll, bool ALWAYS_ANY = false>
 __device__ bool traverse(const TravScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt,
-                         const bool any, int start = 0) {
+                         const bool any, int start = 0, const float4* top = nullptr, int nTop = 0) {
   best.ref = kInvalid;
   if (s.primCount == 0 || start < 0) return false;
   const f3 inv = safeInv(r.dir);
@@ -258,7 +277,7 @@ __device__ bool traverse(const TravScene& s, const Ray& r, Hit& best, uint32_t& 
   if (KM & kMaskMesh) pre = triPre(r.dir);
   TravState st;
   travInit(r, st, best, start);
-  while (!travStep<COUNT, KM, ALWAYS_ANY>(s, r, inv, pre, st, best, overflow, cnt, any)) {
+  while (!travStep<COUNT, KM, ALWAYS_ANY>(s, r, inv, pre, st, best, overflow, cnt, any, top, nTop)) {
   }
   return best.ref != kInvalid;
 }

@@ -102,6 +102,7 @@ constexpr int kWideLeafMax = 3;
 
 struct DScene {
   const float4* wnodes = nullptr;  // 8-wide nodes (root = 0)
+  uint32_t wideNodes = 0;          // number of 8-wide nodes
   const float4* nodes = nullptr;
   int32_t root = 0;             // child code of the root (when prims > 0)
   uint32_t primCount = 0;       // total primitives
