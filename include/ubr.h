@@ -18,7 +18,8 @@
  *   ubr_render           EmbreeRenderer::render + the finishing steps of
  *                        renderFrame (render/embree_renderer.cpp:1260-1745,
  *                        render/pipeline.cpp:44-50,126-129,182-223,254)
- *   ubr_occluded_batch   EmbreeRenderer::occluded (embree_renderer.cpp:294-357)
+ *   ubr_occluded_batch   EmbreeRenderer::occluded (embree_renderer.cpp:294-357),
+ *   ubr_occluded_filtered_batch   plain and filtered branches
  *   ubr_render_batch     no reference counterpart (many frames per launch)
  *   ubr_adjoint          no reference counterpart (image-loss gradients)
  */
@@ -378,6 +379,23 @@ ubr_status ubr_adjoint(ubr_context* ctx, const ubr_scene* scene, const ubr_rende
 ubr_status ubr_occluded_batch(ubr_context* ctx, const ubr_scene* scene,
                               const float* segs, uint64_t n, float eps,
                               uint8_t* out, int32_t memory);
+
+/* Filtered segment occlusion for the stroke-edge pass's visibility rays:
+ * EmbreeRenderer::occluded with its argument filter (embree_renderer.cpp:
+ * 76-133, 294-357).  Same trimmed open segment as ubr_occluded_batch, but a
+ * candidate hit is not an occluder when it lies on one of segment i's own
+ * mesh faces exclude_faces[exclude_offsets[i] .. exclude_offsets[i+1])
+ * (base-triangle ids, compared modulo the base triangle count of an instanced
+ * mesh), when the ray meets its face at |cos| <= graze_cos_eps, or when the
+ * face's plane passes within coplanar_eps of the segment start (<= 0 disables
+ * either test).  exclude_offsets (n + 1 entries, starting at 0) and
+ * exclude_faces may both be NULL.  All arrays in the memory space `memory`. */
+ubr_status ubr_occluded_filtered_batch(ubr_context* ctx, const ubr_scene* scene,
+                                       const float* segs, uint64_t n, float eps,
+                                       float graze_cos_eps, float coplanar_eps,
+                                       const uint32_t* exclude_offsets,
+                                       const int32_t* exclude_faces,
+                                       uint8_t* out, int32_t memory);
 
 /* Segment occlusion that allocates nothing.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory when

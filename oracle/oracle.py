@@ -44,6 +44,9 @@ def lib():
         L.oracle_intersect.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64] + [C.c_void_p] * 6
         L.oracle_occluded.restype = C.c_int
         L.oracle_occluded.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]
+        L.oracle_occluded_filtered.restype = C.c_int
+        L.oracle_occluded_filtered.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_float, C.c_float,
+                                               C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
         _L = L
     return _L
 
@@ -75,6 +78,22 @@ class OracleScene:
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
         out = np.zeros(len(rays), np.uint8)
         lib().oracle_occluded(self.h, rays.ctypes.data, len(rays), out.ctypes.data)
+        return out
+
+    def occluded_filtered(self, segs: np.ndarray, eps: float, graze_cos_eps: float = 0.0, coplanar_eps: float = 0.0,
+                          exclude_faces=None) -> np.ndarray:
+        segs = np.ascontiguousarray(segs, np.float32).reshape(-1, 6)
+        n = len(segs)
+        out = np.zeros(n, np.uint8)
+        offs = faces = None
+        if exclude_faces is not None:
+            offs = np.zeros(n + 1, np.uint32)
+            np.cumsum([len(f) for f in exclude_faces], out=offs[1:])
+            faces = np.ascontiguousarray(np.concatenate([np.asarray(f, np.int32) for f in exclude_faces] +
+                                                        [np.zeros(1, np.int32)]), np.int32)
+        lib().oracle_occluded_filtered(self.h, segs.ctypes.data, n, eps, graze_cos_eps, coplanar_eps,
+                                       offs.ctypes.data if offs is not None else None,
+                                       faces.ctypes.data if faces is not None else None, out.ctypes.data)
         return out
 
     def render(self, scene: Scene, opt: RenderOptions, threads: int = 0, rows: tuple | None = None) -> FrameResult:

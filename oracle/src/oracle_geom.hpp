@@ -375,6 +375,10 @@ class Bvh {
   void build(const GeomSet* g);
   bool closest(const Ray& r, Hit& h) const;
   bool occluded(const Ray& r) const;
+  // any hit that `accept(kind, primID, hit)` takes; a sphere whose entry point
+  // is refused offers its exit point
+  template <class F>
+  bool occludedIf(const Ray& r, F accept) const;
   size_t nodeCount() const { return nodes_.size(); }
 
  private:
@@ -651,6 +655,40 @@ inline bool Bvh::occluded(const Ray& r) const {
       for (uint32_t i = n.first; i < n.first + n.count; ++i) {
         Hit h;
         if (testPrim(refs_[i], r, pre, r.tnear, r.tfar, h)) return true;
+      }
+    } else {
+      stack[sp++] = n.left;
+      stack[sp++] = n.left + 1;
+    }
+  }
+  return false;
+}
+
+template <class F>
+inline bool Bvh::occludedIf(const Ray& r, F accept) const {
+  if (nodes_.empty()) return false;
+  if (!(r.tnear <= r.tfar)) return false;
+  const V3 inv = safeInv(r.dir);
+  const TriRayPre pre = triPre(r.dir);
+  uint32_t stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp > 0) {
+    const Node& n = nodes_[stack[--sp]];
+    float te;
+    if (!slab(n.box, r.org, inv, r.tnear, r.tfar, te)) continue;
+    if (n.count > 0) {
+      for (uint32_t i = n.first; i < n.first + n.count; ++i) {
+        const PrimRef& p = refs_[i];
+        Hit h;
+        if (!testPrim(p, r, pre, r.tnear, r.tfar, h)) continue;
+        if (accept(p.kind, p.id, h)) return true;
+        if (p.kind == kSphere) {
+          Hit h2;
+          if (testPrim(p, r, pre, std::nextafter(h.t, std::numeric_limits<float>::infinity()), r.tfar, h2) &&
+              accept(p.kind, p.id, h2))
+            return true;
+        }
       }
     } else {
       stack[sp++] = n.left;

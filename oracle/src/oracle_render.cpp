@@ -762,6 +762,62 @@ int oracle_occluded(void* sp, const float* rays, uint64_t n, uint8_t* out) {
   return 0;
 }
 
+// EmbreeRenderer::occluded (embree_renderer.cpp:294-357) with its argument
+// filter excludeFaceFilter (:76-133): segment i is occluded when a hit on the
+// trimmed open segment is not on one of its excluded mesh faces, not grazing
+// (|cos| <= grazeCos) and not coincident (plane within `coplanar` of the start).
+int oracle_occluded_filtered(void* sp, const float* segs, uint64_t n, float eps, float grazeCos, float coplanar,
+                             const uint32_t* offs, const int32_t* faces, uint8_t* out) {
+  const Scene& s = *static_cast<Scene*>(sp);
+  const bool meshPresent = s.geo.geomID[kMesh] != kInvalid;
+  for (uint64_t i = 0; i < n; ++i) {
+    const float* q = segs + 6 * i;
+    const V3 p(q[0], q[1], q[2]), e(q[3], q[4], q[5]);
+    const V3 d = e - p;
+    const float len = std::sqrt(dot(d, d));
+    out[i] = 0;
+    if (len <= 0.0f) continue;
+    const V3 dir(d.x / len, d.y / len, d.z / len);
+    const float tnear = std::max(eps * len, eps);
+    const float tfar = len * (1.0f - eps);
+    if (tnear >= tfar) continue;
+    Ray r;
+    r.org = p; r.dir = dir; r.tnear = tnear; r.tfar = tfar;
+    const int nFaces = (offs && faces && meshPresent) ? int(offs[i + 1] - offs[i]) : 0;
+    const int32_t* fl = (offs && faces) ? faces + offs[i] : nullptr;
+    if (nFaces == 0 && grazeCos <= 0.0f && coplanar <= 0.0f) {
+      out[i] = s.bvh.occluded(r) ? 1 : 0;
+      continue;
+    }
+    auto accept = [&](int kind, uint32_t prim, const Hit& h) {
+      if (nFaces > 0 && kind == kMesh) {
+        uint32_t pr = prim;
+        if (s.baseTri > 0) pr %= uint32_t(s.baseTri);
+        for (int k = 0; k < nFaces; ++k)
+          if (uint32_t(fl[k]) == pr) return false;
+      }
+      if (grazeCos > 0.0f || coplanar > 0.0f) {
+        const float nx = h.Ng.x, ny = h.Ng.y, nz = h.Ng.z;
+        const float dx = r.dir.x, dy = r.dir.y, dz = r.dir.z;
+        const float nlen = std::sqrt(nx * nx + ny * ny + nz * nz);
+        const float dlen = std::sqrt(dx * dx + dy * dy + dz * dz);
+        if (nlen > 0.0f && dlen > 0.0f) {
+          const float dDotN = nx * dx + ny * dy + nz * dz;
+          const float c = std::fabs(dDotN) / (nlen * dlen);
+          if (grazeCos > 0.0f && c <= grazeCos) return false;
+          if (coplanar > 0.0f) {
+            const float perp = h.t * std::fabs(dDotN) / nlen;
+            if (perp <= coplanar) return false;
+          }
+        }
+      }
+      return true;
+    };
+    out[i] = s.bvh.occludedIf(r, accept) ? 1 : 0;
+  }
+  return 0;
+}
+
 // The frame: embree_renderer.cpp:1260-1427 pixel loop (rows [row0, row1) of the
 // hi-res grid, all rows when row1 <= row0), then pipeline.cpp:126-129 fog,
 // :182-192 box downsample, :254 assumed gamma.  `threads` <= 0 uses all cores.

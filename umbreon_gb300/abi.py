@@ -179,6 +179,8 @@ SIGNATURES = {
     "ubr_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderDesc), C.c_void_p, C.POINTER(Grads)]),
     "ubr_occluded_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
                                      C.c_void_p, C.c_int32]),
+    "ubr_occluded_filtered_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float, C.c_float,
+                                              C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
     "ubr_occluded_batch_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_float,
                                              C.c_void_p]),
 }

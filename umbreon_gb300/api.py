@@ -416,6 +416,28 @@ class Context:
                                                eps, out.ctypes.data, abi.MEMORY_HOST))
         return out
 
+    def occluded_filtered(self, built: "BuiltScene", segs: np.ndarray, eps: float, graze_cos_eps: float = 0.0,
+                          coplanar_eps: float = 0.0, exclude_faces=None) -> np.ndarray:
+        """Filtered segment visibility (ubr_occluded_filtered_batch);
+        exclude_faces: one sequence of base-triangle ids per segment, or None."""
+        segs = np.ascontiguousarray(segs, np.float32).reshape(-1, 6)
+        n = len(segs)
+        out = np.zeros(n, np.uint8)
+        offs = faces = None
+        if exclude_faces is not None:
+            lens = np.array([len(f) for f in exclude_faces], np.uint32)
+            offs = np.zeros(n + 1, np.uint32)
+            np.cumsum(lens, out=offs[1:])
+            faces = np.ascontiguousarray(np.concatenate([np.asarray(f, np.int32) for f in exclude_faces])
+                                         if n else np.zeros(0, np.int32), np.int32)
+            if faces.size == 0:
+                faces = np.zeros(1, np.int32)
+        self._check(self._L.ubr_occluded_filtered_batch(
+            self.handle, built.handle, segs.ctypes.data, n, eps, graze_cos_eps, coplanar_eps,
+            offs.ctypes.data if offs is not None else None, faces.ctypes.data if faces is not None else None,
+            out.ctypes.data, abi.MEMORY_HOST))
+        return out
+
     def close(self):
         if getattr(self, "handle", None):
             self._L.ubr_context_destroy(self.handle)

@@ -25,6 +25,9 @@ struct Job {
 };
 ubr_status renderBatch(Context* c, const std::vector<Job>& jobs, ubr_frame* total);
 ubr_status adjoint(Context* c, const Scene* sc, const ubr_render_desc& d, const float* dColor, ubr_grads& g);
+ubr_status occludedFilteredBatch(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps,
+                                 float grazeCos, float coplanar, const uint32_t* offs, const int32_t* faces,
+                                 uint8_t* out, int32_t memory);
 ubr_status occludedBatchNoAlloc(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps,
                                 uint8_t* out);
 
@@ -311,6 +314,19 @@ ubr_status ubr_occluded_batch(ubr_context* c, const ubr_scene* s, const float* s
   if (!s || !s->impl) return setError(&c->impl, UBR_INVALID_ARGUMENT, "occluded_batch: NULL scene");
   cudaSetDevice(c->impl.device);
   return occludedBatch(&c->impl, s->impl, segs, n, eps, out, memory);
+}
+
+ubr_status ubr_occluded_filtered_batch(ubr_context* c, const ubr_scene* s, const float* segs, uint64_t n,
+                                       float eps, float graze_cos_eps, float coplanar_eps,
+                                       const uint32_t* exclude_offsets, const int32_t* exclude_faces, uint8_t* out,
+                                       int32_t memory) {
+  if (!c) return UBR_INVALID_ARGUMENT;
+  if (!s || !s->impl) return setError(&c->impl, UBR_INVALID_ARGUMENT, "occluded_filtered_batch: NULL scene");
+  if (s->impl->ctx != &c->impl)
+    return setError(&c->impl, UBR_INVALID_ARGUMENT, "occluded_filtered_batch: scene from another context");
+  cudaSetDevice(c->impl.device);
+  return occludedFilteredBatch(&c->impl, s->impl, segs, n, eps, graze_cos_eps, coplanar_eps, exclude_offsets,
+                               exclude_faces, out, memory);
 }
 
 ubr_status ubr_occluded_batch_noalloc(ubr_context* c, const ubr_scene* s, const float* segs, uint64_t n, float eps,

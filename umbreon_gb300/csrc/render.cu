@@ -860,6 +860,46 @@ __global__ void k_occluded_segments(DScene s, const float* segs, uint64_t n, flo
   warpCount(&stats[3], ovf);
 }
 
+// EmbreeRenderer::occluded with its argument filter (embree_renderer.cpp:
+// 294-357): the same trimmed open segment, any hit that the segment's filter
+// accepts (own mesh faces, grazing faces and coincident planes are skipped;
+// the plain any-hit test when nothing is filtered).
+__global__ void k_occluded_filtered(DScene s, const float* segs, uint64_t n, float eps, float grazeCos,
+                                    float coplanar, const uint32_t* offs, const int32_t* faces, int meshPresent,
+                                    uint8_t* out, unsigned long long* stats) {
+  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  uint32_t ovf = 0;
+  if (i < n) {
+    const float* q = segs + 6 * i;
+    const f3 a{q[0], q[1], q[2]}, bq{q[3], q[4], q[5]};
+    const f3 d = bq - a;
+    const float len = length(d);
+    uint8_t res = 0;
+    if (len > 0.0f) {
+      const f3 dir{d.x / len, d.y / len, d.z / len};
+      const float tnear = fmaxf(eps * len, eps);
+      const float tfar = len * (1.0f - eps);
+      if (tnear < tfar) {
+        HitFilter f;
+        f.faces = faces && offs ? faces + offs[i] : nullptr;
+        f.nFaces = (faces && offs && meshPresent) ? int(offs[i + 1] - offs[i]) : 0;
+        f.baseTri = s.baseTri;
+        f.grazeCos = grazeCos;
+        f.coplanar = coplanar;
+        const Ray r{a, dir, tnear, tfar};
+        Hit h;
+        const TravScene ts = travOf(s);
+        if (f.nFaces == 0 && grazeCos <= 0.0f && coplanar <= 0.0f)
+          res = traverse<false, kMaskAll, true>(ts, r, h, ovf, nullptr, true) ? 1 : 0;
+        else
+          res = traverse<false, kMaskAll, false, true>(ts, r, h, ovf, nullptr, true, 0, nullptr, 0, &f) ? 1 : 0;
+      }
+    }
+    out[i] = res;
+  }
+  warpCount(&stats[3], ovf);
+}
+
 // Kind bits of a scene, and the instantiated variant that covers a set of kinds.
 int kindMaskBits(const Scene& sc) {
   int m = 0;
@@ -1291,6 +1331,54 @@ ubr_status occludedBatch(Context* c, const Scene* sc, const float* segs, uint64_
   if (st != UBR_OK) return st;
   UBR_CUDA(c, cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), s));
   k_occluded_segments<<<uint32_t((n + 127) / 128), 128, 0, s>>>(sc->view, dsegs, n, eps, dout, stats);
+  UBR_CUDA(c, cudaGetLastError());
+  if (memory != UBR_MEMORY_DEVICE) UBR_CUDA(c, cudaMemcpyAsync(out, dout, size_t(n), cudaMemcpyDeviceToHost, s));
+  UBR_CUDA(c, cudaStreamSynchronize(s));
+  return UBR_OK;
+}
+
+ubr_status occludedFilteredBatch(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps,
+                                 float grazeCos, float coplanar, const uint32_t* offs, const int32_t* faces,
+                                 uint8_t* out, int32_t memory) {
+  if (n == 0) return UBR_OK;
+  if (!segs || !out) return setError(c, UBR_INVALID_ARGUMENT, "occluded_filtered_batch: NULL buffer");
+  if ((offs == nullptr) != (faces == nullptr))
+    return setError(c, UBR_INVALID_ARGUMENT, "occluded_filtered_batch: exclude offsets and faces go together");
+  ubr_status st = UBR_OK;
+  const float* dsegs = segs;
+  const uint32_t* doffs = offs;
+  const int32_t* dfaces = faces;
+  uint8_t* dout = out;
+  cudaStream_t s = c->stream;
+  if (memory != UBR_MEMORY_DEVICE) {
+    uint64_t nf = 0;
+    if (offs) {
+      if (offs[0] != 0) return setError(c, UBR_INVALID_ARGUMENT, "occluded_filtered_batch: offsets[0] != 0");
+      for (uint64_t i = 0; i < n; ++i)
+        if (offs[i + 1] < offs[i])
+          return setError(c, UBR_INVALID_ARGUMENT, "occluded_filtered_batch: offsets decrease");
+      nf = offs[n];
+    }
+    float* ts = scratchT<float>(c, 40, size_t(n) * 6, st);
+    dout = scratchT<uint8_t>(c, 41, size_t(n), st);
+    uint32_t* to = offs ? scratchT<uint32_t>(c, 43, size_t(n) + 1, st) : nullptr;
+    int32_t* tf = offs ? scratchT<int32_t>(c, 44, size_t(nf) + 1, st) : nullptr;
+    if (st != UBR_OK) return st;
+    UBR_CUDA(c, cudaMemcpyAsync(ts, segs, size_t(n) * 6 * sizeof(float), cudaMemcpyHostToDevice, s));
+    if (offs) {
+      UBR_CUDA(c, cudaMemcpyAsync(to, offs, (size_t(n) + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+      if (nf) UBR_CUDA(c, cudaMemcpyAsync(tf, faces, size_t(nf) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    }
+    dsegs = ts;
+    doffs = to;
+    dfaces = tf;
+  }
+  unsigned long long* stats = scratchT<unsigned long long>(c, 42, 8, st);
+  if (st != UBR_OK) return st;
+  UBR_CUDA(c, cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), s));
+  k_occluded_filtered<<<uint32_t((n + 127) / 128), 128, 0, s>>>(sc->view, dsegs, n, eps, grazeCos, coplanar, doffs,
+                                                                dfaces, sc->primCount[kMesh] > 0 ? 1 : 0, dout,
+                                                                stats);
   UBR_CUDA(c, cudaGetLastError());
   if (memory != UBR_MEMORY_DEVICE) UBR_CUDA(c, cudaMemcpyAsync(out, dout, size_t(n), cudaMemcpyDeviceToHost, s));
   UBR_CUDA(c, cudaStreamSynchronize(s));

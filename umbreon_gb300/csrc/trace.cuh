@@ -145,14 +145,51 @@ UBR_D void travInit(const Ray& r, TravState& st, Hit& best, int start = 0) {
 // Visit st.node: test its 8 children, its hit leaves' primitives, choose the
 // next node.  Returns true when the ray is finished (any-hit found, stack
 // empty, or the step bound reached).
+// Candidate-hit filter of the stroke-edge pass's visibility rays
+// (excludeFaceFilter, embree_renderer.cpp:76-133): a hit is not an occluder
+// when it lies on one of the segment's own mesh faces (primID modulo the base
+// triangle count), when the ray meets its face at |cos| <= grazeCos, or when
+// the face's plane passes within `coplanar` of the ray origin.
+struct HitFilter {
+  const int32_t* faces;  // excluded base-triangle ids
+  int nFaces;
+  uint32_t baseTri;      // triangles per instance (0: not instanced)
+  float grazeCos, coplanar;
+};
+UBR_D bool filterAccept(const HitFilter& f, const Ray& r, const Hit& h, uint32_t ref) {
+  if (f.nFaces > 0 && refKind(ref) == kMesh) {
+    uint32_t prim = refPrim(ref);
+    if (f.baseTri > 0) prim %= f.baseTri;
+    for (int k = 0; k < f.nFaces; ++k)
+      if (uint32_t(__ldg(&f.faces[k])) == prim) return false;
+  }
+  if (f.grazeCos > 0.0f || f.coplanar > 0.0f) {
+    const float nx = h.Ng.x, ny = h.Ng.y, nz = h.Ng.z;
+    const float dx = r.dir.x, dy = r.dir.y, dz = r.dir.z;
+    const float nlen = sqrtf(nx * nx + ny * ny + nz * nz);
+    const float dlen = sqrtf(dx * dx + dy * dy + dz * dz);
+    if (nlen > 0.0f && dlen > 0.0f) {
+      const float dDotN = nx * dx + ny * dy + nz * dz;
+      const float c = fabsf(dDotN) / (nlen * dlen);
+      if (f.grazeCos > 0.0f && c <= f.grazeCos) return false;
+      if (f.coplanar > 0.0f) {
+        const float perp = h.t * fabsf(dDotN) / nlen;
+        if (perp <= f.coplanar) return false;
+      }
+    }
+  }
+  return true;
+}
+
 // Wide nodes 0..kTopNodes-1 are the root and the two levels below it (the
 // collapse numbers nodes level by level); a kernel may stage them in shared
 // memory and pass them as `top` (nTop of them).
 constexpr int kTopNodes = 73;
 
-template <bool COUNT, int KM, bool ALWAYS_ANY = false>
+template <bool COUNT, int KM, bool ALWAYS_ANY = false, bool FILTER = false>
 UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPre& pre, TravState& st, Hit& best,
-                    uint32_t& overflow, Count* cnt, bool any, const float4* top = nullptr, int nTop = 0) {
+                    uint32_t& overflow, Count* cnt, bool any, const float4* top = nullptr, int nTop = 0,
+                    const HitFilter* flt = nullptr) {
   if (ALWAYS_ANY) any = true;
   if (++st.steps > s.primCount + 16u) {  // each node at most once per ray in a valid tree
     ++overflow;
@@ -229,6 +266,18 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
     const bool hitLeaf = testLeaf<KM, !ALWAYS_ANY>(s, primBase + q, r, pre, r.tnear, st.tmax, h, ref);
     if (COUNT) cnt->primBytes += leafBytes(refKind(ref));
     if (!hitLeaf) continue;
+    if (FILTER && !filterAccept(*flt, r, h, ref)) {
+      // a rejected sphere entry still leaves its exit point as a candidate
+      bool second = false;
+      if (refKind(ref) == kSphere) {
+        const float4 q4 = __ldg(s.leafGeo + kLeafF4 * (primBase + q));
+        Hit h2;
+        second = isectSphere<true>(r, f3{q4.x, q4.y, q4.z}, q4.w, nextafterf(h.t, kInfF), st.tmax, h2) &&
+                 filterAccept(*flt, r, h2, ref);
+        if (second) h = h2;
+      }
+      if (!second) continue;
+    }
     if (any) {
       best = h;
       best.ref = ref;
@@ -267,9 +316,10 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
 }
 
 // Whole traversal of one ray (one thread per ray).
-template <bool COUNT = false, int KM = kMaskAll, bool ALWAYS_ANY = false>
+template <bool COUNT = false, int KM = kMaskAll, bool ALWAYS_ANY = false, bool FILTER = false>
 __device__ bool traverse(const TravScene& s, const Ray& r, Hit& best, uint32_t& overflow, Count* cnt,
-                         const bool any, int start = 0, const float4* top = nullptr, int nTop = 0) {
+                         const bool any, int start = 0, const float4* top = nullptr, int nTop = 0,
+                         const HitFilter* flt = nullptr) {
   best.ref = kInvalid;
   if (s.primCount == 0 || start < 0) return false;
   const f3 inv = safeInv(r.dir);
@@ -277,7 +327,7 @@ __device__ bool traverse(const TravScene& s, const Ray& r, Hit& best, uint32_t& 
   if (KM & kMaskMesh) pre = triPre(r.dir);
   TravState st;
   travInit(r, st, best, start);
-  while (!travStep<COUNT, KM, ALWAYS_ANY>(s, r, inv, pre, st, best, overflow, cnt, any, top, nTop)) {
+  while (!travStep<COUNT, KM, ALWAYS_ANY, FILTER>(s, r, inv, pre, st, best, overflow, cnt, any, top, nTop, flt)) {
   }
   return best.ref != kInvalid;
 }
