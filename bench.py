@@ -36,6 +36,20 @@ from umbreon_gb300 import replicas  # noqa: E402
 
 METRIC = "ms/frame & Mrays/s (batched vs per-frame GPU) at >=45 dB PSNR; adjoint ms/iter"
 WORKLOAD = "ball_and_stick_20k_1920x1080_ss2_ao16_2lights_shadows_fog"
+# --workload: the scene of the headline line (the others are for profiling one workload alone)
+WORKLOADS = {
+    "ball_and_stick": ("ball_and_stick", WORKLOAD),
+    "space_filling": ("space_filling", "space_filling_2k_640x480"),
+    "molecular_surface": ("molecular_surface", "molecular_surface_2m_tris_2048_alpha0.5_4layers_ao32_shadows"),
+    "differentiable": ("differentiable", "spheres_100k_1024_ao16_enhanced_1light_shadows_fog"),
+}
+
+
+def _workload(args):
+    from umbreon_gb300 import scenes
+    fn, name = WORKLOADS[args.workload]
+    sc, opt = getattr(scenes, fn)()
+    return sc, opt, name
 
 
 def _dist():
@@ -111,7 +125,7 @@ def run_reference(args):
     if rank != 0:
         return
     from umbreon_gb300 import scenes
-    sc, opt = scenes.ball_and_stick()
+    sc, opt, wname = _workload(args)
     threads = os.cpu_count() or 1
     steps = []
     info = None
@@ -127,7 +141,7 @@ def run_reference(args):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_frame, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded PCG32 scene)",
-        "config": {"workload": WORKLOAD, "sample": f"rows {info['rows']} of {info['H']} hi-res rows per step"},
+        "config": {"workload": wname, "sample": f"rows {info['rows']} of {info['H']} hi-res rows per step"},
         "cpu_baseline": {"value": round(mrays, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{info['rows']} hi-res rows of the frame per step (all host threads)"},
         "e2e": {"value": round(mrays, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -392,7 +406,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    sc, opt = scenes.ball_and_stick()
+    sc, opt, wname = _workload(args)
     if args.frame:
         opt.width, opt.height = (int(x) for x in args.frame.lower().split("x"))
     if args.ss:
@@ -478,7 +492,8 @@ def run_ours(args):
                 "launch_ms": round(per_launch_ms, 3)}
 
     # end to end through the C-ABI with host buffers: upload + BVH + render + D2H
-    host_color = np.zeros((opt.height, opt.width, 4), np.float32)
+    # into a pinned host frame (the caller's buffer; pageable memory works too)
+    host_color = torch.zeros((opt.height, opt.width, 4), dtype=torch.float32, pin_memory=True).numpy()
     desc, keepd = sc.to_desc()
     h2d = sum(a.nbytes for a in keepd)
     e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 5))
@@ -516,8 +531,8 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_frame, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded PCG32 random-walk chain)",
-            "config": {"workload": WORKLOAD if not (args.frame or args.ss) else WORKLOAD + "_resized",
+            "data": "synthetic (seeded PCG32 scene generator)",
+            "config": {"workload": wname if not (args.frame or args.ss) else wname + "_resized",
                        "frame": f"{opt.width}x{opt.height} ss{opt.supersample}",
                        "primitives": info["prim_count"], "bvh_nodes": info["bvh_nodes"],
                        "l2": "flushed (256 MB write) before every timed frame",
@@ -548,6 +563,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="ball_and_stick", choices=sorted(WORKLOADS),
+                    help="scene of the headline line (default: the ball-and-stick benchmark frame)")
     ap.add_argument("--builder", type=int, default=0, help="BVH builder (0 library default, 1 radix tree, 2 PLOC)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the other workloads (space filling, "
                     "molecular surface, batched turntable)")

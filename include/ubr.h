@@ -189,6 +189,9 @@ typedef struct ubr_render_desc {
   /* giIntegrator only selects the soft-shadow radius rule
    * (embree_renderer.cpp:452-454); GI itself is out of this library */
   int32_t gi_integrator;
+  /* RenderOptions::aoWriteAov (render_options.hpp:62): fill the AO AOV
+   * outputs of ubr_frame */
+  uint32_t ao_write_aov;
 } ubr_render_desc;
 
 /* Where a frame's buffers live. */
@@ -235,6 +238,19 @@ typedef struct ubr_frame {
   uint64_t node_bytes[2];
   uint64_t prim_bytes[2];
   uint64_t nodes_visited[2];
+  /* AO AOVs of the first hit, output resolution (box-averaged like the
+   * colour), written when the desc sets ao_write_aov (FrameResult::albedo,
+   * normal, bentNormal, contactAo, shapeAo, avgHitDist; frame_result.hpp:48-79,
+   * filled by storeShadingChannels, embree_renderer.cpp:213-233): mesh hits
+   * give the vertex colour, shading normal and the AO estimator's bent
+   * normal / contact / shape openness / mean occluder distance; primitive
+   * hits and background keep the neutral values (0, 0, 0, 1, 1, 0). */
+  float* albedo;          /* 3 per pixel */
+  float* normal;          /* 3 per pixel */
+  float* bent_normal;     /* 3 per pixel */
+  float* contact_ao;      /* 1 per pixel */
+  float* shape_ao;        /* 1 per pixel */
+  float* avg_hit_dist;    /* 1 per pixel */
 } ubr_frame;
 
 /* Context: one GPU, one CUDA stream, one device arena. */

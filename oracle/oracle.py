@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 
 from umbreon_gb300 import abi
-from umbreon_gb300.api import FrameResult, RenderOptions, Scene, make_render_desc
+from umbreon_gb300.api import FrameResult, RenderOptions, Scene, attach_aovs, make_render_desc
 
 HERE = Path(__file__).resolve().parent
 _L = None
@@ -111,12 +111,13 @@ class OracleScene:
         fr.view_z = abi.ptr(vz)
         fr.hit_geom = abi.ptr(hg, C.c_uint32)
         fr.hit_prim = abi.ptr(hp, C.c_uint32)
+        aovs = attach_aovs(fr, opt)
         r0, r1 = rows if rows else (0, 0)
         st = lib().oracle_render_rows(self.h, C.byref(rd), C.byref(fr), threads, r0, r1)
         if st != 0:
             raise RuntimeError("oracle: unsupported request (Principled material)")
         stats = dict(render_ms=fr.render_ms, rays_primary=fr.rays_primary, capped_rays=fr.capped_rays)
-        return FrameResult(opt.width, opt.height, color, depth, vz, hg, hp, fr.render_ms / 1e3, stats)
+        return FrameResult(opt.width, opt.height, color, depth, vz, hg, hp, fr.render_ms / 1e3, stats, **aovs)
 
     def __del__(self):
         try:

@@ -456,6 +456,7 @@ struct Opt {  // the RenderOptions fields this path reads
   float aoSky[3], aoGround[3], aoDiffuseFactor;
   bool shadows; int shadowSamples; int envLights;
   float specularScale; bool transparency, transparentBackground; int maxTransparentLayers;
+  bool aoWriteAov = false;
   bool aoEnhanced() const {  // render_options.hpp:79-82
     return aoFalloffPower > 0.0f || aoMultiScale || aoBentNormal || aoMultibounce || aoLowDiscrepancy ||
            aoDiffuseFactor > 0.0f;
@@ -492,9 +493,11 @@ inline AoShade aoApplyFactors(const Opt& o, const V3& ambLight, const V3& aoUp, 
 }
 
 // ao_shade.hpp:44-72 aoGather + :128-141 computeAoShade (sampleMul 1, wSeed = hi-res width)
+// (ao_shade.hpp:43-72 aoGather: legacy colour + one single-scale quality pass
+// for the AOVs when aoWriteAov asks for them)
 inline AoShade computeAoShade(const Scene& s, const Opt& o, const V3& ambLight, const V3& aoUp,
                               const V3& P, const V3& Ng, const V3& N, const V3& C, float secEps,
-                              uint32_t px, uint32_t py, int wSeed) {
+                              uint32_t px, uint32_t py, int wSeed, AOResult* aovOut = nullptr) {
   if (o.aoSamples <= 0) { AoShade r; r.ambLight = ambLight; return r; }
   AOResult aov;
   float openness;
@@ -504,7 +507,10 @@ inline AoShade computeAoShade(const Scene& s, const Opt& o, const V3& ambLight, 
     openness = aov.openness;
   } else {
     openness = computeAO(s, P, Ng, N, secEps, o.aoSamples, o.aoDistance, px, py, wSeed);
+    if (o.aoWriteAov)
+      aov = computeAOQuality(s, P, Ng, N, secEps, o.aoSamples, o.aoDistance, 0.0f, false, false, px, py, wSeed);
   }
+  if (aovOut) *aovOut = aov;
   return aoApplyFactors(o, ambLight, aoUp, openness, aov, C);
 }
 
@@ -580,7 +586,13 @@ struct Ctx {
   float clipNear, clipFar;
 };
 
-struct HitShade { V3 color; float opacity = 1.0f; };
+struct HitShade {
+  V3 color;
+  float opacity = 1.0f;
+  // AO AOVs (hit_shader.hpp:41-55): set on mesh hits when aoWriteAov is on
+  V3 albedo{0.0f, 0.0f, 0.0f}, normal{0.0f, 0.0f, 0.0f}, bent{0.0f, 0.0f, 0.0f};
+  float contact = 1.0f, shape = 1.0f, avgHit = 0.0f;
+};
 
 // hit_shader.hpp:147-496 shadeHit (POV; GI / edge / principled branches off)
 inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& org, uint32_t px, uint32_t py) {
@@ -607,10 +619,19 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
     const V3 C{cbuf[0], cbuf[1], cbuf[2]};
     const size_t bt = s.baseTri ? hit.primID % s.baseTri : 0;
     const Mat& triMat = s.triMat.empty() ? s.meshMat : s.meshMats[s.triMat[bt]];
-    AoShade ao = computeAoShade(s, c.o, c.ambLight, c.aoUp, P, Ng, N, C, secEps, px, py, c.wHi);
+    AOResult aov;
+    AoShade ao = computeAoShade(s, c.o, c.ambLight, c.aoUp, P, Ng, N, C, secEps, px, py, c.wHi, &aov);
     hs.color = shadeLocal(s, triMat, C, N, V, c.lights, ao.ambLight, c.bg, c.o.specularScale, ao.aoFactor,
                           ao.diffuseAo, P, Ng, secEps, shadowsActive, c.o.shadowSamples, px, py);
     hs.opacity = cbuf[3];
+    if (c.o.aoWriteAov) {  // hit_shader.hpp:207-213
+      hs.albedo = C;
+      hs.normal = N;
+      hs.bent = aov.bent;
+      hs.contact = aov.contact;
+      hs.shape = aov.shape;
+      hs.avgHit = aov.avgHitDist;
+    }
   } else {
     const float* fc = &s.color[kind][4 * hit.primID];
     const Mat& pm = s.mat[kind][hit.primID];
@@ -643,7 +664,13 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
   return hs;
 }
 
-struct PixelOut { float r, g, b, a, depth, viewZ; uint32_t geom, prim; bool capped; uint32_t rays; };
+struct PixelOut {
+  float r, g, b, a, depth, viewZ;
+  uint32_t geom, prim;
+  bool capped;
+  uint32_t rays;
+  HitShade first;  // AOVs of the first hit (neutral values on a miss)
+};
 
 // transparency.hpp:311-522 integratePixel (colour, first-hit depth/viewZ/ids)
 inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32_t px, uint32_t py,
@@ -679,6 +706,7 @@ inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32
       firstViewZ = h.t * dot(rd, camDir);
       po.geom = h.geomID;
       po.prim = h.primID;
+      po.first = hs;
     }
     if (!c.o.transparency || hs.opacity >= kOpaque) {
       base = hs.color;
@@ -852,6 +880,7 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   c.o.specularScale = d.specular_scale; c.o.transparency = d.transparency != 0;
   c.o.transparentBackground = d.transparent_background != 0;
   c.o.maxTransparentLayers = d.max_transparent_layers;
+  c.o.aoWriteAov = d.ao_write_aov != 0;
   // buildSceneLights (embree_renderer.cpp:436-458)
   for (uint32_t i = 0; i < d.light_count; ++i) {
     const ubr_light& dl = d.lights[i];
@@ -898,6 +927,13 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   const size_t npix = static_cast<size_t>(W) * H;
   std::vector<float> color(npix * 4, 0.0f), viewZ(npix, 0.0f), depth(npix, 0.0f);
   std::vector<uint32_t> hg(npix, kInvalid), hp(npix, kInvalid);
+  // AO AOVs (allocateFrameBuffers, embree_renderer.cpp:500-505 defaults)
+  const bool aov = d.ao_write_aov != 0;
+  std::vector<float> aAlb, aNrm, aBent, aCon, aShp, aAvg;
+  if (aov) {
+    aAlb.assign(npix * 3, 0.0f); aNrm.assign(npix * 3, 0.0f); aBent.assign(npix * 3, 0.0f);
+    aCon.assign(npix, 1.0f); aShp.assign(npix, 1.0f); aAvg.assign(npix, 0.0f);
+  }
   if (row1 <= row0) { row0 = 0; row1 = H; }
   std::atomic<int> nextRow{row0};
   std::atomic<uint64_t> rays{0}, capped{0};
@@ -926,6 +962,19 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
         hp[pix] = po.prim;
         myRays += po.rays;
         myCapped += po.capped ? 1 : 0;
+        if (aov) {  // storeShadingChannels / storeGBufChannels (embree_renderer.cpp:213-250)
+          const HitShade& f = po.first;
+          const float a3[3][3] = {{f.albedo.x, f.albedo.y, f.albedo.z}, {f.normal.x, f.normal.y, f.normal.z},
+                                  {f.bent.x, f.bent.y, f.bent.z}};
+          for (int k = 0; k < 3; ++k) {
+            aAlb[3 * pix + k] = a3[0][k];
+            aNrm[3 * pix + k] = a3[1][k];
+            aBent[3 * pix + k] = a3[2][k];
+          }
+          aCon[pix] = f.contact;
+          aShp[pix] = f.shape;
+          aAvg[pix] = f.avgHit;
+        }
       }
     }
     rays += myRays;
@@ -995,6 +1044,35 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
         float vv = fin[4 * i + ch];
         fin[4 * i + ch] = (vv > 0.0f) ? std::pow(vv, g) : 0.0f;
       }
+  }
+  // AO AOVs box-averaged to the output (pipeline.cpp:182-206)
+  if (aov) {
+    auto down = [&](const std::vector<float>& src, int ch, float* dst) {
+      if (!dst) return;
+      if (ss == 1) {
+        std::memcpy(dst, src.data(), src.size() * sizeof(float));
+        return;
+      }
+      const int ow = W / ss, oh = H / ss;
+      const float inv = 1.0f / static_cast<float>(ss * ss);
+      for (int y = 0; y < oh; ++y)
+        for (int x = 0; x < ow; ++x)
+          for (int q = 0; q < ch; ++q) {
+            float acc = 0.0f;
+            for (int dy = 0; dy < ss; ++dy)
+              for (int dx = 0; dx < ss; ++dx) {
+                const float vv = src[(static_cast<size_t>(y * ss + dy) * W + (x * ss + dx)) * ch + q];
+                acc += std::isfinite(vv) ? vv : 0.0f;
+              }
+            dst[(static_cast<size_t>(y) * ow + x) * ch + q] = acc * inv;
+          }
+    };
+    down(aAlb, 3, fr->albedo);
+    down(aNrm, 3, fr->normal);
+    down(aBent, 3, fr->bent_normal);
+    down(aCon, 1, fr->contact_ao);
+    down(aShp, 1, fr->shape_ao);
+    down(aAvg, 1, fr->avg_hit_dist);
   }
   if (fr->color) std::memcpy(fr->color, fin.data(), fin.size() * sizeof(float));
   if (fr->depth) std::memcpy(fr->depth, depth.data(), npix * sizeof(float));

@@ -129,3 +129,35 @@ def test_instances(gpu_ctx, oracle_lib):
     sc, opt = scenes.space_filling(n=300, width=160, height=120)
     sc.instance_offsets = np.array([[0, 0, 0], [12.0, 3.0, -5.0], [-9.0, -6.0, 4.0]], np.float32)
     _compare(gpu_ctx, oracle_lib, sc, opt)
+
+
+def _compare_aovs(g, o, m, tol=1e-3, quantile=0.999):
+    """AO AOVs of the GPU frame against the oracle's on pixels whose
+    subpixels agree on the first hit."""
+    from umbreon_gb300.api import AOV_FIELDS
+    for name, _, _ in AOV_FIELDS:
+        a, b = getattr(g, name), getattr(o, name)
+        assert a is not None and b is not None, name
+        d = np.abs(a - b)
+        d = d[m] if d.ndim == 2 else d[m].reshape(-1)
+        assert float(np.quantile(d, quantile)) <= tol, (name, float(d.max()))
+
+
+@pytest.mark.parametrize("enhanced", [False, True])
+def test_ao_aovs_molecular_surface(gpu_ctx, oracle_lib, enhanced):
+    """aoWriteAov: mesh first hits carry albedo / normal / bent normal /
+    contact / shape / mean occluder distance; sphere hits and background keep
+    the neutral values; ss 2 box-averages them."""
+    sc, opt = scenes.molecular_surface(n_atoms=600, box=16.0, n_spheres=300, width=96, height=96,
+                                       ao_samples=8, layers=2)
+    opt.supersample = 2
+    opt.aoWriteAov = True
+    if enhanced:
+        opt.aoFalloffPower, opt.aoMultiScale = 1.0, True
+    g, o, info = _compare(gpu_ctx, oracle_lib, sc, opt, err_quantile=AO_QUANTILE, hard_max=0.3)
+    m = agree_mask_final(g.hit_geom, g.hit_prim, o.hit_geom, o.hit_prim, 2)
+    _compare_aovs(g, o, m)
+    # the pixels whose four sub-samples are sphere hits carry the neutral AOVs
+    sph = (g.hit_geom.reshape(96, 2, 96, 2) == 1).all(axis=(1, 3))
+    assert sph.sum() > 20
+    assert np.all(g.contactAo[sph] == 1.0) and np.all(g.albedo[sph] == 0.0)

@@ -208,6 +208,7 @@ class RenderOptions:
     transparentBackground: bool = False
     maxTransparentLayers: int = 256
     giIntegrator: int = 2
+    aoWriteAov: bool = False
 
     def aoEnhanced(self) -> bool:
         return (self.aoFalloffPower > 0.0 or self.aoMultiScale or self.aoBentNormal or self.aoMultibounce
@@ -271,6 +272,7 @@ def make_render_desc(scene: Scene, opt: RenderOptions):
     d.transparent_background = int(opt.transparentBackground)
     d.max_transparent_layers = opt.maxTransparentLayers
     d.gi_integrator = opt.giIntegrator
+    d.ao_write_aov = int(opt.aoWriteAov)
     return d, keep
 
 
@@ -286,6 +288,28 @@ class FrameResult:
     hit_prim: np.ndarray
     renderSeconds: float = 0.0
     stats: dict = field(default_factory=dict)
+    # AO AOVs (RenderOptions.aoWriteAov), output resolution
+    albedo: np.ndarray = None      # (H, W, 3)
+    normal: np.ndarray = None      # (H, W, 3)
+    bentNormal: np.ndarray = None  # (H, W, 3)
+    contactAo: np.ndarray = None   # (H, W)
+    shapeAo: np.ndarray = None     # (H, W)
+    avgHitDist: np.ndarray = None  # (H, W)
+
+
+AOV_FIELDS = (("albedo", "albedo", 3), ("normal", "normal", 3), ("bentNormal", "bent_normal", 3),
+              ("contactAo", "contact_ao", 1), ("shapeAo", "shape_ao", 1), ("avgHitDist", "avg_hit_dist", 1))
+
+
+def attach_aovs(fr, opt) -> dict:
+    """Allocate the AO AOV planes of a frame when opt.aoWriteAov asks for them."""
+    out = {}
+    if opt.aoWriteAov:
+        for name, cname, ch in AOV_FIELDS:
+            a = np.zeros((opt.height, opt.width, ch) if ch > 1 else (opt.height, opt.width), np.float32)
+            out[name] = a
+            setattr(fr, cname, abi.ptr(a))
+    return out
 
 
 class Context:
@@ -330,6 +354,7 @@ class Context:
         fr.view_z = abi.ptr(vz)
         fr.hit_geom = abi.ptr(hg, C.c_uint32)
         fr.hit_prim = abi.ptr(hp, C.c_uint32)
+        aovs = attach_aovs(fr, opt)
         cptr = cancel.ctypes.data_as(C.POINTER(C.c_int32)) if cancel is not None else None
         st = self._L.ubr_render(self.handle, built.handle, C.byref(rd), C.byref(fr), cptr, None)
         stats = dict(render_ms=fr.render_ms, total_ms=fr.total_ms, rays_primary=fr.rays_primary,
@@ -337,7 +362,7 @@ class Context:
                      stack_overflows=fr.stack_overflows, layers=fr.layers, kernels=fr.kernels)
         if st not in (abi.UBR_OK,):
             self._check(st)
-        return FrameResult(opt.width, opt.height, color, depth, vz, hg, hp, fr.render_ms / 1e3, stats)
+        return FrameResult(opt.width, opt.height, color, depth, vz, hg, hp, fr.render_ms / 1e3, stats, **aovs)
 
     def render_batch(self, items, want_ids: bool = True, flags: int = 0):
         """Render [(built, scene, opt), ...] in one launch sequence

@@ -49,6 +49,9 @@ struct Bufs {
   uint2* surfC;       // pixel, flags (1 hit, 2 AO, 4 shadows)
   uint8_t* occ;       // per slot * raysPerHit
   float* aoT;         // per slot * aoSamples (enhanced AO nearest t)
+  float4* aovA;       // per hi-res pixel first-hit AOVs (or null): albedo.rgb, contact
+  float4* aovB;       //   normal.xyz, shape
+  float4* aovC;       //   bent normal.xyz, mean occluder distance
   const LightD* lights;
   unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
   uint32_t* counter;  // [0] next-queue size, [1] occlusion work-queue size
@@ -200,7 +203,7 @@ UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, uint32_
       dir = aoDir(p, f, px, py, j);
       o.grazing = dot(dir, N) < 0.01f;
       o.trace = !o.grazing;
-      o.anyHit = !p.aoEnhanced;
+      o.anyHit = !(p.aoEnhanced || p.aoWriteAov);
       o.start = __float_as_int(sb.w);
       tfar = p.aoDistance;
     }
@@ -234,7 +237,8 @@ UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, uint32_
 UBR_D void occlusionWrite(const Params& p, const Bufs& b, uint64_t R, uint64_t aoStride, uint32_t slot, int j,
                           const OccRay& o, bool hit, float t) {
   const uint8_t res = o.grazing ? 1 : (hit ? 1 : 0);
-  if (o.ao && p.aoEnhanced) b.aoT[uint64_t(slot) * aoStride + j] = o.grazing ? -1.0f : (hit ? t : kInfF);
+  if (o.ao && (p.aoEnhanced || p.aoWriteAov))
+    b.aoT[uint64_t(slot) * aoStride + j] = o.grazing ? -1.0f : (hit ? t : kInfF);
   b.occ[uint64_t(slot) * R + j] = res;
 }
 
@@ -280,7 +284,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p1, DScene s1
       h.t = kInfF;
       if (o.trace) {
         const TravScene ts = travOf(s);
-        hit = p.aoEnhanced ? traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit, o.start)
+        hit = (p.aoEnhanced || p.aoWriteAov) ? traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit, o.start)
                            : traverse<COUNT, KM, true>(ts, o.r, h, ovf, &cnt, true, o.start);
         traced = 1;
       }
@@ -328,7 +332,8 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_gs(Params p1, DScene
       h.t = kInfF;
       if (o.trace) {
         const TravScene ts = travOf(s);
-        hit = p.aoEnhanced ? traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit, o.start, sTop, nTop)
+        hit = (p.aoEnhanced || p.aoWriteAov)
+                  ? traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit, o.start, sTop, nTop)
                            : traverse<COUNT, KM, true>(ts, o.r, h, ovf, &cnt, true, o.start, sTop, nTop);
         ++traced;
       }
@@ -426,6 +431,76 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p1
   }
 }
 
+// computeAOQuality accumulation over a hit's stored nearest-hit distances
+// (ambient_occlusion.hpp:171-267), sample order preserved: the openness for
+// the enhanced estimator and the contact / shape / bent-normal / mean
+// occluder distance AOVs.
+struct AoQ {
+  float openness = 1.0f, contact = 1.0f, shape = 1.0f, avgHit = 0.0f;
+  f3 bent{0.0f, 0.0f, 0.0f};
+};
+UBR_D AoQ aoQuality(const Params& p, const float* aoT, uint64_t aoStride, uint32_t i, f3 N, int px, int py,
+                    float power, bool multiScale) {
+  const float R = p.aoDistance;
+  float radius[3], weight[3];
+  int K;
+  if (multiScale) {
+    K = 3;
+    radius[0] = 0.08f * R; radius[1] = 0.30f * R; radius[2] = 1.00f * R;
+    weight[0] = 0.55f; weight[1] = 0.35f; weight[2] = 0.10f;
+  } else {
+    K = 1;
+    radius[0] = radius[1] = radius[2] = R;
+    weight[0] = 1.0f; weight[1] = weight[2] = 0.0f;
+  }
+  const Frame3 f = frameFromNormal(N);
+  float obsScale[3] = {0.0f, 0.0f, 0.0f};
+  float weightedObs = 0.0f, hitDistSum = 0.0f;
+  int nHit = 0;
+  f3 bentAccum{0.0f, 0.0f, 0.0f};
+  for (int k = 0; k < p.aoSamples; ++k) {
+    const f3 dir = aoDir(p, f, px, py, k);
+    if (dot(dir, N) < 0.01f) {
+      obsScale[0] += 1.0f; obsScale[1] += 1.0f; obsScale[2] += 1.0f;
+      weightedObs += 1.0f;
+      continue;
+    }
+    const float th = aoT[uint64_t(i) * aoStride + k];
+    float perSample = 0.0f;
+    for (int q = 0; q < K; ++q) {
+      if (th < radius[q]) {
+        float fk = 1.0f;
+        if (power > 0.0f) {
+          float a = 1.0f - th / radius[q];
+          if (a < 0.0f) a = 0.0f;
+          fk = powf(a, power);
+        }
+        obsScale[q] += fk;
+        perSample += weight[q] * fk;
+      }
+    }
+    weightedObs += perSample;
+    bentAccum = bentAccum + dir * (1.0f - perSample);
+    if (th < R) {
+      hitDistSum += th;
+      ++nHit;
+    }
+  }
+  AoQ r;
+  const float invN = 1.0f / float(p.aoSamples);
+  r.openness = 1.0f - weightedObs * invN;
+  r.contact = 1.0f - obsScale[0] * invN;
+  if (multiScale) {
+    const float wMid = weight[1] + weight[2];
+    r.shape = 1.0f - (weight[1] * obsScale[1] + weight[2] * obsScale[2]) / (wMid * float(p.aoSamples));
+  } else {
+    r.shape = r.openness;
+  }
+  r.bent = safeNormalize(bentAccum, N);
+  r.avgHit = nHit > 0 ? hitDistSum / float(nHit) : R;
+  return r;
+}
+
 template <bool BATCH>
 __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, Bufs b, int layer, uint32_t n,
                                                const uint32_t* queue, uint32_t* outQueue) {
@@ -460,6 +535,7 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
       f3 ambLight = p.ambLight;
       float diffuseAo = 1.0f;
       const uint64_t rb = uint64_t(i) * R;
+      AoQ aq;  // AOVs of this hit (neutral unless computed)
       if (sf.aoOn) {
         float openness;
         f3 bent = sf.N;
@@ -467,51 +543,13 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
           int hits = 0;
           for (int k = 0; k < p.aoSamples; ++k) hits += b.occ[rb + k];
           openness = 1.0f - float(hits) / float(p.aoSamples);
+          // aoWriteAov on the legacy estimator: one single-scale quality pass
+          // over the same sample stream (ao_shade.hpp:58-70)
+          if (p.aoWriteAov && sf.kind == kMesh) aq = aoQuality(p, b.aoT, aoStride, i, sf.N, px, py, 0.0f, false);
         } else {
-          // computeAOQuality accumulation, sample order preserved
-          const float R = p.aoDistance;
-          float radius[3], weight[3];
-          int K;
-          if (p.aoMultiScale) {
-            K = 3;
-            radius[0] = 0.08f * R; radius[1] = 0.30f * R; radius[2] = 1.00f * R;
-            weight[0] = 0.55f; weight[1] = 0.35f; weight[2] = 0.10f;
-          } else {
-            K = 1;
-            radius[0] = radius[1] = radius[2] = R;
-            weight[0] = 1.0f; weight[1] = weight[2] = 0.0f;
-          }
-          const Frame3 f = frameFromNormal(sf.N);
-          float obsScale[3] = {0.0f, 0.0f, 0.0f};
-          float weightedObs = 0.0f;
-          f3 bentAccum{0.0f, 0.0f, 0.0f};
-          for (int k = 0; k < p.aoSamples; ++k) {
-            const f3 dir = aoDir(p, f, px, py, k);
-            if (dot(dir, sf.N) < 0.01f) {
-              obsScale[0] += 1.0f; obsScale[1] += 1.0f; obsScale[2] += 1.0f;
-              weightedObs += 1.0f;
-              continue;
-            }
-            const float th = b.aoT[uint64_t(i) * aoStride + k];
-            float perSample = 0.0f;
-            for (int q = 0; q < K; ++q) {
-              if (th < radius[q]) {
-                float fk = 1.0f;
-                if (p.aoFalloffPower > 0.0f) {
-                  float a = 1.0f - th / radius[q];
-                  if (a < 0.0f) a = 0.0f;
-                  fk = powf(a, p.aoFalloffPower);
-                }
-                obsScale[q] += fk;
-                perSample += weight[q] * fk;
-              }
-            }
-            weightedObs += perSample;
-            bentAccum = bentAccum + dir * (1.0f - perSample);
-          }
-          const float invN = 1.0f / float(p.aoSamples);
-          openness = 1.0f - weightedObs * invN;
-          bent = safeNormalize(bentAccum, sf.N);
+          aq = aoQuality(p, b.aoT, aoStride, i, sf.N, px, py, p.aoFalloffPower, p.aoMultiScale != 0);
+          openness = aq.openness;
+          bent = aq.bent;
         }
         if (p.aoEnhanced && p.aoBentNormal) {
           const float w = 0.5f * (dot(bent, p.aoUp) + 1.0f);
@@ -600,6 +638,14 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
       }
       // --- first-hit capture + compositing (transparency.hpp:394-467) ---
       if (b.depth[gpix] == 0.0f) {
+        if (b.aovA && p.aoWriteAov) {
+          // first-hit AO AOVs (hit_shader.hpp:207-213: mesh hits only)
+          if (sf.kind == kMesh) {
+            b.aovA[gpix] = make_float4(sf.C.x, sf.C.y, sf.C.z, aq.contact);
+            b.aovB[gpix] = make_float4(sf.N.x, sf.N.y, sf.N.z, aq.shape);
+            b.aovC[gpix] = make_float4(aq.bent.x, aq.bent.y, aq.bent.z, aq.avgHit);
+          }
+        }
         b.depth[gpix] = t;
         b.viewZ[gpix] = t * dot(rd, p.camDir);
         b.hitGeom[gpix] = s.geomID[sf.kind];
@@ -712,13 +758,61 @@ __global__ void k_post(Params p1, Batch bt, uint32_t nOut, const float4* colorHi
   out[go] = r;
 }
 
-__global__ void k_init_pixels(uint32_t npix, float* depth, float* viewZ, uint32_t* hg, uint32_t* hp) {
+__global__ void k_init_pixels(uint32_t npix, float* depth, float* viewZ, uint32_t* hg, uint32_t* hp, float4* aovA,
+                              float4* aovB, float4* aovC) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npix) return;
   depth[i] = 0.0f;
   viewZ[i] = 0.0f;
   hg[i] = kInvalid;
   hp[i] = kInvalid;
+  if (aovA) {  // neutral AOVs of a pixel without a mesh first hit
+    aovA[i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    aovB[i] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    aovC[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
+// AO AOVs to the output resolution: box average with the non-finite guard
+// (pipeline.cpp:182-206 boxDownsample of albedo / normal / contact / shape /
+// avgHitDist / bentNormal; a copy at ss == 1), unpacked into the FrameResult
+// plane layouts (3, 3, 3, 1, 1, 1 floats per pixel).
+template <bool BATCH>
+__global__ void k_post_aov(Params p1, Batch bt, uint32_t nOut, const float4* aovA, const float4* aovB,
+                           const float4* aovC, float* alb, float* nrm, float* bent, float* con, float* shp,
+                           float* avg) {
+  const uint32_t go = blockIdx.x * blockDim.x + threadIdx.x;
+  if (go >= nOut) return;
+  const int f = BATCH ? frameOf(bt.outOffs, bt.nFrames, go) : 0;
+  const Params& p = BATCH ? bt.frames[f].p : p1;
+  const size_t pixOff = BATCH ? bt.frames[f].pixOff : 0u;
+  const int o = int(go - (BATCH ? bt.frames[f].outOff : 0u));
+  const int ox = o % p.outW, oy = o / p.outW;
+  const int ss = p.ss;
+  float a[12];
+  if (ss == 1) {
+    const size_t hp = pixOff + size_t(oy) * p.W + ox;
+    const float4 A = aovA[hp], B = aovB[hp], C = aovC[hp];
+    const float v[12] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w, C.x, C.y, C.z, C.w};
+    for (int k = 0; k < 12; ++k) a[k] = v[k];
+  } else {
+    for (int k = 0; k < 12; ++k) a[k] = 0.0f;
+    for (int dy = 0; dy < ss; ++dy)
+      for (int dx = 0; dx < ss; ++dx) {
+        const size_t hp = pixOff + size_t(oy * ss + dy) * p.W + size_t(ox * ss + dx);
+        const float4 A = aovA[hp], B = aovB[hp], C = aovC[hp];
+        const float v[12] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w, C.x, C.y, C.z, C.w};
+        for (int k = 0; k < 12; ++k) a[k] += isfinite(v[k]) ? v[k] : 0.0f;
+      }
+    const float inv = 1.0f / float(ss * ss);
+    for (int k = 0; k < 12; ++k) a[k] *= inv;
+  }
+  alb[3 * size_t(go)] = a[0]; alb[3 * size_t(go) + 1] = a[1]; alb[3 * size_t(go) + 2] = a[2];
+  con[go] = a[3];
+  nrm[3 * size_t(go)] = a[4]; nrm[3 * size_t(go) + 1] = a[5]; nrm[3 * size_t(go) + 2] = a[6];
+  shp[go] = a[7];
+  bent[3 * size_t(go)] = a[8]; bent[3 * size_t(go) + 1] = a[9]; bent[3 * size_t(go) + 2] = a[10];
+  avg[go] = a[11];
 }
 
 }  // namespace
@@ -766,6 +860,7 @@ ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vect
   p.aoSky = f3{d.ao_sky_color[0], d.ao_sky_color[1], d.ao_sky_color[2]};
   p.aoGround = f3{d.ao_ground_color[0], d.ao_ground_color[1], d.ao_ground_color[2]};
   p.aoDiffuseFactor = d.ao_diffuse_factor;
+  p.aoWriteAov = d.ao_write_aov ? 1 : 0;
   p.aoEnhanced = (d.ao_falloff_power > 0.0f || d.ao_multiscale || d.ao_bent_normal || d.ao_multibounce ||
                   d.ao_low_discrepancy || d.ao_diffuse_factor > 0.0f)
                      ? 1
@@ -1018,7 +1113,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   uint64_t npix64 = 0, nout64 = 0;
   uint32_t R = 0, aoStride = 0, aoMin = 0xFFFFFFFFu;
   int km = 0, maxIters = 1;
-  bool secondary = false, enhanced = false, singleLayer = true;
+  bool secondary = false, enhanced = false, singleLayer = true, aov = false;
   for (size_t f = 0; f < nf; ++f) {
     std::vector<LightD> fl;
     Params& p = fds[f].p;
@@ -1035,11 +1130,12 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     nout64 += uint64_t(p.outW) * uint64_t(p.outH);
     R = std::max(R, uint32_t(p.raysPerHit));
     aoMin = std::min(aoMin, uint32_t(p.aoSamples));
-    if (p.aoEnhanced && p.aoSamples > 0) {
+    if ((p.aoEnhanced || p.aoWriteAov) && p.aoSamples > 0) {
       enhanced = true;
       aoStride = std::max(aoStride, uint32_t(p.aoSamples));
     }
     secondary = secondary || p.raysPerHit > 0;
+    aov = aov || p.aoWriteAov;
     if (!(p.maxIters == 1 || jobs[f].scene->opaque)) singleLayer = false;
     maxIters = std::max(maxIters, jobs[f].scene->opaque ? 1 : p.maxIters);
     km |= kindMaskBits(*jobs[f].scene);
@@ -1077,6 +1173,13 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   b.stats = scratchT<unsigned long long>(c, 33, 8, st);
   b.counter = scratchT<uint32_t>(c, 34, 4, st);
   float4* outColor = scratchT<float4>(c, 35, nout, st);
+  float* outAov = nullptr;  // albedo 3, normal 3, bent 3, contact, shape, avg per output pixel
+  if (aov) {
+    b.aovA = scratchT<float4>(c, 70, npix, st);
+    b.aovB = scratchT<float4>(c, 71, npix, st);
+    b.aovC = scratchT<float4>(c, 72, npix, st);
+    outAov = scratchT<float>(c, 73, size_t(nout) * 12, st);
+  }
   Batch bt{};
   if (batch) {
     FrameDesc* dfd = scratchT<FrameDesc>(c, 38, nf, st);
@@ -1156,6 +1259,17 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     mark(4, true);
     if (batch) k_post<true><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.colorHi, b.viewZ, outColor);
     else k_post<false><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.colorHi, b.viewZ, outColor);
+    if (aov) {
+      float* o = outAov;
+      const size_t n = nout;
+      if (batch)
+        k_post_aov<true><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.aovA, b.aovB, b.aovC, o, o + 3 * n,
+                                                             o + 6 * n, o + 9 * n, o + 10 * n, o + 11 * n);
+      else
+        k_post_aov<false><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.aovA, b.aovB, b.aovC, o, o + 3 * n,
+                                                              o + 6 * n, o + 9 * n, o + 10 * n, o + 11 * n);
+      ++kernels;
+    }
     mark(4, false);
     ++kernels;
     UBR_CUDA(c, cudaGetLastError());
@@ -1185,7 +1299,8 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     if (!c->graphExec || key != c->graphKey) {
       UBR_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s);
-      k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim);
+      k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim, b.aovA,
+                                                       b.aovB, b.aovC);
       ubr_status rs = round(0, npix, nullptr, q0);
       if (rs == UBR_OK) rs = post();
       cudaGraph_t graph = nullptr;
@@ -1215,7 +1330,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       cudaGraphDestroy(graph);
       c->graphKey = key;
     } else {
-      kernels = (secondary ? 4u : 2u) + 1u;
+      kernels = (secondary ? 4u : 2u) + 1u + (aov ? 1u : 0u);
     }
     cudaEventRecord(c->ev[2], s);
     UBR_CUDA(c, cudaGraphLaunch(c->graphExec, s));
@@ -1224,7 +1339,8 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     ++kernels;  // k_init_pixels
   } else {
     UBR_CUDA(c, cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s));
-    k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim);
+    k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim, b.aovA,
+                                                       b.aovB, b.aovC);
     ++kernels;
     cudaEventRecord(c->ev[2], s);
     uint32_t n = npix;
@@ -1266,6 +1382,16 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     if (fr.view_z) UBR_CUDA(c, cudaMemcpyAsync(fr.view_z, b.viewZ + po, fpix * 4, kind, s));
     if (fr.hit_geom) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_geom, b.hitGeom + po, fpix * 4, kind, s));
     if (fr.hit_prim) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_prim, b.hitPrim + po, fpix * 4, kind, s));
+    if (p.aoWriteAov) {
+      const float* o = outAov;
+      const size_t n = nout;
+      float* dst[6] = {fr.albedo, fr.normal, fr.bent_normal, fr.contact_ao, fr.shape_ao, fr.avg_hit_dist};
+      const size_t base[6] = {0, 3 * n, 6 * n, 9 * n, 10 * n, 11 * n};
+      const size_t width[6] = {3, 3, 3, 1, 1, 1};
+      for (int k = 0; k < 6; ++k)
+        if (dst[k])
+          UBR_CUDA(c, cudaMemcpyAsync(dst[k], o + base[k] + width[k] * oo, width[k] * fout * 4, kind, s));
+    }
   }
   unsigned long long* hs = reinterpret_cast<unsigned long long*>(static_cast<char*>(c->pinned) + 64);
   UBR_CUDA(c, cudaMemcpyAsync(hs, b.stats, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));

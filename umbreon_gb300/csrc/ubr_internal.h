@@ -449,6 +449,7 @@ struct Params {
   int aoSamples;
   float aoDistance, aoIntensity, aoFalloffPower;
   int aoMultiScale, aoBentNormal, aoMultibounce, aoLowDiscrepancy, aoEnhanced;
+  int aoWriteAov;       // first-hit AO AOVs requested (AO rays trace nearest hits)
   f3 aoSky, aoGround;
   float aoDiffuseFactor;
   int shadowsActive, shadowSamples;

@@ -384,6 +384,7 @@ ubr_render_desc toRenderDesc(const Scene& s, const RenderOptions& o, std::vector
   d.transparent_background = o.transparentBackground;
   d.max_transparent_layers = o.maxTransparentLayers;
   d.gi_integrator = o.giIntegrator;
+  d.ao_write_aov = o.aoWriteAov ? 1u : 0u;
   return d;
 }
 
@@ -434,6 +435,22 @@ FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderP
   fr.color = f.color.data();
   fr.depth = f.depth.data();
   fr.view_z = f.viewZ.empty() ? nullptr : f.viewZ.data();
+  if (opt.aoWriteAov) {
+    // AO AOVs at the output resolution (allocateFrameBuffers neutral values;
+    // renderFrame box-averages them with the colour)
+    f.albedo.assign(nout * 3, 0.0f);
+    f.normal.assign(nout * 3, 0.0f);
+    f.bentNormal.assign(nout * 3, 0.0f);
+    f.contactAo.assign(nout, 1.0f);
+    f.shapeAo.assign(nout, 1.0f);
+    f.avgHitDist.assign(nout, 0.0f);
+    fr.albedo = f.albedo.data();
+    fr.normal = f.normal.data();
+    fr.bent_normal = f.bentNormal.data();
+    fr.contact_ao = f.contactAo.data();
+    fr.shape_ao = f.shapeAo.data();
+    fr.avg_hit_dist = f.avgHitDist.data();
+  }
   // The C-ABI polls a plain int between rounds; mirror the progress cancel
   // flag into it while the render runs.
   volatile int32_t cancelFlag = 0;
