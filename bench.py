@@ -285,11 +285,11 @@ def secondary_workloads(args, flush):
 
     def tuned(sc, opt):
         """Context with the knobs given on the command line, else autotuned."""
-        if args.builder or args.leaf_max or args.trace_mode:
-            return Context(0, bvh_leaf_max=args.leaf_max, trace_mode=args.trace_mode, bvh_builder=args.builder), None
+        knobs = _knobs(args)
+        if knobs is not None:
+            return Context(0, **knobs), knobs
         t = autotune(sc, opt, pixels=512 * 512)
-        return Context(0, bvh_leaf_max=t["bvh_leaf_max"], trace_mode=t["trace_mode"],
-                       bvh_builder=t["bvh_builder"]), {k: t[k] for k in ("bvh_builder", "bvh_leaf_max", "trace_mode")}
+        return Context(0, **t["context"]), t["context"]
 
     # workload 0
     sc, opt = scenes.space_filling()
@@ -335,8 +335,7 @@ def secondary_workloads(args, flush):
                        ("turntable_64_small_256", [(si, sc2, _resized(o, 256)) for si, sc2, o in items])):
         entry = {}
         for mode, graphs in (("batched", True), ("per_frame_graph", True), ("per_frame_no_graph", False)):
-            cx = Context(0, bvh_leaf_max=tune["bvh_leaf_max"], trace_mode=tune["trace_mode"], graphs=graphs,
-                         bvh_builder=args.builder or tune["bvh_builder"])
+            cx = Context(0, graphs=graphs, **(_knobs(args) or tune["context"]))
             built = [cx.build(bs) for bs in bases]
             descs, outs, frames = [], [], []
             for si, sc2, o in its:
@@ -388,6 +387,14 @@ def secondary_workloads(args, flush):
     return out
 
 
+def _knobs(args):
+    """Context tuning fields given on the command line, or None (autotune)."""
+    if not (args.builder or args.leaf_max or args.trace_mode or args.collapse or args.sah_scale):
+        return None
+    return dict(bvh_builder=args.builder, bvh_leaf_max=args.leaf_max, trace_mode=args.trace_mode,
+                bvh_collapse=args.collapse, sah_prim_scale=args.sah_scale)
+
+
 def _resized(opt, res):
     import copy
     o = copy.copy(opt)
@@ -413,12 +420,12 @@ def run_ours(args):
         opt.supersample = args.ss
     # traversal knobs: as given, else what the autotuner picks on a downscaled frame
     tune = None
-    builder, leaf_max, trace_mode = args.builder, args.leaf_max, args.trace_mode
-    if not (builder or leaf_max or trace_mode):
+    knobs = _knobs(args)
+    if knobs is None:
         from umbreon_gb300.autotune import autotune
         tune = autotune(sc, opt, device=local, pixels=512 * 512)
-        builder, leaf_max, trace_mode = tune["bvh_builder"], tune["bvh_leaf_max"], tune["trace_mode"]
-    ctx = Context(local, bvh_leaf_max=leaf_max, trace_mode=trace_mode, bvh_builder=builder)
+        knobs = tune["context"]
+    ctx = Context(local, **knobs)
     built = ctx.build(sc)
     info = built.info()
     import ctypes as C
@@ -536,8 +543,7 @@ def run_ours(args):
                        "frame": f"{opt.width}x{opt.height} ss{opt.supersample}",
                        "primitives": info["prim_count"], "bvh_nodes": info["bvh_nodes"],
                        "l2": "flushed (256 MB write) before every timed frame",
-                       "traversal": {"bvh_builder": builder, "bvh_leaf_max": leaf_max, "trace_mode": trace_mode,
-                                     "autotuned": tune["table"] if tune else None},
+                       "traversal": dict(knobs, autotuned=tune["table"] if tune else None),
                        "parallelism": f"replicas x{ws}"},
             "ms_per_frame": round(ms_frame, 3),
             "phase_ms_per_frame": {n: round(v / args.steps, 3) for n, v in zip(names, phase)},
@@ -565,6 +571,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="ball_and_stick", choices=sorted(WORKLOADS),
                     help="scene of the headline line (default: the ball-and-stick benchmark frame)")
+    ap.add_argument("--collapse", type=int, default=0, help="8-wide collapse (0 default, 1 greedy, 2 SAH)")
+    ap.add_argument("--sah-scale", type=float, default=0.0, help="SAH collapse primitive-cost scale (0 = 1)")
     ap.add_argument("--builder", type=int, default=0, help="BVH builder (0 library default, 1 radix tree, 2 PLOC)")
     ap.add_argument("--no-secondary", action="store_true", help="skip the other workloads (space filling, "
                     "molecular surface, batched turntable)")

@@ -276,7 +276,15 @@ typedef struct ubr_context_desc {
    * codes, 2 = locally-ordered clustering (PLOC) over the same Morton order;
    * leaf sizes above 1 always use the radix tree */
   uint32_t bvh_builder;
-  uint32_t reserved[4];
+  /* binary -> 8-wide collapse (0 = library default): 1 = greedy (open the
+   * largest child, leaves of bvh_leaf_max primitives), 2 = SAH-optimal
+   * dynamic programme choosing every node's children and leaves of 1..3
+   * primitives */
+  uint32_t bvh_collapse;
+  /* SAH collapse: weight of a primitive test against a node visit, as a
+   * multiple of the library's per-kind weights (0 = 1) */
+  float bvh_sah_prim_scale;
+  uint32_t reserved[2];
 } ubr_context_desc;
 
 const char* ubr_status_string(ubr_status s);

@@ -1,5 +1,6 @@
-"""The two BVH builders (Karras radix tree, PLOC clustering) give the same
-frames: hits do not depend on the tree (ties resolve to the lowest ids)."""
+"""The BVH builders (Karras radix tree, PLOC clustering) and collapses
+(greedy, SAH-optimal) give the same frames: hits do not depend on the tree
+(ties resolve to the lowest ids)."""
 import numpy as np
 import pytest
 
@@ -21,15 +22,16 @@ def test_builders_render_identically(name):
     from umbreon_gb300.api import Context
     sc, opt = CASES[name]()
     out = {}
-    for builder in (1, 2):
-        ctx = Context(0, bvh_builder=builder)
+    for key in ((1, 1), (2, 1), (1, 2), (2, 2)):  # (builder, collapse)
+        ctx = Context(0, bvh_builder=key[0], bvh_collapse=key[1])
         b = ctx.build(sc)
         fr = ctx.render(b, sc, opt)
-        out[builder] = (fr.color.copy(), fr.hit_prim.copy(), b.info()["bvh_nodes"])
+        out[key] = (fr.color.copy(), fr.hit_prim.copy(), b.info()["bvh_nodes"])
         b.release()
         ctx.close()
-    assert np.array_equal(out[1][1], out[2][1])
-    assert np.array_equal(out[1][0], out[2][0])
+    for key in out:
+        assert np.array_equal(out[(1, 1)][1], out[key][1]), key
+        assert np.array_equal(out[(1, 1)][0], out[key][0]), key
 
 
 @pytest.mark.parametrize("name", sorted(CASES))

@@ -128,7 +128,7 @@ class ContextDesc(C.Structure):
     _fields_ = [("abi_version", C.c_uint32), ("device", C.c_int32), ("arena_bytes", C.c_uint64),
                 ("stream", C.c_void_p), ("bvh_leaf_max", C.c_uint32), ("trace_mode", C.c_uint32),
                 ("disable_graphs", C.c_uint32), ("bvh_builder", C.c_uint32),
-                ("reserved", C.c_uint32 * 4)]
+                ("bvh_collapse", C.c_uint32), ("bvh_sah_prim_scale", C.c_float), ("reserved", C.c_uint32 * 2)]
 
 
 class SceneInfo(C.Structure):

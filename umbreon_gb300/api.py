@@ -316,12 +316,13 @@ class Context:
     """One GPU, one stream (ubr_context)."""
 
     def __init__(self, device: int = 0, arena_bytes: int = 0, stream: int | None = None, bvh_leaf_max: int = 0,
-                 trace_mode: int = 0, graphs: bool = True, bvh_builder: int = 0):
+                 trace_mode: int = 0, graphs: bool = True, bvh_builder: int = 0, bvh_collapse: int = 0,
+                 sah_prim_scale: float = 0.0):
         L = abi.lib()
         self._L = L
         h = C.c_void_p()
         cd = abi.ContextDesc(abi.ABI_VERSION, device, arena_bytes, stream, bvh_leaf_max, trace_mode,
-                             0 if graphs else 1, bvh_builder)
+                             0 if graphs else 1, bvh_builder, bvh_collapse, sah_prim_scale)
         st = L.ubr_context_create(C.byref(h), C.byref(cd))
         if st != abi.UBR_OK:
             raise abi.UbrError(st, "ubr_context_create failed")

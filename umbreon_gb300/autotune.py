@@ -1,12 +1,19 @@
 """Autotuner for the BVH and traversal knobs of a workload.
 
 Times a representative frame (downscaled to about `pixels` hi-res pixels, so
-tuning costs milliseconds) for every combination of the context tuning
-fields -- BVH builder (Morton radix tree or PLOC clustering, the latter at
-leaf size 1), wide-BVH leaf size (1..3 primitives) and the occlusion kernel
-(one thread per ray, or persistent warps refilling idle lanes) -- and returns
-the fastest.  Results depend on the scene's primitive mix and ray lengths,
-so a caller tunes once per scene class and creates its context with them.
+tuning costs a second or two) for every candidate setting of the context
+tuning fields and returns the fastest:
+
+* BVH builder: Morton radix tree or PLOC clustering over the same order;
+* 8-wide collapse: greedy with a fixed leaf size (1..3 primitives), or the
+  SAH-optimal dynamic programme at a few weights of primitive tests against
+  node visits (its leaves hold 1..3 primitives as the costs decide);
+* occlusion kernel: one thread per ray, persistent warps refilling idle
+  lanes, or a resident grid with the top BVH levels in shared memory.
+
+Results depend on the scene's primitive mix and ray lengths, so a caller
+tunes once per scene class and creates its context with the result
+(`Context(**result["context"])`).
 """
 from __future__ import annotations
 
@@ -16,9 +23,15 @@ import math
 
 from .api import Context
 
+# (label, context fields) of the tree candidates
+TREES = (
+    [(f"greedy_leaf{leaf}", dict(bvh_collapse=1, bvh_leaf_max=leaf)) for leaf in (1, 2, 3)] +
+    [(f"sah_x{scale:g}", dict(bvh_collapse=2, sah_prim_scale=scale)) for scale in (1.0, 2.0, 4.0)]
+)
+
 
 def autotune(scene, opt, device: int = 0, pixels: int = 256 * 256, repeats: int = 3,
-             leaf_sizes=(1, 2, 3), trace_modes=(1, 2, 3), builders=(1, 2)):
+             builders=(1, 2), trees=TREES, trace_modes=(1, 2, 3)):
     small = copy.copy(opt)
     ss = max(1, opt.supersample)
     scale = math.sqrt(pixels / float(opt.width * opt.height * ss * ss))
@@ -26,18 +39,22 @@ def autotune(scene, opt, device: int = 0, pixels: int = 256 * 256, repeats: int 
         small.width = max(16, int(opt.width * scale))
         small.height = max(16, int(opt.height * scale))
     results = {}
-    for builder, leaf, mode in itertools.product(builders, leaf_sizes, trace_modes):
-        if builder == 2 and leaf != 1:
-            continue  # PLOC trees are built for single-primitive leaves
-        ctx = Context(device, bvh_leaf_max=leaf, trace_mode=mode, bvh_builder=builder)
-        built = ctx.build(scene)
-        try:
-            ctx.render(built, scene, small, want_ids=False)  # warm-up (graph capture)
-            best = min(ctx.render(built, scene, small, want_ids=False).stats["total_ms"] for _ in range(repeats))
-        finally:
-            built.release()
-            ctx.close()
-        results[(builder, leaf, mode)] = best
-    (builder, leaf, mode), ms = min(results.items(), key=lambda kv: kv[1])
-    return {"bvh_builder": builder, "bvh_leaf_max": leaf, "trace_mode": mode, "ms": ms,
-            "table": {f"builder{b}_leaf{l}_mode{m}": round(v, 4) for (b, l, m), v in results.items()}}
+    for builder, (tlabel, tfields) in itertools.product(builders, trees):
+        # one scene build per tree; the occlusion kernel is a render-time choice
+        for mode in trace_modes:
+            fields = dict(tfields, bvh_builder=builder, trace_mode=mode)
+            ctx = Context(device, **fields)
+            built = ctx.build(scene)
+            try:
+                ctx.render(built, scene, small, want_ids=False)  # warm-up (graph capture)
+                best = min(ctx.render(built, scene, small, want_ids=False).stats["total_ms"]
+                           for _ in range(repeats))
+            finally:
+                built.release()
+                ctx.close()
+            results[(builder, tlabel, mode)] = (best, fields)
+    (builder, tlabel, mode), (ms, fields) = min(results.items(), key=lambda kv: kv[1][0])
+    return {"context": fields, "bvh_builder": builder, "tree": tlabel, "trace_mode": mode, "ms": ms,
+            "bvh_leaf_max": fields.get("bvh_leaf_max", 0), "bvh_collapse": fields["bvh_collapse"],
+            "sah_prim_scale": fields.get("sah_prim_scale", 0.0),
+            "table": {f"builder{b}_{t}_mode{m}": round(v[0], 4) for (b, t, m), v in results.items()}}

@@ -146,6 +146,20 @@ ubr_status ubr_context_create(ubr_context** out, const ubr_context_desc* desc) {
     }
     x.builder = int(desc->bvh_builder);
   }
+  if (desc && desc->bvh_collapse) {
+    if (desc->bvh_collapse > 2) {
+      delete c;
+      return UBR_INVALID_ARGUMENT;
+    }
+    x.collapse = int(desc->bvh_collapse);
+  }
+  if (desc && desc->bvh_sah_prim_scale != 0.0f) {
+    if (!(desc->bvh_sah_prim_scale > 0.0f && desc->bvh_sah_prim_scale < 1000.0f)) {
+      delete c;
+      return UBR_INVALID_ARGUMENT;
+    }
+    x.sahPrimScale = desc->bvh_sah_prim_scale;
+  }
   if (cudaSetDevice(dev) != cudaSuccess) {
     delete c;
     return UBR_CUDA_ERROR;

@@ -602,7 +602,7 @@ __device__ __forceinline__ void writeBinNode(float4* nodes, int node, int c0, fl
 }
 
 __global__ void k_ploc_merge(int nc, const int* nn, int* code, float4* lo, float4* hi, int* cnt, float4* nodes,
-                             int2* ranges, int* nodeCounter, int* valid) {
+                             int2* ranges, int* nodeCounter, int* valid, int* leafParent, int* nodeParent) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nc) return;
   const int j = nn[i];
@@ -611,6 +611,11 @@ __global__ void k_ploc_merge(int nc, const int* nn, int* code, float4* lo, float
     const int node = atomicAdd(nodeCounter, 1);
     const float4 l0 = lo[i], h0 = hi[i], l1 = lo[j], h1 = hi[j];
     writeBinNode(nodes, node, code[i], l0, h0, code[j], l1, h1);
+    const int c0 = code[i], c1 = code[j];
+    if (c0 < 0) leafParent[~c0] = node << 1;
+    else nodeParent[c0] = node << 1;
+    if (c1 < 0) leafParent[~c1] = (node << 1) | 1;
+    else nodeParent[c1] = (node << 1) | 1;
     const int c = cnt[i] + cnt[j];
     ranges[node] = make_int2(0, c - 1);  // only the primitive count is read
     code[i] = node;
@@ -668,6 +673,247 @@ __device__ __forceinline__ void quantize(float lo, float hi, float p, float sc, 
   while (b < 255 && fmaf(float(b), sc, p) < hi) ++b;
   qlo = uint32_t(a);
   qhi = uint32_t(b);
+}
+
+// SAH-optimal collapse of the binary tree into 8-wide nodes (the dynamic
+// programme of Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal
+// on GPUs Through Compressed Wide BVHs", HPG 2017).  For binary node n and
+// j = 1..7 child slots, C(n, j) is the least cost of covering n's subtree
+// with at most j children of a wide node: C(n, 1) = min(leaf cost, internal
+// cost), C(n, j) = min(best split of j slots over n's two children,
+// C(n, j - 1)).  Leaf cost = area x the primitives' test costs (leaves hold
+// at most kWideLeafMax primitives), internal cost = area x node cost + the
+// best split of 8 slots.  Costs are per unit of node-visit work; primitive
+// test weights by kind reflect the intersectors' instruction counts.
+constexpr float kSahNode = 1.0f;
+__device__ __forceinline__ float sahPrimCost(int kind) {
+  return kind == kSphere ? 0.12f : kind == kMesh ? 0.16f : kind == kCone ? 0.25f : 0.35f;
+}
+constexpr float kSahInf = 3.0e38f;
+constexpr int kSahStride = 8;  // per node: C(n,1..7) and the sum of primitive costs
+
+// Cost row of a child: an internal node's stored row, or a single primitive.
+__device__ __forceinline__ void sahChildRow(const float* cost, int code, float3 lo, float3 hi,
+                                            const uint32_t* leafRef, float* row, float& sumC, int& cnt,
+                                            const int2* brange, float primScale) {
+  if (code < 0) {
+    const float c = primScale * sahPrimCost(refKind(leafRef[~code]));
+    const float a = halfArea(lo, hi) * c;
+    for (int j = 1; j <= 7; ++j) row[j] = a;
+    sumC = c;
+    cnt = 1;
+  } else {
+    const float* r = cost + kSahStride * code;
+    for (int j = 1; j <= 7; ++j) row[j] = __ldcg(r + j - 1);
+    sumC = __ldcg(r + 7);
+    cnt = brange[code].y - brange[code].x + 1;
+  }
+}
+
+// Bottom-up: one thread per leaf walks to the root; the second child to
+// arrive at a node computes the node's row (the refit pattern).
+__global__ void k_sah_costs(int n, const float4* nodes, const int2* brange, const uint32_t* leafRef,
+                            const int* leafParent, const int* nodeParent, int* counters, float* cost,
+                            uint8_t* dec, float primScale) {
+  const int sIdx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sIdx >= n) return;
+  int pinfo = leafParent[sIdx];
+  while (pinfo >= 0) {
+    const int p = pinfo >> 1;
+    __threadfence();
+    if (atomicAdd(&counters[p], 1) == 0) return;
+    __threadfence();
+    int c0, c1;
+    float3 lo0, hi0, lo1, hi1;
+    binChild(nodes, p, 0, c0, lo0, hi0);
+    binChild(nodes, p, 1, c1, lo1, hi1);
+    float r0[8], r1[8], s0, s1;
+    int n0, n1;
+    sahChildRow(cost, c0, lo0, hi0, leafRef, r0, s0, n0, brange, primScale);
+    sahChildRow(cost, c1, lo1, hi1, leafRef, r1, s1, n1, brange, primScale);
+    const float3 lo = make_float3(fminf(lo0.x, lo1.x), fminf(lo0.y, lo1.y), fminf(lo0.z, lo1.z));
+    const float3 hi = make_float3(fmaxf(hi0.x, hi1.x), fmaxf(hi0.y, hi1.y), fmaxf(hi0.z, hi1.z));
+    const float A = halfArea(lo, hi);
+    // best split of j slots over the two children, j = 2..8
+    float dist[9];
+    uint8_t split[9];
+    for (int j = 2; j <= 8; ++j) {
+      float best = kSahInf;
+      int bk = 1;
+      for (int k = 1; k < j; ++k) {
+        if (k > 7 || j - k > 7) continue;
+        const float c = r0[k] + r1[j - k];
+        if (c < best) {
+          best = c;
+          bk = k;
+        }
+      }
+      dist[j] = best;
+      split[j] = uint8_t(bk);
+    }
+    const int cnt = n0 + n1;
+    const float sumC = s0 + s1;
+    const float cLeaf = cnt <= kWideLeafMax ? A * sumC : kSahInf;
+    const float cInt = A * kSahNode + dist[8];
+    float* out = cost + kSahStride * p;
+    uint8_t* d = dec + 8 * p;
+    float cj = fminf(cLeaf, cInt);
+    out[0] = cj;
+    d[0] = cLeaf <= cInt ? 1 : 0;  // j = 1: 1 leaf, 0 wide node
+    for (int j = 2; j <= 7; ++j) {
+      if (dist[j] < cj) {
+        cj = dist[j];
+        d[j - 1] = split[j];       // split j slots: k to child 0
+      } else {
+        d[j - 1] = 0;              // no better than j - 1 slots
+      }
+      out[j - 1] = cj;
+    }
+    out[7] = sumC;
+    d[7] = split[8];               // the split of a wide node's 8 slots
+    pinfo = nodeParent[p];
+  }
+}
+
+// Primitive slots of a binary subtree with at most kWideLeafMax primitives.
+__device__ __forceinline__ int subtreePrims(const float4* nodes, int code, int* out) {
+  int stack[kWideLeafMax + 1], sp = 0, nOut = 0;
+  stack[sp++] = code;
+  while (sp > 0 && nOut < kWideLeafMax) {
+    const int c = stack[--sp];
+    if (c < 0) {
+      out[nOut++] = ~c;
+    } else {
+      const float4 cc = nodes[kNodeF4 * c + 3];
+      if (sp + 2 > kWideLeafMax + 1) break;
+      stack[sp++] = __float_as_int(cc.y);
+      stack[sp++] = __float_as_int(cc.x);
+    }
+  }
+  return nOut;
+}
+
+// Top-down collapse with the DP's decisions: a wide node made from binary
+// node n takes the children the 8-slot split of n selects; a child is a
+// single primitive, a leaf of up to kWideLeafMax primitives, or a binary node
+// that becomes a wide node of the next level.
+__global__ void k_collapse_sah(const float4* bnodes, const uint8_t* dec, const int* workCode, const int* workWide,
+                               int workCount, int* nextCode, int* nextWide, int* cursors, float4* wnodes,
+                               const uint32_t* srcRef, const float4* srcGeo, uint32_t* dstRef, float4* dstGeo) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= workCount) return;
+  const int code = workCode[i];
+  const int w = workWide[i];
+  int ec[8], et[8];  // child code, type: 0 leaf, 1 wide node
+  float3 elo[8], ehi[8];
+  int en = 0;
+  // stack of (binary parent, side, slots)
+  int sp = 0;
+  int stP[16], stS[16], stJ[16];
+  const int k8 = dec[8 * code + 7];
+  stP[sp] = code; stS[sp] = 1; stJ[sp] = 8 - k8; ++sp;
+  stP[sp] = code; stS[sp] = 0; stJ[sp] = k8; ++sp;
+  while (sp > 0 && en < 8) {
+    --sp;
+    const int par = stP[sp], side = stS[sp], j = stJ[sp];
+    int c;
+    float3 lo, hi;
+    binChild(bnodes, par, side, c, lo, hi);
+    if (c < 0) {
+      ec[en] = c; et[en] = 0; elo[en] = lo; ehi[en] = hi; ++en;
+      continue;
+    }
+    int jj = j;
+    while (jj > 1 && dec[8 * c + jj - 1] == 0) --jj;
+    if (jj <= 1) {
+      ec[en] = c; et[en] = dec[8 * c] ? 0 : 1; elo[en] = lo; ehi[en] = hi; ++en;
+      continue;
+    }
+    const int k = dec[8 * c + jj - 1];
+    if (sp + 2 > 16) break;  // cannot happen: at most 8 open entries
+    stP[sp] = c; stS[sp] = 1; stJ[sp] = jj - k; ++sp;
+    stP[sp] = c; stS[sp] = 0; stJ[sp] = k; ++sp;
+  }
+  int nInt = 0, nLeaf = 0;
+  int prims[8][kWideLeafMax], pc[8];
+  for (int k = 0; k < en; ++k) {
+    if (et[k] == 1) {
+      ++nInt;
+      pc[k] = 0;
+    } else {
+      pc[k] = subtreePrims(bnodes, ec[k], prims[k]);
+      nLeaf += pc[k];
+    }
+  }
+  const int childBase = nInt ? atomicAdd(&cursors[0], nInt) : 0;
+  const int primBase = nLeaf ? atomicAdd(&cursors[1], nLeaf) : 0;
+  const int pushBase = nInt ? atomicAdd(&cursors[2], nInt) : 0;
+  float3 p = elo[0], hmax = ehi[0];
+  for (int k = 1; k < en; ++k) {
+    p = make_float3(fminf(p.x, elo[k].x), fminf(p.y, elo[k].y), fminf(p.z, elo[k].z));
+    hmax = make_float3(fmaxf(hmax.x, ehi[k].x), fmaxf(hmax.y, ehi[k].y), fmaxf(hmax.z, ehi[k].z));
+  }
+  const uint32_t exX = scaleExp(hmax.x - p.x), exY = scaleExp(hmax.y - p.y), exZ = scaleExp(hmax.z - p.z);
+  const float scX = __uint_as_float(exX << 23), scY = __uint_as_float(exY << 23), scZ = __uint_as_float(exZ << 23);
+  uint32_t meta[2] = {0u, 0u}, qlx[2] = {0u, 0u}, qly[2] = {0u, 0u}, qlz[2] = {0u, 0u};
+  uint32_t qhx[2] = {0u, 0u}, qhy[2] = {0u, 0u}, qhz[2] = {0u, 0u};
+  int order[8];
+  {
+    int o = 0;
+    for (int k = 0; k < en; ++k)
+      if (et[k] == 1) order[o++] = k;
+    for (int k = 0; k < en; ++k)
+      if (et[k] == 0) order[o++] = k;
+  }
+  int kInt = 0, off = 0;
+  for (int slot = 0; slot < en; ++slot) {
+    const int k = order[slot];
+    uint32_t a, b;
+    const int wd = slot >> 2, sh = (slot & 3) * 8;
+    quantize(elo[k].x, ehi[k].x, p.x, scX, a, b);
+    qlx[wd] |= a << sh;
+    qhx[wd] |= b << sh;
+    quantize(elo[k].y, ehi[k].y, p.y, scY, a, b);
+    qly[wd] |= a << sh;
+    qhy[wd] |= b << sh;
+    quantize(elo[k].z, ehi[k].z, p.z, scZ, a, b);
+    qlz[wd] |= a << sh;
+    qhz[wd] |= b << sh;
+    uint32_t m;
+    if (et[k] == 1) {
+      m = 0x80u | uint32_t(kInt);
+      nextCode[pushBase + kInt] = ec[k];
+      nextWide[pushBase + kInt] = childBase + kInt;
+      ++kInt;
+    } else {
+      const int cnt = pc[k];
+      m = (uint32_t(cnt) << 5) | uint32_t(off);
+      for (int q = 0; q < cnt; ++q) {
+        const int d = primBase + off + q, sidx = prims[k][q];
+        dstRef[d] = srcRef[sidx];
+        for (int f = 0; f < kLeafF4; ++f) dstGeo[kLeafF4 * d + f] = srcGeo[kLeafF4 * sidx + f];
+      }
+      off += cnt;
+    }
+    meta[wd] |= m << sh;
+  }
+  for (int k = en; k < 8; ++k) {
+    const int wd = k >> 2, sh = (k & 3) * 8;
+    qlx[wd] |= 255u << sh;
+    qly[wd] |= 255u << sh;
+    qlz[wd] |= 255u << sh;
+  }
+  float4* o = wnodes + kWideF4 * w;
+  o[0] = make_float4(p.x, p.y, p.z,
+                     __uint_as_float(exX | (exY << 8) | (exZ << 16) | (uint32_t(nInt) << 24) | (uint32_t(en) << 28)));
+  o[1] = make_float4(__int_as_float(childBase), __int_as_float(primBase), __uint_as_float(meta[0]),
+                     __uint_as_float(meta[1]));
+  o[2] = make_float4(__uint_as_float(qlx[0]), __uint_as_float(qlx[1]), __uint_as_float(qly[0]),
+                     __uint_as_float(qly[1]));
+  o[3] = make_float4(__uint_as_float(qlz[0]), __uint_as_float(qlz[1]), __uint_as_float(qhx[0]),
+                     __uint_as_float(qhx[1]));
+  o[4] = make_float4(__uint_as_float(qhy[0]), __uint_as_float(qhy[1]), __uint_as_float(qhz[0]),
+                     __uint_as_float(qhz[1]));
 }
 
 // Top-down collapse of the binary LBVH into 8-wide nodes, one level of wide
@@ -933,7 +1179,7 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
     if ((st = scratchGet(c, 8, tmpBytes, &pTmp)) != UBR_OK) return fail(st);
     UBR_CUDA(c, cub::DeviceRadixSort::SortKeys(pTmp, tmpBytes, (unsigned long long*)pKeys,
                                                (unsigned long long*)pKeys2, int(n), 0, 30 + idxBits, c->stream));
-    const bool ploc = n > 1 && c->builder == 2 && c->leafMax == 1;
+    const bool ploc = n > 1 && c->builder == 2 && (c->leafMax == 1 || c->collapse == 2);
     if (n > 1 && !ploc)
       k_hierarchy<<<int((n - 1 + TB - 1) / TB), TB, 0, c->stream>>>(int(n), (const unsigned long long*)pKeys2,
                                                                    (float4*)pNodes, (int*)pLeafP, (int*)pNodeP,
@@ -973,7 +1219,8 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
                                                    (int*)pNn);
         k_ploc_merge<<<g, kPlocBlock, 0, c->stream>>>(nc, (const int*)pNn, (int*)pCode[cur], (float4*)pCLo[cur],
                                                       (float4*)pCHi[cur], (int*)pCCnt[cur], (float4*)pNodes,
-                                                      (int2*)pRange, (int*)pPc, (int*)pValid);
+                                                      (int2*)pRange, (int*)pPc, (int*)pValid, (int*)pLeafP,
+                                                      (int*)pNodeP);
         UBR_CUDA(c, cub::DeviceScan::ExclusiveSum(pScan, scanBytes, (const int*)pValid, (int*)pPos, nc,
                                                   c->stream));
         k_ploc_compact<<<g, kPlocBlock, 0, c->stream>>>(
@@ -991,6 +1238,20 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
       if (hostPc[0] != int(n) - 1) return fail(setError(c, UBR_INTERNAL, "PLOC node count mismatch"));
       rootCodeDev = int(n) - 2;  // the last merge makes the root
     }
+    // SAH collapse: the DP's cost rows and decisions, bottom-up
+    const bool sah = n > 1 && c->collapse == 2;
+    void *pCost = nullptr, *pDec = nullptr, *pSahCnt = nullptr;
+    if (sah) {
+      const size_t nn1 = size_t(n) - 1;
+      if ((st = scratchGet(c, 11, sizeof(float) * kSahStride * nn1, &pCost)) != UBR_OK) return fail(st);
+      if ((st = scratchGet(c, 12, 8 * nn1, &pDec)) != UBR_OK) return fail(st);
+      if ((st = scratchGet(c, 13, sizeof(int) * nn1, &pSahCnt)) != UBR_OK) return fail(st);
+      UBR_CUDA(c, cudaMemsetAsync(pSahCnt, 0, sizeof(int) * nn1, c->stream));
+      k_sah_costs<<<grid, TB, 0, c->stream>>>(int(n), (const float4*)pNodes, (const int2*)pRange,
+                                              (const uint32_t*)pRef, (const int*)pLeafP, (const int*)pNodeP,
+                                              (int*)pSahCnt, (float*)pCost, (uint8_t*)pDec, c->sahPrimScale);
+      UBR_CUDA(c, cudaGetLastError());
+    }
     // collapse to 8-wide, level by level: cursors = {wide nodes, leaf prims, next work}
     {
       const int rootCode = n > 1 ? (rootCodeDev >= 0 ? rootCodeDev : 0) : ~0;
@@ -1003,11 +1264,17 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
       int* hostCur = static_cast<int*>(c->pinned);
       while (count > 0) {
         UBR_CUDA(c, cudaMemsetAsync(static_cast<int*>(pCur) + 2, 0, sizeof(int), c->stream));
-        k_collapse<<<(count + 127) / 128, 128, 0, c->stream>>>(
-            (const float4*)pNodes, (const int2*)pRange, (const float4*)pLo, (const float4*)pHi,
-            (const int*)pWc[cur], (const int*)pWw[cur], count, c->leafMax, (int*)pWc[cur ^ 1], (int*)pWw[cur ^ 1],
-            (int*)pCur,
-            (float4*)pWide, (const uint32_t*)pRef, (const float4*)pGeo, (uint32_t*)pRef2, (float4*)pGeo2);
+        if (sah)
+          k_collapse_sah<<<(count + 127) / 128, 128, 0, c->stream>>>(
+              (const float4*)pNodes, (const uint8_t*)pDec, (const int*)pWc[cur], (const int*)pWw[cur], count,
+              (int*)pWc[cur ^ 1], (int*)pWw[cur ^ 1], (int*)pCur, (float4*)pWide, (const uint32_t*)pRef,
+              (const float4*)pGeo, (uint32_t*)pRef2, (float4*)pGeo2);
+        else
+          k_collapse<<<(count + 127) / 128, 128, 0, c->stream>>>(
+              (const float4*)pNodes, (const int2*)pRange, (const float4*)pLo, (const float4*)pHi,
+              (const int*)pWc[cur], (const int*)pWw[cur], count, c->leafMax, (int*)pWc[cur ^ 1],
+              (int*)pWw[cur ^ 1], (int*)pCur, (float4*)pWide, (const uint32_t*)pRef, (const float4*)pGeo,
+              (uint32_t*)pRef2, (float4*)pGeo2);
         UBR_CUDA(c, cudaGetLastError());
         UBR_CUDA(c, cudaMemcpyAsync(hostCur, pCur, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         UBR_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -25,6 +25,8 @@ struct Context {
   uint64_t arenaCap = 0;     // 0 = unlimited
   int leafMax = 1;           // wide-BVH leaf size (1..kWideLeafMax); 1 measured fastest
   int builder = 1;           // binary tree before the 8-wide collapse: 1 Karras radix tree, 2 PLOC
+  int collapse = 1;          // 8-wide collapse: 1 greedy (fixed leaf size), 2 SAH-optimal (leaves 1..3)
+  float sahPrimScale = 1.0f; // SAH collapse: weight of primitive tests against node visits
   int traceMode = 1;         // occlusion kernel: 1 one thread per ray (measured faster), 2 persistent
   uint64_t arenaUsed = 0;
   std::string lastError;
