@@ -507,9 +507,16 @@ def run_ours(args):
     e2e_rays = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    t_build = t_flat = t_up = 0.0
     for _ in range(e2e_steps):
         h = C.c_void_p()
+        tb = time.perf_counter()
         ctx._check(ctx._L.ubr_scene_build(ctx.handle, C.byref(desc), C.byref(h)))
+        t_build += time.perf_counter() - tb
+        si = abi.SceneInfo()
+        ctx._L.ubr_scene_get_info(h, C.byref(si))
+        t_flat += si.flatten_ms
+        t_up += si.upload_ms
         fr = abi.Frame()
         fr.memory = abi.MEMORY_HOST
         fr.color = abi.ptr(host_color)
@@ -519,6 +526,9 @@ def run_ours(args):
     e2e_s = max(time.perf_counter() - t0, 1e-9)
     e2e = None if args.no_e2e else {"value": round(e2e_rays * ws / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(host_color.nbytes), "ms_per_step": round(e2e_s / max(1, e2e_steps) * 1e3, 2),
+           "scene_build_ms_per_step": round(t_build / max(1, e2e_steps) * 1e3, 2),
+           "of_which_flatten_ms": round(t_flat / max(1, e2e_steps), 2),
+           "of_which_upload_ms": round(t_up / max(1, e2e_steps), 2),
            "steps": e2e_steps}
 
     cpu = None

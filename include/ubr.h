@@ -310,9 +310,11 @@ typedef struct ubr_scene_info {
   uint32_t geom_id[4];     /* UBR_INVALID_ID when the kind is absent */
   uint64_t bvh_nodes;
   uint64_t device_bytes;
-  double build_ms;
+  double build_ms;         /* host wall time of ubr_scene_build */
   float bounds_lo[3];
   float bounds_hi[3];
+  double flatten_ms;       /* of which: host flattening (primID order, chains, materials) */
+  double upload_ms;        /*           allocations + host-to-device copies queued */
 } ubr_scene_info;
 ubr_status ubr_scene_get_info(const ubr_scene* scene, ubr_scene_info* info);
 

@@ -134,7 +134,7 @@ class ContextDesc(C.Structure):
 class SceneInfo(C.Structure):
     _fields_ = [("prim_count", C.c_uint64 * 4), ("geom_id", C.c_uint32 * 4), ("bvh_nodes", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("build_ms", C.c_double), ("bounds_lo", C.c_float * 3),
-                ("bounds_hi", C.c_float * 3)]
+                ("bounds_hi", C.c_float * 3), ("flatten_ms", C.c_double), ("upload_ms", C.c_double)]
 
 
 class BatchItem(C.Structure):

@@ -486,7 +486,7 @@ class BuiltScene:
         self.ctx._check(self.ctx._L.ubr_scene_get_info(self.handle, C.byref(i)))
         return dict(prim_count=list(i.prim_count), geom_id=list(i.geom_id), bvh_nodes=i.bvh_nodes,
                     device_bytes=i.device_bytes, build_ms=i.build_ms, bounds_lo=list(i.bounds_lo),
-                    bounds_hi=list(i.bounds_hi))
+                    bounds_hi=list(i.bounds_hi), flatten_ms=i.flatten_ms, upload_ms=i.upload_ms)
 
     def release(self):
         if self.handle:

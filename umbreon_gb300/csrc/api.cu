@@ -47,8 +47,10 @@ ubr_status devAlloc(Context* c, DevBuf& b, size_t bytes) {
   if (c->arenaCap && c->arenaUsed + bytes > c->arenaCap)
     return setError(c, UBR_OUT_OF_MEMORY, "device arena cap exceeded");
   void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, bytes);
-  if (e != cudaSuccess) return cudaFail(c, e, "cudaMalloc");
+  // stream-ordered from the context's pool: after the first frames a scene
+  // build or a scratch growth reuses pooled memory instead of cudaMalloc
+  cudaError_t e = c->pool ? cudaMallocFromPoolAsync(&p, bytes, c->pool, c->stream) : cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) return cudaFail(c, e, "device allocation");
   b.ptr = p;
   b.bytes = bytes;
   c->arenaUsed += bytes;
@@ -57,7 +59,8 @@ ubr_status devAlloc(Context* c, DevBuf& b, size_t bytes) {
 
 void devFree(Context* c, DevBuf& b) {
   if (b.ptr) {
-    cudaFree(b.ptr);
+    if (c->pool) cudaFreeAsync(b.ptr, c->stream);
+    else cudaFree(b.ptr);
     c->arenaUsed -= b.bytes;
   }
   b.ptr = nullptr;
@@ -174,6 +177,20 @@ ubr_status ubr_context_create(ubr_context** out, const ubr_context_desc* desc) {
     x.ownStream = true;
   }
   for (cudaEvent_t& e : x.ev) cudaEventCreate(&e);
+  {
+    // the context's device memory pool; freed blocks stay in the pool
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    if (cudaMemPoolCreate(&x.pool, &props) == cudaSuccess) {
+      uint64_t keep = ~0ull;
+      cudaMemPoolSetAttribute(x.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    } else {
+      cudaGetLastError();
+      x.pool = nullptr;  // plain cudaMalloc
+    }
+  }
   if (cudaMallocHost(&x.pinned, 4096) != cudaSuccess) {
     cudaGetLastError();
     x.pinned = nullptr;
@@ -198,6 +215,11 @@ ubr_status ubr_context_destroy(ubr_context* c) {
   }
   x.sceneHandles.clear();
   for (DevBuf& b : x.scratch) devFree(&x, b);
+  if (x.pool) {
+    cudaStreamSynchronize(x.stream);
+    cudaMemPoolDestroy(x.pool);
+    x.pool = nullptr;
+  }
   for (cudaEvent_t& e : x.ev)
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t& e : x.pev)
@@ -264,6 +286,8 @@ ubr_status ubr_scene_get_info(const ubr_scene* s, ubr_scene_info* info) {
   info->bvh_nodes = sc.nodes;
   info->device_bytes = sc.deviceBytes;
   info->build_ms = sc.buildMs;
+  info->flatten_ms = sc.flattenMs;
+  info->upload_ms = sc.uploadMs;
   for (int k = 0; k < 3; ++k) {
     info->bounds_lo[k] = sc.lo[k];
     info->bounds_hi[k] = sc.hi[k];

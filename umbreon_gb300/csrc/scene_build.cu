@@ -73,13 +73,23 @@ struct MatHash {
 struct MatTable {
   std::unordered_map<MatKey, uint32_t, MatHash> map;
   std::vector<ubr_material>* out;
+  ubr_material last{};
+  uint32_t lastId = kInvalid;
   uint32_t get(const ubr_material& m) {
+    // runs of one material (the common case) skip the hash lookup
+    if (lastId != kInvalid && std::memcmp(&m, &last, sizeof(ubr_material)) == 0) return lastId;
     MatKey k{m};
     auto it = map.find(k);
-    if (it != map.end()) return it->second;
-    const uint32_t id = static_cast<uint32_t>(out->size());
-    out->push_back(m);
-    map.emplace(k, id);
+    uint32_t id;
+    if (it != map.end()) {
+      id = it->second;
+    } else {
+      id = static_cast<uint32_t>(out->size());
+      out->push_back(m);
+      map.emplace(k, id);
+    }
+    last = m;
+    lastId = id;
     return id;
   }
 };
@@ -181,6 +191,15 @@ void flattenCylinders(const ubr_scene_desc& d, const std::vector<f3>& offs, Host
       s.rcClip.push_back(make_float4(cr.x, cr.y, cr.z, 0.0f));
     }
   }
+  {
+    const size_t nc = capIdx.size() * offs.size();
+    s.ccV.reserve(2 * nc);
+    s.ccIdx.reserve(nc);
+    s.color[kCone].reserve(nc);
+    s.mat[kCone].reserve(nc);
+    s.fromEdge[kCone].reserve(nc);
+    s.opacity1[kCone].reserve(nc);
+  }
   for (const f3& off : offs) {
     for (int i : capIdx) {
       const uint32_t base = uint32_t(s.ccV.size());
@@ -263,6 +282,11 @@ ubr_status flatten(Context* c, const ubr_scene_desc& d, HostScene& s) {
   if (d.sphere_count > 0) {
     s.geomID[kSphere] = nextGeom++;
     s.baseSph = uint32_t(d.sphere_count);
+    const size_t ns = d.sphere_count * offs.size();
+    s.sph.reserve(ns);
+    s.color[kSphere].reserve(ns);
+    s.mat[kSphere].reserve(ns);
+    s.fromEdge[kSphere].reserve(ns);
     for (const f3& off : offs)
       for (uint64_t i = 0; i < d.sphere_count; ++i) {
         const float* q = d.sphere_center_radius + 4 * i;
@@ -1079,6 +1103,7 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   HostScene hs;
   st = flatten(c, d, hs);
   if (st != UBR_OK) return st;
+  const auto tFlat = std::chrono::steady_clock::now();
   if (hs.principled)
     return setError(c, UBR_INVALID_ARGUMENT,
                     "Principled materials are not supported by this library (POV finish only)");
@@ -1131,6 +1156,7 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
     if ((st = upload(c, sc, hs.fromEdge[k], &v.primFromEdge[k])) != UBR_OK) return fail(st);
     if ((st = upload(c, sc, hs.opacity1[k], &v.primOpacity1[k])) != UBR_OK) return fail(st);
   }
+  const auto tUp = std::chrono::steady_clock::now();
   if (n > 0) {
     BuildIn in{dpos, v.meshIdx, dsph, drcV, drcIdx, drcFl, dccV, dccIdx, nTri, nSph, nRc, nCc};
     void *pLo, *pHi, *pKeys, *pKeys2, *pCb, *pLeafP, *pNodeP, *pCnt, *pNodes, *pRef, *pGeo;
@@ -1314,6 +1340,8 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   for (const DevBuf& b : sc->bufs) sc->deviceBytes += b.bytes;
   const auto t1 = std::chrono::steady_clock::now();
   sc->buildMs = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  sc->flattenMs = std::chrono::duration<double, std::milli>(tFlat - t0).count();
+  sc->uploadMs = std::chrono::duration<double, std::milli>(tUp - tFlat).count();
   *out = sc;
   return UBR_OK;
 }

@@ -39,6 +39,7 @@ struct Context {
   cudaGraphExec_t graphExec = nullptr;
   std::vector<unsigned char> graphKey;  // launch parameters the graph was captured with
   std::vector<void*> sceneHandles;      // live ubr_scene handles built on this context
+  cudaMemPool_t pool = nullptr;         // stream-ordered device allocations (scenes, scratch)
 };
 
 struct Scene {
@@ -50,6 +51,8 @@ struct Scene {
   bool opaque = true;        // every primitive fully opaque: frames are one layer deep
   uint64_t deviceBytes = 0;
   double buildMs = 0.0;
+  double flattenMs = 0.0;    // host: validation, primID ordering, chaining, material table
+  double uploadMs = 0.0;     // host: allocations and copies queued
   float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 };
 
