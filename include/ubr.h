@@ -253,7 +253,10 @@ typedef struct ubr_frame {
   float* avg_hit_dist;    /* 1 per pixel */
 } ubr_frame;
 
-/* Context: one GPU, one CUDA stream, one device arena. */
+/* Context: one GPU, one CUDA stream, one device arena.  Scenes and frame
+ * scratch are allocated stream-ordered from the context's own memory pool;
+ * memory released by ubr_scene_release or scratch growth stays in that pool
+ * for reuse until ubr_context_destroy. */
 typedef struct ubr_context ubr_context;
 typedef struct ubr_scene ubr_scene;
 

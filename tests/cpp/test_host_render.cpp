@@ -127,6 +127,29 @@ int main() {
     const float a = umbreon::render(sc, off).color[kC], b = umbreon::render(sc, on).color[kC];
     c("shadow off ~0.84, on ~0.2", near(a, 0.84f, 0.03f) && near(b, 0.2f, 0.03f));
   }
+  {  // AO AOVs (aoWriteAov): mesh first hit carries albedo = C, normal = N and an
+     // open quad's contact / shape openness 1; empty when not requested
+    umbreon::Scene sc;
+    sc.mesh = quad({0.5f, 0.6f, 0.7f, 1.0f});
+    sc.camera = cam();
+    sc.lights.push_back(key());
+    umbreon::RenderOptions o = o5();
+    o.aoSamples = 8;
+    o.aoDistance = 2.0f;
+    umbreon::FrameResult plain = umbreon::render(sc, o);
+    c("no AOVs unless asked", plain.albedo.empty() && plain.contactAo.empty());
+    o.aoWriteAov = true;
+    umbreon::FrameResult f = umbreon::render(sc, o);
+    const std::size_t p = 12;
+    c("AOV sizes", f.albedo.size() == 75 && f.normal.size() == 75 && f.bentNormal.size() == 75 &&
+                       f.contactAo.size() == 25 && f.shapeAo.size() == 25 && f.avgHitDist.size() == 25);
+    c("albedo = vertex colour", near(f.albedo[3 * p], 0.5f, 1e-6f) && near(f.albedo[3 * p + 2], 0.7f, 1e-6f));
+    c("normal = +z", near(f.normal[3 * p + 2], 1.0f, 1e-6f));
+    c("open quad: contact = shape = 1, no occluder", near(f.contactAo[p], 1.0f, 1e-6f) &&
+                                                         near(f.shapeAo[p], 1.0f, 1e-6f) &&
+                                                         near(f.avgHitDist[p], 2.0f, 1e-6f));
+    c("colour unchanged by the AOVs", near(f.color[kC], plain.color[kC], 0.0f));
+  }
   {  // unsupported requests throw like the reference's failures
     umbreon::Scene sc;
     sc.mesh = quad({1, 1, 1, 1});
