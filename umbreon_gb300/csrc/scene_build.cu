@@ -250,26 +250,38 @@ ubr_status flatten(Context* c, const ubr_scene_desc& d, HostScene& s) {
   const uint64_t baseV = d.mesh_vertex_count, baseT = d.mesh_triangle_count;
   if (baseV >= 3 && baseT > 0) {
     s.geomID[kMesh] = nextGeom++;
-    for (const f3& off : offs)
+    // baked per instance (scene_build.cpp:150-152), written in place
+    const size_t nInst = offs.size();
+    s.pos.resize(3 * baseV * nInst);
+    s.nrm.resize(3 * baseV * nInst);
+    s.col.resize(baseV * nInst);
+    s.idx.resize(3 * baseT * nInst);
+    for (size_t ci = 0; ci < nInst; ++ci) {
+      const f3 off = offs[ci];
+      float* pos = s.pos.data() + 3 * baseV * ci;
+      float* nrm = s.nrm.data() + 3 * baseV * ci;
+      float4* col = s.col.data() + baseV * ci;
       for (uint64_t v = 0; v < baseV; ++v) {
         const f3 p = ld3(d.mesh_positions, v) + off;
-        s.pos.push_back(p.x);
-        s.pos.push_back(p.y);
-        s.pos.push_back(p.z);
-        for (int k = 0; k < 3; ++k) s.nrm.push_back(d.mesh_normals ? d.mesh_normals[3 * v + k] : 0.0f);
-        if (d.mesh_colors)
-          s.col.push_back(make_float4(d.mesh_colors[4 * v], d.mesh_colors[4 * v + 1], d.mesh_colors[4 * v + 2],
-                                      d.mesh_colors[4 * v + 3]));
-        else
-          s.col.push_back(make_float4(0, 0, 0, 1));
+        pos[3 * v] = p.x;
+        pos[3 * v + 1] = p.y;
+        pos[3 * v + 2] = p.z;
       }
-    for (size_t ci = 0; ci < offs.size(); ++ci)
-      for (uint64_t t = 0; t < baseT; ++t)
-        for (int k = 0; k < 3; ++k) {
-          const uint64_t corner = 3 * t + k;
-          const uint32_t cv = d.mesh_index ? d.mesh_index[corner] : uint32_t(corner);
-          s.idx.push_back(uint32_t(ci * baseV + cv));
-        }
+      if (d.mesh_normals) std::memcpy(nrm, d.mesh_normals, 3 * baseV * sizeof(float));
+      else std::memset(nrm, 0, 3 * baseV * sizeof(float));
+      if (d.mesh_colors) {
+        std::memcpy(col, d.mesh_colors, baseV * sizeof(float4));
+      } else {
+        for (uint64_t v = 0; v < baseV; ++v) col[v] = make_float4(0, 0, 0, 1);
+      }
+      uint32_t* idx = s.idx.data() + 3 * baseT * ci;
+      const uint32_t vb = uint32_t(ci * baseV);
+      if (d.mesh_index) {
+        for (uint64_t k = 0; k < 3 * baseT; ++k) idx[k] = vb + d.mesh_index[k];
+      } else {
+        for (uint64_t k = 0; k < 3 * baseT; ++k) idx[k] = vb + uint32_t(k);
+      }
+    }
     s.baseTri = uint32_t(baseT);
     s.meshMat = mt.get(d.mesh_material);
     if (d.mesh_tri_material) {
@@ -568,6 +580,7 @@ __global__ void k_refit(BuildIn in, int n, int idxBits, const unsigned long long
 // is always mutual, so every round merges at least once.
 constexpr int kPlocRadius = 16;
 constexpr int kPlocBlock = 256;
+constexpr int kPlocBatch = 4;  // merge rounds between host reads of the cluster count
 
 __device__ __forceinline__ float unionArea(float4 alo, float4 ahi, float4 blo, float4 bhi) {
   const float ex = fmaxf(ahi.x, bhi.x) - fminf(alo.x, blo.x);
@@ -587,8 +600,9 @@ __global__ void k_ploc_init(int n, int idxBits, const unsigned long long* keys, 
   cnt[i] = 1;
 }
 
-__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(int nc, const float4* lo, const float4* hi, int* nn) {
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(const int* ncIn, const float4* lo, const float4* hi, int* nn) {
   __shared__ float4 sLo[kPlocBlock + 2 * kPlocRadius], sHi[kPlocBlock + 2 * kPlocRadius];
+  const int nc = *ncIn;
   const int b0 = blockIdx.x * kPlocBlock - kPlocRadius;
   for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += kPlocBlock) {
     const int j = b0 + k;
@@ -625,10 +639,15 @@ __device__ __forceinline__ void writeBinNode(float4* nodes, int node, int c0, fl
   nd[3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.0f, 0.0f);
 }
 
-__global__ void k_ploc_merge(int nc, const int* nn, int* code, float4* lo, float4* hi, int* cnt, float4* nodes,
-                             int2* ranges, int* nodeCounter, int* valid, int* leafParent, int* nodeParent) {
+__global__ void k_ploc_merge(const int* ncIn, int ncCap, const int* nn, int* code, float4* lo, float4* hi, int* cnt,
+                             float4* nodes, int2* ranges, int* nodeCounter, int* valid, int* leafParent,
+                             int* nodeParent) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nc) return;
+  if (i >= ncCap) return;
+  if (i >= *ncIn) {  // past the clusters of this round: nothing to keep
+    valid[i] = 0;
+    return;
+  }
   const int j = nn[i];
   const bool mutual = j >= 0 && nn[j] == i;
   if (mutual && i < j) {
@@ -652,12 +671,12 @@ __global__ void k_ploc_merge(int nc, const int* nn, int* code, float4* lo, float
   }
 }
 
-__global__ void k_ploc_compact(int nc, const int* valid, const int* pos, const int* code, const float4* lo,
+__global__ void k_ploc_compact(int ncCap, const int* valid, const int* pos, const int* code, const float4* lo,
                                const float4* hi, const int* cnt, int* code2, float4* lo2, float4* hi2, int* cnt2,
                                int* newCount) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nc) return;
-  if (i == nc - 1) *newCount = pos[i] + valid[i];
+  if (i >= ncCap) return;
+  if (i == ncCap - 1) *newCount = pos[i] + valid[i];
   if (!valid[i]) return;
   const int o = pos[i];
   code2[o] = code[i];
@@ -1237,29 +1256,42 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
       k_ploc_init<<<grid, TB, 0, c->stream>>>(int(n), idxBits, (const unsigned long long*)pKeys2,
                                               (const float4*)pLo, (const float4*)pHi, (int*)pCode[0],
                                               (float4*)pCLo[0], (float4*)pCHi[0], (int*)pCCnt[0]);
-      int nc = int(n), cur = 0, rounds = 0;
+      // rounds run kPlocBatch at a time between host reads of the cluster
+      // count; the count of each round lives on the device (pPc[1], pPc[2])
+      // and bounds the work of the next, the host's last read bounds the grid
+      const int nInit = int(n);
+      UBR_CUDA(c, cudaMemcpyAsync(static_cast<int*>(pPc) + 1, &nInit, sizeof(int), cudaMemcpyHostToDevice,
+                                  c->stream));
+      int ncCap = int(n), cur = 0, which = 0, rounds = 0;
       int* hostPc = static_cast<int*>(c->pinned);
-      while (nc > 1) {
-        const int g = (nc + kPlocBlock - 1) / kPlocBlock;
-        k_ploc_nn<<<g, kPlocBlock, 0, c->stream>>>(nc, (const float4*)pCLo[cur], (const float4*)pCHi[cur],
-                                                   (int*)pNn);
-        k_ploc_merge<<<g, kPlocBlock, 0, c->stream>>>(nc, (const int*)pNn, (int*)pCode[cur], (float4*)pCLo[cur],
-                                                      (float4*)pCHi[cur], (int*)pCCnt[cur], (float4*)pNodes,
-                                                      (int2*)pRange, (int*)pPc, (int*)pValid, (int*)pLeafP,
-                                                      (int*)pNodeP);
-        UBR_CUDA(c, cub::DeviceScan::ExclusiveSum(pScan, scanBytes, (const int*)pValid, (int*)pPos, nc,
-                                                  c->stream));
-        k_ploc_compact<<<g, kPlocBlock, 0, c->stream>>>(
-            nc, (const int*)pValid, (const int*)pPos, (const int*)pCode[cur], (const float4*)pCLo[cur],
-            (const float4*)pCHi[cur], (const int*)pCCnt[cur], (int*)pCode[cur ^ 1], (float4*)pCLo[cur ^ 1],
-            (float4*)pCHi[cur ^ 1], (int*)pCCnt[cur ^ 1], static_cast<int*>(pPc) + 1);
+      while (ncCap > 1) {
+        const int g = (ncCap + kPlocBlock - 1) / kPlocBlock;
+        for (int r = 0; r < kPlocBatch; ++r) {
+          const int* ncIn = static_cast<const int*>(pPc) + 1 + which;
+          int* ncOut = static_cast<int*>(pPc) + 1 + (which ^ 1);
+          k_ploc_nn<<<g, kPlocBlock, 0, c->stream>>>(ncIn, (const float4*)pCLo[cur], (const float4*)pCHi[cur],
+                                                     (int*)pNn);
+          k_ploc_merge<<<g, kPlocBlock, 0, c->stream>>>(ncIn, ncCap, (const int*)pNn, (int*)pCode[cur],
+                                                        (float4*)pCLo[cur], (float4*)pCHi[cur], (int*)pCCnt[cur],
+                                                        (float4*)pNodes, (int2*)pRange, (int*)pPc, (int*)pValid,
+                                                        (int*)pLeafP, (int*)pNodeP);
+          UBR_CUDA(c, cub::DeviceScan::ExclusiveSum(pScan, scanBytes, (const int*)pValid, (int*)pPos, ncCap,
+                                                    c->stream));
+          k_ploc_compact<<<g, kPlocBlock, 0, c->stream>>>(
+              ncCap, (const int*)pValid, (const int*)pPos, (const int*)pCode[cur], (const float4*)pCLo[cur],
+              (const float4*)pCHi[cur], (const int*)pCCnt[cur], (int*)pCode[cur ^ 1], (float4*)pCLo[cur ^ 1],
+              (float4*)pCHi[cur ^ 1], (int*)pCCnt[cur ^ 1], ncOut);
+          which ^= 1;
+          cur ^= 1;
+        }
         UBR_CUDA(c, cudaGetLastError());
-        UBR_CUDA(c, cudaMemcpyAsync(hostPc, pPc, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        UBR_CUDA(c, cudaMemcpyAsync(hostPc, pPc, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         UBR_CUDA(c, cudaStreamSynchronize(c->stream));
-        const int next = hostPc[1];
-        if (!(next < nc) || ++rounds > (1 << 20)) return fail(setError(c, UBR_INTERNAL, "PLOC did not converge"));
-        nc = next;
-        cur ^= 1;
+        const int next = hostPc[1 + which];
+        rounds += kPlocBatch;
+        if (!(next < ncCap || next == 1) || rounds > (1 << 20))
+          return fail(setError(c, UBR_INTERNAL, "PLOC did not converge"));
+        ncCap = next;
       }
       if (hostPc[0] != int(n) - 1) return fail(setError(c, UBR_INTERNAL, "PLOC node count mismatch"));
       rootCodeDev = int(n) - 2;  // the last merge makes the root
