@@ -192,6 +192,14 @@ typedef struct ubr_render_desc {
   /* RenderOptions::aoWriteAov (render_options.hpp:62): fill the AO AOV
    * outputs of ubr_frame */
   uint32_t ao_write_aov;
+  /* RenderOptions::aaMode / aaThreshold / aaDepth (render_options.hpp:26-39):
+   * 1 = adaptive AA (centre sample per output pixel, refinement mask,
+   * flagged blocks shaded per subpixel, the others replicate a centre
+   * re-shaded with ss^2 AO / soft-shadow samples); aaDepth above the
+   * supersample factor is not supported (UBR_INVALID_ARGUMENT) */
+  int32_t aa_mode;
+  float aa_threshold;
+  int32_t aa_depth;
 } ubr_render_desc;
 
 /* Where a frame's buffers live. */
@@ -251,6 +259,9 @@ typedef struct ubr_frame {
   float* contact_ao;      /* 1 per pixel */
   float* shape_ao;        /* 1 per pixel */
   float* avg_hit_dist;    /* 1 per pixel */
+  /* adaptive AA refinement mask, output resolution, 1 = refined
+   * (FrameResult::aaMask with aaDebug); written when aa_mode = 1 */
+  float* aa_mask;
 } ubr_frame;
 
 /* Context: one GPU, one CUDA stream, one device arena.  Scenes and frame

@@ -13,6 +13,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <functional>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -457,6 +458,7 @@ struct Opt {  // the RenderOptions fields this path reads
   bool shadows; int shadowSamples; int envLights;
   float specularScale; bool transparency, transparentBackground; int maxTransparentLayers;
   bool aoWriteAov = false;
+  int aaMode = 0;
   bool aoEnhanced() const {  // render_options.hpp:79-82
     return aoFalloffPower > 0.0f || aoMultiScale || aoBentNormal || aoMultibounce || aoLowDiscrepancy ||
            aoDiffuseFactor > 0.0f;
@@ -592,6 +594,7 @@ struct HitShade {
   // AO AOVs (hit_shader.hpp:41-55): set on mesh hits when aoWriteAov is on
   V3 albedo{0.0f, 0.0f, 0.0f}, normal{0.0f, 0.0f, 0.0f}, bent{0.0f, 0.0f, 0.0f};
   float contact = 1.0f, shape = 1.0f, avgHit = 0.0f;
+  int group = 0;  // CueMol section of the hit (hit_shader.hpp:277, 457)
 };
 
 // hit_shader.hpp:147-496 shadeHit (POV; GI / edge / principled branches off)
@@ -631,7 +634,11 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
       hs.contact = aov.contact;
       hs.shape = aov.shape;
       hs.avgHit = aov.avgHitDist;
+    } else if (c.o.aaMode == 1) {  // :214-220 (the adaptive-AA mask reads N)
+      hs.albedo = C;
+      hs.normal = N;
     }
+    hs.group = s.triGroup.empty() ? 0 : s.triGroup[s.baseTri ? hit.primID % s.baseTri : hit.primID];
   } else {
     const float* fc = &s.color[kind][4 * hit.primID];
     const Mat& pm = s.mat[kind][hit.primID];
@@ -651,6 +658,8 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
     hs.color = shadeLocal(s, pm, C, N, V, c.lights, ambLight, c.bg, c.o.specularScale, aoFactor, diffuseAo,
                           P, Ng, secEps, primShadows, c.o.shadowSamples, px, py);
     hs.opacity = fc[3];
+    hs.group = s.group[kind][hit.primID];
+    if (c.o.aaMode == 1) hs.normal = N;  // hit_shader.hpp:321
     if (kind != kSphere) {
       const float op1 = s.opacity1[kind][hit.primID];
       if (op1 >= 0.0f) {
@@ -676,6 +685,7 @@ struct PixelOut {
 inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32_t px, uint32_t py,
                                const V3& camDir) {
   PixelOut po{};
+  po.first.group = -1;  // background sentinel (transparency.hpp:337)
   po.geom = kInvalid;
   po.prim = kInvalid;
   V3 Cf{0.0f, 0.0f, 0.0f};
@@ -881,6 +891,7 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   c.o.transparentBackground = d.transparent_background != 0;
   c.o.maxTransparentLayers = d.max_transparent_layers;
   c.o.aoWriteAov = d.ao_write_aov != 0;
+  c.o.aaMode = d.aa_mode;
   // buildSceneLights (embree_renderer.cpp:436-458)
   for (uint32_t i = 0; i < d.light_count; ++i) {
     const ubr_light& dl = d.lights[i];
@@ -935,6 +946,200 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
     aCon.assign(npix, 1.0f); aShp.assign(npix, 1.0f); aAvg.assign(npix, 0.0f);
   }
   if (row1 <= row0) { row0 = 0; row1 = H; }
+  // storePixelResult (embree_renderer.cpp:213-250): one hi-res sample
+  auto store = [&](size_t pix, const PixelOut& po) {
+    color[4 * pix] = po.r; color[4 * pix + 1] = po.g; color[4 * pix + 2] = po.b; color[4 * pix + 3] = po.a;
+    depth[pix] = po.depth;
+    viewZ[pix] = po.viewZ;
+    hg[pix] = po.geom;
+    hp[pix] = po.prim;
+    if (aov) {
+      const HitShade& f = po.first;
+      const float a3[3][3] = {{f.albedo.x, f.albedo.y, f.albedo.z}, {f.normal.x, f.normal.y, f.normal.z},
+                              {f.bent.x, f.bent.y, f.bent.z}};
+      for (int k = 0; k < 3; ++k) {
+        aAlb[3 * pix + k] = a3[0][k];
+        aNrm[3 * pix + k] = a3[1][k];
+        aBent[3 * pix + k] = a3[2][k];
+      }
+      aCon[pix] = f.contact;
+      aShp[pix] = f.shape;
+      aAvg[pix] = f.avgHit;
+    }
+  };
+  // primary ray through lattice point (px, py) of a Wl x Hl lattice
+  auto rayAtL = [&](int px, int py, int Wl, int Hl, V3& org, V3& rd) {
+    const float v = 1.0f - 2.0f * (static_cast<float>(py) + 0.5f) / static_cast<float>(Hl);
+    const float u = 2.0f * (static_cast<float>(px) + 0.5f) / static_cast<float>(Wl) - 1.0f;
+    if (d.cam_orthographic) {
+      org = camPos + right * (u * halfW) + trueUp * (v * halfH);
+      rd = dir;
+    } else {
+      org = camPos;
+      rd = normalize(dir + right * (u * persHalfW) + trueUp * (v * persHalfH));
+    }
+  };
+  auto rayAt = [&](int px, int py, V3& org, V3& rd) { rayAtL(px, py, W, H, org, rd); };
+  // Adaptive AA (embree_renderer.cpp:1379-1670, render/adaptive_aa.hpp):
+  // centre sample per output pixel, refinement mask, flagged blocks shaded
+  // per subpixel, the others replicate a centre re-shaded with ss^2 AO and
+  // soft-shadow samples; aaDepth > ss shades each flagged cell as the box
+  // average of kFine^2 samples of a finer lattice (:1542-1590).
+  const bool adaptive = d.aa_mode == 1 && (ss > 1 || d.aa_depth > 1) && W % ss == 0 && H % ss == 0;
+  if (adaptive) {
+    const int Wf = W / ss, Hf = H / ss, cSub = ss / 2;
+    const int kFine = std::max(1, (d.aa_depth + ss - 1) / ss);
+    Ctx cf = c;
+    cf.wHi = W * kFine;  // seeds live on the (W k) x (H k) lattice
+    auto shadeCell = [&](int px, int py) -> PixelOut {
+      PixelOut acc{};
+      for (int b = 0; b < kFine; ++b)
+        for (int a = 0; a < kFine; ++a) {
+          const int pxk = px * kFine + a, pyk = py * kFine + b;
+          V3 org, rd;
+          rayAtL(pxk, pyk, W * kFine, H * kFine, org, rd);
+          const PixelOut pr = integratePixel(cf, org, rd, uint32_t(pxk), uint32_t(pyk), dir);
+          if (a == 0 && b == 0) {
+            acc = pr;  // discrete fields and AOVs: the first sample
+          } else {
+            acc.r += pr.r;
+            acc.g += pr.g;
+            acc.b += pr.b;
+            acc.a += pr.a;
+            acc.depth += pr.depth;
+            acc.viewZ += pr.viewZ;
+          }
+        }
+      const float inv = 1.0f / static_cast<float>(kFine * kFine);
+      acc.r *= inv;
+      acc.g *= inv;
+      acc.b *= inv;
+      acc.a *= inv;
+      acc.depth *= inv;
+      acc.viewZ *= inv;
+      return acc;
+    };
+    int nt0 = threads > 0 ? threads : static_cast<int>(std::thread::hardware_concurrency());
+    if (nt0 < 1) nt0 = 1;
+    auto parallelRows = [&](int n, const std::function<void(int)>& fn) {
+      std::atomic<int> next{0};
+      auto w = [&]() {
+        for (int y = next.fetch_add(1); y < n; y = next.fetch_add(1)) fn(y);
+      };
+      std::vector<std::thread> pool;
+      for (int i = 1; i < nt0; ++i) pool.emplace_back(w);
+      w();
+      for (auto& th : pool) th.join();
+    };
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<PixelOut> centers(static_cast<size_t>(Wf) * Hf);
+    parallelRows(Hf, [&](int Y) {
+      for (int X = 0; X < Wf; ++X) {
+        V3 org, rd;
+        rayAt(X * ss + cSub, Y * ss + cSub, org, rd);
+        centers[static_cast<size_t>(Y) * Wf + X] =
+            integratePixel(c, org, rd, uint32_t(X * ss + cSub), uint32_t(Y * ss + cSub), dir);
+      }
+    });
+    // buildAaMask (adaptive_aa.hpp:64-180): 4-neighbour pair predicates, one dilation
+    const float thr = d.aa_threshold;
+    const bool persp = !d.cam_orthographic;
+    const float pixelWorldSize = d.cam_orthographic ? (d.cam_height / static_cast<float>(Hf))
+                                                    : (2.0f * persHalfH / static_cast<float>(Hf));
+    auto pairRefine = [&](const PixelOut& a, const PixelOut& b, float za0, float zb1) {
+      if (a.geom != b.geom || a.first.group != b.first.group) return true;
+      if (std::fabs(a.r - b.r) > thr || std::fabs(a.g - b.g) > thr || std::fabs(a.b - b.b) > thr ||
+          std::fabs(a.a - b.a) > thr)
+        return true;
+      if (a.geom == kInvalid || b.geom == kInvalid) return false;
+      const V3 na = a.first.normal, nb = b.first.normal;
+      const float la = na.x * na.x + na.y * na.y + na.z * na.z;
+      const float lb = nb.x * nb.x + nb.y * nb.y + nb.z * nb.z;
+      if (la > 0.0f && lb > 0.0f) {
+        const float dd = na.x * nb.x + na.y * nb.y + na.z * nb.z;
+        if (1.0f - dd > 0.3f) return true;
+      }
+      const float step = std::fabs(b.viewZ - a.viewZ);
+      const float sa = std::fabs(a.viewZ - za0);
+      const float sb = std::fabs(zb1 - b.viewZ);
+      const float slope = sa < sb ? sa : sb;
+      float absTerm = 12.0f * pixelWorldSize;
+      if (persp) {
+        const float zmin = std::fabs(a.viewZ) < std::fabs(b.viewZ) ? std::fabs(a.viewZ) : std::fabs(b.viewZ);
+        absTerm *= zmin;
+      }
+      const float th = 3.0f * slope > absTerm ? 3.0f * slope : absTerm;
+      return step > th;
+    };
+    auto at = [&](int x, int y) -> const PixelOut& { return centers[static_cast<size_t>(y) * Wf + x]; };
+    std::vector<uint8_t> raw(static_cast<size_t>(Wf) * Hf, 0), mask(raw.size(), 0);
+    for (int y = 0; y < Hf; ++y)
+      for (int x = 0; x + 1 < Wf; ++x) {
+        const PixelOut &a = at(x, y), &b = at(x + 1, y);
+        const float za0 = x > 0 ? at(x - 1, y).viewZ : 2.0f * a.viewZ - b.viewZ;
+        const float zb1 = x + 2 < Wf ? at(x + 2, y).viewZ : 2.0f * b.viewZ - a.viewZ;
+        if (pairRefine(a, b, za0, zb1)) raw[size_t(y) * Wf + x] = raw[size_t(y) * Wf + x + 1] = 1;
+      }
+    for (int y = 0; y + 1 < Hf; ++y)
+      for (int x = 0; x < Wf; ++x) {
+        const PixelOut &a = at(x, y), &b = at(x, y + 1);
+        const float za0 = y > 0 ? at(x, y - 1).viewZ : 2.0f * a.viewZ - b.viewZ;
+        const float zb1 = y + 2 < Hf ? at(x, y + 2).viewZ : 2.0f * b.viewZ - a.viewZ;
+        if (pairRefine(a, b, za0, zb1)) raw[size_t(y) * Wf + x] = raw[size_t(y + 1) * Wf + x] = 1;
+      }
+    for (int y = 0; y < Hf; ++y)
+      for (int x = 0; x < Wf; ++x) {
+        uint8_t v = 0;
+        for (int dy = -1; dy <= 1 && !v; ++dy)
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int xx = x + dx, yy = y + dy;
+            if (xx < 0 || yy < 0 || xx >= Wf || yy >= Hf) continue;
+            if (raw[size_t(yy) * Wf + xx]) { v = 1; break; }
+          }
+        mask[size_t(y) * Wf + x] = v;
+      }
+    if (fr->aa_mask) for (size_t i = 0; i < mask.size(); ++i) fr->aa_mask[i] = float(mask[i]);
+    // replication context: ss^2 AO and (stochastic) soft-shadow samples
+    const bool soft = d.shadow_samples > 1 && d.light_radius_deg > 0.0f;
+    const bool needBoost = ss > 1 && (d.ao_samples > 0 || soft);
+    Ctx cb = c;
+    cb.o.aoSamples = c.o.aoSamples * ss * ss;
+    cb.o.shadowSamples = c.o.shadowSamples * (soft ? ss * ss : 1);
+    parallelRows(Hf, [&](int Y) {
+      for (int X = 0; X < Wf; ++X) {
+        const size_t XY = static_cast<size_t>(Y) * Wf + X;
+        if (!mask[XY]) {
+          PixelOut rep = centers[XY];
+          if (needBoost) {
+            V3 org, rd;
+            rayAt(X * ss + cSub, Y * ss + cSub, org, rd);
+            rep = integratePixel(cb, org, rd, uint32_t(X * ss + cSub), uint32_t(Y * ss + cSub), dir);
+          }
+          for (int j = 0; j < ss; ++j)
+            for (int i = 0; i < ss; ++i) store(static_cast<size_t>(Y * ss + j) * W + (X * ss + i), rep);
+          continue;
+        }
+        for (int j = 0; j < ss; ++j)
+          for (int i = 0; i < ss; ++i) {
+            const int px = X * ss + i, py = Y * ss + j;
+            if (kFine == 1 && i == cSub && j == cSub) {
+              store(static_cast<size_t>(py) * W + px, centers[XY]);
+              continue;
+            }
+            if (kFine > 1) {
+              store(static_cast<size_t>(py) * W + px, shadeCell(px, py));
+              continue;
+            }
+            V3 org, rd;
+            rayAt(px, py, org, rd);
+            store(static_cast<size_t>(py) * W + px, integratePixel(c, org, rd, uint32_t(px), uint32_t(py), dir));
+          }
+      }
+    });
+    const auto t1 = std::chrono::steady_clock::now();
+    fr->render_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    row0 = row1 = 0;  // the pixel loop below has nothing left to do
+  }
   std::atomic<int> nextRow{row0};
   std::atomic<uint64_t> rays{0}, capped{0};
   auto worker = [&]() {
@@ -955,26 +1160,9 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
         }
         const PixelOut po = integratePixel(c, org, rd, static_cast<uint32_t>(px), static_cast<uint32_t>(py), dir);
         const size_t pix = static_cast<size_t>(py) * W + px;
-        color[4 * pix] = po.r; color[4 * pix + 1] = po.g; color[4 * pix + 2] = po.b; color[4 * pix + 3] = po.a;
-        depth[pix] = po.depth;
-        viewZ[pix] = po.viewZ;
-        hg[pix] = po.geom;
-        hp[pix] = po.prim;
+        store(pix, po);
         myRays += po.rays;
         myCapped += po.capped ? 1 : 0;
-        if (aov) {  // storeShadingChannels / storeGBufChannels (embree_renderer.cpp:213-250)
-          const HitShade& f = po.first;
-          const float a3[3][3] = {{f.albedo.x, f.albedo.y, f.albedo.z}, {f.normal.x, f.normal.y, f.normal.z},
-                                  {f.bent.x, f.bent.y, f.bent.z}};
-          for (int k = 0; k < 3; ++k) {
-            aAlb[3 * pix + k] = a3[0][k];
-            aNrm[3 * pix + k] = a3[1][k];
-            aBent[3 * pix + k] = a3[2][k];
-          }
-          aCon[pix] = f.contact;
-          aShp[pix] = f.shape;
-          aAvg[pix] = f.avgHit;
-        }
       }
     }
     rays += myRays;
@@ -988,7 +1176,7 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   worker();
   for (auto& th : pool) th.join();
   const auto t1 = std::chrono::steady_clock::now();
-  fr->render_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  if (!adaptive) fr->render_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   fr->rays_primary = rays.load();
   fr->capped_rays = capped.load();
 

@@ -209,6 +209,10 @@ class RenderOptions:
     maxTransparentLayers: int = 256
     giIntegrator: int = 2
     aoWriteAov: bool = False
+    aaMode: int = 0
+    aaThreshold: float = 0.1
+    aaDepth: int = 0
+    aaDebug: bool = False
 
     def aoEnhanced(self) -> bool:
         return (self.aoFalloffPower > 0.0 or self.aoMultiScale or self.aoBentNormal or self.aoMultibounce
@@ -273,6 +277,7 @@ def make_render_desc(scene: Scene, opt: RenderOptions):
     d.max_transparent_layers = opt.maxTransparentLayers
     d.gi_integrator = opt.giIntegrator
     d.ao_write_aov = int(opt.aoWriteAov)
+    d.aa_mode, d.aa_threshold, d.aa_depth = opt.aaMode, opt.aaThreshold, opt.aaDepth
     return d, keep
 
 
@@ -295,6 +300,7 @@ class FrameResult:
     contactAo: np.ndarray = None   # (H, W)
     shapeAo: np.ndarray = None     # (H, W)
     avgHitDist: np.ndarray = None  # (H, W)
+    aaMask: np.ndarray = None      # (H, W) adaptive-AA refinement mask (aaDebug)
 
 
 AOV_FIELDS = (("albedo", "albedo", 3), ("normal", "normal", 3), ("bentNormal", "bent_normal", 3),
@@ -302,8 +308,12 @@ AOV_FIELDS = (("albedo", "albedo", 3), ("normal", "normal", 3), ("bentNormal", "
 
 
 def attach_aovs(fr, opt) -> dict:
-    """Allocate the AO AOV planes of a frame when opt.aoWriteAov asks for them."""
+    """Allocate the AO AOV planes of a frame when opt.aoWriteAov asks for
+    them, and the adaptive-AA mask when opt.aaDebug does."""
     out = {}
+    if opt.aaMode == 1 and opt.aaDebug:
+        out["aaMask"] = np.zeros((opt.height, opt.width), np.float32)
+        fr.aa_mask = abi.ptr(out["aaMask"])
     if opt.aoWriteAov:
         for name, cname, ch in AOV_FIELDS:
             a = np.zeros((opt.height, opt.width, ch) if ch > 1 else (opt.height, opt.width), np.float32)

@@ -52,12 +52,18 @@ struct Bufs {
   float4* aovA;       // per hi-res pixel first-hit AOVs (or null): albedo.rgb, contact
   float4* aovB;       //   normal.xyz, shape
   float4* aovC;       //   bent normal.xyz, mean occluder distance
+  float4* aaN;        // per hi-res pixel (adaptive AA, or null): first-hit normal.xyz, section (int bits)
+  const uint32_t* coord;  // fine-lattice pass (or null): lattice index of each pixel slot
   const LightD* lights;
   unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
   uint32_t* counter;  // [0] next-queue size, [1] occlusion work-queue size
   uint32_t* occQueue; // queue slots of hits that cast AO / shadow rays
   unsigned long long* cursor;  // next ray of the persistent occlusion kernel
 };
+
+// Lattice index of pixel slot gpix: the slot itself, or its entry in the
+// coordinate table of a fine-lattice pass.
+UBR_D uint32_t latticeOf(const Bufs& b, uint32_t gpix) { return b.coord ? __ldg(&b.coord[gpix]) : gpix; }
 
 // Per-frame record of a batched launch (device array): the frame's
 // parameters and scene, and where its pixels start in the batch's global
@@ -100,11 +106,11 @@ __global__ void __launch_bounds__(128, 8) k_trace_closest(Params p1, DScene s1, 
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t traced = 0, ovf = 0;
   if (i < n) {
-    const uint32_t gpix = layer == 0 ? i : queue[i];
+    const uint32_t gpix = queue ? queue[i] : i;
     const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
-    const uint32_t pix = gpix - (BATCH ? bt.frames[f].pixOff : 0u);
+    const uint32_t pix = BATCH ? gpix - bt.frames[f].pixOff : latticeOf(b, gpix);
     const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
     f3 org, rd;
     primaryRay(p, px, py, org, rd);
@@ -132,11 +138,11 @@ __global__ void __launch_bounds__(128) k_surface(Params p1, DScene s1, Batch bt,
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool cast = false;
   if (i < n) {
-    const uint32_t gpix = layer == 0 ? i : queue[i];
+    const uint32_t gpix = queue ? queue[i] : i;
     const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
-    const uint32_t pix = gpix - (BATCH ? bt.frames[f].pixOff : 0u);
+    const uint32_t pix = BATCH ? gpix - bt.frames[f].pixOff : latticeOf(b, gpix);
     const float4 ha = b.hitA[i];
     const uint32_t ref = __float_as_uint(ha.w);
     if (ref == kInvalid) {
@@ -278,7 +284,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p1, DScene s1
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
     if (j < p.raysPerHit) {
-      const OccRay o = occlusionRay(p, b, slot, sc.x - (BATCH ? bt.frames[f].pixOff : 0u), sc.y, j);
+      const OccRay o = occlusionRay(p, b, slot, BATCH ? sc.x - bt.frames[f].pixOff : latticeOf(b, sc.x), sc.y, j);
       bool hit = false;
       Hit h;
       h.t = kInfF;
@@ -326,7 +332,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_gs(Params p1, DScene
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
     if (j < p.raysPerHit) {
-      const OccRay o = occlusionRay(p, b, slot, sc.x - (BATCH ? bt.frames[f].pixOff : 0u), sc.y, j);
+      const OccRay o = occlusionRay(p, b, slot, BATCH ? sc.x - bt.frames[f].pixOff : latticeOf(b, sc.x), sc.y, j);
       bool hit = false;
       Hit h;
       h.t = kInfF;
@@ -392,7 +398,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p1
           f = BATCH ? int(sc.y >> 8) : 0;
           const Params& p = BATCH ? bt.frames[f].p : p1;
           const DScene& s = BATCH ? bt.frames[f].s : s1;
-          if (j < p.raysPerHit) o = occlusionRay(p, b, slot, sc.x - (BATCH ? bt.frames[f].pixOff : 0u), sc.y, j);
+          if (j < p.raysPerHit) o = occlusionRay(p, b, slot, BATCH ? sc.x - bt.frames[f].pixOff : latticeOf(b, sc.x), sc.y, j);
           else o.trace = o.grazing = o.ao = false;
           if (j >= p.raysPerHit) {
             // stride padding of a frame with fewer rays per hit: nothing to do
@@ -508,14 +514,14 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
   bool push = false;
   uint32_t gpix = 0, capped = 0;
   if (i < n) {
-    gpix = layer == 0 ? i : queue[i];
+    gpix = queue ? queue[i] : i;
     const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
     const LightD* lights = b.lights + p.lightOff;
     const uint64_t R = BATCH ? uint64_t(bt.R) : uint64_t(p.raysPerHit);
     const uint64_t aoStride = BATCH ? uint64_t(bt.aoStride) : uint64_t(p.aoSamples);
-    const uint32_t pix = gpix - (BATCH ? bt.frames[f].pixOff : 0u);
+    const uint32_t pix = BATCH ? gpix - bt.frames[f].pixOff : latticeOf(b, gpix);
     const int px = int(pix % uint32_t(p.W)), py = int(pix / uint32_t(p.W));
     float4 acc = layer == 0 ? make_float4(0, 0, 0, 0) : b.accum[gpix];
     f3 base = p.bg;
@@ -646,6 +652,17 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
             b.aovC[gpix] = make_float4(aq.bent.x, aq.bent.y, aq.bent.z, aq.avgHit);
           }
         }
+        if (b.aaN && p.aaMode == 1) {
+          // first-hit shading normal and section for the adaptive-AA mask
+          // (hit_shader.hpp:214-220, 277, 321, 457)
+          int grp = 0;
+          if (sf.kind == kMesh) {
+            if (s.meshTriGroup) grp = __ldg(&s.meshTriGroup[s.baseTri ? sf.prim % s.baseTri : sf.prim]);
+          } else if (s.primGroup[sf.kind]) {
+            grp = __ldg(&s.primGroup[sf.kind][sf.prim]);
+          }
+          b.aaN[gpix] = make_float4(sf.N.x, sf.N.y, sf.N.z, __int_as_float(grp));
+        }
         b.depth[gpix] = t;
         b.viewZ[gpix] = t * dot(rd, p.camDir);
         b.hitGeom[gpix] = s.geomID[sf.kind];
@@ -758,10 +775,14 @@ __global__ void k_post(Params p1, Batch bt, uint32_t nOut, const float4* colorHi
   out[go] = r;
 }
 
+// First-hit state of a pixel before its primary ray (all pixels, or the
+// pixels of a list when `list` is set).
 __global__ void k_init_pixels(uint32_t npix, float* depth, float* viewZ, uint32_t* hg, uint32_t* hp, float4* aovA,
-                              float4* aovB, float4* aovC) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= npix) return;
+                              float4* aovB, float4* aovC, float4* aaN = nullptr, const uint32_t* list = nullptr) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= npix) return;
+  const uint32_t i = list ? list[k] : k;
+  if (aaN) aaN[i] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
   depth[i] = 0.0f;
   viewZ[i] = 0.0f;
   hg[i] = kInvalid;
@@ -815,6 +836,205 @@ __global__ void k_post_aov(Params p1, Batch bt, uint32_t nOut, const float4* aov
   avg[go] = a[11];
 }
 
+// ---- Adaptive AA (embree_renderer.cpp:1379-1670, render/adaptive_aa.hpp) ----
+// Phase 1 shades the centre subpixel (ss/2, ss/2) of each output pixel; the
+// refinement mask compares 4-neighbour centre pairs and is dilated once; the
+// flagged blocks shade their remaining subpixels, the others replicate their
+// centre (re-shaded first with ss^2 AO / soft-shadow samples).
+struct AaGrid {
+  const float4* color;  // hi-res colour before fog
+  const float* viewZ;
+  const uint32_t* geom;
+  const float4* nrm;    // first-hit normal.xyz, section id (int bits)
+  int W, ss, cSub, Wf, Hf;
+  float thr, pixelWorldSize;
+  int persp;
+};
+
+UBR_D uint32_t aaCentre(const AaGrid& g, int x, int y) {
+  return uint32_t(y * g.ss + g.cSub) * uint32_t(g.W) + uint32_t(x * g.ss + g.cSub);
+}
+
+// aaPairNeedsRefine (adaptive_aa.hpp:65-111): a and b are neighbouring
+// centres, za0 / zb1 the view z one step beyond each (or extrapolated).
+UBR_D bool aaPairRefine(const AaGrid& g, uint32_t a, uint32_t b, float za0, float zb1) {
+  const uint32_t ga = g.geom[a], gb = g.geom[b];
+  const float4 na = g.nrm[a], nb = g.nrm[b];
+  if (ga != gb || __float_as_int(na.w) != __float_as_int(nb.w)) return true;
+  const float4 ca = g.color[a], cb = g.color[b];
+  if (fabsf(ca.x - cb.x) > g.thr || fabsf(ca.y - cb.y) > g.thr || fabsf(ca.z - cb.z) > g.thr ||
+      fabsf(ca.w - cb.w) > g.thr)
+    return true;
+  if (ga == kInvalid || gb == kInvalid) return false;
+  const float la = na.x * na.x + na.y * na.y + na.z * na.z;
+  const float lb = nb.x * nb.x + nb.y * nb.y + nb.z * nb.z;
+  if (la > 0.0f && lb > 0.0f) {
+    const float dd = na.x * nb.x + na.y * nb.y + na.z * nb.z;
+    if (1.0f - dd > 0.3f) return true;
+  }
+  const float za = g.viewZ[a], zb = g.viewZ[b];
+  const float step = fabsf(zb - za);
+  const float sa = fabsf(za - za0), sb = fabsf(zb1 - zb);
+  const float slope = sa < sb ? sa : sb;
+  float absTerm = 12.0f * g.pixelWorldSize;
+  if (g.persp) absTerm *= fabsf(za) < fabsf(zb) ? fabsf(za) : fabsf(zb);
+  const float th = 3.0f * slope > absTerm ? 3.0f * slope : absTerm;
+  return step > th;
+}
+
+// Horizontal pair (x0, x0 + 1) or vertical pair (y0, y0 + 1) of buildAaMask
+// (adaptive_aa.hpp:132-161).
+UBR_D bool aaPairH(const AaGrid& g, int x0, int y) {
+  const uint32_t a = aaCentre(g, x0, y), b = aaCentre(g, x0 + 1, y);
+  const float za = g.viewZ[a], zb = g.viewZ[b];
+  const float za0 = x0 > 0 ? g.viewZ[aaCentre(g, x0 - 1, y)] : 2.0f * za - zb;
+  const float zb1 = x0 + 2 < g.Wf ? g.viewZ[aaCentre(g, x0 + 2, y)] : 2.0f * zb - za;
+  return aaPairRefine(g, a, b, za0, zb1);
+}
+UBR_D bool aaPairV(const AaGrid& g, int x, int y0) {
+  const uint32_t a = aaCentre(g, x, y0), b = aaCentre(g, x, y0 + 1);
+  const float za = g.viewZ[a], zb = g.viewZ[b];
+  const float za0 = y0 > 0 ? g.viewZ[aaCentre(g, x, y0 - 1)] : 2.0f * za - zb;
+  const float zb1 = y0 + 2 < g.Hf ? g.viewZ[aaCentre(g, x, y0 + 2)] : 2.0f * zb - za;
+  return aaPairRefine(g, a, b, za0, zb1);
+}
+
+// centre subpixel of every output pixel, in output raster order
+__global__ void k_aa_centres(AaGrid g, uint32_t* list) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= uint32_t(g.Wf) * uint32_t(g.Hf)) return;
+  list[o] = aaCentre(g, int(o % uint32_t(g.Wf)), int(o / uint32_t(g.Wf)));
+}
+
+// raw mask: an output pixel is flagged when any of its (up to four) pairs is
+__global__ void k_aa_raw(AaGrid g, uint8_t* raw) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= uint32_t(g.Wf) * uint32_t(g.Hf)) return;
+  const int x = int(o % uint32_t(g.Wf)), y = int(o / uint32_t(g.Wf));
+  bool r = (x > 0 && aaPairH(g, x - 1, y)) || (x + 1 < g.Wf && aaPairH(g, x, y)) ||
+           (y > 0 && aaPairV(g, x, y - 1)) || (y + 1 < g.Hf && aaPairV(g, x, y));
+  raw[o] = r ? 1 : 0;
+}
+
+// dilateMask3x3 (adaptive_aa.hpp:35-56), then the work lists: every
+// non-centre subpixel of a flagged block (every subpixel when `withCentre`,
+// for the fine lattice), and the centre of every other block; `maskOut`
+// (output resolution, 1 = refined) when requested.
+__global__ void k_aa_lists(AaGrid g, const uint8_t* raw, uint32_t* flagged, uint32_t* centres,
+                           uint32_t* counts, float* maskOut, bool withCentre) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = o < uint32_t(g.Wf) * uint32_t(g.Hf);
+  int x = 0, y = 0;
+  bool m = false;
+  if (valid) {
+    x = int(o % uint32_t(g.Wf));
+    y = int(o / uint32_t(g.Wf));
+    for (int dy = -1; dy <= 1 && !m; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int xx = x + dx, yy = y + dy;
+        if (xx < 0 || yy < 0 || xx >= g.Wf || yy >= g.Hf) continue;
+        if (raw[uint32_t(yy) * uint32_t(g.Wf) + uint32_t(xx)]) {
+          m = true;
+          break;
+        }
+      }
+    if (maskOut) maskOut[o] = m ? 1.0f : 0.0f;
+  }
+  const uint32_t c = valid ? aaCentre(g, x, y) : 0u;
+  int off;
+  int base = warpPushBase(valid && !m, &counts[1], off);
+  if (valid && !m) centres[base + off] = c;
+  // subpixel k of each flagged block in this warp lands in one contiguous run
+  const int n2 = g.ss * g.ss;
+  for (int k = 0; k < n2; ++k) {
+    const int i = k % g.ss, j = k / g.ss;
+    const bool push = valid && m && (withCentre || !(i == g.cSub && j == g.cSub));
+    base = warpPushBase(push, &counts[0], off);
+    if (push) flagged[base + off] = uint32_t(y * g.ss + j) * uint32_t(g.W) + uint32_t(x * g.ss + i);
+  }
+}
+
+// unflagged blocks: the centre's first-hit state and colour to every subpixel
+__global__ void k_aa_replicate(AaGrid g, const uint32_t* centres, const uint32_t* counts, float4* color,
+                               float* depth, float* viewZ, uint32_t* hg, uint32_t* hp, float4* aovA, float4* aovB,
+                               float4* aovC) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= counts[1]) return;
+  const uint32_t c = centres[k];
+  const int cx = int(c % uint32_t(g.W)), cy = int(c / uint32_t(g.W));
+  const int x0 = cx - g.cSub, y0 = cy - g.cSub;
+  const float4 col = color[c];
+  const float d = depth[c], z = viewZ[c];
+  const uint32_t gi = hg[c], pi = hp[c];
+  float4 a = make_float4(0, 0, 0, 0), b2 = a, c3 = a;
+  if (aovA) {
+    a = aovA[c];
+    b2 = aovB[c];
+    c3 = aovC[c];
+  }
+  for (int j = 0; j < g.ss; ++j)
+    for (int i = 0; i < g.ss; ++i) {
+      const uint32_t t = uint32_t(y0 + j) * uint32_t(g.W) + uint32_t(x0 + i);
+      if (t == c) continue;
+      color[t] = col;
+      depth[t] = d;
+      viewZ[t] = z;
+      hg[t] = gi;
+      hp[t] = pi;
+      if (aovA) {
+        aovA[t] = a;
+        aovB[t] = b2;
+        aovC[t] = c3;
+      }
+    }
+}
+
+// Fine-lattice samples of the flagged cells (embree_renderer.cpp:1542-1590):
+// chunk sample t is point (t % k, t / k % k) of cell cell0 + t / k^2 on the
+// (W k) x (H k) lattice.
+__global__ void k_aa_fine_coords(AaGrid g, const uint32_t* cells, uint32_t cell0, uint32_t n, int k,
+                                 uint32_t* coord) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const uint32_t uk = uint32_t(k), k2 = uk * uk;
+  const uint32_t cell = cells[cell0 + t / k2], sub = t % k2;
+  const uint32_t cx = cell % uint32_t(g.W), cy = cell / uint32_t(g.W);
+  coord[t] = (cy * uk + sub / uk) * (uint32_t(g.W) * uk) + cx * uk + sub % uk;
+}
+
+// Box average of each cell's k^2 samples into the hi-res buffers: colour,
+// depth and view z summed in sample order then scaled by 1 / k^2; first hit
+// and AOVs from the first sample.
+__global__ void k_aa_fine_reduce(const uint32_t* cells, uint32_t cell0, uint32_t nCells, int k, Bufs fine, Bufs b) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nCells) return;
+  const uint32_t k2 = uint32_t(k) * uint32_t(k);
+  const uint32_t c = cells[cell0 + t];
+  const uint32_t s0 = t * k2;
+  float4 acc = fine.colorHi[s0];
+  float d = fine.depth[s0], z = fine.viewZ[s0];
+  for (uint32_t q = 1; q < k2; ++q) {
+    const float4 v = fine.colorHi[s0 + q];
+    acc.x += v.x;
+    acc.y += v.y;
+    acc.z += v.z;
+    acc.w += v.w;
+    d += fine.depth[s0 + q];
+    z += fine.viewZ[s0 + q];
+  }
+  const float inv = 1.0f / float(k2);
+  b.colorHi[c] = make_float4(acc.x * inv, acc.y * inv, acc.z * inv, acc.w * inv);
+  b.depth[c] = d * inv;
+  b.viewZ[c] = z * inv;
+  b.hitGeom[c] = fine.hitGeom[s0];
+  b.hitPrim[c] = fine.hitPrim[s0];
+  if (b.aovA) {
+    b.aovA[c] = fine.aovA[s0];
+    b.aovB[c] = fine.aovB[s0];
+    b.aovC[c] = fine.aovC[s0];
+  }
+}
+
 }  // namespace
 
 // Host-side parameter setup: computeCameraBasis (embree_renderer.cpp:375-386),
@@ -861,6 +1081,8 @@ ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vect
   p.aoGround = f3{d.ao_ground_color[0], d.ao_ground_color[1], d.ao_ground_color[2]};
   p.aoDiffuseFactor = d.ao_diffuse_factor;
   p.aoWriteAov = d.ao_write_aov ? 1 : 0;
+  p.aaMode = d.aa_mode == 1 ? 1 : 0;  // any other value renders the full grid
+  p.aaThreshold = d.aa_threshold;
   p.aoEnhanced = (d.ao_falloff_power > 0.0f || d.ao_multiscale || d.ao_bent_normal || d.ao_multibounce ||
                   d.ao_low_discrepancy || d.ao_diffuse_factor > 0.0f)
                      ? 1
@@ -1148,6 +1370,20 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   const Params& p1 = fds[0].p;
   const DScene& s1 = fds[0].s;
   ubr_status st = UBR_OK;
+  // adaptive AA (one frame per call): supersampled, or a fine lattice at ss 1
+  const ubr_render_desc& d0 = *jobs[0].desc;
+  const bool adaptive = !batch && p1.aaMode == 1 && (p1.ss > 1 || d0.aa_depth > 1);
+  if (batch)
+    for (size_t f = 0; f < nf; ++f)
+      if (fds[f].p.aaMode == 1 && (fds[f].p.ss > 1 || jobs[f].desc->aa_depth > 1))
+        return setError(c, UBR_INVALID_ARGUMENT, "render batch: adaptive AA renders one frame per call");
+  // fine lattice of flagged cells: kFine^2 samples per hi-res cell
+  const int kFine = adaptive ? std::max(1, (d0.aa_depth + p1.ss - 1) / p1.ss) : 1;
+  const uint32_t k2 = uint32_t(kFine) * uint32_t(kFine);
+  if (kFine > 1 && (uint64_t(p1.W) * kFine * uint64_t(p1.H) * kFine >= (1ull << 32) || k2 > (1u << 16)))
+    return setError(c, UBR_INVALID_ARGUMENT, "render desc: aa_depth lattice too large");
+  // per-slot buffers hold a full frame, or one chunk of fine samples
+  const uint32_t nslot = std::max(npix, k2);
   Bufs b{};
   b.accum = scratchT<float4>(c, 16, npix, st);
   b.tnear = scratchT<float>(c, 17, npix, st);
@@ -1156,20 +1392,21 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   b.viewZ = scratchT<float>(c, 20, npix, st);
   b.hitGeom = scratchT<uint32_t>(c, 21, npix, st);
   b.hitPrim = scratchT<uint32_t>(c, 22, npix, st);
-  b.hitA = scratchT<float4>(c, 23, npix, st);
-  b.hitB = scratchT<float4>(c, 24, npix, st);
-  uint32_t* q0 = scratchT<uint32_t>(c, 25, npix, st);
-  uint32_t* q1 = scratchT<uint32_t>(c, 26, npix, st);
+  b.hitA = scratchT<float4>(c, 23, nslot, st);
+  b.hitB = scratchT<float4>(c, 24, nslot, st);
+  uint32_t* q0 = scratchT<uint32_t>(c, 25, nslot, st);
+  uint32_t* q1 = scratchT<uint32_t>(c, 26, nslot, st);
   if (secondary) {
-    b.surfA = scratchT<float4>(c, 27, npix, st);
-    b.surfB = scratchT<float4>(c, 28, npix, st);
-    b.surfC = scratchT<uint2>(c, 29, npix, st);
-    b.occQueue = scratchT<uint32_t>(c, 36, npix, st);
+    b.surfA = scratchT<float4>(c, 27, nslot, st);
+    b.surfB = scratchT<float4>(c, 28, nslot, st);
+    b.surfC = scratchT<uint2>(c, 29, nslot, st);
+    b.occQueue = scratchT<uint32_t>(c, 36, nslot, st);
     b.cursor = scratchT<unsigned long long>(c, 37, 1, st);
-    b.occ = scratchT<uint8_t>(c, 30, size_t(npix) * R, st);
-    if (enhanced) b.aoT = scratchT<float>(c, 31, size_t(npix) * aoStride, st);
+    b.occ = scratchT<uint8_t>(c, 30, size_t(nslot) * R, st);
+    if (enhanced) b.aoT = scratchT<float>(c, 31, size_t(nslot) * aoStride, st);
   }
   LightD* dl = scratchT<LightD>(c, 32, lights.size() + 1, st);
+  b.lights = dl;
   b.stats = scratchT<unsigned long long>(c, 33, 8, st);
   b.counter = scratchT<uint32_t>(c, 34, 4, st);
   float4* outColor = scratchT<float4>(c, 35, nout, st);
@@ -1179,6 +1416,62 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     b.aovB = scratchT<float4>(c, 71, npix, st);
     b.aovC = scratchT<float4>(c, 72, npix, st);
     outAov = scratchT<float>(c, 73, size_t(nout) * 12, st);
+  }
+  const uint32_t nCentre = uint32_t(p1.outW) * uint32_t(p1.outH);
+  uint32_t *aaList0 = nullptr, *aaList1 = nullptr, *aaCounts = nullptr;
+  uint8_t* aaRaw = nullptr;
+  float* aaMaskOut = nullptr;
+  Params pBoost{}, pFine{};
+  std::vector<LightD> lightsBoost;
+  LightD* dlBoost = nullptr;
+  bool needBoost = false;
+  Bufs bFine{};
+  uint32_t fineCap = 0;  // fine samples per chunk (a multiple of kFine^2)
+  uint32_t* fineCoord = nullptr;
+  if (adaptive) {
+    const int ss = p1.ss;
+    b.aaN = scratchT<float4>(c, 74, npix, st);
+    aaList0 = scratchT<uint32_t>(c, 75, nCentre, st);
+    aaList1 = scratchT<uint32_t>(c, 76, size_t(nCentre) * size_t(ss * ss), st);
+    aaRaw = scratchT<uint8_t>(c, 77, nCentre, st);
+    aaCounts = scratchT<uint32_t>(c, 78, 2, st);
+    if (jobs[0].frame->aa_mask) aaMaskOut = scratchT<float>(c, 79, nCentre, st);
+    // replication context (embree_renderer.cpp:1592-1608): ss^2 AO samples,
+    // ss^2 soft-shadow samples when shadows are stochastic
+    const bool soft = d0.shadow_samples > 1 && d0.light_radius_deg > 0.0f;
+    needBoost = ss > 1 && (d0.ao_samples > 0 || soft);
+    if (needBoost) {
+      ubr_render_desc db = d0;
+      db.ao_samples = d0.ao_samples * ss * ss;
+      if (soft) db.shadow_samples = d0.shadow_samples * ss * ss;
+      st = makeParams(c, db, pBoost, lightsBoost);
+      if (st != UBR_OK) return st;
+      dlBoost = scratchT<LightD>(c, 80, lightsBoost.size() + 1, st);
+    }
+    if (kFine > 1) {
+      // the (W k) x (H k) lattice: same camera, seeds on the finer grid
+      pFine = p1;
+      pFine.W = p1.W * kFine;
+      pFine.H = p1.H * kFine;
+      fineCap = (nslot / k2) * k2;
+      bFine = b;
+      bFine.lights = dl;
+      bFine.aaN = nullptr;
+      bFine.accum = scratchT<float4>(c, 81, fineCap, st);
+      bFine.tnear = scratchT<float>(c, 82, fineCap, st);
+      bFine.colorHi = scratchT<float4>(c, 83, fineCap, st);
+      bFine.depth = scratchT<float>(c, 84, fineCap, st);
+      bFine.viewZ = scratchT<float>(c, 85, fineCap, st);
+      bFine.hitGeom = scratchT<uint32_t>(c, 86, fineCap, st);
+      bFine.hitPrim = scratchT<uint32_t>(c, 87, fineCap, st);
+      fineCoord = scratchT<uint32_t>(c, 88, fineCap, st);
+      bFine.coord = fineCoord;
+      if (aov) {
+        bFine.aovA = scratchT<float4>(c, 89, fineCap, st);
+        bFine.aovB = scratchT<float4>(c, 90, fineCap, st);
+        bFine.aovC = scratchT<float4>(c, 91, fineCap, st);
+      }
+    }
   }
   Batch bt{};
   if (batch) {
@@ -1197,7 +1490,6 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     bt.aoStride = aoStride;
   }
   if (st != UBR_OK) return st;
-  b.lights = dl;
   cudaStream_t s = c->stream;
   uint32_t kernels = 0;
   const uint32_t flags = total ? total->flags : 0u;
@@ -1222,34 +1514,35 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   };
   const int TB = 128;
   // one transparency round of device work
-  auto round = [&](int layer, uint32_t n, const uint32_t* queue, uint32_t* outQ) -> ubr_status {
-    UBR_CUDA(c, cudaMemsetAsync(b.counter, 0, 2 * sizeof(uint32_t), s));
+  auto round = [&](const Params& pr, const Bufs& br, uint32_t Rr, int layer, uint32_t n, const uint32_t* queue,
+                   uint32_t* outQ) -> ubr_status {
+    UBR_CUDA(c, cudaMemsetAsync(br.counter, 0, 2 * sizeof(uint32_t), s));
     const uint32_t grid = (n + TB - 1) / TB;
     mark(0, true);
-    launchClosest(km, count, batch, grid, TB, s, p1, s1, bt, b, layer, n, queue);
+    launchClosest(km, count, batch, grid, TB, s, pr, s1, bt, br, layer, n, queue);
     mark(0, false);
     ++kernels;
     if (secondary) {
       mark(1, true);
-      if (batch) k_surface<true><<<grid, TB, 0, s>>>(p1, s1, bt, b, layer, n, queue);
-      else k_surface<false><<<grid, TB, 0, s>>>(p1, s1, bt, b, layer, n, queue);
+      if (batch) k_surface<true><<<grid, TB, 0, s>>>(pr, s1, bt, br, layer, n, queue);
+      else k_surface<false><<<grid, TB, 0, s>>>(pr, s1, bt, br, layer, n, queue);
       mark(1, false);
-      const uint64_t nr = uint64_t(n) * uint64_t(R);
+      const uint64_t nr = uint64_t(n) * uint64_t(Rr);
       mark(2, true);
       if (c->traceMode == 1) {
-        launchOcclusion(km, count, batch, uint32_t((nr + TB - 1) / TB), TB, s, p1, s1, bt, b, n);
+        launchOcclusion(km, count, batch, uint32_t((nr + TB - 1) / TB), TB, s, pr, s1, bt, br, n);
       } else if (c->traceMode == 3) {
-        launchOcclusionGridStride(km, count, batch, gridStrideGrid(c->device), TB, s, p1, s1, bt, b);
+        launchOcclusionGridStride(km, count, batch, gridStrideGrid(c->device), TB, s, pr, s1, bt, br);
       } else {
-        UBR_CUDA(c, cudaMemsetAsync(b.cursor, 0, sizeof(unsigned long long), s));
-        launchOcclusionPersistent(km, count, batch, persistentGrid(c->device), TB, s, p1, s1, bt, b);
+        UBR_CUDA(c, cudaMemsetAsync(br.cursor, 0, sizeof(unsigned long long), s));
+        launchOcclusionPersistent(km, count, batch, persistentGrid(c->device), TB, s, pr, s1, bt, br);
       }
       mark(2, false);
       kernels += 2;
     }
     mark(3, true);
-    if (batch) k_shade<true><<<grid, TB, 0, s>>>(p1, s1, bt, b, layer, n, queue, outQ);
-    else k_shade<false><<<grid, TB, 0, s>>>(p1, s1, bt, b, layer, n, queue, outQ);
+    if (batch) k_shade<true><<<grid, TB, 0, s>>>(pr, s1, bt, br, layer, n, queue, outQ);
+    else k_shade<false><<<grid, TB, 0, s>>>(pr, s1, bt, br, layer, n, queue, outQ);
     mark(3, false);
     ++kernels;
     UBR_CUDA(c, cudaGetLastError());
@@ -1278,9 +1571,106 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   cudaEventRecord(c->ev[0], s);
   if (!lights.empty())
     UBR_CUDA(c, cudaMemcpyAsync(dl, lights.data(), lights.size() * sizeof(LightD), cudaMemcpyHostToDevice, s));
+  if (dlBoost && !lightsBoost.empty())
+    UBR_CUDA(c, cudaMemcpyAsync(dlBoost, lightsBoost.data(), lightsBoost.size() * sizeof(LightD),
+                                cudaMemcpyHostToDevice, s));
   int layer = 0;
   bool cancelled = false;
-  const bool useGraph = singleLayer && !prof && !count && c->useGraphs;
+  uint32_t* hostCount = static_cast<uint32_t*>(c->pinned);
+  // all transparency rounds of one set of pixels: the first round over
+  // `list` (all pixels when null), later rounds over the survivors
+  auto runLayers = [&](const Params& pr, const Bufs& br, uint32_t Rr, const uint32_t* list,
+                       uint32_t n) -> ubr_status {
+    const uint32_t* queue = list;
+    uint32_t* qs[2] = {q0, q1};
+    int l = 0;
+    for (; l < maxIters && n > 0; ++l) {
+      uint32_t* outQ = qs[l & 1];
+      const ubr_status rs = round(pr, br, Rr, l, n, queue, outQ);
+      if (rs != UBR_OK) return rs;
+      if (l + 1 >= maxIters) {
+        ++l;
+        break;
+      }
+      UBR_CUDA(c, cudaMemcpyAsync(hostCount, br.counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      UBR_CUDA(c, cudaStreamSynchronize(s));
+      n = *hostCount;
+      queue = outQ;
+      if (progress) *progress = uint64_t(l + 1);
+      if (cancel && *cancel) {
+        cancelled = true;
+        ++l;
+        break;
+      }
+    }
+    layer = std::max(layer, l);
+    return UBR_OK;
+  };
+  // adaptive AA passes: centres, mask, flagged subpixels, re-shaded centres,
+  // replication (embree_renderer.cpp:1379-1670)
+  auto runAdaptive = [&]() -> ubr_status {
+    AaGrid g{};
+    g.color = b.colorHi;
+    g.viewZ = b.viewZ;
+    g.geom = b.hitGeom;
+    g.nrm = b.aaN;
+    g.W = p1.W;
+    g.ss = p1.ss;
+    g.cSub = p1.ss / 2;
+    g.Wf = p1.outW;
+    g.Hf = p1.outH;
+    g.thr = p1.aaThreshold;
+    g.persp = d0.cam_orthographic ? 0 : 1;
+    g.pixelWorldSize = d0.cam_orthographic ? d0.cam_height / float(g.Hf) : 2.0f * p1.persHalfH / float(g.Hf);
+    const uint32_t gridC = (nCentre + 255) / 256;
+    k_aa_centres<<<gridC, 256, 0, s>>>(g, aaList0);
+    ++kernels;
+    ubr_status rs = runLayers(p1, b, R, aaList0, nCentre);
+    if (rs != UBR_OK || cancelled) return rs;
+    k_aa_raw<<<gridC, 256, 0, s>>>(g, aaRaw);
+    UBR_CUDA(c, cudaMemsetAsync(aaCounts, 0, 2 * sizeof(uint32_t), s));
+    k_aa_lists<<<gridC, 256, 0, s>>>(g, aaRaw, aaList1, aaList0, aaCounts, aaMaskOut, kFine > 1);
+    kernels += 2;
+    uint32_t* hc = hostCount + 2;
+    UBR_CUDA(c, cudaMemcpyAsync(hc, aaCounts, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    UBR_CUDA(c, cudaStreamSynchronize(s));
+    const uint32_t nFlagged = hc[0], nCentres = hc[1];
+    if (kFine == 1) {
+      rs = runLayers(p1, b, R, aaList1, nFlagged);
+      if (rs != UBR_OK || cancelled) return rs;
+    } else {
+      // flagged cells in chunks of fineCap / k^2 cells
+      const uint32_t cellsPerChunk = fineCap / k2;
+      for (uint32_t cell0 = 0; cell0 < nFlagged; cell0 += cellsPerChunk) {
+        const uint32_t nc = std::min(cellsPerChunk, nFlagged - cell0), n = nc * k2;
+        k_aa_fine_coords<<<(n + 255) / 256, 256, 0, s>>>(g, aaList1, cell0, n, kFine, fineCoord);
+        k_init_pixels<<<(n + 255) / 256, 256, 0, s>>>(n, bFine.depth, bFine.viewZ, bFine.hitGeom, bFine.hitPrim,
+                                                      bFine.aovA, bFine.aovB, bFine.aovC);
+        kernels += 2;
+        rs = runLayers(pFine, bFine, R, nullptr, n);
+        if (rs != UBR_OK || cancelled) return rs;
+        k_aa_fine_reduce<<<(nc + 255) / 256, 256, 0, s>>>(aaList1, cell0, nc, kFine, bFine, b);
+        ++kernels;
+      }
+    }
+    if (needBoost && nCentres > 0) {
+      k_init_pixels<<<(nCentres + 255) / 256, 256, 0, s>>>(nCentres, b.depth, b.viewZ, b.hitGeom, b.hitPrim,
+                                                           b.aovA, b.aovB, b.aovC, b.aaN, aaList0);
+      ++kernels;
+      Bufs bb = b;
+      bb.lights = dlBoost;
+      rs = runLayers(pBoost, bb, uint32_t(pBoost.raysPerHit), aaList0, nCentres);
+      if (rs != UBR_OK || cancelled) return rs;
+    }
+    if (nCentres > 0) {
+      k_aa_replicate<<<(nCentres + 255) / 256, 256, 0, s>>>(g, aaList0, aaCounts, b.colorHi, b.depth, b.viewZ,
+                                                            b.hitGeom, b.hitPrim, b.aovA, b.aovB, b.aovC);
+      ++kernels;
+    }
+    UBR_CUDA(c, cudaGetLastError());
+    return UBR_OK;
+  };
+  const bool useGraph = singleLayer && !prof && !count && c->useGraphs && !adaptive;
   if (useGraph) {
     // key: everything the captured launches depend on
     std::vector<unsigned char> key(sizeof(Params) + sizeof(DScene) + sizeof(Batch) + sizeof(Bufs) + 64);
@@ -1301,7 +1691,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s);
       k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim, b.aovA,
                                                        b.aovB, b.aovC);
-      ubr_status rs = round(0, npix, nullptr, q0);
+      ubr_status rs = round(p1, b, R, 0, npix, nullptr, q0);
       if (rs == UBR_OK) rs = post();
       cudaGraph_t graph = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(s, &graph);
@@ -1340,32 +1730,11 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   } else {
     UBR_CUDA(c, cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s));
     k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim, b.aovA,
-                                                       b.aovB, b.aovC);
+                                                       b.aovB, b.aovC, b.aaN);
     ++kernels;
     cudaEventRecord(c->ev[2], s);
-    uint32_t n = npix;
-    const uint32_t* queue = nullptr;
-    uint32_t* qs[2] = {q0, q1};
-    uint32_t* hostCount = static_cast<uint32_t*>(c->pinned);
-    for (; layer < maxIters && n > 0; ++layer) {
-      uint32_t* outQ = qs[layer & 1];
-      st = round(layer, n, queue, outQ);
-      if (st != UBR_OK) return st;
-      if (layer + 1 >= maxIters) {
-        ++layer;
-        break;
-      }
-      UBR_CUDA(c, cudaMemcpyAsync(hostCount, b.counter, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-      UBR_CUDA(c, cudaStreamSynchronize(s));
-      n = *hostCount;
-      queue = outQ;
-      if (progress) *progress = uint64_t(layer + 1);
-      if (cancel && *cancel) {
-        cancelled = true;
-        ++layer;
-        break;
-      }
-    }
+    st = adaptive ? runAdaptive() : runLayers(p1, b, R, nullptr, npix);
+    if (st != UBR_OK) return st;
     cudaEventRecord(c->ev[3], s);
     st = post();
     if (st != UBR_OK) return st;
@@ -1382,6 +1751,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     if (fr.view_z) UBR_CUDA(c, cudaMemcpyAsync(fr.view_z, b.viewZ + po, fpix * 4, kind, s));
     if (fr.hit_geom) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_geom, b.hitGeom + po, fpix * 4, kind, s));
     if (fr.hit_prim) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_prim, b.hitPrim + po, fpix * 4, kind, s));
+    if (fr.aa_mask && aaMaskOut) UBR_CUDA(c, cudaMemcpyAsync(fr.aa_mask, aaMaskOut, fout * 4, kind, s));
     if (p.aoWriteAov) {
       const float* o = outAov;
       const size_t n = nout;

@@ -51,6 +51,8 @@ struct HostScene {
   std::vector<uint32_t> mat[4];
   std::vector<uint8_t> fromEdge[4];
   std::vector<float> opacity1[4];
+  std::vector<uint16_t> group[4];     // CueMol section per primitive (primID order)
+  std::vector<uint16_t> triGroup;     // per base triangle
   std::vector<ubr_material> mats;
   uint32_t geomID[4] = {kInvalid, kInvalid, kInvalid, kInvalid};
   bool principled = false;
@@ -118,6 +120,7 @@ void flattenCylinders(const ubr_scene_desc& d, const std::vector<f3>& offs, Host
                                         d.cyl_color[4 * i + 2], d.cyl_color[4 * i + 3]));
     s.mat[kind].push_back(mt.get(d.cyl_material[i]));
     s.fromEdge[kind].push_back(d.cyl_from_edge && d.cyl_from_edge[i] ? 1 : 0);
+    s.group[kind].push_back(grp(i));
     s.opacity1[kind].push_back(op1(i));
   };
   if (!openIdx.empty()) {
@@ -283,6 +286,7 @@ ubr_status flatten(Context* c, const ubr_scene_desc& d, HostScene& s) {
       }
     }
     s.baseTri = uint32_t(baseT);
+    if (d.mesh_tri_group) s.triGroup.assign(d.mesh_tri_group, d.mesh_tri_group + baseT);
     s.meshMat = mt.get(d.mesh_material);
     if (d.mesh_tri_material) {
       std::vector<uint32_t> remap(d.mesh_material_count);
@@ -307,6 +311,7 @@ ubr_status flatten(Context* c, const ubr_scene_desc& d, HostScene& s) {
                                                d.sphere_color[4 * i + 2], d.sphere_color[4 * i + 3]));
         s.mat[kSphere].push_back(mt.get(d.sphere_material[i]));
         s.fromEdge[kSphere].push_back(d.sphere_from_edge && d.sphere_from_edge[i] ? 1 : 0);
+        s.group[kSphere].push_back(d.sphere_group ? d.sphere_group[i] : uint16_t(0));
       }
   }
   flattenCylinders(d, offs, s, mt);
@@ -1174,7 +1179,9 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
     if ((st = upload(c, sc, hs.mat[k], &v.primMat[k])) != UBR_OK) return fail(st);
     if ((st = upload(c, sc, hs.fromEdge[k], &v.primFromEdge[k])) != UBR_OK) return fail(st);
     if ((st = upload(c, sc, hs.opacity1[k], &v.primOpacity1[k])) != UBR_OK) return fail(st);
+    if ((st = upload(c, sc, hs.group[k], &v.primGroup[k])) != UBR_OK) return fail(st);
   }
+  if ((st = upload(c, sc, hs.triGroup, &v.meshTriGroup)) != UBR_OK) return fail(st);
   const auto tUp = std::chrono::steady_clock::now();
   if (n > 0) {
     BuildIn in{dpos, v.meshIdx, dsph, drcV, drcIdx, drcFl, dccV, dccIdx, nTri, nSph, nRc, nCc};

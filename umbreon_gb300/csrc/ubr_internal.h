@@ -120,6 +120,8 @@ struct DScene {
   const uint32_t* primMat[4] = {nullptr, nullptr, nullptr, nullptr};
   const uint8_t* primFromEdge[4] = {nullptr, nullptr, nullptr, nullptr};
   const float* primOpacity1[4] = {nullptr, nullptr, nullptr, nullptr};
+  const uint16_t* primGroup[4] = {nullptr, nullptr, nullptr, nullptr};  // CueMol section
+  const uint16_t* meshTriGroup = nullptr;  // per base triangle (or null: section 0)
   const float4* rcClip = nullptr;      // 2 per round segment (clipL, clipR)
   const float4* sph = nullptr;         // per sphere (centre, radius), primID order
   uint32_t baseSph = 0;                // spheres per instance (primID % baseSph = input sphere)
@@ -450,6 +452,8 @@ struct Params {
   float aoDistance, aoIntensity, aoFalloffPower;
   int aoMultiScale, aoBentNormal, aoMultibounce, aoLowDiscrepancy, aoEnhanced;
   int aoWriteAov;       // first-hit AO AOVs requested (AO rays trace nearest hits)
+  int aaMode;           // 1: adaptive AA (first-hit normal and section captured)
+  float aaThreshold;
   f3 aoSky, aoGround;
   float aoDiffuseFactor;
   int shadowsActive, shadowSamples;

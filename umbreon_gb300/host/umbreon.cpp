@@ -385,6 +385,9 @@ ubr_render_desc toRenderDesc(const Scene& s, const RenderOptions& o, std::vector
   d.max_transparent_layers = o.maxTransparentLayers;
   d.gi_integrator = o.giIntegrator;
   d.ao_write_aov = o.aoWriteAov ? 1u : 0u;
+  d.aa_mode = o.aaMode;
+  d.aa_threshold = o.aaThreshold;
+  d.aa_depth = o.aaDepth;
   return d;
 }
 
@@ -406,7 +409,6 @@ void rejectUnsupported(const Scene& scene, const RenderOptions& opt) {
 // One GPU pass: the work of renderFrame (pipeline.cpp:20-256) minus edges,
 // GI and denoise.
 FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderProgress* progress) {
-  if (opt.aaMode == 1) logMessage(LogLevel::Warning, "adaptive AA runs as full grid supersampling on the GPU");
   if (opt.aoResDiv > 1 || opt.aoResDiv < 0)
     logMessage(LogLevel::Warning, "coarse-grid AO runs as inline per-hit AO on the GPU");
   if (opt.denoiser != 0) logMessage(LogLevel::Warning, "the denoiser is not part of the GB300 path; skipped");
@@ -435,6 +437,11 @@ FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderP
   fr.color = f.color.data();
   fr.depth = f.depth.data();
   fr.view_z = f.viewZ.empty() ? nullptr : f.viewZ.data();
+  if (opt.aaMode == 1 && opt.aaDebug) {
+    // refinement mask at the output resolution (embree_renderer.cpp:1539)
+    f.aaMask.assign(nout, 0.0f);
+    fr.aa_mask = f.aaMask.data();
+  }
   if (opt.aoWriteAov) {
     // AO AOVs at the output resolution (allocateFrameBuffers neutral values;
     // renderFrame box-averages them with the colour)
