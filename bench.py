@@ -20,6 +20,7 @@ Multi-GPU: frames are independent, so N GPUs run N replicas of the frame
 from __future__ import annotations
 
 import argparse
+import copy
 import json
 import math
 import os
@@ -305,6 +306,7 @@ def secondary_workloads(args, flush):
     t0 = time.perf_counter()
     sc, opt = scenes.molecular_surface()
     gen_s = time.perf_counter() - t0
+    mol = (sc, opt)
     ctx, tn = tuned(sc, opt)
     b = ctx.build(sc)
     info = b.info()
@@ -317,6 +319,24 @@ def secondary_workloads(args, flush):
                                      "rays_per_frame": int(rays), "layers": int(layers), "phase_ms": ph,
                                      "cpu": cpu, "traversal": tn}
     ctx.close()
+    # adaptive AA (aaMode 1) against the full supersample grid on the
+    # ball-and-stick frame and on a molecular surface with mesh AO
+    for label, (sc, opt) in (("ball_and_stick_1920x1080_ss2", scenes.ball_and_stick()),
+                             ("molecular_surface_1024_ss2", _resized_ss(mol, 1024, 2))):
+        ctx, tn = tuned(sc, opt)
+        b = ctx.build(sc)
+        ms_g, rays_g, _, _ = _device_frames(ctx, b, sc, opt, 5, 3, flush)
+        ad = copy.copy(opt)
+        ad.aaMode = 1
+        ms_a, rays_a, ph_a, _ = _device_frames(ctx, b, sc, ad, 5, 3, flush)
+        dbg = copy.copy(ad)
+        dbg.aaDebug = True
+        flagged = float(ctx.render(b, sc, dbg, want_ids=False).aaMask.mean())
+        b.release()
+        ctx.close()
+        out["adaptive_aa_" + label] = {"grid_ms": round(ms_g, 3), "adaptive_ms": round(ms_a, 3),
+                                       "speedup": round(ms_g / ms_a, 2), "flagged_fraction": round(flagged, 4),
+                                       "grid_rays": int(rays_g), "adaptive_rays": int(rays_a)}
     # workload 4: forward frame vs adjoint (device buffers, L2 flushed)
     sc, opt = scenes.differentiable()
     ctx, tn = tuned(sc, opt)
@@ -396,10 +416,16 @@ def _knobs(args):
 
 
 def _resized(opt, res):
-    import copy
     o = copy.copy(opt)
     o.width = o.height = res
     return o
+
+
+def _resized_ss(scene_opt, res, ss):
+    sc, opt = scene_opt
+    o = _resized(opt, res)
+    o.supersample = ss
+    return sc, o
 
 
 def run_ours(args):

@@ -196,7 +196,9 @@ typedef struct ubr_render_desc {
    * 1 = adaptive AA (centre sample per output pixel, refinement mask,
    * flagged blocks shaded per subpixel, the others replicate a centre
    * re-shaded with ss^2 AO / soft-shadow samples); aaDepth above the
-   * supersample factor is not supported (UBR_INVALID_ARGUMENT) */
+   * supersample factor shades each flagged cell as the box average of
+   * ceil(aaDepth / ss)^2 samples of a finer lattice; other aa_mode values
+   * render the full grid */
   int32_t aa_mode;
   float aa_threshold;
   int32_t aa_depth;
@@ -347,8 +349,10 @@ ubr_status ubr_render(ubr_context* ctx, const ubr_scene* scene,
  * replayed from a CUDA graph.  Items may use different scenes, cameras,
  * resolutions and options; each item's outputs go to its own frame buffers.
  * `total` (may be NULL) receives the batch's statistics; its `flags` select
- * profiling as for ubr_render.  No reference counterpart (the reference
- * renders one frame per call). */
+ * profiling as for ubr_render.  Adaptive-AA items (aa_mode = 1 with
+ * supersample > 1 or aa_depth > 1) return UBR_INVALID_ARGUMENT: their passes
+ * depend on per-frame host decisions, so they go through ubr_render.  No
+ * reference counterpart (the reference renders one frame per call). */
 typedef struct ubr_batch_item {
   const ubr_scene* scene;
   const ubr_render_desc* desc;

@@ -47,8 +47,28 @@ def lib():
         L.oracle_occluded_filtered.restype = C.c_int
         L.oracle_occluded_filtered.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_float, C.c_float,
                                                C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_aa_mask.restype = C.c_int
+        L.oracle_aa_mask.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 5 + [C.c_float, C.c_float, C.c_int,
+                                                                              C.c_void_p]
         _L = L
     return _L
+
+
+def aa_mask(rgba, view_z, geom, group, normal, threshold=0.1, pixel_world_size=0.1, perspective=False):
+    """Adaptive-AA refinement mask (Hf, Wf) of hand-built centre records:
+    rgba (Hf, Wf, 4), view_z (Hf, Wf), geom / group (Hf, Wf), normal (Hf, Wf, 3)."""
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    Hf, Wf = rgba.shape[:2]
+    vz = np.ascontiguousarray(view_z, np.float32)
+    g = np.ascontiguousarray(geom, np.uint32)
+    gr = np.ascontiguousarray(group, np.int32)
+    nr = np.ascontiguousarray(normal, np.float32)
+    out = np.zeros((Hf, Wf), np.uint8)
+    st = lib().oracle_aa_mask(Wf, Hf, rgba.ctypes.data, vz.ctypes.data, g.ctypes.data, gr.ctypes.data,
+                              nr.ctypes.data, threshold, pixel_world_size, int(perspective), out.ctypes.data)
+    if st != 0:
+        raise ValueError("aa_mask: empty grid")
+    return out
 
 
 class OracleScene:

@@ -753,6 +753,84 @@ inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32
 
 using namespace oracle;
 
+// Centre record of one output pixel for the adaptive-AA mask: colour before
+// fog, view z, first-hit geomID / section (background: kInvalid / -1) and
+// shading normal (zero when the path leaves it unset).
+struct AaCentre {
+  float r, g, b, a, viewZ;
+  uint32_t geom;
+  int group;
+  V3 normal;
+};
+
+// aaPairNeedsRefine (adaptive_aa.hpp:65-111) with the default AaMaskParams
+// (normal delta 0.3, depth factor 3, absolute floor 12 output pixels).
+inline bool aaPairRefine(const AaCentre& a, const AaCentre& b, float za0, float zb1, float thr,
+                         float pixelWorldSize, bool persp) {
+  if (a.geom != b.geom || a.group != b.group) return true;
+  if (std::fabs(a.r - b.r) > thr || std::fabs(a.g - b.g) > thr || std::fabs(a.b - b.b) > thr ||
+      std::fabs(a.a - b.a) > thr)
+    return true;
+  if (a.geom == kInvalid || b.geom == kInvalid) return false;
+  const V3 na = a.normal, nb = b.normal;
+  const float la = na.x * na.x + na.y * na.y + na.z * na.z;
+  const float lb = nb.x * nb.x + nb.y * nb.y + nb.z * nb.z;
+  if (la > 0.0f && lb > 0.0f) {
+    const float dd = na.x * nb.x + na.y * nb.y + na.z * nb.z;
+    if (1.0f - dd > 0.3f) return true;
+  }
+  const float step = std::fabs(b.viewZ - a.viewZ);
+  const float sa = std::fabs(a.viewZ - za0);
+  const float sb = std::fabs(zb1 - b.viewZ);
+  const float slope = sa < sb ? sa : sb;
+  float absTerm = 12.0f * pixelWorldSize;
+  if (persp) {
+    const float zmin = std::fabs(a.viewZ) < std::fabs(b.viewZ) ? std::fabs(a.viewZ) : std::fabs(b.viewZ);
+    absTerm *= zmin;
+  }
+  const float th = 3.0f * slope > absTerm ? 3.0f * slope : absTerm;
+  return step > th;
+}
+
+// buildAaMask (adaptive_aa.hpp:121-161, edges mode off): horizontal then
+// vertical pairs with the outer view z (linear extrapolation at the border),
+// then dilateMask3x3 (:35-56).
+inline void buildAaMask(int Wf, int Hf, const AaCentre* c, float thr, float pixelWorldSize, bool persp,
+                        uint8_t* mask) {
+  auto at = [&](int x, int y) -> const AaCentre& { return c[static_cast<size_t>(y) * Wf + x]; };
+  std::vector<uint8_t> raw(static_cast<size_t>(Wf) * Hf, 0);
+  for (int y = 0; y < Hf; ++y)
+    for (int x = 0; x + 1 < Wf; ++x) {
+      const AaCentre &a = at(x, y), &b = at(x + 1, y);
+      const float za0 = x > 0 ? at(x - 1, y).viewZ : 2.0f * a.viewZ - b.viewZ;
+      const float zb1 = x + 2 < Wf ? at(x + 2, y).viewZ : 2.0f * b.viewZ - a.viewZ;
+      if (aaPairRefine(a, b, za0, zb1, thr, pixelWorldSize, persp))
+        raw[size_t(y) * Wf + x] = raw[size_t(y) * Wf + x + 1] = 1;
+    }
+  for (int y = 0; y + 1 < Hf; ++y)
+    for (int x = 0; x < Wf; ++x) {
+      const AaCentre &a = at(x, y), &b = at(x, y + 1);
+      const float za0 = y > 0 ? at(x, y - 1).viewZ : 2.0f * a.viewZ - b.viewZ;
+      const float zb1 = y + 2 < Hf ? at(x, y + 2).viewZ : 2.0f * b.viewZ - a.viewZ;
+      if (aaPairRefine(a, b, za0, zb1, thr, pixelWorldSize, persp))
+        raw[size_t(y) * Wf + x] = raw[size_t(y + 1) * Wf + x] = 1;
+    }
+  for (int y = 0; y < Hf; ++y)
+    for (int x = 0; x < Wf; ++x) {
+      uint8_t v = 0;
+      for (int dy = -1; dy <= 1 && !v; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int xx = x + dx, yy = y + dy;
+          if (xx < 0 || yy < 0 || xx >= Wf || yy >= Hf) continue;
+          if (raw[size_t(yy) * Wf + xx]) {
+            v = 1;
+            break;
+          }
+        }
+      mask[size_t(y) * Wf + x] = v;
+    }
+}
+
 extern "C" {
 
 void* oracle_scene_create(const ubr_scene_desc* d) {
@@ -860,6 +938,21 @@ int oracle_occluded_filtered(void* sp, const float* segs, uint64_t n, float eps,
 // hi-res grid, all rows when row1 <= row0), then pipeline.cpp:126-129 fog,
 // :182-192 box downsample, :254 assumed gamma.  `threads` <= 0 uses all cores.
 // Returns 0, or -1 for an unsupported request (Principled material).
+// The adaptive-AA mask of hand-built centre records (rgba 4, normal 3 floats
+// per output pixel): the predicates the reference's mask tests drive
+// (tests/test_adaptive_aa.cpp:233-316).
+int oracle_aa_mask(int Wf, int Hf, const float* rgba, const float* viewZ, const uint32_t* geom, const int32_t* group,
+                   const float* normal, float threshold, float pixelWorldSize, int perspective, uint8_t* mask) {
+  if (Wf <= 0 || Hf <= 0) return -1;
+  const size_t n = static_cast<size_t>(Wf) * Hf;
+  std::vector<AaCentre> c(n);
+  for (size_t i = 0; i < n; ++i)
+    c[i] = AaCentre{rgba[4 * i], rgba[4 * i + 1], rgba[4 * i + 2], rgba[4 * i + 3], viewZ[i], geom[i], group[i],
+                    V3{normal[3 * i], normal[3 * i + 1], normal[3 * i + 2]}};
+  buildAaMask(Wf, Hf, c.data(), threshold, pixelWorldSize, perspective != 0, mask);
+  return 0;
+}
+
 int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int threads, int row0,
                        int row1) {
   const Scene& s = *static_cast<Scene*>(sp);
@@ -1041,63 +1134,16 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
             integratePixel(c, org, rd, uint32_t(X * ss + cSub), uint32_t(Y * ss + cSub), dir);
       }
     });
-    // buildAaMask (adaptive_aa.hpp:64-180): 4-neighbour pair predicates, one dilation
-    const float thr = d.aa_threshold;
-    const bool persp = !d.cam_orthographic;
+    // buildAaMask (adaptive_aa.hpp:121-190) over the centre records
     const float pixelWorldSize = d.cam_orthographic ? (d.cam_height / static_cast<float>(Hf))
                                                     : (2.0f * persHalfH / static_cast<float>(Hf));
-    auto pairRefine = [&](const PixelOut& a, const PixelOut& b, float za0, float zb1) {
-      if (a.geom != b.geom || a.first.group != b.first.group) return true;
-      if (std::fabs(a.r - b.r) > thr || std::fabs(a.g - b.g) > thr || std::fabs(a.b - b.b) > thr ||
-          std::fabs(a.a - b.a) > thr)
-        return true;
-      if (a.geom == kInvalid || b.geom == kInvalid) return false;
-      const V3 na = a.first.normal, nb = b.first.normal;
-      const float la = na.x * na.x + na.y * na.y + na.z * na.z;
-      const float lb = nb.x * nb.x + nb.y * nb.y + nb.z * nb.z;
-      if (la > 0.0f && lb > 0.0f) {
-        const float dd = na.x * nb.x + na.y * nb.y + na.z * nb.z;
-        if (1.0f - dd > 0.3f) return true;
-      }
-      const float step = std::fabs(b.viewZ - a.viewZ);
-      const float sa = std::fabs(a.viewZ - za0);
-      const float sb = std::fabs(zb1 - b.viewZ);
-      const float slope = sa < sb ? sa : sb;
-      float absTerm = 12.0f * pixelWorldSize;
-      if (persp) {
-        const float zmin = std::fabs(a.viewZ) < std::fabs(b.viewZ) ? std::fabs(a.viewZ) : std::fabs(b.viewZ);
-        absTerm *= zmin;
-      }
-      const float th = 3.0f * slope > absTerm ? 3.0f * slope : absTerm;
-      return step > th;
-    };
-    auto at = [&](int x, int y) -> const PixelOut& { return centers[static_cast<size_t>(y) * Wf + x]; };
-    std::vector<uint8_t> raw(static_cast<size_t>(Wf) * Hf, 0), mask(raw.size(), 0);
-    for (int y = 0; y < Hf; ++y)
-      for (int x = 0; x + 1 < Wf; ++x) {
-        const PixelOut &a = at(x, y), &b = at(x + 1, y);
-        const float za0 = x > 0 ? at(x - 1, y).viewZ : 2.0f * a.viewZ - b.viewZ;
-        const float zb1 = x + 2 < Wf ? at(x + 2, y).viewZ : 2.0f * b.viewZ - a.viewZ;
-        if (pairRefine(a, b, za0, zb1)) raw[size_t(y) * Wf + x] = raw[size_t(y) * Wf + x + 1] = 1;
-      }
-    for (int y = 0; y + 1 < Hf; ++y)
-      for (int x = 0; x < Wf; ++x) {
-        const PixelOut &a = at(x, y), &b = at(x, y + 1);
-        const float za0 = y > 0 ? at(x, y - 1).viewZ : 2.0f * a.viewZ - b.viewZ;
-        const float zb1 = y + 2 < Hf ? at(x, y + 2).viewZ : 2.0f * b.viewZ - a.viewZ;
-        if (pairRefine(a, b, za0, zb1)) raw[size_t(y) * Wf + x] = raw[size_t(y + 1) * Wf + x] = 1;
-      }
-    for (int y = 0; y < Hf; ++y)
-      for (int x = 0; x < Wf; ++x) {
-        uint8_t v = 0;
-        for (int dy = -1; dy <= 1 && !v; ++dy)
-          for (int dx = -1; dx <= 1; ++dx) {
-            const int xx = x + dx, yy = y + dy;
-            if (xx < 0 || yy < 0 || xx >= Wf || yy >= Hf) continue;
-            if (raw[size_t(yy) * Wf + xx]) { v = 1; break; }
-          }
-        mask[size_t(y) * Wf + x] = v;
-      }
+    std::vector<AaCentre> rec(centers.size());
+    for (size_t i = 0; i < centers.size(); ++i) {
+      const PixelOut& po = centers[i];
+      rec[i] = AaCentre{po.r, po.g, po.b, po.a, po.viewZ, po.geom, po.first.group, po.first.normal};
+    }
+    std::vector<uint8_t> mask(centers.size(), 0);
+    buildAaMask(Wf, Hf, rec.data(), d.aa_threshold, pixelWorldSize, !d.cam_orthographic, mask.data());
     if (fr->aa_mask) for (size_t i = 0; i < mask.size(); ++i) fr->aa_mask[i] = float(mask[i]);
     // replication context: ss^2 AO and (stochastic) soft-shadow samples
     const bool soft = d.shadow_samples > 1 && d.light_radius_deg > 0.0f;

@@ -150,6 +150,24 @@ int main() {
                                                          near(f.avgHitDist[p], 2.0f, 1e-6f));
     c("colour unchanged by the AOVs", near(f.color[kC], plain.color[kC], 0.0f));
   }
+  {  // adaptive AA: a flat quad flags nothing and replicates its centres; the
+     // mask is returned at the output resolution only with aaDebug
+    umbreon::Scene sc;
+    sc.mesh = quad({0.5f, 0.6f, 0.7f, 1.0f});
+    sc.camera = cam();
+    sc.lights.push_back(key());
+    umbreon::RenderOptions o = o5();
+    o.supersample = 2;
+    const umbreon::FrameResult grid = umbreon::render(sc, o);
+    o.aaMode = 1;
+    c("no mask without aaDebug", umbreon::render(sc, o).aaMask.empty());
+    o.aaDebug = true;
+    const umbreon::FrameResult f = umbreon::render(sc, o);
+    bool none = f.aaMask.size() == 25;
+    for (float v : f.aaMask) none = none && v == 0.0f;
+    c("flat quad: mask of 25 zeros", none);
+    c("adaptive centre = grid colour", near(f.color[kC], grid.color[kC], 1e-6f));
+  }
   {  // unsupported requests throw like the reference's failures
     umbreon::Scene sc;
     sc.mesh = quad({1, 1, 1, 1});

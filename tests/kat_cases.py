@@ -302,6 +302,103 @@ def case_ao_determinism():
     return [(sc, o), (sc, o)], check
 
 
+# --- adaptive antialiasing (test_adaptive_aa.cpp:89-125 fixtures, :333-606) ---
+
+def _scene_x(x0, x1):
+    """Quad over [x0, x1] x [-2, 2] at z = 0 facing +Z, colour (0.5, 0.6,
+    0.7), material 0.2 / 0.8, the ortho rig, one 0.5 key light, background 0.1."""
+    pos = np.array([(x0, -2, 0), (x1, -2, 0), (x1, 2, 0), (x0, -2, 0), (x1, 2, 0), (x0, 2, 0)], np.float32)
+    sc = Scene(mesh_positions=pos, mesh_normals=np.tile([0, 0, 1], (6, 1)).astype(np.float32),
+               mesh_colors=np.tile(np.array([0.5, 0.6, 0.7, 1.0], np.float32), (6, 1)),
+               mesh_material=abi.material(ambient=0.2, diffuse=0.8))
+    sc.camera = scenes.ortho_cam()
+    sc.lights = [scenes.key_light()]
+    sc.background = (0.1, 0.1, 0.1)
+    return sc
+
+
+def _close(a, b, eps):
+    return a.color.shape == b.color.shape and float(np.abs(a.color - b.color).max()) <= eps
+
+
+def _equal(a, b):
+    return np.array_equal(a.color, b.color) and np.array_equal(a.depth, b.depth)
+
+
+def case_aa_uniform():
+    sc = _scene_x(-2.0, 2.0)
+    grid = RenderOptions(width=6, height=6, supersample=2)
+    adap = RenderOptions(width=6, height=6, supersample=2, aaMode=1)
+    def check(fs):
+        return [("uniform: adaptive == grid within 1e-6", _close(fs[0], fs[1], 1e-6)),
+                ("uniform: final size 6x6", fs[1].color.shape[:2] == (6, 6))]
+    return [(sc, grid), (sc, adap)], check
+
+
+def case_aa_silhouette():
+    sc = _scene_x(-2.0, 0.0)
+    grid = RenderOptions(width=9, height=9, supersample=3)
+    adap = RenderOptions(width=9, height=9, supersample=3, aaMode=1, aaDebug=True)
+    def check(fs):
+        a, b = fs
+        m = b.aaMask > 0
+        return [("silhouette: adaptive == grid within 1e-6", _close(a, b, 1e-6)),
+                ("silhouette: flagged pixels bitwise grid", m.any() and np.array_equal(a.color[m], b.color[m])),
+                ("mask sized 9x9", b.aaMask.shape == (9, 9)),
+                ("silhouette column 4 flagged", bool(np.all(b.aaMask[:, 4] > 0))),
+                ("far columns quiet", bool(np.all(b.aaMask[:, 0] == 0) and np.all(b.aaMask[:, 8] == 0)))]
+    return [(sc, grid), (sc, adap)], check
+
+
+def case_aa_determinism():
+    sc = _scene_x(-2.0, 0.0)
+    adap = RenderOptions(width=9, height=9, supersample=3, aaMode=1, aoSamples=8, aoDistance=100.0,
+                         shadows=True, shadowSamples=4, lightRadius=2.0)
+    def check(fs):
+        return [("adaptive + AO + soft shadows deterministic (bitwise)", _equal(fs[0], fs[1]))]
+    return [(sc, adap), (sc, adap)], check
+
+
+def case_aa_ao_compensation():
+    sc = _scene_x(-2.0, 2.0)
+    z = 0.4
+    slab = np.array([(0.2, -2, z), (4, -2, z), (4, 2, z), (0.2, -2, z), (4, 2, z), (0.2, 2, z)], np.float32)
+    sc.mesh_positions = np.concatenate([sc.mesh_positions, slab])
+    sc.mesh_normals = np.concatenate([sc.mesh_normals, np.tile([0, 0, -1], (6, 1)).astype(np.float32)])
+    sc.mesh_colors = np.concatenate([sc.mesh_colors, np.tile([0, 0, 0, 1], (6, 1)).astype(np.float32)])
+    sc.mesh_material = abi.material(ambient=1.0, diffuse=0.0)
+    sc.lights = []
+    grid = RenderOptions(width=8, height=8, supersample=2, aoSamples=16, aoDistance=100.0)
+    adap = RenderOptions(width=8, height=8, supersample=2, aoSamples=16, aoDistance=100.0, aaMode=1)
+    def check(fs):
+        a, b = fs[0].color[4, 6, 0], fs[1].color[4, 6, 0]
+        return [("AO compensation: unflagged pixel within 0.05 of the grid", abs(float(a) - float(b)) < 0.05)]
+    return [(sc, grid), (sc, adap)], check
+
+
+def case_aa_depth_equal_ss():
+    sc = _scene_x(-2.0, 0.0)
+    o1 = RenderOptions(width=9, height=9, supersample=3, aaMode=1)
+    o2 = RenderOptions(width=9, height=9, supersample=3, aaMode=1, aaDepth=3)
+    def check(fs):
+        return [("aa-depth == ss: bitwise aa-depth 0", _equal(fs[0], fs[1]))]
+    return [(sc, o1), (sc, o2)], check
+
+
+def case_aa_depth_ss1():
+    sc = _scene_x(-2.0, 0.0)
+    grid = RenderOptions(width=9, height=9)
+    adap = RenderOptions(width=9, height=9, aaMode=1, aaDepth=2, aaDebug=True)
+    def check(fs):
+        a, b = fs
+        m = b.aaMask > 0
+        same = (a.color == b.color).all(-1)
+        return [("aa-depth ss=1: mask 9x9", b.aaMask.shape == (9, 9)),
+                ("aa-depth ss=1: unflagged bitwise 1-sample grid", bool(np.all(same[~m]))),
+                ("aa-depth ss=1: some flagged pixels refined", bool(np.any(~same[m])))]
+    return [(sc, grid), (sc, adap)], check
+
+
 CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
 
 
