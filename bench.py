@@ -313,6 +313,7 @@ def secondary_workloads(args, flush):
     ms, rays, ph, layers = _device_frames(ctx, b, sc, opt, 3, 3, flush)
     b.release()
     cpu = _cpu_full_or_band(sc, opt, threads, 4.0) if not args.no_cpu else None
+    mol_knobs = tn
     out["molecular_surface_2048"] = {"triangles": int(info["prim_count"][0]), "spheres": int(info["prim_count"][1]),
                                      "bvh_build_ms": round(info["build_ms"], 1), "generate_s": round(gen_s, 1),
                                      "ms_per_frame": round(ms, 3), "Mrays_s": round(rays / ms / 1e3, 1),
@@ -337,6 +338,25 @@ def secondary_workloads(args, flush):
         out["adaptive_aa_" + label] = {"grid_ms": round(ms_g, 3), "adaptive_ms": round(ms_a, 3),
                                        "speedup": round(ms_g / ms_a, 2), "flagged_fraction": round(flagged, 4),
                                        "grid_rays": int(rays_g), "adaptive_rays": int(rays_a)}
+    # coarse-grid AO (aoResDiv 2: one AO gather per 2x2 block of first hits,
+    # interpolated, own rays where the guides reject) against AO rays at
+    # every hit, on the molecular surface frame
+    sc, opt = mol
+    ctx = Context(0, **mol_knobs)
+    b = ctx.build(sc)
+    ms_i, rays_i, _, _ = _device_frames(ctx, b, sc, opt, 3, 2, flush)
+    co = copy.copy(opt)
+    co.aoResDiv = 2
+    ms_c, rays_c, ph_c, _ = _device_frames(ctx, b, sc, co, 3, 2, flush)
+    dbg = copy.copy(co)
+    dbg.aoResDebug = True
+    patched = float(ctx.render(b, sc, dbg, want_ids=False).aoPatchMask.mean())
+    b.release()
+    ctx.close()
+    out["coarse_ao_molecular_surface_2048"] = {"inline_ms": round(ms_i, 3), "coarse_div2_ms": round(ms_c, 3),
+                                               "speedup": round(ms_i / ms_c, 2), "rays_inline": int(rays_i),
+                                               "rays_coarse": int(rays_c), "patched_first_hits": round(patched, 4),
+                                               "coarse_phase_ms": ph_c}
     # workload 4: forward frame vs adjoint (device buffers, L2 flushed)
     sc, opt = scenes.differentiable()
     ctx, tn = tuned(sc, opt)
@@ -444,7 +464,8 @@ def run_ours(args):
         opt.width, opt.height = (int(x) for x in args.frame.lower().split("x"))
     if args.ss:
         opt.supersample = args.ss
-    # traversal knobs: as given, else what the autotuner picks on a downscaled frame
+    # traversal knobs: as given, else what the autotuner picks (downscaled sweep,
+    # finalists re-timed on the full frame)
     tune = None
     knobs = _knobs(args)
     if knobs is None:
@@ -579,7 +600,8 @@ def run_ours(args):
                        "frame": f"{opt.width}x{opt.height} ss{opt.supersample}",
                        "primitives": info["prim_count"], "bvh_nodes": info["bvh_nodes"],
                        "l2": "flushed (256 MB write) before every timed frame",
-                       "traversal": dict(knobs, autotuned=tune["table"] if tune else None),
+                       "traversal": dict(knobs, autotuned=tune["table"] if tune else None,
+                                         finalists_full_frame_ms=tune["finalists_full_frame_ms"] if tune else None),
                        "parallelism": f"replicas x{ws}"},
             "ms_per_frame": round(ms_frame, 3),
             "phase_ms_per_frame": {n: round(v / args.steps, 3) for n, v in zip(names, phase)},

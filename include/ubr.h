@@ -202,6 +202,12 @@ typedef struct ubr_render_desc {
   int32_t aa_mode;
   float aa_threshold;
   int32_t aa_depth;
+  /* RenderOptions::aoResDiv (render_options.hpp:64-74): > 1 gathers the AO
+   * once per cell of the hi-res grid divided by this factor (on the first
+   * hits of that coarse grid) and lets each shaded hit interpolate it with
+   * normal / depth guides, falling back to its own AO rays where the guides
+   * reject; -1 = the supersample factor; 0 or 1 = AO rays at every hit */
+  int32_t ao_res_div;
 } ubr_render_desc;
 
 /* Where a frame's buffers live. */
@@ -264,6 +270,10 @@ typedef struct ubr_frame {
   /* adaptive AA refinement mask, output resolution, 1 = refined
    * (FrameResult::aaMask with aaDebug); written when aa_mode = 1 */
   float* aa_mask;
+  /* coarse-grid AO fallback mask, hi-res, 1 = the first hit gathered its own
+   * AO (FrameResult::aoPatchMask with aoResDebug); written when the coarse
+   * grid is active */
+  float* ao_patch_mask;
 } ubr_frame;
 
 /* Context: one GPU, one CUDA stream, one device arena.  Scenes and frame

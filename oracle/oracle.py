@@ -47,11 +47,33 @@ def lib():
         L.oracle_occluded_filtered.restype = C.c_int
         L.oracle_occluded_filtered.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_float, C.c_float,
                                                C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_coarse_ao_lookup.restype = C.c_int
+        L.oracle_coarse_ao_lookup.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 8 + [
+            C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_void_p, C.c_float, C.c_void_p]
         L.oracle_aa_mask.restype = C.c_int
         L.oracle_aa_mask.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 5 + [C.c_float, C.c_float, C.c_int,
                                                                               C.c_void_p]
         _L = L
     return _L
+
+
+def coarse_ao_lookup(openness, normal, depth, hit, lattice, px, py, N, z, bent=None, contact=None, shape=None,
+                     avg=None):
+    """One coarse-grid AO lookup on a hand-built (h, w) grid; returns None when
+    the guides reject, else (openness, bent (3,), contact, shape, avgHitDist)."""
+    op = np.ascontiguousarray(openness, np.float32)
+    h, w = op.shape
+    arrs = [op, np.ascontiguousarray(normal, np.float32), np.ascontiguousarray(depth, np.float32),
+            np.ascontiguousarray(hit, np.uint8)]
+    q = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (bent, contact, shape, avg)]
+    n = np.ascontiguousarray(N, np.float32)
+    out = np.zeros(7, np.float32)
+    ok = lib().oracle_coarse_ao_lookup(w, h, *[a.ctypes.data for a in arrs],
+                                       *[None if a is None else a.ctypes.data for a in q],
+                                       lattice[0], lattice[1], px, py, n.ctypes.data, z, out.ctypes.data)
+    if not ok:
+        return None
+    return float(out[0]), out[1:4].copy(), float(out[4]), float(out[5]), float(out[6])
 
 
 def aa_mask(rgba, view_z, geom, group, normal, threshold=0.1, pixel_world_size=0.1, perspective=False):

@@ -579,14 +579,100 @@ inline V3 shadeLocal(const Scene& s, const Mat& mat, const V3& C, const V3& N, c
   return out;
 }
 
+// ao/ao_coarse.hpp:55-66 CoarseAoGrid: AO gathered once per coarse cell plus
+// the lookup guides (shading normal, primary hit distance, eligibility).
+struct CoarseAo {
+  int w = 0, h = 0;
+  bool quality = false;  // bent / contact / shape / avgHitDist gathered
+  std::vector<float> openness, bent, contact, shape, avgHitDist, normal, depth;
+  std::vector<uint8_t> hit;
+};
+
 struct Ctx {
   const Scene* s;
   std::vector<Light> lights;
   V3 ambLight, bg, aoUp;
   Opt o;
-  int wHi;
+  int wHi;  // seed lattice width (hi-res width; W k on a fine lattice)
   float clipNear, clipFar;
+  const CoarseAo* coarse = nullptr;  // coarse-grid AO when active
+  int frameW = 0, frameH = 0;        // hi-res frame size (lookup lattice height)
 };
+
+// ao/ao_coarse.hpp:152-203 sampleCoarseAo: bilinear x normal^32 x depth
+// weights over the 2x2 surrounding cells, rejected below a weight sum of 0.3.
+inline bool sampleCoarseAo(const CoarseAo& g, int latW, int latH, uint32_t px, uint32_t py, const V3& N, float z,
+                           float& openness, AOResult& aov) {
+  if (g.w <= 0 || g.h <= 0) return false;
+  const float sx = (static_cast<float>(px) + 0.5f) * static_cast<float>(g.w) / static_cast<float>(latW) - 0.5f;
+  const float sy = (static_cast<float>(py) + 0.5f) * static_cast<float>(g.h) / static_cast<float>(latH) - 0.5f;
+  const int bx = static_cast<int>(std::floor(sx));
+  const int by = static_cast<int>(std::floor(sy));
+  const float fx = sx - static_cast<float>(bx);
+  const float fy = sy - static_cast<float>(by);
+  float wSum = 0.0f, opSum = 0.0f, contactSum = 0.0f, shapeSum = 0.0f, ahdSum = 0.0f;
+  V3 bentSum{0.0f, 0.0f, 0.0f};
+  for (int dy = 0; dy < 2; ++dy) {
+    const int cy = by + dy;
+    if (cy < 0 || cy >= g.h) continue;
+    for (int dx = 0; dx < 2; ++dx) {
+      const int cx = bx + dx;
+      if (cx < 0 || cx >= g.w) continue;
+      const size_t cp = static_cast<size_t>(cy) * g.w + cx;
+      if (!g.hit[cp]) continue;
+      const float wb = (dx ? fx : 1.0f - fx) * (dy ? fy : 1.0f - fy);
+      const V3 Nc{g.normal[cp * 3], g.normal[cp * 3 + 1], g.normal[cp * 3 + 2]};
+      const float nd = dot(N, Nc);
+      if (nd <= 0.0f) continue;
+      const float wn = std::pow(nd, 32.0f);
+      const float zc = g.depth[cp];
+      const float wz = std::exp(-std::fabs(z - zc) / (0.02f * z + 1e-6f));
+      const float wgt = wb * wn * wz;
+      if (wgt <= 0.0f) continue;
+      wSum += wgt;
+      opSum += wgt * g.openness[cp];
+      if (g.quality) {
+        bentSum.x += wgt * g.bent[cp * 3];
+        bentSum.y += wgt * g.bent[cp * 3 + 1];
+        bentSum.z += wgt * g.bent[cp * 3 + 2];
+        contactSum += wgt * g.contact[cp];
+        shapeSum += wgt * g.shape[cp];
+        ahdSum += wgt * g.avgHitDist[cp];
+      }
+    }
+  }
+  if (wSum < 0.3f) return false;
+  const float inv = 1.0f / wSum;
+  openness = opSum * inv;
+  aov = AOResult{};
+  aov.openness = openness;
+  if (g.quality) {
+    aov.bent = safeNormalize(V3{bentSum.x * inv, bentSum.y * inv, bentSum.z * inv}, N);
+    aov.contact = contactSum * inv;
+    aov.shape = shapeSum * inv;
+    aov.avgHitDist = ahdSum * inv;
+  }
+  return true;
+}
+
+// hit_shader.hpp:129-145 aoShadeForHit: the coarse-grid lookup first (the hit
+// is its own guide: N and its primary-ray distance), else the exact inline
+// gather with the unchanged seeds, marking the hit as patched.
+inline AoShade aoShadeForHit(const Ctx& c, const V3& P, const V3& Ng, const V3& N, const V3& C, float secEps,
+                             float hitT, uint32_t px, uint32_t py, uint8_t* patched, AOResult* aovOut = nullptr) {
+  if (c.coarse != nullptr && c.o.aoSamples > 0) {
+    const int latW = c.wHi;
+    const int latH = static_cast<int>(static_cast<int64_t>(latW) * c.frameH / c.frameW);
+    float openness;
+    AOResult aov;
+    if (sampleCoarseAo(*c.coarse, latW, latH, px, py, N, hitT, openness, aov)) {
+      if (aovOut) *aovOut = aov;
+      return aoApplyFactors(c.o, c.ambLight, c.aoUp, openness, aov, C);
+    }
+    if (patched) *patched = 1;
+  }
+  return computeAoShade(*c.s, c.o, c.ambLight, c.aoUp, P, Ng, N, C, secEps, px, py, c.wHi, aovOut);
+}
 
 struct HitShade {
   V3 color;
@@ -595,6 +681,7 @@ struct HitShade {
   V3 albedo{0.0f, 0.0f, 0.0f}, normal{0.0f, 0.0f, 0.0f}, bent{0.0f, 0.0f, 0.0f};
   float contact = 1.0f, shape = 1.0f, avgHit = 0.0f;
   int group = 0;  // CueMol section of the hit (hit_shader.hpp:277, 457)
+  uint8_t aoPatched = 0;  // coarse-grid AO fell back to the inline gather (hit_shader.hpp:60)
 };
 
 // hit_shader.hpp:147-496 shadeHit (POV; GI / edge / principled branches off)
@@ -623,7 +710,7 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
     const size_t bt = s.baseTri ? hit.primID % s.baseTri : 0;
     const Mat& triMat = s.triMat.empty() ? s.meshMat : s.meshMats[s.triMat[bt]];
     AOResult aov;
-    AoShade ao = computeAoShade(s, c.o, c.ambLight, c.aoUp, P, Ng, N, C, secEps, px, py, c.wHi, &aov);
+    AoShade ao = aoShadeForHit(c, P, Ng, N, C, secEps, hit.t, px, py, &hs.aoPatched, &aov);
     hs.color = shadeLocal(s, triMat, C, N, V, c.lights, ao.ambLight, c.bg, c.o.specularScale, ao.aoFactor,
                           ao.diffuseAo, P, Ng, secEps, shadowsActive, c.o.shadowSamples, px, py);
     hs.opacity = cbuf[3];
@@ -649,7 +736,7 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
     V3 ambLight = c.ambLight;
     float diffuseAo = 1.0f;
     if (!fromEdge) {
-      AoShade ao = computeAoShade(s, c.o, c.ambLight, c.aoUp, P, Ng, N, C, secEps, px, py, c.wHi);
+      AoShade ao = aoShadeForHit(c, P, Ng, N, C, secEps, hit.t, px, py, &hs.aoPatched);
       aoFactor = ao.aoFactor;
       ambLight = ao.ambLight;
       diffuseAo = ao.diffuseAo;
@@ -938,6 +1025,37 @@ int oracle_occluded_filtered(void* sp, const float* segs, uint64_t n, float eps,
 // hi-res grid, all rows when row1 <= row0), then pipeline.cpp:126-129 fog,
 // :182-192 box downsample, :254 assumed gamma.  `threads` <= 0 uses all cores.
 // Returns 0, or -1 for an unsupported request (Principled material).
+// One coarse-grid AO lookup on a hand-built grid (the unit cases of the
+// reference's tests/test_ao_coarse.cpp:97-204): returns 1 and fills out[0..6]
+// = openness, bent.xyz, contact, shape, avgHitDist when accepted, 0 when the
+// guides reject.  bent / contact / shape / avg may be NULL (legacy grid).
+int oracle_coarse_ao_lookup(int w, int h, const float* openness, const float* normal, const float* depth,
+                            const uint8_t* hit, const float* bent, const float* contact, const float* shape,
+                            const float* avg, int latW, int latH, uint32_t px, uint32_t py, const float* N, float z,
+                            float* out) {
+  CoarseAo g;
+  const size_t n = static_cast<size_t>(w) * h;
+  g.w = w;
+  g.h = h;
+  g.openness.assign(openness, openness + n);
+  g.normal.assign(normal, normal + 3 * n);
+  g.depth.assign(depth, depth + n);
+  g.hit.assign(hit, hit + n);
+  g.quality = bent != nullptr;
+  if (g.quality) {
+    g.bent.assign(bent, bent + 3 * n);
+    g.contact.assign(contact, contact + n);
+    g.shape.assign(shape, shape + n);
+    g.avgHitDist.assign(avg, avg + n);
+  }
+  float op = 0.0f;
+  AOResult aov;
+  if (!sampleCoarseAo(g, latW, latH, px, py, V3{N[0], N[1], N[2]}, z, op, aov)) return 0;
+  const float r[7] = {op, aov.bent.x, aov.bent.y, aov.bent.z, aov.contact, aov.shape, aov.avgHitDist};
+  for (int k = 0; k < 7; ++k) out[k] = r[k];
+  return 1;
+}
+
 // The adaptive-AA mask of hand-built centre records (rgba 4, normal 3 floats
 // per output pixel): the predicates the reference's mask tests drive
 // (tests/test_adaptive_aa.cpp:233-316).
@@ -1025,6 +1143,8 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   c.bg = V3{d.background[0], d.background[1], d.background[2]};
   c.aoUp = d.ao_use_camera_up ? trueUp : safeNormalize(V3{d.ao_up[0], d.ao_up[1], d.ao_up[2]}, trueUp);
   c.wHi = W;
+  c.frameW = W;
+  c.frameH = H;
   c.clipNear = d.clip_near;
   c.clipFar = d.clip_far;
 
@@ -1040,12 +1160,14 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   }
   if (row1 <= row0) { row0 = 0; row1 = H; }
   // storePixelResult (embree_renderer.cpp:213-250): one hi-res sample
+  float* patchMask = nullptr;  // set once the coarse AO grid is active
   auto store = [&](size_t pix, const PixelOut& po) {
     color[4 * pix] = po.r; color[4 * pix + 1] = po.g; color[4 * pix + 2] = po.b; color[4 * pix + 3] = po.a;
     depth[pix] = po.depth;
     viewZ[pix] = po.viewZ;
     hg[pix] = po.geom;
     hp[pix] = po.prim;
+    if (patchMask) patchMask[pix] = static_cast<float>(po.first.aoPatched);
     if (aov) {
       const HitShade& f = po.first;
       const float a3[3][3] = {{f.albedo.x, f.albedo.y, f.albedo.z}, {f.normal.x, f.normal.y, f.normal.z},
@@ -1073,6 +1195,111 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
     }
   };
   auto rayAt = [&](int px, int py, V3& org, V3& rd) { rayAtL(px, py, W, H, org, rd); };
+  int nThreads = threads > 0 ? threads : static_cast<int>(std::thread::hardware_concurrency());
+  if (nThreads < 1) nThreads = 1;
+  auto parallelRange = [&](int n, const std::function<void(int)>& fn) {
+    std::atomic<int> next{0};
+    auto w = [&]() {
+      for (int y = next.fetch_add(1); y < n; y = next.fetch_add(1)) fn(y);
+    };
+    std::vector<std::thread> pool;
+    for (int i = 1; i < nThreads; ++i) pool.emplace_back(w);
+    w();
+    for (auto& th : pool) th.join();
+  };
+  // Coarse-grid AO pre-pass (embree_renderer.cpp:527-553; pipeline.cpp:68
+  // resolves -1 to the supersample factor): the first-hit G-buffer of a
+  // ceil(W / div) x ceil(H / div) grid (pt1_gbuffer.hpp:83-196, no clip
+  // range, mesh hits and non-outline primitives eligible) and one AO gather
+  // per eligible cell seeded on the coarse lattice (ao_coarse.hpp:73-140).
+  CoarseAo coarse;
+  {
+    const int div = d.ao_res_div < 0 ? ss : d.ao_res_div;
+    bool eligible = !s.geo.triIdx.empty();
+    for (int k = 1; k < 4 && !eligible; ++k)
+      for (uint8_t fe : s.fromEdge[k])
+        if (!fe) {
+          eligible = true;
+          break;
+        }
+    if (div > 1 && d.ao_samples > 0 && eligible) {
+      const int hw = (W + div - 1) / div, hh = (H + div - 1) / div;
+      const size_t nc = static_cast<size_t>(hw) * hh;
+      coarse.w = hw;
+      coarse.h = hh;
+      coarse.quality = c.o.aoEnhanced() || c.o.aoWriteAov;
+      coarse.openness.assign(nc, 1.0f);
+      coarse.normal.assign(nc * 3, 0.0f);
+      coarse.depth.assign(nc, 0.0f);
+      coarse.hit.assign(nc, 0);
+      if (coarse.quality) {
+        coarse.bent.assign(nc * 3, 0.0f);
+        coarse.contact.assign(nc, 1.0f);
+        coarse.shape.assign(nc, 1.0f);
+        coarse.avgHitDist.assign(nc, 0.0f);
+      }
+      parallelRange(hh, [&](int cy) {
+        for (int cx = 0; cx < hw; ++cx) {
+          V3 org, rd;
+          rayAtL(cx, cy, hw, hh, org, rd);
+          Ray r;
+          r.org = org; r.dir = rd; r.tnear = 0.0f; r.tfar = kInf;
+          Hit h;
+          if (!s.bvh.closest(r, h)) continue;
+          const int kind = kindOfGeom(s, h.geomID);
+          V3 N, Ng;
+          if (kind == kMesh) {
+            const uint32_t* tri = &s.geo.triIdx[3 * h.primID];
+            const float w0 = 1.0f - h.u - h.v;
+            float nb[3];
+            for (int k = 0; k < 3; ++k)
+              nb[k] = w0 * s.nrm[3 * tri[0] + k] + h.u * s.nrm[3 * tri[1] + k] + h.v * s.nrm[3 * tri[2] + k];
+            N = safeNormalize(V3{nb[0], nb[1], nb[2]});
+            Ng = safeNormalize(h.Ng);
+          } else {
+            if (s.fromEdge[kind][h.primID]) continue;
+            N = safeNormalize(h.Ng);
+            Ng = N;
+          }
+          if (dot(N, rd) > 0.0f) N = V3{-N.x, -N.y, -N.z};
+          if (dot(Ng, rd) > 0.0f) Ng = V3{-Ng.x, -Ng.y, -Ng.z};
+          const size_t cp = static_cast<size_t>(cy) * hw + cx;
+          const V3 P{org.x + rd.x * h.t, org.y + rd.y * h.t, org.z + rd.z * h.t};
+          const float secEps = selfIntersectEps(P, N, h.t);
+          AOResult aov;
+          float op;
+          if (c.o.aoEnhanced()) {
+            aov = computeAOQuality(s, P, Ng, N, secEps, c.o.aoSamples, c.o.aoDistance, c.o.aoFalloffPower,
+                                   c.o.aoMultiScale, c.o.aoLowDiscrepancy, uint32_t(cx), uint32_t(cy), hw);
+            op = aov.openness;
+          } else {
+            op = computeAO(s, P, Ng, N, secEps, c.o.aoSamples, c.o.aoDistance, uint32_t(cx), uint32_t(cy), hw);
+            if (c.o.aoWriteAov)
+              aov = computeAOQuality(s, P, Ng, N, secEps, c.o.aoSamples, c.o.aoDistance, 0.0f, false, false,
+                                     uint32_t(cx), uint32_t(cy), hw);
+          }
+          coarse.openness[cp] = op;
+          coarse.normal[cp * 3] = N.x;
+          coarse.normal[cp * 3 + 1] = N.y;
+          coarse.normal[cp * 3 + 2] = N.z;
+          coarse.depth[cp] = h.t;
+          coarse.hit[cp] = 1;
+          if (coarse.quality) {
+            coarse.bent[cp * 3] = aov.bent.x;
+            coarse.bent[cp * 3 + 1] = aov.bent.y;
+            coarse.bent[cp * 3 + 2] = aov.bent.z;
+            coarse.contact[cp] = aov.contact;
+            coarse.shape[cp] = aov.shape;
+            coarse.avgHitDist[cp] = aov.avgHitDist;
+          }
+        }
+      });
+      c.coarse = &coarse;
+      patchMask = fr->ao_patch_mask;
+      if (patchMask) std::fill(patchMask, patchMask + npix, 0.0f);
+    }
+  }
+  const bool coarseOn = c.coarse != nullptr;
   // Adaptive AA (embree_renderer.cpp:1379-1670, render/adaptive_aa.hpp):
   // centre sample per output pixel, refinement mask, flagged blocks shaded
   // per subpixel, the others replicate a centre re-shaded with ss^2 AO and
@@ -1147,9 +1374,9 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
     if (fr->aa_mask) for (size_t i = 0; i < mask.size(); ++i) fr->aa_mask[i] = float(mask[i]);
     // replication context: ss^2 AO and (stochastic) soft-shadow samples
     const bool soft = d.shadow_samples > 1 && d.light_radius_deg > 0.0f;
-    const bool needBoost = ss > 1 && (d.ao_samples > 0 || soft);
+    const bool needBoost = ss > 1 && ((d.ao_samples > 0 && !coarseOn) || soft);
     Ctx cb = c;
-    cb.o.aoSamples = c.o.aoSamples * ss * ss;
+    cb.o.aoSamples = c.o.aoSamples * (coarseOn ? 1 : ss * ss);
     cb.o.shadowSamples = c.o.shadowSamples * (soft ? ss * ss : 1);
     parallelRows(Hf, [&](int Y) {
       for (int X = 0; X < Wf; ++X) {

@@ -399,6 +399,99 @@ def case_aa_depth_ss1():
     return [(sc, grid), (sc, adap)], check
 
 
+# --- coarse-grid AO (test_ao_coarse.cpp:40-76 rig, :210-384) ---
+
+def ao_coarse_scene(slab=True):
+    """Ambient-only white floor with a black slab over the +x half, the ortho
+    rig, no lights, background 0.1."""
+    pos = [(-2, -2, 0), (2, -2, 0), (2, 2, 0), (-2, -2, 0), (2, 2, 0), (-2, 2, 0)]
+    nrm = [(0, 0, 1)] * 6
+    col = [(1, 1, 1, 1)] * 6
+    if slab:
+        z = 0.4
+        pos += [(0.2, -2, z), (4, -2, z), (4, 2, z), (0.2, -2, z), (4, 2, z), (0.2, 2, z)]
+        nrm += [(0, 0, -1)] * 6
+        col += [(0, 0, 0, 1)] * 6
+    sc = Scene(mesh_positions=np.array(pos, np.float32), mesh_normals=np.array(nrm, np.float32),
+               mesh_colors=np.array(col, np.float32), mesh_material=abi.material(ambient=1.0, diffuse=0.0))
+    sc.camera = scenes.ortho_cam()
+    sc.lights = []
+    sc.background = (0.1, 0.1, 0.1)
+    return sc
+
+
+def _with(opt, **kw):
+    o = RenderOptions(**{k: getattr(opt, k) for k in opt.__dataclass_fields__})
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def case_ao_coarse_inline_neutrality():
+    sc = ao_coarse_scene()
+    o0 = RenderOptions(width=8, height=8, supersample=2, aoSamples=16, aoDistance=100.0)
+    e0 = _with(o0, aoMultiScale=True, aoMultibounce=True)
+    def check(fs):
+        return [("legacy: div 0 == div 1 bitwise", np.array_equal(fs[0].color, fs[1].color)),
+                ("enhanced: div 0 == div 1 bitwise", np.array_equal(fs[2].color, fs[3].color))]
+    return [(sc, o0), (sc, _with(o0, aoResDiv=1)), (sc, e0), (sc, _with(e0, aoResDiv=1))], check
+
+
+def case_ao_coarse_close_to_inline():
+    sc = ao_coarse_scene()
+    full = RenderOptions(width=16, height=16, supersample=3, aoSamples=256, aoDistance=100.0, aoLowDiscrepancy=True)
+    f32 = _with(full, aoSamples=32, aoLowDiscrepancy=False)
+    def check(fs):
+        return [("coarse vs inline within 0.05 (256 spp + LD)", _close(fs[0], fs[1], 0.05)),
+                ("coarse vs inline mean |diff| < 0.02 (32 spp)",
+                 float(np.mean(np.abs(fs[2].color - fs[3].color))) < 0.02)]
+    return [(sc, full), (sc, _with(full, aoResDiv=-1)), (sc, f32), (sc, _with(f32, aoResDiv=-1))], check
+
+
+def case_ao_coarse_fallback_exact():
+    sc = ao_coarse_scene()
+    full = RenderOptions(width=24, height=24, aoSamples=16, aoDistance=100.0)
+    def check(fs):
+        a, b = fs
+        ok = b.aoPatchMask is not None and b.aoPatchMask.shape == (24, 24)
+        m = b.aoPatchMask > 0 if ok else None
+        return [("patch mask at render resolution", ok),
+                ("patch mask fires somewhere, not everywhere", ok and 0 < int(m.sum()) < 24 * 24),
+                ("patched pixels bitwise the inline render", ok and np.array_equal(a.color[m], b.color[m]))]
+    return [(sc, full), (sc, _with(full, aoResDiv=2, aoResDebug=True))], check
+
+
+def case_ao_coarse_determinism():
+    sc = ao_coarse_scene()
+    o = RenderOptions(width=12, height=12, supersample=2, aoSamples=16, aoDistance=100.0, aoResDiv=-1)
+    def check(fs):
+        return [("coarse AO deterministic (bitwise)", np.array_equal(fs[0].color, fs[1].color))]
+    return [(sc, o), (sc, o)], check
+
+
+def case_ao_coarse_adaptive():
+    sc = ao_coarse_scene()
+    g = RenderOptions(width=12, height=12, supersample=3, aoSamples=16, aoDistance=100.0, aoResDiv=-1)
+    a = _with(g, aaMode=1)
+    def check(fs):
+        return [("adaptive + coarse deterministic", np.array_equal(fs[1].color, fs[2].color)),
+                ("adaptive + coarse within 0.05 of grid + coarse", _close(fs[0], fs[1], 0.05))]
+    return [(sc, g), (sc, a), (sc, a)], check
+
+
+def case_ao_coarse_transparency():
+    sc = ao_coarse_scene()
+    z = 1.0
+    shell = np.array([(-2, -2, z), (2, -2, z), (2, 2, z), (-2, -2, z), (2, 2, z), (-2, 2, z)], np.float32)
+    sc.mesh_positions = np.concatenate([sc.mesh_positions, shell])
+    sc.mesh_normals = np.concatenate([sc.mesh_normals, np.tile([0, 0, 1], (6, 1)).astype(np.float32)])
+    sc.mesh_colors = np.concatenate([sc.mesh_colors, np.tile([0.5, 0.7, 0.9, 0.4], (6, 1)).astype(np.float32)])
+    full = RenderOptions(width=12, height=12, supersample=2, aoSamples=16, aoDistance=100.0)
+    def check(fs):
+        return [("transparent shell: coarse within 0.05 of inline", _close(fs[0], fs[1], 0.05))]
+    return [(sc, full), (sc, _with(full, aoResDiv=-1))], check
+
+
 CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
 
 

@@ -104,7 +104,7 @@ class RenderDesc(C.Structure):
         ("env_angle", C.c_float), ("specular_scale", C.c_float), ("transparency", C.c_uint32),
         ("transparent_background", C.c_uint32), ("max_transparent_layers", C.c_int32),
         ("gi_integrator", C.c_int32), ("ao_write_aov", C.c_uint32), ("aa_mode", C.c_int32),
-        ("aa_threshold", C.c_float), ("aa_depth", C.c_int32),
+        ("aa_threshold", C.c_float), ("aa_depth", C.c_int32), ("ao_res_div", C.c_int32),
     ]
 
 
@@ -117,7 +117,7 @@ class Frame(C.Structure):
         ("layers", C.c_uint32), ("kernels", C.c_uint32), ("phase_ms", C.c_double * 5),
         ("node_bytes", C.c_uint64 * 2), ("prim_bytes", C.c_uint64 * 2), ("nodes_visited", C.c_uint64 * 2),
         ("albedo", f32p), ("normal", f32p), ("bent_normal", f32p), ("contact_ao", f32p), ("shape_ao", f32p),
-        ("avg_hit_dist", f32p), ("aa_mask", f32p),
+        ("avg_hit_dist", f32p), ("aa_mask", f32p), ("ao_patch_mask", f32p),
     ]
 
 

@@ -213,6 +213,8 @@ class RenderOptions:
     aaThreshold: float = 0.1
     aaDepth: int = 0
     aaDebug: bool = False
+    aoResDiv: int = 0        # coarse-grid AO divisor (-1 = supersample factor; 0 / 1 = per hit)
+    aoResDebug: bool = False  # return the coarse-AO fallback mask
 
     def aoEnhanced(self) -> bool:
         return (self.aoFalloffPower > 0.0 or self.aoMultiScale or self.aoBentNormal or self.aoMultibounce
@@ -278,6 +280,7 @@ def make_render_desc(scene: Scene, opt: RenderOptions):
     d.gi_integrator = opt.giIntegrator
     d.ao_write_aov = int(opt.aoWriteAov)
     d.aa_mode, d.aa_threshold, d.aa_depth = opt.aaMode, opt.aaThreshold, opt.aaDepth
+    d.ao_res_div = opt.aoResDiv
     return d, keep
 
 
@@ -301,6 +304,7 @@ class FrameResult:
     shapeAo: np.ndarray = None     # (H, W)
     avgHitDist: np.ndarray = None  # (H, W)
     aaMask: np.ndarray = None      # (H, W) adaptive-AA refinement mask (aaDebug)
+    aoPatchMask: np.ndarray = None  # (Hss, Wss) coarse-AO fallback mask (aoResDebug)
 
 
 AOV_FIELDS = (("albedo", "albedo", 3), ("normal", "normal", 3), ("bentNormal", "bent_normal", 3),
@@ -309,8 +313,14 @@ AOV_FIELDS = (("albedo", "albedo", 3), ("normal", "normal", 3), ("bentNormal", "
 
 def attach_aovs(fr, opt) -> dict:
     """Allocate the AO AOV planes of a frame when opt.aoWriteAov asks for
-    them, and the adaptive-AA mask when opt.aaDebug does."""
+    them, the adaptive-AA mask when opt.aaDebug does, and the coarse-AO
+    fallback mask when opt.aoResDebug does."""
     out = {}
+    ss = max(1, opt.supersample)
+    div = ss if opt.aoResDiv < 0 else opt.aoResDiv
+    if opt.aoResDebug and div > 1 and opt.aoSamples > 0:
+        out["aoPatchMask"] = np.zeros((opt.height * ss, opt.width * ss), np.float32)
+        fr.ao_patch_mask = abi.ptr(out["aoPatchMask"])
     if opt.aaMode == 1 and opt.aaDebug:
         out["aaMask"] = np.zeros((opt.height, opt.width), np.float32)
         fr.aa_mask = abi.ptr(out["aaMask"])

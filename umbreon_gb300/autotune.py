@@ -2,7 +2,8 @@
 
 Times a representative frame (downscaled to about `pixels` hi-res pixels, so
 tuning costs a second or two) for every candidate setting of the context
-tuning fields and returns the fastest:
+tuning fields, re-times the best few on the full frame, and returns the
+fastest:
 
 * BVH builder: Morton radix tree or PLOC clustering over the same order;
 * 8-wide collapse: greedy with a fixed leaf size (1..3 primitives), or the
@@ -30,8 +31,19 @@ TREES = (
 )
 
 
+def _time(fields, scene, opt, device, repeats, key="total_ms"):
+    ctx = Context(device, **fields)
+    built = ctx.build(scene)
+    try:
+        ctx.render(built, scene, opt, want_ids=False)  # warm-up (graph capture)
+        return min(ctx.render(built, scene, opt, want_ids=False).stats[key] for _ in range(repeats))
+    finally:
+        built.release()
+        ctx.close()
+
+
 def autotune(scene, opt, device: int = 0, pixels: int = 256 * 256, repeats: int = 3,
-             builders=(1, 2), trees=TREES, trace_modes=(1, 2, 3)):
+             builders=(1, 2), trees=TREES, trace_modes=(1, 2, 3), finalists: int = 3):
     small = copy.copy(opt)
     ss = max(1, opt.supersample)
     scale = math.sqrt(pixels / float(opt.width * opt.height * ss * ss))
@@ -40,21 +52,21 @@ def autotune(scene, opt, device: int = 0, pixels: int = 256 * 256, repeats: int 
         small.height = max(16, int(opt.height * scale))
     results = {}
     for builder, (tlabel, tfields) in itertools.product(builders, trees):
-        # one scene build per tree; the occlusion kernel is a render-time choice
         for mode in trace_modes:
             fields = dict(tfields, bvh_builder=builder, trace_mode=mode)
-            ctx = Context(device, **fields)
-            built = ctx.build(scene)
-            try:
-                ctx.render(built, scene, small, want_ids=False)  # warm-up (graph capture)
-                best = min(ctx.render(built, scene, small, want_ids=False).stats["total_ms"]
-                           for _ in range(repeats))
-            finally:
-                built.release()
-                ctx.close()
-            results[(builder, tlabel, mode)] = (best, fields)
-    (builder, tlabel, mode), (ms, fields) = min(results.items(), key=lambda kv: kv[1][0])
+            results[(builder, tlabel, mode)] = (_time(fields, scene, small, device, repeats), fields)
+    ranked = sorted(results.items(), key=lambda kv: kv[1][0])
+    final = {}
+    if scale < 1.0 and finalists > 1:
+        # candidates within a few per cent on the small frame can swap order
+        # at full size: re-time the best few on the real frame
+        for key, (_, fields) in ranked[:finalists]:
+            final[key] = (_time(fields, scene, opt, device, repeats, key="render_ms"), fields)
+        (builder, tlabel, mode), (ms, fields) = min(final.items(), key=lambda kv: kv[1][0])
+    else:
+        (builder, tlabel, mode), (ms, fields) = ranked[0]
     return {"context": fields, "bvh_builder": builder, "tree": tlabel, "trace_mode": mode, "ms": ms,
             "bvh_leaf_max": fields.get("bvh_leaf_max", 0), "bvh_collapse": fields["bvh_collapse"],
             "sah_prim_scale": fields.get("sah_prim_scale", 0.0),
-            "table": {f"builder{b}_{t}_mode{m}": round(v[0], 4) for (b, t, m), v in results.items()}}
+            "table": {f"builder{b}_{t}_mode{m}": round(v[0], 4) for (b, t, m), v in results.items()},
+            "finalists_full_frame_ms": {f"builder{b}_{t}_mode{m}": round(v[0], 4) for (b, t, m), v in final.items()}}

@@ -54,6 +54,11 @@ struct Bufs {
   float4* aovC;       //   bent normal.xyz, mean occluder distance
   float4* aaN;        // per hi-res pixel (adaptive AA, or null): first-hit normal.xyz, section (int bits)
   const uint32_t* coord;  // fine-lattice pass (or null): lattice index of each pixel slot
+  const float4* cgN;      // coarse AO grid (or null): shading normal.xyz, primary hit distance
+  const float4* cgQ;      //   openness, contact, shape, mean occluder distance
+  const float4* cgB;      //   bent normal.xyz (quality estimator only, else null)
+  const uint8_t* cgHit;   //   1 = AO-eligible first hit
+  float* aoPatch;         // per hi-res pixel (or null): 1 = the first hit gathered its own AO
   const LightD* lights;
   unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
   uint32_t* counter;  // [0] next-queue size, [1] occlusion work-queue size
@@ -64,6 +69,68 @@ struct Bufs {
 // Lattice index of pixel slot gpix: the slot itself, or its entry in the
 // coordinate table of a fine-lattice pass.
 UBR_D uint32_t latticeOf(const Bufs& b, uint32_t gpix) { return b.coord ? __ldg(&b.coord[gpix]) : gpix; }
+
+// AO of a coarse grid cell or of an interpolated lookup: openness and the
+// quality-estimator channels (neutral when not gathered).
+struct AoQ {
+  float openness = 1.0f, contact = 1.0f, shape = 1.0f, avgHit = 0.0f;
+  f3 bent{0.0f, 0.0f, 0.0f};
+};
+
+// sampleCoarseAo (ao/ao_coarse.hpp:152-203): the hit at lattice point
+// (px, py) of the p.W x p.H lattice, with shading normal N and primary-ray
+// distance z, blends the 2x2 surrounding coarse cells with bilinear x
+// (N.Nc)^32 x exp(-|z - zc| / (0.02 z + 1e-6)) weights; rejected (false)
+// below a weight sum of 0.3.
+UBR_D bool coarseAoLookup(const Params& p, const Bufs& b, int px, int py, f3 N, float z, AoQ& q) {
+  const float sx = (float(px) + 0.5f) * float(p.cgW) / float(p.W) - 0.5f;
+  const float sy = (float(py) + 0.5f) * float(p.cgH) / float(p.H) - 0.5f;
+  const int bx = int(floorf(sx)), by = int(floorf(sy));
+  const float fx = sx - float(bx), fy = sy - float(by);
+  float wSum = 0.0f, opSum = 0.0f, contactSum = 0.0f, shapeSum = 0.0f, ahdSum = 0.0f;
+  f3 bentSum{0.0f, 0.0f, 0.0f};
+  for (int dy = 0; dy < 2; ++dy) {
+    const int cy = by + dy;
+    if (cy < 0 || cy >= p.cgH) continue;
+    for (int dx = 0; dx < 2; ++dx) {
+      const int cx = bx + dx;
+      if (cx < 0 || cx >= p.cgW) continue;
+      const uint32_t cp = uint32_t(cy) * uint32_t(p.cgW) + uint32_t(cx);
+      if (!__ldg(&b.cgHit[cp])) continue;
+      const float wb = (dx ? fx : 1.0f - fx) * (dy ? fy : 1.0f - fy);
+      const float4 nz = __ldg(&b.cgN[cp]);
+      const float nd = dot(N, f3{nz.x, nz.y, nz.z});
+      if (nd <= 0.0f) continue;
+      const float wn = powf(nd, 32.0f);
+      const float wz = expf(-fabsf(z - nz.w) / (0.02f * z + 1e-6f));
+      const float wgt = wb * wn * wz;
+      if (wgt <= 0.0f) continue;
+      const float4 cq = __ldg(&b.cgQ[cp]);
+      wSum += wgt;
+      opSum += wgt * cq.x;
+      if (b.cgB) {
+        const float4 cb = __ldg(&b.cgB[cp]);
+        bentSum.x += wgt * cb.x;
+        bentSum.y += wgt * cb.y;
+        bentSum.z += wgt * cb.z;
+        contactSum += wgt * cq.y;
+        shapeSum += wgt * cq.z;
+        ahdSum += wgt * cq.w;
+      }
+    }
+  }
+  if (wSum < 0.3f) return false;
+  const float inv = 1.0f / wSum;
+  q = AoQ{};
+  q.openness = opSum * inv;
+  if (b.cgB) {
+    q.bent = safeNormalize(f3{bentSum.x * inv, bentSum.y * inv, bentSum.z * inv}, N);
+    q.contact = contactSum * inv;
+    q.shape = shapeSum * inv;
+    q.avgHit = ahdSum * inv;
+  }
+  return true;
+}
 
 // Per-frame record of a batched launch (device array): the frame's
 // parameters and scene, and where its pixels start in the batch's global
@@ -157,9 +224,16 @@ __global__ void __launch_bounds__(128) k_surface(Params p1, DScene s1, Batch bt,
       f3 ng = dot(sf.Ng, sf.N) < 0.0f ? neg(sf.Ng) : sf.Ng;
       ng = safeNormalize(ng, sf.N);
       const f3 O = sf.P + ng * sf.secEps;
+      // coarse-grid AO: a hit the grid lookup accepts casts no AO rays
+      // (hit_shader.hpp:129-145)
+      bool aoCast = sf.aoOn;
+      if (aoCast && p.aoCoarse) {
+        AoQ q;
+        if (coarseAoLookup(p, b, px, py, sf.N, ha.x, q)) aoCast = false;
+      }
       // subtree that holds everything the hit's AO rays can meet
       int start = 0;
-      if (sf.aoOn) {
+      if (aoCast) {
         f3 lo, hi;
         aoBox(O, p.aoDistance, lo, hi);
         start = boxStartNode(travOf(s), lo, hi);
@@ -167,7 +241,7 @@ __global__ void __launch_bounds__(128) k_surface(Params p1, DScene s1, Batch bt,
       b.surfA[i] = make_float4(O.x, O.y, O.z, sf.secEps);
       b.surfB[i] = make_float4(sf.N.x, sf.N.y, sf.N.z, __int_as_float(start));
       // flags: 1 hit, 2 casts AO, 4 casts shadows; bits 8.. the frame index
-      const uint32_t flags = 1u | (sf.aoOn ? 2u : 0u) | (sf.shOn ? 4u : 0u) | (uint32_t(f) << 8);
+      const uint32_t flags = 1u | (aoCast ? 2u : 0u) | (sf.shOn ? 4u : 0u) | (uint32_t(f) << 8);
       b.surfC[i] = make_uint2(gpix, flags);
       cast = (flags & 6u) != 0u;
     }
@@ -441,10 +515,6 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion_persistent(Params p1
 // (ambient_occlusion.hpp:171-267), sample order preserved: the openness for
 // the enhanced estimator and the contact / shape / bent-normal / mean
 // occluder distance AOVs.
-struct AoQ {
-  float openness = 1.0f, contact = 1.0f, shape = 1.0f, avgHit = 0.0f;
-  f3 bent{0.0f, 0.0f, 0.0f};
-};
 UBR_D AoQ aoQuality(const Params& p, const float* aoT, uint64_t aoStride, uint32_t i, f3 N, int px, int py,
                     float power, bool multiScale) {
   const float R = p.aoDistance;
@@ -542,10 +612,19 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
       float diffuseAo = 1.0f;
       const uint64_t rb = uint64_t(i) * R;
       AoQ aq;  // AOVs of this hit (neutral unless computed)
+      bool patched = false;
       if (sf.aoOn) {
         float openness;
         f3 bent = sf.N;
-        if (!p.aoEnhanced) {
+        AoQ cq;
+        const bool coarse = p.aoCoarse && coarseAoLookup(p, b, px, py, sf.N, ha.x, cq);
+        patched = p.aoCoarse && !coarse;
+        if (coarse) {
+          // interpolated grid values (legacy grids leave the AOV defaults)
+          aq = cq;
+          openness = cq.openness;
+          bent = cq.bent;
+        } else if (!p.aoEnhanced) {
           int hits = 0;
           for (int k = 0; k < p.aoSamples; ++k) hits += b.occ[rb + k];
           openness = 1.0f - float(hits) / float(p.aoSamples);
@@ -663,6 +742,7 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
           }
           b.aaN[gpix] = make_float4(sf.N.x, sf.N.y, sf.N.z, __int_as_float(grp));
         }
+        if (b.aoPatch) b.aoPatch[gpix] = patched ? 1.0f : 0.0f;
         b.depth[gpix] = t;
         b.viewZ[gpix] = t * dot(rd, p.camDir);
         b.hitGeom[gpix] = s.geomID[sf.kind];
@@ -778,11 +858,13 @@ __global__ void k_post(Params p1, Batch bt, uint32_t nOut, const float4* colorHi
 // First-hit state of a pixel before its primary ray (all pixels, or the
 // pixels of a list when `list` is set).
 __global__ void k_init_pixels(uint32_t npix, float* depth, float* viewZ, uint32_t* hg, uint32_t* hp, float4* aovA,
-                              float4* aovB, float4* aovC, float4* aaN = nullptr, const uint32_t* list = nullptr) {
+                              float4* aovB, float4* aovC, float4* aaN = nullptr, const uint32_t* list = nullptr,
+                              float* aoPatch = nullptr) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= npix) return;
   const uint32_t i = list ? list[k] : k;
   if (aaN) aaN[i] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+  if (aoPatch) aoPatch[i] = 0.0f;
   depth[i] = 0.0f;
   viewZ[i] = 0.0f;
   hg[i] = kInvalid;
@@ -957,7 +1039,7 @@ __global__ void k_aa_lists(AaGrid g, const uint8_t* raw, uint32_t* flagged, uint
 // unflagged blocks: the centre's first-hit state and colour to every subpixel
 __global__ void k_aa_replicate(AaGrid g, const uint32_t* centres, const uint32_t* counts, float4* color,
                                float* depth, float* viewZ, uint32_t* hg, uint32_t* hp, float4* aovA, float4* aovB,
-                               float4* aovC) {
+                               float4* aovC, float* aoPatch) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= counts[1]) return;
   const uint32_t c = centres[k];
@@ -966,6 +1048,7 @@ __global__ void k_aa_replicate(AaGrid g, const uint32_t* centres, const uint32_t
   const float4 col = color[c];
   const float d = depth[c], z = viewZ[c];
   const uint32_t gi = hg[c], pi = hp[c];
+  const float patch = aoPatch ? aoPatch[c] : 0.0f;
   float4 a = make_float4(0, 0, 0, 0), b2 = a, c3 = a;
   if (aovA) {
     a = aovA[c];
@@ -981,6 +1064,7 @@ __global__ void k_aa_replicate(AaGrid g, const uint32_t* centres, const uint32_t
       viewZ[t] = z;
       hg[t] = gi;
       hp[t] = pi;
+      if (aoPatch) aoPatch[t] = patch;
       if (aovA) {
         aovA[t] = a;
         aovB[t] = b2;
@@ -1028,11 +1112,105 @@ __global__ void k_aa_fine_reduce(const uint32_t* cells, uint32_t cell0, uint32_t
   b.viewZ[c] = z * inv;
   b.hitGeom[c] = fine.hitGeom[s0];
   b.hitPrim[c] = fine.hitPrim[s0];
+  if (b.aoPatch) b.aoPatch[c] = fine.aoPatch[s0];
   if (b.aovA) {
     b.aovA[c] = fine.aovA[s0];
     b.aovB[c] = fine.aovB[s0];
     b.aovC[c] = fine.aovC[s0];
   }
+}
+
+// ---- Coarse-grid AO pre-pass (embree_renderer.cpp:527-553) ----
+// The first-hit G-buffer of the coarse grid (pt1_gbuffer.hpp:83-196: primary
+// rays through the cell centres of the same camera plane, no clip range; mesh
+// hits with the interpolated normal, non-outline primitives with the
+// geometric one, both turned toward the viewer) and, per eligible cell, the
+// surface record of its AO gather (ao_coarse.hpp:73-140: epsilon from the hit
+// distance with N in place of the ray direction).  `pc` is the frame's
+// parameters with W x H = the coarse grid, so AO seeds live on that lattice.
+template <bool COUNT, int KM, bool BATCH>
+__global__ void __launch_bounds__(128) k_cao_trace(Params pc, DScene s, Bufs b, float4* cgN, uint8_t* cgHit) {
+  const uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nc = uint32_t(pc.W) * uint32_t(pc.H);
+  bool cast = false;
+  if (cell < nc) {
+    const int cx = int(cell % uint32_t(pc.W)), cy = int(cell / uint32_t(pc.W));
+    f3 org, rd;
+    primaryRay(pc, cx, cy, org, rd);
+    Ray r{org, rd, 0.0f, kInfF};
+    Hit h;
+    uint32_t ovf = 0;
+    Count cnt;
+    traverse<false, KM>(travOf(s), r, h, ovf, &cnt, false);
+    uint8_t eligible = 0;
+    f3 N{0.0f, 0.0f, 0.0f}, Ng{0.0f, 0.0f, 0.0f};
+    if (h.ref != kInvalid) {
+      const int kind = refKind(h.ref);
+      const uint32_t prim = refPrim(h.ref);
+      if (kind == kMesh) {
+        const uint32_t i0 = __ldg(&s.meshIdx[3 * prim]), i1 = __ldg(&s.meshIdx[3 * prim + 1]),
+                       i2 = __ldg(&s.meshIdx[3 * prim + 2]);
+        const float w0 = 1.0f - h.u - h.v;
+        float nb[3];
+        for (int k = 0; k < 3; ++k)
+          nb[k] = w0 * __ldg(&s.meshNrm[3 * i0 + k]) + h.u * __ldg(&s.meshNrm[3 * i1 + k]) +
+                  h.v * __ldg(&s.meshNrm[3 * i2 + k]);
+        N = safeNormalize(f3{nb[0], nb[1], nb[2]});
+        Ng = safeNormalize(h.Ng);
+        eligible = 1;
+      } else if (!__ldg(&s.primFromEdge[kind][prim])) {
+        N = safeNormalize(h.Ng);
+        Ng = N;
+        eligible = 1;
+      }
+    }
+    cgHit[cell] = eligible;
+    if (eligible) {
+      if (dot(N, rd) > 0.0f) N = neg(N);
+      if (dot(Ng, rd) > 0.0f) Ng = neg(Ng);
+      const float t = h.t;
+      cgN[cell] = make_float4(N.x, N.y, N.z, t);
+      const f3 P{org.x + rd.x * t, org.y + rd.y * t, org.z + rd.z * t};
+      const float eps = selfIntersectEps(P, N, t);
+      f3 ng = dot(Ng, N) < 0.0f ? neg(Ng) : Ng;
+      ng = safeNormalize(ng, N);
+      const f3 O = P + ng * eps;
+      f3 lo, hi;
+      aoBox(O, pc.aoDistance, lo, hi);
+      const int start = boxStartNode(travOf(s), lo, hi);
+      b.surfA[cell] = make_float4(O.x, O.y, O.z, eps);
+      b.surfB[cell] = make_float4(N.x, N.y, N.z, __int_as_float(start));
+      b.surfC[cell] = make_uint2(cell, 3u);
+      cast = true;
+    }
+  }
+  int off;
+  const int qb = warpPushBase(cast, b.counter + 1, off);
+  if (cast) b.occQueue[qb + off] = cell;
+}
+
+// Per eligible cell, the AO estimate from its rays (aoGather,
+// ao_shade.hpp:44-72): binary openness, or the quality estimator when AO is
+// enhanced; with AOVs requested the legacy openness plus a single-scale
+// quality pass.
+__global__ void k_cao_finish(Params pc, Bufs b, const uint8_t* cgHit, float4* cgQ, float4* cgB) {
+  const uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= uint32_t(pc.W) * uint32_t(pc.H) || !cgHit[cell]) return;
+  const int cx = int(cell % uint32_t(pc.W)), cy = int(cell / uint32_t(pc.W));
+  const uint64_t n = uint64_t(pc.aoSamples);
+  const f3 N = ld3(b.surfB[cell]);
+  AoQ q;
+  if (!pc.aoEnhanced) {
+    int hits = 0;
+    for (uint64_t k = 0; k < n; ++k) hits += b.occ[uint64_t(cell) * n + k];
+    const float openness = 1.0f - float(hits) / float(pc.aoSamples);
+    if (pc.aoWriteAov) q = aoQuality(pc, b.aoT, n, cell, N, cx, cy, 0.0f, false);
+    q.openness = openness;
+  } else {
+    q = aoQuality(pc, b.aoT, n, cell, N, cx, cy, pc.aoFalloffPower, pc.aoMultiScale != 0);
+  }
+  cgQ[cell] = make_float4(q.openness, q.contact, q.shape, q.avgHit);
+  if (cgB) cgB[cell] = make_float4(q.bent.x, q.bent.y, q.bent.z, 0.0f);
 }
 
 }  // namespace
@@ -1417,6 +1595,48 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     b.aovC = scratchT<float4>(c, 72, npix, st);
     outAov = scratchT<float>(c, 73, size_t(nout) * 12, st);
   }
+  // coarse-grid AO (one frame per call; pipeline.cpp:68 resolves -1 to ss;
+  // embree_renderer.cpp:531 needs AO and a mesh or a non-outline primitive)
+  if (batch)
+    for (size_t f = 0; f < nf; ++f) {
+      const int dv = jobs[f].desc->ao_res_div < 0 ? fds[f].p.ss : jobs[f].desc->ao_res_div;
+      if (dv > 1 && fds[f].p.aoSamples > 0)
+        return setError(c, UBR_INVALID_ARGUMENT, "render batch: coarse-grid AO renders one frame per call");
+    }
+  Params pCoarse{};
+  bool coarseOn = false;
+  uint32_t nCell = 0;
+  float4 *cgN = nullptr, *cgQ = nullptr, *cgB = nullptr;
+  uint8_t* cgHit = nullptr;
+  if (!batch) {
+    const int div = d0.ao_res_div < 0 ? p1.ss : d0.ao_res_div;
+    if (div > 1 && p1.aoSamples > 0 && jobs[0].scene->aoReceivers) {
+      coarseOn = true;
+      Params& pm = fds[0].p;
+      pm.aoCoarse = 1;
+      pm.cgW = (p1.W + div - 1) / div;
+      pm.cgH = (p1.H + div - 1) / div;
+      nCell = uint32_t(pm.cgW) * uint32_t(pm.cgH);
+      cgN = scratchT<float4>(c, 92, nCell, st);
+      cgQ = scratchT<float4>(c, 93, nCell, st);
+      cgHit = scratchT<uint8_t>(c, 94, nCell, st);
+      if (p1.aoEnhanced || p1.aoWriteAov) cgB = scratchT<float4>(c, 95, nCell, st);
+      if (jobs[0].frame->ao_patch_mask) b.aoPatch = scratchT<float>(c, 96, npix, st);
+      b.cgN = cgN;
+      b.cgQ = cgQ;
+      b.cgB = cgB;
+      b.cgHit = cgHit;
+      // the coarse lattice: AO rays only, seeds on the grid
+      pCoarse = p1;
+      pCoarse.aoCoarse = 0;
+      pCoarse.W = p1.cgW;
+      pCoarse.H = p1.cgH;
+      pCoarse.raysPerHit = p1.aoSamples;
+      pCoarse.shadowRays = 0;
+      pCoarse.shadowsActive = 0;
+      pCoarse.nLights = 0;
+    }
+  }
   const uint32_t nCentre = uint32_t(p1.outW) * uint32_t(p1.outH);
   uint32_t *aaList0 = nullptr, *aaList1 = nullptr, *aaCounts = nullptr;
   uint8_t* aaRaw = nullptr;
@@ -1439,13 +1659,16 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     // replication context (embree_renderer.cpp:1592-1608): ss^2 AO samples,
     // ss^2 soft-shadow samples when shadows are stochastic
     const bool soft = d0.shadow_samples > 1 && d0.light_radius_deg > 0.0f;
-    needBoost = ss > 1 && (d0.ao_samples > 0 || soft);
+    needBoost = ss > 1 && ((d0.ao_samples > 0 && !coarseOn) || soft);
     if (needBoost) {
       ubr_render_desc db = d0;
-      db.ao_samples = d0.ao_samples * ss * ss;
+      if (!coarseOn) db.ao_samples = d0.ao_samples * ss * ss;  // the grid is smooth already
       if (soft) db.shadow_samples = d0.shadow_samples * ss * ss;
       st = makeParams(c, db, pBoost, lightsBoost);
       if (st != UBR_OK) return st;
+      pBoost.aoCoarse = p1.aoCoarse;
+      pBoost.cgW = p1.cgW;
+      pBoost.cgH = p1.cgH;
       dlBoost = scratchT<LightD>(c, 80, lightsBoost.size() + 1, st);
     }
     if (kFine > 1) {
@@ -1466,6 +1689,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       bFine.hitPrim = scratchT<uint32_t>(c, 87, fineCap, st);
       fineCoord = scratchT<uint32_t>(c, 88, fineCap, st);
       bFine.coord = fineCoord;
+      bFine.aoPatch = b.aoPatch ? scratchT<float>(c, 97, fineCap, st) : nullptr;
       if (aov) {
         bFine.aovA = scratchT<float4>(c, 89, fineCap, st);
         bFine.aovB = scratchT<float4>(c, 90, fineCap, st);
@@ -1545,6 +1769,33 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     else k_shade<false><<<grid, TB, 0, s>>>(pr, s1, bt, br, layer, n, queue, outQ);
     mark(3, false);
     ++kernels;
+    UBR_CUDA(c, cudaGetLastError());
+    return UBR_OK;
+  };
+  // coarse-grid AO pre-pass: G-buffer + AO rays of the grid cells, then the
+  // per-cell estimate (device-only, so graph capture keeps it)
+  auto coarsePrepass = [&]() -> ubr_status {
+    if (!coarseOn) return UBR_OK;
+    UBR_CUDA(c, cudaMemsetAsync(b.counter, 0, 2 * sizeof(uint32_t), s));
+    const uint32_t grid = (nCell + TB - 1) / TB;
+    mark(1, true);
+    UBR_KM_DISPATCH(k_cao_trace, km, false, false, grid, TB, s, pCoarse, s1, b, cgN, cgHit);
+    mark(1, false);
+    const uint64_t nr = uint64_t(nCell) * uint64_t(pCoarse.raysPerHit);
+    mark(2, true);
+    if (c->traceMode == 1) {
+      launchOcclusion(km, count, false, uint32_t((nr + TB - 1) / TB), TB, s, pCoarse, s1, bt, b, nCell);
+    } else if (c->traceMode == 3) {
+      launchOcclusionGridStride(km, count, false, gridStrideGrid(c->device), TB, s, pCoarse, s1, bt, b);
+    } else {
+      UBR_CUDA(c, cudaMemsetAsync(b.cursor, 0, sizeof(unsigned long long), s));
+      launchOcclusionPersistent(km, count, false, persistentGrid(c->device), TB, s, pCoarse, s1, bt, b);
+    }
+    mark(2, false);
+    mark(3, true);
+    k_cao_finish<<<(nCell + 255) / 256, 256, 0, s>>>(pCoarse, b, cgHit, cgQ, cgB);
+    mark(3, false);
+    kernels += 3;
     UBR_CUDA(c, cudaGetLastError());
     return UBR_OK;
   };
@@ -1645,7 +1896,8 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
         const uint32_t nc = std::min(cellsPerChunk, nFlagged - cell0), n = nc * k2;
         k_aa_fine_coords<<<(n + 255) / 256, 256, 0, s>>>(g, aaList1, cell0, n, kFine, fineCoord);
         k_init_pixels<<<(n + 255) / 256, 256, 0, s>>>(n, bFine.depth, bFine.viewZ, bFine.hitGeom, bFine.hitPrim,
-                                                      bFine.aovA, bFine.aovB, bFine.aovC);
+                                                      bFine.aovA, bFine.aovB, bFine.aovC, nullptr, nullptr,
+                                                      bFine.aoPatch);
         kernels += 2;
         rs = runLayers(pFine, bFine, R, nullptr, n);
         if (rs != UBR_OK || cancelled) return rs;
@@ -1655,7 +1907,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     }
     if (needBoost && nCentres > 0) {
       k_init_pixels<<<(nCentres + 255) / 256, 256, 0, s>>>(nCentres, b.depth, b.viewZ, b.hitGeom, b.hitPrim,
-                                                           b.aovA, b.aovB, b.aovC, b.aaN, aaList0);
+                                                           b.aovA, b.aovB, b.aovC, b.aaN, aaList0, b.aoPatch);
       ++kernels;
       Bufs bb = b;
       bb.lights = dlBoost;
@@ -1664,7 +1916,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     }
     if (nCentres > 0) {
       k_aa_replicate<<<(nCentres + 255) / 256, 256, 0, s>>>(g, aaList0, aaCounts, b.colorHi, b.depth, b.viewZ,
-                                                            b.hitGeom, b.hitPrim, b.aovA, b.aovB, b.aovC);
+                                                            b.hitGeom, b.hitPrim, b.aovA, b.aovB, b.aovC, b.aoPatch);
       ++kernels;
     }
     UBR_CUDA(c, cudaGetLastError());
@@ -1690,8 +1942,9 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       UBR_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s);
       k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim, b.aovA,
-                                                       b.aovB, b.aovC);
-      ubr_status rs = round(p1, b, R, 0, npix, nullptr, q0);
+                                                       b.aovB, b.aovC, nullptr, nullptr, b.aoPatch);
+      ubr_status rs = coarsePrepass();
+      if (rs == UBR_OK) rs = round(p1, b, R, 0, npix, nullptr, q0);
       if (rs == UBR_OK) rs = post();
       cudaGraph_t graph = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(s, &graph);
@@ -1730,9 +1983,11 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   } else {
     UBR_CUDA(c, cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s));
     k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim, b.aovA,
-                                                       b.aovB, b.aovC, b.aaN);
+                                                       b.aovB, b.aovC, b.aaN, nullptr, b.aoPatch);
     ++kernels;
     cudaEventRecord(c->ev[2], s);
+    st = coarsePrepass();
+    if (st != UBR_OK) return st;
     st = adaptive ? runAdaptive() : runLayers(p1, b, R, nullptr, npix);
     if (st != UBR_OK) return st;
     cudaEventRecord(c->ev[3], s);
@@ -1752,6 +2007,8 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     if (fr.hit_geom) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_geom, b.hitGeom + po, fpix * 4, kind, s));
     if (fr.hit_prim) UBR_CUDA(c, cudaMemcpyAsync(fr.hit_prim, b.hitPrim + po, fpix * 4, kind, s));
     if (fr.aa_mask && aaMaskOut) UBR_CUDA(c, cudaMemcpyAsync(fr.aa_mask, aaMaskOut, fout * 4, kind, s));
+    if (fr.ao_patch_mask && b.aoPatch)
+      UBR_CUDA(c, cudaMemcpyAsync(fr.ao_patch_mask, b.aoPatch + po, fpix * 4, kind, s));
     if (p.aoWriteAov) {
       const float* o = outAov;
       const size_t n = nout;

@@ -1149,6 +1149,13 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   for (int k = 0; k < 4; ++k) v.geomID[k] = hs.geomID[k];
   v.primCount = n;
   sc->opaque = hs.opaque;
+  sc->aoReceivers = nTri > 0;
+  for (int k = 1; k < 4 && !sc->aoReceivers; ++k)
+    for (uint8_t fe : hs.fromEdge[k])
+      if (!fe) {
+        sc->aoReceivers = true;
+        break;
+      }
   v.baseTri = hs.baseTri;
   v.meshMat = hs.meshMat;
   cudaEventRecord(c->ev[0], c->stream);

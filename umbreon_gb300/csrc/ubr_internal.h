@@ -454,6 +454,8 @@ struct Params {
   int aoWriteAov;       // first-hit AO AOVs requested (AO rays trace nearest hits)
   int aaMode;           // 1: adaptive AA (first-hit normal and section captured)
   float aaThreshold;
+  int aoCoarse;         // coarse-grid AO active: hits look up the grid before casting AO rays
+  int cgW, cgH;         // coarse AO grid size
   f3 aoSky, aoGround;
   float aoDiffuseFactor;
   int shadowsActive, shadowSamples;

@@ -388,6 +388,7 @@ ubr_render_desc toRenderDesc(const Scene& s, const RenderOptions& o, std::vector
   d.aa_mode = o.aaMode;
   d.aa_threshold = o.aaThreshold;
   d.aa_depth = o.aaDepth;
+  d.ao_res_div = o.aoResDiv;
   return d;
 }
 
@@ -409,8 +410,6 @@ void rejectUnsupported(const Scene& scene, const RenderOptions& opt) {
 // One GPU pass: the work of renderFrame (pipeline.cpp:20-256) minus edges,
 // GI and denoise.
 FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderProgress* progress) {
-  if (opt.aoResDiv > 1 || opt.aoResDiv < 0)
-    logMessage(LogLevel::Warning, "coarse-grid AO runs as inline per-hit AO on the GPU");
   if (opt.denoiser != 0) logMessage(LogLevel::Warning, "the denoiser is not part of the GB300 path; skipped");
   const int ss = std::max(1, opt.supersample);
   FrameResult f;
@@ -437,6 +436,12 @@ FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderP
   fr.color = f.color.data();
   fr.depth = f.depth.data();
   fr.view_z = f.viewZ.empty() ? nullptr : f.viewZ.data();
+  const int aoDiv = opt.aoResDiv < 0 ? ss : opt.aoResDiv;
+  if (opt.aoResDebug && aoDiv > 1 && opt.aoSamples > 0) {
+    // coarse-AO fallback mask at the render resolution (embree_renderer.cpp:549-550)
+    f.aoPatchMask.assign(nhi, 0.0f);
+    fr.ao_patch_mask = f.aoPatchMask.data();
+  }
   if (opt.aaMode == 1 && opt.aaDebug) {
     // refinement mask at the output resolution (embree_renderer.cpp:1539)
     f.aaMask.assign(nout, 0.0f);
