@@ -74,7 +74,9 @@ typedef struct ubr_material {
   uint32_t metallic;       /* bool */
   float reflection;
   float emission;
-  uint32_t model;          /* 0 Pov, 1 Principled, 2 Toon */
+  uint32_t model;          /* 0 Pov, 1 Principled (GGX direct pass, the
+                            * pbr_* fields; anisotropy on spheres and
+                            * cylinders), 2 Toon (shaded as Pov) */
   float pbr_metallic;
   float pbr_roughness;
   float pbr_specular;

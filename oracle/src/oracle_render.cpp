@@ -7,9 +7,9 @@
 // operation order so that, built with -ffp-contract=off, results match the
 // reference's own code on the same intersections bit for bit.
 //
-// Scope: the POV shading model (the Principled branch, shading.hpp:88, and
-// every GI / edge / adaptive-AA / coarse-AO branch are outside the path and
-// rejected or ignored as documented at each site).
+// Scope: the POV and Principled (direct pass) shading models, adaptive AA and
+// coarse-grid AO; the GI and edge branches are outside the path and rejected
+// or ignored as documented at each site.
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -51,15 +51,17 @@ inline Frame frameFromNormal(V3 n) {
 }
 inline float radians(float deg) { return deg * 0.01745329252f; }  // scene.hpp:78
 
-struct Mat {  // umbreon::Material subset read by the POV shader
+struct Mat {  // umbreon::Material (scene.hpp:130-175) as the shaders read it
   float ambient, diffuse, specular, roughness, brilliance, phong, phongSize;
   bool metallic;
   float reflection, emission;
-  uint32_t model;
+  uint32_t model;  // 0 Pov, 1 Principled, 2 Toon (shaded as Pov)
+  float pbrMetallic, pbrRoughness, pbrSpecular, pbrAnisotropy, pbrAnisotropyRotation;
 };
 Mat fromAbi(const ubr_material& m) {
   return {m.ambient, m.diffuse, m.specular, m.roughness, m.brilliance, m.phong,
-          m.phong_size, m.metallic != 0, m.reflection, m.emission, m.model};
+          m.phong_size, m.metallic != 0, m.reflection, m.emission, m.model,
+          m.pbr_metallic, m.pbr_roughness, m.pbr_specular, m.pbr_anisotropy, m.pbr_anisotropy_rotation};
 }
 
 struct Light {  // secondary_rays.hpp:26-31
@@ -85,7 +87,9 @@ struct Scene {
   std::vector<uint16_t> group[4];
   std::vector<uint8_t> fromEdge[4];
   std::vector<float> opacity1[4];
-  bool principled = false;
+  // per-segment unit axis of cylinders (curve_build.cpp:163-167, 243-245),
+  // built only when an anisotropic principled cylinder exists
+  std::vector<V3> axis[4];
 };
 
 float roundKey(float x) { return x; }
@@ -103,6 +107,9 @@ void buildCylinders(const ubr_scene_desc& d, const std::vector<V3>& offs, Scene&
   auto P1 = [&](int i) { return V3(d.cyl_p1[3 * i], d.cyl_p1[3 * i + 1], d.cyl_p1[3 * i + 2]); };
   auto op1 = [&](int i) { return d.cyl_opacity1 ? d.cyl_opacity1[i] : -1.0f; };
   auto grp = [&](int i) { return d.cyl_group ? d.cyl_group[i] : uint16_t(0); };
+  bool axisTables = false;
+  for (size_t i = 0; i < n && !axisTables; ++i)
+    axisTables = d.cyl_material[i].model == 1 && d.cyl_material[i].pbr_anisotropy != 0.0f;
   auto pushSide = [&](int kind, int i) {
     for (int k = 0; k < 4; ++k) s.color[kind].push_back(d.cyl_color[4 * i + k]);
     s.mat[kind].push_back(fromAbi(d.cyl_material[i]));
@@ -165,6 +172,7 @@ void buildCylinders(const ubr_scene_desc& d, const std::vector<V3>& offs, Scene&
           if (j < nc - 1) fl |= 2u;
           s.geo.rcFlags.push_back(fl);
           pushSide(kRound, openIdx[chain[j]]);
+          if (axisTables) s.axis[kRound].push_back(safeNormalize(a1[chain[j]] - a0[chain[j]]));
         }
       };
       for (int sg = 0; sg < static_cast<int>(no); ++sg)
@@ -182,6 +190,7 @@ void buildCylinders(const ubr_scene_desc& d, const std::vector<V3>& offs, Scene&
         for (float f : {a.x, a.y, a.z, r, b.x, b.y, b.z, r}) s.geo.ccV.push_back(f);
         s.geo.ccIdx.push_back(base);
         pushSide(kCone, idx);
+        if (axisTables) s.axis[kCone].push_back(safeNormalize(P1(idx) - P0(idx)));
       }
     }
   }
@@ -194,7 +203,6 @@ Scene* buildScene(const ubr_scene_desc& d) {
   for (size_t i = 0; i < d.instance_count; ++i)
     offs.push_back({d.instance_offsets[3 * i], d.instance_offsets[3 * i + 1], d.instance_offsets[3 * i + 2]});
   if (offs.empty()) offs.push_back(V3());
-  auto checkModel = [&](const ubr_material& m) { if (m.model == 1) s->principled = true; };
   // mesh
   const size_t baseV = d.mesh_vertex_count;
   const size_t baseT = d.mesh_triangle_count;
@@ -218,10 +226,8 @@ Scene* buildScene(const ubr_scene_desc& d) {
         }
     s->baseTri = baseT;
     s->meshMat = fromAbi(d.mesh_material);
-    checkModel(d.mesh_material);
     for (uint32_t i = 0; i < d.mesh_material_count; ++i) {
       s->meshMats.push_back(fromAbi(d.mesh_materials[i]));
-      checkModel(d.mesh_materials[i]);
     }
     if (d.mesh_tri_material) s->triMat.assign(d.mesh_tri_material, d.mesh_tri_material + baseT);
     if (d.mesh_tri_group) s->triGroup.assign(d.mesh_tri_group, d.mesh_tri_group + baseT);
@@ -236,12 +242,10 @@ Scene* buildScene(const ubr_scene_desc& d) {
         s->geo.sph.push_back(c[2] + off.z); s->geo.sph.push_back(c[3]);
         for (int k = 0; k < 4; ++k) s->color[kSphere].push_back(d.sphere_color[4 * i + k]);
         s->mat[kSphere].push_back(fromAbi(d.sphere_material[i]));
-        checkModel(d.sphere_material[i]);
         s->group[kSphere].push_back(d.sphere_group ? d.sphere_group[i] : 0);
         s->fromEdge[kSphere].push_back(d.sphere_from_edge && d.sphere_from_edge[i] ? 1 : 0);
       }
   }
-  for (size_t i = 0; i < d.cylinder_count; ++i) checkModel(d.cyl_material[i]);
   buildCylinders(d, offs, *s);
   if (!s->geo.rcIdx.empty()) s->geo.geomID[kRound] = nextGeom++;
   if (!s->geo.ccIdx.empty()) s->geo.geomID[kCone] = nextGeom++;
@@ -579,6 +583,164 @@ inline V3 shadeLocal(const Scene& s, const Mat& mat, const V3& C, const V3& N, c
   return out;
 }
 
+// shading/principled.hpp:35-126: the GGX helpers of the principled model.
+constexpr float kGgxDirectAlphaMin = 1.0e-3f;
+inline V3 principledF0(const Mat& m, const V3& C) {
+  const float dd = 0.08f * m.pbrSpecular;
+  const float t = m.pbrMetallic;
+  return V3{dd + (C.x - dd) * t, dd + (C.y - dd) * t, dd + (C.z - dd) * t};
+}
+inline V3 schlickF(const V3& F0, float u) {
+  float c = 1.0f - u;
+  if (c < 0.0f) c = 0.0f;
+  if (c > 1.0f) c = 1.0f;
+  const float c5 = c * c * c * c * c;
+  return V3{F0.x + (1.0f - F0.x) * c5, F0.y + (1.0f - F0.y) * c5, F0.z + (1.0f - F0.z) * c5};
+}
+inline float ggxD(float a2, float ndh) {
+  if (ndh <= 0.0f) return 0.0f;
+  const float t = ndh * ndh * (a2 - 1.0f) + 1.0f;
+  return a2 / (3.14159265358979323846f * t * t);
+}
+inline float ggxLambda(float a2, float cosT) {
+  const float c2 = std::fmax(cosT * cosT, 1.0e-12f);
+  const float t2 = (1.0f - c2) / c2;
+  return 0.5f * (std::sqrt(1.0f + a2 * t2) - 1.0f);
+}
+inline float principledAspect(float anisotropy) {
+  float a = std::fabs(anisotropy);
+  if (a > 1.0f) a = 1.0f;
+  return std::sqrt(1.0f - 0.9f * a);
+}
+inline float ggxDAniso(float ax, float ay, float hx, float hy, float hz) {
+  if (hz <= 0.0f) return 0.0f;
+  const float sx = hx / ax, sy = hy / ay;
+  const float t = sx * sx + sy * sy + hz * hz;
+  return 1.0f / (3.14159265358979323846f * ax * ay * t * t);
+}
+inline float ggxLambdaAniso(float ax, float ay, float vx, float vy, float vz) {
+  const float z2 = std::fmax(vz * vz, 1.0e-12f);
+  const float t2 = (ax * ax * vx * vx + ay * ay * vy * vy) / z2;
+  return 0.5f * (std::sqrt(1.0f + t2) - 1.0f);
+}
+
+// shading/principled.hpp:139-302 shadePrincipled (direct pass, no traced
+// reflection): one GGX lobe with Schlick Fresnel; an area light (shadows on,
+// samples > 1, radius > 0) evaluates visibility and BRDF per cone sample on
+// its own ('PBRD'-tagged) per-pixel stream.  `tangent` (anisotropy frame,
+// sphere / cylinder hits) or null.
+inline V3 shadePrincipled(const Scene& s, const Mat& mat, const V3& C, const V3& N, const V3& V,
+                          const std::vector<Light>& lights, const V3& ambLight, const V3& bg, const V3& aoFactor,
+                          float diffuseAo, const V3& P, const V3& Ng, float eps, bool shadowsOn, int shadowSamples,
+                          uint32_t px, uint32_t py, const V3* tangent) {
+  V3 out{mat.emission * C.x + aoFactor.x * mat.ambient * C.x * ambLight.x,
+         mat.emission * C.y + aoFactor.y * mat.ambient * C.y * ambLight.y,
+         mat.emission * C.z + aoFactor.z * mat.ambient * C.z * ambLight.z};
+  const float kd = mat.diffuse * (1.0f - mat.pbrMetallic);
+  const V3 F0 = principledF0(mat, C);
+  const float f0max = std::fmax(F0.x, std::fmax(F0.y, F0.z));
+  float alpha = mat.pbrRoughness * mat.pbrRoughness;
+  if (alpha < kGgxDirectAlphaMin) alpha = kGgxDirectAlphaMin;
+  const float a2 = alpha * alpha;
+  const float ndv = std::fmax(dot(N, V), 1.0e-4f);
+  const float lamV = ggxLambda(a2, ndv);
+  constexpr float kPi = 3.14159265358979323846f;
+  // principledAnisoCtx (:110-126)
+  bool anActive = false;
+  V3 at1, at2;
+  float ax = 0.0f, ay = 0.0f;
+  if (tangent != nullptr && mat.pbrAnisotropy != 0.0f) {
+    anActive = true;
+    at1 = *tangent;
+    at2 = cross(N, at1);
+    const float aspect = principledAspect(mat.pbrAnisotropy);
+    ax = alpha / aspect;
+    if (ax > 1.0f) ax = 1.0f;
+    ay = alpha * aspect;
+    if (ax < kGgxDirectAlphaMin) ax = kGgxDirectAlphaMin;
+    if (ay < kGgxDirectAlphaMin) ay = kGgxDirectAlphaMin;
+  }
+  const float lamVA = anActive ? ggxLambdaAniso(ax, ay, dot(V, at1), dot(V, at2), ndv) : 0.0f;
+  auto specWeight = [&](const V3& H, float ndh, const V3& w, float ndlw) {
+    if (!anActive) {
+      const float G2 = 1.0f / (1.0f + lamV + ggxLambda(a2, ndlw));
+      return kPi * ggxD(a2, ndh) * G2 / (4.0f * ndv);
+    }
+    const float G2 = 1.0f / (1.0f + lamVA + ggxLambdaAniso(ax, ay, dot(w, at1), dot(w, at2), ndlw));
+    return kPi * ggxDAniso(ax, ay, dot(H, at1), dot(H, at2), ndh) * G2 / (4.0f * ndv);
+  };
+  uint32_t s0 = px, s1 = py;
+  uint32_t t0 = px ^ 0x50425244u, t1 = py;
+  for (const Light& l : lights) {
+    const float ndl = dot(N, l.L);
+    if (ndl <= 0.0f) continue;
+    const bool areaPath = shadowsOn && shadowSamples > 1 && l.radius > 0.0f;
+    if (!areaPath) {
+      const float shadowFactor = shadowsOn ? computeShadow(s, P, Ng, N, eps, l, shadowSamples, s0, s1) : 1.0f;
+      const V3 Lc{l.color.x * shadowFactor, l.color.y * shadowFactor, l.color.z * shadowFactor};
+      const float dk = kd * ndl * diffuseAo;
+      out.x += dk * C.x * Lc.x;
+      out.y += dk * C.y * Lc.y;
+      out.z += dk * C.z * Lc.z;
+      if (!l.highlight) continue;
+      if (f0max > 0.0f) {
+        const V3 H = normalize(V3{l.L.x + V.x, l.L.y + V.y, l.L.z + V.z});
+        const float ndh = dot(N, H);
+        if (ndh > 0.0f) {
+          const float sW = specWeight(H, ndh, l.L, ndl);
+          const V3 F = schlickF(F0, dot(V, H));
+          out.x += sW * F.x * Lc.x;
+          out.y += sW * F.y * Lc.y;
+          out.z += sW * F.z * Lc.z;
+        }
+      }
+    } else {
+      V3 ng = (dot(Ng, N) < 0.0f) ? V3{-Ng.x, -Ng.y, -Ng.z} : Ng;
+      ng = safeNormalize(ng, N);
+      const V3 O = P + ng * eps;
+      float accD = 0.0f;
+      V3 accS{0.0f, 0.0f, 0.0f};
+      for (int k = 0; k < shadowSamples; ++k) {
+        tea2(t0, t1);
+        const V3 w = sampleLightDir(l, u32ToUnorm(t0), u32ToUnorm(t1));
+        const float ndlS = dot(N, w);
+        if (ndlS <= 0.0f) continue;
+        if (occludedQ(s, O, w, eps, kInf)) continue;
+        accD += ndlS;
+        if (l.highlight && f0max > 0.0f) {
+          const V3 H = normalize(V3{w.x + V.x, w.y + V.y, w.z + V.z});
+          const float ndh = dot(N, H);
+          if (ndh > 0.0f) {
+            const float sW = specWeight(H, ndh, w, ndlS);
+            const V3 F = schlickF(F0, dot(V, H));
+            accS.x += sW * F.x;
+            accS.y += sW * F.y;
+            accS.z += sW * F.z;
+          }
+        }
+      }
+      const float inv = 1.0f / static_cast<float>(shadowSamples);
+      const float dk = kd * diffuseAo * inv * accD;
+      out.x += dk * C.x * l.color.x;
+      out.y += dk * C.y * l.color.y;
+      out.z += dk * C.z * l.color.z;
+      out.x += inv * accS.x * l.color.x;
+      out.y += inv * accS.y * l.color.y;
+      out.z += inv * accS.z * l.color.z;
+    }
+  }
+  if (mat.reflection > 0.0f) {
+    out.x += mat.reflection * bg.x;
+    out.y += mat.reflection * bg.y;
+    out.z += mat.reflection * bg.z;
+  } else if (f0max > 0.0f) {
+    out.x += F0.x * bg.x;
+    out.y += F0.y * bg.y;
+    out.z += F0.z * bg.z;
+  }
+  return out;
+}
+
 // ao/ao_coarse.hpp:55-66 CoarseAoGrid: AO gathered once per coarse cell plus
 // the lookup guides (shading normal, primary hit distance, eligibility).
 struct CoarseAo {
@@ -684,7 +846,7 @@ struct HitShade {
   uint8_t aoPatched = 0;  // coarse-grid AO fell back to the inline gather (hit_shader.hpp:60)
 };
 
-// hit_shader.hpp:147-496 shadeHit (POV; GI / edge / principled branches off)
+// hit_shader.hpp:147-496 shadeHit (POV and principled direct; GI / edge branches off)
 inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& org, uint32_t px, uint32_t py) {
   const Scene& s = *c.s;
   HitShade hs;
@@ -711,7 +873,10 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
     const Mat& triMat = s.triMat.empty() ? s.meshMat : s.meshMats[s.triMat[bt]];
     AOResult aov;
     AoShade ao = aoShadeForHit(c, P, Ng, N, C, secEps, hit.t, px, py, &hs.aoPatched, &aov);
-    hs.color = shadeLocal(s, triMat, C, N, V, c.lights, ao.ambLight, c.bg, c.o.specularScale, ao.aoFactor,
+    hs.color = triMat.model == 1
+                   ? shadePrincipled(s, triMat, C, N, V, c.lights, ao.ambLight, c.bg, ao.aoFactor, ao.diffuseAo, P,
+                                     Ng, secEps, shadowsActive, c.o.shadowSamples, px, py, nullptr)
+                   : shadeLocal(s, triMat, C, N, V, c.lights, ao.ambLight, c.bg, c.o.specularScale, ao.aoFactor,
                           ao.diffuseAo, P, Ng, secEps, shadowsActive, c.o.shadowSamples, px, py);
     hs.opacity = cbuf[3];
     if (c.o.aoWriteAov) {  // hit_shader.hpp:207-213
@@ -742,8 +907,46 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
       diffuseAo = ao.diffuseAo;
     }
     const bool primShadows = !fromEdge && shadowsActive;
-    hs.color = shadeLocal(s, pm, C, N, V, c.lights, ambLight, c.bg, c.o.specularScale, aoFactor, diffuseAo,
-                          P, Ng, secEps, primShadows, c.o.shadowSamples, px, py);
+    // anisotropy tangent frame (hit_shader.hpp:373-425): sphere = meridian of
+    // the world +y pole, cylinder = axis projected onto the tangent plane;
+    // poles, caps and degenerate projections stay isotropic
+    V3 anisoT{0.0f, 0.0f, 0.0f};
+    bool tanValid = false;
+    if (pm.model == 1 && pm.pbrAnisotropy != 0.0f && !fromEdge) {
+      V3 t1{0.0f, 0.0f, 0.0f};
+      if (kind == kSphere) {
+        if (std::fabs(N.y) < 0.999f) {
+          const V3 tPhi = safeNormalize(cross(V3{0.0f, 1.0f, 0.0f}, N));
+          t1 = cross(N, tPhi);
+          tanValid = true;
+        }
+      } else if (!s.axis[kind].empty()) {
+        const V3 A = s.axis[kind][hit.primID];
+        const V3 ngu = safeNormalize(Ng, N);
+        if (std::fabs(dot(ngu, A)) < 0.99f) {
+          const float andn = dot(A, N);
+          const V3 proj{A.x - N.x * andn, A.y - N.y * andn, A.z - N.z * andn};
+          if (dot(proj, proj) >= 1.0e-12f) {
+            t1 = safeNormalize(proj);
+            tanValid = true;
+          }
+        }
+      }
+      if (tanValid) {
+        if (pm.pbrAnisotropyRotation != 0.0f) {
+          const float ang = pm.pbrAnisotropyRotation * 6.2831853072f;
+          const V3 t2 = cross(N, t1);
+          const float ca = std::cos(ang), sa = std::sin(ang);
+          t1 = V3{ca * t1.x + sa * t2.x, ca * t1.y + sa * t2.y, ca * t1.z + sa * t2.z};
+        }
+        anisoT = t1;
+      }
+    }
+    hs.color = pm.model == 1
+                   ? shadePrincipled(s, pm, C, N, V, c.lights, ambLight, c.bg, aoFactor, diffuseAo, P, Ng, secEps,
+                                     primShadows, c.o.shadowSamples, px, py, tanValid ? &anisoT : nullptr)
+                   : shadeLocal(s, pm, C, N, V, c.lights, ambLight, c.bg, c.o.specularScale, aoFactor, diffuseAo,
+                                P, Ng, secEps, primShadows, c.o.shadowSamples, px, py);
     hs.opacity = fc[3];
     hs.group = s.group[kind][hit.primID];
     if (c.o.aaMode == 1) hs.normal = N;  // hit_shader.hpp:321
@@ -1075,7 +1278,6 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
                        int row1) {
   const Scene& s = *static_cast<Scene*>(sp);
   const ubr_render_desc& d = *rdsc;
-  if (s.principled) return -1;
   const int ss = std::max(1, d.supersample);
   const int W = d.width * ss, H = d.height * ss;
   // computeCameraBasis (embree_renderer.cpp:375-386)

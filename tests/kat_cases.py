@@ -492,6 +492,118 @@ def case_ao_coarse_transparency():
     return [(sc, full), (sc, _with(full, aoResDiv=-1))], check
 
 
+# --- principled materials, direct pass (test_principled.cpp:33-161 rig) ---
+
+def _pov_diffuse():
+    return abi.material(ambient=0.2, diffuse=0.8, specular=0.0, phong=0.0, brilliance=1.0, reflection=0.0)
+
+
+def _pbr(metallic, roughness, specular, anisotropy=0.0, rotation=0.0):
+    m = _pov_diffuse()
+    m["model"] = 1
+    m["pbr_metallic"], m["pbr_roughness"], m["pbr_specular"] = metallic, roughness, specular
+    m["pbr_anisotropy"], m["pbr_anisotropy_rotation"] = anisotropy, rotation
+    return m
+
+
+def _unit(v):
+    v = np.asarray(v, np.float64)
+    return tuple(float(x) for x in v / np.linalg.norm(v))
+
+
+def pbr_scene(floor_mat, sphere_mat, fill=False, bond_mat=None):
+    """Floor quad (y = 0, 8 x 8) + unit sphere at (0, 1, 0), perspective
+    camera, one distant light; optional capped bond along x (addBond)."""
+    c = [(-4, 0, -4), (4, 0, -4), (4, 0, 4), (-4, 0, -4), (4, 0, 4), (-4, 0, 4)]
+    sc = Scene(mesh_positions=np.array(c, np.float32),
+               mesh_normals=np.tile([0, 1, 0], (6, 1)).astype(np.float32),
+               mesh_colors=np.tile([0.7, 0.7, 0.7, 1.0], (6, 1)).astype(np.float32), mesh_material=floor_mat,
+               sphere_center_radius=np.array([[0, 1, 0, 1]], np.float32),
+               sphere_color=np.array([[0.8, 0.3, 0.3, 1.0]], np.float32),
+               sphere_material=np.array([sphere_mat], abi.MATERIAL_DTYPE))
+    if bond_mat is not None:
+        sc.cyl_p0 = np.array([[-2.0, 1.4, 1.0]], np.float32)
+        sc.cyl_p1 = np.array([[2.0, 1.4, 1.0]], np.float32)
+        sc.cyl_radius = np.array([0.5], np.float32)
+        sc.cyl_color = np.array([[0.85, 0.7, 0.3, 1.0]], np.float32)
+        sc.cyl_material = np.array([bond_mat], abi.MATERIAL_DTYPE)
+        sc.cyl_open = np.zeros(1, np.uint8)
+    sc.camera = Camera(position=(0.0, 3.0, 8.0), direction=_unit((0, -0.35, -1)), up=(0.0, 1.0, 0.0),
+                       orthographic=False, fovy=40.0)
+    sc.lights = [DistantLight(direction=_unit((-0.4, -1.0, -0.3)), color=(1.0, 1.0, 1.0), intensity=0.8,
+                              castsHighlight=not fill)]
+    sc.background = (0.9, 0.9, 0.95)
+    sc.ambientColor = (0.5, 0.5, 0.5)
+    return sc
+
+
+def _opts(**kw):
+    return RenderOptions(width=48, height=36, **kw)
+
+
+def _lum(f):
+    c = f.color.astype(np.float64)
+    return float(np.mean(0.2126 * c[..., 0] + 0.7152 * c[..., 1] + 0.0722 * c[..., 2]))
+
+
+def case_pbr_diffuse_parity():
+    pov = pbr_scene(_pov_diffuse(), _pov_diffuse())
+    pbr = pbr_scene(_pbr(0.0, 0.5, 0.0), _pbr(0.0, 0.5, 0.0))
+    def check(fs):
+        return [("diffuse parity, shadows off (bitwise)", np.array_equal(fs[0].color, fs[1].color)),
+                ("diffuse parity, hard shadows (bitwise)", np.array_equal(fs[2].color, fs[3].color))]
+    return [(pov, _opts()), (pbr, _opts()), (pov, _opts(shadows=True)), (pbr, _opts(shadows=True))], check
+
+
+def case_pbr_determinism_and_area_light():
+    m = _pbr(0.6, 0.25, 0.5)
+    sc = pbr_scene(m, m)
+    hard = _opts(shadows=True)
+    area = _opts(shadows=True, shadowSamples=4, lightRadius=8.6)
+    def check(fs):
+        return [("principled render run-to-run bit-exact", np.array_equal(fs[0].color, fs[1].color)),
+                ("area-light path run-to-run bit-exact", np.array_equal(fs[2].color, fs[3].color)),
+                ("area light changes the principled render", not np.array_equal(fs[0].color, fs[2].color))]
+    return [(sc, hard), (sc, hard), (sc, area), (sc, area)], check
+
+
+def case_pbr_fill_light_roughness_inert():
+    r1, r2 = _pbr(0.8, 0.1, 0.5), _pbr(0.8, 0.7, 0.5)
+    def check(fs):
+        return [("fill light: roughness does not enter (bitwise)", np.array_equal(fs[0].color, fs[1].color))]
+    return [(pbr_scene(r1, r1, fill=True), _opts()), (pbr_scene(r2, r2, fill=True), _opts())], check
+
+
+def case_pbr_roughness_and_metal():
+    r1, r2, metal = _pbr(1.0, 0.15, 0.5), _pbr(1.0, 0.6, 0.5), _pbr(1.0, 0.3, 0.5)
+    def check(fs):
+        return [("roughness changes the principled render", not np.array_equal(fs[0].color, fs[1].color)),
+                ("metal visible in basic mode", _lum(fs[2]) > 0.05),
+                ("metal visible in AO mode", _lum(fs[3]) > 0.05),
+                ("AO-mode principled render bit-exact", np.array_equal(fs[3].color, fs[4].color))]
+    ao = _opts(aoSamples=8)
+    return [(pbr_scene(r1, r1), _opts()), (pbr_scene(r2, r2), _opts()), (pbr_scene(metal, metal), _opts()),
+            (pbr_scene(metal, metal), ao), (pbr_scene(metal, metal), ao)], check
+
+
+def case_pbr_anisotropy():
+    iso = _pbr(1.0, 0.35, 0.5)
+    mesh_aniso = _pbr(1.0, 0.35, 0.5, anisotropy=0.8)
+    diffuse = _pbr(0.0, 0.5, 0.0)
+    an, rot = _pbr(1.0, 0.35, 0.5, 0.8, 0.0), _pbr(1.0, 0.35, 0.5, 0.8, 0.25)
+    def check(fs):
+        return [("mesh anisotropy is bitwise inert", np.array_equal(fs[0].color, fs[1].color)),
+                ("anisotropy changes the direct highlight (primitives)", not np.array_equal(fs[2].color, fs[3].color)),
+                ("anisotropic render finite", bool(np.all(np.isfinite(fs[2].color)))),
+                ("anisotropyRotation reorients the lobe", not np.array_equal(fs[2].color, fs[4].color)),
+                ("anisotropic render run-to-run bit-exact", np.array_equal(fs[4].color, fs[5].color))]
+    return [(pbr_scene(mesh_aniso, diffuse), _opts()), (pbr_scene(iso, diffuse), _opts()),
+            (pbr_scene(_pov_diffuse(), an, bond_mat=an), _opts()),
+            (pbr_scene(_pov_diffuse(), iso, bond_mat=iso), _opts()),
+            (pbr_scene(_pov_diffuse(), rot, bond_mat=rot), _opts()),
+            (pbr_scene(_pov_diffuse(), rot, bond_mat=rot), _opts())], check
+
+
 CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
 
 

@@ -658,6 +658,11 @@ ubr_status adjointCheck(Context* c, const Scene& sc, const ubr_render_desc& d, c
     return setError(c, UBR_INVALID_ARGUMENT, "adjoint: soft shadows are not differentiable");
   if (p.aoSamples > 0 && p.aoEnhanced && (p.aoBentNormal || p.aoMultibounce))
     return setError(c, UBR_INVALID_ARGUMENT, "adjoint: AO bent normal / multibounce are not differentiable");
+  if (sc.principled) return setError(c, UBR_INVALID_ARGUMENT, "adjoint: principled materials are not differentiable");
+  if (p.aaMode == 1 && (p.ss > 1 || d.aa_depth > 1))
+    return setError(c, UBR_INVALID_ARGUMENT, "adjoint: adaptive AA is not differentiable (use the grid)");
+  if ((d.ao_res_div < 0 ? p.ss : d.ao_res_div) > 1 && p.aoSamples > 0)
+    return setError(c, UBR_INVALID_ARGUMENT, "adjoint: coarse-grid AO is not differentiable");
   return UBR_OK;
 }
 

@@ -241,7 +241,10 @@ __global__ void __launch_bounds__(128) k_surface(Params p1, DScene s1, Batch bt,
       b.surfA[i] = make_float4(O.x, O.y, O.z, sf.secEps);
       b.surfB[i] = make_float4(sf.N.x, sf.N.y, sf.N.z, __int_as_float(start));
       // flags: 1 hit, 2 casts AO, 4 casts shadows; bits 8.. the frame index
-      const uint32_t flags = 1u | (aoCast ? 2u : 0u) | (sf.shOn ? 4u : 0u) | (uint32_t(f) << 8);
+      // bit 3: principled material (its area-light samples use their own stream)
+      const bool pbr = __ldg(&s.mats[sf.mat].model) == 1u;
+      const uint32_t flags =
+          1u | (aoCast ? 2u : 0u) | (sf.shOn ? 4u : 0u) | (pbr ? 8u : 0u) | (uint32_t(f) << 8);
       b.surfC[i] = make_uint2(gpix, flags);
       cast = (flags & 6u) != 0u;
     }
@@ -302,10 +305,17 @@ UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, uint32_
           const LightD Q = lights[q];
           if (Q.soft && dot(N, Q.L) > 0.0f) consumed += Q.samples;
         }
-        uint32_t s0 = uint32_t(px), s1 = uint32_t(py);
+        // principled area lights draw from the 'PBRD'-tagged stream
+        // (principled.hpp:174-175), advanced the same way
+        uint32_t s0 = (flags & 8u) ? (uint32_t(px) ^ 0x50425244u) : uint32_t(px), s1 = uint32_t(py);
         const int stepsRng = consumed + (k - L.rayOffset) + 1;
         for (int q = 0; q < stepsRng; ++q) tea2(s0, s1);
         dir = sampleLightDir(L, u32ToUnorm(s0), u32ToUnorm(s1));
+        // a principled sample below the horizon is never queried (:262)
+        if ((flags & 8u) && !(dot(N, dir) > 0.0f)) {
+          o.r = Ray{ld3(sa), dir, sa.w, tfar};
+          return o;
+        }
       }
       o.trace = true;
     }
@@ -577,6 +587,187 @@ UBR_D AoQ aoQuality(const Params& p, const float* aoT, uint64_t aoStride, uint32
   return r;
 }
 
+// Anisotropy tangent of a principled sphere / cylinder hit (hit_shader.hpp:
+// 373-425): the meridian of the world +y pole on a sphere, the axis projected
+// onto the tangent plane on a cylinder (none at poles, caps or degenerate
+// projections), turned by the material's rotation (in turns).
+UBR_D bool anisoTangent(const DScene& s, const Surf& sf, float rotation, f3& t1) {
+  const f3 N = sf.N;
+  bool valid = false;
+  if (sf.kind == kSphere) {
+    if (fabsf(N.y) < 0.999f) {
+      const f3 tPhi = safeNormalize(cross(f3{0.0f, 1.0f, 0.0f}, N));
+      t1 = cross(N, tPhi);
+      valid = true;
+    }
+  } else if (s.primAxis[sf.kind]) {
+    const float4 a4 = __ldg(&s.primAxis[sf.kind][sf.prim]);
+    const f3 A{a4.x, a4.y, a4.z};
+    const f3 ngu = safeNormalize(sf.Ng, N);
+    if (fabsf(dot(ngu, A)) < 0.99f) {
+      const float andn = dot(A, N);
+      const f3 proj{A.x - N.x * andn, A.y - N.y * andn, A.z - N.z * andn};
+      if (dot(proj, proj) >= 1.0e-12f) {
+        t1 = safeNormalize(proj);
+        valid = true;
+      }
+    }
+  }
+  if (valid && rotation != 0.0f) {
+    const float ang = rotation * 6.2831853072f;
+    const f3 t2 = cross(N, t1);
+    const float ca = cosf(ang), sa = sinf(ang);
+    t1 = f3{ca * t1.x + sa * t2.x, ca * t1.y + sa * t2.y, ca * t1.z + sa * t2.z};
+  }
+  return valid;
+}
+
+// GGX helpers of principled.hpp:35-98.
+UBR_D float ggxD(float a2, float ndh) {
+  if (ndh <= 0.0f) return 0.0f;
+  const float t = ndh * ndh * (a2 - 1.0f) + 1.0f;
+  return a2 / (3.14159265358979323846f * t * t);
+}
+UBR_D float ggxLambda(float a2, float cosT) {
+  const float c2 = fmaxf(cosT * cosT, 1.0e-12f);
+  const float t2 = (1.0f - c2) / c2;
+  return 0.5f * (sqrtf(1.0f + a2 * t2) - 1.0f);
+}
+UBR_D float ggxDAniso(float ax, float ay, float hx, float hy, float hz) {
+  if (hz <= 0.0f) return 0.0f;
+  const float sx = hx / ax, sy = hy / ay;
+  const float t = sx * sx + sy * sy + hz * hz;
+  return 1.0f / (3.14159265358979323846f * ax * ay * t * t);
+}
+UBR_D float ggxLambdaAniso(float ax, float ay, float vx, float vy, float vz) {
+  const float z2 = fmaxf(vz * vz, 1.0e-12f);
+  const float t2 = (ax * ax * vx * vx + ay * ay * vy * vy) / z2;
+  return 0.5f * (sqrtf(1.0f + t2) - 1.0f);
+}
+
+// shadePrincipled (principled.hpp:139-302), direct pass without traced
+// reflection: one GGX lobe with Schlick Fresnel; an area light (shadows on,
+// samples > 1, radius > 0) weighs visibility x BRDF per cone sample on the
+// 'PBRD'-tagged per-pixel stream.  `occ` = this hit's shadow-ray results
+// (light order, rayOffset per light).
+UBR_D f3 shadePrincipled(const Params& p, const ubr_material& m, const Surf& sf, const LightD* lights,
+                         const uint8_t* occ, f3 aoFactor, f3 ambLight, float diffuseAo, int px, int py,
+                         const f3* tangent) {
+  const f3 C = sf.C, N = sf.N, V = sf.V;
+  f3 out{m.emission * C.x + aoFactor.x * m.ambient * C.x * ambLight.x,
+         m.emission * C.y + aoFactor.y * m.ambient * C.y * ambLight.y,
+         m.emission * C.z + aoFactor.z * m.ambient * C.z * ambLight.z};
+  const float kd = m.diffuse * (1.0f - m.pbr_metallic);
+  const float dd = 0.08f * m.pbr_specular, tm = m.pbr_metallic;
+  const f3 F0{dd + (C.x - dd) * tm, dd + (C.y - dd) * tm, dd + (C.z - dd) * tm};
+  const float f0max = fmaxf(F0.x, fmaxf(F0.y, F0.z));
+  float alpha = m.pbr_roughness * m.pbr_roughness;
+  if (alpha < 1.0e-3f) alpha = 1.0e-3f;
+  const float a2 = alpha * alpha;
+  const float ndv = fmaxf(dot(N, V), 1.0e-4f);
+  const float lamV = ggxLambda(a2, ndv);
+  const float kPi = 3.14159265358979323846f;
+  bool an = false;
+  f3 at1{0.0f, 0.0f, 0.0f}, at2{0.0f, 0.0f, 0.0f};
+  float ax = 0.0f, ay = 0.0f;
+  if (tangent != nullptr && m.pbr_anisotropy != 0.0f) {
+    an = true;
+    at1 = *tangent;
+    at2 = cross(N, at1);
+    float aa = fabsf(m.pbr_anisotropy);
+    if (aa > 1.0f) aa = 1.0f;
+    const float aspect = sqrtf(1.0f - 0.9f * aa);
+    ax = alpha / aspect;
+    if (ax > 1.0f) ax = 1.0f;
+    ay = alpha * aspect;
+    if (ax < 1.0e-3f) ax = 1.0e-3f;
+    if (ay < 1.0e-3f) ay = 1.0e-3f;
+  }
+  const float lamVA = an ? ggxLambdaAniso(ax, ay, dot(V, at1), dot(V, at2), ndv) : 0.0f;
+  auto specWeight = [&](f3 H, float ndh, f3 w, float ndlw) {
+    if (!an) {
+      const float G2 = 1.0f / (1.0f + lamV + ggxLambda(a2, ndlw));
+      return kPi * ggxD(a2, ndh) * G2 / (4.0f * ndv);
+    }
+    const float G2 = 1.0f / (1.0f + lamVA + ggxLambdaAniso(ax, ay, dot(w, at1), dot(w, at2), ndlw));
+    return kPi * ggxDAniso(ax, ay, dot(H, at1), dot(H, at2), ndh) * G2 / (4.0f * ndv);
+  };
+  auto schlick = [&](float u) {
+    float c = 1.0f - u;
+    if (c < 0.0f) c = 0.0f;
+    if (c > 1.0f) c = 1.0f;
+    const float c5 = c * c * c * c * c;
+    return f3{F0.x + (1.0f - F0.x) * c5, F0.y + (1.0f - F0.y) * c5, F0.z + (1.0f - F0.z) * c5};
+  };
+  uint32_t t0 = uint32_t(px) ^ 0x50425244u, t1 = uint32_t(py);
+  for (int l = 0; l < p.nLights; ++l) {
+    const LightD L = lights[l];
+    const float ndl = dot(N, L.L);
+    if (ndl <= 0.0f) continue;
+    const bool areaPath = sf.shOn && L.soft;
+    if (!areaPath) {
+      const float shadowFactor = (sf.shOn && occ[L.rayOffset]) ? 0.0f : 1.0f;
+      const f3 Lc{L.color.x * shadowFactor, L.color.y * shadowFactor, L.color.z * shadowFactor};
+      const float dk = kd * ndl * diffuseAo;
+      out.x += dk * C.x * Lc.x;
+      out.y += dk * C.y * Lc.y;
+      out.z += dk * C.z * Lc.z;
+      if (!L.highlight) continue;
+      if (f0max > 0.0f) {
+        const f3 H = normalize(f3{L.L.x + V.x, L.L.y + V.y, L.L.z + V.z});
+        const float ndh = dot(N, H);
+        if (ndh > 0.0f) {
+          const float sW = specWeight(H, ndh, L.L, ndl);
+          const f3 F = schlick(dot(V, H));
+          out.x += sW * F.x * Lc.x;
+          out.y += sW * F.y * Lc.y;
+          out.z += sW * F.z * Lc.z;
+        }
+      }
+    } else {
+      float accD = 0.0f;
+      f3 accS{0.0f, 0.0f, 0.0f};
+      for (int k = 0; k < L.samples; ++k) {
+        tea2(t0, t1);
+        const f3 w = sampleLightDir(L, u32ToUnorm(t0), u32ToUnorm(t1));
+        const float ndlS = dot(N, w);
+        if (ndlS <= 0.0f) continue;
+        if (occ[L.rayOffset + k]) continue;
+        accD += ndlS;
+        if (L.highlight && f0max > 0.0f) {
+          const f3 H = normalize(f3{w.x + V.x, w.y + V.y, w.z + V.z});
+          const float ndh = dot(N, H);
+          if (ndh > 0.0f) {
+            const float sW = specWeight(H, ndh, w, ndlS);
+            const f3 F = schlick(dot(V, H));
+            accS.x += sW * F.x;
+            accS.y += sW * F.y;
+            accS.z += sW * F.z;
+          }
+        }
+      }
+      const float inv = 1.0f / float(L.samples);
+      const float dk = kd * diffuseAo * inv * accD;
+      out.x += dk * C.x * L.color.x;
+      out.y += dk * C.y * L.color.y;
+      out.z += dk * C.z * L.color.z;
+      out.x += inv * accS.x * L.color.x;
+      out.y += inv * accS.y * L.color.y;
+      out.z += inv * accS.z * L.color.z;
+    }
+  }
+  if (m.reflection > 0.0f) {
+    out.x += m.reflection * p.bg.x;
+    out.y += m.reflection * p.bg.y;
+    out.z += m.reflection * p.bg.z;
+  } else if (f0max > 0.0f) {
+    out.x += F0.x * p.bg.x;
+    out.y += F0.y * p.bg.y;
+    out.z += F0.z * p.bg.z;
+  }
+  return out;
+}
+
 template <bool BATCH>
 __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, Bufs b, int layer, uint32_t n,
                                                const uint32_t* queue, uint32_t* outQueue) {
@@ -654,11 +845,20 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
         }
         if (p.aoDiffuseFactor > 0.0f) diffuseAo = 1.0f - p.aoDiffuseFactor * (1.0f - openness);
       }
-      // --- shadeLocal, POV branch (shading.hpp:96-191) ---
       const f3 C = sf.C, N = sf.N, V = sf.V;
-      f3 out{m.emission * C.x + aoFactor.x * m.ambient * C.x * ambLight.x,
-             m.emission * C.y + aoFactor.y * m.ambient * C.y * ambLight.y,
-             m.emission * C.z + aoFactor.z * m.ambient * C.z * ambLight.z};
+      f3 out;
+      if (m.model == 1u) {
+        // --- principled direct pass (shading.hpp:88-91 -> principled.hpp) ---
+        f3 anisoT{0.0f, 0.0f, 0.0f};
+        const bool tanValid = sf.kind != kMesh && !sf.fromEdge && m.pbr_anisotropy != 0.0f &&
+                              anisoTangent(s, sf, m.pbr_anisotropy_rotation, anisoT);
+        out = shadePrincipled(p, m, sf, lights, b.occ + rb + p.aoSamples, aoFactor, ambLight, diffuseAo, px, py,
+                              tanValid ? &anisoT : nullptr);
+      } else {
+      // --- shadeLocal, POV branch (shading.hpp:96-191) ---
+      out = f3{m.emission * C.x + aoFactor.x * m.ambient * C.x * ambLight.x,
+               m.emission * C.y + aoFactor.y * m.ambient * C.y * ambLight.y,
+               m.emission * C.z + aoFactor.z * m.ambient * C.z * ambLight.z};
       const float ex = blinnExp(m.roughness);
       for (int l = 0; l < p.nLights; ++l) {
         const LightD L = lights[l];
@@ -720,6 +920,7 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
         out.x += m.reflection * p.bg.x;
         out.y += m.reflection * p.bg.y;
         out.z += m.reflection * p.bg.z;
+      }
       }
       // --- first-hit capture + compositing (transparency.hpp:394-467) ---
       if (b.depth[gpix] == 0.0f) {

@@ -52,6 +52,7 @@ struct HostScene {
   std::vector<uint8_t> fromEdge[4];
   std::vector<float> opacity1[4];
   std::vector<uint16_t> group[4];     // CueMol section per primitive (primID order)
+  std::vector<float4> axis[4];        // cylinder unit axis (anisotropic principled scenes only)
   std::vector<uint16_t> triGroup;     // per base triangle
   std::vector<ubr_material> mats;
   uint32_t geomID[4] = {kInvalid, kInvalid, kInvalid, kInvalid};
@@ -115,6 +116,15 @@ void flattenCylinders(const ubr_scene_desc& d, const std::vector<f3>& offs, Host
   }
   auto op1 = [&](int i) { return d.cyl_opacity1 ? d.cyl_opacity1[i] : -1.0f; };
   auto grp = [&](int i) { return d.cyl_group ? d.cyl_group[i] : uint16_t(0); };
+  // per-segment axes only when an anisotropic principled cylinder exists
+  // (curve_build.cpp:45-54): the tangent frame of its highlight
+  bool axisTables = false;
+  for (size_t i = 0; i < n && !axisTables; ++i)
+    axisTables = d.cyl_material[i].model == 1 && d.cyl_material[i].pbr_anisotropy != 0.0f;
+  auto pushAxis = [&](int kind, f3 a) {
+    const f3 u = safeNormalize(a);
+    s.axis[kind].push_back(make_float4(u.x, u.y, u.z, 0.0f));
+  };
   auto side = [&](int kind, int i) {
     s.color[kind].push_back(make_float4(d.cyl_color[4 * i], d.cyl_color[4 * i + 1],
                                         d.cyl_color[4 * i + 2], d.cyl_color[4 * i + 3]));
@@ -174,6 +184,7 @@ void flattenCylinders(const ubr_scene_desc& d, const std::vector<f3>& offs, Host
           if (j < nc - 1) fl |= 2u;
           s.rcFlags.push_back(fl);
           side(kRound, openIdx[chain[j]]);
+          if (axisTables) pushAxis(kRound, a1[chain[j]] - a0[chain[j]]);
         }
       };
       for (int sg = 0; sg < int(no); ++sg)
@@ -212,6 +223,7 @@ void flattenCylinders(const ubr_scene_desc& d, const std::vector<f3>& offs, Host
       s.ccV.push_back(make_float4(b.x, b.y, b.z, r));
       s.ccIdx.push_back(base);
       side(kCone, i);
+      if (axisTables) pushAxis(kCone, ld3(d.cyl_p1, i) - ld3(d.cyl_p0, i));
     }
   }
 }
@@ -1128,9 +1140,6 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   st = flatten(c, d, hs);
   if (st != UBR_OK) return st;
   const auto tFlat = std::chrono::steady_clock::now();
-  if (hs.principled)
-    return setError(c, UBR_INVALID_ARGUMENT,
-                    "Principled materials are not supported by this library (POV finish only)");
   Scene* sc = new Scene();
   sc->ctx = c;
   auto fail = [&](ubr_status s) {
@@ -1149,6 +1158,7 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   for (int k = 0; k < 4; ++k) v.geomID[k] = hs.geomID[k];
   v.primCount = n;
   sc->opaque = hs.opaque;
+  sc->principled = hs.principled;
   sc->aoReceivers = nTri > 0;
   for (int k = 1; k < 4 && !sc->aoReceivers; ++k)
     for (uint8_t fe : hs.fromEdge[k])
@@ -1187,6 +1197,7 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
     if ((st = upload(c, sc, hs.fromEdge[k], &v.primFromEdge[k])) != UBR_OK) return fail(st);
     if ((st = upload(c, sc, hs.opacity1[k], &v.primOpacity1[k])) != UBR_OK) return fail(st);
     if ((st = upload(c, sc, hs.group[k], &v.primGroup[k])) != UBR_OK) return fail(st);
+    if ((st = upload(c, sc, hs.axis[k], &v.primAxis[k])) != UBR_OK) return fail(st);
   }
   if ((st = upload(c, sc, hs.triGroup, &v.meshTriGroup)) != UBR_OK) return fail(st);
   const auto tUp = std::chrono::steady_clock::now();

@@ -387,6 +387,7 @@ struct Surf {
   uint32_t mat;
   float secEps;
   bool aoOn, shOn;
+  bool fromEdge;  // outline decoration primitive (no AO, no shadows)
 };
 
 // secondary_rays.hpp:38-46
@@ -428,12 +429,14 @@ UBR_D Surf surfaceAt(const Params& p, const DScene& s, f3 org, f3 rd, float t, u
     sf.mat = s.meshTriMat ? __ldg(&s.meshTriMat[s.baseTri ? sf.prim % s.baseTri : 0]) : s.meshMat;
     sf.aoOn = p.aoSamples > 0;
     sf.shOn = shadowsActive;
+    sf.fromEdge = false;
   } else {
     const float4 fc = __ldg(&s.primColor[sf.kind][sf.prim]);
     sf.mat = __ldg(&s.primMat[sf.kind][sf.prim]);
     sf.N = faceForward(normalize(Ng), rd);
     sf.C = f3{fc.x, fc.y, fc.z};
     const bool fromEdge = __ldg(&s.primFromEdge[sf.kind][sf.prim]) != 0;
+    sf.fromEdge = fromEdge;
     sf.aoOn = !fromEdge && p.aoSamples > 0;
     sf.shOn = !fromEdge && shadowsActive;
     sf.opacity = fc.w;

@@ -50,6 +50,7 @@ struct Scene {
   uint64_t nodes = 0;
   bool opaque = true;        // every primitive fully opaque: frames are one layer deep
   bool aoReceivers = false;  // a mesh or a non-outline primitive exists (coarse AO grid eligible)
+  bool principled = false;   // some material uses the principled model
   uint64_t deviceBytes = 0;
   double buildMs = 0.0;
   double flattenMs = 0.0;    // host: validation, primID ordering, chaining, material table

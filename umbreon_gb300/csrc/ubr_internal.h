@@ -120,6 +120,7 @@ struct DScene {
   const uint32_t* primMat[4] = {nullptr, nullptr, nullptr, nullptr};
   const uint8_t* primFromEdge[4] = {nullptr, nullptr, nullptr, nullptr};
   const float* primOpacity1[4] = {nullptr, nullptr, nullptr, nullptr};
+  const float4* primAxis[4] = {nullptr, nullptr, nullptr, nullptr};  // cylinder unit axis, or null
   const uint16_t* primGroup[4] = {nullptr, nullptr, nullptr, nullptr};  // CueMol section
   const uint16_t* meshTriGroup = nullptr;  // per base triangle (or null: section 0)
   const float4* rcClip = nullptr;      // 2 per round segment (clipL, clipR)

@@ -399,12 +399,6 @@ void rejectUnsupported(const Scene& scene, const RenderOptions& opt) {
   if (opt.gi) throw std::runtime_error("umbreon::render: GI is not part of the GB300 ray-cast + shade library");
   if (opt.strokeEdges.enable || opt.objectSpaceEdges.enable)
     throw std::runtime_error("umbreon::render: edge passes are not part of the GB300 ray-cast + shade library");
-  auto principled = [](const Material& m) { return m.model == ShadingModel::Principled; };
-  bool p = principled(scene.mesh.material);
-  for (const Material& m : scene.mesh.materials) p = p || principled(m);
-  for (const Sphere& s : scene.spheres) p = p || principled(s.material);
-  for (const Cylinder& c : scene.cylinders) p = p || principled(c.material);
-  if (p) throw std::runtime_error("umbreon::render: Principled materials are not supported (POV finish only)");
 }
 
 // One GPU pass: the work of renderFrame (pipeline.cpp:20-256) minus edges,
