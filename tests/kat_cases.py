@@ -604,6 +604,95 @@ def case_pbr_anisotropy():
             (pbr_scene(_pov_diffuse(), rot, bond_mat=rot), _opts())], check
 
 
+# --- fog (test_fog.cpp:30-97), restated through a render: the quad at view
+# z 10 of the ortho rig, mesh Lambert colour (0.30, 0.36, 0.42) ---
+
+def _fogged(start, end, color=(1.0, 1.0, 1.0), bg=(0.4, 0.1, 0.2)):
+    from umbreon_gb300.api import Fog
+    sc = scenes.quad_scene(bg=bg)
+    sc.fog = Fog(enabled=True, color=color, start=start, end=end)
+    return sc
+
+
+def case_fog_linear():
+    def check(fs):
+        mid, before, after, bgf = centre(fs[0]), centre(fs[1]), centre(fs[2]), fs[0].color[0, 0]
+        return [("f = 0.5: R = mix(1, 0.30, 0.5)", approx(mid[0], 0.65, 1e-4)),
+                ("f = 0.5: B = mix(1, 0.42, 0.5)", approx(mid[2], 0.71, 1e-4)),
+                ("opaque: alpha untouched", approx(mid[3], 1.0, 1e-6)),
+                ("before start: unfogged", approx(before[0], 0.30, 1e-4)),
+                ("after end: full fog colour", approx(after[0], 1.0, 1e-6)),
+                ("background (view z 0) skipped", approx(bgf[0], 0.4, 1e-6) and approx(bgf[2], 0.2, 1e-6))]
+    sc = _fogged(5.0, 15.0)
+    sc.mesh_positions = sc.mesh_positions * np.array([0.5, 0.5, 1.0], np.float32)  # leave background corners
+    return [(sc, o5()), (_fogged(12.0, 20.0), o5()), (_fogged(2.0, 8.0), o5())], check
+
+
+def case_fog_degenerate_slab():
+    def check(fs):
+        return [("degenerate slab: near side unfogged", approx(centre(fs[0])[0], 0.30, 1e-4)),
+                ("degenerate slab: far side full fog", approx(centre(fs[1])[0], 1.0, 1e-6))]
+    return [(_fogged(12.0, 12.0), o5()), (_fogged(8.0, 8.0), o5())], check
+
+
+def case_fog_transparent_background():
+    fog = (0.7, 0.8, 0.9)
+    def check(fs):
+        op, tr = centre(fs[0]), centre(fs[1])
+        f = 0.625  # (15 - 10) / (15 - 7)
+        over = [tr[k] * tr[3] + fog[k] * (1.0 - tr[3]) for k in range(3)]
+        return [("transparent: RGB unchanged", approx(tr[0], 0.30, 1e-4)),
+                ("transparent: alpha faded by f", approx(tr[3], f, 1e-5)),
+                ("transparent over fog colour == opaque",
+                 all(approx(over[k], op[k], 1e-5) for k in range(3)))]
+    return [(_fogged(7.0, 15.0, fog), o5()), (_fogged(7.0, 15.0, fog), o5(transparentBackground=True))], check
+
+
+# --- clip planes (test_clip_planes.cpp:14-70): unit sphere at the origin,
+# ortho camera at z 10, blue background ---
+
+def _clip_scene(near=None, far=None):
+    sc = scenes.material_sphere_scene((1.0, 0.0, 0.0, 1.0), abi.material(ambient=0.2, diffuse=0.8), (0.0, 0.0, 1.0))
+    if near is not None:
+        sc.clipNear = near
+    if far is not None:
+        sc.clipFar = far
+    return sc
+
+
+def case_clip_planes():
+    def check(fs):
+        c0, cf, cn, cc = (centre(f) for f in fs)
+        return [("no clip: centre hits the sphere", c0[0] > 0.3 and c0[2] < 0.5),
+                ("clipFar 8: background", approx(cf[2], 1.0, 1e-4) and cf[0] < 1e-4),
+                ("clipNear 12: background", cn[0] < 1e-4),
+                ("clipNear 10: interior back wall at view z 11", 10.5 < float(fs[3].viewZ[2, 2]) < 11.5)]
+    return [(_clip_scene(), o5()), (_clip_scene(far=8.0), o5()), (_clip_scene(near=12.0), o5()),
+            (_clip_scene(near=10.0), o5())], check
+
+
+# --- indexed mesh (test_mesh_indexed.cpp:23-93) ---
+
+def case_mesh_indexed_equals_deindexed():
+    pos = np.array([(-2, -2, 0), (2, -2, 0), (2, 2, 0), (-2, 2, 0)], np.float32)
+    idx = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    col = np.tile(np.array([0.5, 0.6, 0.7, 1.0], np.float32), (4, 1))
+    nrm = np.tile(np.array([0, 0, 1], np.float32), (4, 1))
+    def mk(p, n, c, i):
+        sc = Scene(mesh_positions=p, mesh_normals=n, mesh_colors=c, mesh_index=i,
+                   mesh_material=abi.material(ambient=0.2, diffuse=0.8))
+        sc.camera = scenes.ortho_cam()
+        sc.background = (0.1, 0.2, 0.3)
+        sc.lights = [DistantLight(direction=(0.0, 0.0, -1.0), intensity=0.5)]
+        return sc
+    flat = idx.reshape(-1)
+    de = mk(pos[flat], nrm[flat], col[flat], None)
+    opt = RenderOptions(width=24, height=24, supersample=2)
+    def check(fs):
+        return [("indexed vs de-indexed render bit-identical", np.array_equal(fs[0].color, fs[1].color))]
+    return [(mk(pos, nrm, col, idx), opt), (de, opt)], check
+
+
 CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
 
 
