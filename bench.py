@@ -549,6 +549,21 @@ def run_ours(args):
     # into a pinned host frame (the caller's buffer; pageable memory works too)
     host_color = torch.zeros((opt.height, opt.width, 4), dtype=torch.float32, pin_memory=True).numpy()
     desc, keepd = sc.to_desc()
+    # a one-call render builds the scene every frame: its context is tuned for
+    # build + frame (the device-resident number above for the frame alone)
+    e2e_knobs = _knobs(args)
+    if e2e_knobs is None and not args.no_e2e:
+        from umbreon_gb300.autotune import autotune
+        e2e_knobs = autotune(sc, opt, device=local, pixels=512 * 512, objective="frame")["context"]
+    ectx = Context(local, **e2e_knobs) if not args.no_e2e else ctx
+    if not args.no_e2e:  # warm-up: pool growth, graph capture
+        hw = C.c_void_p()
+        ectx._check(ectx._L.ubr_scene_build(ectx.handle, C.byref(desc), C.byref(hw)))
+        frw = abi.Frame()
+        frw.memory = abi.MEMORY_HOST
+        frw.color = abi.ptr(host_color)
+        ectx._check(ectx._L.ubr_render(ectx.handle, hw, C.byref(rd), C.byref(frw), None, None))
+        ectx._L.ubr_scene_release(hw)
     h2d = sum(a.nbytes for a in keepd)
     e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 5))
     e2e_rays = 0
@@ -558,25 +573,27 @@ def run_ours(args):
     for _ in range(e2e_steps):
         h = C.c_void_p()
         tb = time.perf_counter()
-        ctx._check(ctx._L.ubr_scene_build(ctx.handle, C.byref(desc), C.byref(h)))
+        ectx._check(ectx._L.ubr_scene_build(ectx.handle, C.byref(desc), C.byref(h)))
         t_build += time.perf_counter() - tb
         si = abi.SceneInfo()
-        ctx._L.ubr_scene_get_info(h, C.byref(si))
+        ectx._L.ubr_scene_get_info(h, C.byref(si))
         t_flat += si.flatten_ms
         t_up += si.upload_ms
         fr = abi.Frame()
         fr.memory = abi.MEMORY_HOST
         fr.color = abi.ptr(host_color)
-        ctx._check(ctx._L.ubr_render(ctx.handle, h, C.byref(rd), C.byref(fr), None, None))
+        ectx._check(ectx._L.ubr_render(ectx.handle, h, C.byref(rd), C.byref(fr), None, None))
         e2e_rays += fr.rays_primary + fr.rays_occlusion
-        ctx._L.ubr_scene_release(h)
+        ectx._L.ubr_scene_release(h)
     e2e_s = max(time.perf_counter() - t0, 1e-9)
+    if ectx is not ctx:
+        ectx.close()
     e2e = None if args.no_e2e else {"value": round(e2e_rays * ws / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(host_color.nbytes), "ms_per_step": round(e2e_s / max(1, e2e_steps) * 1e3, 2),
            "scene_build_ms_per_step": round(t_build / max(1, e2e_steps) * 1e3, 2),
            "of_which_flatten_ms": round(t_flat / max(1, e2e_steps), 2),
            "of_which_upload_ms": round(t_up / max(1, e2e_steps), 2),
-           "steps": e2e_steps}
+           "steps": e2e_steps, "traversal": e2e_knobs}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
