@@ -3,6 +3,7 @@
 // test_render_shadows_gi.cpp), group-alpha blending and async/cancel, written
 // against the unchanged public API.
 #include <chrono>
+#include <cmath>
 #include <stdexcept>
 #include <vector>
 
@@ -167,6 +168,43 @@ int main() {
     for (float v : f.aaMask) none = none && v == 0.0f;
     c("flat quad: mask of 25 zeros", none);
     c("adaptive centre = grid colour", near(f.color[kC], grid.color[kC], 1e-6f));
+  }
+  {  // principled materials render through the drop-in: metallic = 0 and
+     // specular = 0 is the POV diffuse-only image bitwise; a metal differs
+    umbreon::Scene pov;
+    pov.mesh = quad({0.5f, 0.6f, 0.7f, 1.0f});
+    pov.mesh.material.specular = 0.0f;
+    pov.camera = cam();
+    pov.lights.push_back(key());
+    umbreon::Scene pbr = pov;
+    pbr.mesh.material.model = umbreon::ShadingModel::Principled;
+    pbr.mesh.material.pbr.metallic = 0.0f;
+    pbr.mesh.material.pbr.specular = 0.0f;
+    const umbreon::FrameResult a = umbreon::render(pov, o5()), b = umbreon::render(pbr, o5());
+    bool same = a.color.size() == b.color.size();
+    for (std::size_t i = 0; same && i < a.color.size(); ++i) same = a.color[i] == b.color[i];
+    c("principled diffuse-only == POV diffuse-only (bitwise)", same);
+    umbreon::Scene metal = pbr;
+    metal.mesh.material.pbr.metallic = 1.0f;
+    metal.mesh.material.pbr.specular = 0.5f;
+    metal.mesh.material.pbr.roughness = 0.3f;
+    const umbreon::FrameResult m = umbreon::render(metal, o5());
+    c("principled metal differs and stays finite", m.color[kC] != a.color[kC] && std::isfinite(m.color[kC]));
+  }
+  {  // coarse-grid AO through the drop-in: the fallback mask is hi-res
+    umbreon::Scene sc;
+    sc.mesh = quad({0.8f, 0.8f, 0.8f, 1.0f});
+    sc.camera = cam();
+    sc.lights.push_back(key());
+    umbreon::RenderOptions o = o5();
+    o.supersample = 2;
+    o.aoSamples = 8;
+    o.aoDistance = 2.0f;
+    o.aoResDiv = -1;
+    o.aoResDebug = true;
+    const umbreon::FrameResult f = umbreon::render(sc, o);
+    c("coarse AO: patch mask at render resolution", f.aoPatchMask.size() == 100);
+    c("coarse AO: open quad stays lit", f.color[kC] > 0.3f);
   }
   {  // unsupported requests throw like the reference's failures
     umbreon::Scene sc;

@@ -2020,6 +2020,9 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     UBR_CUDA(c, cudaGetLastError());
     return UBR_OK;
   };
+  // a cancel raised before the call renders nothing (embree_renderer.cpp:
+  // 1395-1398 bails before the first chunk of rows)
+  if (cancel && *cancel) return setError(c, UBR_CANCELLED, "render cancelled");
   cudaEventRecord(c->ev[0], s);
   if (!lights.empty())
     UBR_CUDA(c, cudaMemcpyAsync(dl, lights.data(), lights.size() * sizeof(LightD), cudaMemcpyHostToDevice, s));
