@@ -210,6 +210,11 @@ typedef struct ubr_render_desc {
    * normal / depth guides, falling back to its own AO rays where the guides
    * reject; -1 = the supersample factor; 0 or 1 = AO rays at every hit */
   int32_t ao_res_div;
+  /* the stroke-edge pass's first-hit G-buffer (RenderOptions::strokeEdges
+   * enables it in the reference, transparency.hpp:394-428, 470-481): fills
+   * the gb_* planes of ubr_frame; the edge pass itself is the caller's.
+   * Not with adaptive AA or in a batch (UBR_INVALID_ARGUMENT). */
+  uint32_t edge_gbuffer;
 } ubr_render_desc;
 
 /* Where a frame's buffers live. */
@@ -276,6 +281,20 @@ typedef struct ubr_frame {
    * AO (FrameResult::aoPatchMask with aoResDebug); written when the coarse
    * grid is active */
   float* ao_patch_mask;
+  /* edge G-buffer, hi-res, written when edge_gbuffer = 1 (FrameResult::
+   * objectId / materialId / normal / surfAlpha / clipCut / clipNearVz /
+   * clipFarVz): (section << 2) | kind and the global material index of the
+   * first hit (0xFFFFFFFF on background), its shading normal (3 per pixel)
+   * and opacity; with clip planes set, 1 where a backface first hit has its
+   * clipped-away front confirmed, and on background pixels the view z of
+   * the first surface removed in front of the near / beyond the far plane */
+  uint32_t* gb_object_id;
+  uint32_t* gb_material_id;
+  float* gb_normal;
+  float* gb_surf_alpha;
+  uint8_t* gb_clip_cut;
+  float* gb_clip_near_vz;
+  float* gb_clip_far_vz;
 } ubr_frame;
 
 /* Context: one GPU, one CUDA stream, one device arena.  Scenes and frame

@@ -157,7 +157,7 @@ class OracleScene:
         r0, r1 = rows if rows else (0, 0)
         st = lib().oracle_render_rows(self.h, C.byref(rd), C.byref(fr), threads, r0, r1)
         if st != 0:
-            raise RuntimeError("oracle: unsupported request (Principled material)")
+            raise RuntimeError("oracle: unsupported request (adaptive AA with the edge G-buffer)")
         stats = dict(render_ms=fr.render_ms, rays_primary=fr.rays_primary, capped_rays=fr.capped_rays)
         return FrameResult(opt.width, opt.height, color, depth, vz, hg, hp, fr.render_ms / 1e3, stats, **aovs)
 

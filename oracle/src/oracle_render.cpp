@@ -77,6 +77,7 @@ struct Scene {
   // mesh (scene_build.cpp:16-88): attributes per baked vertex
   std::vector<float> nrm, col;
   size_t baseTri = 0;
+  uint32_t baseSpheres = 0;      // Scene::spheres.size() (edge materialId block)
   std::vector<Mat> meshMats;     // Mesh::materials
   Mat meshMat{};
   std::vector<uint8_t> triMat;   // per base triangle
@@ -233,6 +234,7 @@ Scene* buildScene(const ubr_scene_desc& d) {
     if (d.mesh_tri_group) s->triGroup.assign(d.mesh_tri_group, d.mesh_tri_group + baseT);
   }
   // spheres (scene_build.cpp:91-129)
+  s->baseSpheres = static_cast<uint32_t>(d.sphere_count);
   if (d.sphere_count > 0) {
     s->geo.geomID[kSphere] = nextGeom++;
     for (const V3& off : offs)
@@ -463,6 +465,7 @@ struct Opt {  // the RenderOptions fields this path reads
   float specularScale; bool transparency, transparentBackground; int maxTransparentLayers;
   bool aoWriteAov = false;
   int aaMode = 0;
+  bool edgeGbuffer = false;  // capture the stroke-edge pass's first-hit G-buffer
   bool aoEnhanced() const {  // render_options.hpp:79-82
     return aoFalloffPower > 0.0f || aoMultiScale || aoBentNormal || aoMultibounce || aoLowDiscrepancy ||
            aoDiffuseFactor > 0.0f;
@@ -844,6 +847,9 @@ struct HitShade {
   float contact = 1.0f, shape = 1.0f, avgHit = 0.0f;
   int group = 0;  // CueMol section of the hit (hit_shader.hpp:277, 457)
   uint8_t aoPatched = 0;  // coarse-grid AO fell back to the inline gather (hit_shader.hpp:60)
+  // edge G-buffer (hit_shader.hpp:278-300, 460-478): (section << 2) | kind and
+  // the global material index; background sentinels
+  uint32_t objectId = 0xFFFFFFFFu, materialId = 0xFFFFFFFFu;
 };
 
 // hit_shader.hpp:147-496 shadeHit (POV and principled direct; GI / edge branches off)
@@ -891,6 +897,11 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
       hs.normal = N;
     }
     hs.group = s.triGroup.empty() ? 0 : s.triGroup[s.baseTri ? hit.primID % s.baseTri : hit.primID];
+    if (c.o.edgeGbuffer) {
+      hs.normal = N;
+      hs.objectId = (static_cast<uint32_t>(hs.group) << 2) | static_cast<uint32_t>(kMesh);
+      hs.materialId = s.triMat.empty() ? 0u : static_cast<uint32_t>(s.triMat[hit.primID % s.triMat.size()]);
+    }
   } else {
     const float* fc = &s.color[kind][4 * hit.primID];
     const Mat& pm = s.mat[kind][hit.primID];
@@ -950,6 +961,16 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
     hs.opacity = fc[3];
     hs.group = s.group[kind][hit.primID];
     if (c.o.aaMode == 1) hs.normal = N;  // hit_shader.hpp:321
+    if (c.o.edgeGbuffer) {
+      // global materialId: per-kind blocks after the mesh materials, the raw
+      // primitive index inside (scene_build.cpp:104-123, curve_build.cpp:154-179)
+      hs.normal = N;
+      hs.objectId = (static_cast<uint32_t>(hs.group) << 2) | static_cast<uint32_t>(kind);
+      const uint32_t meshMats = static_cast<uint32_t>(s.meshMats.size());
+      if (kind == kSphere) hs.materialId = meshMats + hit.primID;
+      else if (kind == kRound) hs.materialId = meshMats + s.baseSpheres + hit.primID;
+      else hs.materialId = meshMats + s.baseSpheres + static_cast<uint32_t>(s.geo.rcIdx.size()) + hit.primID;
+    }
     if (kind != kSphere) {
       const float op1 = s.opacity1[kind][hit.primID];
       if (op1 >= 0.0f) {
@@ -969,7 +990,29 @@ struct PixelOut {
   bool capped;
   uint32_t rays;
   HitShade first;  // AOVs of the first hit (neutral values on a miss)
+  // clip-cut G-buffer (transparency.hpp:424-428, 470-481)
+  uint8_t clipCut = 0;
+  float clipNearVz = 0.0f, clipFarVz = 0.0f;
 };
+
+// transparency.hpp:131-186: backface test, the any-hit confirmation of a
+// clipped-away front, the first hit of a t range as view z
+inline bool clipConfirmFront(const Scene& s, const V3& org, const V3& rd, float tMax) {
+  Ray r;
+  r.org = org; r.dir = rd;
+  r.tnear = std::max(1.0e-4f, 1.0e-4f * tMax);
+  r.tfar = tMax * (1.0f - 1.0e-4f);
+  if (r.tnear >= r.tfar) return false;
+  return s.bvh.occluded(r);
+}
+inline float clipProbeRange(const Scene& s, const V3& org, const V3& rd, const V3& camDir, float t0, float t1) {
+  if (t0 >= t1) return 0.0f;
+  Ray r;
+  r.org = org; r.dir = rd; r.tnear = t0; r.tfar = t1;
+  Hit h;
+  if (!s.bvh.closest(r, h)) return 0.0f;
+  return h.t * dot(rd, camDir);
+}
 
 // transparency.hpp:311-522 integratePixel (colour, first-hit depth/viewZ/ids)
 inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32_t px, uint32_t py,
@@ -984,9 +1027,11 @@ inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32
   float baseCov = c.o.transparentBackground ? 0.0f : 1.0f;
   // clipRangeT (transparency.hpp:118-129)
   float ctn = 0.0f, ctf = kInf;
+  bool clipOn = false;
   if (!(c.clipNear <= -kInf && c.clipFar >= kInf)) {
     const float cosr = dot(rd, camDir);
     if (!(cosr <= 1.0e-6f)) {
+      clipOn = true;
       if (c.clipNear > 0.0f) ctn = c.clipNear / cosr;
       if (c.clipFar < kInf) ctf = c.clipFar / cosr;
     }
@@ -1007,6 +1052,10 @@ inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32
       po.geom = h.geomID;
       po.prim = h.primID;
       po.first = hs;
+      // a backface first hit whose clipped-away front exists (:424-428)
+      if (clipOn && ctn > 0.0f && c.o.edgeGbuffer && dot(h.Ng, rd) > 0.0f &&
+          clipConfirmFront(*c.s, org, rd, ctn))
+        po.clipCut = 1;
     }
     if (!c.o.transparency || hs.opacity >= kOpaque) {
       base = hs.color;
@@ -1025,6 +1074,12 @@ inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32
                                      std::fmax(std::fabs(hitP.z), dirMax * h.t));
     tnear = h.t + epsScale * 0x1.0fp-21f;
     if (iter == maxIters - 1) po.capped = true;
+  }
+  // background under clipping: what the planes removed along the ray (:470-481)
+  if (clipOn && c.o.edgeGbuffer && nearDepth == 0.0f) {
+    if (ctn > 0.0f)
+      po.clipNearVz = clipProbeRange(*c.s, org, rd, camDir, std::max(1.0e-4f, 1.0e-6f * ctn), ctn * (1.0f - 1.0e-6f));
+    if (ctf < kInf) po.clipFarVz = clipProbeRange(*c.s, org, rd, camDir, ctf * (1.0f + 1.0e-6f), kInf);
   }
   const float floorW = (1.0f - Af) * baseCov;
   float outA = Af + floorW;
@@ -1305,6 +1360,7 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   c.o.maxTransparentLayers = d.max_transparent_layers;
   c.o.aoWriteAov = d.ao_write_aov != 0;
   c.o.aaMode = d.aa_mode;
+  c.o.edgeGbuffer = d.edge_gbuffer != 0;
   // buildSceneLights (embree_renderer.cpp:436-458)
   for (uint32_t i = 0; i < d.light_count; ++i) {
     const ubr_light& dl = d.lights[i];
@@ -1370,6 +1426,19 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
     hg[pix] = po.geom;
     hp[pix] = po.prim;
     if (patchMask) patchMask[pix] = static_cast<float>(po.first.aoPatched);
+    if (c.o.edgeGbuffer) {  // storeGBufChannels (embree_renderer.cpp:240-262)
+      if (fr->gb_object_id) fr->gb_object_id[pix] = po.first.objectId;
+      if (fr->gb_material_id) fr->gb_material_id[pix] = po.first.materialId;
+      if (fr->gb_surf_alpha) fr->gb_surf_alpha[pix] = po.geom == kInvalid ? 1.0f : po.first.opacity;
+      if (fr->gb_normal) {
+        fr->gb_normal[3 * pix] = po.first.normal.x;
+        fr->gb_normal[3 * pix + 1] = po.first.normal.y;
+        fr->gb_normal[3 * pix + 2] = po.first.normal.z;
+      }
+      if (fr->gb_clip_cut) fr->gb_clip_cut[pix] = po.clipCut;
+      if (fr->gb_clip_near_vz) fr->gb_clip_near_vz[pix] = po.clipNearVz;
+      if (fr->gb_clip_far_vz) fr->gb_clip_far_vz[pix] = po.clipFarVz;
+    }
     if (aov) {
       const HitShade& f = po.first;
       const float a3[3][3] = {{f.albedo.x, f.albedo.y, f.albedo.z}, {f.normal.x, f.normal.y, f.normal.z},
@@ -1508,6 +1577,9 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   // soft-shadow samples; aaDepth > ss shades each flagged cell as the box
   // average of kFine^2 samples of a finer lattice (:1542-1590).
   const bool adaptive = d.aa_mode == 1 && (ss > 1 || d.aa_depth > 1) && W % ss == 0 && H % ss == 0;
+  // adaptive AA with the edge G-buffer probes replicated subpixels
+  // (embree_renderer.cpp:1611-1640); not restated
+  if (adaptive && d.edge_gbuffer) return -3;
   if (adaptive) {
     const int Wf = W / ss, Hf = H / ss, cSub = ss / 2;
     const int kFine = std::max(1, (d.aa_depth + ss - 1) / ss);

@@ -671,6 +671,21 @@ def case_clip_planes():
             (_clip_scene(near=10.0), o5())], check
 
 
+def case_clip_cut_gbuffer():
+    """test_clip_planes.cpp:52-96 with the edge G-buffer on."""
+    def check(fs):
+        near10, far8, near12 = fs
+        return [("clipNear 10: interior back wall flagged clip-cut", int(near10.clipCut[2, 2]) == 1),
+                ("clipNear 10: corner miss ray unflagged", int(near10.clipCut[0, 0]) == 0),
+                ("clipNear 10: corner records no removed hit",
+                 near10.clipNearVz[0, 0] == 0.0 and near10.clipFarVz[0, 0] == 0.0),
+                ("clipFar 8: removed hit (view z 9) beyond the plane", approx(far8.clipFarVz[2, 2], 9.0, 1e-2)),
+                ("clipFar 8: nothing recorded in front of a near plane", far8.clipNearVz[2, 2] == 0.0),
+                ("clipNear 12: removed hit in front of the plane", approx(near12.clipNearVz[2, 2], 9.0, 1e-2))]
+    g = o5(edgeGBuffer=True)
+    return [(_clip_scene(near=10.0), g), (_clip_scene(far=8.0), g), (_clip_scene(near=12.0), g)], check
+
+
 # --- indexed mesh (test_mesh_indexed.cpp:23-93) ---
 
 def case_mesh_indexed_equals_deindexed():

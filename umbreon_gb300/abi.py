@@ -105,6 +105,7 @@ class RenderDesc(C.Structure):
         ("transparent_background", C.c_uint32), ("max_transparent_layers", C.c_int32),
         ("gi_integrator", C.c_int32), ("ao_write_aov", C.c_uint32), ("aa_mode", C.c_int32),
         ("aa_threshold", C.c_float), ("aa_depth", C.c_int32), ("ao_res_div", C.c_int32),
+        ("edge_gbuffer", C.c_uint32),
     ]
 
 
@@ -118,6 +119,8 @@ class Frame(C.Structure):
         ("node_bytes", C.c_uint64 * 2), ("prim_bytes", C.c_uint64 * 2), ("nodes_visited", C.c_uint64 * 2),
         ("albedo", f32p), ("normal", f32p), ("bent_normal", f32p), ("contact_ao", f32p), ("shape_ao", f32p),
         ("avg_hit_dist", f32p), ("aa_mask", f32p), ("ao_patch_mask", f32p),
+        ("gb_object_id", u32p), ("gb_material_id", u32p), ("gb_normal", f32p), ("gb_surf_alpha", f32p),
+        ("gb_clip_cut", C.POINTER(C.c_uint8)), ("gb_clip_near_vz", f32p), ("gb_clip_far_vz", f32p),
     ]
 
 

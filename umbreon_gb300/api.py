@@ -215,6 +215,7 @@ class RenderOptions:
     aaDebug: bool = False
     aoResDiv: int = 0        # coarse-grid AO divisor (-1 = supersample factor; 0 / 1 = per hit)
     aoResDebug: bool = False  # return the coarse-AO fallback mask
+    edgeGBuffer: bool = False  # return the stroke-edge pass's first-hit G-buffer (hi-res)
 
     def aoEnhanced(self) -> bool:
         return (self.aoFalloffPower > 0.0 or self.aoMultiScale or self.aoBentNormal or self.aoMultibounce
@@ -281,6 +282,7 @@ def make_render_desc(scene: Scene, opt: RenderOptions):
     d.ao_write_aov = int(opt.aoWriteAov)
     d.aa_mode, d.aa_threshold, d.aa_depth = opt.aaMode, opt.aaThreshold, opt.aaDepth
     d.ao_res_div = opt.aoResDiv
+    d.edge_gbuffer = int(opt.edgeGBuffer)
     return d, keep
 
 
@@ -305,6 +307,13 @@ class FrameResult:
     avgHitDist: np.ndarray = None  # (H, W)
     aaMask: np.ndarray = None      # (H, W) adaptive-AA refinement mask (aaDebug)
     aoPatchMask: np.ndarray = None  # (Hss, Wss) coarse-AO fallback mask (aoResDebug)
+    objectId: np.ndarray = None     # (Hss, Wss) edge G-buffer (edgeGBuffer): (section << 2) | kind
+    materialId: np.ndarray = None   # (Hss, Wss) global material index
+    gbNormal: np.ndarray = None     # (Hss, Wss, 3) first-hit shading normal
+    surfAlpha: np.ndarray = None    # (Hss, Wss) first-hit opacity
+    clipCut: np.ndarray = None      # (Hss, Wss) uint8
+    clipNearVz: np.ndarray = None   # (Hss, Wss)
+    clipFarVz: np.ndarray = None    # (Hss, Wss)
 
 
 AOV_FIELDS = (("albedo", "albedo", 3), ("normal", "normal", 3), ("bentNormal", "bent_normal", 3),
@@ -321,6 +330,17 @@ def attach_aovs(fr, opt) -> dict:
     if opt.aoResDebug and div > 1 and opt.aoSamples > 0:
         out["aoPatchMask"] = np.zeros((opt.height * ss, opt.width * ss), np.float32)
         fr.ao_patch_mask = abi.ptr(out["aoPatchMask"])
+    if opt.edgeGBuffer:
+        hw = (opt.height * ss, opt.width * ss)
+        planes = (("objectId", "gb_object_id", np.uint32, ()), ("materialId", "gb_material_id", np.uint32, ()),
+                  ("gbNormal", "gb_normal", np.float32, (3,)), ("surfAlpha", "gb_surf_alpha", np.float32, ()),
+                  ("clipCut", "gb_clip_cut", np.uint8, ()), ("clipNearVz", "gb_clip_near_vz", np.float32, ()),
+                  ("clipFarVz", "gb_clip_far_vz", np.float32, ()))
+        for name, cname, dt, tail in planes:
+            a = np.zeros(hw + tail, dt)
+            out[name] = a
+            ctype = {np.uint32: C.c_uint32, np.uint8: C.c_uint8}.get(dt, C.c_float)
+            setattr(fr, cname, a.ctypes.data_as(C.POINTER(ctype)))
     if opt.aaMode == 1 and opt.aaDebug:
         out["aaMask"] = np.zeros((opt.height, opt.width), np.float32)
         fr.aa_mask = abi.ptr(out["aaMask"])

@@ -59,6 +59,14 @@ struct Bufs {
   const float4* cgB;      //   bent normal.xyz (quality estimator only, else null)
   const uint8_t* cgHit;   //   1 = AO-eligible first hit
   float* aoPatch;         // per hi-res pixel (or null): 1 = the first hit gathered its own AO
+  // edge G-buffer per hi-res pixel (or null), in the ubr_frame plane layouts
+  uint32_t* gbObj;
+  uint32_t* gbMat;
+  float* gbNrm;           // 3 per pixel
+  float* gbAlpha;
+  uint8_t* gbClip;        // 0, 1, or 2 = backface first hit awaiting the front check
+  float* gbNear;
+  float* gbFar;
   const LightD* lights;
   unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
   uint32_t* counter;  // [0] next-queue size, [1] occlusion work-queue size
@@ -944,6 +952,29 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
           b.aaN[gpix] = make_float4(sf.N.x, sf.N.y, sf.N.z, __int_as_float(grp));
         }
         if (b.aoPatch) b.aoPatch[gpix] = patched ? 1.0f : 0.0f;
+        if (b.gbObj) {
+          // edge G-buffer (hit_shader.hpp:278-300, 460-478; transparency.hpp:394-428)
+          uint32_t grp = 0, mat;
+          if (sf.kind == kMesh) {
+            const uint32_t bt = s.baseTri ? sf.prim % s.baseTri : sf.prim;
+            if (s.meshTriGroup) grp = __ldg(&s.meshTriGroup[bt]);
+            mat = s.meshTriMatId ? uint32_t(__ldg(&s.meshTriMatId[bt])) : 0u;
+          } else {
+            if (s.primGroup[sf.kind]) grp = __ldg(&s.primGroup[sf.kind][sf.prim]);
+            mat = s.meshMatCount + sf.prim;
+            if (sf.kind != kSphere) mat += s.baseSpheres;
+            if (sf.kind == kCone) mat += s.roundCount;
+          }
+          b.gbObj[gpix] = (grp << 2) | uint32_t(sf.kind);
+          b.gbMat[gpix] = mat;
+          b.gbNrm[3 * size_t(gpix)] = sf.N.x;
+          b.gbNrm[3 * size_t(gpix) + 1] = sf.N.y;
+          b.gbNrm[3 * size_t(gpix) + 2] = sf.N.z;
+          b.gbAlpha[gpix] = sf.opacity;
+          float ctn, ctf;
+          clipRange(p, rd, ctn, ctf);
+          if (b.gbClip && clipOn(p, rd) && ctn > 0.0f && dot(sf.Ng, rd) > 0.0f) b.gbClip[gpix] = 2;
+        }
         b.depth[gpix] = t;
         b.viewZ[gpix] = t * dot(rd, p.camDir);
         b.hitGeom[gpix] = s.geomID[sf.kind];
@@ -1414,6 +1445,67 @@ __global__ void k_cao_finish(Params pc, Bufs b, const uint8_t* cgHit, float4* cg
   if (cgB) cgB[cell] = make_float4(q.bent.x, q.bent.y, q.bent.z, 0.0f);
 }
 
+// ---- Edge G-buffer (transparency.hpp:131-186, 394-428, 470-481) ----
+__global__ void k_gb_init(uint32_t npix, Bufs b) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  b.gbObj[i] = kInvalid;
+  b.gbMat[i] = kInvalid;
+  b.gbNrm[3 * size_t(i)] = 0.0f;
+  b.gbNrm[3 * size_t(i) + 1] = 0.0f;
+  b.gbNrm[3 * size_t(i) + 2] = 0.0f;
+  b.gbAlpha[i] = 1.0f;
+  if (b.gbClip) {
+    b.gbClip[i] = 0;
+    b.gbNear[i] = 0.0f;
+    b.gbFar[i] = 0.0f;
+  }
+}
+
+// With clip planes: a backface first hit is a clip-cut interior when an
+// any-hit ray finds the clipped-away front over [max(1e-4, 1e-4 tn),
+// tn (1 - 1e-4)); a background pixel records the view z of the first
+// surface removed in front of the near plane and beyond the far plane.
+template <int KM>
+__global__ void __launch_bounds__(128) k_gb_clip(Params p, DScene s, Bufs b, uint32_t npix) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  const int px = int(i % uint32_t(p.W)), py = int(i / uint32_t(p.W));
+  f3 org, rd;
+  primaryRay(p, px, py, org, rd);
+  if (!clipOn(p, rd)) return;
+  float ctn, ctf;
+  clipRange(p, rd, ctn, ctf);
+  const TravScene ts = travOf(s);
+  uint32_t ovf = 0;
+  Count cnt;
+  if (b.gbClip[i] == 2) {
+    const float tn = fmaxf(1.0e-4f, 1.0e-4f * ctn), tf = ctn * (1.0f - 1.0e-4f);
+    bool front = false;
+    if (tn < tf) {
+      Hit h;
+      front = traverse<false, KM>(ts, Ray{org, rd, tn, tf}, h, ovf, &cnt, true);
+    }
+    b.gbClip[i] = front ? 1 : 0;
+  } else if (b.hitGeom[i] == kInvalid) {
+    const float camCos = dot(rd, p.camDir);
+    if (ctn > 0.0f) {
+      const float t0 = fmaxf(1.0e-4f, 1.0e-6f * ctn), t1 = ctn * (1.0f - 1.0e-6f);
+      if (t0 < t1) {
+        Hit h;
+        if (traverse<false, KM>(ts, Ray{org, rd, t0, t1}, h, ovf, &cnt, false)) b.gbNear[i] = h.t * camCos;
+      }
+    }
+    if (ctf < kInfF) {
+      const float t0 = ctf * (1.0f + 1.0e-6f);
+      if (t0 < kInfF) {
+        Hit h;
+        if (traverse<false, KM>(ts, Ray{org, rd, t0, kInfF}, h, ovf, &cnt, false)) b.gbFar[i] = h.t * camCos;
+      }
+    }
+  }
+}
+
 }  // namespace
 
 // Host-side parameter setup: computeCameraBasis (embree_renderer.cpp:375-386),
@@ -1644,6 +1736,16 @@ int kindMask(const Scene& sc) { return roundKindMask(kindMaskBits(sc)); }
     }                                                                                                        \
   } while (0)
 
+// kind-mask dispatch of a kernel templated on the mask alone
+#define UBR_KM_DISPATCH1(KERNEL, km, grid, tb, stream, ...)                                   \
+  do {                                                                                      \
+    switch (km) {                                                                           \
+      case kMaskMesh: KERNEL<kMaskMesh><<<grid, tb, 0, stream>>>(__VA_ARGS__); break;       \
+      case kMaskSphere: KERNEL<kMaskSphere><<<grid, tb, 0, stream>>>(__VA_ARGS__); break;   \
+      default: KERNEL<kMaskAll><<<grid, tb, 0, stream>>>(__VA_ARGS__);                      \
+    }                                                                                       \
+  } while (0)
+
 void launchClosest(int km, bool count, bool batch, uint32_t grid, int tb, cudaStream_t st, const Params& p,
                    const DScene& s, const Batch& bt, const Bufs& b, int layer, uint32_t n, const uint32_t* queue) {
   UBR_KM_DISPATCH(k_trace_closest, km, count, batch, grid, tb, st, p, s, bt, b, layer, n, queue);
@@ -1838,6 +1940,24 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       pCoarse.nLights = 0;
     }
   }
+  // edge G-buffer (one frame per call, grid frames)
+  for (size_t f = 0; f < nf; ++f)
+    if (jobs[f].desc->edge_gbuffer && (batch || adaptive))
+      return setError(c, UBR_INVALID_ARGUMENT,
+                      "render: the edge G-buffer needs a single grid frame (no batch, no adaptive AA)");
+  const bool edgeGb = !batch && d0.edge_gbuffer != 0;
+  const bool clipPlanes = !(p1.clipNear <= -kInfF && p1.clipFar >= kInfF);
+  if (edgeGb) {
+    b.gbObj = scratchT<uint32_t>(c, 98, npix, st);
+    b.gbMat = scratchT<uint32_t>(c, 99, npix, st);
+    b.gbNrm = scratchT<float>(c, 100, size_t(npix) * 3, st);
+    b.gbAlpha = scratchT<float>(c, 101, npix, st);
+    if (clipPlanes) {
+      b.gbClip = scratchT<uint8_t>(c, 102, npix, st);
+      b.gbNear = scratchT<float>(c, 103, npix, st);
+      b.gbFar = scratchT<float>(c, 104, npix, st);
+    }
+  }
   const uint32_t nCentre = uint32_t(p1.outW) * uint32_t(p1.outH);
   uint32_t *aaList0 = nullptr, *aaList1 = nullptr, *aaCounts = nullptr;
   uint8_t* aaRaw = nullptr;
@@ -2000,6 +2120,16 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     UBR_CUDA(c, cudaGetLastError());
     return UBR_OK;
   };
+  auto gbInit = [&]() {
+    if (!edgeGb) return;
+    k_gb_init<<<(npix + 255) / 256, 256, 0, s>>>(npix, b);
+    ++kernels;
+  };
+  auto gbClip = [&]() {
+    if (!edgeGb || !clipPlanes) return;
+    UBR_KM_DISPATCH1(k_gb_clip, km, (npix + 127) / 128, 128, s, p1, s1, b, npix);
+    ++kernels;
+  };
   auto post = [&]() -> ubr_status {
     mark(4, true);
     if (batch) k_post<true><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.colorHi, b.viewZ, outColor);
@@ -2147,8 +2277,10 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       cudaMemsetAsync(b.stats, 0, 8 * sizeof(unsigned long long), s);
       k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim, b.aovA,
                                                        b.aovB, b.aovC, nullptr, nullptr, b.aoPatch);
+      gbInit();
       ubr_status rs = coarsePrepass();
       if (rs == UBR_OK) rs = round(p1, b, R, 0, npix, nullptr, q0);
+      if (rs == UBR_OK) gbClip();
       if (rs == UBR_OK) rs = post();
       cudaGraph_t graph = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(s, &graph);
@@ -2177,7 +2309,8 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       cudaGraphDestroy(graph);
       c->graphKey = key;
     } else {
-      kernels = (secondary ? 4u : 2u) + 1u + (aov ? 1u : 0u);
+      kernels = (secondary ? 4u : 2u) + 1u + (aov ? 1u : 0u) + (coarseOn ? 3u : 0u) +
+                (edgeGb ? (clipPlanes ? 2u : 1u) : 0u);
     }
     cudaEventRecord(c->ev[2], s);
     UBR_CUDA(c, cudaGraphLaunch(c->graphExec, s));
@@ -2189,11 +2322,13 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     k_init_pixels<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.depth, b.viewZ, b.hitGeom, b.hitPrim, b.aovA,
                                                        b.aovB, b.aovC, b.aaN, nullptr, b.aoPatch);
     ++kernels;
+    gbInit();
     cudaEventRecord(c->ev[2], s);
     st = coarsePrepass();
     if (st != UBR_OK) return st;
     st = adaptive ? runAdaptive() : runLayers(p1, b, R, nullptr, npix);
     if (st != UBR_OK) return st;
+    if (!cancelled) gbClip();
     cudaEventRecord(c->ev[3], s);
     st = post();
     if (st != UBR_OK) return st;
@@ -2213,6 +2348,29 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     if (fr.aa_mask && aaMaskOut) UBR_CUDA(c, cudaMemcpyAsync(fr.aa_mask, aaMaskOut, fout * 4, kind, s));
     if (fr.ao_patch_mask && b.aoPatch)
       UBR_CUDA(c, cudaMemcpyAsync(fr.ao_patch_mask, b.aoPatch + po, fpix * 4, kind, s));
+    if (edgeGb) {
+      if (fr.gb_object_id) UBR_CUDA(c, cudaMemcpyAsync(fr.gb_object_id, b.gbObj, fpix * 4, kind, s));
+      if (fr.gb_material_id) UBR_CUDA(c, cudaMemcpyAsync(fr.gb_material_id, b.gbMat, fpix * 4, kind, s));
+      if (fr.gb_normal) UBR_CUDA(c, cudaMemcpyAsync(fr.gb_normal, b.gbNrm, fpix * 12, kind, s));
+      if (fr.gb_surf_alpha) UBR_CUDA(c, cudaMemcpyAsync(fr.gb_surf_alpha, b.gbAlpha, fpix * 4, kind, s));
+      if (b.gbClip) {
+        if (fr.gb_clip_cut) UBR_CUDA(c, cudaMemcpyAsync(fr.gb_clip_cut, b.gbClip, fpix, kind, s));
+        if (fr.gb_clip_near_vz) UBR_CUDA(c, cudaMemcpyAsync(fr.gb_clip_near_vz, b.gbNear, fpix * 4, kind, s));
+        if (fr.gb_clip_far_vz) UBR_CUDA(c, cudaMemcpyAsync(fr.gb_clip_far_vz, b.gbFar, fpix * 4, kind, s));
+      } else {
+        // no clip planes: nothing is cut and nothing recorded
+        if (fr.gb_clip_cut) {
+          if (fr.memory == UBR_MEMORY_DEVICE) UBR_CUDA(c, cudaMemsetAsync(fr.gb_clip_cut, 0, fpix, s));
+          else std::memset(fr.gb_clip_cut, 0, fpix);
+        }
+        float* zs[2] = {fr.gb_clip_near_vz, fr.gb_clip_far_vz};
+        for (float* z : zs) {
+          if (!z) continue;
+          if (fr.memory == UBR_MEMORY_DEVICE) UBR_CUDA(c, cudaMemsetAsync(z, 0, fpix * 4, s));
+          else std::memset(z, 0, fpix * 4);
+        }
+      }
+    }
     if (p.aoWriteAov) {
       const float* o = outAov;
       const size_t n = nout;

@@ -37,6 +37,7 @@ struct HostScene {
   std::vector<float4> col;            // per baked vertex
   std::vector<uint32_t> idx;          // 3 per triangle (baked)
   std::vector<uint32_t> triMat;       // per base triangle (material index)
+  std::vector<uint8_t> triMatId;      // per base triangle: the caller's Mesh::triMaterialId
   uint32_t meshMat = 0;
   uint32_t baseTri = 0;
   std::vector<float4> sph;            // (c, r)
@@ -305,6 +306,7 @@ ubr_status flatten(Context* c, const ubr_scene_desc& d, HostScene& s) {
       for (uint32_t i = 0; i < d.mesh_material_count; ++i) remap[i] = mt.get(d.mesh_materials[i]);
       s.triMat.resize(baseT);
       for (uint64_t t = 0; t < baseT; ++t) s.triMat[t] = remap[d.mesh_tri_material[t]];
+      s.triMatId.assign(d.mesh_tri_material, d.mesh_tri_material + baseT);
     }
   }
   if (d.sphere_count > 0) {
@@ -1181,6 +1183,11 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   if ((st = upload(c, sc, hs.col, &v.meshCol)) != UBR_OK) return fail(st);
   if ((st = upload(c, sc, hs.idx, &v.meshIdx)) != UBR_OK) return fail(st);
   if ((st = upload(c, sc, hs.triMat, &v.meshTriMat)) != UBR_OK) return fail(st);
+  if ((st = upload(c, sc, hs.triMatId, &v.meshTriMatId)) != UBR_OK) return fail(st);
+  // edge G-buffer material blocks (scene_build.cpp:151-155, 104-123; curve_build.cpp:179)
+  v.meshMatCount = uint32_t(d.mesh_material_count);
+  v.baseSpheres = uint32_t(d.sphere_count);
+  v.roundCount = uint32_t(hs.rcIdx.size());
   if ((st = upload(c, sc, hs.sph, &dsph)) != UBR_OK) return fail(st);
   v.sph = dsph;
   v.baseSph = hs.baseSph;

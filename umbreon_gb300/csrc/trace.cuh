@@ -45,6 +45,13 @@ UBR_D void clipRange(const Params& p, f3 rd, float& tn, float& tf) {
   if (p.clipFar < kInfF) tf = p.clipFar / cosr;
 }
 
+// clipRangeT's `on` (transparency.hpp:118-129): clip planes set and the ray
+// not degenerate or backward
+UBR_D bool clipOn(const Params& p, f3 rd) {
+  if (p.clipNear <= -kInfF && p.clipFar >= kInfF) return false;
+  return !(dot(rd, p.camDir) <= 1.0e-6f);
+}
+
 UBR_D bool slabHit(float lox, float hix, float loy, float hiy, float loz, float hiz, const f3& o,
                    const f3& inv, float tnear, float tmax, float& tEntry) {
   const float t0x = (lox - o.x) * inv.x, t1x = (hix - o.x) * inv.x;

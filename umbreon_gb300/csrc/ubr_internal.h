@@ -113,6 +113,10 @@ struct DScene {
   const float4* meshCol = nullptr;     // per vertex
   const uint32_t* meshIdx = nullptr;   // 3 per triangle
   const uint32_t* meshTriMat = nullptr;// per base triangle -> material table index
+  const uint8_t* meshTriMatId = nullptr;  // per base triangle: the caller's material id (or null)
+  uint32_t meshMatCount = 0;           // Mesh::materials.size()
+  uint32_t baseSpheres = 0;            // Scene::spheres.size()
+  uint32_t roundCount = 0;             // open-cylinder segments (all instances)
   uint32_t meshMat = 0;                // when meshTriMat == nullptr
   uint32_t baseTri = 0;
   // per-kind side tables (primID order); index 0 unused
