@@ -183,3 +183,25 @@ def test_fine_lattice_at_ss1_equals_ss2_grid(gpu_ctx):
     assert m.any() and (~m).any()
     assert np.array_equal(ad.color[m], grid2.color[m])
     assert np.array_equal(ad.color[~m], grid1.color[~m])
+
+
+def test_boosted_centres_reuse_centre_ao(gpu_ctx):
+    """Opaque frames with the tea2 AO stream: the boosted centre copies its
+    first aoSamples AO results from the centre pass instead of tracing them.
+    Same image as the persistent occlusion kernel (which traces them all),
+    with fewer occlusion rays."""
+    from umbreon_gb300.api import Context
+    sc, opt = scenes.molecular_surface(n_atoms=600, box=16.0, n_spheres=300, width=96, height=96,
+                                       ao_samples=8, layers=2)
+    sc.mesh_colors = sc.mesh_colors.copy()
+    sc.mesh_colors[:, 3] = 1.0  # opaque: one layer
+    opt.supersample = 2
+    a = _adaptive(opt)
+    traced = Context(0, trace_mode=2)
+    try:
+        full = _render(traced, sc, a)
+    finally:
+        traced.close()
+    reused = _render(gpu_ctx, sc, a)
+    assert np.array_equal(reused.color, full.color)
+    assert reused.stats["rays_occlusion"] < full.stats["rays_occlusion"]

@@ -67,6 +67,11 @@ struct Bufs {
   uint8_t* gbClip;        // 0, 1, or 2 = backface first hit awaiting the front check
   float* gbNear;
   float* gbFar;
+  // AO results of an earlier pass over the same hits (adaptive AA's boosted
+  // centres), indexed by output pixel: ray j of output pixel o at o * reuseR + j
+  const uint8_t* reuseOcc;
+  const float* reuseAoT;  // stride Params::reuseAo
+  uint32_t reuseR;
   const LightD* lights;
   unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
   uint32_t* counter;  // [0] next-queue size, [1] occlusion work-queue size
@@ -375,7 +380,15 @@ __global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p1, DScene s1
     const int f = BATCH ? int(sc.y >> 8) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
-    if (j < p.raysPerHit) {
+    if (!BATCH && b.reuseOcc && j < p.reuseAo && (sc.y & 2u)) {
+      // the same AO ray (origin, direction, range) was traced by the centre
+      // pass: copy its result
+      const uint32_t pix = latticeOf(b, sc.x);
+      const uint32_t px = pix % uint32_t(p.W), py = pix / uint32_t(p.W);
+      const uint64_t o = uint64_t(py / uint32_t(p.ss)) * uint32_t(p.outW) + px / uint32_t(p.ss);
+      b.occ[uint64_t(slot) * R + j] = b.reuseOcc[o * b.reuseR + j];
+      if (p.aoEnhanced || p.aoWriteAov) b.aoT[uint64_t(slot) * aoStride + j] = b.reuseAoT[o * uint64_t(p.reuseAo) + j];
+    } else if (j < p.raysPerHit) {
       const OccRay o = occlusionRay(p, b, slot, BATCH ? sc.x - bt.frames[f].pixOff : latticeOf(b, sc.x), sc.y, j);
       bool hit = false;
       Hit h;
@@ -1963,6 +1976,8 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   uint8_t* aaRaw = nullptr;
   float* aaMaskOut = nullptr;
   Params pBoost{}, pFine{};
+  uint8_t* reuseOccBuf = nullptr;
+  float* reuseAoTBuf = nullptr;
   std::vector<LightD> lightsBoost;
   LightD* dlBoost = nullptr;
   bool needBoost = false;
@@ -1990,6 +2005,15 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       pBoost.aoCoarse = p1.aoCoarse;
       pBoost.cgW = p1.cgW;
       pBoost.cgH = p1.cgH;
+      // the boosted centre's first aoSamples AO rays are the centre pass's
+      // own (the tea2 stream does not depend on the sample count; the
+      // low-discrepancy set does): copy them instead of tracing, for single
+      // layer frames and the per-ray occlusion kernel
+      if (p1.aoSamples > 0 && !p1.aoLowDiscrepancy && !coarseOn && singleLayer && c->traceMode == 1) {
+        pBoost.reuseAo = p1.aoSamples;
+        reuseOccBuf = scratchT<uint8_t>(c, 105, size_t(nCentre) * R, st);
+        if (p1.aoEnhanced || p1.aoWriteAov) reuseAoTBuf = scratchT<float>(c, 106, size_t(nCentre) * p1.aoSamples, st);
+      }
       dlBoost = scratchT<LightD>(c, 80, lightsBoost.size() + 1, st);
     }
     if (kFine > 1) {
@@ -2212,6 +2236,12 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     ++kernels;
     ubr_status rs = runLayers(p1, b, R, aaList0, nCentre);
     if (rs != UBR_OK || cancelled) return rs;
+    if (reuseOccBuf) {  // the centre pass's AO results, slot = output pixel
+      UBR_CUDA(c, cudaMemcpyAsync(reuseOccBuf, b.occ, size_t(nCentre) * R, cudaMemcpyDeviceToDevice, s));
+      if (reuseAoTBuf)
+        UBR_CUDA(c, cudaMemcpyAsync(reuseAoTBuf, b.aoT, size_t(nCentre) * p1.aoSamples * sizeof(float),
+                                    cudaMemcpyDeviceToDevice, s));
+    }
     k_aa_raw<<<gridC, 256, 0, s>>>(g, aaRaw);
     UBR_CUDA(c, cudaMemsetAsync(aaCounts, 0, 2 * sizeof(uint32_t), s));
     k_aa_lists<<<gridC, 256, 0, s>>>(g, aaRaw, aaList1, aaList0, aaCounts, aaMaskOut, kFine > 1);
@@ -2245,6 +2275,9 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       ++kernels;
       Bufs bb = b;
       bb.lights = dlBoost;
+      bb.reuseOcc = reuseOccBuf;
+      bb.reuseAoT = reuseAoTBuf;
+      bb.reuseR = R;
       rs = runLayers(pBoost, bb, uint32_t(pBoost.raysPerHit), aaList0, nCentres);
       if (rs != UBR_OK || cancelled) return rs;
     }

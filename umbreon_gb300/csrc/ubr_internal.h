@@ -461,6 +461,7 @@ struct Params {
   float aaThreshold;
   int aoCoarse;         // coarse-grid AO active: hits look up the grid before casting AO rays
   int cgW, cgH;         // coarse AO grid size
+  int reuseAo;          // AO rays 0..reuseAo-1 of a hit are copied from an earlier pass (Bufs::reuseOcc)
   f3 aoSky, aoGround;
   float aoDiffuseFactor;
   int shadowsActive, shadowSamples;
