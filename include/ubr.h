@@ -213,7 +213,7 @@ typedef struct ubr_render_desc {
   /* the stroke-edge pass's first-hit G-buffer (RenderOptions::strokeEdges
    * enables it in the reference, transparency.hpp:394-428, 470-481): fills
    * the gb_* planes of ubr_frame; the edge pass itself is the caller's.
-   * Not with adaptive AA or in a batch (UBR_INVALID_ARGUMENT). */
+   * Not with adaptive AA (UBR_INVALID_ARGUMENT). */
   uint32_t edge_gbuffer;
 } ubr_render_desc;
 
@@ -380,10 +380,11 @@ ubr_status ubr_render(ubr_context* ctx, const ubr_scene* scene,
  * replayed from a CUDA graph.  Items may use different scenes, cameras,
  * resolutions and options; each item's outputs go to its own frame buffers.
  * `total` (may be NULL) receives the batch's statistics; its `flags` select
- * profiling as for ubr_render.  Adaptive-AA items (aa_mode = 1 with
- * supersample > 1 or aa_depth > 1) return UBR_INVALID_ARGUMENT: their passes
- * depend on per-frame host decisions, so they go through ubr_render.  No
- * reference counterpart (the reference renders one frame per call). */
+ * profiling as for ubr_render.  Items whose passes depend on per-frame host
+ * decisions (adaptive AA, the coarse AO grid, the edge G-buffer) run as their
+ * own launch sequences after the batched rest; `total` then sums the
+ * statistics.  No reference counterpart (the reference renders one frame per
+ * call). */
 typedef struct ubr_batch_item {
   const ubr_scene* scene;
   const ubr_render_desc* desc;

@@ -133,16 +133,21 @@ def test_adaptive_threshold_zero_flags_more(gpu_ctx):
     assert np.all(lo >= hi)
 
 
-def test_adaptive_batch_rejected(gpu_ctx):
-    """Adaptive AA renders one frame per call; a batch that asks for it is an
-    INVALID_ARGUMENT, not a silent grid render."""
+def test_adaptive_frames_in_a_batch(gpu_ctx):
+    """A batch runs adaptive-AA items as their own passes: each equals the
+    frame rendered alone."""
     sc, opt = _case("space_filling_soft_shadows")
     b = gpu_ctx.build(sc)
     try:
-        with pytest.raises(UbrError):
-            gpu_ctx.render_batch([(b, sc, _adaptive(opt)), (b, sc, _adaptive(opt))])
+        a = _adaptive(opt)
+        grid = copy.copy(opt)
+        frames, stats = gpu_ctx.render_batch([(b, sc, a), (b, sc, grid), (b, sc, a)])
+        alone_a = gpu_ctx.render(b, sc, a)
+        alone_g = gpu_ctx.render(b, sc, grid)
     finally:
         b.release()
+    assert np.array_equal(frames[0].color, alone_a.color) and np.array_equal(frames[2].color, alone_a.color)
+    assert np.array_equal(frames[1].color, alone_g.color)
 
 
 @pytest.mark.parametrize("ss,depth", [(1, 2), (2, 3), (2, 4)])

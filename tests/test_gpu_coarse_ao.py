@@ -88,12 +88,19 @@ def test_coarse_ao_cuts_ao_rays(gpu_ctx):
     assert g.stats["rays_occlusion"] < 0.5 * f.stats["rays_occlusion"], (g.stats, f.stats)
 
 
-def test_coarse_ao_batch_rejected(gpu_ctx):
-    from umbreon_gb300.abi import UbrError
+def test_coarse_ao_frames_in_a_batch(gpu_ctx):
+    """A batch runs coarse-AO items as their own passes: each equals the frame
+    rendered alone."""
     sc, opt = _case("div2_ss1")
+    opt.aoResDebug = False
+    inline = copy.copy(opt)
+    inline.aoResDiv = 0
     b = gpu_ctx.build(sc)
     try:
-        with pytest.raises(UbrError):
-            gpu_ctx.render_batch([(b, sc, opt), (b, sc, opt)])
+        frames, stats = gpu_ctx.render_batch([(b, sc, opt), (b, sc, inline)])
+        alone = gpu_ctx.render(b, sc, opt)
+        alone_i = gpu_ctx.render(b, sc, inline)
     finally:
         b.release()
+    assert np.array_equal(frames[0].color, alone.color)
+    assert np.array_equal(frames[1].color, alone_i.color)

@@ -2456,8 +2456,70 @@ ubr_status renderFrame(Context* c, const Scene* sc, const ubr_render_desc& d, ub
   return runFrames(c, jobs, &fr, cancel, progress);
 }
 
+// Frames whose passes depend on per-frame host decisions (adaptive AA, the
+// coarse AO grid, the edge G-buffer) each run as their own launch sequence
+// after the batched rest; `total` then sums the statistics.
+static bool needsOwnPass(const ubr_render_desc& d) {
+  const int ss = d.supersample < 1 ? 1 : d.supersample;
+  if (d.aa_mode == 1 && (ss > 1 || d.aa_depth > 1)) return true;
+  if (d.edge_gbuffer) return true;
+  return (d.ao_res_div < 0 ? ss : d.ao_res_div) > 1 && d.ao_samples > 0;
+}
+
 ubr_status renderBatch(Context* c, const std::vector<Job>& jobs, ubr_frame* total) {
-  return runFrames(c, jobs, total, nullptr, nullptr);
+  std::vector<Job> together, alone;
+  for (const Job& j : jobs) (needsOwnPass(*j.desc) ? alone : together).push_back(j);
+  if (alone.empty()) return runFrames(c, jobs, total, nullptr, nullptr);
+  const uint32_t flags = total ? total->flags : 0u;
+  ubr_frame sum{};
+  auto add = [&](const ubr_frame& t) {
+    sum.total_ms += t.total_ms;
+    sum.render_ms += t.render_ms;
+    sum.rays_primary += t.rays_primary;
+    sum.rays_occlusion += t.rays_occlusion;
+    sum.capped_rays += t.capped_rays;
+    sum.stack_overflows += t.stack_overflows;
+    sum.layers = std::max(sum.layers, t.layers);
+    sum.kernels += t.kernels;
+    for (int k = 0; k < 5; ++k) sum.phase_ms[k] += t.phase_ms[k];
+    for (int k = 0; k < 2; ++k) {
+      sum.node_bytes[k] += t.node_bytes[k];
+      sum.prim_bytes[k] += t.prim_bytes[k];
+      sum.nodes_visited[k] += t.nodes_visited[k];
+    }
+  };
+  if (!together.empty()) {
+    ubr_frame t{};
+    t.flags = flags;
+    const ubr_status st = runFrames(c, together, &t, nullptr, nullptr);
+    if (st != UBR_OK) return st;
+    add(t);
+  }
+  for (const Job& j : alone) {
+    ubr_frame t{};
+    t.flags = flags;
+    const ubr_status st = runFrames(c, std::vector<Job>{j}, &t, nullptr, nullptr);
+    if (st != UBR_OK) return st;
+    add(t);
+  }
+  if (total) {
+    // statistics only: the frames' own buffers were written per item
+    total->total_ms = sum.total_ms;
+    total->render_ms = sum.render_ms;
+    total->rays_primary = sum.rays_primary;
+    total->rays_occlusion = sum.rays_occlusion;
+    total->capped_rays = sum.capped_rays;
+    total->stack_overflows = sum.stack_overflows;
+    total->layers = sum.layers;
+    total->kernels = sum.kernels;
+    for (int k = 0; k < 5; ++k) total->phase_ms[k] = sum.phase_ms[k];
+    for (int k = 0; k < 2; ++k) {
+      total->node_bytes[k] = sum.node_bytes[k];
+      total->prim_bytes[k] = sum.prim_bytes[k];
+      total->nodes_visited[k] = sum.nodes_visited[k];
+    }
+  }
+  return UBR_OK;
 }
 
 ubr_status occludedBatch(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps, uint8_t* out,
