@@ -1279,10 +1279,6 @@ int oracle_occluded_filtered(void* sp, const float* segs, uint64_t n, float eps,
   return 0;
 }
 
-// The frame: embree_renderer.cpp:1260-1427 pixel loop (rows [row0, row1) of the
-// hi-res grid, all rows when row1 <= row0), then pipeline.cpp:126-129 fog,
-// :182-192 box downsample, :254 assumed gamma.  `threads` <= 0 uses all cores.
-// Returns 0, or -1 for an unsupported request (Principled material).
 // One coarse-grid AO lookup on a hand-built grid (the unit cases of the
 // reference's tests/test_ao_coarse.cpp:97-204): returns 1 and fills out[0..6]
 // = openness, bent.xyz, contact, shape, avgHitDist when accepted, 0 when the
@@ -1329,6 +1325,11 @@ int oracle_aa_mask(int Wf, int Hf, const float* rgba, const float* viewZ, const 
   return 0;
 }
 
+// The frame: embree_renderer.cpp:1260-1427 pixel loop (rows [row0, row1) of the
+// hi-res grid, all rows when row1 <= row0; the adaptive-AA passes of
+// :1379-1670 when asked for), then pipeline.cpp:126-129 fog, :182-192 box
+// downsample, :254 assumed gamma.  `threads` <= 0 uses all cores.  Returns 0,
+// or -3 for adaptive AA together with the edge G-buffer (not restated).
 int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int threads, int row0,
                        int row1) {
   const Scene& s = *static_cast<Scene*>(sp);
