@@ -120,3 +120,26 @@ def test_empty_batch_and_queries(gpu_ctx):
         assert out.shape == (0,)
     finally:
         b.release()
+
+
+def test_arena_cap_reports_out_of_memory(gpu_ctx):
+    """A context whose device arena cap is too small for the frame refuses
+    with UBR_OUT_OF_MEMORY and stays usable for smaller work."""
+    from umbreon_gb300.api import Context
+    sc, opt = scenes.space_filling(n=200, width=64, height=48)
+    small = Context(0, arena_bytes=4 << 20)
+    try:
+        b = small.build(sc)
+        try:
+            big = copy.copy(opt)
+            big.width, big.height, big.supersample = 1024, 1024, 2
+            with pytest.raises(UbrError) as e:
+                small.render(b, sc, big, want_ids=False)
+            assert e.value.status == abi.UBR_OUT_OF_MEMORY
+            tiny = copy.copy(opt)
+            tiny.width, tiny.height = 16, 12
+            assert small.render(b, sc, tiny).color.shape == (12, 16, 4)
+        finally:
+            b.release()
+    finally:
+        small.close()
