@@ -215,6 +215,19 @@ typedef struct ubr_render_desc {
    * the gb_* planes of ubr_frame; the edge pass itself is the caller's.
    * Not with adaptive AA (UBR_INVALID_ARGUMENT). */
   uint32_t edge_gbuffer;
+  /* RenderOptions::denoiser / denoiseIters / denoiseSigmaZ / denoiseSigmaN /
+   * denoiseSigmaL / denoiseDemodulateAlbedo (render_options.hpp:255-268):
+   * 1 (a-trous) or 2 (OIDN, absent here: the a-trous runs, as the reference
+   * does without OIDN) filters the final-resolution linear colour before the
+   * gamma (pipeline.cpp:224-252), guided by the AO AOV normal and albedo; it
+   * runs only when ao_write_aov provides them, as in the reference without
+   * GI. */
+  int32_t denoiser;
+  int32_t denoise_iters;
+  float denoise_sigma_z;
+  float denoise_sigma_n;
+  float denoise_sigma_l;
+  uint32_t denoise_demodulate_albedo;
 } ubr_render_desc;
 
 /* Where a frame's buffers live. */

@@ -1176,6 +1176,107 @@ inline void buildAaMask(int Wf, int Hf, const AaCentre* c, float thr, float pixe
     }
 }
 
+// experimental/irradiance_cache/denoise_atrous.cpp:27-220 denoiseAtrous on the
+// final-resolution linear colour (4 floats per pixel): edge-avoiding a-trous
+// wavelet (B3 spline, 2^i hole spacing) with normal, luminance-variance and
+// (GI only, absent here) position edge-stops; illumination demodulated by the
+// albedo when given.  normal / albedo: 3 floats per pixel.
+inline void denoiseAtrous(int W, int H, float* color, const float* normal, const float* albedo, int iters,
+                          float sigmaNIn, float sigmaLIn) {
+  const size_t N = static_cast<size_t>(W) * H;
+  if (W <= 0 || H <= 0 || iters <= 0 || normal == nullptr) return;
+  const float kEps = 1.0e-3f;
+  auto luminance = [](float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; };
+  const float sigmaN = sigmaNIn;
+  const float sigmaL = std::max(1.0e-4f, sigmaLIn);
+  std::vector<unsigned char> valid(N, 0);
+  for (size_t p = 0; p < N; ++p) {
+    const float nx = normal[p * 3], ny = normal[p * 3 + 1], nz = normal[p * 3 + 2];
+    valid[p] = (nx * nx + ny * ny + nz * nz) > 0.25f ? 1 : 0;
+  }
+  std::vector<float> irr(N * 3);
+  for (size_t p = 0; p < N; ++p)
+    for (int c = 0; c < 3; ++c) {
+      float v = color[p * 4 + c];
+      if (albedo) {
+        const float a = albedo[p * 3 + c];
+        v /= (a > kEps ? a : kEps);
+      }
+      irr[p * 3 + c] = v;
+    }
+  std::vector<float> var(N, 0.0f);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t p = static_cast<size_t>(y) * W + x;
+      if (!valid[p]) continue;
+      float sm = 0.0f, s2 = 0.0f;
+      int n = 0;
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int qx = x + dx, qy = y + dy;
+          if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+          const size_t q = static_cast<size_t>(qy) * W + qx;
+          if (!valid[q]) continue;
+          const float l = luminance(irr[q * 3], irr[q * 3 + 1], irr[q * 3 + 2]);
+          sm += l;
+          s2 += l * l;
+          ++n;
+        }
+      if (n > 0) {
+        const float mean = sm / n;
+        var[p] = std::max(0.0f, s2 / n - mean * mean);
+      }
+    }
+  const float h5[5] = {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f};
+  std::vector<float> next(N * 3), lum(N);
+  for (int it = 0; it < iters; ++it) {
+    const int step = 1 << it;
+    for (size_t p = 0; p < N; ++p) lum[p] = luminance(irr[p * 3], irr[p * 3 + 1], irr[p * 3 + 2]);
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const size_t p = static_cast<size_t>(y) * W + x;
+        if (!valid[p]) {
+          for (int c = 0; c < 3; ++c) next[p * 3 + c] = irr[p * 3 + c];
+          continue;
+        }
+        const V3 np{normal[p * 3], normal[p * 3 + 1], normal[p * 3 + 2]};
+        const float lp = lum[p];
+        const float lDenom = sigmaL * std::sqrt(var[p]) + kEps;
+        float sum[3] = {0.0f, 0.0f, 0.0f};
+        float wsum = 0.0f;
+        for (int dy = -2; dy <= 2; ++dy) {
+          const int qy = y + dy * step;
+          if (qy < 0 || qy >= H) continue;
+          for (int dx = -2; dx <= 2; ++dx) {
+            const int qx = x + dx * step;
+            if (qx < 0 || qx >= W) continue;
+            const size_t q = static_cast<size_t>(qy) * W + qx;
+            if (!valid[q]) continue;
+            float w = h5[dx + 2] * h5[dy + 2];
+            const V3 nq{normal[q * 3], normal[q * 3 + 1], normal[q * 3 + 2]};
+            const float nd = std::max(0.0f, dot(np, nq));
+            w *= std::pow(nd, sigmaN);
+            w *= std::exp(-std::fabs(lp - lum[q]) / lDenom);
+            sum[0] += w * irr[q * 3];
+            sum[1] += w * irr[q * 3 + 1];
+            sum[2] += w * irr[q * 3 + 2];
+            wsum += w;
+          }
+        }
+        for (int c = 0; c < 3; ++c) next[p * 3 + c] = wsum > 0.0f ? sum[c] / wsum : irr[p * 3 + c];
+      }
+    irr.swap(next);
+  }
+  for (size_t p = 0; p < N; ++p) {
+    if (!valid[p]) continue;
+    for (int c = 0; c < 3; ++c) {
+      float v = irr[p * 3 + c];
+      if (albedo) v *= albedo[p * 3 + c];
+      color[p * 4 + c] = std::max(0.0f, v);
+    }
+  }
+}
+
 extern "C" {
 
 void* oracle_scene_create(const ubr_scene_desc* d) {
@@ -1770,6 +1871,36 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
         }
   } else {
     fin.swap(color);
+  }
+  // pipeline.cpp:224-252: the a-trous denoiser on the final-resolution linear
+  // colour, guided by the AO AOV normal / albedo (without GI the reference
+  // allocates those planes only for aoWriteAov)
+  if (d.denoiser != 0 && aov) {
+    const int ow = W / ss, oh = H / ss;
+    const size_t no = static_cast<size_t>(ow) * oh;
+    std::vector<float> dn(no * 3), da(no * 3);
+    auto downTo = [&](const std::vector<float>& src, std::vector<float>& dst) {
+      if (ss == 1) {
+        dst = src;
+        return;
+      }
+      const float inv = 1.0f / static_cast<float>(ss * ss);
+      for (int y = 0; y < oh; ++y)
+        for (int x = 0; x < ow; ++x)
+          for (int q = 0; q < 3; ++q) {
+            float acc = 0.0f;
+            for (int dy = 0; dy < ss; ++dy)
+              for (int dx = 0; dx < ss; ++dx) {
+                const float vv = src[(static_cast<size_t>(y * ss + dy) * W + (x * ss + dx)) * 3 + q];
+                acc += std::isfinite(vv) ? vv : 0.0f;
+              }
+            dst[(static_cast<size_t>(y) * ow + x) * 3 + q] = acc * inv;
+          }
+    };
+    downTo(aNrm, dn);
+    downTo(aAlb, da);
+    denoiseAtrous(ow, oh, fin.data(), dn.data(), d.denoise_demodulate_albedo ? da.data() : nullptr,
+                  std::max(0, d.denoise_iters), d.denoise_sigma_n, d.denoise_sigma_l);
   }
   // image_ops.cpp:37-46 applyAssumedGamma
   const float g = d.assumed_gamma;

@@ -105,7 +105,9 @@ class RenderDesc(C.Structure):
         ("transparent_background", C.c_uint32), ("max_transparent_layers", C.c_int32),
         ("gi_integrator", C.c_int32), ("ao_write_aov", C.c_uint32), ("aa_mode", C.c_int32),
         ("aa_threshold", C.c_float), ("aa_depth", C.c_int32), ("ao_res_div", C.c_int32),
-        ("edge_gbuffer", C.c_uint32),
+        ("edge_gbuffer", C.c_uint32), ("denoiser", C.c_int32), ("denoise_iters", C.c_int32),
+        ("denoise_sigma_z", C.c_float), ("denoise_sigma_n", C.c_float), ("denoise_sigma_l", C.c_float),
+        ("denoise_demodulate_albedo", C.c_uint32),
     ]
 
 

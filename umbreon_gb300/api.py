@@ -216,6 +216,12 @@ class RenderOptions:
     aoResDiv: int = 0        # coarse-grid AO divisor (-1 = supersample factor; 0 / 1 = per hit)
     aoResDebug: bool = False  # return the coarse-AO fallback mask
     edgeGBuffer: bool = False  # return the stroke-edge pass's first-hit G-buffer (hi-res)
+    denoiser: int = 0          # 0 none, 1 a-trous, 2 OIDN (runs the a-trous); needs aoWriteAov guides
+    denoiseIters: int = 5
+    denoiseSigmaZ: float = 1.0
+    denoiseSigmaN: float = 128.0
+    denoiseSigmaL: float = 4.0
+    denoiseDemodulateAlbedo: bool = True
 
     def aoEnhanced(self) -> bool:
         return (self.aoFalloffPower > 0.0 or self.aoMultiScale or self.aoBentNormal or self.aoMultibounce
@@ -283,6 +289,9 @@ def make_render_desc(scene: Scene, opt: RenderOptions):
     d.aa_mode, d.aa_threshold, d.aa_depth = opt.aaMode, opt.aaThreshold, opt.aaDepth
     d.ao_res_div = opt.aoResDiv
     d.edge_gbuffer = int(opt.edgeGBuffer)
+    d.denoiser, d.denoise_iters = opt.denoiser, opt.denoiseIters
+    d.denoise_sigma_z, d.denoise_sigma_n, d.denoise_sigma_l = opt.denoiseSigmaZ, opt.denoiseSigmaN, opt.denoiseSigmaL
+    d.denoise_demodulate_albedo = int(opt.denoiseDemodulateAlbedo)
     return d, keep
 
 

@@ -1519,6 +1519,126 @@ __global__ void __launch_bounds__(128) k_gb_clip(Params p, DScene s, Bufs b, uin
   }
 }
 
+// ---- A-trous denoiser (experimental/irradiance_cache/denoise_atrous.cpp:27-220,
+// pipeline.cpp:224-252) on the final-resolution linear colour, guided by the
+// AO AOV normal (and albedo, demodulated); no position guide without GI ----
+UBR_D float lumOf(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+
+__global__ void k_dn_init(uint32_t n, const float4* color, const float* nrm, const float* alb, uint8_t* valid,
+                          float* irr) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const float nx = nrm[3 * size_t(p)], ny = nrm[3 * size_t(p) + 1], nz = nrm[3 * size_t(p) + 2];
+  valid[p] = (nx * nx + ny * ny + nz * nz) > 0.25f ? 1 : 0;
+  const float4 c = color[p];
+  const float cv[3] = {c.x, c.y, c.z};
+  for (int k = 0; k < 3; ++k) {
+    float v = cv[k];
+    if (alb) {
+      const float a = alb[3 * size_t(p) + k];
+      v /= (a > 1.0e-3f ? a : 1.0e-3f);
+    }
+    irr[3 * size_t(p) + k] = v;
+  }
+}
+
+// luminance variance over the valid 3x3 neighbourhood
+__global__ void k_dn_var(int W, int H, const uint8_t* valid, const float* irr, float* var) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= uint32_t(W) * uint32_t(H)) return;
+  float v = 0.0f;
+  if (valid[p]) {
+    const int x = int(p % uint32_t(W)), y = int(p / uint32_t(W));
+    float sm = 0.0f, s2 = 0.0f;
+    int n = 0;
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int qx = x + dx, qy = y + dy;
+        if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+        const size_t q = size_t(qy) * W + qx;
+        if (!valid[q]) continue;
+        const float l = lumOf(irr[3 * q], irr[3 * q + 1], irr[3 * q + 2]);
+        sm += l;
+        s2 += l * l;
+        ++n;
+      }
+    if (n > 0) {
+      const float mean = sm / float(n);
+      v = fmaxf(0.0f, s2 / float(n) - mean * mean);
+    }
+  }
+  var[p] = v;
+}
+
+__global__ void k_dn_lum(uint32_t n, const float* irr, float* lum) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n) lum[p] = lumOf(irr[3 * size_t(p)], irr[3 * size_t(p) + 1], irr[3 * size_t(p) + 2]);
+}
+
+// one a-trous iteration: 5x5 B3 taps at 2^it spacing, normal^sigmaN and
+// exp(-|dl| / (sigmaL sqrt(var) + 1e-3)) edge-stops
+__global__ void k_dn_iter(int W, int H, int step, const uint8_t* valid, const float* nrm, const float* irr,
+                          const float* lum, const float* var, float sigmaN, float sigmaL, float* next) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= uint32_t(W) * uint32_t(H)) return;
+  if (!valid[p]) {
+    next[3 * size_t(p)] = irr[3 * size_t(p)];
+    next[3 * size_t(p) + 1] = irr[3 * size_t(p) + 1];
+    next[3 * size_t(p) + 2] = irr[3 * size_t(p) + 2];
+    return;
+  }
+  const float h5[5] = {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f};
+  const int x = int(p % uint32_t(W)), y = int(p / uint32_t(W));
+  const f3 np{nrm[3 * size_t(p)], nrm[3 * size_t(p) + 1], nrm[3 * size_t(p) + 2]};
+  const float lp = lum[p];
+  const float lDenom = sigmaL * sqrtf(var[p]) + 1.0e-3f;
+  float sum[3] = {0.0f, 0.0f, 0.0f};
+  float wsum = 0.0f;
+  for (int dy = -2; dy <= 2; ++dy) {
+    const int qy = y + dy * step;
+    if (qy < 0 || qy >= H) continue;
+    for (int dx = -2; dx <= 2; ++dx) {
+      const int qx = x + dx * step;
+      if (qx < 0 || qx >= W) continue;
+      const size_t q = size_t(qy) * W + qx;
+      if (!valid[q]) continue;
+      float w = h5[dx + 2] * h5[dy + 2];
+      const f3 nq{nrm[3 * q], nrm[3 * q + 1], nrm[3 * q + 2]};
+      const float nd = fmaxf(0.0f, dot(np, nq));
+      w *= powf(nd, sigmaN);
+      w *= expf(-fabsf(lp - lum[q]) / lDenom);
+      sum[0] += w * irr[3 * q];
+      sum[1] += w * irr[3 * q + 1];
+      sum[2] += w * irr[3 * q + 2];
+      wsum += w;
+    }
+  }
+  for (int k = 0; k < 3; ++k) next[3 * size_t(p) + k] = wsum > 0.0f ? sum[k] / wsum : irr[3 * size_t(p) + k];
+}
+
+__global__ void k_dn_write(uint32_t n, const uint8_t* valid, const float* irr, const float* alb, float4* color) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n || !valid[p]) return;
+  float v[3];
+  for (int k = 0; k < 3; ++k) {
+    v[k] = irr[3 * size_t(p) + k];
+    if (alb) v[k] *= alb[3 * size_t(p) + k];
+    v[k] = fmaxf(0.0f, v[k]);
+  }
+  color[p] = make_float4(v[0], v[1], v[2], color[p].w);
+}
+
+// applyAssumedGamma (image_ops.cpp:37-46) after the denoiser
+__global__ void k_gamma(uint32_t n, float4* color, float g) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  float4 r = color[p];
+  r.x = r.x > 0.0f ? powf(r.x, g) : 0.0f;
+  r.y = r.y > 0.0f ? powf(r.y, g) : 0.0f;
+  r.z = r.z > 0.0f ? powf(r.z, g) : 0.0f;
+  color[p] = r;
+}
+
 }  // namespace
 
 // Host-side parameter setup: computeCameraBasis (embree_renderer.cpp:375-386),
@@ -1971,6 +2091,17 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       b.gbFar = scratchT<float>(c, 104, npix, st);
     }
   }
+  // a-trous denoiser: one grid frame with the AO AOV guides
+  const bool denoise = !batch && aov && d0.denoiser != 0 && d0.denoise_iters > 0;
+  uint8_t* dnValid = nullptr;
+  float *dnIrr[2] = {nullptr, nullptr}, *dnLum = nullptr, *dnVar = nullptr;
+  if (denoise) {
+    dnValid = scratchT<uint8_t>(c, 107, nout, st);
+    dnIrr[0] = scratchT<float>(c, 108, size_t(nout) * 3, st);
+    dnIrr[1] = scratchT<float>(c, 109, size_t(nout) * 3, st);
+    dnLum = scratchT<float>(c, 110, nout, st);
+    dnVar = scratchT<float>(c, 111, nout, st);
+  }
   const uint32_t nCentre = uint32_t(p1.outW) * uint32_t(p1.outH);
   uint32_t *aaList0 = nullptr, *aaList1 = nullptr, *aaCounts = nullptr;
   uint8_t* aaRaw = nullptr;
@@ -2156,8 +2287,11 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   };
   auto post = [&]() -> ubr_status {
     mark(4, true);
+    // with the denoiser the gamma waits until after it
+    Params pp = p1;
+    if (denoise) pp.gamma = 1.0f;
     if (batch) k_post<true><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.colorHi, b.viewZ, outColor);
-    else k_post<false><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.colorHi, b.viewZ, outColor);
+    else k_post<false><<<(nout + 255) / 256, 256, 0, s>>>(pp, bt, nout, b.colorHi, b.viewZ, outColor);
     if (aov) {
       float* o = outAov;
       const size_t n = nout;
@@ -2168,6 +2302,31 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
         k_post_aov<false><<<(nout + 255) / 256, 256, 0, s>>>(p1, bt, nout, b.aovA, b.aovB, b.aovC, o, o + 3 * n,
                                                               o + 6 * n, o + 9 * n, o + 10 * n, o + 11 * n);
       ++kernels;
+    }
+    if (denoise) {
+      const int W = p1.outW, H = p1.outH;
+      const uint32_t g = (nout + 255) / 256;
+      const float* nrm = outAov + 3 * size_t(nout);
+      const float* alb = d0.denoise_demodulate_albedo ? outAov : nullptr;
+      k_dn_init<<<g, 256, 0, s>>>(nout, outColor, nrm, alb, dnValid, dnIrr[0]);
+      k_dn_var<<<g, 256, 0, s>>>(W, H, dnValid, dnIrr[0], dnVar);
+      kernels += 2;
+      const int iters = std::max(0, d0.denoise_iters);
+      const float sigmaL = std::max(1.0e-4f, d0.denoise_sigma_l);
+      int cur = 0;
+      for (int it = 0; it < iters; ++it) {
+        k_dn_lum<<<g, 256, 0, s>>>(nout, dnIrr[cur], dnLum);
+        k_dn_iter<<<g, 256, 0, s>>>(W, H, 1 << it, dnValid, nrm, dnIrr[cur], dnLum, dnVar, d0.denoise_sigma_n, sigmaL,
+                                    dnIrr[cur ^ 1]);
+        cur ^= 1;
+        kernels += 2;
+      }
+      k_dn_write<<<g, 256, 0, s>>>(nout, dnValid, dnIrr[cur], alb, outColor);
+      ++kernels;
+      if (!(fabsf(p1.gamma - 1.0f) <= 1.0e-4f)) {
+        k_gamma<<<g, 256, 0, s>>>(nout, outColor, p1.gamma);
+        ++kernels;
+      }
     }
     mark(4, false);
     ++kernels;
@@ -2343,7 +2502,10 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       c->graphKey = key;
     } else {
       kernels = (secondary ? 4u : 2u) + 1u + (aov ? 1u : 0u) + (coarseOn ? 3u : 0u) +
-                (edgeGb ? (clipPlanes ? 2u : 1u) : 0u);
+                (edgeGb ? (clipPlanes ? 2u : 1u) : 0u) +
+                (denoise ? 3u + 2u * uint32_t(std::max(0, d0.denoise_iters)) +
+                               (fabsf(p1.gamma - 1.0f) <= 1.0e-4f ? 0u : 1u)
+                         : 0u);
     }
     cudaEventRecord(c->ev[2], s);
     UBR_CUDA(c, cudaGraphLaunch(c->graphExec, s));
@@ -2463,6 +2625,7 @@ static bool needsOwnPass(const ubr_render_desc& d) {
   const int ss = d.supersample < 1 ? 1 : d.supersample;
   if (d.aa_mode == 1 && (ss > 1 || d.aa_depth > 1)) return true;
   if (d.edge_gbuffer) return true;
+  if (d.denoiser != 0 && d.ao_write_aov) return true;
   return (d.ao_res_div < 0 ? ss : d.ao_res_div) > 1 && d.ao_samples > 0;
 }
 

@@ -1,8 +1,10 @@
 // RenderOptions of the umbreon API (same fields and defaults as the
 // reference).  This library honours the ray-cast + shade fields: output size,
-// supersample, AO (legacy and enhanced estimators), shadows, environment dome,
-// specular scale and transparency.  GI, edge passes and the denoiser are not
-// part of it (see umbreon.hpp for how render() treats them).
+// supersample, adaptive AA, AO (legacy and enhanced estimators, AOVs,
+// coarse grid), shadows, environment dome, specular scale, transparency and
+// the a-trous denoiser (OIDN requests run it, as the reference does without
+// OIDN).  GI and the edge passes are not part of it (see umbreon.hpp for how
+// render() treats them).
 #pragma once
 
 #include "render/edge_types.hpp"

@@ -1,14 +1,14 @@
 // umbreon public API, GB300 edition.
 //
 // render() runs the ray-cast + shade frame on the GPU through the C-ABI in
-// ubr.h: scene upload and LBVH build, primary rays through the transparency
-// walk, POV shading with AO and shadow rays, fog, supersample resolve and
-// assumed gamma.  Group-alpha blending (Scene::groupBlend) runs one GPU pass
-// per group on the host side exactly as the reference composes them.
+// ubr.h: scene upload and BVH build, primary rays through the transparency
+// walk, POV and Principled (direct) shading with AO and shadow rays, fog,
+// supersample resolve or adaptive AA, coarse-grid AO, the a-trous denoiser
+// and assumed gamma.  Group-alpha blending (Scene::groupBlend) runs one GPU
+// pass per group on the host side exactly as the reference composes them.
 // Requests outside this library throw std::runtime_error: GI (gi), stroke or
-// object-space edges, Principled materials.  Quality knobs without a GPU
-// variant fall back with a logged warning: adaptive AA and coarse-grid AO
-// render the full grid / inline AO, the denoiser is skipped.
+// object-space edges.  An OIDN denoiser request runs the a-trous with a
+// logged warning, as the reference does when built without OIDN.
 #pragma once
 
 #include <chrono>

@@ -389,6 +389,12 @@ ubr_render_desc toRenderDesc(const Scene& s, const RenderOptions& o, std::vector
   d.aa_threshold = o.aaThreshold;
   d.aa_depth = o.aaDepth;
   d.ao_res_div = o.aoResDiv;
+  d.denoiser = o.denoiser;
+  d.denoise_iters = o.denoiseIters;
+  d.denoise_sigma_z = o.denoiseSigmaZ;
+  d.denoise_sigma_n = o.denoiseSigmaN;
+  d.denoise_sigma_l = o.denoiseSigmaL;
+  d.denoise_demodulate_albedo = o.denoiseDemodulateAlbedo ? 1u : 0u;
   return d;
 }
 
@@ -404,7 +410,9 @@ void rejectUnsupported(const Scene& scene, const RenderOptions& opt) {
 // One GPU pass: the work of renderFrame (pipeline.cpp:20-256) minus edges,
 // GI and denoise.
 FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderProgress* progress) {
-  if (opt.denoiser != 0) logMessage(LogLevel::Warning, "the denoiser is not part of the GB300 path; skipped");
+  if (opt.denoiser == 2)
+    logMessage(LogLevel::Warning,
+               "OIDN denoiser backend not built; falling back to the built-in a-trous denoiser");
   const int ss = std::max(1, opt.supersample);
   FrameResult f;
   f.width = opt.width;
@@ -481,6 +489,8 @@ FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderP
   f.pt1Timing.bvhBuild = info.build_ms / 1e3;
   f.pt1Timing.primary = f.renderSeconds;
   f.cancelled = st == UBR_CANCELLED;
+  // pipeline.cpp:231-251: which backend ran (the a-trous, also for OIDN requests)
+  if (opt.denoiser != 0) f.denoiserUsed = 1;
   if (fr.capped_rays > 0)
     logMessage(LogLevel::Warning,
                "%llu ray(s) reached the transparent-layer cap (%d); transmission past that depth was dropped",
