@@ -128,6 +128,39 @@ UBR_D float byteToFloat(uint32_t q, int b) {
   return __uint_as_float(__byte_perm(q, 0x4B000000u, 0x7540u + uint32_t(b))) - 8388608.0f;
 }
 
+// Packed pairs of floats for the slab test of two children at once:
+// sm_100-family add/mul/fma on .f32x2 round each lane like the scalar
+// instruction (round to nearest even), so the pair form gives the same bits
+// as two scalar operations with half the instructions issued.
+typedef unsigned long long f2x;
+UBR_D f2x pk2(float a, float b) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+UBR_D void up2(f2x v, float& a, float& b) { asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
+UBR_D f2x fma2(f2x a, f2x b, f2x c) {
+  f2x d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+UBR_D f2x add2(f2x a, f2x b) {
+  f2x d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+UBR_D f2x mul2(f2x a, f2x b) {
+  f2x d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// Bytes b and b+1 of q as a float pair (byteToFloat on both).
+UBR_D f2x bytePairToFloat2(uint32_t q, int b, f2x bias) {
+  return add2(pk2(__uint_as_float(__byte_perm(q, 0x4B000000u, 0x7540u + uint32_t(b))),
+                  __uint_as_float(__byte_perm(q, 0x4B000000u, 0x7540u + uint32_t(b + 1)))),
+              bias);
+}
+
 // Traversal state of one ray, resumable one node at a time (the persistent
 // occlusion kernel interleaves rays at node granularity).
 struct TravState {
@@ -245,15 +278,33 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
   uint32_t hitInt = 0, primMask = 0;
   float nearT = kInfF;
   int nearK = -1;
+  const f2x bias2 = pk2(-8388608.0f, -8388608.0f), grow2 = pk2(kSlabGrow, kSlabGrow);
+  const f2x sx2 = pk2(sx, sx), sy2 = pk2(sy, sy), sz2 = pk2(sz, sz);
+  const f2x ox2 = pk2(ox, ox), oy2 = pk2(oy, oy), oz2 = pk2(oz, oz);
+  float tminP[8], tmaxP[8];
+#pragma unroll
+  for (int k = 0; k < 8; k += 2) {
+    const int w = k >> 2, b = k & 3;
+    float tnx[2], tfx[2], tny[2], tfy[2], tnz[2], tfz[2];
+    up2(fma2(bytePairToFloat2(qnx[w], b, bias2), sx2, ox2), tnx[0], tnx[1]);
+    up2(fma2(bytePairToFloat2(qfx[w], b, bias2), sx2, ox2), tfx[0], tfx[1]);
+    up2(fma2(bytePairToFloat2(qny[w], b, bias2), sy2, oy2), tny[0], tny[1]);
+    up2(fma2(bytePairToFloat2(qfy[w], b, bias2), sy2, oy2), tfy[0], tfy[1]);
+    up2(fma2(bytePairToFloat2(qnz[w], b, bias2), sz2, oz2), tnz[0], tnz[1]);
+    up2(fma2(bytePairToFloat2(qfz[w], b, bias2), sz2, oz2), tfz[0], tfz[1]);
+    float tmx[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      tminP[k + j] = fmaxf(fmaxf(tnx[j], tny[j]), fmaxf(tnz[j], r.tnear));
+      tmx[j] = fminf(fminf(tfx[j], tfy[j]), fminf(tfz[j], st.tmax));
+    }
+    up2(mul2(pk2(tmx[0], tmx[1]), grow2), tmaxP[k], tmaxP[k + 1]);
+  }
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     const int w = k >> 2;
-    const float tnx = fmaf(byteToFloat(qnx[w], k & 3), sx, ox), tfx = fmaf(byteToFloat(qfx[w], k & 3), sx, ox);
-    const float tny = fmaf(byteToFloat(qny[w], k & 3), sy, oy), tfy = fmaf(byteToFloat(qfy[w], k & 3), sy, oy);
-    const float tnz = fmaf(byteToFloat(qnz[w], k & 3), sz, oz), tfz = fmaf(byteToFloat(qfz[w], k & 3), sz, oz);
-    const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tnear));
-    const float tmx = fminf(fminf(tfx, tfy), fminf(tfz, st.tmax));
-    const bool hit = k < nCh && tmin <= tmx * kSlabGrow;
+    const float tmin = tminP[k];
+    const bool hit = k < nCh && tmin <= tmaxP[k];
     if (k < nInt) {
       hitInt |= hit ? (1u << k) : 0u;
       const bool nearer = hit && tmin < nearT;
