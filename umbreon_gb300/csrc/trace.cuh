@@ -275,9 +275,6 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
                            nz ? __float_as_uint(n4.w) : __float_as_uint(n3.y)};
   const uint32_t qfz[2] = {nz ? __float_as_uint(n3.x) : __float_as_uint(n4.z),
                            nz ? __float_as_uint(n3.y) : __float_as_uint(n4.w)};
-  uint32_t hitInt = 0, primMask = 0;
-  float nearT = kInfF;
-  int nearK = -1;
   const f2x bias2 = pk2(-8388608.0f, -8388608.0f), grow2 = pk2(kSlabGrow, kSlabGrow);
   const f2x sx2 = pk2(sx, sx), sy2 = pk2(sy, sy), sz2 = pk2(sz, sz);
   const f2x ox2 = pk2(ox, ox), oy2 = pk2(oy, oy), oz2 = pk2(oz, oz);
@@ -300,20 +297,28 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
     }
     up2(mul2(pk2(tmx[0], tmx[1]), grow2), tmaxP[k], tmaxP[k + 1]);
   }
+  // slot mask of the hit children; internal children come first (nInt), then
+  // leaves; slots past nCh are empty
+  uint32_t hitMask = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) hitMask |= tminP[k] <= tmaxP[k] ? (1u << k) : 0u;
+  hitMask &= (1u << nCh) - 1u;
+  const uint32_t hitInt = hitMask & ((1u << nInt) - 1u);
+  // each hit leaf's meta byte (count << 5 | offset) adds its primitives
+  uint32_t primMask = 0;
+  for (uint32_t leafHit = hitMask & ~hitInt; leafHit; leafHit &= leafHit - 1u) {
+    const int k = __ffs(leafHit) - 1;
+    const uint32_t m = __byte_perm(k < 4 ? meta0 : meta1, 0u, 0x4440u | uint32_t(k & 3));
+    primMask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+  }
+  // nearest hit internal child (lowest slot on ties)
+  float nearT = kInfF;
+  int nearK = -1;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    const int w = k >> 2;
-    const float tmin = tminP[k];
-    const bool hit = k < nCh && tmin <= tmaxP[k];
-    if (k < nInt) {
-      hitInt |= hit ? (1u << k) : 0u;
-      const bool nearer = hit && tmin < nearT;
-      nearT = nearer ? tmin : nearT;
-      nearK = nearer ? k : nearK;
-    } else if (hit) {
-      const uint32_t m = ((w == 0 ? meta0 : meta1) >> ((k & 3) * 8)) & 0xFFu;
-      primMask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
-    }
+    const bool nearer = ((hitInt >> k) & 1u) && tminP[k] < nearT;
+    nearT = nearer ? tminP[k] : nearT;
+    nearK = nearer ? k : nearK;
   }
   // primitives of the hit leaves
   while (primMask) {
