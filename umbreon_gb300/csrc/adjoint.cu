@@ -78,7 +78,6 @@ UBR_D void atomicAdd3(float* a, uint32_t k, f3 v) {
 }
 
 UBR_D f3 mul3(f3 a, f3 b) { return f3{a.x * b.x, a.y * b.y, a.z * b.z}; }
-UBR_D float sum3(f3 a) { return a.x + a.y + a.z; }
 
 // d(a / |a|) transposed applied to g: (g - n (n.g)) / |a| with n = a / |a|
 UBR_D f3 normalizeBack(f3 n, float len, f3 g) {

@@ -1841,8 +1841,6 @@ int roundKindMask(int m) {
   }
 }
 
-int kindMask(const Scene& sc) { return roundKindMask(kindMaskBits(sc)); }
-
 #define UBR_LAUNCH3(KERNEL, KM, count, batch, grid, tb, stream, ...)                  \
   do {                                                                                \
     if (count) {                                                                      \
