@@ -398,7 +398,7 @@ ubr_render_desc toRenderDesc(const Scene& s, const RenderOptions& o, std::vector
   return d;
 }
 
-void rejectUnsupported(const Scene& scene, const RenderOptions& opt) {
+void rejectUnsupported(const RenderOptions& opt) {
   if (opt.strokeEdges.enable && opt.objectSpaceEdges.enable)
     throw std::runtime_error(
         "umbreon::render: strokeEdges and objectSpaceEdges are mutually exclusive; enable at most one");
@@ -407,8 +407,8 @@ void rejectUnsupported(const Scene& scene, const RenderOptions& opt) {
     throw std::runtime_error("umbreon::render: edge passes are not part of the GB300 ray-cast + shade library");
 }
 
-// One GPU pass: the work of renderFrame (pipeline.cpp:20-256) minus edges,
-// GI and denoise.
+// One GPU pass: the work of renderFrame (pipeline.cpp:20-256) minus the
+// edge passes and GI.
 FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderProgress* progress) {
   if (opt.denoiser == 2)
     logMessage(LogLevel::Warning,
@@ -534,7 +534,7 @@ Scene hideGroups(const Scene& s, const std::vector<uint8_t>& hide) {
 }
 
 FrameResult renderImpl(const Scene& scene, const RenderOptions& opt, RenderProgress* progress) {
-  rejectUnsupported(scene, opt);
+  rejectUnsupported(opt);
   if (scene.groupBlend.empty()) {
     FrameResult f = renderFrameGpu(scene, opt, progress);
     if (progress && !f.cancelled) progress->markDone();
