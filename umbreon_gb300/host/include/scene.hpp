@@ -81,8 +81,9 @@ struct Aabb {
 
 enum class ShadingModel : uint8_t { Pov = 0, Principled = 1, Toon = 2 };
 
-// POV finish.  This library shades the Pov and Toon models (identical lobes);
-// Principled materials are rejected by render().
+// POV finish plus the principled parameters.  This library shades the Pov
+// and Toon models (identical lobes) and the Principled model's direct pass
+// (GGX / Smith / Schlick, src/umbreon/shading/principled.hpp:139).
 struct Material {
   float ambient = 0.2f;
   float diffuse = 0.8f;
