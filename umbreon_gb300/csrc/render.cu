@@ -362,9 +362,11 @@ UBR_D void occRayOf(uint64_t rid, uint32_t nq, uint64_t R, uint64_t A, uint32_t&
   }
 }
 
-// One thread per AO / shadow ray.
+// One thread per AO / shadow ray.  Mesh scenes run 9 blocks per SM (56
+// registers), the others 8 (64 registers): measured best for each.
 template <bool COUNT, int KM, bool BATCH>
-__global__ void __launch_bounds__(128, 8) k_trace_occlusion(Params p1, DScene s1, Batch bt, Bufs b, uint32_t n) {
+__global__ void __launch_bounds__(128, (KM & kMaskMesh) ? 9 : 8)
+    k_trace_occlusion(Params p1, DScene s1, Batch bt, Bufs b, uint32_t n) {
   Count cnt;
   const uint64_t tid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t R = BATCH ? uint64_t(bt.R) : uint64_t(p1.raysPerHit);
