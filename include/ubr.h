@@ -188,8 +188,9 @@ typedef struct ubr_render_desc {
   uint32_t transparency;
   uint32_t transparent_background;
   int32_t max_transparent_layers;
-  /* giIntegrator only selects the soft-shadow radius rule
-   * (embree_renderer.cpp:452-454); GI itself is out of this library */
+  /* giIntegrator selects the soft-shadow radius rule
+   * (embree_renderer.cpp:452-454) and, with gi (below), the integrator:
+   * only 1 (pt1) is built here */
   int32_t gi_integrator;
   /* RenderOptions::aoWriteAov (render_options.hpp:62): fill the AO AOV
    * outputs of ubr_frame */
@@ -228,6 +229,30 @@ typedef struct ubr_render_desc {
   float denoise_sigma_n;
   float denoise_sigma_l;
   uint32_t denoise_demodulate_albedo;
+  /* pt1 GI gather: RenderOptions::gi with giIntegrator = 1 (pt1, the
+   * reference's frozen one-bounce anchor), pt1Spp, giBounces, giMaxDistance
+   * (0 = unbounded), giIntensity, giEnvIntensity, pt1Seed, pt1SkyMode /
+   * pt1SkyRadiance (the gather's miss term; mode 1 takes ao_ground_color as
+   * the ground tint), pt1Ld and pt1Clamp (render_options.hpp:85-151).  The
+   * gather runs at every pixel of the supersampled grid (pt1GatherDiv = 1)
+   * with no denoise of the indirect term (pt1Denoise = false); the reduced
+   * gather grid with its upsample and edge patch, the OIDN / a-trous
+   * denoise of E, pt2 and the irradiance cache are not part of this
+   * library.  gi != 0 needs gi_integrator = 1, pt1_spp >= 1,
+   * gi_bounces >= 1, no adaptive AA and no coarse-grid AO (the reference
+   * turns those two off under GI, pipeline.cpp:60-78), and one frame per
+   * call (not ubr_render_batch); otherwise UBR_INVALID_ARGUMENT. */
+  uint32_t gi;
+  int32_t pt1_spp;
+  int32_t gi_bounces;
+  float gi_max_distance;
+  float gi_intensity;
+  float gi_env_intensity;
+  uint32_t pt1_seed;
+  int32_t pt1_sky_mode;
+  float pt1_sky_radiance[3];
+  uint32_t pt1_ld;
+  float pt1_clamp;
 } ubr_render_desc;
 
 /* Where a frame's buffers live. */

@@ -466,6 +466,14 @@ struct Opt {  // the RenderOptions fields this path reads
   bool aoWriteAov = false;
   int aaMode = 0;
   bool edgeGbuffer = false;  // capture the stroke-edge pass's first-hit G-buffer
+  // pt1 GI gather (render_options.hpp:85-151; the gather at every hi-res
+  // pixel, no denoise of E)
+  bool gi = false;
+  int pt1Spp = 8, giBounces = 1, pt1SkyMode = 0;
+  float giMaxDistance = 0.0f, giIntensity = 1.0f, giEnvIntensity = 1.0f, pt1Clamp = 0.0f;
+  uint32_t pt1Seed = 0;
+  float pt1SkyRadiance[3] = {1.0f, 1.0f, 1.0f};
+  bool pt1Ld = true;
   bool aoEnhanced() const {  // render_options.hpp:79-82
     return aoFalloffPower > 0.0f || aoMultiScale || aoBentNormal || aoMultibounce || aoLowDiscrepancy ||
            aoDiffuseFactor > 0.0f;
@@ -842,6 +850,8 @@ inline AoShade aoShadeForHit(const Ctx& c, const V3& P, const V3& Ng, const V3& 
 struct HitShade {
   V3 color;
   float opacity = 1.0f;
+  V3 giRefl{0.0f, 0.0f, 0.0f};  // kd * pigment of a GI-eligible hit (hit_shader.hpp:48-54)
+  uint8_t giElig = 0;
   // AO AOVs (hit_shader.hpp:41-55): set on mesh hits when aoWriteAov is on
   V3 albedo{0.0f, 0.0f, 0.0f}, normal{0.0f, 0.0f, 0.0f}, bent{0.0f, 0.0f, 0.0f};
   float contact = 1.0f, shape = 1.0f, avgHit = 0.0f;
@@ -853,6 +863,15 @@ struct HitShade {
 };
 
 // hit_shader.hpp:147-496 shadeHit (POV and principled direct; GI / edge branches off)
+// Material::diffuseWeight / toonLike (scene.hpp:171-196)
+inline float matDiffuseWeight(const Mat& m) { return m.model == 1 ? m.diffuse * (1.0f - m.pbrMetallic) : m.diffuse; }
+inline bool matToonLike(const Mat& m) {
+  if (m.model == 2) return true;
+  if (m.model != 0) return false;
+  if (m.specular > 1.0f || m.phong > 1.0f || m.brilliance == 0.0f) return true;
+  return m.diffuse <= 0.0f && m.specular <= 0.0f && m.phong <= 0.0f && m.reflection <= 0.0f;
+}
+
 inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& org, uint32_t px, uint32_t py) {
   const Scene& s = *c.s;
   HitShade hs;
@@ -879,6 +898,16 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
     const Mat& triMat = s.triMat.empty() ? s.meshMat : s.meshMats[s.triMat[bt]];
     AOResult aov;
     AoShade ao = aoShadeForHit(c, P, Ng, N, C, secEps, hit.t, px, py, &hs.aoPatched, &aov);
+    // hit_shader.hpp:221-242: under GI the constant ambient gives way to the
+    // gathered indirect; toon finishes keep a unit ambient and get none
+    if (c.o.gi && matToonLike(triMat)) {
+      ao.ambLight = V3{1.0f, 1.0f, 1.0f};
+    } else if (c.o.gi) {
+      const float kd = matDiffuseWeight(triMat);
+      hs.giRefl = V3{kd * C.x, kd * C.y, kd * C.z};
+      hs.giElig = 1;
+      ao.ambLight = V3{0.0f, 0.0f, 0.0f};
+    }
     hs.color = triMat.model == 1
                    ? shadePrincipled(s, triMat, C, N, V, c.lights, ao.ambLight, c.bg, ao.aoFactor, ao.diffuseAo, P,
                                      Ng, secEps, shadowsActive, c.o.shadowSamples, px, py, nullptr)
@@ -892,7 +921,7 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
       hs.contact = aov.contact;
       hs.shape = aov.shape;
       hs.avgHit = aov.avgHitDist;
-    } else if (c.o.aaMode == 1) {  // :214-220 (the adaptive-AA mask reads N)
+    } else if (c.o.gi || c.o.aaMode == 1) {  // :214-220 (the adaptive-AA mask reads N)
       hs.albedo = C;
       hs.normal = N;
     }
@@ -916,6 +945,17 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
       aoFactor = ao.aoFactor;
       ambLight = ao.ambLight;
       diffuseAo = ao.diffuseAo;
+      // hit_shader.hpp:351-365 (pt1): a real primitive receives the
+      // gathered indirect like the mesh
+      if (c.o.gi && matToonLike(pm)) {
+        ambLight = V3{1.0f, 1.0f, 1.0f};
+      } else if (c.o.gi) {
+        const float kd = matDiffuseWeight(pm);
+        hs.giRefl = V3{kd * C.x, kd * C.y, kd * C.z};
+        hs.giElig = 1;
+        hs.normal = N;
+        ambLight = V3{0.0f, 0.0f, 0.0f};
+      }
     }
     const bool primShadows = !fromEdge && shadowsActive;
     // anisotropy tangent frame (hit_shader.hpp:373-425): sphere = meridian of
@@ -990,6 +1030,7 @@ struct PixelOut {
   bool capped;
   uint32_t rays;
   HitShade first;  // AOVs of the first hit (neutral values on a miss)
+  V3 firstPos{0.0f, 0.0f, 0.0f};  // org + rd * nearDepth (transparency.hpp:410-411)
   // clip-cut G-buffer (transparency.hpp:424-428, 470-481)
   uint8_t clipCut = 0;
   float clipNearVz = 0.0f, clipFarVz = 0.0f;
@@ -1015,6 +1056,171 @@ inline float clipProbeRange(const Scene& s, const V3& org, const V3& rd, const V
 }
 
 // transparency.hpp:311-522 integratePixel (colour, first-hit depth/viewZ/ids)
+// irradiance_cache.hpp:176-184 hashU32
+inline uint32_t hashU32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7FEB352Du;
+  x ^= x >> 15;
+  x *= 0x846CA68Bu;
+  x ^= x >> 16;
+  return x;
+}
+
+// irradiance_cache.hpp:188-196 environmentRadiance with the pt1 sky
+// (embree_renderer.cpp:590-601): the gather's miss term
+inline V3 pt1Environment(const Ctx& c, const V3& wi) {
+  const V3 sky{c.o.pt1SkyRadiance[0], c.o.pt1SkyRadiance[1], c.o.pt1SkyRadiance[2]};
+  const V3 gr = c.o.pt1SkyMode == 1 ? V3{c.o.aoGround[0], c.o.aoGround[1], c.o.aoGround[2]} : sky;
+  const float w = 0.5f * (dot(wi, c.aoUp) + 1.0f);
+  const float e = c.o.giEnvIntensity;
+  return V3{e * c.ambLight.x * (gr.x + (sky.x - gr.x) * w), e * c.ambLight.y * (gr.y + (sky.y - gr.y) * w),
+            e * c.ambLight.z * (gr.z + (sky.z - gr.z) * w)};
+}
+
+// pt1_gather.hpp:117-227 pt1EvalVertex, pt1 form: the vertex's reflected
+// direct light through the hard centre shadow ray of each light
+// (secondary_rays.hpp:116-134 with one sample), its reflectance kd * C, and
+// the normal faced toward the ray origin.  Outline primitives end the path.
+inline bool pt1EvalVertex(const Ctx& c, const Hit& h, const V3& O, const V3& wi, V3& rad, V3& alb, V3& Py,
+                          V3& Ny) {
+  const Scene& s = *c.s;
+  const int kind = kindOfGeom(s, h.geomID);
+  V3 C, NgSh;
+  const Mat* m;
+  if (kind == kMesh) {
+    const uint32_t* tri = &s.geo.triIdx[3 * h.primID];
+    const float w0 = 1.0f - h.u - h.v;
+    float nb[3], cb[3];
+    for (int k = 0; k < 3; ++k)
+      nb[k] = w0 * s.nrm[3 * tri[0] + k] + h.u * s.nrm[3 * tri[1] + k] + h.v * s.nrm[3 * tri[2] + k];
+    for (int k = 0; k < 3; ++k)
+      cb[k] = w0 * s.col[4 * tri[0] + k] + h.u * s.col[4 * tri[1] + k] + h.v * s.col[4 * tri[2] + k];
+    Ny = normalize(V3{nb[0], nb[1], nb[2]});
+    C = V3{cb[0], cb[1], cb[2]};
+    const size_t bt = s.baseTri ? h.primID % s.baseTri : 0;
+    m = s.triMat.empty() ? &s.meshMat : &s.meshMats[s.triMat[bt]];
+    NgSh = h.Ng;
+  } else {
+    if (s.fromEdge[kind][h.primID]) return false;
+    const float* fc = &s.color[kind][4 * h.primID];
+    m = &s.mat[kind][h.primID];
+    C = V3{fc[0], fc[1], fc[2]};
+    Ny = safeNormalize(h.Ng);
+    NgSh = Ny;
+  }
+  const float kd = matDiffuseWeight(*m);
+  if (dot(Ny, wi) > 0.0f) Ny = V3{-Ny.x, -Ny.y, -Ny.z};
+  Py = V3{O.x + wi.x * h.t, O.y + wi.y * h.t, O.z + wi.z * h.t};
+  const float eps = selfIntersectEps(Py, wi, h.t);
+  V3 E{0.0f, 0.0f, 0.0f};
+  for (const Light& l : c.lights) {
+    const float ndl = dot(Ny, l.L);
+    if (ndl <= 0.0f) continue;
+    V3 ng = (dot(NgSh, Ny) < 0.0f) ? V3{-NgSh.x, -NgSh.y, -NgSh.z} : NgSh;
+    ng = safeNormalize(ng, Ny);
+    const V3 So{Py.x + ng.x * eps, Py.y + ng.y * eps, Py.z + ng.z * eps};
+    const float sh = occludedQ(s, So, l.L, eps, kInf) ? 0.0f : 1.0f;
+    E.x += ndl * l.color.x * sh;
+    E.y += ndl * l.color.y * sh;
+    E.z += ndl * l.color.z * sh;
+  }
+  rad = V3{kd * C.x * E.x, kd * C.y * E.y, kd * C.z * E.z};
+  alb = V3{kd * C.x, kd * C.y, kd * C.z};
+  return true;
+}
+
+// pt1_gather.hpp:268-523 pt1GatherPoint, pt1 form (no reservoir, no Sobol,
+// no emission): E_stored = (1/spp) sum over cosine-hemisphere paths of the
+// NEE radiance at each vertex and the sky where the path escapes; Russian
+// roulette from the second vertex on.
+inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, uint32_t seed, float epsT) {
+  const Scene& s = *c.s;
+  const int spp = c.o.pt1Spp;
+  const Frame f = frameFromNormal(N);
+  const float eps = selfIntersectEps(P, N, epsT);
+  const V3 O{P.x + N.x * eps, P.y + N.y * eps, P.z + N.z * eps};
+  const int maxB = c.o.giBounces < 1 ? 1 : c.o.giBounces;
+  const float maxD = c.o.giMaxDistance > 0.0f ? c.o.giMaxDistance : kInf;
+  float cpx = 0.0f, cpy = 0.0f;
+  if (c.o.pt1Ld) {
+    uint32_t c0 = seed, c1 = 0x9E3779B9u;
+    tea2(c0, c1);
+    cpx = u32ToUnorm(c0);
+    cpy = u32ToUnorm(c1);
+  }
+  V3 Esum{0.0f, 0.0f, 0.0f};
+  for (int sI = 0; sI < spp; ++sI) {
+    uint32_t s0 = seed, s1 = static_cast<uint32_t>(sI);
+    tea2(s0, s1);
+    float u1, u2;
+    if (c.o.pt1Ld) {
+      u1 = static_cast<float>(sI) / static_cast<float>(spp) + cpx;
+      u2 = radicalInverse2(static_cast<uint32_t>(sI)) + cpy;
+      if (u1 >= 1.0f) u1 -= 1.0f;
+      if (u2 >= 1.0f) u2 -= 1.0f;
+    } else {
+      u1 = u32ToUnorm(s0);
+      u2 = u32ToUnorm(s1);
+    }
+    V3 wi = cosineSampleHemisphere(u1, u2, f);
+    const bool horizonOk = dot(wi, Ng) > 0.0f;
+    V3 org = O;
+    float tnear = eps;
+    V3 thr{1.0f, 1.0f, 1.0f}, L{0.0f, 0.0f, 0.0f};
+    for (int b = 1; horizonOk && b <= maxB; ++b) {
+      Ray r;
+      r.org = org; r.dir = wi; r.tnear = tnear; r.tfar = maxD;
+      Hit h;
+      if (!s.bvh.closest(r, h)) {
+        const V3 env = pt1Environment(c, wi);
+        L.x += thr.x * env.x;
+        L.y += thr.y * env.y;
+        L.z += thr.z * env.z;
+        break;
+      }
+      V3 rad, alb, Py, Ny;
+      if (!pt1EvalVertex(c, h, org, wi, rad, alb, Py, Ny)) break;
+      L.x += thr.x * rad.x;
+      L.y += thr.y * rad.y;
+      L.z += thr.z * rad.z;
+      if (b == maxB) break;
+      thr.x *= alb.x;
+      thr.y *= alb.y;
+      thr.z *= alb.z;
+      if (b >= 2) {
+        tea2(s0, s1);
+        float pc = std::fmax(thr.x, std::fmax(thr.y, thr.z));
+        pc = std::fmin(0.95f, std::fmax(0.05f, pc));
+        if (u32ToUnorm(s0) >= pc) break;
+        const float inv = 1.0f / pc;
+        thr.x *= inv;
+        thr.y *= inv;
+        thr.z *= inv;
+      }
+      tea2(s0, s1);
+      const Frame fv = frameFromNormal(Ny);
+      wi = cosineSampleHemisphere(u32ToUnorm(s0), u32ToUnorm(s1), fv);
+      const float epsV = selfIntersectEps(Py, wi, h.t);
+      org = V3{Py.x + Ny.x * epsV, Py.y + Ny.y * epsV, Py.z + Ny.z * epsV};
+      tnear = epsV;
+    }
+    if (c.o.pt1Clamp > 0.0f) {
+      const float lum = 0.2126f * L.x + 0.7152f * L.y + 0.0722f * L.z;
+      if (lum > c.o.pt1Clamp) {
+        const float k = c.o.pt1Clamp / lum;
+        L.x *= k;
+        L.y *= k;
+        L.z *= k;
+      }
+    }
+    Esum.x += L.x;
+    Esum.y += L.y;
+    Esum.z += L.z;
+  }
+  const float invN = 1.0f / static_cast<float>(spp > 0 ? spp : 1);
+  return V3{Esum.x * invN, Esum.y * invN, Esum.z * invN};
+}
+
 inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32_t px, uint32_t py,
                                const V3& camDir) {
   PixelOut po{};
@@ -1052,6 +1258,7 @@ inline PixelOut integratePixel(const Ctx& c, const V3& org, const V3& rd, uint32
       po.geom = h.geomID;
       po.prim = h.primID;
       po.first = hs;
+      po.firstPos = V3{org.x + rd.x * h.t, org.y + rd.y * h.t, org.z + rd.z * h.t};
       // a backface first hit whose clipped-away front exists (:424-428)
       if (clipOn && ctn > 0.0f && c.o.edgeGbuffer && dot(h.Ng, rd) > 0.0f &&
           clipConfirmFront(*c.s, org, rd, ctn))
@@ -1454,6 +1661,12 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   c.o.aoFalloffPower = d.ao_falloff_power; c.o.aoMultiScale = d.ao_multiscale != 0;
   c.o.aoBentNormal = d.ao_bent_normal != 0; c.o.aoMultibounce = d.ao_multibounce != 0;
   c.o.aoLowDiscrepancy = d.ao_low_discrepancy != 0;
+  c.o.gi = d.gi != 0;
+  c.o.pt1Spp = d.pt1_spp; c.o.giBounces = d.gi_bounces; c.o.pt1SkyMode = d.pt1_sky_mode;
+  c.o.giMaxDistance = d.gi_max_distance; c.o.giIntensity = d.gi_intensity;
+  c.o.giEnvIntensity = d.gi_env_intensity; c.o.pt1Clamp = d.pt1_clamp; c.o.pt1Seed = d.pt1_seed;
+  for (int k = 0; k < 3; ++k) c.o.pt1SkyRadiance[k] = d.pt1_sky_radiance[k];
+  c.o.pt1Ld = d.pt1_ld != 0;
   for (int k = 0; k < 3; ++k) { c.o.aoSky[k] = d.ao_sky_color[k]; c.o.aoGround[k] = d.ao_ground_color[k]; }
   c.o.aoDiffuseFactor = d.ao_diffuse_factor;
   c.o.shadows = d.shadows != 0; c.o.shadowSamples = d.shadow_samples; c.o.envLights = d.env_lights;
@@ -1521,7 +1734,23 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   if (row1 <= row0) { row0 = 0; row1 = H; }
   // storePixelResult (embree_renderer.cpp:213-250): one hi-res sample
   float* patchMask = nullptr;  // set once the coarse AO grid is active
+  // GI seeds per hi-res pixel (storeShadingChannels, embree_renderer.cpp:184-193)
+  std::vector<float> giPos, giNrm, giRef, giDep;
+  std::vector<uint8_t> giEl;
+  if (c.o.gi) {
+    giPos.assign(npix * 3, 0.0f); giNrm.assign(npix * 3, 0.0f); giRef.assign(npix * 3, 0.0f);
+    giDep.assign(npix, 0.0f); giEl.assign(npix, 0);
+  }
   auto store = [&](size_t pix, const PixelOut& po) {
+    if (c.o.gi) {
+      for (int k = 0; k < 3; ++k) {
+        giPos[3 * pix + k] = (&po.firstPos.x)[k];
+        giNrm[3 * pix + k] = (&po.first.normal.x)[k];
+        giRef[3 * pix + k] = (&po.first.giRefl.x)[k];
+      }
+      giDep[pix] = po.depth;
+      giEl[pix] = po.geom == kInvalid ? 0 : po.first.giElig;
+    }
     color[4 * pix] = po.r; color[4 * pix + 1] = po.g; color[4 * pix + 2] = po.b; color[4 * pix + 3] = po.a;
     depth[pix] = po.depth;
     viewZ[pix] = po.viewZ;
@@ -1829,6 +2058,25 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   fr->rays_primary = rays.load();
   fr->capped_rays = capped.load();
 
+  // embree_renderer.cpp:1708-1712, 860-927: the pt1 gather at every eligible
+  // hi-res pixel (gatherPt1Grid, pt1_gather.hpp:525-614: seed = hashU32(pix ^
+  // hashU32(pt1Seed)), shading normal as the horizon normal, first-hit t as
+  // the epsilon scale), then colour += giIntensity * (kd * pigment) * E
+  if (c.o.gi) {
+    const uint32_t seedMix = hashU32(c.o.pt1Seed);
+    for (size_t pix = 0; pix < npix; ++pix) {
+      if (!giEl[pix]) continue;
+      const V3 P{giPos[3 * pix], giPos[3 * pix + 1], giPos[3 * pix + 2]};
+      const V3 N{giNrm[3 * pix], giNrm[3 * pix + 1], giNrm[3 * pix + 2]};
+      const uint32_t seed = hashU32(static_cast<uint32_t>(pix) ^ seedMix);
+      const float tEps = giDep[pix] > 0.0f ? giDep[pix] : 1.0f;
+      const V3 E = pt1GatherPoint(c, P, N, N, seed, tEps);
+      const float gI = c.o.giIntensity;
+      color[4 * pix] += gI * giRef[3 * pix] * E.x;
+      color[4 * pix + 1] += gI * giRef[3 * pix + 1] * E.y;
+      color[4 * pix + 2] += gI * giRef[3 * pix + 2] * E.z;
+    }
+  }
   // fog.cpp:7-36 applyFog on the hi-res viewZ (pipeline.cpp:126-129)
   if (d.fog_enabled) {
     for (size_t i = 0; i < npix; ++i) {

@@ -108,6 +108,10 @@ class RenderDesc(C.Structure):
         ("edge_gbuffer", C.c_uint32), ("denoiser", C.c_int32), ("denoise_iters", C.c_int32),
         ("denoise_sigma_z", C.c_float), ("denoise_sigma_n", C.c_float), ("denoise_sigma_l", C.c_float),
         ("denoise_demodulate_albedo", C.c_uint32),
+        ("gi", C.c_uint32), ("pt1_spp", C.c_int32), ("gi_bounces", C.c_int32), ("gi_max_distance", C.c_float),
+        ("gi_intensity", C.c_float), ("gi_env_intensity", C.c_float), ("pt1_seed", C.c_uint32),
+        ("pt1_sky_mode", C.c_int32), ("pt1_sky_radiance", C.c_float * 3), ("pt1_ld", C.c_uint32),
+        ("pt1_clamp", C.c_float),
     ]
 
 

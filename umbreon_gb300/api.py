@@ -222,6 +222,23 @@ class RenderOptions:
     denoiseSigmaN: float = 128.0
     denoiseSigmaL: float = 4.0
     denoiseDemodulateAlbedo: bool = True
+    # pt1 GI gather (render_options.hpp:85-178).  Built: giIntegrator 1 with
+    # the gather at every supersampled pixel (pt1GatherDiv 1, or -1 / 0
+    # resolving to 1) and pt1Denoise off; other GI settings raise ValueError.
+    gi: bool = False
+    pt1Spp: int = 8
+    giBounces: int = 1
+    giMaxDistance: float = 0.0
+    giIntensity: float = 1.0
+    giEnvIntensity: float = 1.0
+    pt1Seed: int = 0
+    pt1SkyMode: int = 0
+    pt1SkyRadiance: tuple = (1.0, 1.0, 1.0)
+    pt1Ld: bool = True
+    pt1Clamp: float = 0.0
+    pt1GatherDiv: int = -1
+    pt1HalfRes: bool = True
+    pt1Denoise: bool = True
 
     def aoEnhanced(self) -> bool:
         return (self.aoFalloffPower > 0.0 or self.aoMultiScale or self.aoBentNormal or self.aoMultibounce
@@ -292,7 +309,44 @@ def make_render_desc(scene: Scene, opt: RenderOptions):
     d.denoiser, d.denoise_iters = opt.denoiser, opt.denoiseIters
     d.denoise_sigma_z, d.denoise_sigma_n, d.denoise_sigma_l = opt.denoiseSigmaZ, opt.denoiseSigmaN, opt.denoiseSigmaL
     d.denoise_demodulate_albedo = int(opt.denoiseDemodulateAlbedo)
+    if opt.gi:
+        check_gi(opt)
+        # pipeline.cpp:60-78: adaptive AA and coarse-grid AO fall back to the
+        # grid and per-hit AO under GI
+        if d.aa_mode == 1:
+            d.aa_mode = 0
+        if (max(1, opt.supersample) if opt.aoResDiv < 0 else opt.aoResDiv) > 1:
+            d.ao_res_div = 0
+        d.gi = 1
+        d.pt1_spp, d.gi_bounces = opt.pt1Spp, opt.giBounces
+        d.gi_max_distance, d.gi_intensity, d.gi_env_intensity = opt.giMaxDistance, opt.giIntensity, opt.giEnvIntensity
+        d.pt1_seed, d.pt1_sky_mode = opt.pt1Seed & 0xFFFFFFFF, opt.pt1SkyMode
+        for k in range(3):
+            d.pt1_sky_radiance[k] = opt.pt1SkyRadiance[k]
+        d.pt1_ld, d.pt1_clamp = int(opt.pt1Ld), opt.pt1Clamp
     return d, keep
+
+
+def gi_gather_div(opt) -> int:
+    """The pt1 gather grid divisor the reference resolves (pipeline.cpp
+    resolves -1 to the supersample factor; embree_renderer.cpp:717-719 maps 0
+    to 2 or 1 through pt1HalfRes)."""
+    div = opt.pt1GatherDiv
+    if div < 0:
+        div = max(1, opt.supersample)
+    if div == 0:
+        div = 2 if opt.pt1HalfRes else 1
+    return max(1, div)
+
+
+def check_gi(opt) -> None:
+    """Raise ValueError for the GI settings this library does not build."""
+    if opt.giIntegrator != 1:
+        raise ValueError("gi: only giIntegrator 1 (pt1) is built")
+    if gi_gather_div(opt) != 1:
+        raise ValueError("gi: only the full-resolution pt1 gather (pt1GatherDiv 1) is built")
+    if opt.pt1Denoise:
+        raise ValueError("gi: the denoise of the indirect term is not built (set pt1Denoise False)")
 
 
 @dataclass

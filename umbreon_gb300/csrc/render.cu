@@ -73,6 +73,11 @@ struct Bufs {
   const float* reuseAoT;  // stride Params::reuseAo
   uint32_t reuseR;
   const LightD* lights;
+  // pt1 GI gather inputs per hi-res pixel (or null): first-hit position.xyz,
+  // first-hit t; shading normal.xyz, eligibility (1/0); reflectance kd * C
+  float4* giA;
+  float4* giB;
+  float4* giR;
   unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
   uint32_t* counter;  // [0] next-queue size, [1] occlusion work-queue size
   uint32_t* occQueue; // queue slots of hits that cast AO / shadow rays
@@ -791,6 +796,216 @@ UBR_D f3 shadePrincipled(const Params& p, const ubr_material& m, const Surf& sf,
   return out;
 }
 
+// Material::toonLike / diffuseWeight (scene.hpp:171-196).
+UBR_D bool toonLike(const ubr_material& m) {
+  if (m.model == 2u) return true;
+  if (m.model != 0u) return false;
+  if (m.specular > 1.0f || m.phong > 1.0f || m.brilliance == 0.0f) return true;
+  return m.diffuse <= 0.0f && m.specular <= 0.0f && m.phong <= 0.0f && m.reflection <= 0.0f;
+}
+UBR_D float diffuseWeight(const ubr_material& m) { return m.model == 1u ? m.diffuse * (1.0f - m.pbr_metallic) : m.diffuse; }
+
+// 32-bit integer hash (irradiance_cache.hpp:176-184): seeds the gather's
+// per-pixel stream and the bounce vertices' shadow streams.
+UBR_HD uint32_t hashU32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7FEB352Du;
+  x ^= x >> 15;
+  x *= 0x846CA68Bu;
+  x ^= x >> 16;
+  return x;
+}
+
+// The pt1 gather's constants (embree_renderer.cpp:581-612).
+struct GiP {
+  int spp, bounces, ld;
+  float maxDist, clampLum;
+  uint32_t seedMix;   // hashU32(pt1Seed)
+  float envI;         // giEnvIntensity
+  f3 amb, sky, ground, envUp;
+};
+
+// environmentRadiance (irradiance_cache.hpp:188-196): the gather's miss term.
+UBR_D f3 giEnvironment(const GiP& g, f3 wi) {
+  const float w = 0.5f * (dot(wi, g.envUp) + 1.0f);
+  const float e = g.envI;
+  return f3{e * g.amb.x * (g.ground.x + (g.sky.x - g.ground.x) * w),
+            e * g.amb.y * (g.ground.y + (g.sky.y - g.ground.y) * w),
+            e * g.amb.z * (g.ground.z + (g.sky.z - g.ground.z) * w)};
+}
+
+// pt1EvalVertex (pt1_gather.hpp:117-227, pt1 form): a gather-ray hit as a path
+// vertex -- its reflected, hard-shadow-tested direct light (the light's centre
+// ray, whatever the light's radius), its reflectance kd * C, position and
+// shading normal faced toward the ray origin.  Outline primitives end the path.
+template <int KM>
+UBR_D bool pt1Vertex(const DScene& s, const LightD* lights, int nLights, const Hit& h, f3 O, f3 wi, f3& rad,
+                     f3& alb, f3& Py, f3& Ny) {
+  const int kind = refKind(h.ref);
+  const uint32_t prim = refPrim(h.ref);
+  f3 C, NgSh;
+  uint32_t mi;
+  if (kind == kMesh) {
+    const uint32_t i0 = __ldg(&s.meshIdx[3 * prim]), i1 = __ldg(&s.meshIdx[3 * prim + 1]),
+                   i2 = __ldg(&s.meshIdx[3 * prim + 2]);
+    const float w0 = 1.0f - h.u - h.v;
+    float nb[3];
+    for (int k = 0; k < 3; ++k)
+      nb[k] = w0 * __ldg(&s.meshNrm[3 * i0 + k]) + h.u * __ldg(&s.meshNrm[3 * i1 + k]) +
+              h.v * __ldg(&s.meshNrm[3 * i2 + k]);
+    const float4 c0 = __ldg(&s.meshCol[i0]), c1 = __ldg(&s.meshCol[i1]), c2 = __ldg(&s.meshCol[i2]);
+    C = f3{w0 * c0.x + h.u * c1.x + h.v * c2.x, w0 * c0.y + h.u * c1.y + h.v * c2.y,
+           w0 * c0.z + h.u * c1.z + h.v * c2.z};
+    Ny = normalize(f3{nb[0], nb[1], nb[2]});
+    mi = s.meshTriMat ? __ldg(&s.meshTriMat[s.baseTri ? prim % s.baseTri : 0]) : s.meshMat;
+    NgSh = h.Ng;
+  } else {
+    if (__ldg(&s.primFromEdge[kind][prim])) return false;
+    const float4 fc = __ldg(&s.primColor[kind][prim]);
+    mi = __ldg(&s.primMat[kind][prim]);
+    C = f3{fc.x, fc.y, fc.z};
+    Ny = safeNormalize(h.Ng);
+    NgSh = Ny;
+  }
+  const float kd = diffuseWeight(s.mats[mi]);
+  if (dot(Ny, wi) > 0.0f) Ny = neg(Ny);
+  Py = f3{O.x + wi.x * h.t, O.y + wi.y * h.t, O.z + wi.z * h.t};
+  const float eps = selfIntersectEps(Py, wi, h.t);
+  f3 ng = dot(NgSh, Ny) < 0.0f ? neg(NgSh) : NgSh;
+  ng = safeNormalize(ng, Ny);
+  const f3 So{Py.x + ng.x * eps, Py.y + ng.y * eps, Py.z + ng.z * eps};
+  f3 E{0.0f, 0.0f, 0.0f};
+  for (int l = 0; l < nLights; ++l) {
+    const LightD L = lights[l];
+    const float ndl = dot(Ny, L.L);
+    if (ndl <= 0.0f) continue;
+    Ray r{So, L.L, eps, kInfF};
+    Hit hh;
+    uint32_t ovf = 0;
+    Count cnt;
+    const float sh = traverse<false, KM>(travOf(s), r, hh, ovf, &cnt, true) ? 0.0f : 1.0f;
+    E.x += ndl * L.color.x * sh;
+    E.y += ndl * L.color.y * sh;
+    E.z += ndl * L.color.z * sh;
+  }
+  rad = f3{kd * C.x * E.x, kd * C.y * E.y, kd * C.z * E.z};
+  alb = f3{kd * C.x, kd * C.y, kd * C.z};
+  return true;
+}
+
+// gatherPt1Grid + pt1GatherPoint (pt1_gather.hpp:268-614, pt1 form) at every
+// eligible pixel of the hi-res grid, then the [E] composite
+// colour += giIntensity * (kd * pigment) * E (embree_renderer.cpp:908-927).
+// One thread walks one pixel's spp paths: cosine-hemisphere first bounce
+// (Hammersley + Cranley-Patterson shift when ld, else the tea2 stream),
+// closest-hit traversal, NEE at every vertex, the sky on escape, cosine
+// continuation and Russian roulette from the second vertex on.
+template <int KM>
+__global__ void __launch_bounds__(128) k_pt1_gather(Params p, GiP g, DScene s, Bufs b, uint32_t npix) {
+  const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= npix) return;
+  const float4 gb = b.giB[pix];
+  if (gb.w == 0.0f) return;
+  const float4 ga = b.giA[pix];
+  const LightD* lights = b.lights + p.lightOff;
+  const f3 P{ga.x, ga.y, ga.z}, N{gb.x, gb.y, gb.z};
+  const f3 Ng = N;  // the full-resolution gather passes no geometric normal
+  const uint32_t seed = hashU32(pix ^ g.seedMix);
+  const float tEps = ga.w > 0.0f ? ga.w : 1.0f;
+  const Frame3 f = frameFromNormal(N);
+  const float eps = selfIntersectEps(P, N, tEps);
+  const f3 O{P.x + N.x * eps, P.y + N.y * eps, P.z + N.z * eps};
+  const int spp = g.spp, maxB = g.bounces < 1 ? 1 : g.bounces;
+  float cpx = 0.0f, cpy = 0.0f;
+  if (g.ld) {
+    uint32_t c0 = seed, c1 = 0x9E3779B9u;
+    tea2(c0, c1);
+    cpx = u32ToUnorm(c0);
+    cpy = u32ToUnorm(c1);
+  }
+  const TravScene ts = travOf(s);
+  f3 Esum{0.0f, 0.0f, 0.0f};
+  for (int sI = 0; sI < spp; ++sI) {
+    uint32_t s0 = seed, s1 = uint32_t(sI);
+    tea2(s0, s1);
+    float u1, u2;
+    if (g.ld) {
+      u1 = float(sI) / float(spp) + cpx;
+      u2 = radicalInverse2(uint32_t(sI)) + cpy;
+      if (u1 >= 1.0f) u1 -= 1.0f;
+      if (u2 >= 1.0f) u2 -= 1.0f;
+    } else {
+      u1 = u32ToUnorm(s0);
+      u2 = u32ToUnorm(s1);
+    }
+    f3 wi = cosineSampleHemisphere(u1, u2, f);
+    const bool horizonOk = dot(wi, Ng) > 0.0f;
+    f3 org = O;
+    float tnear = eps;
+    f3 thr{1.0f, 1.0f, 1.0f}, L{0.0f, 0.0f, 0.0f};
+    for (int bnc = 1; horizonOk && bnc <= maxB; ++bnc) {
+      Ray r{org, wi, tnear, g.maxDist};
+      Hit h;
+      uint32_t ovf = 0;
+      Count cnt;
+      traverse<false, KM>(ts, r, h, ovf, &cnt, false);
+      if (h.ref == kInvalid) {
+        const f3 env = giEnvironment(g, wi);
+        L.x += thr.x * env.x;
+        L.y += thr.y * env.y;
+        L.z += thr.z * env.z;
+        break;
+      }
+      f3 rad, alb, Py, Ny;
+      if (!pt1Vertex<KM>(s, lights, p.nLights, h, org, wi, rad, alb, Py, Ny)) break;
+      L.x += thr.x * rad.x;
+      L.y += thr.y * rad.y;
+      L.z += thr.z * rad.z;
+      if (bnc == maxB) break;
+      thr.x *= alb.x;
+      thr.y *= alb.y;
+      thr.z *= alb.z;
+      if (bnc >= 2) {
+        tea2(s0, s1);
+        float pc = fmaxf(thr.x, fmaxf(thr.y, thr.z));
+        pc = fminf(0.95f, fmaxf(0.05f, pc));
+        if (u32ToUnorm(s0) >= pc) break;
+        const float inv = 1.0f / pc;
+        thr.x *= inv;
+        thr.y *= inv;
+        thr.z *= inv;
+      }
+      tea2(s0, s1);
+      const Frame3 fv = frameFromNormal(Ny);
+      wi = cosineSampleHemisphere(u32ToUnorm(s0), u32ToUnorm(s1), fv);
+      const float epsV = selfIntersectEps(Py, wi, h.t);
+      org = f3{Py.x + Ny.x * epsV, Py.y + Ny.y * epsV, Py.z + Ny.z * epsV};
+      tnear = epsV;
+    }
+    if (g.clampLum > 0.0f) {
+      const float lum = 0.2126f * L.x + 0.7152f * L.y + 0.0722f * L.z;
+      if (lum > g.clampLum) {
+        const float k = g.clampLum / lum;
+        L.x *= k;
+        L.y *= k;
+        L.z *= k;
+      }
+    }
+    Esum.x += L.x;
+    Esum.y += L.y;
+    Esum.z += L.z;
+  }
+  const float invN = 1.0f / float(spp > 0 ? spp : 1);
+  const f3 E{Esum.x * invN, Esum.y * invN, Esum.z * invN};
+  const float4 rf = b.giR[pix];
+  const float gI = p.giIntensity;
+  float4 c = b.colorHi[pix];
+  c.x += gI * rf.x * E.x;
+  c.y += gI * rf.y * E.y;
+  c.z += gI * rf.z * E.z;
+  b.colorHi[pix] = c;
+}
+
 template <bool BATCH>
 __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, Bufs b, int layer, uint32_t n,
                                                const uint32_t* queue, uint32_t* outQueue) {
@@ -827,6 +1042,7 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
       const uint64_t rb = uint64_t(i) * R;
       AoQ aq;  // AOVs of this hit (neutral unless computed)
       bool patched = false;
+      bool giElig = false;
       if (sf.aoOn) {
         float openness;
         f3 bent = sf.N;
@@ -867,6 +1083,17 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
           aoFactor = f3{sv, sv, sv};
         }
         if (p.aoDiffuseFactor > 0.0f) diffuseAo = 1.0f - p.aoDiffuseFactor * (1.0f - openness);
+      }
+      // --- GI (hit_shader.hpp:221-242, 351-365): an eligible hit (mesh, or a
+      // real primitive) drops its constant ambient for the gathered indirect
+      // the post-pass adds; toon finishes keep a unit ambient and no indirect ---
+      if (p.gi && (sf.kind == kMesh || !sf.fromEdge)) {
+        if (toonLike(m)) {
+          ambLight = f3{1.0f, 1.0f, 1.0f};
+        } else {
+          giElig = true;
+          ambLight = f3{0.0f, 0.0f, 0.0f};
+        }
       }
       const f3 C = sf.C, N = sf.N, V = sf.V;
       f3 out;
@@ -967,6 +1194,14 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
           b.aaN[gpix] = make_float4(sf.N.x, sf.N.y, sf.N.z, __int_as_float(grp));
         }
         if (b.aoPatch) b.aoPatch[gpix] = patched ? 1.0f : 0.0f;
+        if (b.giA) {
+          // first-hit gather seed (transparency.hpp:407-415): position, the
+          // face-forwarded shading normal, eligibility and kd * pigment
+          const float kd = diffuseWeight(m);
+          b.giA[gpix] = make_float4(sf.P.x, sf.P.y, sf.P.z, t);
+          b.giB[gpix] = make_float4(sf.N.x, sf.N.y, sf.N.z, giElig ? 1.0f : 0.0f);
+          b.giR[gpix] = make_float4(kd * sf.C.x, kd * sf.C.y, kd * sf.C.z, 0.0f);
+        }
         if (b.gbObj) {
           // edge G-buffer (hit_shader.hpp:278-300, 460-478; transparency.hpp:394-428)
           uint32_t grp = 0, mat;
@@ -1650,6 +1885,14 @@ ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vect
   if (d.abi_version != UBR_ABI_VERSION) return setError(c, UBR_INVALID_ARGUMENT, "render desc: abi_version mismatch");
   if (d.width <= 0 || d.height <= 0) return setError(c, UBR_INVALID_ARGUMENT, "render desc: width/height must be > 0");
   const int ss = d.supersample < 1 ? 1 : d.supersample;
+  if (d.gi) {
+    if (d.gi_integrator != 1) return setError(c, UBR_INVALID_ARGUMENT, "render desc: gi needs gi_integrator 1 (pt1)");
+    if (d.pt1_spp < 1 || d.gi_bounces < 1)
+      return setError(c, UBR_INVALID_ARGUMENT, "render desc: gi needs pt1_spp >= 1 and gi_bounces >= 1");
+    if (d.aa_mode == 1) return setError(c, UBR_INVALID_ARGUMENT, "render desc: adaptive AA is not supported with gi");
+    if ((d.ao_res_div < 0 ? ss : d.ao_res_div) > 1 && d.ao_samples > 0)
+      return setError(c, UBR_INVALID_ARGUMENT, "render desc: coarse-grid AO is not supported with gi");
+  }
   if (int64_t(d.width) * ss * int64_t(d.height) * ss >= (1ll << 31))
     return setError(c, UBR_INVALID_ARGUMENT, "render desc: supersampled frame too large");
   if (d.light_count && !d.lights) return setError(c, UBR_INVALID_ARGUMENT, "render desc: lights is NULL");
@@ -1687,6 +1930,8 @@ ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vect
   p.aoGround = f3{d.ao_ground_color[0], d.ao_ground_color[1], d.ao_ground_color[2]};
   p.aoDiffuseFactor = d.ao_diffuse_factor;
   p.aoWriteAov = d.ao_write_aov ? 1 : 0;
+  p.gi = d.gi ? 1 : 0;
+  p.giIntensity = d.gi_intensity;
   p.aaMode = d.aa_mode == 1 ? 1 : 0;  // any other value renders the full grid
   p.aaThreshold = d.aa_threshold;
   p.aoEnhanced = (d.ao_falloff_power > 0.0f || d.ao_multiscale || d.ao_bent_normal || d.ao_multibounce ||
@@ -2002,6 +2247,27 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   b.accum = scratchT<float4>(c, 16, npix, st);
   b.tnear = scratchT<float>(c, 17, npix, st);
   b.colorHi = scratchT<float4>(c, 18, npix, st);
+  const bool giOn = p1.gi != 0;
+  GiP gp{};
+  if (giOn) {
+    if (batch) return setError(c, UBR_INVALID_ARGUMENT, "render desc: gi renders one frame per call");
+    b.giA = scratchT<float4>(c, 112, npix, st);
+    b.giB = scratchT<float4>(c, 113, npix, st);
+    b.giR = scratchT<float4>(c, 114, npix, st);
+    // embree_renderer.cpp:581-612: gather sky (uniform, or gradient toward
+    // ao_ground_color), up axis = the AO up axis, tfar = giMaxDistance or inf
+    gp.spp = d0.pt1_spp;
+    gp.bounces = d0.gi_bounces;
+    gp.ld = d0.pt1_ld ? 1 : 0;
+    gp.maxDist = d0.gi_max_distance > 0.0f ? d0.gi_max_distance : kInfF;
+    gp.clampLum = d0.pt1_clamp;
+    gp.seedMix = hashU32(d0.pt1_seed);
+    gp.envI = d0.gi_env_intensity;
+    gp.amb = p1.ambLight;
+    gp.envUp = p1.aoUp;
+    gp.sky = f3{d0.pt1_sky_radiance[0], d0.pt1_sky_radiance[1], d0.pt1_sky_radiance[2]};
+    gp.ground = d0.pt1_sky_mode == 1 ? f3{d0.ao_ground_color[0], d0.ao_ground_color[1], d0.ao_ground_color[2]} : gp.sky;
+  }
   b.depth = scratchT<float>(c, 19, npix, st);
   b.viewZ = scratchT<float>(c, 20, npix, st);
   b.hitGeom = scratchT<uint32_t>(c, 21, npix, st);
@@ -2448,7 +2714,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     UBR_CUDA(c, cudaGetLastError());
     return UBR_OK;
   };
-  const bool useGraph = singleLayer && !prof && !count && c->useGraphs && !adaptive;
+  const bool useGraph = singleLayer && !prof && !count && c->useGraphs && !adaptive && !giOn;
   if (useGraph) {
     // key: everything the captured launches depend on
     std::vector<unsigned char> key(sizeof(Params) + sizeof(DScene) + sizeof(Batch) + sizeof(Bufs) + 64);
@@ -2521,8 +2787,15 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     cudaEventRecord(c->ev[2], s);
     st = coarsePrepass();
     if (st != UBR_OK) return st;
+    if (giOn) UBR_CUDA(c, cudaMemsetAsync(b.giB, 0, size_t(npix) * sizeof(float4), s));
     st = adaptive ? runAdaptive() : runLayers(p1, b, R, nullptr, npix);
     if (st != UBR_OK) return st;
+    if (giOn && !cancelled) {
+      // the pt1 gather and [E] composite, before fog (embree_renderer.cpp:1708-1712)
+      UBR_KM_DISPATCH1(k_pt1_gather, km, (npix + 127) / 128, 128, s, p1, gp, s1, b, npix);
+      ++kernels;
+      UBR_CUDA(c, cudaGetLastError());
+    }
     if (!cancelled) gbClip();
     cudaEventRecord(c->ev[3], s);
     st = post();

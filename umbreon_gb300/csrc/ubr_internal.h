@@ -474,6 +474,8 @@ struct Params {
   int raysPerHit;       // AO rays + all lights' shadow rays
   int shadowRays;       // sum of LightD::samples (0 when shadows inactive)
   int lightOff;         // first light of this frame in the lights array
+  int gi;               // pt1 GI: eligible hits drop their ambient; first hits captured for the gather
+  float giIntensity;
 };
 
 }  // namespace ubr

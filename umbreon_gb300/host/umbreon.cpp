@@ -395,6 +395,22 @@ ubr_render_desc toRenderDesc(const Scene& s, const RenderOptions& o, std::vector
   d.denoise_sigma_n = o.denoiseSigmaN;
   d.denoise_sigma_l = o.denoiseSigmaL;
   d.denoise_demodulate_albedo = o.denoiseDemodulateAlbedo ? 1u : 0u;
+  if (o.gi) {
+    // pipeline.cpp:60-78: adaptive AA and coarse-grid AO fall back under GI
+    if (d.aa_mode == 1) d.aa_mode = 0;
+    if ((o.aoResDiv < 0 ? std::max(1, o.supersample) : o.aoResDiv) > 1) d.ao_res_div = 0;
+    d.gi = 1u;
+    d.pt1_spp = o.pt1Spp;
+    d.gi_bounces = o.giBounces;
+    d.gi_max_distance = o.giMaxDistance;
+    d.gi_intensity = o.giIntensity;
+    d.gi_env_intensity = o.giEnvIntensity;
+    d.pt1_seed = o.pt1Seed;
+    d.pt1_sky_mode = o.pt1SkyMode;
+    for (int k = 0; k < 3; ++k) d.pt1_sky_radiance[k] = o.pt1SkyRadiance[k];
+    d.pt1_ld = o.pt1Ld ? 1u : 0u;
+    d.pt1_clamp = o.pt1Clamp;
+  }
   return d;
 }
 
@@ -402,7 +418,19 @@ void rejectUnsupported(const RenderOptions& opt) {
   if (opt.strokeEdges.enable && opt.objectSpaceEdges.enable)
     throw std::runtime_error(
         "umbreon::render: strokeEdges and objectSpaceEdges are mutually exclusive; enable at most one");
-  if (opt.gi) throw std::runtime_error("umbreon::render: GI is not part of the GB300 ray-cast + shade library");
+  if (opt.gi) {
+    // built: the pt1 gather at every supersampled pixel, without the denoise
+    // of the indirect term (pt1GatherDiv -1 resolves to the supersample
+    // factor in pipeline.cpp, 0 to pt1HalfRes in embree_renderer.cpp:717-719)
+    int div = opt.pt1GatherDiv < 0 ? std::max(1, opt.supersample) : opt.pt1GatherDiv;
+    if (div == 0) div = opt.pt1HalfRes ? 2 : 1;
+    if (opt.giIntegrator != 1)
+      throw std::runtime_error("umbreon::render: only the pt1 GI integrator (giIntegrator = 1) is built");
+    if (div > 1)
+      throw std::runtime_error("umbreon::render: only the full-resolution pt1 gather (pt1GatherDiv = 1) is built");
+    if (opt.pt1Denoise)
+      throw std::runtime_error("umbreon::render: the denoise of the pt1 indirect term is not built (pt1Denoise)");
+  }
   if (opt.strokeEdges.enable || opt.objectSpaceEdges.enable)
     throw std::runtime_error("umbreon::render: edge passes are not part of the GB300 ray-cast + shade library");
 }
