@@ -273,6 +273,33 @@ def _cpu_full_or_band(sc, opt, threads, target_s):
             "sample": f"{r['rows']} of {r['H']} hi-res rows", "cores": threads}
 
 
+def gi_workload(args, flush):
+    """pt1 GI gather (giIntegrator 1, 8 spp, one bounce, full-resolution
+    gather, no denoise of E) on workload 0 with its light shadowed: the frame
+    with and without GI, the gather's share and its path rate."""
+    from umbreon_gb300 import scenes
+    from umbreon_gb300.api import Context
+    from umbreon_gb300.autotune import autotune
+    sc, opt = scenes.space_filling()
+    opt.shadows = True
+    knobs = _knobs(args)
+    if knobs is None:
+        knobs = autotune(sc, opt, pixels=512 * 512)["context"]
+    ctx = Context(0, **knobs)
+    b = ctx.build(sc)
+    ms_d, _, _, _ = _device_frames(ctx, b, sc, opt, 10, 3, flush)
+    gi = copy.copy(opt)
+    gi.gi, gi.giIntegrator, gi.pt1Denoise, gi.pt1GatherDiv, gi.pt1Spp, gi.giBounces = True, 1, False, 1, 8, 1
+    ms_gi, _, _, _ = _device_frames(ctx, b, sc, gi, 10, 3, flush)
+    hits = int((ctx.render(b, sc, gi).hit_geom != 0xFFFFFFFF).sum())
+    b.release()
+    ctx.close()
+    g_ms = max(ms_gi - ms_d, 1e-6)
+    return {"pt1_gi_space_filling_640x480_8spp": {
+        "ms_per_frame_direct": round(ms_d, 4), "ms_per_frame_gi": round(ms_gi, 4), "gather_ms": round(g_ms, 4),
+        "gather_pixels": hits, "gather_Mpaths_s": round(hits * 8 / g_ms / 1e3, 1), "traversal": knobs}}
+
+
 def secondary_workloads(args, flush):
     """Workloads 0, 2 and 3 (space filling, molecular surface, batched
     turntable), GPU device-resident, with the CPU restatement beside them."""
@@ -424,6 +451,7 @@ def secondary_workloads(args, flush):
         entry["pixels"] = int(sum(o.width * o.height for _, _, o in its))
         res[label] = entry
     out["turntable_batch"] = res
+    out.update(gi_workload(args, flush))
     return out
 
 
