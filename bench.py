@@ -12,10 +12,15 @@ buffers: scene upload + GPU BVH build + render + copy of the frame back.
 --impl reference times the reference's CPU path on the host cores.  The
 reference itself (Embree 4 + oneTBB) cannot be built on the GPU host, so
 this arm runs the CPU restatement of the same path (oracle/, kind "port")
-on all host threads, on a row band of the same frame.
+on all host threads; every step renders the whole frame, and rays are
+counted as the GPU counts them (closest-hit calls + AO / shadow rays handed
+to a traversal).
 
 Multi-GPU: frames are independent, so N GPUs run N replicas of the frame
-(weak scaling, no collective on the data path).
+(weak scaling, no collective on the data path): under torchrun each rank
+renders the headline frame on its own GPU; `--gpus N` without torchrun
+starts the N ranks itself.  With N > 1 the 64-frame turntable list is also
+split into contiguous blocks, one per rank.
 """
 from __future__ import annotations
 
@@ -121,64 +126,114 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+L2_POLICY = "flushed (256 MB write) before every timed frame"
+
+
+def _config(sc, opt, wname, ws):
+    """The workload as both arms name it (same keys and values)."""
+    return {"workload": wname, "frame": f"{opt.width}x{opt.height} ss{opt.supersample}",
+            "spheres": sc.sphere_count(), "cylinders": sc.cylinder_count(), "triangles": sc.triangle_count(),
+            "l2": L2_POLICY, "parallelism": f"replicas x{ws}"}
+
+
+class _CpuFlush:
+    """256 MB host write before each timed CPU frame (the CPU arm's cache flush)."""
+
+    def __init__(self):
+        import numpy as np
+        self.buf = np.empty(256 * 1024 * 1024, np.uint8)
+        self.i = 0
+
+    def __call__(self):
+        self.i = (self.i + 1) & 255
+        self.buf.fill(self.i)
+
+
+def _cpu_frame(osc, sc, opt, threads, rows=None):
+    """One CPU render of the frame (or of a band of hi-res rows): the rays the
+    oracle traced (closest-hit calls + AO / shadow rays it handed to a
+    traversal, the unit the GPU counts) and the wall time of the call."""
+    t0 = time.perf_counter()
+    f = osc.render(sc, opt, threads=threads, rows=rows)
+    secs = time.perf_counter() - t0
+    return {"rays": int(f.stats["rays_primary"] + f.stats["rays_occlusion"]), "secs": secs}
+
+
 def run_reference(args):
+    """The reference's CPU path (its restatement, kind "port") on all host
+    threads: every step renders the WHOLE frame of the same workload; the
+    value is traced rays over the summed wall time of the K timed frames."""
     ws, rank, local = _dist()
     if rank != 0:
         return
-    from umbreon_gb300 import scenes
+    from oracle import oracle
     sc, opt, wname = _workload(args)
     threads = os.cpu_count() or 1
+    osc = oracle.OracleScene(sc)
+    flush = _CpuFlush()
     steps = []
-    info = None
     for i in range(args.warmup + args.steps):
-        r = _cpu_band(sc, opt, threads, target_s=args.cpu_seconds / max(1, args.steps))
+        flush()
+        r = _cpu_frame(osc, sc, opt, threads)
         if i >= args.warmup:
             steps.append(r)
-        info = r
-    mrays = sum(s["rays"] for s in steps) / sum(s["secs"] for s in steps) / 1e6
-    ms_frame = sum(s["secs"] * s["frame_rays"] / s["rays"] for s in steps) / len(steps) * 1e3
+    secs = sum(s["secs"] for s in steps)
+    mrays = sum(s["rays"] for s in steps) / secs / 1e6
+    ss = max(1, opt.supersample)
+    sample = f"whole frame ({opt.width * ss}x{opt.height * ss} hi-res samples) per step, all host threads"
     line = {
         "impl": "reference", "metric": METRIC, "value": round(mrays, 3), "unit": "Mrays/s",
-        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_frame, 2),
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(secs / len(steps) * 1e3, 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded PCG32 scene)",
-        "config": {"workload": wname, "sample": f"rows {info['rows']} of {info['H']} hi-res rows per step"},
+        "data": "synthetic (seeded PCG32 scene generator)",
+        "config": _config(sc, opt, wname, ws),
+        "rays_per_frame": int(steps[0]["rays"]),
         "cpu_baseline": {"value": round(mrays, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": f"{info['rows']} hi-res rows of the frame per step (all host threads)"},
+                         "sample": sample},
         "e2e": {"value": round(mrays, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def _cpu_band(sc, opt, threads, target_s):
-    """One CPU step: oracle on a band of rows, rays counted by the oracle's
-    own primary count plus the occlusion rays it traced (estimated from the
-    GPU-identical ray layout: AO samples and one ray per lit light per hit)."""
+def _cpu_baseline(sc, opt, threads, target_s, max_frames=5):
+    """The GPU arm's CPU leg: whole frames of the same workload (cache flushed
+    before each) until about target_s of CPU work, at least one."""
     from oracle import oracle
-    osc = _cpu_band.cache.get(id(sc))
-    if osc is None:
-        osc = oracle.OracleScene(sc)
-        _cpu_band.cache[id(sc)] = osc
+    osc = oracle.OracleScene(sc)
+    flush = _CpuFlush()
+    runs = []
+    while not runs or (sum(r["secs"] for r in runs) < target_s and len(runs) < max_frames):
+        flush()
+        runs.append(_cpu_frame(osc, sc, opt, threads))
+    secs = sum(r["secs"] for r in runs)
+    ss = max(1, opt.supersample)
+    return {"value": round(sum(r["rays"] for r in runs) / secs / 1e6, 3), "unit": "Mrays/s", "cores": threads,
+            "kind": "port", "sample": f"{len(runs)} whole frame(s) of {opt.width * ss}x{opt.height * ss} hi-res "
+                                      f"samples, all host threads",
+            "ms_per_frame": round(secs / len(runs) * 1e3, 1), "rays_per_frame": runs[0]["rays"]}
+
+
+def _cpu_full_or_band(sc, opt, threads, target_s):
+    """CPU restatement on the whole frame when one frame fits in about
+    target_s, else on a middle band of hi-res rows sized to about target_s
+    (rays counted by the oracle on that band)."""
+    from oracle import oracle
+    osc = oracle.OracleScene(sc)
     ss = max(1, opt.supersample)
     H = opt.height * ss
-    W = opt.width * ss
     mid = H // 2
-    if not hasattr(_cpu_band, "rate"):
-        rows = max(2, H // 200)
-        f = osc.render(sc, opt, threads=threads, rows=(mid - rows // 2, mid - rows // 2 + rows))
-        _cpu_band.rate = max(f.stats["render_ms"], 1e-3) / rows
-    want = int(min(H, max(2, target_s * 1e3 / _cpu_band.rate)))
+    probe_rows = max(2, H // 200)
+    r = _cpu_frame(osc, sc, opt, threads, rows=(mid - probe_rows // 2, mid - probe_rows // 2 + probe_rows))
+    want = int(min(H, max(2, target_s / max(r["secs"], 1e-6) * probe_rows)))
+    if want >= H:
+        r = _cpu_frame(osc, sc, opt, threads)
+        return {"Mrays_s": round(r["rays"] / r["secs"] / 1e6, 3), "ms_per_frame": round(r["secs"] * 1e3, 1),
+                "sample": "whole frame", "cores": threads}
     r0 = max(0, mid - want // 2)
-    t0 = time.perf_counter()
-    f = osc.render(sc, opt, threads=threads, rows=(r0, r0 + want))
-    secs = time.perf_counter() - t0
-    hits = int((f.hit_geom[r0:r0 + want] != 0xFFFFFFFF).sum())
-    rays = f.stats["rays_primary"] + hits * (opt.aoSamples + (len(sc.lights) if opt.shadows else 0))
-    frame_rays = rays * H / want
-    return {"rays": rays, "secs": secs, "rows": want, "H": H, "W": W, "frame_rays": frame_rays}
-
-
-_cpu_band.cache = {}
+    r = _cpu_frame(osc, sc, opt, threads, rows=(r0, r0 + want))
+    return {"Mrays_s": round(r["rays"] / r["secs"] / 1e6, 3),
+            "ms_per_frame_est": round(r["secs"] * H / want * 1e3, 1),
+            "sample": f"{want} of {H} hi-res rows (middle band)", "cores": threads}
 
 
 def _device_frames(ctx, built, sc, opt, steps, warmup, flush):
@@ -261,16 +316,6 @@ def _adjoint_timing(ctx, built, sc, opt, flush, ms_forward, rays_forward, steps=
             "adjoint_samples": int(samples),
             "gradients": "sphere colour/centre/radius (device arrays) + material, light, ambient, "
                          "background, fog, AO globals"}
-
-
-def _cpu_full_or_band(sc, opt, threads, target_s):
-    """CPU restatement timed on a band of rows sized to about target_s."""
-    _cpu_band.cache.clear()
-    _cpu_band.__dict__.pop("rate", None)
-    r = _cpu_band(sc, opt, threads, target_s)
-    return {"Mrays_s": round(r["rays"] / r["secs"] / 1e6, 3),
-            "ms_per_frame": round(r["secs"] * r["frame_rays"] / r["rays"] * 1e3, 1),
-            "sample": f"{r['rows']} of {r['H']} hi-res rows", "cores": threads}
 
 
 def gi_workload(args, flush):
@@ -476,6 +521,36 @@ def _resized_ss(scene_opt, res, ss):
     return sc, o
 
 
+def turntable_partitioned(args, rank, ws, local):
+    """The 64-frame turntable list split across ranks (contiguous blocks,
+    replicas.partition): each rank builds the scenes its block needs and
+    renders its block as one batch; frames/s of the whole job (slowest
+    rank's time).  No data crosses ranks."""
+    import torch
+    from umbreon_gb300 import scenes
+    from umbreon_gb300.api import Context
+    bases, items = scenes.turntable_batch()
+    mine = [items[i] for i in replicas.partition(len(items), rank, ws)]
+    ctx = Context(local, **(_knobs(args) or {}))
+    built = {si: ctx.build(bases[si]) for si in sorted({it[0] for it in mine})}
+    batch = [(built[si], sc, o) for si, sc, o in mine]
+    for _ in range(2):
+        ctx.render_batch(batch, want_ids=False)
+
+    def step():
+        t0 = time.perf_counter()
+        ctx.render_batch(batch, want_ids=False)
+        torch.cuda.synchronize()
+        return len(batch), (time.perf_counter() - t0) * 1e3
+
+    job = replicas.timed_steps(step, 3, sync=torch.cuda.synchronize, device=f"cuda:{local}")
+    for b in built.values():
+        b.release()
+    ctx.close()
+    return {"frames_per_s": round(job["units_per_s"], 1), "frames_this_rank": len(mine),
+            "ms_per_batch_slowest_rank": round(job["ms_max"] / 3, 3), "timing": "host wall time, 3 batches"}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -526,29 +601,28 @@ def run_ours(args):
     cf = frame(abi.FRAME_COUNT | abi.FRAME_PROFILE)
     ctr = {"node_bytes": list(cf.node_bytes), "prim_bytes": list(cf.prim_bytes),
            "nodes_visited": list(cf.nodes_visited), "rays": [cf.rays_primary, cf.rays_occlusion]}
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    total_ms, phase = 0.0, [0.0] * 5
-    rays = 0
-    kernels = 0
+    phase = [0.0] * 5
+    tally = {"rays": 0, "kernels": 0}
+
+    def step():
+        flush.zero_()
+        torch.cuda.synchronize()
+        fr = frame(abi.FRAME_PROFILE)
+        for k in range(5):
+            phase[k] += fr.phase_ms[k]
+        n = fr.rays_primary + fr.rays_occlusion
+        tally["rays"] += n
+        tally["kernels"] += fr.kernels
+        return n, fr.total_ms
+
     wall0 = time.perf_counter()
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            fr = frame(abi.FRAME_PROFILE)
-            total_ms += fr.total_ms
-            for k in range(5):
-                phase[k] += fr.phase_ms[k]
-            rays += fr.rays_primary + fr.rays_occlusion
-            kernels += fr.kernels
-        torch.cuda.synchronize()
+        # replicas: the job's time is the slowest rank's, its rays those of all ranks
+        job = replicas.timed_steps(step, args.steps, sync=torch.cuda.synchronize, device=f"cuda:{local}")
     wall = time.perf_counter() - wall0
-    # replicas: the job's time is the slowest rank's, its rays those of all ranks
-    rays_s, total_ms = replicas.job_throughput(rays, total_ms, device=f"cuda:{local}")
-    ms_frame = total_ms / args.steps
-    value = rays_s / 1e6
+    rays, kernels = tally["rays"], tally["kernels"]
+    ms_frame = job["ms_max"] / args.steps
+    value = job["units_per_s"] / 1e6
 
     # roofline of the dominant kernel (per launch = per frame here)
     names = ["trace_closest", "surface", "trace_occlusion", "shade", "post"]
@@ -572,6 +646,12 @@ def run_ours(args):
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": traffic, "algorithmic_bytes_per_launch": int(alg),
                 "launch_ms": round(per_launch_ms, 3)}
+        lim = ROOT / "profiles" / "limiter.json"
+        if lim.exists():
+            # what bounds the kernel in fact (ncu counters of the committed
+            # capture): the node bytes come from L1/L2, so the HBM fraction
+            # above is a node-fetch delivery rate, not DRAM use
+            roof["limiter"] = json.loads(lim.read_text()).get(names[dom])
 
     # end to end through the C-ABI with host buffers: upload + BVH + render + D2H
     # into a pinned host frame (the caller's buffer; pageable memory works too)
@@ -594,30 +674,32 @@ def run_ours(args):
         ectx._L.ubr_scene_release(hw)
     h2d = sum(a.nbytes for a in keepd)
     e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 5))
-    e2e_rays = 0
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    t_build = t_flat = t_up = 0.0
-    for _ in range(e2e_steps):
+    acc = {"build": 0.0, "flat": 0.0, "up": 0.0}
+
+    def e2e_step():
+        t0 = time.perf_counter()
         h = C.c_void_p()
-        tb = time.perf_counter()
         ectx._check(ectx._L.ubr_scene_build(ectx.handle, C.byref(desc), C.byref(h)))
-        t_build += time.perf_counter() - tb
+        acc["build"] += time.perf_counter() - t0
         si = abi.SceneInfo()
         ectx._L.ubr_scene_get_info(h, C.byref(si))
-        t_flat += si.flatten_ms
-        t_up += si.upload_ms
+        acc["flat"] += si.flatten_ms
+        acc["up"] += si.upload_ms
         fr = abi.Frame()
         fr.memory = abi.MEMORY_HOST
         fr.color = abi.ptr(host_color)
         ectx._check(ectx._L.ubr_render(ectx.handle, h, C.byref(rd), C.byref(fr), None, None))
-        e2e_rays += fr.rays_primary + fr.rays_occlusion
         ectx._L.ubr_scene_release(h)
-    e2e_s = max(time.perf_counter() - t0, 1e-9)
+        return fr.rays_primary + fr.rays_occlusion, (time.perf_counter() - t0) * 1e3
+
+    ejob = replicas.timed_steps(e2e_step, e2e_steps, sync=torch.cuda.synchronize, device=f"cuda:{local}") \
+        if e2e_steps else None
+    t_build, t_flat, t_up = acc["build"], acc["flat"], acc["up"]
     if ectx is not ctx:
         ectx.close()
-    e2e = None if args.no_e2e else {"value": round(e2e_rays * ws / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(host_color.nbytes), "ms_per_step": round(e2e_s / max(1, e2e_steps) * 1e3, 2),
+    e2e = None if args.no_e2e else {
+           "value": round(ejob["units_per_s"] / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(host_color.nbytes), "ms_per_step": round(ejob["ms_max"] / e2e_steps, 2),
            "scene_build_ms_per_step": round(t_build / max(1, e2e_steps) * 1e3, 2),
            "of_which_flatten_ms": round(t_flat / max(1, e2e_steps), 2),
            "of_which_upload_ms": round(t_up / max(1, e2e_steps), 2),
@@ -625,11 +707,11 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        r = _cpu_band(sc, opt, threads, target_s=args.cpu_seconds)
-        cpu = {"value": round(r["rays"] / r["secs"] / 1e6, 3), "unit": "Mrays/s", "cores": threads,
-               "kind": "port", "sample": f"{r['rows']} of {r['H']} hi-res rows of the same frame",
-               "ms_per_frame_est": round(r["secs"] * r["frame_rays"] / r["rays"] * 1e3, 1)}
+        cpu = _cpu_baseline(sc, opt, os.cpu_count() or 1, target_s=args.cpu_seconds)
+
+    batch_part = None
+    if ws > 1 and not args.no_secondary:
+        batch_part = turntable_partitioned(args, rank, ws, local)
 
     secondary = None
     if rank == 0 and ws == 1 and not args.no_secondary:
@@ -641,13 +723,10 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms_frame, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded PCG32 scene generator)",
-            "config": {"workload": wname if not (args.frame or args.ss) else wname + "_resized",
-                       "frame": f"{opt.width}x{opt.height} ss{opt.supersample}",
-                       "primitives": info["prim_count"], "bvh_nodes": info["bvh_nodes"],
-                       "l2": "flushed (256 MB write) before every timed frame",
-                       "traversal": dict(knobs, autotuned=tune["table"] if tune else None,
-                                         finalists_full_frame_ms=tune["finalists_full_frame_ms"] if tune else None),
-                       "parallelism": f"replicas x{ws}"},
+            "config": _config(sc, opt, wname if not (args.frame or args.ss) else wname + "_resized", ws),
+            "bvh": {"nodes": info["bvh_nodes"], "primitives_by_kind": info["prim_count"],
+                    "traversal": dict(knobs, autotuned=tune["table"] if tune else None,
+                                      finalists_full_frame_ms=tune["finalists_full_frame_ms"] if tune else None)},
             "ms_per_frame": round(ms_frame, 3),
             "phase_ms_per_frame": {n: round(v / args.steps, 3) for n, v in zip(names, phase)},
             "rays_per_frame": int(rays / args.steps),
@@ -656,6 +735,8 @@ def run_ours(args):
             "gpu_launches": int(kernels), "clocks": clk.summary(),
             "workloads": secondary,
         }
+        if batch_part is not None:
+            line["turntable_partitioned"] = batch_part
         print(json.dumps(line), flush=True)
     built.release()
     ctx.close()
@@ -686,6 +767,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # --gpus N outside torchrun: run N ranks (one per GPU) on this node
+        sys.exit(replicas.launch(args.gpus, str(Path(__file__).resolve()), sys.argv[1:]))
+    ws = _dist()[0]
+    if ws != args.gpus:
+        sys.exit(f"bench.py: --gpus {args.gpus} but {ws} ranks were started")
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -489,7 +489,9 @@ ubr_status ubr_adjoint(ubr_context* ctx, const ubr_scene* scene, const ubr_rende
 /* Segment occlusion for the stroke-edge pass: out[i] = 1 when any geometry
  * lies strictly inside segment (p[i], q[i]) trimmed by eps
  * (embree_renderer.cpp:294-315 plain any-hit branch).  segs = 6*n floats
- * (px py pz qx qy qz), in the memory space given by `memory`. */
+ * (px py pz qx qy qz), in the memory space given by `memory`.  Returns
+ * UBR_TRAVERSAL_LIMIT (answers still written) when a traversal ran out of
+ * stack, since its answer may have missed an occluder. */
 ubr_status ubr_occluded_batch(ubr_context* ctx, const ubr_scene* scene,
                               const float* segs, uint64_t n, float eps,
                               uint8_t* out, int32_t memory);
@@ -503,7 +505,8 @@ ubr_status ubr_occluded_batch(ubr_context* ctx, const ubr_scene* scene,
  * mesh), when the ray meets its face at |cos| <= graze_cos_eps, or when the
  * face's plane passes within coplanar_eps of the segment start (<= 0 disables
  * either test).  exclude_offsets (n + 1 entries, starting at 0) and
- * exclude_faces may both be NULL.  All arrays in the memory space `memory`. */
+ * exclude_faces may both be NULL.  All arrays in the memory space `memory`.
+ * Traversal overflow: UBR_TRAVERSAL_LIMIT, as ubr_occluded_batch. */
 ubr_status ubr_occluded_filtered_batch(ubr_context* ctx, const ubr_scene* scene,
                                        const float* segs, uint64_t n, float eps,
                                        float graze_cos_eps, float coplanar_eps,
@@ -516,13 +519,14 @@ ubr_status ubr_occluded_filtered_batch(ubr_context* ctx, const ubr_scene* scene,
  * they query -- a host with its own strict GPU memory budget, a plugin
  * sandbox whose host owns every device allocation, or a per-frame loop that
  * must not risk an allocation failure or the synchronisation that
- * cudaMalloc/cudaFree can cause.  Same answer as ubr_occluded_batch on HOST
- * buffers (segs = 6*n floats, out = n bytes), staged through one fixed device
- * array compiled into the library (about 12.5 MiB, held by every GPU that
- * loads the library until the process exits).
+ * cudaMalloc/cudaFree can cause.  Same answers and status as
+ * ubr_occluded_batch on HOST buffers (segs = 6*n floats, out = n bytes),
+ * staged through one fixed device array compiled into the library (about
+ * 12.5 MiB, held by every GPU that loads the library until the process
+ * exits).
  *   - n may be at most 524,288; larger n returns UBR_INVALID_ARGUMENT.
- *   - The first call on a device resolves the array's device address with
- *     that device current; make that first call before any stream capture.
+ *   - The first call on a context resolves the array's device address on
+ *     the context's device; make that first call before any stream capture.
  *   - Every call on a device shares the one array: calls whose GPU work
  *     overlaps (other threads, other contexts on the same device) race. */
 ubr_status ubr_occluded_batch_noalloc(ubr_context* ctx, const ubr_scene* scene,

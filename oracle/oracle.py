@@ -158,7 +158,8 @@ class OracleScene:
         st = lib().oracle_render_rows(self.h, C.byref(rd), C.byref(fr), threads, r0, r1)
         if st != 0:
             raise RuntimeError("oracle: unsupported request (adaptive AA with the edge G-buffer)")
-        stats = dict(render_ms=fr.render_ms, rays_primary=fr.rays_primary, capped_rays=fr.capped_rays)
+        stats = dict(render_ms=fr.render_ms, rays_primary=fr.rays_primary, rays_occlusion=fr.rays_occlusion,
+                     capped_rays=fr.capped_rays)
         return FrameResult(opt.width, opt.height, color, depth, vz, hg, hp, fr.render_ms / 1e3, stats, **aovs)
 
     def __del__(self):

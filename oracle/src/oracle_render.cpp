@@ -299,8 +299,14 @@ inline V3 cosineSampleHemisphere(float u1, float u2, const Frame& f) {
   const float y = std::sin(phi) * r;
   return f.t * x + f.b * y + f.n * z;
 }
+// Occlusion-type rays (AO, shadow, AO nearest-hit) traced by this thread:
+// every call below is one traced ray, the same unit the GPU's occlusion
+// kernel counts (rays it hands to a traversal).
+thread_local uint64_t tOccRays = 0;
+
 // secondary_rays.hpp:79-97 occluded
 inline bool occludedQ(const Scene& s, const V3& P, const V3& dir, float tnear, float tfar) {
+  ++tOccRays;
   Ray r;
   r.org = P; r.dir = dir; r.tnear = tnear; r.tfar = tfar;
   return s.bvh.occluded(r);
@@ -350,6 +356,7 @@ inline float computeAO(const Scene& s, const V3& P, const V3& Ng, const V3& Ns, 
 }
 // ambient_occlusion.hpp:72-94 intersectNearest
 inline float intersectNearest(const Scene& s, const V3& O, const V3& dir, float tnear, float tfar) {
+  ++tOccRays;
   Ray r;
   r.org = O; r.dir = dir; r.tnear = tnear; r.tfar = tfar;
   Hit h;
@@ -2019,9 +2026,10 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
     row0 = row1 = 0;  // the pixel loop below has nothing left to do
   }
   std::atomic<int> nextRow{row0};
-  std::atomic<uint64_t> rays{0}, capped{0};
+  std::atomic<uint64_t> rays{0}, capped{0}, occRays{0};
   auto worker = [&]() {
     uint64_t myRays = 0, myCapped = 0;
+    const uint64_t occ0 = tOccRays;
     for (;;) {
       const int py = nextRow.fetch_add(1);
       if (py >= row1) break;
@@ -2045,6 +2053,7 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
     }
     rays += myRays;
     capped += myCapped;
+    occRays += tOccRays - occ0;
   };
   int nt = threads > 0 ? threads : static_cast<int>(std::thread::hardware_concurrency());
   if (nt < 1) nt = 1;
@@ -2057,6 +2066,7 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   if (!adaptive) fr->render_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   fr->rays_primary = rays.load();
   fr->capped_rays = capped.load();
+  fr->rays_occlusion = occRays.load();
 
   // embree_renderer.cpp:1708-1712, 860-927: the pt1 gather at every eligible
   // hi-res pixel (gatherPt1Grid, pt1_gather.hpp:525-614: seed = hashU32(pix ^

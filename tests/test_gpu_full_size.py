@@ -1,63 +1,170 @@
 """The benchmark configurations at their full sizes, GPU against the oracle.
 
-The GPU renders each whole frame (the bench's own scene and options); the
-oracle renders a band of hi-res rows of the same frame (its cost scales with
-the rows), and the band is held to the grid parity bars: first-hit agreement
->= 99.9 %, PSNR >= 45 dB, |error| <= 1e-3 at the 99.9th percentile of output
-pixels whose subpixels agree on the first hit (AO / shadow sample flips at
-grazing occluders are the remainder)."""
+The GPU renders each whole frame (the bench's own scene and options).  The
+oracle renders:
+
+* the WHOLE frame of the ball-and-stick headline (1920x1080 ss2) and of the
+  100k-sphere frame (1024^2), as the reference renders a frame (its pixel
+  loop, render/embree_renderer.cpp:1393-1427, is the unit of work);
+* four bands of hi-res rows spread over the 2048^2 molecular surface (top,
+  upper middle, lower middle, bottom: 12.5 % of its rows);
+* one band of rows of every one of the 64 turntable frames.
+
+Bars: first-hit (geomID, primID) agreement >= 99.9 %, PSNR >= 45 dB (linear
+and sRGB), and on output pixels whose subpixels agree on the first hit
+|error| <= 1e-3 at the 99.9th percentile (an AO or shadow ray that grazes an
+occluder may flip between the float orders of the two sides; one flip moves
+a pixel by a whole sample's weight).  The strict maximum and the number of
+pixels above 1e-3 are reported beside the quantile; the deterministic pass
+(no AO, no shadow rays) is held to the strict maximum itself.
+
+Set UBR_PARITY_REPORT to a file path to get these figures as JSON lines.
+"""
+import copy
+import json
+import os
+
 import numpy as np
 import pytest
 
-from parity import agree_mask_final, id_agreement, psnr_linear, psnr_srgb
+from parity import agree_mask_final, psnr_linear, psnr_srgb
 from umbreon_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
 QUANTILE = 0.999
+TOL = 1e-3
 
 
-def _band_parity(gpu_ctx, oracle_lib, sc, opt, rows):
+def _report(name, info):
+    path = os.environ.get("UBR_PARITY_REPORT")
+    if path:
+        with open(path, "a") as f:
+            f.write(json.dumps(dict(case=name, **info)) + "\n")
+
+
+def _compare(g, o, ss, bands):
+    """Parity figures over the given hi-res row bands [(r0, r1), ...]."""
+    agree_n = hits = 0
+    tot = 0
+    diffs, gcs, ocs = [], [], []
+    for r0, r1 in bands:
+        assert r0 % ss == 0 and r1 % ss == 0
+        hs, os_ = slice(r0, r1), slice(r0 // ss, r1 // ss)
+        a = (g.hit_geom[hs] == o.hit_geom[hs]) & (g.hit_prim[hs] == o.hit_prim[hs])
+        agree_n += int(a.sum())
+        tot += a.size
+        hits += int((g.hit_geom[hs] != 0xFFFFFFFF).sum())
+        m = agree_mask_final(g.hit_geom[hs], g.hit_prim[hs], o.hit_geom[hs], o.hit_prim[hs], ss)
+        gc, oc = g.color[os_], o.color[os_]
+        diffs.append(np.abs(gc - oc)[m].reshape(-1, 4).max(axis=1))
+        gcs.append(gc)
+        ocs.append(oc)
+    return _figures(agree_n / tot, hits / tot, np.concatenate(diffs), np.concatenate(gcs), np.concatenate(ocs))
+
+
+def _figures(agree, hits, d, gc, oc):
+    return dict(agree=agree, hits=hits, pixels=int(d.size),
+                err_q999=float(np.quantile(d, QUANTILE)) if d.size else 0.0,
+                err_max=float(d.max()) if d.size else 0.0,
+                above_1e3=int((d > TOL).sum()), frac_above_1e3=float((d > TOL).mean()) if d.size else 0.0,
+                psnr_lin=psnr_linear(gc, oc), psnr_srgb=psnr_srgb(gc, oc))
+
+
+def _check(name, info, strict=False):
+    _report(name, info)
+    assert info["hits"] > 0.05, info  # the frame shows geometry
+    assert info["agree"] >= 0.999, info
+    assert info["psnr_lin"] >= 45.0 and info["psnr_srgb"] >= 45.0, info
+    assert info["err_q999"] <= TOL, info
+    if strict:
+        assert info["err_max"] <= TOL, info
+
+
+def _render_both(gpu_ctx, oracle_lib, sc, opt, bands=None):
     b = gpu_ctx.build(sc)
     try:
         g = gpu_ctx.render(b, sc, opt)
     finally:
         b.release()
-    o = oracle_lib.OracleScene(sc).render(sc, opt, rows=rows)
+    osc = oracle_lib.OracleScene(sc)
     ss = max(1, opt.supersample)
-    r0, r1 = rows
-    assert r0 % ss == 0 and r1 % ss == 0
-    hs = slice(r0, r1)
-    os_ = slice(r0 // ss, r1 // ss)
-    agree = id_agreement(g.hit_geom[hs], g.hit_prim[hs], o.hit_geom[hs], o.hit_prim[hs])
-    m = agree_mask_final(g.hit_geom[hs], g.hit_prim[hs], o.hit_geom[hs], o.hit_prim[hs], ss)
-    gc, oc = g.color[os_], o.color[os_]
-    diff = np.abs(gc - oc)[m]
-    info = dict(agree=agree, hits=float(np.mean(g.hit_geom[hs] != 0xFFFFFFFF)),
-                err=float(np.quantile(diff, QUANTILE)), worst=float(diff.max()),
-                psnr_lin=psnr_linear(gc, oc), psnr_srgb=psnr_srgb(gc, oc))
-    assert info["hits"] > 0.05, info  # the band shows geometry
-    assert agree >= 0.999, info
-    assert info["psnr_lin"] >= 45.0 and info["psnr_srgb"] >= 45.0, info
-    assert info["err"] <= 1e-3, info
-    return info
+    H = opt.height * ss
+    if bands is None:
+        o = osc.render(sc, opt)
+        return g, o, [(0, H)]
+    o = None
+    for r0, r1 in bands:
+        ob = osc.render(sc, opt, rows=(r0, r1))
+        if o is None:
+            o = ob
+        else:  # merge the band into one frame
+            o.hit_geom[r0:r1] = ob.hit_geom[r0:r1]
+            o.hit_prim[r0:r1] = ob.hit_prim[r0:r1]
+            o.color[r0 // ss:r1 // ss] = ob.color[r0 // ss:r1 // ss]
+    return g, o, bands
 
 
-def test_ball_and_stick_1920x1080_ss2(gpu_ctx, oracle_lib):
+def test_ball_and_stick_1920x1080_ss2_whole_frame(gpu_ctx, oracle_lib):
     sc, opt = scenes.ball_and_stick()
-    _band_parity(gpu_ctx, oracle_lib, sc, opt, (1000, 1160))
+    g, o, bands = _render_both(gpu_ctx, oracle_lib, sc, opt)
+    _check("ball_and_stick_1920x1080_ss2", _compare(g, o, opt.supersample, bands))
 
 
-def test_molecular_surface_2048(gpu_ctx, oracle_lib):
+def test_ball_and_stick_whole_frame_deterministic_pass(gpu_ctx, oracle_lib):
+    """No AO and no shadow rays: every value is a deterministic function of
+    the first hits, held to max |error| <= 1e-3 on every agreeing pixel."""
+    sc, opt = scenes.ball_and_stick()
+    opt = copy.copy(opt)
+    opt.aoSamples = 0
+    opt.shadows = False
+    g, o, bands = _render_both(gpu_ctx, oracle_lib, sc, opt)
+    _check("ball_and_stick_1920x1080_ss2_no_ao_no_shadows", _compare(g, o, opt.supersample, bands), strict=True)
+
+
+def test_molecular_surface_2048_four_bands(gpu_ctx, oracle_lib):
     sc, opt = scenes.molecular_surface()
-    _band_parity(gpu_ctx, oracle_lib, sc, opt, (1000, 1048))
+    H = opt.height * max(1, opt.supersample)
+    bands = [(r, r + 64) for r in (256, 704, 1280, 1728)]
+    assert bands[-1][1] <= H
+    g, o, bands = _render_both(gpu_ctx, oracle_lib, sc, opt, bands)
+    _check("molecular_surface_2048_4x64_rows", _compare(g, o, max(1, opt.supersample), bands))
 
 
-def test_differentiable_100k_1024(gpu_ctx, oracle_lib):
+def test_differentiable_100k_1024_whole_frame(gpu_ctx, oracle_lib):
     sc, opt = scenes.differentiable()
-    _band_parity(gpu_ctx, oracle_lib, sc, opt, (480, 560))
+    g, o, bands = _render_both(gpu_ctx, oracle_lib, sc, opt)
+    _check("spheres_100k_1024_enhanced_ao_fog", _compare(g, o, max(1, opt.supersample), bands))
 
 
-def test_turntable_largest_frame(gpu_ctx, oracle_lib):
+def test_turntable_every_frame(gpu_ctx, oracle_lib):
+    """All 64 frames of the batched workload, each GPU frame rendered alone
+    and a 64-row band of it checked against the oracle (the bars over the
+    union of the bands, and per frame the first-hit agreement)."""
     bases, items = scenes.turntable_batch()
-    si, sc, opt = max(items, key=lambda it: (it[2].width, bases[it[0]].sphere_count()))
-    _band_parity(gpu_ctx, oracle_lib, sc, opt, (opt.height // 2 - 32, opt.height // 2 + 32))
+    built = [gpu_ctx.build(bs) for bs in bases]
+    oscs = {}
+    try:
+        agree_n = tot = hits = 0
+        diffs, gcs, ocs = [], [], []
+        for k, (si, sc, opt) in enumerate(items):
+            g = gpu_ctx.render(built[si], sc, opt)
+            if si not in oscs:
+                oscs[si] = oracle_lib.OracleScene(sc)
+            r0 = (k * 37 % max(1, opt.height // 64)) * 64  # bands at varying heights
+            rs = slice(r0, r0 + 64)
+            o = oscs[si].render(sc, opt, rows=(r0, r0 + 64))
+            a = (g.hit_geom[rs] == o.hit_geom[rs]) & (g.hit_prim[rs] == o.hit_prim[rs])
+            assert a.mean() >= 0.995, (k, float(a.mean()))  # per frame; the union is held to 99.9 %
+            agree_n += int(a.sum())
+            tot += a.size
+            hits += int((g.hit_geom[rs] != 0xFFFFFFFF).sum())
+            m = agree_mask_final(g.hit_geom[rs], g.hit_prim[rs], o.hit_geom[rs], o.hit_prim[rs], 1)
+            diffs.append(np.abs(g.color[rs] - o.color[rs])[m].reshape(-1, 4).max(axis=1))
+            gcs.append(g.color[rs].reshape(-1, 4))
+            ocs.append(o.color[rs].reshape(-1, 4))
+        info = _figures(agree_n / tot, hits / tot, np.concatenate(diffs), np.concatenate(gcs), np.concatenate(ocs))
+        info["frames"] = len(items)
+        _check("turntable_64_frames_64_row_bands", info)
+    finally:
+        for b in built:
+            b.release()

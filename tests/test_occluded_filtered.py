@@ -109,3 +109,30 @@ def test_gpu_matches_oracle(graze, coplanar):
     assert ref.sum() > 1000 and (ref == 0).sum() > 1000
     # filtering only removes occluders
     assert np.all(got <= plain)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("workload", ["ball_and_stick", "molecular_surface"])
+def test_gpu_plain_segments_match_oracle(workload):
+    """ubr_occluded_batch (the plain any-hit branch, embree_renderer.cpp:
+    294-315) against the oracle's test of the same trimmed open segments, on
+    spheres + capped cylinders and on a mesh + spheres."""
+    from oracle import oracle
+    from umbreon_gb300.api import Context
+    if workload == "ball_and_stick":
+        sc, _ = scenes.ball_and_stick(n=4000, width=32, height=32, supersample=1)
+        rng = np.random.default_rng(11)
+        pos = sc.sphere_center_radius[:, :3]
+        a = rng.uniform(pos.min(0) - 1.0, pos.max(0) + 1.0, size=(50000, 3))
+        segs = np.concatenate([a, a + rng.normal(scale=3.0, size=(50000, 3))], 1).astype(np.float32)
+    else:
+        sc, _ = scenes.molecular_surface(n_atoms=400, n_spheres=150, box=14.0, width=32, height=32, ao_samples=0)
+        segs, _ = _random_queries(sc, 50000, seed=5)
+    ref = oracle.OracleScene(sc).occluded_filtered(segs, 1e-4)
+    ctx = Context(0)
+    built = ctx.build(sc)
+    got = ctx.occluded(built, segs, 1e-4)
+    built.release()
+    ctx.close()
+    assert (got == ref).mean() >= 0.9995, int((got != ref).sum())
+    assert ref.sum() > 1000 and (ref == 0).sum() > 1000

@@ -60,3 +60,63 @@ def test_two_gloo_ranks_slowest_rank_sets_the_time():
     # slowest rank: 32 frames x 2 ms; all ranks: 64,000 rays
     assert ms0 == ms1 == 64.0
     assert u0 == u1 == pytest.approx(64000.0 / 0.064)
+
+
+def _timed_rank_main(rank, world, port, q):
+    """One rank of the bench's replica loop with a stub render: rank r renders
+    its block of the 64-frame list, each frame 1,000 rays in (r + 1) ms."""
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE=str(world), RANK=str(rank),
+                      LOCAL_RANK=str(rank))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        mine = replicas.partition(64, rank, world)
+        calls = []
+
+        def step():  # one "batch" = this rank's frames
+            calls.append(1)
+            return 1000.0 * len(mine), float(len(mine) * (rank + 1))
+
+        job = replicas.timed_steps(step, 3)
+        q.put((rank, len(calls), job))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_timed_replica_loop():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_timed_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted((q.get(timeout=120) for _ in procs), key=lambda t: t[0])
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, ncalls, job in out:
+        assert ncalls == 3
+        # the slowest rank (rank 1: 32 frames x 2 ms x 3 batches) sets the time;
+        # units are both ranks' 3 x 64,000 rays
+        assert job["ms_max"] == 3 * 32 * 2.0
+        assert job["units_all"] == 3 * 64000.0
+        assert job["units_per_s"] == pytest.approx(3 * 64000.0 / (3 * 32 * 2.0e-3))
+    assert out[0][2]["local_units"] == 3 * 32000.0
+
+
+def test_launch_command_runs_n_ranks_on_localhost():
+    cmd = replicas.launch_cmd(4, "bench.py", ["--gpus", "4", "--steps", "2"], port=29999)
+    assert cmd[1:3] == ["-m", "torch.distributed.run"]
+    assert "--nproc-per-node=4" in cmd and "--master-addr=127.0.0.1" in cmd and "--master-port=29999" in cmd
+    assert cmd[-5:] == ["bench.py", "--gpus", "4", "--steps", "2"]
+
+
+def test_bench_refuses_a_rank_count_that_does_not_match_gpus(tmp_path):
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, WORLD_SIZE="1", RANK="0", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--impl", "reference"],
+                       env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0 and "--gpus 2 but 1 ranks" in r.stderr

@@ -20,7 +20,6 @@
 // bit-reproducible.
 #include <algorithm>
 #include <chrono>
-#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -2958,6 +2957,17 @@ ubr_status renderBatch(Context* c, const std::vector<Job>& jobs, ubr_frame* tota
   return UBR_OK;
 }
 
+// End of a segment query: wait for its answers and report a traversal that
+// ran out of stack or steps (its answer may have missed an occluder) as
+// UBR_TRAVERSAL_LIMIT; the answers are written either way.
+ubr_status finishQuery(Context* c, const unsigned long long* stats) {
+  unsigned long long ovf = 0;
+  UBR_CUDA(c, cudaMemcpyAsync(&ovf, stats + 3, sizeof(ovf), cudaMemcpyDeviceToHost, c->stream));
+  UBR_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (ovf) return setError(c, UBR_TRAVERSAL_LIMIT, "traversal stack overflow");
+  return UBR_OK;
+}
+
 ubr_status occludedBatch(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps, uint8_t* out,
                          int32_t memory) {
   if (n == 0) return UBR_OK;
@@ -2979,8 +2989,7 @@ ubr_status occludedBatch(Context* c, const Scene* sc, const float* segs, uint64_
   k_occluded_segments<<<uint32_t((n + 127) / 128), 128, 0, s>>>(sc->view, dsegs, n, eps, dout, stats);
   UBR_CUDA(c, cudaGetLastError());
   if (memory != UBR_MEMORY_DEVICE) UBR_CUDA(c, cudaMemcpyAsync(out, dout, size_t(n), cudaMemcpyDeviceToHost, s));
-  UBR_CUDA(c, cudaStreamSynchronize(s));
-  return UBR_OK;
+  return finishQuery(c, stats);
 }
 
 ubr_status occludedFilteredBatch(Context* c, const Scene* sc, const float* segs, uint64_t n, float eps,
@@ -3027,8 +3036,7 @@ ubr_status occludedFilteredBatch(Context* c, const Scene* sc, const float* segs,
                                                                 stats);
   UBR_CUDA(c, cudaGetLastError());
   if (memory != UBR_MEMORY_DEVICE) UBR_CUDA(c, cudaMemcpyAsync(out, dout, size_t(n), cudaMemcpyDeviceToHost, s));
-  UBR_CUDA(c, cudaStreamSynchronize(s));
-  return UBR_OK;
+  return finishQuery(c, stats);
 }
 
 }  // namespace ubr
@@ -3055,21 +3063,18 @@ namespace ubr {
 
 namespace {
 
-// Device address of g_noallocScratch for each device, resolved once per
-// device (with that device current) by the first call made on it.
-std::mutex g_noallocMutex;
-void* g_noallocPtr[64] = {};
-
+// Device address of g_noallocScratch, resolved by the first allocation-free
+// call made on a context (its device is current on the calling thread then:
+// every entry point makes it so) and kept in the context.  A context never
+// outlives its device's primary context, so the address stays valid for it.
 ubr_status noallocScratch(Context* c, unsigned char** out) {
-  if (c->device < 0 || c->device >= 64) return setError(c, UBR_INVALID_ARGUMENT, "device ordinal out of range");
-  std::lock_guard<std::mutex> lk(g_noallocMutex);
-  if (!g_noallocPtr[c->device]) {
+  if (!c->noallocArray) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
     if (e != cudaSuccess) return cudaFail(c, e, "cudaGetSymbolAddress(g_noallocScratch)");
-    g_noallocPtr[c->device] = p;
+    c->noallocArray = p;
   }
-  *out = static_cast<unsigned char*>(g_noallocPtr[c->device]);
+  *out = static_cast<unsigned char*>(c->noallocArray);
   return UBR_OK;
 }
 
@@ -3095,11 +3100,7 @@ ubr_status occludedBatchNoAlloc(Context* c, const Scene* sc, const float* segs, 
   k_occluded_segments<<<uint32_t((n + 127) / 128), 128, 0, s>>>(sc->view, dsegs, n, eps, dout, stats);
   UBR_CUDA(c, cudaGetLastError());
   UBR_CUDA(c, cudaMemcpyAsync(out, dout, size_t(n), cudaMemcpyDeviceToHost, s));
-  unsigned long long ovf = 0;
-  UBR_CUDA(c, cudaMemcpyAsync(&ovf, stats + 3, sizeof(ovf), cudaMemcpyDeviceToHost, s));
-  UBR_CUDA(c, cudaStreamSynchronize(s));
-  if (ovf) return setError(c, UBR_TRAVERSAL_LIMIT, "traversal stack overflow");
-  return UBR_OK;
+  return finishQuery(c, stats);
 }
 
 }  // namespace ubr

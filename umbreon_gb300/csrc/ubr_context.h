@@ -40,6 +40,7 @@ struct Context {
   std::vector<unsigned char> graphKey;  // launch parameters the graph was captured with
   std::vector<void*> sceneHandles;      // live ubr_scene handles built on this context
   cudaMemPool_t pool = nullptr;         // stream-ordered device allocations (scenes, scratch)
+  void* noallocArray = nullptr;         // device address of the allocation-free query's fixed array
 };
 
 struct Scene {

@@ -9,6 +9,9 @@ GPUs, gloo on the CPU).
 from __future__ import annotations
 
 import os
+import socket
+import subprocess
+import sys
 
 
 def env_ranks():
@@ -47,3 +50,49 @@ def job_throughput(local_units: float, local_ms: float, device=None) -> tuple[fl
     ms = max_over_ranks(local_ms, device)
     units = sum_over_ranks(local_units, device)
     return units / (ms / 1e3), ms
+
+
+def barrier() -> None:
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.barrier()
+
+
+def timed_steps(step, steps: int, sync=lambda: None, device=None) -> dict:
+    """The per-rank timed loop of a replica job.
+
+    Every rank runs `steps` calls of ``step()`` between a barrier and a
+    ``sync()`` (``torch.cuda.synchronize`` on a GPU) on both sides.  A step
+    returns (units, ms): the units it processed and its own duration (CUDA
+    events on a GPU).  The job's time is the slowest rank's summed step time,
+    its units those of all ranks.  Returns the job figures and this rank's."""
+    barrier()
+    sync()
+    units = ms = 0.0
+    for _ in range(steps):
+        u, m = step()
+        units += u
+        ms += m
+    sync()
+    barrier()
+    units_s, ms_max = job_throughput(units, ms, device)
+    return {"units_per_s": units_s, "ms_max": ms_max, "units_all": sum_over_ranks(units, device),
+            "local_units": units, "local_ms": ms}
+
+
+def free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def launch_cmd(n: int, script: str, argv: list[str], port: int | None = None) -> list[str]:
+    """torchrun command line that runs `script argv` as n ranks on this node."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+            "--master-addr=127.0.0.1", f"--master-port={port or free_port()}", script] + list(argv)
+
+
+def launch(n: int, script: str, argv: list[str]) -> int:
+    """Run `script` as n ranks (one per GPU) when this process was not
+    started by torchrun; returns the launcher's exit code."""
+    return subprocess.call(launch_cmd(n, script, argv))
