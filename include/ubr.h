@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define UBR_ABI_VERSION 1u
+#define UBR_ABI_VERSION 2u
 
 /* Status codes.  The reference throws std::runtime_error on device/BVH
  * failure (scene_build.cpp:164-168, embree_renderer.cpp:1271-1286); the host
@@ -229,19 +229,17 @@ typedef struct ubr_render_desc {
   float denoise_sigma_n;
   float denoise_sigma_l;
   uint32_t denoise_demodulate_albedo;
-  /* pt1 GI gather: RenderOptions::gi with giIntegrator = 1 (pt1, the
-   * reference's frozen one-bounce anchor), pt1Spp, giBounces, giMaxDistance
-   * (0 = unbounded), giIntensity, giEnvIntensity, pt1Seed, pt1SkyMode /
-   * pt1SkyRadiance (the gather's miss term; mode 1 takes ao_ground_color as
-   * the ground tint), pt1Ld and pt1Clamp (render_options.hpp:85-151).  The
-   * gather runs at every pixel of the supersampled grid (pt1GatherDiv = 1)
-   * with no denoise of the indirect term (pt1Denoise = false); the reduced
-   * gather grid with its upsample and edge patch, the OIDN / a-trous
-   * denoise of E, pt2 and the irradiance cache are not part of this
-   * library.  gi != 0 needs gi_integrator = 1, pt1_spp >= 1,
-   * gi_bounces >= 1, no adaptive AA and no coarse-grid AO (the reference
-   * turns those two off under GI, pipeline.cpp:60-78), and one frame per
-   * call (not ubr_render_batch); otherwise UBR_INVALID_ARGUMENT. */
+  /* GI: RenderOptions::gi with the path-traced gather (pt1, the
+   * reference's frozen anchor, giIntegrator = 1; pt2, its default, = 2),
+   * pt1Spp, giBounces, giMaxDistance (0 = unbounded), giIntensity,
+   * giEnvIntensity, pt1Seed, pt1SkyMode / pt1SkyRadiance (the gather's miss
+   * term; mode 1 takes ao_ground_color as the ground tint), pt1Ld and
+   * pt1Clamp (render_options.hpp:85-151).  gi != 0 needs gi_integrator 1
+   * or 2, pt1_spp >= 1, gi_bounces >= 1, no adaptive AA and no coarse-grid
+   * AO (the reference turns those two off under GI, pipeline.cpp:60-78), and
+   * one frame per call (not ubr_render_batch); otherwise
+   * UBR_INVALID_ARGUMENT.  The irradiance cache (giIntegrator 0) is not part
+   * of this library. */
   uint32_t gi;
   int32_t pt1_spp;
   int32_t gi_bounces;
@@ -253,6 +251,43 @@ typedef struct ubr_render_desc {
   float pt1_sky_radiance[3];
   uint32_t pt1_ld;
   float pt1_clamp;
+  /* the gather grid and what follows it (render_options.hpp:130-176):
+   * pt1GatherDiv (-1 = the supersample factor, 0 = pt1HalfRes ? 2 : 1,
+   * k >= 1 = a ceil(W/k) x ceil(H/k) grid with its own primary rays),
+   * pt1HalfRes, pt1Denoise (the a-trous filter on E at gather resolution:
+   * OIDN is absent, as in a reference build without it), the joint-bilateral
+   * upsample's pt1UpsampleNormalPow / pt1UpsampleDepthScale, and the
+   * silhouette edge patch pt1EdgePatch / pt1EdgePatchSppMul /
+   * pt1EdgePatchThresh.  The denoise takes denoise_iters / denoise_sigma_*
+   * above. */
+  int32_t pt1_gather_div;
+  uint32_t pt1_half_res;
+  uint32_t pt1_denoise;
+  float pt1_upsample_normal_pow;
+  float pt1_upsample_depth_scale;
+  uint32_t pt1_edge_patch;
+  int32_t pt1_edge_patch_spp_mul;
+  float pt1_edge_patch_thresh;
+  /* pt2 (gi_integrator = 2, render_options.hpp:178-252): first-bounce
+   * pattern (0 Owen-scrambled Sobol per pixel, 1 blue noise), emission at
+   * gather vertices, ReSTIR rounds / radius / unbiased / M cap / W clamp,
+   * adaptive spp (threshold, multiplier), emissive-triangle NEE, traced
+   * mirror reflection, glossy reflection (spp, denoise). */
+  int32_t pt2_pattern;
+  uint32_t pt2_emissive;
+  int32_t pt2_rounds;
+  float pt2_radius;
+  uint32_t pt2_unbiased;
+  float pt2_m_cap;
+  float pt2_w_clamp;
+  uint32_t pt2_adaptive;
+  float pt2_adaptive_thresh;
+  int32_t pt2_adaptive_mul;
+  uint32_t pt2_emissive_nee;
+  uint32_t pt2_reflect;
+  uint32_t pt2_glossy;
+  int32_t pt2_glossy_spp;
+  uint32_t pt2_glossy_denoise;
 } ubr_render_desc;
 
 /* Where a frame's buffers live. */
@@ -333,6 +368,16 @@ typedef struct ubr_frame {
   uint8_t* gb_clip_cut;
   float* gb_clip_near_vz;
   float* gb_clip_far_vz;
+  /* GI statistics (FrameResult::pt1Timing, pt1Rays; frame_result.hpp): the
+   * device ms of the gather G-buffer, the gather, the denoise of E, the
+   * upsample and the edge patch; the gather rays (all bounces), the NEE
+   * shadow rays, the G-buffer primary rays, and the number of pixels the
+   * edge patch re-gathered */
+  double gi_ms[5];
+  uint64_t gi_gather_rays;
+  uint64_t gi_nee_rays;
+  uint64_t gi_gbuffer_rays;
+  uint64_t gi_patched_pixels;
 } ubr_frame;
 
 /* Context: one GPU, one CUDA stream, one device arena.  Scenes and frame

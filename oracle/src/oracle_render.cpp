@@ -481,6 +481,13 @@ struct Opt {  // the RenderOptions fields this path reads
   uint32_t pt1Seed = 0;
   float pt1SkyRadiance[3] = {1.0f, 1.0f, 1.0f};
   bool pt1Ld = true;
+  // the gather grid and what follows it (render_options.hpp:130-176)
+  int pt1GatherDiv = 1;  // resolved divisor
+  bool pt1Denoise = false, pt1EdgePatch = false;
+  float pt1UpNormalPow = 32.0f, pt1UpDepthScale = 0.02f, pt1EdgePatchThresh = 0.3f;
+  int pt1EdgePatchSppMul = 4;
+  int denoiseIters = 5;
+  float denoiseSigmaN = 128.0f, denoiseSigmaZ = 1.0f, denoiseSigmaL = 4.0f;
   bool aoEnhanced() const {  // render_options.hpp:79-82
     return aoFalloffPower > 0.0f || aoMultiScale || aoBentNormal || aoMultibounce || aoLowDiscrepancy ||
            aoDiffuseFactor > 0.0f;
@@ -1140,9 +1147,10 @@ inline bool pt1EvalVertex(const Ctx& c, const Hit& h, const V3& O, const V3& wi,
 // no emission): E_stored = (1/spp) sum over cosine-hemisphere paths of the
 // NEE radiance at each vertex and the sky where the path escapes; Russian
 // roulette from the second vertex on.
-inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, uint32_t seed, float epsT) {
+inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, uint32_t seed, float epsT, int spp,
+                         float* occOut) {
   const Scene& s = *c.s;
-  const int spp = c.o.pt1Spp;
+  int nOcc = 0;
   const Frame f = frameFromNormal(N);
   const float eps = selfIntersectEps(P, N, epsT);
   const V3 O{P.x + N.x * eps, P.y + N.y * eps, P.z + N.z * eps};
@@ -1171,6 +1179,7 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
     }
     V3 wi = cosineSampleHemisphere(u1, u2, f);
     const bool horizonOk = dot(wi, Ng) > 0.0f;
+    if (!horizonOk) ++nOcc;
     V3 org = O;
     float tnear = eps;
     V3 thr{1.0f, 1.0f, 1.0f}, L{0.0f, 0.0f, 0.0f};
@@ -1185,6 +1194,7 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
         L.z += thr.z * env.z;
         break;
       }
+      if (b == 1) ++nOcc;
       V3 rad, alb, Py, Ny;
       if (!pt1EvalVertex(c, h, org, wi, rad, alb, Py, Ny)) break;
       L.x += thr.x * rad.x;
@@ -1225,6 +1235,7 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
     Esum.z += L.z;
   }
   const float invN = 1.0f / static_cast<float>(spp > 0 ? spp : 1);
+  if (occOut) *occOut = static_cast<float>(nOcc) * invN;
   return V3{Esum.x * invN, Esum.y * invN, Esum.z * invN};
 }
 
@@ -1396,13 +1407,14 @@ inline void buildAaMask(int Wf, int Hf, const AaCentre* c, float thr, float pixe
 // (GI only, absent here) position edge-stops; illumination demodulated by the
 // albedo when given.  normal / albedo: 3 floats per pixel.
 inline void denoiseAtrous(int W, int H, float* color, const float* normal, const float* albedo, int iters,
-                          float sigmaNIn, float sigmaLIn) {
+                          float sigmaNIn, float sigmaLIn, const float* position = nullptr, float sigmaZIn = 1.0f) {
   const size_t N = static_cast<size_t>(W) * H;
   if (W <= 0 || H <= 0 || iters <= 0 || normal == nullptr) return;
   const float kEps = 1.0e-3f;
   auto luminance = [](float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; };
   const float sigmaN = sigmaNIn;
   const float sigmaL = std::max(1.0e-4f, sigmaLIn);
+  const float sigmaZ = std::max(1.0e-4f, sigmaZIn);
   std::vector<unsigned char> valid(N, 0);
   for (size_t p = 0; p < N; ++p) {
     const float nx = normal[p * 3], ny = normal[p * 3 + 1], nz = normal[p * 3 + 2];
@@ -1418,6 +1430,28 @@ inline void denoiseAtrous(int W, int H, float* color, const float* normal, const
       }
       irr[p * 3 + c] = v;
     }
+  // position guide: the largest step to a valid 4-neighbour (floor kEps)
+  std::vector<float> posGrad;
+  if (position) {
+    posGrad.assign(N, kEps);
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const size_t p = static_cast<size_t>(y) * W + x;
+        if (!valid[p]) continue;
+        const V3 pp{position[p * 3], position[p * 3 + 1], position[p * 3 + 2]};
+        float g = kEps;
+        const int nb[4][2] = {{1, 0}, {-1, 0}, {0, 1}, {0, -1}};
+        for (auto& dd : nb) {
+          const int qx = x + dd[0], qy = y + dd[1];
+          if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
+          const size_t q = static_cast<size_t>(qy) * W + qx;
+          if (!valid[q]) continue;
+          const V3 pq{position[q * 3], position[q * 3 + 1], position[q * 3 + 2]};
+          g = std::max(g, length(pp - pq));
+        }
+        posGrad[p] = g;
+      }
+  }
   std::vector<float> var(N, 0.0f);
   for (int y = 0; y < H; ++y)
     for (int x = 0; x < W; ++x) {
@@ -1454,8 +1488,10 @@ inline void denoiseAtrous(int W, int H, float* color, const float* normal, const
           continue;
         }
         const V3 np{normal[p * 3], normal[p * 3 + 1], normal[p * 3 + 2]};
+        const V3 pp = position ? V3{position[p * 3], position[p * 3 + 1], position[p * 3 + 2]} : V3{0, 0, 0};
         const float lp = lum[p];
         const float lDenom = sigmaL * std::sqrt(var[p]) + kEps;
+        const float zDenom = position ? (sigmaZ * posGrad[p] * step + kEps) : 1.0f;
         float sum[3] = {0.0f, 0.0f, 0.0f};
         float wsum = 0.0f;
         for (int dy = -2; dy <= 2; ++dy) {
@@ -1470,6 +1506,10 @@ inline void denoiseAtrous(int W, int H, float* color, const float* normal, const
             const V3 nq{normal[q * 3], normal[q * 3 + 1], normal[q * 3 + 2]};
             const float nd = std::max(0.0f, dot(np, nq));
             w *= std::pow(nd, sigmaN);
+            if (position) {
+              const V3 pq{position[q * 3], position[q * 3 + 1], position[q * 3 + 2]};
+              w *= std::exp(-length(pp - pq) / zDenom);
+            }
             w *= std::exp(-std::fabs(lp - lum[q]) / lDenom);
             sum[0] += w * irr[q * 3];
             sum[1] += w * irr[q * 3 + 1];
@@ -1488,6 +1528,319 @@ inline void denoiseAtrous(int W, int H, float* color, const float* normal, const
       if (albedo) v *= albedo[p * 3 + c];
       color[p * 4 + c] = std::max(0.0f, v);
     }
+  }
+}
+
+// Runs fn(row) for rows [0, n) on nt threads (rows handed out one at a time).
+inline void forRows(int n, int nt, const std::function<void(int)>& fn) {
+  std::atomic<int> next{0};
+  auto w = [&]() {
+    for (int y = next.fetch_add(1); y < n; y = next.fetch_add(1)) fn(y);
+  };
+  std::vector<std::thread> pool;
+  for (int i = 1; i < nt; ++i) pool.emplace_back(w);
+  w();
+  for (auto& th : pool) th.join();
+}
+
+// The camera basis of the render grid (Pt1CameraBasis, pt1_gbuffer.hpp:33-42).
+struct Cam {
+  V3 pos, dir, right, up;
+  bool ortho;
+  float halfW, halfH, persHalfW, persHalfH;
+};
+
+// A gather grid's first hits (Pt1GBuffer, pt1_gbuffer.hpp:70-80).
+struct GiGrid {
+  int w = 0, h = 0;
+  std::vector<float> pos, nrm, gnrm, dep;
+  std::vector<uint8_t> hit;
+};
+
+// pt1_gbuffer.hpp:83-196 tracePt1GBuffer: one primary ray per point of a
+// w x h grid over the render grid's image plane, closest hit in [0, inf):
+// mesh hits take the interpolated vertex normal, real primitives their
+// geometric normal; both normals face the viewer; outline primitives and
+// misses stay zero.
+inline void tracePt1GBuffer(const Ctx& c, const Cam& cam, int w, int h, GiGrid& g, int nt) {
+  const Scene& s = *c.s;
+  const size_t n = static_cast<size_t>(w) * h;
+  g.w = w;
+  g.h = h;
+  g.pos.assign(n * 3, 0.0f);
+  g.nrm.assign(n * 3, 0.0f);
+  g.gnrm.assign(n * 3, 0.0f);
+  g.dep.assign(n, 0.0f);
+  g.hit.assign(n, 0);
+  forRows(h, nt, [&](int py) {
+    const float v = 1.0f - 2.0f * (static_cast<float>(py) + 0.5f) / static_cast<float>(h);
+    for (int px = 0; px < w; ++px) {
+      const float u = 2.0f * (static_cast<float>(px) + 0.5f) / static_cast<float>(w) - 1.0f;
+      V3 org, rd;
+      if (cam.ortho) {
+        org = cam.pos + cam.right * (u * cam.halfW) + cam.up * (v * cam.halfH);
+        rd = cam.dir;
+      } else {
+        org = cam.pos;
+        rd = normalize(cam.dir + cam.right * (u * cam.persHalfW) + cam.up * (v * cam.persHalfH));
+      }
+      Ray r;
+      r.org = org; r.dir = rd; r.tnear = 0.0f; r.tfar = kInf;
+      Hit hh;
+      if (!s.bvh.closest(r, hh)) continue;
+      const int kind = kindOfGeom(s, hh.geomID);
+      V3 N, Ng;
+      if (kind == kMesh) {
+        const uint32_t* tri = &s.geo.triIdx[3 * hh.primID];
+        const float w0 = 1.0f - hh.u - hh.v;
+        float nb[3];
+        for (int k = 0; k < 3; ++k)
+          nb[k] = w0 * s.nrm[3 * tri[0] + k] + hh.u * s.nrm[3 * tri[1] + k] + hh.v * s.nrm[3 * tri[2] + k];
+        N = safeNormalize(V3{nb[0], nb[1], nb[2]});
+        Ng = safeNormalize(hh.Ng);
+      } else {
+        if (s.fromEdge[kind][hh.primID]) continue;
+        N = safeNormalize(hh.Ng);
+        Ng = N;
+      }
+      if (dot(N, rd) > 0.0f) N = V3{-N.x, -N.y, -N.z};
+      if (dot(Ng, rd) > 0.0f) Ng = V3{-Ng.x, -Ng.y, -Ng.z};
+      const size_t pix = static_cast<size_t>(py) * w + px;
+      const V3 P{org.x + rd.x * hh.t, org.y + rd.y * hh.t, org.z + rd.z * hh.t};
+      g.pos[3 * pix] = P.x; g.pos[3 * pix + 1] = P.y; g.pos[3 * pix + 2] = P.z;
+      g.nrm[3 * pix] = N.x; g.nrm[3 * pix + 1] = N.y; g.nrm[3 * pix + 2] = N.z;
+      g.gnrm[3 * pix] = Ng.x; g.gnrm[3 * pix + 1] = Ng.y; g.gnrm[3 * pix + 2] = Ng.z;
+      g.dep[pix] = hh.t;
+      g.hit[pix] = 1;
+    }
+  });
+}
+
+// pt1_gather.hpp:525-614 gatherPt1Grid: E and the first-bounce hit fraction
+// at every marked point of a W x H grid, seeded hashU32(pix ^
+// hashU32(pt1Seed)); the primary hit distance scales the origin epsilon;
+// gnrm null: the shading normal is the horizon normal.
+inline void gatherGrid(const Ctx& c, int W, int H, const float* pos, const float* nrm, const float* gnrm,
+                       const uint8_t* mark, const float* dep, int spp, std::vector<float>& E,
+                       std::vector<float>& occ, int nt) {
+  const size_t n = static_cast<size_t>(W) * H;
+  E.assign(n * 3, 0.0f);
+  occ.assign(n, 0.0f);
+  const uint32_t seedMix = hashU32(c.o.pt1Seed);
+  forRows(H, nt, [&](int py) {
+    for (int px = 0; px < W; ++px) {
+      const size_t pix = static_cast<size_t>(py) * W + px;
+      if (!mark[pix]) continue;
+      const V3 P{pos[3 * pix], pos[3 * pix + 1], pos[3 * pix + 2]};
+      const V3 N{nrm[3 * pix], nrm[3 * pix + 1], nrm[3 * pix + 2]};
+      const V3 Ng = gnrm ? V3{gnrm[3 * pix], gnrm[3 * pix + 1], gnrm[3 * pix + 2]} : N;
+      const uint32_t seed = hashU32(static_cast<uint32_t>(pix) ^ seedMix);
+      const float tEps = dep[pix] > 0.0f ? dep[pix] : 1.0f;
+      float o = 0.0f;
+      const V3 e = pt1GatherPoint(c, P, N, Ng, seed, tEps, spp, &o);
+      E[3 * pix] = e.x; E[3 * pix + 1] = e.y; E[3 * pix + 2] = e.z;
+      occ[pix] = o;
+    }
+  });
+}
+
+// pt1_denoise.cpp:20-80 denoisePt1E without OIDN: non-finite E scrubbed to
+// zero, then the a-trous filter on E (alpha 1) with the normal and position
+// guides and no albedo demodulation.
+inline void denoisePt1E(int w, int h, std::vector<float>& E, const float* nrm, const float* pos, const Opt& o) {
+  const size_t n = static_cast<size_t>(w) * h;
+  for (float& v : E)
+    if (!std::isfinite(v)) v = 0.0f;
+  std::vector<float> rgba(n * 4);
+  for (size_t p = 0; p < n; ++p) {
+    rgba[4 * p] = E[3 * p]; rgba[4 * p + 1] = E[3 * p + 1]; rgba[4 * p + 2] = E[3 * p + 2]; rgba[4 * p + 3] = 1.0f;
+  }
+  denoiseAtrous(w, h, rgba.data(), nrm, nullptr, std::max(0, o.denoiseIters), o.denoiseSigmaN, o.denoiseSigmaL,
+                pos, o.denoiseSigmaZ);
+  for (size_t p = 0; p < n; ++p) {
+    E[3 * p] = rgba[4 * p]; E[3 * p + 1] = rgba[4 * p + 1]; E[3 * p + 2] = rgba[4 * p + 2];
+  }
+}
+
+// pt1_upsample.hpp:40-199 upsampleJointBilateral: E and the hit fraction of
+// every eligible render-grid pixel from the 2x2 gather points around its
+// centre (bilinear x max(0, N.Nh)^normalPow x exp(-|z - zh| / (depthScale z +
+// 1e-6))); dead weights fall back to the quad's nearest valid point, then
+// (fallbackR > 0) the window's; patch marks dead or weak (below thresh) pixels.
+inline void upsampleJointBilateral(int W, int H, const float* fnrm, const float* fdep, const uint8_t* felig,
+                                   const GiGrid& lo, const std::vector<float>& Elo, const std::vector<float>& occLo,
+                                   float normalPow, float depthScale, int fallbackR, std::vector<float>& E,
+                                   std::vector<float>& occ, std::vector<uint8_t>* patch, float thresh) {
+  const size_t n = static_cast<size_t>(W) * H;
+  E.assign(n * 3, 0.0f);
+  occ.assign(n, 0.0f);
+  if (patch) patch->assign(n, 0);
+  const int hw = lo.w, hh = lo.h;
+  for (int py = 0; py < H; ++py) {
+    const float sy = (static_cast<float>(py) + 0.5f) * hh / H - 0.5f;
+    const int by = static_cast<int>(std::floor(sy));
+    const float fy = sy - static_cast<float>(by);
+    for (int px = 0; px < W; ++px) {
+      const size_t pix = static_cast<size_t>(py) * W + px;
+      if (!felig[pix]) continue;
+      const float sx = (static_cast<float>(px) + 0.5f) * hw / W - 0.5f;
+      const int bx = static_cast<int>(std::floor(sx));
+      const float fx = sx - static_cast<float>(bx);
+      const V3 Nf{fnrm[3 * pix], fnrm[3 * pix + 1], fnrm[3 * pix + 2]};
+      const float zf = fdep[pix];
+      float wSum = 0.0f, oSum = 0.0f, bestBilin = -1.0f;
+      V3 eSum{0.0f, 0.0f, 0.0f};
+      long bestPix = -1;
+      for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+          const int hx = std::min(std::max(bx + dx, 0), hw - 1), hy = std::min(std::max(by + dy, 0), hh - 1);
+          const size_t hp = static_cast<size_t>(hy) * hw + hx;
+          if (!lo.hit[hp]) continue;
+          const float wb = (dx ? fx : 1.0f - fx) * (dy ? fy : 1.0f - fy);
+          if (wb > bestBilin) {
+            bestBilin = wb;
+            bestPix = static_cast<long>(hp);
+          }
+          const V3 Nh{lo.nrm[3 * hp], lo.nrm[3 * hp + 1], lo.nrm[3 * hp + 2]};
+          const float wn = std::pow(std::fmax(0.0f, dot(Nf, Nh)), normalPow);
+          const float wz = std::exp(-std::fabs(zf - lo.dep[hp]) / (depthScale * zf + 1e-6f));
+          const float w = wb * wn * wz;
+          wSum += w;
+          eSum.x += w * Elo[3 * hp];
+          eSum.y += w * Elo[3 * hp + 1];
+          eSum.z += w * Elo[3 * hp + 2];
+          oSum += w * occLo[hp];
+        }
+      long src = -1;
+      if (wSum >= 1e-6f) {
+        if (patch && wSum < thresh) (*patch)[pix] = 1;
+        const float inv = 1.0f / wSum;
+        E[3 * pix] = eSum.x * inv; E[3 * pix + 1] = eSum.y * inv; E[3 * pix + 2] = eSum.z * inv;
+        occ[pix] = oSum * inv;
+        continue;
+      }
+      if (patch) (*patch)[pix] = 1;
+      if (bestPix >= 0) {
+        src = bestPix;
+      } else if (fallbackR > 0) {
+        float bestD2 = 1e30f;
+        for (int wy = by - fallbackR + 1; wy <= by + fallbackR; ++wy) {
+          if (wy < 0 || wy >= hh) continue;
+          for (int wx = bx - fallbackR + 1; wx <= bx + fallbackR; ++wx) {
+            if (wx < 0 || wx >= hw) continue;
+            const size_t hp = static_cast<size_t>(wy) * hw + wx;
+            if (!lo.hit[hp]) continue;
+            const float ddx = static_cast<float>(wx) - sx, ddy = static_cast<float>(wy) - sy;
+            const float d2 = ddx * ddx + ddy * ddy;
+            if (d2 < bestD2) {
+              bestD2 = d2;
+              src = static_cast<long>(hp);
+            }
+          }
+        }
+      }
+      if (src >= 0) {
+        E[3 * pix] = Elo[3 * src]; E[3 * pix + 1] = Elo[3 * src + 1]; E[3 * pix + 2] = Elo[3 * src + 2];
+        occ[pix] = occLo[src];
+      }
+    }
+  }
+}
+
+// pt1_upsample.hpp:214-248 smoothPatchedPixels: each marked pixel's E
+// becomes the guide-weighted mean of its (2r+1)^2 eligible neighbourhood in a
+// snapshot (itself at weight 1; weights below 1e-4 dropped).
+inline void smoothPatchedPixels(int W, int H, const std::vector<uint8_t>& mask, const float* fnrm, const float* fdep,
+                                const uint8_t* felig, float normalPow, float depthScale, int radius,
+                                std::vector<float>& E, std::vector<float>& occ) {
+  const std::vector<float> Es = E, os = occ;
+  for (int py = 0; py < H; ++py)
+    for (int px = 0; px < W; ++px) {
+      const size_t pix = static_cast<size_t>(py) * W + px;
+      if (!mask[pix]) continue;
+      const V3 Nf{fnrm[3 * pix], fnrm[3 * pix + 1], fnrm[3 * pix + 2]};
+      const float zf = fdep[pix];
+      float wSum = 1.0f, oSum = os[pix];
+      V3 eSum{Es[3 * pix], Es[3 * pix + 1], Es[3 * pix + 2]};
+      for (int dy = -radius; dy <= radius; ++dy) {
+        const int ny = py + dy;
+        if (ny < 0 || ny >= H) continue;
+        for (int dx = -radius; dx <= radius; ++dx) {
+          if (dx == 0 && dy == 0) continue;
+          const int nx = px + dx;
+          if (nx < 0 || nx >= W) continue;
+          const size_t q = static_cast<size_t>(ny) * W + nx;
+          if (!felig[q]) continue;
+          const V3 Nn{fnrm[3 * q], fnrm[3 * q + 1], fnrm[3 * q + 2]};
+          const float wn = std::pow(std::fmax(0.0f, dot(Nf, Nn)), normalPow);
+          const float wz = std::exp(-std::fabs(zf - fdep[q]) / (depthScale * zf + 1e-6f));
+          const float w = wn * wz;
+          if (w < 1e-4f) continue;
+          wSum += w;
+          eSum.x += w * Es[3 * q];
+          eSum.y += w * Es[3 * q + 1];
+          eSum.z += w * Es[3 * q + 2];
+          oSum += w * os[q];
+        }
+      }
+      const float inv = 1.0f / wSum;
+      E[3 * pix] = eSum.x * inv; E[3 * pix + 1] = eSum.y * inv; E[3 * pix + 2] = eSum.z * inv;
+      occ[pix] = oSum * inv;
+    }
+}
+
+// embree_renderer.cpp:560-934 runPt1GiPass (pt1): the gather on the render
+// grid (k = 1) or on a ceil(W/k) x ceil(H/k) grid with its own primary rays,
+// the denoise of E at gather resolution, the upsample, the edge patch, and
+// the [E] composite colour += giIntensity * (kd * pigment) * E.
+inline void runPt1GiPass(const Ctx& c, const Cam& cam, int W, int H, const std::vector<float>& pos,
+                         const std::vector<float>& nrm, const std::vector<float>& refl, const std::vector<float>& dep,
+                         const std::vector<uint8_t>& elig, std::vector<float>& color, int nt,
+                         uint64_t* patchedOut) {
+  const Opt& o = c.o;
+  const int k = std::max(1, o.pt1GatherDiv);
+  const int spp = std::max(1, o.pt1Spp);
+  std::vector<float> E, occ;
+  if (k > 1) {
+    const int hw = (W + k - 1) / k, hh = (H + k - 1) / k;
+    GiGrid g;
+    tracePt1GBuffer(c, cam, hw, hh, g, nt);
+    std::vector<float> Eh, occh;
+    gatherGrid(c, hw, hh, g.pos.data(), g.nrm.data(), g.gnrm.data(), g.hit.data(), g.dep.data(), spp, Eh, occh,
+               nt);
+    if (o.pt1Denoise) denoisePt1E(hw, hh, Eh, g.nrm.data(), g.pos.data(), o);
+    std::vector<uint8_t> patch;
+    upsampleJointBilateral(W, H, nrm.data(), dep.data(), elig.data(), g, Eh, occh, o.pt1UpNormalPow,
+                           o.pt1UpDepthScale, k <= 2 ? 0 : k, E, occ, o.pt1EdgePatch ? &patch : nullptr,
+                           o.pt1EdgePatchThresh);
+    if (o.pt1EdgePatch) {
+      uint64_t count = 0;
+      for (uint8_t m : patch) count += m;
+      if (patchedOut) *patchedOut = count;
+      if (count > 0) {
+        std::vector<float> Ep, occp;
+        gatherGrid(c, W, H, pos.data(), nrm.data(), nullptr, patch.data(), dep.data(),
+                   spp * std::max(1, o.pt1EdgePatchSppMul), Ep, occp, nt);
+        for (size_t i = 0; i < patch.size(); ++i) {
+          if (!patch[i]) continue;
+          E[3 * i] = Ep[3 * i]; E[3 * i + 1] = Ep[3 * i + 1]; E[3 * i + 2] = Ep[3 * i + 2];
+          occ[i] = occp[i];
+        }
+        smoothPatchedPixels(W, H, patch, nrm.data(), dep.data(), elig.data(), o.pt1UpNormalPow, o.pt1UpDepthScale,
+                            2, E, occ);
+      }
+    }
+  } else {
+    gatherGrid(c, W, H, pos.data(), nrm.data(), nullptr, elig.data(), dep.data(), spp, E, occ, nt);
+    if (o.pt1Denoise) denoisePt1E(W, H, E, nrm.data(), pos.data(), o);
+  }
+  const float gI = o.giIntensity;
+  const size_t n = static_cast<size_t>(W) * H;
+  for (size_t pix = 0; pix < n; ++pix) {
+    if (!elig[pix]) continue;
+    color[4 * pix] += gI * refl[3 * pix] * E[3 * pix];
+    color[4 * pix + 1] += gI * refl[3 * pix + 1] * E[3 * pix + 1];
+    color[4 * pix + 2] += gI * refl[3 * pix + 2] * E[3 * pix + 2];
   }
 }
 
@@ -1674,6 +2027,23 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   c.o.giEnvIntensity = d.gi_env_intensity; c.o.pt1Clamp = d.pt1_clamp; c.o.pt1Seed = d.pt1_seed;
   for (int k = 0; k < 3; ++k) c.o.pt1SkyRadiance[k] = d.pt1_sky_radiance[k];
   c.o.pt1Ld = d.pt1_ld != 0;
+  {
+    // pt1GatherDiv: -1 = the supersample factor (pipeline.cpp), 0 = pt1HalfRes ? 2 : 1 (embree_renderer.cpp:717-719)
+    int k = d.pt1_gather_div;
+    if (k < 0) k = std::max(1, d.supersample);
+    if (k == 0) k = d.pt1_half_res ? 2 : 1;
+    c.o.pt1GatherDiv = std::max(1, k);
+  }
+  c.o.pt1Denoise = d.pt1_denoise != 0;
+  c.o.pt1EdgePatch = d.pt1_edge_patch != 0;
+  c.o.pt1UpNormalPow = d.pt1_upsample_normal_pow;
+  c.o.pt1UpDepthScale = d.pt1_upsample_depth_scale;
+  c.o.pt1EdgePatchThresh = d.pt1_edge_patch_thresh;
+  c.o.pt1EdgePatchSppMul = d.pt1_edge_patch_spp_mul;
+  c.o.denoiseIters = d.denoise_iters;
+  c.o.denoiseSigmaN = d.denoise_sigma_n;
+  c.o.denoiseSigmaZ = d.denoise_sigma_z;
+  c.o.denoiseSigmaL = d.denoise_sigma_l;
   for (int k = 0; k < 3; ++k) { c.o.aoSky[k] = d.ao_sky_color[k]; c.o.aoGround[k] = d.ao_ground_color[k]; }
   c.o.aoDiffuseFactor = d.ao_diffuse_factor;
   c.o.shadows = d.shadows != 0; c.o.shadowSamples = d.shadow_samples; c.o.envLights = d.env_lights;
@@ -2068,24 +2438,12 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   fr->capped_rays = capped.load();
   fr->rays_occlusion = occRays.load();
 
-  // embree_renderer.cpp:1708-1712, 860-927: the pt1 gather at every eligible
-  // hi-res pixel (gatherPt1Grid, pt1_gather.hpp:525-614: seed = hashU32(pix ^
-  // hashU32(pt1Seed)), shading normal as the horizon normal, first-hit t as
-  // the epsilon scale), then colour += giIntensity * (kd * pigment) * E
+  // embree_renderer.cpp:1708-1712: the GI pass before fog
   if (c.o.gi) {
-    const uint32_t seedMix = hashU32(c.o.pt1Seed);
-    for (size_t pix = 0; pix < npix; ++pix) {
-      if (!giEl[pix]) continue;
-      const V3 P{giPos[3 * pix], giPos[3 * pix + 1], giPos[3 * pix + 2]};
-      const V3 N{giNrm[3 * pix], giNrm[3 * pix + 1], giNrm[3 * pix + 2]};
-      const uint32_t seed = hashU32(static_cast<uint32_t>(pix) ^ seedMix);
-      const float tEps = giDep[pix] > 0.0f ? giDep[pix] : 1.0f;
-      const V3 E = pt1GatherPoint(c, P, N, N, seed, tEps);
-      const float gI = c.o.giIntensity;
-      color[4 * pix] += gI * giRef[3 * pix] * E.x;
-      color[4 * pix + 1] += gI * giRef[3 * pix + 1] * E.y;
-      color[4 * pix + 2] += gI * giRef[3 * pix + 2] * E.z;
-    }
+    const Cam cam{camPos, dir, right, trueUp, d.cam_orthographic != 0, halfW, halfH, persHalfW, persHalfH};
+    uint64_t patched = 0;
+    runPt1GiPass(c, cam, W, H, giPos, giNrm, giRef, giDep, giEl, color, nt, &patched);
+    fr->gi_patched_pixels = patched;
   }
   // fog.cpp:7-36 applyFog on the hi-res viewZ (pipeline.cpp:126-129)
   if (d.fog_enabled) {

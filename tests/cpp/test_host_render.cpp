@@ -206,19 +206,28 @@ int main() {
     c("coarse AO: patch mask at render resolution", f.aoPatchMask.size() == 100);
     c("coarse AO: open quad stays lit", f.color[kC] > 0.3f);
   }
-  {  // unsupported requests throw like the reference's failures
+  {  // pt1 GI at its defaults renders (reduced gather grid, denoise, upsample,
+     // edge patch); the irradiance cache is not built and throws
     umbreon::Scene sc;
     sc.mesh = quad({1, 1, 1, 1});
     sc.camera = cam();
+    sc.lights.push_back(key());
     umbreon::RenderOptions o = o5();
+    o.supersample = 2;
     o.gi = true;
+    o.giIntegrator = 1;
+    const umbreon::FrameResult f = umbreon::render(sc, o);
+    c("pt1 defaults: frame rendered", f.color.size() == 100 && f.color[kC] > 0.0f);
+    c("pt1 defaults: gather rays counted", f.pt1Rays.gatherRays > 0 && f.pt1Rays.gbufferRays > 0);
+    c("pt1 defaults: a-trous denoise of E reported", f.pt1DenoiserUsed == 1);
+    o.giIntegrator = 0;
     bool threw = false;
     try {
       umbreon::render(sc, o);
     } catch (const std::runtime_error&) {
       threw = true;
     }
-    c("gi request throws std::runtime_error", threw);
+    c("irradiance-cache GI request throws std::runtime_error", threw);
   }
   {  // async == blocking; cancel before start yields a cancelled frame
     umbreon::Scene sc;

@@ -1,6 +1,7 @@
-"""The pt1 GI gather (integrator/pt1/pt1_gather.hpp at every supersampled
-pixel, the [E] composite of render/embree_renderer.cpp:908-927) on the GPU
-against the oracle.
+"""The pt1 GI pass (integrator/pt1/: the gather on the render grid or on a
+reduced grid with its own primary rays, the denoise of E, the joint-bilateral
+upsample, the silhouette edge patch, and the [E] composite of
+render/embree_renderer.cpp:560-934) on the GPU against the oracle.
 
 Both sides draw the same per-pixel sample streams (hashU32(pix ^
 hashU32(pt1Seed)), tea2, Hammersley + Cranley-Patterson when pt1Ld), so the
@@ -88,4 +89,50 @@ def test_molecular_surface_gi_transparent(gpu_ctx, oracle_lib):
     sc, opt = scenes.molecular_surface(n_atoms=300, box=14.0, n_spheres=60, width=72, height=72, ao_samples=4,
                                        layers=2)
     _gi(opt, pt1Spp=4, giBounces=2, supersample=1)
+    _compare(gpu_ctx, oracle_lib, sc, opt)
+
+
+def _defaults(opt, **kw):
+    """GI on with every pt1 option at the reference's default (gather grid =
+    the supersample factor, a-trous denoise of E, upsample, edge patch)."""
+    opt.gi, opt.giIntegrator = True, 1
+    for k, v in kw.items():
+        setattr(opt, k, v)
+    return opt
+
+
+def test_lone_sphere_known_answer_reduced_grid(gpu_ctx):
+    mat = scenes.pov_material()
+    sc = scenes.material_sphere_scene((0.6, 0.4, 0.2, 1.0), mat, (0.0, 0.0, 0.0))
+    sc.lights = []
+    for ss, div in ((2, -1), (1, 3)):
+        opt = _defaults(RenderOptions(width=48, height=48, supersample=ss), pt1Spp=4, giIntensity=0.5,
+                        giEnvIntensity=2.0, pt1GatherDiv=div)
+        b = gpu_ctx.build(sc)
+        try:
+            g = gpu_ctx.render(b, sc, opt)
+        finally:
+            b.release()
+        hit = (g.hit_geom != KINVALID).reshape(48 * ss, 48, ss).all(-1).reshape(48, ss, 48).all(1)
+        col = g.color[..., :3]
+        want = 0.5 * float(mat["diffuse"]) * np.array([0.6, 0.4, 0.2], np.float32) * 2.0
+        assert int(hit.sum()) > 100
+        np.testing.assert_allclose(col[hit], np.broadcast_to(want, col[hit].shape), rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("ss,div,denoise,patch", [(2, -1, True, True), (1, 2, True, True), (1, 3, True, True),
+                                                  (2, 1, True, False), (1, 2, False, True)])
+def test_ball_and_stick_default_pipeline(gpu_ctx, oracle_lib, ss, div, denoise, patch):
+    """The reference's default pt1 pipeline: reduced gather grid with its own
+    primary rays, the a-trous denoise of E, the joint-bilateral upsample and
+    the silhouette edge patch, against the oracle's restatement of each."""
+    sc, opt = scenes.ball_and_stick(n=800, width=80, height=48, supersample=ss, ao_samples=4)
+    _defaults(opt, pt1Spp=4, giBounces=2, pt1GatherDiv=div, pt1Denoise=denoise, pt1EdgePatch=patch)
+    _compare(gpu_ctx, oracle_lib, sc, opt)
+
+
+def test_molecular_surface_default_pipeline(gpu_ctx, oracle_lib):
+    sc, opt = scenes.molecular_surface(n_atoms=300, box=14.0, n_spheres=60, width=72, height=72, ao_samples=4,
+                                       layers=2)
+    _defaults(opt, pt1Spp=4, supersample=2)
     _compare(gpu_ctx, oracle_lib, sc, opt)

@@ -67,15 +67,87 @@ def test_occluder_darkens_the_gather(oracle_lib):
     assert a > 0
 
 
-@pytest.mark.parametrize("bad,msg", [(dict(giIntegrator=2), "pt1"), (dict(pt1Denoise=True), "denoise"),
-                                     (dict(supersample=2, pt1GatherDiv=-1), "full-resolution"),
-                                     (dict(pt1GatherDiv=0, pt1HalfRes=True), "full-resolution")])
-def test_unbuilt_gi_settings_raise(bad, msg):
-    opt = RenderOptions(width=8, height=8, gi=True, giIntegrator=1, pt1Denoise=False, pt1GatherDiv=1)
-    for k, v in bad.items():
-        setattr(opt, k, v)
-    with pytest.raises(ValueError, match=msg):
+def test_only_the_cache_integrator_is_refused():
+    opt = RenderOptions(width=8, height=8, gi=True, giIntegrator=0)
+    with pytest.raises(ValueError, match="irradiance-cache"):
         api.check_gi(opt)
+    for integ in (1, 2):
+        opt.giIntegrator = integ
+        api.check_gi(opt)
+
+
+@pytest.mark.parametrize("ss,div", [(1, 2), (2, -1), (2, 1), (3, -1), (1, 3)])
+@pytest.mark.parametrize("denoise,patch", [(True, True), (False, True), (True, False)])
+def test_default_pipeline_known_answer(oracle_lib, ss, div, denoise, patch):
+    """The whole pt1 pipeline at the reference's defaults (gather grid =
+    the supersample factor, a-trous denoise of E, joint-bilateral upsample,
+    edge patch) keeps the lone sphere's constant E = sky exactly: every stage
+    is a normalised weighted mean of that constant."""
+    sc, opt, kd = _lone_sphere(pt1Spp=4, giIntensity=0.5, giEnvIntensity=2.0)
+    opt.supersample, opt.pt1GatherDiv, opt.pt1Denoise, opt.pt1EdgePatch = ss, div, denoise, patch
+    o = oracle_lib.render(sc, opt)
+    hit = (o.hit_geom != KINVALID).reshape(32 * ss, 32, ss).all(-1).reshape(32, ss, 32).all(1)
+    col = o.color[..., :3]
+    want = 0.5 * kd * np.array([0.6, 0.4, 0.2], np.float32) * 2.0
+    assert 50 < int(hit.sum()) < 32 * 32
+    np.testing.assert_allclose(col[hit], np.broadcast_to(want, col[hit].shape), rtol=2e-6, atol=1e-7)
+
+
+def _closed_box():
+    """A closed box, floor z = 0 to ceiling z = 1, walls at x, y = +-1, all
+    faces' vertex normals pointing inward, seen from inside by a camera
+    looking down at the floor's middle.  No gather ray escapes to the sky;
+    the light travels straight down, so the floor's shadow rays hit the
+    ceiling, the ceiling faces away from it and the walls are edge-on."""
+    from umbreon_gb300.api import Camera, DistantLight, Scene
+    c = [(x, y, z) for z in (0.0, 1.0) for y in (-1.0, 1.0) for x in (-1.0, 1.0)]
+    quads = [((0, 1, 3, 2), (0, 0, 1)), ((4, 6, 7, 5), (0, 0, -1)), ((0, 4, 5, 1), (0, 1, 0)),
+             ((2, 3, 7, 6), (0, -1, 0)), ((0, 2, 6, 4), (1, 0, 0)), ((1, 5, 7, 3), (-1, 0, 0))]
+    pos, nrm = [], []
+    for (a, b, cc, d), n in quads:
+        for i in (a, b, cc, a, cc, d):
+            pos.append(c[i])
+            nrm.append(n)
+    col = np.tile(np.array([0.8, 0.7, 0.6, 1.0], np.float32), (len(pos), 1))
+    sc = Scene(mesh_positions=np.array(pos, np.float32), mesh_normals=np.array(nrm, np.float32), mesh_colors=col)
+    sc.camera = Camera(position=(0.0, 0.0, 0.5), direction=(0.0, 0.0, -1.0), up=(0.0, 1.0, 0.0),
+                       orthographic=True, height=0.5)
+    sc.lights = [DistantLight(direction=(0.0, 0.0, -1.0), intensity=1.0)]
+    return sc
+
+
+@pytest.mark.parametrize("bounces", [1, 3])
+def test_closed_room_gathers_nothing(oracle_lib, bounces):
+    """No sky is visible and every gather vertex's light is occluded (ceiling
+    vertices' shadow rays hit the floor; floor vertices face away from the
+    light), so E = 0.  The floor's own light is shadowed by the ceiling and
+    GI drops the constant ambient: the GI frame is black, the frame without
+    GI is the ambient term alone."""
+    sc = _closed_box()
+    opt = RenderOptions(width=16, height=16, gi=True, giIntegrator=1, pt1Spp=8, giBounces=bounces, shadows=True)
+    o = oracle_lib.render(sc, opt)
+    assert np.all(o.hit_geom != KINVALID)
+    assert np.all(o.color[..., :3] == 0.0)
+    opt.gi = False
+    d = oracle_lib.render(sc, opt)
+    want = 0.2 * np.array([0.8, 0.7, 0.6], np.float32)
+    np.testing.assert_allclose(d.color[..., :3], np.broadcast_to(want, d.color[..., :3].shape), rtol=1e-6)
+
+
+def test_gather_distance_cut_sees_only_sky(oracle_lib):
+    """giMaxDistance below the distance to any wall or the ceiling: every
+    gather ray ends short and counts as a miss, so E = the uniform sky
+    exactly."""
+    sc = _closed_box()
+    opt = RenderOptions(width=16, height=16, gi=True, giIntegrator=1, pt1Spp=8, giMaxDistance=0.5, giEnvIntensity=1.5)
+    o = oracle_lib.render(sc, opt)
+    opt.giMaxDistance = 0.0
+    closed = oracle_lib.render(sc, opt)
+    # the same frame with the cut: E = sky = ambient (1, 1, 1) x 1.5 on top of the closed room's frame
+    kd = 0.8  # Mesh::material default diffuse
+    diff = o.color[..., :3] - closed.color[..., :3]
+    want = kd * np.array([0.8, 0.7, 0.6], np.float32) * 1.5
+    np.testing.assert_allclose(diff, np.broadcast_to(want, diff.shape), rtol=1e-5, atol=1e-6)
 
 
 def test_gather_div_resolution():

@@ -13,7 +13,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent.parent
 LIBDIR = Path(__file__).resolve().parent / "lib"
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 INVALID_ID = 0xFFFFFFFF
 
 STATUS = {
@@ -112,6 +112,14 @@ class RenderDesc(C.Structure):
         ("gi_intensity", C.c_float), ("gi_env_intensity", C.c_float), ("pt1_seed", C.c_uint32),
         ("pt1_sky_mode", C.c_int32), ("pt1_sky_radiance", C.c_float * 3), ("pt1_ld", C.c_uint32),
         ("pt1_clamp", C.c_float),
+        ("pt1_gather_div", C.c_int32), ("pt1_half_res", C.c_uint32), ("pt1_denoise", C.c_uint32),
+        ("pt1_upsample_normal_pow", C.c_float), ("pt1_upsample_depth_scale", C.c_float),
+        ("pt1_edge_patch", C.c_uint32), ("pt1_edge_patch_spp_mul", C.c_int32), ("pt1_edge_patch_thresh", C.c_float),
+        ("pt2_pattern", C.c_int32), ("pt2_emissive", C.c_uint32), ("pt2_rounds", C.c_int32),
+        ("pt2_radius", C.c_float), ("pt2_unbiased", C.c_uint32), ("pt2_m_cap", C.c_float),
+        ("pt2_w_clamp", C.c_float), ("pt2_adaptive", C.c_uint32), ("pt2_adaptive_thresh", C.c_float),
+        ("pt2_adaptive_mul", C.c_int32), ("pt2_emissive_nee", C.c_uint32), ("pt2_reflect", C.c_uint32),
+        ("pt2_glossy", C.c_uint32), ("pt2_glossy_spp", C.c_int32), ("pt2_glossy_denoise", C.c_uint32),
     ]
 
 
@@ -127,6 +135,8 @@ class Frame(C.Structure):
         ("avg_hit_dist", f32p), ("aa_mask", f32p), ("ao_patch_mask", f32p),
         ("gb_object_id", u32p), ("gb_material_id", u32p), ("gb_normal", f32p), ("gb_surf_alpha", f32p),
         ("gb_clip_cut", C.POINTER(C.c_uint8)), ("gb_clip_near_vz", f32p), ("gb_clip_far_vz", f32p),
+        ("gi_ms", C.c_double * 5), ("gi_gather_rays", C.c_uint64), ("gi_nee_rays", C.c_uint64),
+        ("gi_gbuffer_rays", C.c_uint64), ("gi_patched_pixels", C.c_uint64),
     ]
 
 

@@ -222,9 +222,7 @@ class RenderOptions:
     denoiseSigmaN: float = 128.0
     denoiseSigmaL: float = 4.0
     denoiseDemodulateAlbedo: bool = True
-    # pt1 GI gather (render_options.hpp:85-178).  Built: giIntegrator 1 with
-    # the gather at every supersampled pixel (pt1GatherDiv 1, or -1 / 0
-    # resolving to 1) and pt1Denoise off; other GI settings raise ValueError.
+    # GI (render_options.hpp:85-252): the pt1 / pt2 path-traced gather
     gi: bool = False
     pt1Spp: int = 8
     giBounces: int = 1
@@ -239,6 +237,26 @@ class RenderOptions:
     pt1GatherDiv: int = -1
     pt1HalfRes: bool = True
     pt1Denoise: bool = True
+    pt1UpsampleNormalPow: float = 32.0
+    pt1UpsampleDepthScale: float = 0.02
+    pt1EdgePatch: bool = True
+    pt1EdgePatchSppMul: int = 4
+    pt1EdgePatchThresh: float = 0.3
+    pt2Pattern: int = 1
+    pt2Emissive: bool = True
+    pt2Rounds: int = 0
+    pt2Radius: float = 16.0
+    pt2Unbiased: bool = False
+    pt2MCap: float = 100.0
+    pt2WClamp: float = 0.0
+    pt2Adaptive: bool = False
+    pt2AdaptiveThresh: float = 0.15
+    pt2AdaptiveMul: int = 4
+    pt2EmissiveNee: bool = True
+    pt2Reflect: bool = True
+    pt2Glossy: bool = True
+    pt2GlossySpp: int = 8
+    pt2GlossyDenoise: bool = True
 
     def aoEnhanced(self) -> bool:
         return (self.aoFalloffPower > 0.0 or self.aoMultiScale or self.aoBentNormal or self.aoMultibounce
@@ -324,6 +342,16 @@ def make_render_desc(scene: Scene, opt: RenderOptions):
         for k in range(3):
             d.pt1_sky_radiance[k] = opt.pt1SkyRadiance[k]
         d.pt1_ld, d.pt1_clamp = int(opt.pt1Ld), opt.pt1Clamp
+        d.pt1_gather_div, d.pt1_half_res, d.pt1_denoise = opt.pt1GatherDiv, int(opt.pt1HalfRes), int(opt.pt1Denoise)
+        d.pt1_upsample_normal_pow, d.pt1_upsample_depth_scale = opt.pt1UpsampleNormalPow, opt.pt1UpsampleDepthScale
+        d.pt1_edge_patch, d.pt1_edge_patch_spp_mul = int(opt.pt1EdgePatch), opt.pt1EdgePatchSppMul
+        d.pt1_edge_patch_thresh = opt.pt1EdgePatchThresh
+        d.pt2_pattern, d.pt2_emissive, d.pt2_rounds = opt.pt2Pattern, int(opt.pt2Emissive), opt.pt2Rounds
+        d.pt2_radius, d.pt2_unbiased, d.pt2_m_cap = opt.pt2Radius, int(opt.pt2Unbiased), opt.pt2MCap
+        d.pt2_w_clamp, d.pt2_adaptive = opt.pt2WClamp, int(opt.pt2Adaptive)
+        d.pt2_adaptive_thresh, d.pt2_adaptive_mul = opt.pt2AdaptiveThresh, opt.pt2AdaptiveMul
+        d.pt2_emissive_nee, d.pt2_reflect, d.pt2_glossy = int(opt.pt2EmissiveNee), int(opt.pt2Reflect), int(opt.pt2Glossy)
+        d.pt2_glossy_spp, d.pt2_glossy_denoise = opt.pt2GlossySpp, int(opt.pt2GlossyDenoise)
     return d, keep
 
 
@@ -341,12 +369,8 @@ def gi_gather_div(opt) -> int:
 
 def check_gi(opt) -> None:
     """Raise ValueError for the GI settings this library does not build."""
-    if opt.giIntegrator != 1:
-        raise ValueError("gi: only giIntegrator 1 (pt1) is built")
-    if gi_gather_div(opt) != 1:
-        raise ValueError("gi: only the full-resolution pt1 gather (pt1GatherDiv 1) is built")
-    if opt.pt1Denoise:
-        raise ValueError("gi: the denoise of the indirect term is not built (set pt1Denoise False)")
+    if opt.giIntegrator not in (1, 2):
+        raise ValueError("gi: the irradiance-cache integrator (giIntegrator 0) is not part of this library")
 
 
 @dataclass

@@ -224,6 +224,8 @@ ubr_status ubr_context_destroy(ubr_context* c) {
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t& e : x.pev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t& e : x.giEv)
+    if (e) cudaEventDestroy(e);
   if (x.graphExec) cudaGraphExecDestroy(x.graphExec);
   if (x.pinned) cudaFreeHost(x.pinned);
   if (x.ownStream && x.stream) cudaStreamDestroy(x.stream);

@@ -41,6 +41,7 @@ struct Context {
   std::vector<void*> sceneHandles;      // live ubr_scene handles built on this context
   cudaMemPool_t pool = nullptr;         // stream-ordered device allocations (scenes, scratch)
   void* noallocArray = nullptr;         // device address of the allocation-free query's fixed array
+  cudaEvent_t giEv[6] = {};             // GI pass stage boundaries, created on first use
 };
 
 struct Scene {

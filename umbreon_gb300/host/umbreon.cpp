@@ -410,6 +410,29 @@ ubr_render_desc toRenderDesc(const Scene& s, const RenderOptions& o, std::vector
     for (int k = 0; k < 3; ++k) d.pt1_sky_radiance[k] = o.pt1SkyRadiance[k];
     d.pt1_ld = o.pt1Ld ? 1u : 0u;
     d.pt1_clamp = o.pt1Clamp;
+    d.pt1_gather_div = o.pt1GatherDiv;  // -1 (the supersample factor) resolved by the library
+    d.pt1_half_res = o.pt1HalfRes ? 1u : 0u;
+    d.pt1_denoise = o.pt1Denoise ? 1u : 0u;
+    d.pt1_upsample_normal_pow = o.pt1UpsampleNormalPow;
+    d.pt1_upsample_depth_scale = o.pt1UpsampleDepthScale;
+    d.pt1_edge_patch = o.pt1EdgePatch ? 1u : 0u;
+    d.pt1_edge_patch_spp_mul = o.pt1EdgePatchSppMul;
+    d.pt1_edge_patch_thresh = o.pt1EdgePatchThresh;
+    d.pt2_pattern = o.pt2Pattern;
+    d.pt2_emissive = o.pt2Emissive ? 1u : 0u;
+    d.pt2_rounds = o.pt2Rounds;
+    d.pt2_radius = o.pt2Radius;
+    d.pt2_unbiased = o.pt2Unbiased ? 1u : 0u;
+    d.pt2_m_cap = o.pt2MCap;
+    d.pt2_w_clamp = o.pt2WClamp;
+    d.pt2_adaptive = o.pt2Adaptive ? 1u : 0u;
+    d.pt2_adaptive_thresh = o.pt2AdaptiveThresh;
+    d.pt2_adaptive_mul = o.pt2AdaptiveMul;
+    d.pt2_emissive_nee = o.pt2EmissiveNee ? 1u : 0u;
+    d.pt2_reflect = o.pt2Reflect ? 1u : 0u;
+    d.pt2_glossy = o.pt2Glossy ? 1u : 0u;
+    d.pt2_glossy_spp = o.pt2GlossySpp;
+    d.pt2_glossy_denoise = o.pt2GlossyDenoise ? 1u : 0u;
   }
   return d;
 }
@@ -418,19 +441,9 @@ void rejectUnsupported(const RenderOptions& opt) {
   if (opt.strokeEdges.enable && opt.objectSpaceEdges.enable)
     throw std::runtime_error(
         "umbreon::render: strokeEdges and objectSpaceEdges are mutually exclusive; enable at most one");
-  if (opt.gi) {
-    // built: the pt1 gather at every supersampled pixel, without the denoise
-    // of the indirect term (pt1GatherDiv -1 resolves to the supersample
-    // factor in pipeline.cpp, 0 to pt1HalfRes in embree_renderer.cpp:717-719)
-    int div = opt.pt1GatherDiv < 0 ? std::max(1, opt.supersample) : opt.pt1GatherDiv;
-    if (div == 0) div = opt.pt1HalfRes ? 2 : 1;
-    if (opt.giIntegrator != 1)
-      throw std::runtime_error("umbreon::render: only the pt1 GI integrator (giIntegrator = 1) is built");
-    if (div > 1)
-      throw std::runtime_error("umbreon::render: only the full-resolution pt1 gather (pt1GatherDiv = 1) is built");
-    if (opt.pt1Denoise)
-      throw std::runtime_error("umbreon::render: the denoise of the pt1 indirect term is not built (pt1Denoise)");
-  }
+  if (opt.gi && opt.giIntegrator != 1 && opt.giIntegrator != 2)
+    throw std::runtime_error(
+        "umbreon::render: the irradiance-cache GI integrator (giIntegrator = 0) is not part of this library");
   if (opt.strokeEdges.enable || opt.objectSpaceEdges.enable)
     throw std::runtime_error("umbreon::render: edge passes are not part of the GB300 ray-cast + shade library");
 }
@@ -516,6 +529,16 @@ FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderP
   f.renderSeconds = fr.render_ms / 1e3;
   f.pt1Timing.bvhBuild = info.build_ms / 1e3;
   f.pt1Timing.primary = f.renderSeconds;
+  if (opt.gi) {
+    // embree_renderer.cpp:859-1123: the GI pass's split and ray counts
+    f.pt1Timing.gather = (fr.gi_ms[0] + fr.gi_ms[1] + fr.gi_ms[4]) / 1e3;
+    f.pt1Timing.denoise = fr.gi_ms[2] / 1e3;
+    f.pt1Timing.upsample = fr.gi_ms[3] / 1e3;
+    f.pt1Rays.gatherRays = fr.gi_gather_rays;
+    f.pt1Rays.neeRays = fr.gi_nee_rays;
+    f.pt1Rays.gbufferRays = fr.gi_gbuffer_rays;
+    if (opt.pt1Denoise) f.pt1DenoiserUsed = 1;  // the a-trous (OIDN absent)
+  }
   f.cancelled = st == UBR_CANCELLED;
   // pipeline.cpp:231-251: which backend ran (the a-trous, also for OIDN requests)
   if (opt.denoiser != 0) f.denoiserUsed = 1;
