@@ -369,11 +369,12 @@ typedef struct ubr_frame {
   float* gb_clip_near_vz;
   float* gb_clip_far_vz;
   /* GI statistics (FrameResult::pt1Timing, pt1Rays; frame_result.hpp): the
-   * device ms of the gather G-buffer, the gather, the denoise of E, the
-   * upsample and the edge patch; the gather rays (all bounces), the NEE
-   * shadow rays, the G-buffer primary rays, and the number of pixels the
-   * edge patch re-gathered */
-  double gi_ms[5];
+   * device ms of the gather G-buffer, the gather (with pt2's adaptive
+   * refinement), the denoise of E, the upsample, the edge patch, and pt2's
+   * traced mirror + glossy reflection; the gather rays (all bounces and the
+   * reflection rays), the NEE shadow rays, the G-buffer primary rays, and
+   * the number of pixels the edge patch re-gathered */
+  double gi_ms[6];
   uint64_t gi_gather_rays;
   uint64_t gi_nee_rays;
   uint64_t gi_gbuffer_rays;

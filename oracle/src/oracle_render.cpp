@@ -91,7 +91,157 @@ struct Scene {
   // per-segment unit axis of cylinders (curve_build.cpp:163-167, 243-245),
   // built only when an anisotropic principled cylinder exists
   std::vector<V3> axis[4];
+  // pt2 emissive primitives sampled as lights (pt2_emissive.hpp:37-97):
+  // triangles first, then CSG records (sphere, cylinder side, cylinder cap)
+  struct EmitTri { V3 p0, p1, p2, e0, e1, e2, ng; float area; };
+  struct EmitCsg { int kind; V3 p0, axis, Le; float len, radius, area; };  // kind 1 sphere 2 side 3 cap
+  std::vector<EmitTri> emTris;
+  std::vector<EmitCsg> emCsg;
+  std::vector<float> emCdf, emPdf;
+  std::vector<uint32_t> emTriIndex, emSphereIndex;
+  std::vector<std::array<uint32_t, 3>> emCylIndex;  // side, cap0, cap1 per capped-cylinder primID
+  bool emEmpty() const { return emTris.empty() && emCsg.empty(); }
 };
+
+// pt2_emissive.hpp:104-277 pt2BuildEmissiveLights: the base mesh triangles
+// whose material emits (un-offset corners), then the real emissive spheres
+// and capped cylinders in primID order (instance offsets outer), one
+// power-weighted CDF (area x luminance) accumulated in double.
+void buildEmitters(const ubr_scene_desc& d, const std::vector<V3>& offs, Scene& s) {
+  const float kPi = 3.14159265358979323846f;
+  auto lum = [](const V3& c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; };
+  const size_t nt = d.mesh_vertex_count >= 3 ? d.mesh_triangle_count : 0;
+  bool meshEm = d.mesh_material.emission > 0.0f;
+  for (uint32_t i = 0; i < d.mesh_material_count && d.mesh_materials; ++i)
+    meshEm = meshEm || d.mesh_materials[i].emission > 0.0f;
+  bool csgEm = false;
+  for (size_t i = 0; i < d.sphere_count; ++i)
+    csgEm = csgEm || (!(d.sphere_from_edge && d.sphere_from_edge[i]) && d.sphere_material[i].emission > 0.0f &&
+                      d.sphere_center_radius[4 * i + 3] > 0.0f);
+  for (size_t i = 0; i < d.cylinder_count; ++i)
+    csgEm = csgEm || (!(d.cyl_from_edge && d.cyl_from_edge[i]) && !(d.cyl_open && d.cyl_open[i]) &&
+                      d.cyl_material[i].emission > 0.0f && d.cyl_radius[i] > 0.0f);
+  if (!(meshEm && nt > 0) && !csgEm) return;
+  std::vector<float> power;
+  if (meshEm && nt > 0) {
+    s.emTriIndex.assign(nt, 0xFFFFFFFFu);
+    for (size_t t = 0; t < nt; ++t) {
+      const ubr_material& mm = d.mesh_tri_material ? d.mesh_materials[d.mesh_tri_material[t]] : d.mesh_material;
+      if (mm.emission <= 0.0f) continue;
+      Scene::EmitTri et;
+      V3* P[3] = {&et.p0, &et.p1, &et.p2};
+      V3* E[3] = {&et.e0, &et.e1, &et.e2};
+      for (int k = 0; k < 3; ++k) {
+        const uint32_t v = d.mesh_index ? d.mesh_index[3 * t + k] : static_cast<uint32_t>(3 * t + k);
+        *P[k] = V3{d.mesh_positions[3 * v], d.mesh_positions[3 * v + 1], d.mesh_positions[3 * v + 2]};
+        const float* cc = d.mesh_colors ? d.mesh_colors + 4 * size_t(v) : nullptr;
+        *E[k] = cc ? V3{mm.emission * cc[0], mm.emission * cc[1], mm.emission * cc[2]} : V3{0.0f, 0.0f, 0.0f};
+      }
+      const V3 a{et.p1.x - et.p0.x, et.p1.y - et.p0.y, et.p1.z - et.p0.z};
+      const V3 b{et.p2.x - et.p0.x, et.p2.y - et.p0.y, et.p2.z - et.p0.z};
+      const V3 cr{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+      const float len = std::sqrt(dot(cr, cr));
+      if (len <= 0.0f) continue;
+      et.area = 0.5f * len;
+      et.ng = V3{cr.x / len, cr.y / len, cr.z / len};
+      const V3 avg{(et.e0.x + et.e1.x + et.e2.x) / 3.0f, (et.e0.y + et.e1.y + et.e2.y) / 3.0f,
+                   (et.e0.z + et.e1.z + et.e2.z) / 3.0f};
+      const float pw = et.area * lum(avg);
+      if (pw <= 0.0f) continue;
+      s.emTriIndex[t] = static_cast<uint32_t>(s.emTris.size());
+      s.emTris.push_back(et);
+      power.push_back(pw);
+    }
+    if (s.emTris.empty()) s.emTriIndex.clear();
+  }
+  if (csgEm) {
+    s.emSphereIndex.assign(d.sphere_count * offs.size(), 0xFFFFFFFFu);
+    uint32_t prim = 0;
+    for (const V3& off : offs)
+      for (size_t i = 0; i < d.sphere_count; ++i, ++prim) {
+        const ubr_material& m = d.sphere_material[i];
+        const float r = d.sphere_center_radius[4 * i + 3];
+        if ((d.sphere_from_edge && d.sphere_from_edge[i]) || !(m.emission > 0.0f) || !(r > 0.0f)) continue;
+        Scene::EmitCsg ec{};
+        ec.kind = 1;
+        ec.p0 = V3{d.sphere_center_radius[4 * i] + off.x, d.sphere_center_radius[4 * i + 1] + off.y,
+                   d.sphere_center_radius[4 * i + 2] + off.z};
+        ec.axis = V3{0.0f, 0.0f, 1.0f};
+        ec.radius = r;
+        ec.area = 4.0f * kPi * r * r;
+        ec.Le = V3{m.emission * d.sphere_color[4 * i], m.emission * d.sphere_color[4 * i + 1],
+                   m.emission * d.sphere_color[4 * i + 2]};
+        const float pw = ec.area * lum(ec.Le);
+        if (!(pw > 0.0f)) continue;
+        s.emSphereIndex[prim] = static_cast<uint32_t>(s.emCsg.size());
+        s.emCsg.push_back(ec);
+        power.push_back(pw);
+      }
+    std::vector<size_t> capIdx;
+    for (size_t i = 0; i < d.cylinder_count; ++i)
+      if (!(d.cyl_open && d.cyl_open[i])) capIdx.push_back(i);
+    s.emCylIndex.assign(capIdx.size() * offs.size(), {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu});
+    prim = 0;
+    for (const V3& off : offs)
+      for (size_t i : capIdx) {
+        const uint32_t me = prim++;
+        const ubr_material& m = d.cyl_material[i];
+        const float r = d.cyl_radius[i];
+        if ((d.cyl_from_edge && d.cyl_from_edge[i]) || !(m.emission > 0.0f) || !(r > 0.0f)) continue;
+        const V3 p0{d.cyl_p0[3 * i] + off.x, d.cyl_p0[3 * i + 1] + off.y, d.cyl_p0[3 * i + 2] + off.z};
+        const V3 p1{d.cyl_p1[3 * i] + off.x, d.cyl_p1[3 * i + 1] + off.y, d.cyl_p1[3 * i + 2] + off.z};
+        const V3 dd{p1.x - p0.x, p1.y - p0.y, p1.z - p0.z};
+        const float len = std::sqrt(dot(dd, dd));
+        if (!(len > 0.0f)) continue;
+        Scene::EmitCsg ec{};
+        ec.axis = V3{dd.x / len, dd.y / len, dd.z / len};
+        ec.radius = r;
+        ec.Le = V3{m.emission * d.cyl_color[4 * i], m.emission * d.cyl_color[4 * i + 1],
+                   m.emission * d.cyl_color[4 * i + 2]};
+        const float l = lum(ec.Le);
+        auto& ref = s.emCylIndex[me];
+        ec.kind = 2;
+        ec.p0 = p0;
+        ec.len = len;
+        ec.area = 2.0f * kPi * r * len;
+        if (ec.area * l > 0.0f) {
+          ref[0] = static_cast<uint32_t>(s.emCsg.size());
+          s.emCsg.push_back(ec);
+          power.push_back(ec.area * l);
+        }
+        ec.kind = 3;
+        ec.len = 0.0f;
+        ec.area = kPi * r * r;
+        if (ec.area * l > 0.0f) {
+          ec.p0 = p0;
+          ref[1] = static_cast<uint32_t>(s.emCsg.size());
+          s.emCsg.push_back(ec);
+          power.push_back(ec.area * l);
+          ec.p0 = p1;
+          ref[2] = static_cast<uint32_t>(s.emCsg.size());
+          s.emCsg.push_back(ec);
+          power.push_back(ec.area * l);
+        }
+      }
+    if (s.emCsg.empty()) {
+      s.emSphereIndex.clear();
+      s.emCylIndex.clear();
+    }
+  }
+  if (s.emEmpty()) {
+    s.emTriIndex.clear();
+    return;
+  }
+  double total = 0.0;
+  for (float pw : power) total += pw;
+  double acc = 0.0;
+  for (float pw : power) {
+    acc += pw;
+    s.emCdf.push_back(static_cast<float>(acc / total));
+    s.emPdf.push_back(static_cast<float>(pw / total));
+  }
+  s.emCdf.back() = 1.0f;
+}
 
 float roundKey(float x) { return x; }
 
@@ -249,6 +399,7 @@ Scene* buildScene(const ubr_scene_desc& d) {
       }
   }
   buildCylinders(d, offs, *s);
+  buildEmitters(d, offs, *s);
   if (!s->geo.rcIdx.empty()) s->geo.geomID[kRound] = nextGeom++;
   if (!s->geo.ccIdx.empty()) s->geo.geomID[kCone] = nextGeom++;
   s->bvh.build(&s->geo);
@@ -488,6 +639,13 @@ struct Opt {  // the RenderOptions fields this path reads
   int pt1EdgePatchSppMul = 4;
   int denoiseIters = 5;
   float denoiseSigmaN = 128.0f, denoiseSigmaZ = 1.0f, denoiseSigmaL = 4.0f;
+  // pt2 (render_options.hpp:178-252)
+  int giIntegrator = 1, pt2Pattern = 1, pt2AdaptiveMul = 4, pt2GlossySpp = 8;
+  bool pt2Emissive = true, pt2EmissiveNee = true, pt2Reflect = true, pt2Glossy = true, pt2GlossyDenoise = true;
+  bool pt2Adaptive = false;
+  float pt2AdaptiveThresh = 0.15f;
+  bool pt2() const { return gi && giIntegrator == 2; }
+  bool traceRefl() const { return pt2() && pt2Reflect; }
   bool aoEnhanced() const {  // render_options.hpp:79-82
     return aoFalloffPower > 0.0f || aoMultiScale || aoBentNormal || aoMultibounce || aoLowDiscrepancy ||
            aoDiffuseFactor > 0.0f;
@@ -550,7 +708,7 @@ inline V3 shadeLocal(const Scene& s, const Mat& mat, const V3& C, const V3& N, c
                      const std::vector<Light>& lights, const V3& ambLight, const V3& bg,
                      float specularScale, const V3& aoFactor, float diffuseAo, const V3& P,
                      const V3& Ng, float eps, bool shadowsOn, int shadowSamples, uint32_t px,
-                     uint32_t py) {
+                     uint32_t py, bool traceRefl = false) {
   V3 out{mat.emission * C.x + aoFactor.x * mat.ambient * C.x * ambLight.x,
          mat.emission * C.y + aoFactor.y * mat.ambient * C.y * ambLight.y,
          mat.emission * C.z + aoFactor.z * mat.ambient * C.z * ambLight.z};
@@ -600,7 +758,8 @@ inline V3 shadeLocal(const Scene& s, const Mat& mat, const V3& C, const V3& N, c
       out.z += sc * hl.z;
     }
   }
-  if (mat.reflection > 0.0f) {
+  // the fake reflection x background; pt2's traced pass owns it instead (:181-190)
+  if (mat.reflection > 0.0f && !traceRefl) {
     out.x += mat.reflection * bg.x;
     out.y += mat.reflection * bg.y;
     out.z += mat.reflection * bg.z;
@@ -657,7 +816,7 @@ inline float ggxLambdaAniso(float ax, float ay, float vx, float vy, float vz) {
 inline V3 shadePrincipled(const Scene& s, const Mat& mat, const V3& C, const V3& N, const V3& V,
                           const std::vector<Light>& lights, const V3& ambLight, const V3& bg, const V3& aoFactor,
                           float diffuseAo, const V3& P, const V3& Ng, float eps, bool shadowsOn, int shadowSamples,
-                          uint32_t px, uint32_t py, const V3* tangent) {
+                          uint32_t px, uint32_t py, const V3* tangent, bool traceRefl = false) {
   V3 out{mat.emission * C.x + aoFactor.x * mat.ambient * C.x * ambLight.x,
          mat.emission * C.y + aoFactor.y * mat.ambient * C.y * ambLight.y,
          mat.emission * C.z + aoFactor.z * mat.ambient * C.z * ambLight.z};
@@ -754,16 +913,28 @@ inline V3 shadePrincipled(const Scene& s, const Mat& mat, const V3& C, const V3&
       out.z += inv * accS.z * l.color.z;
     }
   }
-  if (mat.reflection > 0.0f) {
-    out.x += mat.reflection * bg.x;
-    out.y += mat.reflection * bg.y;
-    out.z += mat.reflection * bg.z;
-  } else if (f0max > 0.0f) {
-    out.x += F0.x * bg.x;
-    out.y += F0.y * bg.y;
-    out.z += F0.z * bg.z;
+  // principled.hpp:277-302: the environment term, owned by pt2's traced pass
+  if (!traceRefl) {
+    if (mat.reflection > 0.0f) {
+      out.x += mat.reflection * bg.x;
+      out.y += mat.reflection * bg.y;
+      out.z += mat.reflection * bg.z;
+    } else if (f0max > 0.0f) {
+      out.x += F0.x * bg.x;
+      out.y += F0.y * bg.y;
+      out.z += F0.z * bg.z;
+    }
   }
   return out;
+}
+
+// shading.hpp:48-60 pt2GgxAlphaFromRoughness: sqrt(2 / (blinnExp + 2)),
+// a mirror (0) below 0.015, at most 1
+inline float ggxAlphaFromRoughness(float roughness) {
+  const float e = blinnExp(roughness);
+  const float a = std::sqrt(2.0f / (e + 2.0f));
+  if (a < 0.015f) return 0.0f;
+  return a < 1.0f ? a : 1.0f;
 }
 
 // ao/ao_coarse.hpp:55-66 CoarseAoGrid: AO gathered once per coarse cell plus
@@ -874,6 +1045,9 @@ struct HitShade {
   // edge G-buffer (hit_shader.hpp:278-300, 460-478): (section << 2) | kind and
   // the global material index; background sentinels
   uint32_t objectId = 0xFFFFFFFFu, materialId = 0xFFFFFFFFu;
+  // pt2 traced reflection of this hit (hit_shader.hpp:61-80)
+  float reflAmt = 0.0f, reflAlpha = 0.0f, reflAspect = 1.0f;
+  V3 reflF0{1.0f, 1.0f, 1.0f}, reflTan{0.0f, 0.0f, 0.0f};
 };
 
 // hit_shader.hpp:147-496 shadeHit (POV and principled direct; GI / edge branches off)
@@ -922,11 +1096,27 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
       hs.giElig = 1;
       ao.ambLight = V3{0.0f, 0.0f, 0.0f};
     }
+    // hit_shader.hpp:243-270: traced-reflection ownership under pt2
+    const bool pbrSpec = triMat.model == 1 && (triMat.pbrMetallic > 1e-4f || triMat.pbrSpecular > 1e-4f);
+    const bool traceRefl = c.o.traceRefl() && (triMat.model == 1 ? pbrSpec : triMat.reflection > 0.0f);
+    if (traceRefl) {
+      if (triMat.model == 1) {
+        hs.reflAmt = 1.0f;
+        hs.reflF0 = principledF0(triMat, C);
+        if (c.o.pt2Glossy) {
+          const float a = triMat.pbrRoughness * triMat.pbrRoughness;
+          hs.reflAlpha = a >= 0.015f ? a : 0.0f;
+        }
+      } else {
+        hs.reflAmt = triMat.reflection;
+        if (c.o.pt2Glossy && triMat.specular > 0.0f) hs.reflAlpha = ggxAlphaFromRoughness(triMat.roughness);
+      }
+    }
     hs.color = triMat.model == 1
                    ? shadePrincipled(s, triMat, C, N, V, c.lights, ao.ambLight, c.bg, ao.aoFactor, ao.diffuseAo, P,
-                                     Ng, secEps, shadowsActive, c.o.shadowSamples, px, py, nullptr)
+                                     Ng, secEps, shadowsActive, c.o.shadowSamples, px, py, nullptr, traceRefl)
                    : shadeLocal(s, triMat, C, N, V, c.lights, ao.ambLight, c.bg, c.o.specularScale, ao.aoFactor,
-                          ao.diffuseAo, P, Ng, secEps, shadowsActive, c.o.shadowSamples, px, py);
+                          ao.diffuseAo, P, Ng, secEps, shadowsActive, c.o.shadowSamples, px, py, traceRefl);
     hs.opacity = cbuf[3];
     if (c.o.aoWriteAov) {  // hit_shader.hpp:207-213
       hs.albedo = C;
@@ -1007,11 +1197,32 @@ inline HitShade shadeHit(const Ctx& c, const Hit& hit, const V3& rd, const V3& o
         anisoT = t1;
       }
     }
+    // hit_shader.hpp:426-452: traced-reflection ownership, primitive path
+    const bool pbrSpecP = pm.model == 1 && (pm.pbrMetallic > 1e-4f || pm.pbrSpecular > 1e-4f);
+    const bool traceReflP = c.o.traceRefl() && !fromEdge && (pm.model == 1 ? pbrSpecP : pm.reflection > 0.0f);
+    if (traceReflP) {
+      if (pm.model == 1) {
+        hs.reflAmt = 1.0f;
+        hs.reflF0 = principledF0(pm, C);
+        if (c.o.pt2Glossy) {
+          const float a = pm.pbrRoughness * pm.pbrRoughness;
+          hs.reflAlpha = a >= 0.015f ? a : 0.0f;
+          if (tanValid) {
+            hs.reflTan = anisoT;
+            hs.reflAspect = principledAspect(pm.pbrAnisotropy);
+          }
+        }
+      } else {
+        hs.reflAmt = pm.reflection;
+        if (c.o.pt2Glossy && pm.specular > 0.0f) hs.reflAlpha = ggxAlphaFromRoughness(pm.roughness);
+      }
+    }
     hs.color = pm.model == 1
                    ? shadePrincipled(s, pm, C, N, V, c.lights, ambLight, c.bg, aoFactor, diffuseAo, P, Ng, secEps,
-                                     primShadows, c.o.shadowSamples, px, py, tanValid ? &anisoT : nullptr)
+                                     primShadows, c.o.shadowSamples, px, py, tanValid ? &anisoT : nullptr,
+                                     traceReflP)
                    : shadeLocal(s, pm, C, N, V, c.lights, ambLight, c.bg, c.o.specularScale, aoFactor, diffuseAo,
-                                P, Ng, secEps, primShadows, c.o.shadowSamples, px, py);
+                                P, Ng, secEps, primShadows, c.o.shadowSamples, px, py, traceReflP);
     hs.opacity = fc[3];
     hs.group = s.group[kind][hit.primID];
     if (c.o.aaMode == 1) hs.normal = N;  // hit_shader.hpp:321
@@ -1091,12 +1302,14 @@ inline V3 pt1Environment(const Ctx& c, const V3& wi) {
             e * c.ambLight.z * (gr.z + (sky.z - gr.z) * w)};
 }
 
-// pt1_gather.hpp:117-227 pt1EvalVertex, pt1 form: the vertex's reflected
-// direct light through the hard centre shadow ray of each light
-// (secondary_rays.hpp:116-134 with one sample), its reflectance kd * C, and
-// the normal faced toward the ray origin.  Outline primitives end the path.
+// pt1_gather.hpp:117-227 pt1EvalVertex: the vertex's reflected direct light
+// through one shadow ray per light (the centre ray; with a stream, pt2, an
+// area light's ray is drawn from its cone), its reflectance kd * C, its
+// emission * C when asked, and the normal faced toward the ray origin.
+// Outline primitives end the path.
 inline bool pt1EvalVertex(const Ctx& c, const Hit& h, const V3& O, const V3& wi, V3& rad, V3& alb, V3& Py,
-                          V3& Ny) {
+                          V3& Ny, bool addEmission = false, uint32_t* r0 = nullptr, uint32_t* r1 = nullptr,
+                          V3* emitted = nullptr) {
   const Scene& s = *c.s;
   const int kind = kindOfGeom(s, h.geomID);
   V3 C, NgSh;
@@ -1133,22 +1346,276 @@ inline bool pt1EvalVertex(const Ctx& c, const Hit& h, const V3& O, const V3& wi,
     V3 ng = (dot(NgSh, Ny) < 0.0f) ? V3{-NgSh.x, -NgSh.y, -NgSh.z} : NgSh;
     ng = safeNormalize(ng, Ny);
     const V3 So{Py.x + ng.x * eps, Py.y + ng.y * eps, Py.z + ng.z * eps};
-    const float sh = occludedQ(s, So, l.L, eps, kInf) ? 0.0f : 1.0f;
+    V3 dir = l.L;
+    if (r0 && l.radius > 0.0f) {
+      tea2(*r0, *r1);
+      dir = sampleLightDir(l, u32ToUnorm(*r0), u32ToUnorm(*r1));
+    }
+    const float sh = occludedQ(s, So, dir, eps, kInf) ? 0.0f : 1.0f;
     E.x += ndl * l.color.x * sh;
     E.y += ndl * l.color.y * sh;
     E.z += ndl * l.color.z * sh;
   }
   rad = V3{kd * C.x * E.x, kd * C.y * E.y, kd * C.z * E.z};
   alb = V3{kd * C.x, kd * C.y, kd * C.z};
+  if (emitted) {
+    *emitted = V3{0.0f, 0.0f, 0.0f};
+    if (addEmission && m->emission > 0.0f) *emitted = V3{m->emission * C.x, m->emission * C.y, m->emission * C.z};
+  }
   return true;
 }
 
-// pt1_gather.hpp:268-523 pt1GatherPoint, pt1 form (no reservoir, no Sobol,
-// no emission): E_stored = (1/spp) sum over cosine-hemisphere paths of the
-// NEE radiance at each vertex and the sky where the path escapes; Russian
-// roulette from the second vertex on.
+// ---- pt2 sampler (pt2_sampler.hpp): hash-based Owen-scrambled Sobol after
+// Burley (JCGT 9(4), 2020) and the blue-noise pixel arrangement ----
+inline uint32_t owenHash(uint32_t n, uint32_t seed) {
+  n ^= n * 0x3d20adeau;
+  n += seed;
+  n *= (seed >> 16) | 1u;
+  n ^= n * 0x05526c56u;
+  n ^= n * 0x53a22864u;
+  return n;
+}
+inline uint32_t owenHashBase4(uint32_t n, uint32_t seed) {
+  n ^= n * 0x3d20adeau;
+  n ^= (n >> 1) & (n << 1) & 0x55555555u;
+  n += seed;
+  n *= (seed >> 16) | 1u;
+  n ^= (n >> 1) & (n << 1) & 0x55555555u;
+  n ^= n * 0x05526c56u;
+  n ^= n * 0x53a22864u;
+  return n;
+}
+inline uint32_t reverseBits(uint32_t x) {
+  uint32_t r = 0;
+  for (int i = 0; i < 32; ++i) r |= ((x >> i) & 1u) << (31 - i);
+  return r;
+}
+inline uint32_t expandBits16(uint32_t x) {
+  x &= 0x0000ffffu;
+  x = (x ^ (x << 8)) & 0x00ff00ffu;
+  x = (x ^ (x << 4)) & 0x0f0f0f0fu;
+  x = (x ^ (x << 2)) & 0x33333333u;
+  x = (x ^ (x << 1)) & 0x55555555u;
+  return x;
+}
+// dimension 1's direction numbers in reversed-bit order: Pascal's triangle mod 2
+inline uint32_t sobolDir1(uint32_t i) {
+  uint32_t v = 1u;
+  for (uint32_t k = 0; k < i; ++k) v ^= v << 1;
+  return v;
+}
+inline float sobolDim(uint32_t revIndex, int dim, uint32_t scramble) {
+  uint32_t result = 0;
+  if (dim == 0) {
+    result = reverseBits(revIndex);
+  } else {
+    uint32_t i = 0;
+    while (revIndex != 0u) {
+      uint32_t j = 0;
+      while (!(revIndex & (0x80000000u >> j))) ++j;
+      result ^= sobolDir1(i + j);
+      i += j + 1;
+      revIndex <<= j;
+      revIndex <<= 1;
+    }
+  }
+  return static_cast<float>(reverseBits(owenHash(result, scramble))) * (1.0f / 4294967808.0f);
+}
+inline void sobol2D(uint32_t index, uint32_t seed, float& u1, float& u2) {
+  index = owenHash(reverseBits(index), seed ^ 0xf8ade99au);
+  u1 = sobolDim(index, 0, seed ^ 0xe0aaaf76u);
+  u2 = sobolDim(index, 1, seed ^ 0x94964d4eu);
+}
+inline uint32_t nextPow2(uint32_t n) {
+  uint32_t q = 1;
+  while (q < n) q <<= 1;
+  return q;
+}
+
+// ---- pt2 emissive NEE (pt2_emissive.hpp:279-520) ----
+inline float emitPdfTri(const Scene& s, uint32_t ti, float dist2, float cosL) {
+  if (cosL <= 1.0e-6f) return 0.0f;
+  return s.emPdf[ti] * dist2 / (cosL * s.emTris[ti].area);
+}
+
+// one power-sampled emitter draw (exactly two tea2 draws), visibility, the
+// balance-heuristic weight against the cosine gather
+inline V3 emissiveNee(const Scene& s, const V3& P, const V3& N, const V3& Ng, float epsT, uint32_t& s0,
+                      uint32_t& s1) {
+  const V3 zero{0.0f, 0.0f, 0.0f};
+  const float kPi = 3.14159265358979323846f;
+  tea2(s0, s1);
+  const float u = u32ToUnorm(s0);
+  uint32_t lo = 0, hi = static_cast<uint32_t>(s.emCdf.size() - 1);
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) / 2;
+    if (s.emCdf[mid] < u) lo = mid + 1;
+    else hi = mid;
+  }
+  const uint32_t triCount = static_cast<uint32_t>(s.emTris.size());
+  V3 dir, Le;
+  float target, pdfSA;
+  if (lo < triCount) {
+    const Scene::EmitTri& t = s.emTris[lo];
+    tea2(s0, s1);
+    const float b0 = u32ToUnorm(s0), b1 = u32ToUnorm(s1);
+    const float sq = std::sqrt(b0);
+    const float w1 = 1.0f - sq, w2 = b1 * sq, w0 = 1.0f - w1 - w2;
+    const V3 S{t.p0.x * w0 + t.p1.x * w1 + t.p2.x * w2, t.p0.y * w0 + t.p1.y * w1 + t.p2.y * w2,
+               t.p0.z * w0 + t.p1.z * w1 + t.p2.z * w2};
+    Le = V3{t.e0.x * w0 + t.e1.x * w1 + t.e2.x * w2, t.e0.y * w0 + t.e1.y * w1 + t.e2.y * w2,
+            t.e0.z * w0 + t.e1.z * w1 + t.e2.z * w2};
+    const V3 d{S.x - P.x, S.y - P.y, S.z - P.z};
+    const float dist2 = dot(d, d);
+    if (dist2 <= 1.0e-12f) return zero;
+    const float dist = std::sqrt(dist2);
+    dir = V3{d.x / dist, d.y / dist, d.z / dist};
+    const float cosP = dot(N, dir);
+    if (cosP <= 0.0f) return zero;
+    const float cosL = std::fabs(dot(t.ng, dir));
+    pdfSA = emitPdfTri(s, lo, dist2, cosL);
+    if (pdfSA <= 0.0f) return zero;
+    target = dist;
+  } else {
+    const Scene::EmitCsg& g = s.emCsg[lo - triCount];
+    tea2(s0, s1);
+    const float u1 = u32ToUnorm(s0), u2 = u32ToUnorm(s1);
+    const float phi = 2.0f * kPi * u2;
+    Le = g.Le;
+    if (g.kind == 1) {
+      const V3 d{g.p0.x - P.x, g.p0.y - P.y, g.p0.z - P.z};
+      const float dc2 = dot(d, d);
+      const float r2 = g.radius * g.radius;
+      if (dc2 <= r2 * 1.0002f) return zero;
+      const float dc = std::sqrt(dc2);
+      const float sin2Max = r2 / dc2;
+      const float cosMax = std::sqrt(std::fmax(0.0f, 1.0f - sin2Max));
+      const float oneMinusCos = sin2Max / (1.0f + cosMax);
+      const float cosT = 1.0f - u1 * oneMinusCos;
+      const float sinT = std::sqrt(std::fmax(0.0f, 1.0f - cosT * cosT));
+      const Frame fr = frameFromNormal(V3{d.x / dc, d.y / dc, d.z / dc});
+      const float sx = sinT * std::cos(phi), sy = sinT * std::sin(phi);
+      dir = V3{fr.t.x * sx + fr.b.x * sy + fr.n.x * cosT, fr.t.y * sx + fr.b.y * sy + fr.n.y * cosT,
+               fr.t.z * sx + fr.b.z * sy + fr.n.z * cosT};
+      pdfSA = s.emPdf[lo] / (2.0f * kPi * oneMinusCos);
+      const float b = dot(d, dir);
+      const float disc = std::fmax(0.0f, b * b - (dc2 - r2));
+      target = b - std::sqrt(disc);
+    } else {
+      const Frame fr = frameFromNormal(g.axis);
+      V3 S, nS;
+      if (g.kind == 2) {
+        nS = V3{fr.t.x * std::cos(phi) + fr.b.x * std::sin(phi), fr.t.y * std::cos(phi) + fr.b.y * std::sin(phi),
+                fr.t.z * std::cos(phi) + fr.b.z * std::sin(phi)};
+        const float hgt = u1 * g.len;
+        S = V3{g.p0.x + g.axis.x * hgt + nS.x * g.radius, g.p0.y + g.axis.y * hgt + nS.y * g.radius,
+               g.p0.z + g.axis.z * hgt + nS.z * g.radius};
+      } else {
+        const float rr = g.radius * std::sqrt(u1);
+        S = V3{g.p0.x + (fr.t.x * std::cos(phi) + fr.b.x * std::sin(phi)) * rr,
+               g.p0.y + (fr.t.y * std::cos(phi) + fr.b.y * std::sin(phi)) * rr,
+               g.p0.z + (fr.t.z * std::cos(phi) + fr.b.z * std::sin(phi)) * rr};
+        nS = g.axis;
+      }
+      const V3 d{S.x - P.x, S.y - P.y, S.z - P.z};
+      const float dist2 = dot(d, d);
+      if (dist2 <= 1.0e-12f) return zero;
+      const float dist = std::sqrt(dist2);
+      dir = V3{d.x / dist, d.y / dist, d.z / dist};
+      const float cosL = std::fabs(dot(nS, dir));
+      if (cosL <= 1.0e-6f) return zero;
+      pdfSA = s.emPdf[lo] * dist2 / (cosL * g.area);
+      target = dist;
+    }
+    const float cosP0 = dot(N, dir);
+    if (cosP0 <= 0.0f) return zero;
+    if (pdfSA <= 0.0f) return zero;
+  }
+  const float cosP = dot(N, dir);
+  const float eps = selfIntersectEps(P, dir, epsT);
+  V3 ng = (dot(Ng, N) < 0.0f) ? V3{-Ng.x, -Ng.y, -Ng.z} : Ng;
+  ng = safeNormalize(ng, N);
+  const V3 O{P.x + ng.x * eps, P.y + ng.y * eps, P.z + ng.z * eps};
+  const float tf = target - 2.0f * eps;
+  if (eps < tf && occludedQ(s, O, dir, eps, tf)) return zero;
+  const float pdfCos = cosP * (1.0f / kPi);
+  const float w = pdfSA / (pdfSA + pdfCos);
+  const float k = w * cosP / (kPi * pdfSA);
+  return V3{Le.x * k, Le.y * k, Le.z * k};
+}
+
+// pt2EmissiveHitWeight: the cosine side's balance weight of a first-bounce
+// hit on an NEE-covered emitter; 1 otherwise
+inline float emissiveHitWeight(const Scene& s, int kind, uint32_t prim, const V3& O, const V3& wi, float tfar,
+                               float cosP, const V3& ngHit) {
+  if (s.emEmpty()) return 1.0f;
+  const float kPi = 3.14159265358979323846f;
+  const float pdfCos = (cosP > 0.0f ? cosP : 0.0f) * (1.0f / kPi);
+  if (pdfCos <= 0.0f) return 1.0f;
+  const uint32_t triCount = static_cast<uint32_t>(s.emTris.size());
+  if (kind == kMesh) {
+    if (prim >= s.emTriIndex.size()) return 1.0f;
+    const uint32_t ti = s.emTriIndex[prim];
+    if (ti == 0xFFFFFFFFu) return 1.0f;
+    const float cosL = std::fabs(dot(s.emTris[ti].ng, wi));
+    const float pdfSA = emitPdfTri(s, ti, tfar * tfar, cosL);
+    if (pdfSA <= 0.0f) return 1.0f;
+    return pdfCos / (pdfCos + pdfSA);
+  }
+  if (kind == kSphere) {
+    if (prim >= s.emSphereIndex.size()) return 1.0f;
+    const uint32_t ci = s.emSphereIndex[prim];
+    if (ci == 0xFFFFFFFFu) return 1.0f;
+    const Scene::EmitCsg& g = s.emCsg[ci];
+    const V3 d{g.p0.x - O.x, g.p0.y - O.y, g.p0.z - O.z};
+    const float dc2 = dot(d, d);
+    const float r2 = g.radius * g.radius;
+    if (dc2 <= r2 * 1.0002f) return 1.0f;
+    const float sin2Max = r2 / dc2;
+    const float cosMax = std::sqrt(std::fmax(0.0f, 1.0f - sin2Max));
+    const float oneMinusCos = sin2Max / (1.0f + cosMax);
+    if (oneMinusCos <= 0.0f) return 1.0f;
+    const float pdfSA = s.emPdf[triCount + ci] / (2.0f * kPi * oneMinusCos);
+    if (pdfSA <= 0.0f) return 1.0f;
+    return pdfCos / (pdfCos + pdfSA);
+  }
+  if (kind == kCone) {
+    if (prim >= s.emCylIndex.size()) return 1.0f;
+    const auto& ref = s.emCylIndex[prim];
+    uint32_t part = ref[0];
+    const uint32_t probe = ref[0] != 0xFFFFFFFFu ? ref[0] : ref[1] != 0xFFFFFFFFu ? ref[1] : ref[2];
+    if (probe == 0xFFFFFFFFu) return 1.0f;
+    const V3 axis = s.emCsg[probe].axis;
+    const V3 ng = safeNormalize(ngHit, axis);
+    const float nu = dot(ng, axis);
+    if (nu >= 0.99f) part = ref[2];
+    else if (nu <= -0.99f) part = ref[1];
+    if (part == 0xFFFFFFFFu) return 1.0f;
+    const float cosL = std::fabs(dot(ng, wi));
+    if (cosL <= 1.0e-6f) return 1.0f;
+    const float pdfSA = s.emPdf[triCount + part] * tfar * tfar / (cosL * s.emCsg[part].area);
+    if (pdfSA <= 0.0f) return 1.0f;
+    return pdfCos / (pdfCos + pdfSA);
+  }
+  return 1.0f;
+}
+
+// pt2's gather configuration at one point (Pt1GatherExt / Pt2GatherCfg)
+struct GatherExt {
+  bool pt2 = false;
+  uint32_t idxBase = 0, seed = 0;  // the point's Sobol section / scramble seed
+  int sampleOffset = 0;
+  V3* halfSum = nullptr;
+};
+
+// pt1_gather.hpp:268-523 pt1GatherPoint: E_stored = (1/spp) sum over
+// cosine-hemisphere paths of the NEE radiance at each vertex and the sky
+// where the path escapes; Russian roulette from the second vertex on.  With
+// pt2 (ext): the first bounce from the scrambled Sobol point, the path's
+// stream drives area-light jitter, vertices add their MIS-weighted emission,
+// and each sample adds one emissive NEE draw at the origin.
 inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, uint32_t seed, float epsT, int spp,
-                         float* occOut) {
+                         float* occOut, const GatherExt* ext = nullptr) {
   const Scene& s = *c.s;
   int nOcc = 0;
   const Frame f = frameFromNormal(N);
@@ -1156,6 +1623,9 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
   const V3 O{P.x + N.x * eps, P.y + N.y * eps, P.z + N.z * eps};
   const int maxB = c.o.giBounces < 1 ? 1 : c.o.giBounces;
   const float maxD = c.o.giMaxDistance > 0.0f ? c.o.giMaxDistance : kInf;
+  const bool pt2 = ext && ext->pt2;
+  const bool emitNee = pt2 && c.o.pt2Emissive && c.o.pt2EmissiveNee && !s.emEmpty();
+  const int sOff = ext ? ext->sampleOffset : 0;
   float cpx = 0.0f, cpy = 0.0f;
   if (c.o.pt1Ld) {
     uint32_t c0 = seed, c1 = 0x9E3779B9u;
@@ -1165,10 +1635,12 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
   }
   V3 Esum{0.0f, 0.0f, 0.0f};
   for (int sI = 0; sI < spp; ++sI) {
-    uint32_t s0 = seed, s1 = static_cast<uint32_t>(sI);
+    uint32_t s0 = seed, s1 = static_cast<uint32_t>(sI + sOff);
     tea2(s0, s1);
     float u1, u2;
-    if (c.o.pt1Ld) {
+    if (pt2) {
+      sobol2D(ext->idxBase + static_cast<uint32_t>(sI + sOff), ext->seed, u1, u2);
+    } else if (c.o.pt1Ld) {
       u1 = static_cast<float>(sI) / static_cast<float>(spp) + cpx;
       u2 = radicalInverse2(static_cast<uint32_t>(sI)) + cpy;
       if (u1 >= 1.0f) u1 -= 1.0f;
@@ -1180,6 +1652,7 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
     V3 wi = cosineSampleHemisphere(u1, u2, f);
     const bool horizonOk = dot(wi, Ng) > 0.0f;
     if (!horizonOk) ++nOcc;
+    const float cand0Cos = dot(wi, N);
     V3 org = O;
     float tnear = eps;
     V3 thr{1.0f, 1.0f, 1.0f}, L{0.0f, 0.0f, 0.0f};
@@ -1195,11 +1668,16 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
         break;
       }
       if (b == 1) ++nOcc;
-      V3 rad, alb, Py, Ny;
-      if (!pt1EvalVertex(c, h, org, wi, rad, alb, Py, Ny)) break;
-      L.x += thr.x * rad.x;
-      L.y += thr.y * rad.y;
-      L.z += thr.z * rad.z;
+      V3 rad, alb, Py, Ny, em{0.0f, 0.0f, 0.0f};
+      if (!pt1EvalVertex(c, h, org, wi, rad, alb, Py, Ny, pt2 && c.o.pt2Emissive, pt2 ? &s0 : nullptr,
+                         pt2 ? &s1 : nullptr, &em))
+        break;
+      float emW = 1.0f;
+      if (emitNee && b == 1)
+        emW = emissiveHitWeight(s, kindOfGeom(s, h.geomID), h.primID, org, wi, h.t, cand0Cos, h.Ng);
+      L.x += thr.x * (rad.x + emW * em.x);
+      L.y += thr.y * (rad.y + emW * em.y);
+      L.z += thr.z * (rad.z + emW * em.z);
       if (b == maxB) break;
       thr.x *= alb.x;
       thr.y *= alb.y;
@@ -1221,6 +1699,12 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
       org = V3{Py.x + Ny.x * epsV, Py.y + Ny.y * epsV, Py.z + Ny.z * epsV};
       tnear = epsV;
     }
+    if (emitNee) {
+      const V3 e = emissiveNee(s, P, N, Ng, epsT, s0, s1);
+      L.x += e.x;
+      L.y += e.y;
+      L.z += e.z;
+    }
     if (c.o.pt1Clamp > 0.0f) {
       const float lum = 0.2126f * L.x + 0.7152f * L.y + 0.0722f * L.z;
       if (lum > c.o.pt1Clamp) {
@@ -1233,6 +1717,11 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
     Esum.x += L.x;
     Esum.y += L.y;
     Esum.z += L.z;
+    if (ext && ext->halfSum && sI < spp / 2) {
+      ext->halfSum->x += L.x;
+      ext->halfSum->y += L.y;
+      ext->halfSum->z += L.z;
+    }
   }
   const float invN = 1.0f / static_cast<float>(spp > 0 ? spp : 1);
   if (occOut) *occOut = static_cast<float>(nOcc) * invN;
@@ -1619,13 +2108,23 @@ inline void tracePt1GBuffer(const Ctx& c, const Cam& cam, int w, int h, GiGrid& 
 // pt1_gather.hpp:525-614 gatherPt1Grid: E and the first-bounce hit fraction
 // at every marked point of a W x H grid, seeded hashU32(pix ^
 // hashU32(pt1Seed)); the primary hit distance scales the origin epsilon;
-// gnrm null: the shading normal is the horizon normal.
+// gnrm null: the shading normal is the horizon normal.  pt2 (pt2.pt2): each
+// point's sampler (pt2MakePixelSampler: blue-noise section of length sppPow2
+// along the scrambled Morton curve, or its own sequence), the sample offset
+// of a refinement pass, and the half sums for adaptive spp.
+struct GridPt2 {
+  bool pt2 = false;
+  uint32_t sppPow2 = 1;
+  int sampleOffset = 0;
+  std::vector<float>* halfE = nullptr;
+};
 inline void gatherGrid(const Ctx& c, int W, int H, const float* pos, const float* nrm, const float* gnrm,
                        const uint8_t* mark, const float* dep, int spp, std::vector<float>& E,
-                       std::vector<float>& occ, int nt) {
+                       std::vector<float>& occ, int nt, const GridPt2& g2 = GridPt2()) {
   const size_t n = static_cast<size_t>(W) * H;
   E.assign(n * 3, 0.0f);
   occ.assign(n, 0.0f);
+  if (g2.halfE) g2.halfE->assign(n * 3, 0.0f);
   const uint32_t seedMix = hashU32(c.o.pt1Seed);
   forRows(H, nt, [&](int py) {
     for (int px = 0; px < W; ++px) {
@@ -1637,11 +2136,72 @@ inline void gatherGrid(const Ctx& c, int W, int H, const float* pos, const float
       const uint32_t seed = hashU32(static_cast<uint32_t>(pix) ^ seedMix);
       const float tEps = dep[pix] > 0.0f ? dep[pix] : 1.0f;
       float o = 0.0f;
-      const V3 e = pt1GatherPoint(c, P, N, Ng, seed, tEps, spp, &o);
+      GatherExt ext;
+      V3 half{0.0f, 0.0f, 0.0f};
+      if (g2.pt2) {
+        ext.pt2 = true;
+        if (c.o.pt2Pattern == 1) {
+          const uint32_t morton = (expandBits16(static_cast<uint32_t>(px)) << 1) |
+                                  expandBits16(static_cast<uint32_t>(py));
+          ext.idxBase = reverseBits(owenHashBase4(reverseBits(morton), seedMix)) * g2.sppPow2;
+          ext.seed = seedMix;
+        } else {
+          ext.idxBase = 0;
+          ext.seed = seed;
+        }
+        ext.sampleOffset = g2.sampleOffset;
+        if (g2.halfE) ext.halfSum = &half;
+      }
+      const V3 e = pt1GatherPoint(c, P, N, Ng, seed, tEps, spp, &o, g2.pt2 ? &ext : nullptr);
       E[3 * pix] = e.x; E[3 * pix + 1] = e.y; E[3 * pix + 2] = e.z;
       occ[pix] = o;
+      if (g2.halfE) {
+        (*g2.halfE)[3 * pix] = half.x; (*g2.halfE)[3 * pix + 1] = half.y; (*g2.halfE)[3 * pix + 2] = half.z;
+      }
     }
   });
+}
+
+// pt2_adaptive.hpp:30-121: refinement mask (|lum(E) - lum(halfSum)/(spp/2)|
+// above threshold x sqrt(lum) for dark points, x lum otherwise; every point
+// when spp < 2), one 3x3 dilation, and the weighted-mean merge
+inline void adaptiveMask(int W, int H, const std::vector<float>& E, const std::vector<float>& halfE,
+                         const uint8_t* elig, int spp, float threshold, std::vector<uint8_t>& mask) {
+  const size_t n = static_cast<size_t>(W) * H;
+  mask.assign(n, 0);
+  const int nHalf = spp / 2;
+  if (nHalf < 1) {
+    for (size_t i = 0; i < n; ++i) mask[i] = elig[i] ? 1 : 0;
+    return;
+  }
+  const float invHalf = 1.0f / static_cast<float>(nHalf);
+  for (size_t p = 0; p < n; ++p) {
+    if (!elig[p]) continue;
+    const float lumA = 0.2126f * E[3 * p] + 0.7152f * E[3 * p + 1] + 0.0722f * E[3 * p + 2];
+    const float lumH = (0.2126f * halfE[3 * p] + 0.7152f * halfE[3 * p + 1] + 0.0722f * halfE[3 * p + 2]) * invHalf;
+    const float diff = std::fabs(lumA - lumH);
+    const float norm = lumA < 1.0f ? std::sqrt(std::fmax(lumA, 1.0e-4f)) : lumA;
+    if (diff > threshold * norm) mask[p] = 1;
+  }
+}
+inline void dilateMask(int W, int H, const std::vector<uint8_t>& in, const uint8_t* elig, std::vector<uint8_t>& out) {
+  out.assign(in.size(), 0);
+  for (int py = 0; py < H; ++py)
+    for (int px = 0; px < W; ++px) {
+      const size_t pix = static_cast<size_t>(py) * W + px;
+      if (!elig[pix]) continue;
+      uint8_t v = in[pix];
+      for (int dy = -1; dy <= 1 && !v; ++dy) {
+        const int ny = py + dy;
+        if (ny < 0 || ny >= H) continue;
+        for (int dx = -1; dx <= 1 && !v; ++dx) {
+          const int nx = px + dx;
+          if (nx < 0 || nx >= W) continue;
+          v = in[static_cast<size_t>(ny) * W + nx];
+        }
+      }
+      out[pix] = v;
+    }
 }
 
 // pt1_denoise.cpp:20-80 denoisePt1E without OIDN: non-finite E scrubbed to
@@ -1789,25 +2349,101 @@ inline void smoothPatchedPixels(int W, int H, const std::vector<uint8_t>& mask, 
     }
 }
 
-// embree_renderer.cpp:560-934 runPt1GiPass (pt1): the gather on the render
-// grid (k = 1) or on a ceil(W/k) x ceil(H/k) grid with its own primary rays,
-// the denoise of E at gather resolution, the upsample, the edge patch, and
-// the [E] composite colour += giIntensity * (kd * pigment) * E.
+// embree_renderer.cpp:560-1086 runPt1GiPass: the gather on the render grid
+// (k = 1) or on a ceil(W/k) x ceil(H/k) grid with its own primary rays (with
+// pt2's adaptive refinement), the denoise of E at gather resolution, the
+// upsample, the edge patch, the [E] composite colour += giIntensity *
+// (kd * pigment) * E, then pt2's traced mirror and glossy reflection.
+struct ReflPix {  // the first hit's traced-reflection record per render-grid pixel
+  std::vector<float> amt, alpha, aspect, f0, tan;
+};
+inline V3 schlick3(const V3& F0, float u) { return schlickF(F0, u); }
+inline V3 reflectedRadiance(const Ctx& c, const V3& O, const V3& d, float tn, uint32_t r0, uint32_t r1) {
+  Ray r;
+  r.org = O; r.dir = d; r.tnear = tn; r.tfar = kInf;
+  Hit h;
+  if (!c.s->bvh.closest(r, h)) return pt1Environment(c, d);
+  tea2(r0, r1);
+  V3 rad, alb, Py, Ny, em;
+  if (!pt1EvalVertex(c, h, O, d, rad, alb, Py, Ny, c.o.pt2Emissive, &r0, &r1, &em)) return V3{0.0f, 0.0f, 0.0f};
+  const V3 sky = pt1Environment(c, d);
+  return V3{rad.x + alb.x * sky.x, rad.y + alb.y * sky.y, rad.z + alb.z * sky.z};
+}
+// Smith Lambda of GGX (pt2_glossy.hpp:41-56) and visible-normal sampling
+// (Heitz, JCGT 7(4) 2018)
+inline float ggxLambdaIso(float alpha, float cosT) {
+  const float c2 = std::fmax(cosT * cosT, 1.0e-12f);
+  const float t2 = (1.0f - c2) / c2;
+  return 0.5f * (std::sqrt(1.0f + alpha * alpha * t2) - 1.0f);
+}
+inline float ggxLambdaAn(float ax, float ay, const V3& w) {
+  const float z2 = std::fmax(w.z * w.z, 1.0e-12f);
+  const float t2 = (ax * ax * w.x * w.x + ay * ay * w.y * w.y) / z2;
+  return 0.5f * (std::sqrt(1.0f + t2) - 1.0f);
+}
+inline V3 sampleGgxVndf(const V3& wo, float ax, float ay, float u1, float u2) {
+  const V3 Vh = safeNormalize(V3{ax * wo.x, ay * wo.y, wo.z});
+  const V3 T1 = Vh.z < 0.999f ? safeNormalize(cross(V3{0.0f, 0.0f, 1.0f}, Vh)) : V3{1.0f, 0.0f, 0.0f};
+  const V3 T2 = cross(Vh, T1);
+  const float r = std::sqrt(u1);
+  const float phi = 2.0f * 3.14159265358979323846f * u2;
+  const float t1 = r * std::cos(phi);
+  float t2 = r * std::sin(phi);
+  const float sw = 0.5f * (1.0f + Vh.z);
+  t2 = (1.0f - sw) * std::sqrt(std::fmax(0.0f, 1.0f - t1 * t1)) + sw * t2;
+  const float t3 = std::sqrt(std::fmax(0.0f, 1.0f - t1 * t1 - t2 * t2));
+  const V3 Nh{t1 * T1.x + t2 * T2.x + t3 * Vh.x, t1 * T1.y + t2 * T2.y + t3 * Vh.y,
+              t1 * T1.z + t2 * T2.z + t3 * Vh.z};
+  return safeNormalize(V3{ax * Nh.x, ay * Nh.y, std::fmax(0.0f, Nh.z)});
+}
+
 inline void runPt1GiPass(const Ctx& c, const Cam& cam, int W, int H, const std::vector<float>& pos,
                          const std::vector<float>& nrm, const std::vector<float>& refl, const std::vector<float>& dep,
                          const std::vector<uint8_t>& elig, std::vector<float>& color, int nt,
-                         uint64_t* patchedOut) {
+                         uint64_t* patchedOut, const ReflPix* rp, int ss) {
   const Opt& o = c.o;
   const int k = std::max(1, o.pt1GatherDiv);
   const int spp = std::max(1, o.pt1Spp);
+  const bool pt2 = o.pt2();
+  const bool adapt = pt2 && o.pt2Adaptive && spp >= 2;
+  const int extra = adapt ? spp * (std::max(2, o.pt2AdaptiveMul) - 1) : 0;
   std::vector<float> E, occ;
+  // the gather over a grid with pt2's adaptive refinement (embree_renderer.cpp:674-706)
+  auto gather = [&](int gw, int gh, const float* gp, const float* gn, const float* gg, const uint8_t* ge,
+                    const float* gd, std::vector<float>& Eo, std::vector<float>& oo) {
+    GridPt2 g2;
+    g2.pt2 = pt2;
+    g2.sppPow2 = nextPow2(static_cast<uint32_t>(spp + extra));
+    std::vector<float> halfE;
+    if (adapt) g2.halfE = &halfE;
+    gatherGrid(c, gw, gh, gp, gn, gg, ge, gd, spp, Eo, oo, nt, g2);
+    if (!adapt) return;
+    std::vector<uint8_t> m0, m1;
+    adaptiveMask(gw, gh, Eo, halfE, ge, spp, o.pt2AdaptiveThresh, m0);
+    dilateMask(gw, gh, m0, ge, m1);
+    dilateMask(gw, gh, m1, ge, m0);
+    size_t nref = 0;
+    for (uint8_t v : m0) nref += v;
+    if (nref == 0) return;
+    GridPt2 gr = g2;
+    gr.halfE = nullptr;
+    gr.sampleOffset = spp;
+    std::vector<float> Er, occr;
+    gatherGrid(c, gw, gh, gp, gn, gg, m0.data(), gd, extra, Er, occr, nt, gr);
+    const float wB = static_cast<float>(spp) / static_cast<float>(spp + extra);
+    const float wR = 1.0f - wB;
+    for (size_t p = 0; p < m0.size(); ++p) {
+      if (!m0[p]) continue;
+      for (int q = 0; q < 3; ++q) Eo[3 * p + q] = Eo[3 * p + q] * wB + Er[3 * p + q] * wR;
+      oo[p] = oo[p] * wB + occr[p] * wR;
+    }
+  };
   if (k > 1) {
     const int hw = (W + k - 1) / k, hh = (H + k - 1) / k;
     GiGrid g;
     tracePt1GBuffer(c, cam, hw, hh, g, nt);
     std::vector<float> Eh, occh;
-    gatherGrid(c, hw, hh, g.pos.data(), g.nrm.data(), g.gnrm.data(), g.hit.data(), g.dep.data(), spp, Eh, occh,
-               nt);
+    gather(hw, hh, g.pos.data(), g.nrm.data(), g.gnrm.data(), g.hit.data(), g.dep.data(), Eh, occh);
     if (o.pt1Denoise) denoisePt1E(hw, hh, Eh, g.nrm.data(), g.pos.data(), o);
     std::vector<uint8_t> patch;
     upsampleJointBilateral(W, H, nrm.data(), dep.data(), elig.data(), g, Eh, occh, o.pt1UpNormalPow,
@@ -1819,8 +2455,11 @@ inline void runPt1GiPass(const Ctx& c, const Cam& cam, int W, int H, const std::
       if (patchedOut) *patchedOut = count;
       if (count > 0) {
         std::vector<float> Ep, occp;
-        gatherGrid(c, W, H, pos.data(), nrm.data(), nullptr, patch.data(), dep.data(),
-                   spp * std::max(1, o.pt1EdgePatchSppMul), Ep, occp, nt);
+        const int pspp = spp * std::max(1, o.pt1EdgePatchSppMul);
+        GridPt2 gp2;
+        gp2.pt2 = pt2;
+        gp2.sppPow2 = nextPow2(static_cast<uint32_t>(pspp));
+        gatherGrid(c, W, H, pos.data(), nrm.data(), nullptr, patch.data(), dep.data(), pspp, Ep, occp, nt, gp2);
         for (size_t i = 0; i < patch.size(); ++i) {
           if (!patch[i]) continue;
           E[3 * i] = Ep[3 * i]; E[3 * i + 1] = Ep[3 * i + 1]; E[3 * i + 2] = Ep[3 * i + 2];
@@ -1831,7 +2470,7 @@ inline void runPt1GiPass(const Ctx& c, const Cam& cam, int W, int H, const std::
       }
     }
   } else {
-    gatherGrid(c, W, H, pos.data(), nrm.data(), nullptr, elig.data(), dep.data(), spp, E, occ, nt);
+    gather(W, H, pos.data(), nrm.data(), nullptr, elig.data(), dep.data(), E, occ);
     if (o.pt1Denoise) denoisePt1E(W, H, E, nrm.data(), pos.data(), o);
   }
   const float gI = o.giIntensity;
@@ -1841,6 +2480,156 @@ inline void runPt1GiPass(const Ctx& c, const Cam& cam, int W, int H, const std::
     color[4 * pix] += gI * refl[3 * pix] * E[3 * pix];
     color[4 * pix + 1] += gI * refl[3 * pix + 1] * E[3 * pix + 1];
     color[4 * pix + 2] += gI * refl[3 * pix + 2] * E[3 * pix + 2];
+  }
+  if (!rp) return;
+  // pt2_reflect.hpp: one mirror ray per first hit that owns a mirror lobe
+  auto incident = [&](const V3& P) {
+    return cam.ortho ? cam.dir : safeNormalize(V3{P.x - cam.pos.x, P.y - cam.pos.y, P.z - cam.pos.z});
+  };
+  forRows(H, nt, [&](int py) {
+    for (int px = 0; px < W; ++px) {
+      const size_t pix = static_cast<size_t>(py) * W + px;
+      const float kk = rp->amt[pix];
+      if (kk <= 0.0f || rp->alpha[pix] > 0.0f) continue;
+      const V3 P{pos[3 * pix], pos[3 * pix + 1], pos[3 * pix + 2]};
+      const V3 N{nrm[3 * pix], nrm[3 * pix + 1], nrm[3 * pix + 2]};
+      const V3 wi = incident(P);
+      const float indot = dot(wi, N);
+      const V3 rdir = safeNormalize(V3{wi.x - 2.0f * indot * N.x, wi.y - 2.0f * indot * N.y, wi.z - 2.0f * indot * N.z});
+      const float t0 = dep[pix] > 0.0f ? dep[pix] : 1.0f;
+      const float eps = selfIntersectEps(P, rdir, t0);
+      const V3 O{P.x + N.x * eps, P.y + N.y * eps, P.z + N.z * eps};
+      const V3 L = reflectedRadiance(c, O, rdir, eps, static_cast<uint32_t>(pix) ^ 0x52464c54u, 0x4e454531u);
+      float cosI = -indot;
+      if (cosI < 0.0f) cosI = 0.0f;
+      if (cosI > 1.0f) cosI = 1.0f;
+      const V3 F = schlick3(V3{rp->f0[3 * pix], rp->f0[3 * pix + 1], rp->f0[3 * pix + 2]}, cosI);
+      color[4 * pix] += kk * F.x * L.x;
+      color[4 * pix + 1] += kk * F.y * L.y;
+      color[4 * pix + 2] += kk * F.z * L.z;
+    }
+  });
+  if (!o.pt2Glossy) return;
+  bool anyGlossy = false;
+  for (size_t i = 0; i < n && !anyGlossy; ++i) anyGlossy = rp->amt[i] > 0.0f && rp->alpha[i] > 0.0f;
+  if (!anyGlossy) return;
+  // pt2_glossy.hpp: spp VNDF-sampled reflection rays per glossy pixel
+  const int gspp = std::max(1, o.pt2GlossySpp);
+  const uint32_t seedMix = hashU32(o.pt1Seed ^ 0x474c5359u);
+  std::vector<float> Es(n * 3, 0.0f);
+  forRows(H, nt, [&](int py) {
+    for (int px = 0; px < W; ++px) {
+      const size_t pix = static_cast<size_t>(py) * W + px;
+      const float alpha = rp->alpha[pix];
+      if (rp->amt[pix] <= 0.0f || alpha <= 0.0f) continue;
+      const V3 P{pos[3 * pix], pos[3 * pix + 1], pos[3 * pix + 2]};
+      const V3 N{nrm[3 * pix], nrm[3 * pix + 1], nrm[3 * pix + 2]};
+      const V3 wiV = incident(P);
+      bool aniso = false;
+      float ax = alpha, ay = alpha;
+      Frame f;
+      if (!rp->tan.empty()) {
+        const V3 T{rp->tan[3 * pix], rp->tan[3 * pix + 1], rp->tan[3 * pix + 2]};
+        const float aspect = rp->aspect[pix];
+        if (aspect != 1.0f && dot(T, T) > 0.5f) {
+          aniso = true;
+          f = Frame{T, cross(N, T), N};
+          ax = alpha / aspect;
+          if (ax > 1.0f) ax = 1.0f;
+          ay = alpha * aspect;
+        }
+      }
+      if (!aniso) f = frameFromNormal(N);
+      const V3 woW{-wiV.x, -wiV.y, -wiV.z};
+      V3 wo{dot(woW, f.t), dot(woW, f.b), dot(woW, f.n)};
+      if (wo.z < 1.0e-4f) wo.z = 1.0e-4f;
+      wo = safeNormalize(wo);
+      const float lamO = aniso ? ggxLambdaAn(ax, ay, wo) : ggxLambdaIso(alpha, wo.z);
+      const float t0 = dep[pix] > 0.0f ? dep[pix] : 1.0f;
+      const uint32_t seedPix = hashU32(static_cast<uint32_t>(pix)) ^ seedMix;
+      const V3 F0{rp->f0[3 * pix], rp->f0[3 * pix + 1], rp->f0[3 * pix + 2]};
+      V3 sum{0.0f, 0.0f, 0.0f};
+      for (int sI = 0; sI < gspp; ++sI) {
+        float u1, u2;
+        sobol2D(static_cast<uint32_t>(sI), seedPix, u1, u2);
+        const V3 wm = sampleGgxVndf(wo, ax, ay, u1, u2);
+        const float owm = dot(wo, wm);
+        const V3 wl{2.0f * owm * wm.x - wo.x, 2.0f * owm * wm.y - wo.y, 2.0f * owm * wm.z - wo.z};
+        if (wl.z <= 0.0f) continue;
+        const float lamI = aniso ? ggxLambdaAn(ax, ay, wl) : ggxLambdaIso(alpha, wl.z);
+        const float weight = (1.0f + lamO) / (1.0f + lamO + lamI);
+        const V3 rdir = safeNormalize(V3{f.t.x * wl.x + f.b.x * wl.y + f.n.x * wl.z,
+                                         f.t.y * wl.x + f.b.y * wl.y + f.n.y * wl.z,
+                                         f.t.z * wl.x + f.b.z * wl.y + f.n.z * wl.z});
+        const float eps = selfIntersectEps(P, rdir, t0);
+        const V3 O{P.x + N.x * eps, P.y + N.y * eps, P.z + N.z * eps};
+        const V3 L = reflectedRadiance(c, O, rdir, eps, static_cast<uint32_t>(pix) ^ 0x474c5359u,
+                                       0x4e454532u + static_cast<uint32_t>(sI));
+        const V3 F = schlick3(F0, owm);
+        sum.x += weight * F.x * L.x;
+        sum.y += weight * F.y * L.y;
+        sum.z += weight * F.z * L.z;
+      }
+      const float inv = 1.0f / static_cast<float>(gspp);
+      Es[3 * pix] = sum.x * inv; Es[3 * pix + 1] = sum.y * inv; Es[3 * pix + 2] = sum.z * inv;
+    }
+  });
+  if (o.pt1Denoise && o.pt2GlossyDenoise) {
+    if (ss <= 1 || W % ss != 0 || H % ss != 0) {
+      denoisePt1E(W, H, Es, nrm.data(), pos.data(), o);
+    } else {
+      // embree_renderer.cpp:990-1078: glossy-masked downsample to the output
+      // grid, denoise there, joint-bilateral upsample over the glossy pixels
+      const int Wo = W / ss, Ho = H / ss;
+      const size_t no = static_cast<size_t>(Wo) * Ho;
+      GiGrid g;
+      g.w = Wo;
+      g.h = Ho;
+      g.nrm.assign(no * 3, 0.0f);
+      g.dep.assign(no, 0.0f);
+      g.hit.assign(no, 0);
+      g.pos.assign(no * 3, 0.0f);
+      std::vector<float> Eo(no * 3, 0.0f);
+      for (int oy = 0; oy < Ho; ++oy)
+        for (int ox = 0; ox < Wo; ++ox) {
+          const size_t op = static_cast<size_t>(oy) * Wo + ox;
+          V3 eS{0, 0, 0}, nS{0, 0, 0}, pS{0, 0, 0};
+          float zS = 0.0f;
+          int cnt = 0;
+          for (int sy = 0; sy < ss; ++sy)
+            for (int sx = 0; sx < ss; ++sx) {
+              const size_t pix = static_cast<size_t>(oy * ss + sy) * W + (ox * ss + sx);
+              if (rp->amt[pix] <= 0.0f || rp->alpha[pix] <= 0.0f) continue;
+              ++cnt;
+              eS.x += Es[3 * pix]; eS.y += Es[3 * pix + 1]; eS.z += Es[3 * pix + 2];
+              nS.x += nrm[3 * pix]; nS.y += nrm[3 * pix + 1]; nS.z += nrm[3 * pix + 2];
+              pS.x += pos[3 * pix]; pS.y += pos[3 * pix + 1]; pS.z += pos[3 * pix + 2];
+              zS += dep[pix];
+            }
+          if (cnt == 0) continue;
+          const float inv = 1.0f / static_cast<float>(cnt);
+          Eo[3 * op] = eS.x * inv; Eo[3 * op + 1] = eS.y * inv; Eo[3 * op + 2] = eS.z * inv;
+          const V3 nA = safeNormalize(V3{nS.x * inv, nS.y * inv, nS.z * inv});
+          g.nrm[3 * op] = nA.x; g.nrm[3 * op + 1] = nA.y; g.nrm[3 * op + 2] = nA.z;
+          g.dep[op] = zS * inv;
+          g.pos[3 * op] = pS.x * inv; g.pos[3 * op + 1] = pS.y * inv; g.pos[3 * op + 2] = pS.z * inv;
+          g.hit[op] = 1;
+        }
+      denoisePt1E(Wo, Ho, Eo, g.nrm.data(), g.pos.data(), o);
+      std::vector<uint8_t> gel(n, 0);
+      for (size_t i = 0; i < n; ++i) gel[i] = (rp->amt[i] > 0.0f && rp->alpha[i] > 0.0f) ? 1 : 0;
+      const std::vector<float> occLow(no, 1.0f);
+      std::vector<float> Eup, occUp;
+      upsampleJointBilateral(W, H, nrm.data(), dep.data(), gel.data(), g, Eo, occLow, o.pt1UpNormalPow,
+                             o.pt1UpDepthScale, 0, Eup, occUp, nullptr, 0.0f);
+      Es.swap(Eup);
+    }
+  }
+  for (size_t pix = 0; pix < n; ++pix) {
+    if (rp->amt[pix] <= 0.0f || rp->alpha[pix] <= 0.0f) continue;
+    color[4 * pix] += rp->amt[pix] * Es[3 * pix];
+    color[4 * pix + 1] += rp->amt[pix] * Es[3 * pix + 1];
+    color[4 * pix + 2] += rp->amt[pix] * Es[3 * pix + 2];
   }
 }
 
@@ -2040,6 +2829,17 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   c.o.pt1UpDepthScale = d.pt1_upsample_depth_scale;
   c.o.pt1EdgePatchThresh = d.pt1_edge_patch_thresh;
   c.o.pt1EdgePatchSppMul = d.pt1_edge_patch_spp_mul;
+  c.o.giIntegrator = d.gi_integrator;
+  c.o.pt2Pattern = d.pt2_pattern;
+  c.o.pt2Emissive = d.pt2_emissive != 0;
+  c.o.pt2EmissiveNee = d.pt2_emissive_nee != 0;
+  c.o.pt2Reflect = d.pt2_reflect != 0;
+  c.o.pt2Glossy = d.pt2_glossy != 0;
+  c.o.pt2GlossySpp = d.pt2_glossy_spp;
+  c.o.pt2GlossyDenoise = d.pt2_glossy_denoise != 0;
+  c.o.pt2Adaptive = d.pt2_adaptive != 0;
+  c.o.pt2AdaptiveThresh = d.pt2_adaptive_thresh;
+  c.o.pt2AdaptiveMul = d.pt2_adaptive_mul;
   c.o.denoiseIters = d.denoise_iters;
   c.o.denoiseSigmaN = d.denoise_sigma_n;
   c.o.denoiseSigmaZ = d.denoise_sigma_z;
@@ -2114,9 +2914,15 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   // GI seeds per hi-res pixel (storeShadingChannels, embree_renderer.cpp:184-193)
   std::vector<float> giPos, giNrm, giRef, giDep;
   std::vector<uint8_t> giEl;
+  ReflPix rp;
+  const bool reflOn = c.o.gi && c.o.traceRefl();
   if (c.o.gi) {
     giPos.assign(npix * 3, 0.0f); giNrm.assign(npix * 3, 0.0f); giRef.assign(npix * 3, 0.0f);
     giDep.assign(npix, 0.0f); giEl.assign(npix, 0);
+    if (reflOn) {
+      rp.amt.assign(npix, 0.0f); rp.alpha.assign(npix, 0.0f); rp.aspect.assign(npix, 1.0f);
+      rp.f0.assign(npix * 3, 1.0f); rp.tan.assign(npix * 3, 0.0f);
+    }
   }
   auto store = [&](size_t pix, const PixelOut& po) {
     if (c.o.gi) {
@@ -2127,6 +2933,15 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
       }
       giDep[pix] = po.depth;
       giEl[pix] = po.geom == kInvalid ? 0 : po.first.giElig;
+      if (reflOn) {  // storeShadingChannels (embree_renderer.cpp:194-216)
+        rp.amt[pix] = po.first.reflAmt;
+        rp.alpha[pix] = po.first.reflAlpha;
+        rp.aspect[pix] = po.first.reflAspect;
+        for (int k = 0; k < 3; ++k) {
+          rp.f0[3 * pix + k] = (&po.first.reflF0.x)[k];
+          rp.tan[3 * pix + k] = (&po.first.reflTan.x)[k];
+        }
+      }
     }
     color[4 * pix] = po.r; color[4 * pix + 1] = po.g; color[4 * pix + 2] = po.b; color[4 * pix + 3] = po.a;
     depth[pix] = po.depth;
@@ -2442,7 +3257,8 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   if (c.o.gi) {
     const Cam cam{camPos, dir, right, trueUp, d.cam_orthographic != 0, halfW, halfH, persHalfW, persHalfH};
     uint64_t patched = 0;
-    runPt1GiPass(c, cam, W, H, giPos, giNrm, giRef, giDep, giEl, color, nt, &patched);
+    runPt1GiPass(c, cam, W, H, giPos, giNrm, giRef, giDep, giEl, color, nt, &patched, reflOn ? &rp : nullptr,
+                 ss);
     fr->gi_patched_pixels = patched;
   }
   // fog.cpp:7-36 applyFog on the hi-res viewZ (pipeline.cpp:126-129)

@@ -136,3 +136,56 @@ def test_molecular_surface_default_pipeline(gpu_ctx, oracle_lib):
                                        layers=2)
     _defaults(opt, pt1Spp=4, supersample=2)
     _compare(gpu_ctx, oracle_lib, sc, opt)
+
+
+def _pt2_materials(sc, mesh=False):
+    """Mix pt2's features into a scene: emissive spheres and bonds, mirror
+    and glossy POV finishes, principled metal and dielectric, an area light."""
+    from umbreon_gb300 import abi
+    n = sc.sphere_count()
+    mats = np.array(sc.sphere_material, abi.MATERIAL_DTYPE).copy()
+    idx = np.arange(n)
+    mats["emission"][idx % 9 == 0] = 3.0
+    mats["reflection"][idx % 7 == 1] = 0.4                    # mirror (specular 0 -> no lobe)
+    mats["specular"][idx % 7 == 1] = 0.0
+    mats["reflection"][idx % 11 == 2] = 0.3                   # glossy (reflection + highlight)
+    pr = idx % 13 == 3
+    mats["model"][pr] = 1
+    mats["pbr_metallic"][pr] = 1.0
+    mats["pbr_roughness"][pr] = 0.4
+    die = idx % 17 == 4
+    mats["model"][die] = 1
+    mats["pbr_specular"][die] = 0.5
+    mats["pbr_roughness"][die] = 0.05                          # below the glossy cut: a mirror lobe
+    sc.sphere_material = mats
+    if sc.cylinder_count():
+        cm = np.array(sc.cyl_material, abi.MATERIAL_DTYPE).copy()
+        cm["emission"][np.arange(len(cm)) % 10 == 5] = 2.0
+        sc.cyl_material = cm
+    if mesh:
+        m = np.array(sc.mesh_material, abi.MATERIAL_DTYPE).copy()
+        m["emission"] = 0.5
+        sc.mesh_material = m
+    sc.lights[0].angularRadius = 0.05
+    return sc
+
+
+@pytest.mark.parametrize("ss,pattern,adaptive", [(1, 1, False), (2, 1, False), (1, 0, True), (2, 1, True)])
+def test_pt2_ball_and_stick(gpu_ctx, oracle_lib, ss, pattern, adaptive):
+    """pt2 at its defaults (blue-noise Sobol first bounce, emission with the
+    emissive NEE and MIS, traced mirror and glossy reflection with the glossy
+    denoise, area-light NEE jitter) on a mixed-material scene, GPU vs oracle;
+    the per-pixel Sobol pattern and adaptive spp as variants."""
+    sc, opt = scenes.ball_and_stick(n=600, width=64, height=48, supersample=ss, ao_samples=4)
+    _pt2_materials(sc)
+    opt.gi, opt.giIntegrator, opt.pt1Spp = True, 2, 4
+    opt.pt2Pattern, opt.pt2Adaptive, opt.pt2GlossySpp = pattern, adaptive, 4
+    _compare(gpu_ctx, oracle_lib, sc, opt)
+
+
+def test_pt2_molecular_surface_emissive_mesh(gpu_ctx, oracle_lib):
+    sc, opt = scenes.molecular_surface(n_atoms=300, box=14.0, n_spheres=60, width=64, height=64, ao_samples=4,
+                                       layers=2)
+    _pt2_materials(sc, mesh=True)
+    opt.gi, opt.giIntegrator, opt.pt1Spp, opt.pt2GlossySpp = True, 2, 4, 4
+    _compare(gpu_ctx, oracle_lib, sc, opt)

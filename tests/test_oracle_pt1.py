@@ -76,15 +76,17 @@ def test_only_the_cache_integrator_is_refused():
         api.check_gi(opt)
 
 
+@pytest.mark.parametrize("integrator", [1, 2])
 @pytest.mark.parametrize("ss,div", [(1, 2), (2, -1), (2, 1), (3, -1), (1, 3)])
 @pytest.mark.parametrize("denoise,patch", [(True, True), (False, True), (True, False)])
-def test_default_pipeline_known_answer(oracle_lib, ss, div, denoise, patch):
+def test_default_pipeline_known_answer(oracle_lib, ss, div, denoise, patch, integrator):
     """The whole pt1 pipeline at the reference's defaults (gather grid =
     the supersample factor, a-trous denoise of E, joint-bilateral upsample,
     edge patch) keeps the lone sphere's constant E = sky exactly: every stage
     is a normalised weighted mean of that constant."""
     sc, opt, kd = _lone_sphere(pt1Spp=4, giIntensity=0.5, giEnvIntensity=2.0)
     opt.supersample, opt.pt1GatherDiv, opt.pt1Denoise, opt.pt1EdgePatch = ss, div, denoise, patch
+    opt.giIntegrator = integrator
     o = oracle_lib.render(sc, opt)
     hit = (o.hit_geom != KINVALID).reshape(32 * ss, 32, ss).all(-1).reshape(32, ss, 32).all(1)
     col = o.color[..., :3]
@@ -157,3 +159,68 @@ def test_gather_div_resolution():
     assert api.gi_gather_div(o) == 1
     o.supersample, o.pt1GatherDiv = 1, -1
     assert api.gi_gather_div(o) == 1
+
+
+def _pt2_sphere(reflection=0.0, specular=0.0, emission=0.0, **kw):
+    from umbreon_gb300 import abi
+    mat = abi.material(ambient=0.2, diffuse=0.6, specular=specular, reflection=reflection, emission=emission)
+    sc = scenes.material_sphere_scene((0.6, 0.4, 0.2, 1.0), mat, (0.3, 0.3, 0.3))
+    sc.lights = []
+    kw.setdefault("pt1Spp", 4)
+    opt = RenderOptions(width=32, height=32, supersample=1, gi=True, giIntegrator=2, **kw)
+    return sc, opt
+
+
+def test_pt2_mirror_sphere_reflects_the_sky(oracle_lib):
+    """pt2's traced mirror owns the reflection term: a lone mirror-finish
+    sphere's reflected rays all escape, so each hit pixel is the diffuse GI
+    (sky) plus reflection x sky, and the fake reflection x background term
+    is gone."""
+    sc, opt = _pt2_sphere(reflection=0.5, giEnvIntensity=1.5)
+    o = oracle_lib.render(sc, opt)
+    hit = o.hit_geom.reshape(32, 32) != KINVALID
+    col = o.color.reshape(32, 32, 4)[..., :3]
+    want = 0.6 * np.array([0.6, 0.4, 0.2], np.float32) * 1.5 + 0.5 * 1.5
+    np.testing.assert_allclose(col[hit], np.broadcast_to(want, col[hit].shape), rtol=2e-6)
+    opt.pt2Reflect = False  # the fake term returns: + reflection x background
+    f = oracle_lib.render(sc, opt).color.reshape(32, 32, 4)[..., :3]
+    want = 0.6 * np.array([0.6, 0.4, 0.2], np.float32) * 1.5 + 0.5 * 0.3
+    np.testing.assert_allclose(f[hit], np.broadcast_to(want, f[hit].shape), rtol=2e-6)
+
+
+def test_pt2_glossy_lobe_sees_only_sky(oracle_lib):
+    """A glossy finish (reflection with a highlight) samples a GGX lobe; on a
+    lone sphere every sample escapes to the uniform sky, so the traced term is
+    reflection x sky x the mean VNDF weight, which lies in (0, 1]."""
+    sc, opt = _pt2_sphere(reflection=0.5, specular=0.3, pt2GlossySpp=8)
+    o = oracle_lib.render(sc, opt)
+    hit = o.hit_geom.reshape(32, 32) != KINVALID
+    col = o.color.reshape(32, 32, 4)[..., :3]
+    diffuse = 0.6 * np.array([0.6, 0.4, 0.2], np.float32)
+    spec = col[hit] - diffuse
+    assert np.all(spec > 0.0) and np.all(spec <= 0.5 * (1 + 1e-5))
+    np.testing.assert_allclose(spec[:, 0], spec[:, 1], rtol=1e-5)  # grey: the sky, weighted
+
+
+def test_pt2_emitter_lights_a_neighbour(oracle_lib):
+    """pt2 transports emission: an emissive sphere beside a receiver brightens
+    it through the gather (emission at vertices, MIS-weighted against the
+    emissive NEE draw); pt1 and pt2 with emission off do not."""
+    from umbreon_gb300 import abi
+    sc, opt = _pt2_sphere(pt1Spp=16, giEnvIntensity=0.0)
+    em = abi.material(ambient=0.2, diffuse=0.6, emission=4.0)
+    sc.sphere_center_radius = np.array([[0, 0, 0, 1], [2.2, 0, 0.3, 0.8]], np.float32)
+    sc.sphere_color = np.array([[0.6, 0.4, 0.2, 1.0], [1.0, 1.0, 1.0, 1.0]], np.float32)
+    sc.sphere_material = np.array([sc.sphere_material[0], em], abi.MATERIAL_DTYPE)
+    on = oracle_lib.render(sc, opt)
+    opt.pt2Emissive = False
+    off = oracle_lib.render(sc, opt)
+    opt.pt2Emissive, opt.pt2EmissiveNee = True, False
+    bsdf_only = oracle_lib.render(sc, opt)
+    rec = (on.hit_geom.reshape(32, 32) != KINVALID) & (on.hit_prim.reshape(32, 32) == 0)
+    a = on.color.reshape(32, 32, 4)[..., :3][rec].sum()
+    b = off.color.reshape(32, 32, 4)[..., :3][rec].sum()
+    c = bsdf_only.color.reshape(32, 32, 4)[..., :3][rec].sum()
+    assert b == 0.0 and a > 0.0 and c > 0.0
+    # both estimators are unbiased: their means agree within Monte-Carlo noise
+    assert abs(a - c) < 0.15 * a

@@ -135,7 +135,7 @@ class Frame(C.Structure):
         ("avg_hit_dist", f32p), ("aa_mask", f32p), ("ao_patch_mask", f32p),
         ("gb_object_id", u32p), ("gb_material_id", u32p), ("gb_normal", f32p), ("gb_surf_alpha", f32p),
         ("gb_clip_cut", C.POINTER(C.c_uint8)), ("gb_clip_near_vz", f32p), ("gb_clip_far_vz", f32p),
-        ("gi_ms", C.c_double * 5), ("gi_gather_rays", C.c_uint64), ("gi_nee_rays", C.c_uint64),
+        ("gi_ms", C.c_double * 6), ("gi_gather_rays", C.c_uint64), ("gi_nee_rays", C.c_uint64),
         ("gi_gbuffer_rays", C.c_uint64), ("gi_patched_pixels", C.c_uint64),
     ]
 

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <vector>
 
+#include "gi.cuh"
 #include "trace.cuh"
 
 namespace ubr {
@@ -77,6 +78,7 @@ struct Bufs {
   float4* giA;
   float4* giB;
   float4* giR;
+  ReflD rfl;          // pt2 traced-reflection records per hi-res pixel (or null)
   unsigned long long* stats;  // 0 closest rays, 1 occlusion rays, 2 capped, 3 overflow
   uint32_t* counter;  // [0] next-queue size, [1] occlusion work-queue size
   uint32_t* occQueue; // queue slots of hits that cast AO / shadow rays
@@ -679,7 +681,7 @@ UBR_D float ggxLambdaAniso(float ax, float ay, float vx, float vy, float vz) {
 // (light order, rayOffset per light).
 UBR_D f3 shadePrincipled(const Params& p, const ubr_material& m, const Surf& sf, const LightD* lights,
                          const uint8_t* occ, f3 aoFactor, f3 ambLight, float diffuseAo, int px, int py,
-                         const f3* tangent) {
+                         const f3* tangent, bool traceRefl) {
   const f3 C = sf.C, N = sf.N, V = sf.V;
   f3 out{m.emission * C.x + aoFactor.x * m.ambient * C.x * ambLight.x,
          m.emission * C.y + aoFactor.y * m.ambient * C.y * ambLight.y,
@@ -783,592 +785,28 @@ UBR_D f3 shadePrincipled(const Params& p, const ubr_material& m, const Surf& sf,
       out.z += inv * accS.z * L.color.z;
     }
   }
-  if (m.reflection > 0.0f) {
-    out.x += m.reflection * p.bg.x;
-    out.y += m.reflection * p.bg.y;
-    out.z += m.reflection * p.bg.z;
-  } else if (f0max > 0.0f) {
-    out.x += F0.x * p.bg.x;
-    out.y += F0.y * p.bg.y;
-    out.z += F0.z * p.bg.z;
+  // the environment term; pt2's traced reflection owns it instead (:277-302)
+  if (!traceRefl) {
+    if (m.reflection > 0.0f) {
+      out.x += m.reflection * p.bg.x;
+      out.y += m.reflection * p.bg.y;
+      out.z += m.reflection * p.bg.z;
+    } else if (f0max > 0.0f) {
+      out.x += F0.x * p.bg.x;
+      out.y += F0.y * p.bg.y;
+      out.z += F0.z * p.bg.z;
+    }
   }
   return out;
 }
 
-// Material::toonLike / diffuseWeight (scene.hpp:171-196).
-UBR_D bool toonLike(const ubr_material& m) {
-  if (m.model == 2u) return true;
-  if (m.model != 0u) return false;
-  if (m.specular > 1.0f || m.phong > 1.0f || m.brilliance == 0.0f) return true;
-  return m.diffuse <= 0.0f && m.specular <= 0.0f && m.phong <= 0.0f && m.reflection <= 0.0f;
-}
-UBR_D float diffuseWeight(const ubr_material& m) { return m.model == 1u ? m.diffuse * (1.0f - m.pbr_metallic) : m.diffuse; }
-
-// 32-bit integer hash (irradiance_cache.hpp:176-184): seeds the gather's
-// per-pixel stream and the bounce vertices' shadow streams.
-UBR_HD uint32_t hashU32(uint32_t x) {
-  x ^= x >> 16;
-  x *= 0x7FEB352Du;
-  x ^= x >> 15;
-  x *= 0x846CA68Bu;
-  x ^= x >> 16;
-  return x;
-}
-
-// The gather's constants (embree_renderer.cpp:581-612) and its counters.
-struct GiP {
-  int spp, bounces, ld;
-  float maxDist, clampLum;
-  uint32_t seedMix;   // hashU32(pt1Seed)
-  float envI;         // giEnvIntensity
-  f3 amb, sky, ground, envUp;
-  // [0] gather rays (all bounces), [1] NEE shadow rays, [2] G-buffer rays
-  unsigned long long* stats;
-  unsigned long long* overflow;  // the frame's traversal-overflow counter
-};
-
-// A grid the gather runs on, per pixel: the first hit's position and ray
-// distance (pd), its shading normal with the gather eligibility in w (ne),
-// and its geometric normal (ng; null: the shading normal stands in, as the
-// render grid carries none).
-struct GiGrid {
-  int W, H;
-  const float4* pd;
-  const float4* ne;
-  const float4* ng;
-};
-
-// environmentRadiance (irradiance_cache.hpp:188-196): the gather's miss term.
-UBR_D f3 giEnvironment(const GiP& g, f3 wi) {
-  const float w = 0.5f * (dot(wi, g.envUp) + 1.0f);
-  const float e = g.envI;
-  return f3{e * g.amb.x * (g.ground.x + (g.sky.x - g.ground.x) * w),
-            e * g.amb.y * (g.ground.y + (g.sky.y - g.ground.y) * w),
-            e * g.amb.z * (g.ground.z + (g.sky.z - g.ground.z) * w)};
-}
-
-// pt1EvalVertex (pt1_gather.hpp:117-227, pt1 form): a gather-ray hit as a path
-// vertex -- its reflected, hard-shadow-tested direct light (the light's centre
-// ray, whatever the light's radius), its reflectance kd * C, position and
-// shading normal faced toward the ray origin.  Outline primitives end the path.
-template <int KM>
-UBR_D bool pt1Vertex(const DScene& s, const LightD* lights, int nLights, const Hit& h, f3 O, f3 wi, f3& rad,
-                     f3& alb, f3& Py, f3& Ny, uint32_t& nee, uint32_t& ovf) {
-  const int kind = refKind(h.ref);
-  const uint32_t prim = refPrim(h.ref);
-  f3 C, NgSh;
-  uint32_t mi;
-  if (kind == kMesh) {
-    const uint32_t i0 = __ldg(&s.meshIdx[3 * prim]), i1 = __ldg(&s.meshIdx[3 * prim + 1]),
-                   i2 = __ldg(&s.meshIdx[3 * prim + 2]);
-    const float w0 = 1.0f - h.u - h.v;
-    float nb[3];
-    for (int k = 0; k < 3; ++k)
-      nb[k] = w0 * __ldg(&s.meshNrm[3 * i0 + k]) + h.u * __ldg(&s.meshNrm[3 * i1 + k]) +
-              h.v * __ldg(&s.meshNrm[3 * i2 + k]);
-    const float4 c0 = __ldg(&s.meshCol[i0]), c1 = __ldg(&s.meshCol[i1]), c2 = __ldg(&s.meshCol[i2]);
-    C = f3{w0 * c0.x + h.u * c1.x + h.v * c2.x, w0 * c0.y + h.u * c1.y + h.v * c2.y,
-           w0 * c0.z + h.u * c1.z + h.v * c2.z};
-    Ny = normalize(f3{nb[0], nb[1], nb[2]});
-    mi = s.meshTriMat ? __ldg(&s.meshTriMat[s.baseTri ? prim % s.baseTri : 0]) : s.meshMat;
-    NgSh = h.Ng;
-  } else {
-    if (__ldg(&s.primFromEdge[kind][prim])) return false;
-    const float4 fc = __ldg(&s.primColor[kind][prim]);
-    mi = __ldg(&s.primMat[kind][prim]);
-    C = f3{fc.x, fc.y, fc.z};
-    Ny = safeNormalize(h.Ng);
-    NgSh = Ny;
-  }
-  const float kd = diffuseWeight(s.mats[mi]);
-  if (dot(Ny, wi) > 0.0f) Ny = neg(Ny);
-  Py = f3{O.x + wi.x * h.t, O.y + wi.y * h.t, O.z + wi.z * h.t};
-  const float eps = selfIntersectEps(Py, wi, h.t);
-  f3 ng = dot(NgSh, Ny) < 0.0f ? neg(NgSh) : NgSh;
-  ng = safeNormalize(ng, Ny);
-  const f3 So{Py.x + ng.x * eps, Py.y + ng.y * eps, Py.z + ng.z * eps};
-  f3 E{0.0f, 0.0f, 0.0f};
-  for (int l = 0; l < nLights; ++l) {
-    const LightD L = lights[l];
-    const float ndl = dot(Ny, L.L);
-    if (ndl <= 0.0f) continue;
-    Ray r{So, L.L, eps, kInfF};
-    Hit hh;
-    Count cnt;
-    const float sh = traverse<false, KM, true>(travOf(s), r, hh, ovf, &cnt, true) ? 0.0f : 1.0f;
-    ++nee;
-    E.x += ndl * L.color.x * sh;
-    E.y += ndl * L.color.y * sh;
-    E.z += ndl * L.color.z * sh;
-  }
-  rad = f3{kd * C.x * E.x, kd * C.y * E.y, kd * C.z * E.z};
-  alb = f3{kd * C.x, kd * C.y, kd * C.z};
-  return true;
-}
-
-// pt1GatherPoint (pt1_gather.hpp:268-523, pt1 form) at one grid point:
-// E_stored = (1/spp) sum over cosine-hemisphere paths (Hammersley + Cranley-
-// Patterson shift when ld, else the tea2 stream) of the NEE radiance at
-// every vertex and the sky where the path escapes; Russian roulette from
-// the second vertex on; a first bounce below the geometric horizon adds
-// nothing.  Returns (E, first-bounce hit fraction).
-template <int KM>
-UBR_D float4 pt1GatherPoint(const GiP& g, const DScene& s, const LightD* lights, int nLights, f3 P, f3 N, f3 Ng,
-                            float tEps, uint32_t seed, int spp, uint32_t& rays, uint32_t& nee, uint32_t& ovf) {
-  const Frame3 f = frameFromNormal(N);
-  const float eps = selfIntersectEps(P, N, tEps);
-  const f3 O{P.x + N.x * eps, P.y + N.y * eps, P.z + N.z * eps};
-  const int maxB = g.bounces < 1 ? 1 : g.bounces;
-  float cpx = 0.0f, cpy = 0.0f;
-  if (g.ld) {
-    uint32_t c0 = seed, c1 = 0x9E3779B9u;
-    tea2(c0, c1);
-    cpx = u32ToUnorm(c0);
-    cpy = u32ToUnorm(c1);
-  }
-  const TravScene ts = travOf(s);
-  f3 Esum{0.0f, 0.0f, 0.0f};
-  int nOcc = 0;
-  for (int sI = 0; sI < spp; ++sI) {
-    uint32_t s0 = seed, s1 = uint32_t(sI);
-    tea2(s0, s1);
-    float u1, u2;
-    if (g.ld) {
-      u1 = float(sI) / float(spp) + cpx;
-      u2 = radicalInverse2(uint32_t(sI)) + cpy;
-      if (u1 >= 1.0f) u1 -= 1.0f;
-      if (u2 >= 1.0f) u2 -= 1.0f;
-    } else {
-      u1 = u32ToUnorm(s0);
-      u2 = u32ToUnorm(s1);
-    }
-    f3 wi = cosineSampleHemisphere(u1, u2, f);
-    const bool horizonOk = dot(wi, Ng) > 0.0f;
-    if (!horizonOk) ++nOcc;
-    f3 org = O;
-    float tnear = eps;
-    f3 thr{1.0f, 1.0f, 1.0f}, L{0.0f, 0.0f, 0.0f};
-    for (int bnc = 1; horizonOk && bnc <= maxB; ++bnc) {
-      Ray r{org, wi, tnear, g.maxDist};
-      Hit h;
-      Count cnt;
-      traverse<false, KM>(ts, r, h, ovf, &cnt, false);
-      ++rays;
-      if (h.ref == kInvalid) {
-        const f3 env = giEnvironment(g, wi);
-        L.x += thr.x * env.x;
-        L.y += thr.y * env.y;
-        L.z += thr.z * env.z;
-        break;
-      }
-      if (bnc == 1) ++nOcc;
-      f3 rad, alb, Py, Ny;
-      if (!pt1Vertex<KM>(s, lights, nLights, h, org, wi, rad, alb, Py, Ny, nee, ovf)) break;
-      L.x += thr.x * rad.x;
-      L.y += thr.y * rad.y;
-      L.z += thr.z * rad.z;
-      if (bnc == maxB) break;
-      thr.x *= alb.x;
-      thr.y *= alb.y;
-      thr.z *= alb.z;
-      if (bnc >= 2) {
-        tea2(s0, s1);
-        float pc = fmaxf(thr.x, fmaxf(thr.y, thr.z));
-        pc = fminf(0.95f, fmaxf(0.05f, pc));
-        if (u32ToUnorm(s0) >= pc) break;
-        const float inv = 1.0f / pc;
-        thr.x *= inv;
-        thr.y *= inv;
-        thr.z *= inv;
-      }
-      tea2(s0, s1);
-      const Frame3 fv = frameFromNormal(Ny);
-      wi = cosineSampleHemisphere(u32ToUnorm(s0), u32ToUnorm(s1), fv);
-      const float epsV = selfIntersectEps(Py, wi, h.t);
-      org = f3{Py.x + Ny.x * epsV, Py.y + Ny.y * epsV, Py.z + Ny.z * epsV};
-      tnear = epsV;
-    }
-    if (g.clampLum > 0.0f) {
-      const float lum = 0.2126f * L.x + 0.7152f * L.y + 0.0722f * L.z;
-      if (lum > g.clampLum) {
-        const float k = g.clampLum / lum;
-        L.x *= k;
-        L.y *= k;
-        L.z *= k;
-      }
-    }
-    Esum.x += L.x;
-    Esum.y += L.y;
-    Esum.z += L.z;
-  }
-  const float invN = 1.0f / float(spp > 0 ? spp : 1);
-  return make_float4(Esum.x * invN, Esum.y * invN, Esum.z * invN, float(nOcc) * invN);
-}
-
-// gatherPt1Grid (pt1_gather.hpp:525-614): E and the hit fraction of every
-// eligible point of a grid (or of the points a list names), seeded from the
-// grid index: seed = hashU32(pix ^ hashU32(pt1Seed)); the primary hit
-// distance scales the origin epsilon.  One thread per point, 128 per block.
-// Points not eligible get zero (grid form only; a list names eligible
-// points).  `listCount` (device) bounds the list when non-null.
-template <int KM>
-__global__ void __launch_bounds__(128) k_pt1_gather(GiP g, DScene s, const LightD* lights, int nLights, GiGrid grid,
-                                                    const uint32_t* list, const uint32_t* listCount, uint32_t n,
-                                                    int spp, float4* E) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t rays = 0, nee = 0, ovf = 0;
-  const uint32_t cnt = listCount ? min(n, *listCount) : n;
-  if (i < cnt) {
-    const uint32_t pix = list ? list[i] : i;
-    const float4 ne = grid.ne[pix];
-    float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (ne.w != 0.0f) {
-      const float4 pd = grid.pd[pix];
-      const f3 N{ne.x, ne.y, ne.z};
-      f3 Ng = N;
-      if (grid.ng) {
-        const float4 q = grid.ng[pix];
-        Ng = f3{q.x, q.y, q.z};
-      }
-      const uint32_t seed = hashU32(pix ^ g.seedMix);
-      const float tEps = pd.w > 0.0f ? pd.w : 1.0f;
-      e = pt1GatherPoint<KM>(g, s, lights, nLights, f3{pd.x, pd.y, pd.z}, N, Ng, tEps, seed, spp, rays, nee, ovf);
-    }
-    E[pix] = e;
-  }
-  warpCount(&g.stats[0], rays);
-  warpCount(&g.stats[1], nee);
-  warpCount(g.overflow, ovf);
-}
-
-// tracePt1GBuffer (pt1_gbuffer.hpp:83-196): one primary ray per point of a
-// w x h grid over the same image plane as the render grid, closest hit in
-// [0, inf) (no clip planes): position and ray distance, the face-forwarded
-// shading normal (mesh: interpolated vertex normal; primitive: its geometric
-// normal) with hit = 1, the face-forwarded geometric normal.  Outline
-// primitives and misses are not gather points (zeros).
-template <int KM>
-__global__ void __launch_bounds__(128) k_pt1_gbuffer(Params p, DScene s, int w, int h, float4* pd, float4* ne,
-                                                     float4* ng, unsigned long long* stats,
-                                                     unsigned long long* overflow) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t traced = 0, ovf = 0;
-  if (i < uint32_t(w) * uint32_t(h)) {
-    const int px = int(i % uint32_t(w)), py = int(i / uint32_t(w));
-    const float v = 1.0f - 2.0f * (float(py) + 0.5f) / float(h);
-    const float u = 2.0f * (float(px) + 0.5f) / float(w) - 1.0f;
-    f3 org, rd;
-    if (p.ortho) {
-      org = p.camPos + p.right * (u * p.halfW) + p.up * (v * p.halfH);
-      rd = p.camDir;
-    } else {
-      org = p.camPos;
-      rd = normalize(p.camDir + p.right * (u * p.persHalfW) + p.up * (v * p.persHalfH));
-    }
-    Ray r{org, rd, 0.0f, kInfF};
-    Hit hh;
-    Count cnt;
-    traverse<false, KM>(travOf(s), r, hh, ovf, &cnt, false);
-    traced = 1;
-    float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a, c = a;
-    if (hh.ref != kInvalid) {
-      const int kind = refKind(hh.ref);
-      const uint32_t prim = refPrim(hh.ref);
-      bool ok = true;
-      f3 N, Ng;
-      if (kind == kMesh) {
-        const uint32_t i0 = __ldg(&s.meshIdx[3 * prim]), i1 = __ldg(&s.meshIdx[3 * prim + 1]),
-                       i2 = __ldg(&s.meshIdx[3 * prim + 2]);
-        const float w0 = 1.0f - hh.u - hh.v;
-        float nb[3];
-        for (int k = 0; k < 3; ++k)
-          nb[k] = w0 * __ldg(&s.meshNrm[3 * i0 + k]) + hh.u * __ldg(&s.meshNrm[3 * i1 + k]) +
-                  hh.v * __ldg(&s.meshNrm[3 * i2 + k]);
-        N = safeNormalize(f3{nb[0], nb[1], nb[2]});
-        Ng = safeNormalize(hh.Ng);
-      } else {
-        ok = __ldg(&s.primFromEdge[kind][prim]) == 0;
-        N = safeNormalize(hh.Ng);
-        Ng = N;
-      }
-      if (ok) {
-        if (dot(N, rd) > 0.0f) N = neg(N);
-        if (dot(Ng, rd) > 0.0f) Ng = neg(Ng);
-        a = make_float4(org.x + rd.x * hh.t, org.y + rd.y * hh.t, org.z + rd.z * hh.t, hh.t);
-        b = make_float4(N.x, N.y, N.z, 1.0f);
-        c = make_float4(Ng.x, Ng.y, Ng.z, 0.0f);
-      }
-    }
-    pd[i] = a;
-    ne[i] = b;
-    ng[i] = c;
-  }
-  warpCount(&stats[2], traced);
-  warpCount(overflow, ovf);
-}
-
-// ---- denoisePt1E (pt1_denoise.cpp:20-80): the a-trous filter of
-// denoise_atrous.cpp:27-220 on E at gather resolution, normal and position
-// guides, no albedo demodulation (E is irradiance) ----
-constexpr float kDnEps = 1.0e-3f;
-
-UBR_D float lumOf(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
-
-// non-finite E scrubbed to 0; a point is valid when its normal is unit-length
-__global__ void k_gdn_init(uint32_t n, float4* E, const float4* ne, uint8_t* valid, float4* irr) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  float4 e = E[p];
-  if (!isfinite(e.x)) e.x = 0.0f;
-  if (!isfinite(e.y)) e.y = 0.0f;
-  if (!isfinite(e.z)) e.z = 0.0f;
-  E[p] = e;
-  irr[p] = e;
-  const float4 q = ne[p];
-  valid[p] = (q.x * q.x + q.y * q.y + q.z * q.z) > 0.25f ? 1 : 0;
-}
-
-// per valid point: the largest distance to a valid 4-neighbour's position
-// (floor kDnEps) and the luminance variance over the valid 3x3 neighbourhood
-__global__ void k_gdn_aux(int W, int H, const uint8_t* valid, const float4* irr, const float4* pd, float* var,
-                          float* pgrad) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= uint32_t(W) * uint32_t(H)) return;
-  float v = 0.0f, gr = kDnEps;
-  if (valid[p]) {
-    const int x = int(p % uint32_t(W)), y = int(p / uint32_t(W));
-    const float4 pp = pd[p];
-    const int nb[4][2] = {{1, 0}, {-1, 0}, {0, 1}, {0, -1}};
-    for (int k = 0; k < 4; ++k) {
-      const int qx = x + nb[k][0], qy = y + nb[k][1];
-      if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
-      const size_t q = size_t(qy) * W + qx;
-      if (!valid[q]) continue;
-      const float4 pq = pd[q];
-      const float dx = pp.x - pq.x, dy = pp.y - pq.y, dz = pp.z - pq.z;
-      gr = fmaxf(gr, sqrtf(dx * dx + dy * dy + dz * dz));
-    }
-    float sm = 0.0f, s2 = 0.0f;
-    int n = 0;
-    for (int dy = -1; dy <= 1; ++dy)
-      for (int dx = -1; dx <= 1; ++dx) {
-        const int qx = x + dx, qy = y + dy;
-        if (qx < 0 || qx >= W || qy < 0 || qy >= H) continue;
-        const size_t q = size_t(qy) * W + qx;
-        if (!valid[q]) continue;
-        const float4 c = irr[q];
-        const float l = lumOf(c.x, c.y, c.z);
-        sm += l;
-        s2 += l * l;
-        ++n;
-      }
-    if (n > 0) {
-      const float mean = sm / float(n);
-      v = fmaxf(0.0f, s2 / float(n) - mean * mean);
-    }
-  }
-  var[p] = v;
-  pgrad[p] = gr;
-}
-
-// one iteration: 5x5 B3 taps at 2^it spacing with the normal^sigmaN,
-// exp(-|dP| / (sigmaZ grad step + eps)) and exp(-|dl| / (sigmaL sqrt(var) +
-// eps)) edge-stops, in the reference's weight order
-__global__ void k_gdn_iter(int W, int H, int step, const uint8_t* valid, const float4* ne, const float4* pd,
-                           const float4* irr, const float* var, const float* pgrad, float sigmaN, float sigmaZ,
-                           float sigmaL, float4* next) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= uint32_t(W) * uint32_t(H)) return;
-  const float4 ip = irr[p];
-  if (!valid[p]) {
-    next[p] = ip;
-    return;
-  }
-  const float h5[5] = {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f};
-  const int x = int(p % uint32_t(W)), y = int(p / uint32_t(W));
-  const float4 n4 = ne[p], p4 = pd[p];
-  const f3 np{n4.x, n4.y, n4.z}, pp{p4.x, p4.y, p4.z};
-  const float lp = lumOf(ip.x, ip.y, ip.z);
-  const float lDenom = sigmaL * sqrtf(var[p]) + kDnEps;
-  const float zDenom = sigmaZ * pgrad[p] * float(step) + kDnEps;
-  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, wsum = 0.0f;
-  for (int dy = -2; dy <= 2; ++dy) {
-    const int qy = y + dy * step;
-    if (qy < 0 || qy >= H) continue;
-    for (int dx = -2; dx <= 2; ++dx) {
-      const int qx = x + dx * step;
-      if (qx < 0 || qx >= W) continue;
-      const size_t q = size_t(qy) * W + qx;
-      if (!valid[q]) continue;
-      float w = h5[dx + 2] * h5[dy + 2];
-      const float4 nq = ne[q], pq = pd[q], iq = irr[q];
-      const float nd = fmaxf(0.0f, np.x * nq.x + np.y * nq.y + np.z * nq.z);
-      w *= powf(nd, sigmaN);
-      const float ddx = pp.x - pq.x, ddy = pp.y - pq.y, ddz = pp.z - pq.z;
-      w *= expf(-sqrtf(ddx * ddx + ddy * ddy + ddz * ddz) / zDenom);
-      w *= expf(-fabsf(lp - lumOf(iq.x, iq.y, iq.z)) / lDenom);
-      s0 += w * iq.x;
-      s1 += w * iq.y;
-      s2 += w * iq.z;
-      wsum += w;
-    }
-  }
-  next[p] = wsum > 0.0f ? make_float4(s0 / wsum, s1 / wsum, s2 / wsum, ip.w) : ip;
-}
-
-__global__ void k_gdn_write(uint32_t n, const uint8_t* valid, const float4* irr, float4* E) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n || !valid[p]) return;
-  const float4 v = irr[p];
-  E[p] = make_float4(fmaxf(0.0f, v.x), fmaxf(0.0f, v.y), fmaxf(0.0f, v.z), E[p].w);
-}
-
-// upsampleJointBilateral (pt1_upsample.hpp:40-199): E (and the hit fraction)
-// of every eligible render-grid pixel from the 2x2 gather-grid points around
-// its centre, weighted bilinear x max(0, N.Nh)^normalPow x
-// exp(-|z - zh| / (depthScale z + 1e-6)); when every weight dies, the
-// nearest valid point of the quad, then (coarse grids, fallbackR > 0) the
-// nearest valid point of the (2r)^2 window.  With the edge patch on, pixels
-// whose weights died or summed below patchThresh are appended to the patch
-// list.  Pixels not eligible get zero.
-__global__ void k_pt1_upsample(int W, int H, const float4* fpd, const float4* fne, GiGrid lo, const float4* Elo,
-                               float normalPow, float depthScale, int fallbackR, int patchOn, float patchThresh,
-                               float4* E, uint32_t* patchList, uint32_t* patchCount,
-                               unsigned long long* holes) {
-  const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-  bool patch = false, hole = false;
-  if (pix < uint32_t(W) * uint32_t(H)) {
-    const float4 nf4 = fne[pix];
-    float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (nf4.w != 0.0f) {
-      const int px = int(pix % uint32_t(W)), py = int(pix / uint32_t(W));
-      const int hw = lo.W, hh = lo.H;
-      const float sy = (float(py) + 0.5f) * float(hh) / float(H) - 0.5f;
-      const int by = int(floorf(sy));
-      const float fy = sy - float(by);
-      const float sx = (float(px) + 0.5f) * float(hw) / float(W) - 0.5f;
-      const int bx = int(floorf(sx));
-      const float fx = sx - float(bx);
-      const f3 Nf{nf4.x, nf4.y, nf4.z};
-      const float zf = fpd[pix].w;
-      float wSum = 0.0f, e0 = 0.0f, e1 = 0.0f, e2 = 0.0f, oS = 0.0f, bestBilin = -1.0f;
-      int bestPix = -1;
-      for (int dy = 0; dy < 2; ++dy)
-        for (int dx = 0; dx < 2; ++dx) {
-          const int hx = min(max(bx + dx, 0), hw - 1), hy = min(max(by + dy, 0), hh - 1);
-          const int hp = hy * hw + hx;
-          const float4 nh = lo.ne[hp];
-          if (nh.w == 0.0f) continue;
-          const float wb = (dx ? fx : 1.0f - fx) * (dy ? fy : 1.0f - fy);
-          if (wb > bestBilin) {
-            bestBilin = wb;
-            bestPix = hp;
-          }
-          const float wn = powf(fmaxf(0.0f, Nf.x * nh.x + Nf.y * nh.y + Nf.z * nh.z), normalPow);
-          const float zh = lo.pd[hp].w;
-          const float wz = expf(-fabsf(zf - zh) / (depthScale * zf + 1e-6f));
-          const float w = wb * wn * wz;
-          const float4 eh = Elo[hp];
-          wSum += w;
-          e0 += w * eh.x;
-          e1 += w * eh.y;
-          e2 += w * eh.z;
-          oS += w * eh.w;
-        }
-      if (wSum >= 1e-6f) {
-        patch = wSum < patchThresh;
-        const float inv = 1.0f / wSum;
-        out = make_float4(e0 * inv, e1 * inv, e2 * inv, oS * inv);
-      } else if (bestPix >= 0) {
-        patch = true;
-        out = Elo[bestPix];
-      } else {
-        patch = true;
-        int found = -1;
-        if (fallbackR > 0) {
-          float bestD2 = 1e30f;
-          for (int wy = by - fallbackR + 1; wy <= by + fallbackR; ++wy) {
-            if (wy < 0 || wy >= hh) continue;
-            for (int wx = bx - fallbackR + 1; wx <= bx + fallbackR; ++wx) {
-              if (wx < 0 || wx >= hw) continue;
-              const int hp = wy * hw + wx;
-              if (lo.ne[hp].w == 0.0f) continue;
-              const float ddx = float(wx) - sx, ddy = float(wy) - sy;
-              const float d2 = ddx * ddx + ddy * ddy;
-              if (d2 < bestD2) {
-                bestD2 = d2;
-                found = hp;
-              }
-            }
-          }
-        }
-        if (found >= 0) out = Elo[found];
-        else hole = true;
-      }
-      patch = patch && patchOn;
-    }
-    E[pix] = out;
-  }
-  int off;
-  const int base = warpPushBase(patch, patchCount, off);
-  if (patch) patchList[base + off] = pix;
-  warpCount(holes, hole ? 1u : 0u);
-}
-
-// smoothPatchedPixels (pt1_upsample.hpp:214-248), radius 2: each patched
-// pixel's E becomes the guide-weighted mean of its (2r+1)^2 eligible
-// neighbourhood in the snapshot (itself at weight 1; neighbour weights below
-// 1e-4 dropped).
-__global__ void k_pt1_smooth(int W, int H, const uint32_t* list, const uint32_t* count, uint32_t n,
-                             const float4* fpd, const float4* fne, float normalPow, float depthScale, int radius,
-                             const float4* Esrc, float4* E) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= min(n, *count)) return;
-  const uint32_t pix = list[i];
-  const int px = int(pix % uint32_t(W)), py = int(pix / uint32_t(W));
-  const float4 nf = fne[pix];
-  const float zf = fpd[pix].w;
-  const float4 e = Esrc[pix];
-  float wSum = 1.0f, e0 = e.x, e1 = e.y, e2 = e.z, oS = e.w;
-  for (int dy = -radius; dy <= radius; ++dy) {
-    const int ny = py + dy;
-    if (ny < 0 || ny >= H) continue;
-    for (int dx = -radius; dx <= radius; ++dx) {
-      if (dx == 0 && dy == 0) continue;
-      const int nx = px + dx;
-      if (nx < 0 || nx >= W) continue;
-      const size_t q = size_t(ny) * W + nx;
-      const float4 nn = fne[q];
-      if (nn.w == 0.0f) continue;
-      const float wn = powf(fmaxf(0.0f, nf.x * nn.x + nf.y * nn.y + nf.z * nn.z), normalPow);
-      const float zn = fpd[q].w;
-      const float wz = expf(-fabsf(zf - zn) / (depthScale * zf + 1e-6f));
-      const float w = wn * wz;
-      if (w < 1e-4f) continue;
-      const float4 eq = Esrc[q];
-      wSum += w;
-      e0 += w * eq.x;
-      e1 += w * eq.y;
-      e2 += w * eq.z;
-      oS += w * eq.w;
-    }
-  }
-  const float inv = 1.0f / wSum;
-  E[pix] = make_float4(e0 * inv, e1 * inv, e2 * inv, oS * inv);
-}
-
-// The [E] composite (embree_renderer.cpp:908-927): every eligible pixel adds
-// giIntensity * (kd * pigment) * E.
-__global__ void k_pt1_composite(uint32_t n, const float4* ne, const float4* refl, const float4* E, float gI,
-                                float4* color) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n || ne[p].w == 0.0f) return;
-  const float4 rf = refl[p], e = E[p];
-  float4 c = color[p];
-  c.x += gI * rf.x * e.x;
-  c.y += gI * rf.y * e.y;
-  c.z += gI * rf.z * e.z;
-  color[p] = c;
+// pt2GgxAlphaFromRoughness (shading.hpp:48-60): the GGX alpha matched to the
+// Blinn highlight width, sqrt(2 / (blinnExp + 2)); below 0.015 a mirror (0).
+UBR_D float ggxAlphaFromRoughness(float roughness) {
+  const float e = blinnExp(roughness);
+  const float a = sqrtf(2.0f / (e + 2.0f));
+  if (a < 0.015f) return 0.0f;
+  return a < 1.0f ? a : 1.0f;
 }
 
 template <bool BATCH>
@@ -1462,13 +900,38 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
       }
       const f3 C = sf.C, N = sf.N, V = sf.V;
       f3 out;
+      // pt2 traced reflection of this hit (HitShade::reflectivity / reflAlpha
+      // / reflF0 / reflTangent / reflAspect)
+      bool traceRefl = false;
+      float rAmt = 0.0f, rAlpha = 0.0f, rAspect = 1.0f;
+      f3 rF0{1.0f, 1.0f, 1.0f}, rTan{0.0f, 0.0f, 0.0f};
       if (m.model == 1u) {
         // --- principled direct pass (shading.hpp:88-91 -> principled.hpp) ---
         f3 anisoT{0.0f, 0.0f, 0.0f};
         const bool tanValid = sf.kind != kMesh && !sf.fromEdge && m.pbr_anisotropy != 0.0f &&
                               anisoTangent(s, sf, m.pbr_anisotropy_rotation, anisoT);
+        // traced-reflection ownership (hit_shader.hpp:243-270, 426-452): a
+        // specular lobe (metallic or dielectric F0 > 0) reflects, Fresnel
+        // folded into the pass, alpha = roughness^2 (a mirror below 0.015)
+        if (p.pt2Refl && (sf.kind == kMesh || !sf.fromEdge) &&
+            (m.pbr_metallic > 1e-4f || m.pbr_specular > 1e-4f)) {
+          traceRefl = true;
+          rAmt = 1.0f;
+          const float dd = 0.08f * m.pbr_specular, tm = m.pbr_metallic;
+          rF0 = f3{dd + (C.x - dd) * tm, dd + (C.y - dd) * tm, dd + (C.z - dd) * tm};
+          if (p.pt2Glossy) {
+            const float a = m.pbr_roughness * m.pbr_roughness;
+            rAlpha = a >= 0.015f ? a : 0.0f;
+            if (tanValid) {
+              rTan = anisoT;
+              float an = fabsf(m.pbr_anisotropy);
+              if (an > 1.0f) an = 1.0f;
+              rAspect = sqrtf(1.0f - 0.9f * an);
+            }
+          }
+        }
         out = shadePrincipled(p, m, sf, lights, b.occ + rb + p.aoSamples, aoFactor, ambLight, diffuseAo, px, py,
-                              tanValid ? &anisoT : nullptr);
+                              tanValid ? &anisoT : nullptr, traceRefl);
       } else {
       // --- shadeLocal, POV branch (shading.hpp:96-191) ---
       out = f3{m.emission * C.x + aoFactor.x * m.ambient * C.x * ambLight.x,
@@ -1531,7 +994,12 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
           out.z += sc * hl.z;
         }
       }
-      if (m.reflection > 0.0f) {
+      if (p.pt2Refl && (sf.kind == kMesh || !sf.fromEdge) && m.reflection > 0.0f) {
+        traceRefl = true;
+        rAmt = m.reflection;
+        if (p.pt2Glossy && m.specular > 0.0f) rAlpha = ggxAlphaFromRoughness(m.roughness);
+      }
+      if (m.reflection > 0.0f && !traceRefl) {
         out.x += m.reflection * p.bg.x;
         out.y += m.reflection * p.bg.y;
         out.z += m.reflection * p.bg.z;
@@ -1566,6 +1034,13 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
           b.giA[gpix] = make_float4(sf.P.x, sf.P.y, sf.P.z, t);
           b.giB[gpix] = make_float4(sf.N.x, sf.N.y, sf.N.z, giElig ? 1.0f : 0.0f);
           b.giR[gpix] = make_float4(kd * sf.C.x, kd * sf.C.y, kd * sf.C.z, 0.0f);
+          if (b.rfl.amt) {
+            // the first hit's traced-reflection record (storeShadingChannels,
+            // embree_renderer.cpp:194-216)
+            b.rfl.amt[gpix] = make_float4(rAmt, rAlpha, rAspect, 0.0f);
+            b.rfl.f0[gpix] = make_float4(rF0.x, rF0.y, rF0.z, 0.0f);
+            if (b.rfl.tan) b.rfl.tan[gpix] = make_float4(rTan.x, rTan.y, rTan.z, 0.0f);
+          }
         }
         if (b.gbObj) {
           // edge G-buffer (hit_shader.hpp:278-300, 460-478; transparency.hpp:394-428)
@@ -2249,7 +1724,14 @@ ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vect
   if (d.width <= 0 || d.height <= 0) return setError(c, UBR_INVALID_ARGUMENT, "render desc: width/height must be > 0");
   const int ss = d.supersample < 1 ? 1 : d.supersample;
   if (d.gi) {
-    if (d.gi_integrator != 1) return setError(c, UBR_INVALID_ARGUMENT, "render desc: gi needs gi_integrator 1 (pt1)");
+    if (d.gi_integrator != 1 && d.gi_integrator != 2)
+      return setError(c, UBR_INVALID_ARGUMENT, "render desc: gi needs gi_integrator 1 (pt1) or 2 (pt2)");
+    if (d.gi_integrator == 2 && d.pt2_rounds > 0)
+      return setError(c, UBR_INVALID_ARGUMENT, "render desc: pt2 ReSTIR rounds (pt2_rounds > 0) are not built");
+    if (d.gi_integrator == 2 && (d.pt2_pattern < 0 || d.pt2_pattern > 1))
+      return setError(c, UBR_INVALID_ARGUMENT, "render desc: pt2_pattern must be 0 (Sobol) or 1 (blue noise)");
+    if (d.gi_integrator == 2 && d.pt2_reflect && d.pt2_glossy && d.pt2_glossy_spp < 1)
+      return setError(c, UBR_INVALID_ARGUMENT, "render desc: pt2_glossy_spp must be >= 1");
     if (d.pt1_spp < 1 || d.gi_bounces < 1)
       return setError(c, UBR_INVALID_ARGUMENT, "render desc: gi needs pt1_spp >= 1 and gi_bounces >= 1");
     if (d.pt1_gather_div < -1)
@@ -2297,6 +1779,8 @@ ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vect
   p.aoWriteAov = d.ao_write_aov ? 1 : 0;
   p.gi = d.gi ? 1 : 0;
   p.giIntensity = d.gi_intensity;
+  p.pt2Refl = (d.gi && d.gi_integrator == 2 && d.pt2_reflect) ? 1 : 0;
+  p.pt2Glossy = (p.pt2Refl && d.pt2_glossy) ? 1 : 0;
   p.aaMode = d.aa_mode == 1 ? 1 : 0;  // any other value renders the full grid
   p.aaThreshold = d.aa_threshold;
   p.aoEnhanced = (d.ao_falloff_power > 0.0f || d.ao_multiscale || d.ao_bent_normal || d.ao_multibounce ||
@@ -2614,6 +2098,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   b.colorHi = scratchT<float4>(c, 18, npix, st);
   const bool giOn = p1.gi != 0;
   GiP gp{};
+  b.rfl = ReflD{nullptr, nullptr, nullptr};
   if (giOn) {
     if (batch) return setError(c, UBR_INVALID_ARGUMENT, "render desc: gi renders one frame per call");
     b.giA = scratchT<float4>(c, 112, npix, st);
@@ -2633,6 +2118,11 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     gp.sky = f3{d0.pt1_sky_radiance[0], d0.pt1_sky_radiance[1], d0.pt1_sky_radiance[2]};
     gp.ground = d0.pt1_sky_mode == 1 ? f3{d0.ao_ground_color[0], d0.ao_ground_color[1], d0.ao_ground_color[2]} : gp.sky;
     gp.stats = scratchT<unsigned long long>(c, 115, 4, st);
+    if (p1.pt2Refl) {
+      b.rfl.amt = scratchT<float4>(c, 141, npix, st);
+      b.rfl.f0 = scratchT<float4>(c, 142, npix, st);
+      if (p1.pt2Glossy && jobs[0].scene->anisoPrincipled) b.rfl.tan = scratchT<float4>(c, 143, npix, st);
+    }
   }
   b.depth = scratchT<float>(c, 19, npix, st);
   b.viewZ = scratchT<float>(c, 20, npix, st);
@@ -3091,7 +2581,6 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     if (giDiv == 0) giDiv = d0.pt1_half_res ? 2 : 1;
     if (giDiv < 1) giDiv = 1;
   }
-  uint32_t giPatchCount = 0;
   auto giPass = [&]() -> ubr_status {
     ubr_status gs = UBR_OK;
     for (cudaEvent_t& e : c->giEv)
@@ -3099,13 +2588,32 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     gp.overflow = b.stats + 3;
     UBR_CUDA(c, cudaMemsetAsync(gp.stats, 0, 4 * sizeof(unsigned long long), s));
     const LightD* lt = b.lights + p1.lightOff;
+    const int nL = p1.nLights;
     const int spp = d0.pt1_spp;
     const GiGrid full{p1.W, p1.H, b.giA, b.giB, nullptr};
+    // pt2's gather configuration (embree_renderer.cpp:620-660): the sampler,
+    // emission at vertices, emissive NEE when the scene emits; adaptive spp
+    // (spp >= 2) adds spp * (mul - 1) samples where the estimate is noisy
+    const bool pt2 = d0.gi_integrator == 2;
+    gp.pt2 = pt2 ? 1 : 0;
+    gp.pattern = d0.pt2_pattern;
+    gp.emissive = (pt2 && d0.pt2_emissive) ? 1 : 0;
+    gp.em = (pt2 && d0.pt2_emissive && d0.pt2_emissive_nee) ? jobs[0].scene->emit : EmitD{};
+    gp.sampleOffset = 0;
+    gp.halfE = nullptr;
+    const bool adapt = pt2 && d0.pt2_adaptive && spp >= 2;
+    const int extra = adapt ? spp * (std::max(2, d0.pt2_adaptive_mul) - 1) : 0;
+    auto pow2 = [](uint32_t v) {
+      uint32_t q = 1;
+      while (q < v) q <<= 1;
+      return q;
+    };
+    gp.sppPow2 = pow2(uint32_t(spp + extra));
     float4* Ef = scratchT<float4>(c, 116, npix, gs);
     if (gs != UBR_OK) return gs;
     // denoisePt1E on a w x h grid
     auto denoiseE = [&](int w, int h, float4* E, const float4* ne, const float4* pd) -> ubr_status {
-      const uint32_t n = uint32_t(w) * uint32_t(h), g = (n + 255) / 256;
+      const uint32_t n = uint32_t(w) * uint32_t(h);
       ubr_status ds = UBR_OK;
       uint8_t* valid = scratchT<uint8_t>(c, 121, n, ds);
       float4* irrA = scratchT<float4>(c, 122, n, ds);
@@ -3113,21 +2621,53 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       float* var = scratchT<float>(c, 124, n, ds);
       float* pgrad = scratchT<float>(c, 125, n, ds);
       if (ds != UBR_OK) return ds;
-      k_gdn_init<<<g, 256, 0, s>>>(n, E, ne, valid, irrA);
+      giDenoiseInit(s, n, E, ne, valid, irrA);
       ++kernels;
       const int iters = std::max(0, d0.denoise_iters);
       if (iters > 0) {
-        k_gdn_aux<<<g, 256, 0, s>>>(w, h, valid, irrA, pd, var, pgrad);
+        giDenoiseAux(s, w, h, valid, irrA, pd, var, pgrad);
         float4* cur = irrA;
         float4* nxt = irrB;
         for (int it = 0; it < iters; ++it) {
-          k_gdn_iter<<<g, 256, 0, s>>>(w, h, 1 << it, valid, ne, pd, cur, var, pgrad, d0.denoise_sigma_n,
-                                       std::max(1.0e-4f, d0.denoise_sigma_z), std::max(1.0e-4f, d0.denoise_sigma_l),
-                                       nxt);
+          giDenoiseIter(s, w, h, 1 << it, valid, ne, pd, cur, var, pgrad, d0.denoise_sigma_n,
+                        std::max(1.0e-4f, d0.denoise_sigma_z), std::max(1.0e-4f, d0.denoise_sigma_l), nxt);
           std::swap(cur, nxt);
         }
-        k_gdn_write<<<g, 256, 0, s>>>(n, valid, cur, E);
+        giDenoiseWrite(s, n, valid, cur, E);
         kernels += 2u + uint32_t(iters);
+      }
+      UBR_CUDA(c, cudaGetLastError());
+      return UBR_OK;
+    };
+    // the gather over a grid, with pt2's adaptive refinement (pt2_adaptive.hpp:
+    // mask of noisy points, dilated twice, re-gathered continuing their
+    // sequences, merged as a weighted mean)
+    auto gatherGrid = [&](const GiGrid& gr, float4* E) -> ubr_status {
+      const uint32_t n = uint32_t(gr.W) * uint32_t(gr.H);
+      ubr_status as = UBR_OK;
+      float* halfE = adapt ? scratchT<float>(c, 129, size_t(n) * 3, as) : nullptr;
+      if (as != UBR_OK) return as;
+      GiP g0 = gp;
+      g0.halfE = halfE;
+      giGather(km, s, g0, s1, lt, nL, gr, nullptr, nullptr, n, spp, E);
+      ++kernels;
+      if (adapt) {
+        uint8_t* m0 = scratchT<uint8_t>(c, 130, n, as);
+        uint8_t* m1 = scratchT<uint8_t>(c, 131, n, as);
+        uint32_t* list = scratchT<uint32_t>(c, 132, n, as);
+        uint32_t* cnt = scratchT<uint32_t>(c, 133, 4, as);
+        float4* Er = scratchT<float4>(c, 134, n, as);
+        if (as != UBR_OK) return as;
+        UBR_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(uint32_t), s));
+        giAdaptiveMask(s, gr.W, gr.H, E, halfE, gr.ne, spp, d0.pt2_adaptive_thresh, m0);
+        giDilate(s, gr.W, gr.H, m0, gr.ne, m1);
+        giDilate(s, gr.W, gr.H, m1, gr.ne, m0);
+        giMaskList(s, n, m0, list, cnt);
+        GiP g1 = gp;
+        g1.sampleOffset = spp;
+        giGather(km, s, g1, s1, lt, nL, gr, list, cnt, n, extra, Er);
+        giMerge(s, list, cnt, n, spp, extra, Er, E);
+        kernels += 6;
       }
       UBR_CUDA(c, cudaGetLastError());
       return UBR_OK;
@@ -3145,35 +2685,34 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       float4* Esnap = d0.pt1_edge_patch ? scratchT<float4>(c, 128, npix, gs) : nullptr;
       if (gs != UBR_OK) return gs;
       UBR_CUDA(c, cudaMemsetAsync(patchCount, 0, 2 * sizeof(uint32_t), s));
-      UBR_KM_DISPATCH1(k_pt1_gbuffer, km, (nlo + 127) / 128, 128, s, p1, s1, hw, hh, lpd, lne, lng, gp.stats,
-                       b.stats + 3);
+      giGBuffer(km, s, p1, s1, hw, hh, lpd, lne, lng, gp.stats, b.stats + 3);
+      ++kernels;
       const GiGrid lo{hw, hh, lpd, lne, lng};
       cudaEventRecord(c->giEv[1], s);
-      UBR_KM_DISPATCH1(k_pt1_gather, km, (nlo + 127) / 128, 128, s, gp, s1, lt, p1.nLights, lo, nullptr, nullptr,
-                       nlo, spp, Elo);
-      kernels += 2;
+      gs = gatherGrid(lo, Elo);
+      if (gs != UBR_OK) return gs;
       cudaEventRecord(c->giEv[2], s);
       if (d0.pt1_denoise) {
         gs = denoiseE(hw, hh, Elo, lne, lpd);
         if (gs != UBR_OK) return gs;
       }
       cudaEventRecord(c->giEv[3], s);
-      k_pt1_upsample<<<(npix + 127) / 128, 128, 0, s>>>(
-          p1.W, p1.H, b.giA, b.giB, lo, Elo, d0.pt1_upsample_normal_pow, d0.pt1_upsample_depth_scale,
-          giDiv <= 2 ? 0 : giDiv, d0.pt1_edge_patch ? 1 : 0, d0.pt1_edge_patch_thresh, Ef, patchList, patchCount,
-          gp.stats + 3);
+      giUpsample(s, p1.W, p1.H, b.giA, b.giB, lo, Elo, d0.pt1_upsample_normal_pow, d0.pt1_upsample_depth_scale,
+                 giDiv <= 2 ? 0 : giDiv, d0.pt1_edge_patch ? 1 : 0, d0.pt1_edge_patch_thresh, Ef, patchList,
+                 patchCount, gp.stats + 3);
       ++kernels;
       cudaEventRecord(c->giEv[4], s);
       if (d0.pt1_edge_patch) {
         // re-gather the rim pixels at full resolution with spp x the patch
-        // multiplier, then blend them into the field (radius 2)
+        // multiplier (their own sample layout), then blend them into the
+        // field (radius 2)
         const int pspp = spp * std::max(1, d0.pt1_edge_patch_spp_mul);
-        UBR_KM_DISPATCH1(k_pt1_gather, km, (npix + 127) / 128, 128, s, gp, s1, lt, p1.nLights, full, patchList,
-                         patchCount, npix, pspp, Ef);
+        GiP gpat = gp;
+        gpat.sppPow2 = pow2(uint32_t(pspp));
+        giGather(km, s, gpat, s1, lt, nL, full, patchList, patchCount, npix, pspp, Ef);
         UBR_CUDA(c, cudaMemcpyAsync(Esnap, Ef, size_t(npix) * sizeof(float4), cudaMemcpyDeviceToDevice, s));
-        k_pt1_smooth<<<(npix + 127) / 128, 128, 0, s>>>(p1.W, p1.H, patchList, patchCount, npix, b.giA, b.giB,
-                                                        d0.pt1_upsample_normal_pow, d0.pt1_upsample_depth_scale, 2,
-                                                        Esnap, Ef);
+        giSmooth(s, p1.W, p1.H, patchList, patchCount, npix, b.giA, b.giB, d0.pt1_upsample_normal_pow,
+                 d0.pt1_upsample_depth_scale, 2, Esnap, Ef);
         kernels += 2;
         UBR_CUDA(c, cudaMemcpyAsync(static_cast<char*>(c->pinned) + 256, patchCount, sizeof(uint32_t),
                                     cudaMemcpyDeviceToHost, s));
@@ -3181,9 +2720,8 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       cudaEventRecord(c->giEv[5], s);
     } else {
       cudaEventRecord(c->giEv[1], s);
-      UBR_KM_DISPATCH1(k_pt1_gather, km, (npix + 127) / 128, 128, s, gp, s1, lt, p1.nLights, full, nullptr, nullptr,
-                       npix, spp, Ef);
-      ++kernels;
+      gs = gatherGrid(full, Ef);
+      if (gs != UBR_OK) return gs;
       cudaEventRecord(c->giEv[2], s);
       if (d0.pt1_denoise) {
         gs = denoiseE(p1.W, p1.H, Ef, b.giB, b.giA);
@@ -3193,8 +2731,52 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       cudaEventRecord(c->giEv[4], s);
       cudaEventRecord(c->giEv[5], s);
     }
-    k_pt1_composite<<<(npix + 255) / 256, 256, 0, s>>>(npix, b.giB, b.giR, Ef, d0.gi_intensity, b.colorHi);
+    giComposite(s, npix, b.giB, b.giR, Ef, d0.gi_intensity, b.colorHi);
     ++kernels;
+    // pt2 traced reflection (embree_renderer.cpp:935-1086): the mirror pass,
+    // then the glossy GGX gather with its denoise, after the diffuse composite
+    if (p1.pt2Refl && jobs[0].scene->reflective) {
+      GiP gr = gp;
+      gr.sppPow2 = 1;
+      const GiCam cam{p1.camPos, p1.camDir, p1.ortho};
+      giReflect(km, s, gr, s1, lt, nL, full, b.rfl, cam, npix, b.colorHi);
+      ++kernels;
+      if (p1.pt2Glossy && jobs[0].scene->glossy) {
+        const int gspp = std::max(1, d0.pt2_glossy_spp);
+        float4* Es = scratchT<float4>(c, 135, npix, gs);
+        if (gs != UBR_OK) return gs;
+        giGlossy(km, s, gr, s1, lt, nL, full, b.rfl, cam, npix, gspp, d0.pt1_seed, Es);
+        ++kernels;
+        if (d0.pt1_denoise && d0.pt2_glossy_denoise) {
+          const int ssg = p1.ss;
+          if (ssg <= 1 || p1.W % ssg != 0 || p1.H % ssg != 0) {
+            gs = denoiseE(p1.W, p1.H, Es, b.giB, b.giA);  // render grid = output grid
+            if (gs != UBR_OK) return gs;
+          } else {
+            // denoise at the output grid, then back up over the glossy pixels
+            const int Wo = p1.W / ssg, Ho = p1.H / ssg;
+            const uint32_t no = uint32_t(Wo) * uint32_t(Ho);
+            float4* Eo = scratchT<float4>(c, 136, no, gs);
+            float4* pdo = scratchT<float4>(c, 137, no, gs);
+            float4* neo = scratchT<float4>(c, 138, no, gs);
+            float4* gne = scratchT<float4>(c, 139, npix, gs);
+            uint32_t* dummy = scratchT<uint32_t>(c, 140, 4, gs);
+            if (gs != UBR_OK) return gs;
+            giGlossyDown(s, p1.W, p1.H, ssg, b.rfl, Es, b.giA, b.giB, Eo, pdo, neo);
+            gs = denoiseE(Wo, Ho, Eo, neo, pdo);
+            if (gs != UBR_OK) return gs;
+            giGlossyElig(s, npix, b.rfl, b.giB, gne);
+            const GiGrid go{Wo, Ho, pdo, neo, nullptr};
+            giUpsample(s, p1.W, p1.H, b.giA, gne, go, Eo, d0.pt1_upsample_normal_pow, d0.pt1_upsample_depth_scale, 0,
+                       0, 0.0f, Es, dummy, dummy, gp.stats + 3);
+            kernels += 3;
+          }
+        }
+        giGlossyComposite(s, npix, b.rfl, Es, b.colorHi);
+        ++kernels;
+      }
+    }
+    cudaEventRecord(c->giEv[6], s);
     UBR_CUDA(c, cudaGetLastError());
     return UBR_OK;
   };
@@ -3272,6 +2854,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     st = coarsePrepass();
     if (st != UBR_OK) return st;
     if (giOn) UBR_CUDA(c, cudaMemsetAsync(b.giB, 0, size_t(npix) * sizeof(float4), s));
+    if (b.rfl.amt) UBR_CUDA(c, cudaMemsetAsync(b.rfl.amt, 0, size_t(npix) * sizeof(float4), s));
     st = adaptive ? runAdaptive() : runLayers(p1, b, R, nullptr, npix);
     if (st != UBR_OK) return st;
     if (giOn && !cancelled) {
@@ -3364,10 +2947,10 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     fr.node_bytes[1] = hs[6] * uint64_t(kWideF4 * 16);
     fr.prim_bytes[0] = hs[5];
     fr.prim_bytes[1] = hs[7];
-    for (int k = 0; k < 5; ++k) fr.gi_ms[k] = 0.0;
+    for (int k = 0; k < 6; ++k) fr.gi_ms[k] = 0.0;
     fr.gi_gather_rays = fr.gi_nee_rays = fr.gi_gbuffer_rays = fr.gi_patched_pixels = 0;
     if (giOn && !cancelled) {
-      for (int k = 0; k < 5; ++k) {
+      for (int k = 0; k < 6; ++k) {
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, c->giEv[k], c->giEv[k + 1]);
         fr.gi_ms[k] = ms;

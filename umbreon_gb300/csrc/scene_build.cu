@@ -229,6 +229,156 @@ void flattenCylinders(const ubr_scene_desc& d, const std::vector<f3>& offs, Host
   }
 }
 
+// pt2BuildEmissiveLights (integrator/pt2/pt2_emissive.hpp:104-277): the
+// base mesh triangles whose material emits (corners and colours as the
+// caller gave them, un-offset), then the real emissive spheres and capped
+// cylinders in primID order (instance offset outer, scene order inner) --
+// a sphere as one record, a capped cylinder as its lateral surface and two
+// disk caps -- each weighted by area x luminance(emitted radiance) in one CDF
+// accumulated in double.  Records in the EmitD layout (gi.cuh).
+struct HostEmit {
+  std::vector<float4> rec;
+  std::vector<float> cdf, pdf;
+  std::vector<uint32_t> triIndex, sphereIndex;
+  std::vector<uint4> cylIndex;
+  uint32_t triCount = 0;
+};
+
+void buildEmitters(const ubr_scene_desc& d, const std::vector<f3>& offs, HostEmit& e) {
+  auto lum = [](f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; };
+  const uint64_t nt = d.mesh_vertex_count >= 3 ? d.mesh_triangle_count : 0;
+  auto triMat = [&](uint64_t t) -> const ubr_material& {
+    return d.mesh_tri_material ? d.mesh_materials[d.mesh_tri_material[t]] : d.mesh_material;
+  };
+  bool meshEm = d.mesh_material.emission > 0.0f;
+  for (uint32_t i = 0; i < d.mesh_material_count && d.mesh_materials; ++i)
+    meshEm = meshEm || d.mesh_materials[i].emission > 0.0f;
+  bool csgEm = false;
+  for (uint64_t i = 0; i < d.sphere_count; ++i)
+    csgEm = csgEm || (!(d.sphere_from_edge && d.sphere_from_edge[i]) && d.sphere_material[i].emission > 0.0f &&
+                      d.sphere_center_radius[4 * i + 3] > 0.0f);
+  for (uint64_t i = 0; i < d.cylinder_count; ++i)
+    csgEm = csgEm || (!(d.cyl_from_edge && d.cyl_from_edge[i]) && !(d.cyl_open && d.cyl_open[i]) &&
+                      d.cyl_material[i].emission > 0.0f && d.cyl_radius[i] > 0.0f);
+  if (!(meshEm && nt > 0) && !csgEm) return;
+  std::vector<float> power;
+  if (meshEm && nt > 0) {
+    e.triIndex.assign(nt, 0xFFFFFFFFu);
+    for (uint64_t t = 0; t < nt; ++t) {
+      const ubr_material& mm = triMat(t);
+      if (mm.emission <= 0.0f) continue;
+      uint32_t vi[3];
+      for (int k = 0; k < 3; ++k) vi[k] = d.mesh_index ? d.mesh_index[3 * t + k] : uint32_t(3 * t + k);
+      f3 P[3], Em[3];
+      for (int k = 0; k < 3; ++k) {
+        P[k] = ld3(d.mesh_positions, vi[k]);
+        const float* cc = d.mesh_colors ? d.mesh_colors + 4 * size_t(vi[k]) : nullptr;
+        Em[k] = cc ? f3{mm.emission * cc[0], mm.emission * cc[1], mm.emission * cc[2]} : f3{0.0f, 0.0f, 0.0f};
+      }
+      const f3 a = P[1] - P[0], b = P[2] - P[0];
+      const f3 cr{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+      const float len = std::sqrt(cr.x * cr.x + cr.y * cr.y + cr.z * cr.z);
+      if (len <= 0.0f) continue;
+      const float area = 0.5f * len;
+      const f3 avg{(Em[0].x + Em[1].x + Em[2].x) / 3.0f, (Em[0].y + Em[1].y + Em[2].y) / 3.0f,
+                   (Em[0].z + Em[1].z + Em[2].z) / 3.0f};
+      const float pw = area * lum(avg);
+      if (pw <= 0.0f) continue;
+      e.triIndex[t] = uint32_t(power.size());
+      e.rec.push_back(make_float4(P[0].x, P[0].y, P[0].z, area));
+      e.rec.push_back(make_float4(P[1].x, P[1].y, P[1].z, 0.0f));
+      e.rec.push_back(make_float4(P[2].x, P[2].y, P[2].z, 0.0f));
+      for (int k = 0; k < 3; ++k) e.rec.push_back(make_float4(Em[k].x, Em[k].y, Em[k].z, 0.0f));
+      e.rec.push_back(make_float4(cr.x / len, cr.y / len, cr.z / len, 0.0f));
+      power.push_back(pw);
+    }
+    if (power.empty()) e.triIndex.clear();
+  }
+  e.triCount = uint32_t(power.size());
+  if (csgEm) {
+    const float kPi = 3.14159265358979323846f;
+    auto pushCsg = [&](f3 p0, f3 axis, int kind, f3 Le, float radius, float len, float area) {
+      e.rec.push_back(make_float4(p0.x, p0.y, p0.z, area));
+      e.rec.push_back(make_float4(axis.x, axis.y, axis.z, float(kind)));
+      e.rec.push_back(make_float4(Le.x, Le.y, Le.z, radius));
+      e.rec.push_back(make_float4(len, 0.0f, 0.0f, 0.0f));
+      for (int k = 4; k < kEmitF4; ++k) e.rec.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    };
+    const uint32_t nCsg0 = uint32_t(power.size());
+    e.sphereIndex.assign(d.sphere_count * offs.size(), 0xFFFFFFFFu);
+    uint32_t prim = 0;
+    for (const f3& off : offs)
+      for (uint64_t i = 0; i < d.sphere_count; ++i, ++prim) {
+        const ubr_material& m = d.sphere_material[i];
+        const float r = d.sphere_center_radius[4 * i + 3];
+        if ((d.sphere_from_edge && d.sphere_from_edge[i]) || !(m.emission > 0.0f) || !(r > 0.0f)) continue;
+        const f3 Le{m.emission * d.sphere_color[4 * i], m.emission * d.sphere_color[4 * i + 1],
+                    m.emission * d.sphere_color[4 * i + 2]};
+        const float area = 4.0f * kPi * r * r;
+        const float pw = area * lum(Le);
+        if (!(pw > 0.0f)) continue;
+        e.sphereIndex[prim] = uint32_t(power.size()) - e.triCount;
+        const float* q = d.sphere_center_radius + 4 * i;
+        pushCsg(f3{q[0] + off.x, q[1] + off.y, q[2] + off.z}, f3{0.0f, 0.0f, 1.0f}, 1, Le, r, 0.0f, area);
+        power.push_back(pw);
+      }
+    std::vector<uint32_t> capIdx;
+    for (uint64_t i = 0; i < d.cylinder_count; ++i)
+      if (!(d.cyl_open && d.cyl_open[i])) capIdx.push_back(uint32_t(i));
+    const uint32_t none = 0xFFFFFFFFu;
+    e.cylIndex.assign(capIdx.size() * offs.size(), make_uint4(none, none, none, 0));
+    prim = 0;
+    for (const f3& off : offs)
+      for (uint32_t i : capIdx) {
+        const uint32_t me = prim++;
+        const ubr_material& m = d.cyl_material[i];
+        const float r = d.cyl_radius[i];
+        if ((d.cyl_from_edge && d.cyl_from_edge[i]) || !(m.emission > 0.0f) || !(r > 0.0f)) continue;
+        const f3 p0 = ld3(d.cyl_p0, i) + off, p1 = ld3(d.cyl_p1, i) + off;
+        const f3 dd = p1 - p0;
+        const float len = std::sqrt(dd.x * dd.x + dd.y * dd.y + dd.z * dd.z);
+        if (!(len > 0.0f)) continue;
+        const f3 axis{dd.x / len, dd.y / len, dd.z / len};
+        const f3 Le{m.emission * d.cyl_color[4 * i], m.emission * d.cyl_color[4 * i + 1],
+                    m.emission * d.cyl_color[4 * i + 2]};
+        const float l = lum(Le);
+        uint4& ref = e.cylIndex[me];
+        const float aSide = 2.0f * kPi * r * len;
+        if (aSide * l > 0.0f) {
+          ref.x = uint32_t(power.size()) - e.triCount;
+          pushCsg(p0, axis, 2, Le, r, len, aSide);
+          power.push_back(aSide * l);
+        }
+        const float aCap = kPi * r * r;
+        if (aCap * l > 0.0f) {
+          ref.y = uint32_t(power.size()) - e.triCount;
+          pushCsg(p0, axis, 3, Le, r, 0.0f, aCap);
+          power.push_back(aCap * l);
+          ref.z = uint32_t(power.size()) - e.triCount;
+          pushCsg(p1, axis, 3, Le, r, 0.0f, aCap);
+          power.push_back(aCap * l);
+        }
+      }
+    if (uint32_t(power.size()) == nCsg0) {
+      e.sphereIndex.clear();
+      e.cylIndex.clear();
+    }
+  }
+  if (power.empty()) {
+    e = HostEmit{};
+    return;
+  }
+  double total = 0.0;
+  for (float pw : power) total += pw;
+  double acc = 0.0;
+  for (float pw : power) {
+    acc += pw;
+    e.cdf.push_back(float(acc / total));
+    e.pdf.push_back(float(pw / total));
+  }
+  e.cdf.back() = 1.0f;
+}
+
 ubr_status validate(Context* c, const ubr_scene_desc& d) {
   if (d.abi_version != UBR_ABI_VERSION) return setError(c, UBR_INVALID_ARGUMENT, "scene desc: abi_version mismatch");
   if (d.mesh_triangle_count > 0 && d.mesh_vertex_count >= 3 && !d.mesh_positions)
@@ -1198,6 +1348,41 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   if ((st = upload(c, sc, hs.ccV, &dccV)) != UBR_OK) return fail(st);
   if ((st = upload(c, sc, hs.ccIdx, &dccIdx)) != UBR_OK) return fail(st);
   if ((st = upload(c, sc, hs.mats, &v.mats)) != UBR_OK) return fail(st);
+  {
+    // pt2: reflection ownership flags (hit_shader.hpp:243-270) and the
+    // emissive primitives sampled as lights
+    for (const ubr_material& m : hs.mats) {
+      if (m.model == 1u) {
+        if (m.pbr_metallic > 1e-4f || m.pbr_specular > 1e-4f) {
+          sc->reflective = true;
+          sc->glossy = sc->glossy || m.pbr_roughness * m.pbr_roughness >= 0.015f;
+        }
+        if (m.pbr_anisotropy != 0.0f) sc->anisoPrincipled = true;
+      } else if (m.reflection > 0.0f) {
+        sc->reflective = true;
+        sc->glossy = sc->glossy || m.specular > 0.0f;
+      }
+    }
+    std::vector<f3> offs;
+    for (uint64_t i = 0; i < d.instance_count; ++i) offs.push_back(ld3(d.instance_offsets, i));
+    if (offs.empty()) offs.push_back(f3{0, 0, 0});
+    HostEmit he;
+    buildEmitters(d, offs, he);
+    EmitD& em = sc->emit;
+    em.n = uint32_t(he.cdf.size());
+    em.triCount = he.triCount;
+    em.nTriIndex = uint32_t(he.triIndex.size());
+    em.nSphereIndex = uint32_t(he.sphereIndex.size());
+    em.nCylIndex = uint32_t(he.cylIndex.size());
+    if (em.n > 0) {
+      if ((st = upload(c, sc, he.cdf, &em.cdf)) != UBR_OK) return fail(st);
+      if ((st = upload(c, sc, he.pdf, &em.pdfChoose)) != UBR_OK) return fail(st);
+      if ((st = upload(c, sc, he.rec, &em.rec)) != UBR_OK) return fail(st);
+      if ((st = upload(c, sc, he.triIndex, &em.triIndex)) != UBR_OK) return fail(st);
+      if ((st = upload(c, sc, he.sphereIndex, &em.sphereIndex)) != UBR_OK) return fail(st);
+      if ((st = upload(c, sc, he.cylIndex, &em.cylIndex)) != UBR_OK) return fail(st);
+    }
+  }
   for (int k = 1; k < 4; ++k) {
     if ((st = upload(c, sc, hs.color[k], &v.primColor[k])) != UBR_OK) return fail(st);
     if ((st = upload(c, sc, hs.mat[k], &v.primMat[k])) != UBR_OK) return fail(st);

@@ -622,5 +622,27 @@ UBR_D float aoMultibounce(float ao, float albedo) {
   return fmaxf(ao, ((ao * a + bb) * ao + c) * ao);
 }
 
+// Material::toonLike / diffuseWeight (scene.hpp:171-196).
+UBR_D bool toonLike(const ubr_material& m) {
+  if (m.model == 2u) return true;
+  if (m.model != 0u) return false;
+  if (m.specular > 1.0f || m.phong > 1.0f || m.brilliance == 0.0f) return true;
+  return m.diffuse <= 0.0f && m.specular <= 0.0f && m.phong <= 0.0f && m.reflection <= 0.0f;
+}
+UBR_D float diffuseWeight(const ubr_material& m) { return m.model == 1u ? m.diffuse * (1.0f - m.pbr_metallic) : m.diffuse; }
+
+// 32-bit integer hash (irradiance_cache.hpp:176-184): seeds the gather's
+// per-pixel stream and the bounce vertices' shadow streams.
+UBR_HD uint32_t hashU32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7FEB352Du;
+  x ^= x >> 15;
+  x *= 0x846CA68Bu;
+  x ^= x >> 16;
+  return x;
+}
+
+UBR_D float lumOf(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+
 }  // namespace
 }  // namespace ubr

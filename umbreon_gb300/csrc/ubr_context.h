@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "gi.cuh"
 #include "ubr_internal.h"
 
 namespace ubr {
@@ -41,7 +42,7 @@ struct Context {
   std::vector<void*> sceneHandles;      // live ubr_scene handles built on this context
   cudaMemPool_t pool = nullptr;         // stream-ordered device allocations (scenes, scratch)
   void* noallocArray = nullptr;         // device address of the allocation-free query's fixed array
-  cudaEvent_t giEv[6] = {};             // GI pass stage boundaries, created on first use
+  cudaEvent_t giEv[7] = {};             // GI pass stage boundaries, created on first use
 };
 
 struct Scene {
@@ -53,6 +54,12 @@ struct Scene {
   bool opaque = true;        // every primitive fully opaque: frames are one layer deep
   bool aoReceivers = false;  // a mesh or a non-outline primitive exists (coarse AO grid eligible)
   bool principled = false;   // some material uses the principled model
+  // pt2 GI: a first hit can own a traced reflection (POV reflection > 0, or a
+  // principled specular lobe); some can be glossy (a highlight-bearing POV
+  // finish, or principled roughness^2 >= 0.015); an anisotropic principled
+  // sphere / cylinder exists; the emissive primitives sampled as lights
+  bool reflective = false, glossy = false, anisoPrincipled = false;
+  EmitD emit;
   uint64_t deviceBytes = 0;
   double buildMs = 0.0;
   double flattenMs = 0.0;    // host: validation, primID ordering, chaining, material table

@@ -476,6 +476,8 @@ struct Params {
   int lightOff;         // first light of this frame in the lights array
   int gi;               // pt1 GI: eligible hits drop their ambient; first hits captured for the gather
   float giIntensity;
+  int pt2Refl;          // pt2 traced reflection owns the reflection term (first hits recorded)
+  int pt2Glossy;        // ... with GGX lobes for reflective finishes that carry a highlight
 };
 
 }  // namespace ubr

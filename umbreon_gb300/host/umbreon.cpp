@@ -531,7 +531,7 @@ FrameResult renderFrameGpu(const Scene& scene, const RenderOptions& opt, RenderP
   f.pt1Timing.primary = f.renderSeconds;
   if (opt.gi) {
     // embree_renderer.cpp:859-1123: the GI pass's split and ray counts
-    f.pt1Timing.gather = (fr.gi_ms[0] + fr.gi_ms[1] + fr.gi_ms[4]) / 1e3;
+    f.pt1Timing.gather = (fr.gi_ms[0] + fr.gi_ms[1] + fr.gi_ms[4] + fr.gi_ms[5]) / 1e3;
     f.pt1Timing.denoise = fr.gi_ms[2] / 1e3;
     f.pt1Timing.upsample = fr.gi_ms[3] / 1e3;
     f.pt1Rays.gatherRays = fr.gi_gather_rays;
