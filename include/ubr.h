@@ -398,7 +398,9 @@ typedef struct ubr_context_desc {
   uint32_t bvh_leaf_max;
   /* occlusion-ray kernel (0 = library default): 1 = one thread per ray,
    * 2 = persistent warps that refill idle lanes with new rays, 3 = resident
-   * grid striding over the rays with the top BVH levels in shared memory */
+   * grid striding over the rays with the top BVH levels in shared memory,
+   * 4 = one thread per ray with node visits and primitive tests interleaved
+   * one per step */
   uint32_t trace_mode;
   /* 1 = launch every kernel on its own instead of replaying single-layer
    * frames from a captured CUDA graph (0 = graphs, the default) */

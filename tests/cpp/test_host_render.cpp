@@ -220,6 +220,10 @@ int main() {
     c("pt1 defaults: frame rendered", f.color.size() == 100 && f.color[kC] > 0.0f);
     c("pt1 defaults: gather rays counted", f.pt1Rays.gatherRays > 0 && f.pt1Rays.gbufferRays > 0);
     c("pt1 defaults: a-trous denoise of E reported", f.pt1DenoiserUsed == 1);
+    o.giIntegrator = 2;  // the reference's default integrator, every option at its default
+    const umbreon::FrameResult f2 = umbreon::render(sc, o);
+    c("pt2 defaults: frame rendered", f2.color.size() == 100 && f2.color[kC] > 0.0f);
+    c("pt2 defaults: gather rays counted", f2.pt1Rays.gatherRays > 0);
     o.giIntegrator = 0;
     bool threw = false;
     try {

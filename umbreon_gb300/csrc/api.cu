@@ -135,7 +135,7 @@ ubr_status ubr_context_create(ubr_context** out, const ubr_context_desc* desc) {
     x.leafMax = int(desc->bvh_leaf_max);
   }
   if (desc && desc->trace_mode) {
-    if (desc->trace_mode > 3) {
+    if (desc->trace_mode > 4) {
       delete c;
       return UBR_INVALID_ARGUMENT;
     }

@@ -368,11 +368,9 @@ UBR_D void occRayOf(uint64_t rid, uint32_t nq, uint64_t R, uint64_t A, uint32_t&
   }
 }
 
-// One thread per AO / shadow ray.  Mesh scenes run 9 blocks per SM (56
-// registers), the others 8 (64 registers): measured best for each.
-template <bool COUNT, int KM, bool BATCH>
-__global__ void __launch_bounds__(128, (KM & kMaskMesh) ? 9 : 8)
-    k_trace_occlusion(Params p1, DScene s1, Batch bt, Bufs b, uint32_t n) {
+// The occlusion kernel's body: one thread per AO / shadow ray.
+template <bool COUNT, int KM, bool BATCH, bool IL>
+__device__ __forceinline__ void occlusionBody(const Params& p1, const DScene& s1, const Batch& bt, const Bufs& b) {
   Count cnt;
   const uint64_t tid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t R = BATCH ? uint64_t(bt.R) : uint64_t(p1.raysPerHit);
@@ -403,8 +401,12 @@ __global__ void __launch_bounds__(128, (KM & kMaskMesh) ? 9 : 8)
       h.t = kInfF;
       if (o.trace) {
         const TravScene ts = travOf(s);
-        hit = (p.aoEnhanced || p.aoWriteAov) ? traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit, o.start)
-                           : traverse<COUNT, KM, true>(ts, o.r, h, ovf, &cnt, true, o.start);
+        if (p.aoEnhanced || p.aoWriteAov)
+          hit = traverse<COUNT, KM, false>(ts, o.r, h, ovf, &cnt, o.anyHit, o.start);
+        else if (IL)
+          hit = traverseAnyInterleaved<COUNT, KM>(ts, o.r, ovf, &cnt, o.start);
+        else
+          hit = traverse<COUNT, KM, true>(ts, o.r, h, ovf, &cnt, true, o.start);
         traced = 1;
       }
       occlusionWrite(p, b, R, aoStride, slot, j, o, hit, h.t);
@@ -416,6 +418,22 @@ __global__ void __launch_bounds__(128, (KM & kMaskMesh) ? 9 : 8)
     warpCount(&b.stats[6], cnt.nodes);
     warpCount(&b.stats[7], cnt.primBytes);
   }
+}
+
+// One thread per AO / shadow ray.  Mesh scenes run 9 blocks per SM (56
+// registers), the others 8 (64 registers): measured best for each.
+template <bool COUNT, int KM, bool BATCH>
+__global__ void __launch_bounds__(128, (KM & kMaskMesh) ? 9 : 8)
+    k_trace_occlusion(Params p1, DScene s1, Batch bt, Bufs b, uint32_t n) {
+  occlusionBody<COUNT, KM, BATCH, false>(p1, s1, bt, b);
+}
+
+// The same with node visits and primitive tests interleaved one per step
+// (traverseAnyInterleaved) for the binary-visibility rays.
+template <bool COUNT, int KM, bool BATCH>
+__global__ void __launch_bounds__(128, (KM & kMaskMesh) ? 9 : 8)
+    k_trace_occlusion_il(Params p1, DScene s1, Batch bt, Bufs b, uint32_t n) {
+  occlusionBody<COUNT, KM, BATCH, true>(p1, s1, bt, b);
 }
 
 // Resident-grid variant: each CTA stages the top wide nodes (root and the two
@@ -1979,8 +1997,9 @@ void launchClosest(int km, bool count, bool batch, uint32_t grid, int tb, cudaSt
 }
 
 void launchOcclusion(int km, bool count, bool batch, uint32_t grid, int tb, cudaStream_t st, const Params& p,
-                     const DScene& s, const Batch& bt, const Bufs& b, uint32_t n) {
-  UBR_KM_DISPATCH(k_trace_occlusion, km, count, batch, grid, tb, st, p, s, bt, b, n);
+                     const DScene& s, const Batch& bt, const Bufs& b, uint32_t n, bool il = false) {
+  if (il) UBR_KM_DISPATCH(k_trace_occlusion_il, km, count, batch, grid, tb, st, p, s, bt, b, n);
+  else UBR_KM_DISPATCH(k_trace_occlusion, km, count, batch, grid, tb, st, p, s, bt, b, n);
 }
 
 // Resident grid of the persistent occlusion kernel: SMs x resident blocks.
@@ -2262,7 +2281,8 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       // own (the tea2 stream does not depend on the sample count; the
       // low-discrepancy set does): copy them instead of tracing, for single
       // layer frames and the per-ray occlusion kernel
-      if (p1.aoSamples > 0 && !p1.aoLowDiscrepancy && !coarseOn && singleLayer && c->traceMode == 1) {
+      if (p1.aoSamples > 0 && !p1.aoLowDiscrepancy && !coarseOn && singleLayer &&
+          (c->traceMode == 1 || c->traceMode == 4)) {
         pBoost.reuseAo = p1.aoSamples;
         reuseOccBuf = scratchT<uint8_t>(c, 105, size_t(nCentre) * R, st);
         if (p1.aoEnhanced || p1.aoWriteAov) reuseAoTBuf = scratchT<float>(c, 106, size_t(nCentre) * p1.aoSamples, st);
@@ -2351,8 +2371,9 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       mark(1, false);
       const uint64_t nr = uint64_t(n) * uint64_t(Rr);
       mark(2, true);
-      if (c->traceMode == 1) {
-        launchOcclusion(km, count, batch, uint32_t((nr + TB - 1) / TB), TB, s, pr, s1, bt, br, n);
+      if (c->traceMode == 1 || c->traceMode == 4) {
+        launchOcclusion(km, count, batch, uint32_t((nr + TB - 1) / TB), TB, s, pr, s1, bt, br, n,
+                        c->traceMode == 4);
       } else if (c->traceMode == 3) {
         launchOcclusionGridStride(km, count, batch, gridStrideGrid(c->device), TB, s, pr, s1, bt, br);
       } else {
@@ -2381,8 +2402,9 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     mark(1, false);
     const uint64_t nr = uint64_t(nCell) * uint64_t(pCoarse.raysPerHit);
     mark(2, true);
-    if (c->traceMode == 1) {
-      launchOcclusion(km, count, false, uint32_t((nr + TB - 1) / TB), TB, s, pCoarse, s1, bt, b, nCell);
+    if (c->traceMode == 1 || c->traceMode == 4) {
+      launchOcclusion(km, count, false, uint32_t((nr + TB - 1) / TB), TB, s, pCoarse, s1, bt, b, nCell,
+                      c->traceMode == 4);
     } else if (c->traceMode == 3) {
       launchOcclusionGridStride(km, count, false, gridStrideGrid(c->device), TB, s, pCoarse, s1, bt, b);
     } else {

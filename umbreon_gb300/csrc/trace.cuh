@@ -395,6 +395,129 @@ __device__ bool traverse(const TravScene& s, const Ray& r, Hit& best, uint32_t& 
   return best.ref != kInvalid;
 }
 
+// Any-hit traversal that interleaves node visits and primitive tests one at
+// a time (the "if-if" loop of Aila and Laine, "Understanding the Efficiency of
+// Ray Traversal on GPUs", HPG 2009): each iteration a lane either tests ONE
+// pending primitive of the leaves it found, or, with none pending, visits one
+// node.  A lane with several primitives to test no longer holds the whole
+// warp in a leaf loop while the other lanes wait; they make node steps in the
+// same iterations.  Same node slab test, visiting order and primitive tests
+// as travStep, so the answer is the same.
+template <bool COUNT, int KM>
+__device__ bool traverseAnyInterleaved(const TravScene& s, const Ray& r, uint32_t& overflow, Count* cnt,
+                                       int start) {
+  if (s.primCount == 0 || start < 0) return false;
+  const f3 inv = safeInv(r.dir);
+  TriPre pre;
+  if (KM & kMaskMesh) pre = triPre(r.dir);
+  int node = start, sp = 0, pendBase = 0;
+  uint32_t pendMask = 0, steps = 0;
+  uint32_t stack[kStackDepth];
+  const bool nx = inv.x < 0.0f, ny = inv.y < 0.0f, nz = inv.z < 0.0f;
+  const f2x bias2 = pk2(-8388608.0f, -8388608.0f), grow2 = pk2(kSlabGrow, kSlabGrow);
+  for (;;) {
+    if (pendMask) {
+      const int q = __ffs(pendMask) - 1;
+      pendMask &= pendMask - 1u;
+      Hit h;
+      uint32_t ref;
+      const bool hit = testLeaf<KM, false>(s, pendBase + q, r, pre, r.tnear, r.tfar, h, ref);
+      if (COUNT) cnt->primBytes += leafBytes(refKind(ref));
+      if (hit) return true;
+      continue;
+    }
+    if (node < 0) return false;
+    if (++steps > s.primCount + 16u) {
+      ++overflow;
+      return false;
+    }
+    if (COUNT) ++cnt->nodes;
+    const float4* nd = s.wnodes + kWideF4 * node;
+    const float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3), n4 = __ldg(nd + 4);
+    const uint32_t hdr = __float_as_uint(n0.w);
+    const float sx = __uint_as_float((hdr & 0xFFu) << 23) * inv.x;
+    const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * inv.y;
+    const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23) * inv.z;
+    const int nInt = int((hdr >> 24) & 0xFu), nCh = int(hdr >> 28);
+    const float ox = (n0.x - r.org.x) * inv.x, oy = (n0.y - r.org.y) * inv.y, oz = (n0.z - r.org.z) * inv.z;
+    const uint32_t childBase = __float_as_uint(n1.x);
+    const int primBase = __float_as_int(n1.y);
+    const uint32_t meta0 = __float_as_uint(n1.z), meta1 = __float_as_uint(n1.w);
+    const uint32_t qnx[2] = {nx ? __float_as_uint(n3.z) : __float_as_uint(n2.x),
+                             nx ? __float_as_uint(n3.w) : __float_as_uint(n2.y)};
+    const uint32_t qfx[2] = {nx ? __float_as_uint(n2.x) : __float_as_uint(n3.z),
+                             nx ? __float_as_uint(n2.y) : __float_as_uint(n3.w)};
+    const uint32_t qny[2] = {ny ? __float_as_uint(n4.x) : __float_as_uint(n2.z),
+                             ny ? __float_as_uint(n4.y) : __float_as_uint(n2.w)};
+    const uint32_t qfy[2] = {ny ? __float_as_uint(n2.z) : __float_as_uint(n4.x),
+                             ny ? __float_as_uint(n2.w) : __float_as_uint(n4.y)};
+    const uint32_t qnz[2] = {nz ? __float_as_uint(n4.z) : __float_as_uint(n3.x),
+                             nz ? __float_as_uint(n4.w) : __float_as_uint(n3.y)};
+    const uint32_t qfz[2] = {nz ? __float_as_uint(n3.x) : __float_as_uint(n4.z),
+                             nz ? __float_as_uint(n3.y) : __float_as_uint(n4.w)};
+    const f2x sx2 = pk2(sx, sx), sy2 = pk2(sy, sy), sz2 = pk2(sz, sz);
+    const f2x ox2 = pk2(ox, ox), oy2 = pk2(oy, oy), oz2 = pk2(oz, oz);
+    float tminP[8], tmaxP[8];
+#pragma unroll
+    for (int k = 0; k < 8; k += 2) {
+      const int w = k >> 2, b = k & 3;
+      float tnx[2], tfx[2], tny[2], tfy[2], tnz[2], tfz[2];
+      up2(fma2(bytePairToFloat2(qnx[w], b, bias2), sx2, ox2), tnx[0], tnx[1]);
+      up2(fma2(bytePairToFloat2(qfx[w], b, bias2), sx2, ox2), tfx[0], tfx[1]);
+      up2(fma2(bytePairToFloat2(qny[w], b, bias2), sy2, oy2), tny[0], tny[1]);
+      up2(fma2(bytePairToFloat2(qfy[w], b, bias2), sy2, oy2), tfy[0], tfy[1]);
+      up2(fma2(bytePairToFloat2(qnz[w], b, bias2), sz2, oz2), tnz[0], tnz[1]);
+      up2(fma2(bytePairToFloat2(qfz[w], b, bias2), sz2, oz2), tfz[0], tfz[1]);
+      float tmx[2];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        tminP[k + j] = fmaxf(fmaxf(tnx[j], tny[j]), fmaxf(tnz[j], r.tnear));
+        tmx[j] = fminf(fminf(tfx[j], tfy[j]), fminf(tfz[j], r.tfar));
+      }
+      up2(mul2(pk2(tmx[0], tmx[1]), grow2), tmaxP[k], tmaxP[k + 1]);
+    }
+    uint32_t hitMask = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) hitMask |= tminP[k] <= tmaxP[k] ? (1u << k) : 0u;
+    hitMask &= (1u << nCh) - 1u;
+    const uint32_t hitInt = hitMask & ((1u << nInt) - 1u);
+    uint32_t primMask = 0;
+    for (uint32_t leafHit = hitMask & ~hitInt; leafHit; leafHit &= leafHit - 1u) {
+      const int k = __ffs(leafHit) - 1;
+      const uint32_t m = __byte_perm(k < 4 ? meta0 : meta1, 0u, 0x4440u | uint32_t(k & 3));
+      primMask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+    }
+    pendBase = primBase;
+    pendMask = primMask;
+    float nearT = kInfF;
+    int nearK = -1;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const bool nearer = ((hitInt >> k) & 1u) && tminP[k] < nearT;
+      nearT = nearer ? tminP[k] : nearT;
+      nearK = nearer ? k : nearK;
+    }
+    if (nearK >= 0) {
+      const uint32_t rest = hitInt & ~(1u << nearK);
+      if (rest) {
+        if (sp < kStackDepth) stack[sp++] = (childBase << 8) | rest;
+        else ++overflow;
+      }
+      node = int(childBase) + nearK;
+    } else if (sp == 0) {
+      node = -1;
+    } else {
+      const uint32_t g = stack[sp - 1];
+      const uint32_t mask = g & 0xFFu;
+      const int k = __ffs(mask) - 1;
+      const uint32_t left = mask & (mask - 1u);
+      if (left) stack[sp - 1] = (g & ~0xFFu) | left;
+      else --sp;
+      node = int(g >> 8) + k;
+    }
+  }
+}
+
 // Start node for rays that stay inside the box [lo, hi] (AO rays: origin
 // +- the AO distance): descend from the root while exactly one child's
 // quantised box overlaps the box.  Every sibling passed over is disjoint
