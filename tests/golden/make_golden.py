@@ -6,12 +6,11 @@ golden_cases.py.
 For each case: tests/golden/<case>.npz with the output colour (float32 RGBA
 at the final size) and the first-hit geomID / primID planes (uint32 at the
 supersampled size), and one entry in tests/golden/golden.json with the input
-digest, the sizes and the platform that made it.  The reference renderer
-itself cannot be built in this environment (it needs Embree 4 and oneTBB),
-so these frames come from the oracle, whose own pins are the reference's
-known-answer tests (tests/kat_cases.py); the fixtures freeze the oracle's
-output so the GPU tests compare against committed frames and a drift of the
-oracle shows up as a failed CPU test.
+digest, the sizes and the platform that made it.  The frames come from the
+oracle; tests/test_ref_pin.py checks that they are bit for bit the frames
+the reference's own render path produces (compiled against the oracle's
+Embree / oneTBB stand-ins by oracle/build_ref.py), so the GPU tests compare
+against the reference's output.
 """
 import json
 import platform

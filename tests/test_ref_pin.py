@@ -104,3 +104,21 @@ def test_restatement_equals_the_reference_bit_for_bit(ref_build, oracle_lib, nam
     color, depth, vz, _ = ref_build.render(sc, opt)
     assert np.array_equal(o.color, color), float(np.abs(o.color - color).max())
     assert np.array_equal(o.depth, depth)
+
+
+def test_committed_golden_frames_are_the_references(ref_build):
+    """tests/golden's committed frames (the GPU tests' fixtures) are exactly
+    what the reference's own code renders for those inputs."""
+    import json
+    import golden_cases
+    manifest = json.loads((ROOT / "tests" / "golden" / "golden.json").read_text())
+    checked = 0
+    for name, (make, _) in golden_cases.CASES.items():
+        sc, opt = make()
+        if golden_cases.digest(sc, opt) != manifest[name]["digest"]:
+            continue  # this platform's scene generator differs: the fixture is not for these inputs
+        color, _, _, _ = ref_build.render(sc, opt)
+        committed = np.load(ROOT / "tests" / "golden" / f"{name}.npz")["color"]
+        assert np.array_equal(color, committed), name
+        checked += 1
+    assert checked > 0
