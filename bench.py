@@ -528,6 +528,19 @@ def secondary_workloads(args, flush):
             wall = min(r[0] for r in runs)
             entry[mode] = {"ms_per_batch": round(wall * 1e3, 3), "frames_per_s": round(len(its) / wall, 1),
                            "Mrays_s": round(runs[0][1] / wall / 1e6, 1)}
+            if mode == "per_frame_no_graph":
+                # the ceiling of batching: every frame's rays at the ray rate
+                # the largest frame of its scene reaches alone (a launch that
+                # fills the GPU), i.e. no launch gaps, no tails, no idle SMs
+                dev = [(frames[i].total_ms, frames[i].rays_primary + frames[i].rays_occlusion, si, o.width)
+                       for i, (si, sc2, o) in enumerate(its)]
+                rate = {}
+                for ms_f, r_f, si, wdt in sorted(dev, key=lambda t: t[3]):
+                    rate[si] = r_f / ms_f  # the largest frame of each scene wins
+                ideal_ms = sum(r_f / rate[si] for _, r_f, si, _ in dev)
+                entry["device_ms_sum_per_frame_path"] = round(sum(d[0] for d in dev), 3)
+                entry["ideal_ms_at_full_occupancy"] = round(ideal_ms, 3)
+                entry["batching_ceiling_over_per_frame"] = round(wall * 1e3 / ideal_ms, 3)
             for bb in built:
                 bb.release()
             cx.close()

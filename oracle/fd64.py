@@ -41,6 +41,7 @@ class Fd64Desc(C.Structure):
         ("gamma", C.c_double), ("specular_scale", C.c_double),
         ("mat", C.c_double * 9),
         ("metallic", C.c_int32), ("pad", C.c_int32),
+        ("seed_x0", C.c_int32), ("seed_y0", C.c_int32), ("seed_w", C.c_int32), ("pad2", C.c_int32),
     ]
 
 
@@ -63,9 +64,13 @@ _MAT = {name: k for k, name in enumerate(abi.MATERIAL_GRAD_FIELDS)}
 class Fd64Frame:
     """The frame of (scene, opt) in double; spheres only, one shared material."""
 
-    def __init__(self, scene: Scene, opt: RenderOptions, threads: int | None = None):
+    def __init__(self, scene: Scene, opt: RenderOptions, threads: int | None = None, seed_window=None):
+        """seed_window = (x0, y0, W): the frame is the window at (x0, y0) of a
+        W-wide frame, whose pixel coordinates seed the sample streams."""
         rd, _ = make_render_desc(scene, opt)
         d = Fd64Desc()
+        if seed_window is not None:
+            d.seed_x0, d.seed_y0, d.seed_w = seed_window
         d.width, d.height, d.ss = opt.width, opt.height, max(1, opt.supersample)
         d.ortho = int(rd.cam_orthographic)
         for k in range(3):

@@ -82,6 +82,10 @@ struct fd64_desc {
   double gamma, specular_scale;
   double mat[9];  // ambient diffuse specular roughness brilliance phong phong_size reflection emission
   int32_t metallic, pad;
+  // the frame is a window of a larger frame: the per-pixel sample streams are
+  // seeded with the window's pixels' coordinates in that frame (seed_w wide;
+  // 0 = this frame is the whole frame)
+  int32_t seed_x0, seed_y0, seed_w, pad2;
 };
 
 // Visibility record entries per hi-res sample.
@@ -241,10 +245,11 @@ void renderRows(const fd64_desc& d, const double* sph, const double* col, uint64
           radius[0] = R;
           weight[0] = 1.0;
         }
-        const uint32_t base = uint32_t(px) + uint32_t(py) * uint32_t(W);
+        const uint32_t sx = uint32_t(px + d.seed_x0), sy = uint32_t(py + d.seed_y0);
+        const uint32_t base = sx + sy * uint32_t(d.seed_w > 0 ? d.seed_w : W);
         float cpx = 0.0f, cpy = 0.0f;
         if (d.ao_enhanced && d.ao_low_discrepancy) {
-          uint32_t c0 = uint32_t(px) + 1u, c1 = uint32_t(py) + 1u;
+          uint32_t c0 = sx + 1u, c1 = sy + 1u;
           tea2(c0, c1);
           cpx = u32ToUnorm(c0);
           cpy = u32ToUnorm(c1);

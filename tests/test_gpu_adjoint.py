@@ -163,3 +163,104 @@ def test_adjoint_rejects_unsupported(ctx):
     with pytest.raises(abi.UbrError):
         ctx.adjoint(built, sc, opt, np.zeros((32, 32, 4), np.float32))
     built.release()
+
+
+def _crop(sc, opt, x0, y0, w, keep):
+    """The w x w window at (x0, y0) of an orthographic frame as its own
+    frame (same rays up to rounding: the camera moved to the window centre,
+    its height scaled), over the spheres `keep`."""
+    import copy
+    from umbreon_gb300.api import Camera
+    c = copy.deepcopy(sc)
+    o = copy.deepcopy(opt)
+    cam = sc.camera
+    D = np.asarray(cam.direction, np.float64)
+    D /= np.linalg.norm(D)
+    right = np.cross(D, cam.up)
+    right /= np.linalg.norm(right)
+    up = np.cross(right, D)
+    W, H = opt.width, opt.height
+    halfH = 0.5 * cam.height
+    halfW = halfH * W / H
+    pos = (np.asarray(cam.position, np.float64) + right * halfW * (2 * x0 + w - W) / W +
+           up * halfH * (H - 2 * y0 - w) / H)
+    c.camera = Camera(position=tuple(float(v) for v in pos), direction=cam.direction, up=cam.up,
+                      orthographic=True, height=float(cam.height * w / H))
+    c.sphere_center_radius = np.ascontiguousarray(sc.sphere_center_radius[keep])
+    c.sphere_color = np.ascontiguousarray(sc.sphere_color[keep])
+    c.sphere_material = np.ascontiguousarray(np.asarray(sc.sphere_material)[keep])
+    o.width = o.height = w
+    return c, o
+
+
+def _window_spheres(sc, lights, opt, x0, y0, w, margin):
+    """Spheres that a primary, AO or shadow ray of the window's pixels can
+    meet: inside the window's column (inflated by the AO reach), or in the
+    column swept back along a light toward the window (shadow rays)."""
+    cam = sc.camera
+    cr = sc.sphere_center_radius.astype(np.float64)
+    W, H = opt.width, opt.height
+    halfH = 0.5 * cam.height
+    halfW = halfH * W / H
+    px, py = cam.position[0], cam.position[1]
+    xa, xb = px + halfW * (2 * x0 - W) / W, px + halfW * (2 * (x0 + w) - W) / W
+    yb, ya = py + halfH * (1 - 2 * y0 / H), py + halfH * (1 - 2 * (y0 + w) / H)
+    reach = cr[:, 3] + opt.aoDistance * 1.3 + margin
+    keep = (cr[:, 0] > xa - reach) & (cr[:, 0] < xb + reach) & (cr[:, 1] > ya - reach) & (cr[:, 1] < yb + reach)
+    zlo = cr[:, 2].min() - 2.0
+    for L in lights:
+        d = -np.asarray(L.direction, np.float64)
+        d /= np.linalg.norm(d)  # toward the light
+        tmax = np.maximum(0.0, (cr[:, 2] - zlo) / max(d[2], 1e-6))
+        for f in np.linspace(0.0, 1.0, 64):
+            t = tmax * f
+            x, y = cr[:, 0] - t * d[0], cr[:, 1] - t * d[1]
+            r = cr[:, 3] + margin + tmax / 64 * np.hypot(d[0], d[1])
+            keep |= (x > xa - r) & (x < xb + r) & (y > ya - r) & (y < yb + r)
+    return np.flatnonzero(keep)
+
+
+def test_adjoint_benchmark_scene_window(ctx):
+    """The benchmarked configuration itself (100,000 spheres, 1024^2, enhanced
+    AO 16, one shadowed light, fog): the GPU adjoint of the whole frame with
+    the loss on a 32 x 32 window, against FP64 central differences of that
+    window (its own frame over the spheres its rays can meet), for every
+    global parameter and a dozen spheres."""
+    from oracle import fd64
+    sc, opt = scenes.differentiable()
+    tsc, topt = scenes.differentiable_target(sc, opt)
+    x0 = y0 = 496
+    w = 32
+    keep = _window_spheres(sc, sc.lights + tsc.lights, opt, x0, y0, w, margin=0.2)
+    assert 0 < len(keep) < sc.sphere_count()
+    csc, copt = _crop(sc, opt, x0, y0, w, keep)
+    ctsc, ctopt = _crop(tsc, topt, x0, y0, w, keep)
+    seeds = (x0, y0, opt.width)  # the window's pixels seed the full frame's sample streams
+    target = fd64.Fd64Frame(ctsc, ctopt, seed_window=seeds).record()
+    f = fd64.Fd64Frame(csc, copt, seed_window=seeds)
+    img = f.record()
+    wt = fd64.interior_mask(f.primary_ids()).astype(np.float64)
+    d_color = np.zeros((opt.height, opt.width, 4), np.float32)
+    d_color[y0:y0 + w, x0:x0 + w, :3] = (2.0 * wt[..., None] * (img[..., :3] - target[..., :3])).astype(np.float32)
+    built = ctx.build(sc)
+    try:
+        fr = ctx.render(built, sc, opt)
+        gid = np.where(fr.hit_geom == 0xFFFFFFFF, -1, fr.hit_prim.astype(np.int64))[y0:y0 + w, x0:x0 + w]
+        fid = f.primary_ids()
+        assert np.mean(np.where(fid < 0, -1, keep[np.maximum(fid, 0)]) == gid) >= 0.999
+        g = ctx.adjoint(built, sc, opt, d_color, interior_only=True)
+    finally:
+        built.release()
+    rows = _compare(f, g_local(g, keep), GLOBALS, target, wt)
+    _check(rows)
+    rows = _compare(f, g_local(g, keep), _sphere_params(f, 12, seed=3), target, wt)
+    _check(rows, frac_ok=0.95)
+
+
+def g_local(g, keep):
+    """The adjoint's gradients with the per-sphere arrays restricted to the
+    window's spheres (indexed as in the window frame)."""
+    out = dict(g)
+    for k in ("sphere_color", "sphere_center", "sphere_radius"):
+        out[k] = np.asarray(g[k])[keep]
+    return out

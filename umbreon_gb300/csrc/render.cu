@@ -3010,7 +3010,12 @@ static bool needsOwnPass(const ubr_render_desc& d) {
 ubr_status renderBatch(Context* c, const std::vector<Job>& jobs, ubr_frame* total) {
   std::vector<Job> together, alone;
   for (const Job& j : jobs) (needsOwnPass(*j.desc) ? alone : together).push_back(j);
-  if (alone.empty()) return runFrames(c, jobs, total, nullptr, nullptr);
+  // frames that share a scene are made contiguous in the launch (stable
+  // order otherwise): their rays then walk one BVH at a time, which keeps
+  // it resident in L2; every frame still writes its own buffers
+  std::stable_sort(together.begin(), together.end(),
+                   [](const Job& a, const Job& b) { return a.scene < b.scene; });
+  if (alone.empty()) return runFrames(c, together, total, nullptr, nullptr);
   const uint32_t flags = total ? total->flags : 0u;
   ubr_frame sum{};
   auto add = [&](const ubr_frame& t) {
