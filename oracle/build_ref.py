@@ -85,6 +85,26 @@ def build(reference: Path, jobs: int) -> dict:
     return report
 
 
+def build_if_stale(reference: Path = DEFAULT_REF, jobs: int = os.cpu_count() or 4, verbose: bool = False) -> bool:
+    """Build when the reference sources exist and an output is missing or
+    older than the stand-ins, the driver or this recipe.  Returns whether the
+    checker is available afterwards."""
+    if not (reference / "src" / "umbreon" / "umbreon.cpp").exists():
+        return False
+    outs = [OUT / "libumbreon_ref.so"] + [OUT / t for t in TESTS]
+    deps = [Path(__file__)] + sorted((HERE / "shim").rglob("*")) + sorted((HERE / "ref").glob("*")) + sorted(
+        (HERE / "src").glob("*.hpp"))
+    deps = [d for d in deps if d.is_file()]
+    newest = max(d.stat().st_mtime for d in deps)
+    if all(o.exists() and o.stat().st_mtime >= newest for o in outs):
+        return True
+    rep = build(reference, jobs)
+    ok = bool(rep["library"] and rep["library"]["ok"]) and all(t["built"] for t in rep["tests"].values())
+    if verbose:
+        print(("built " if ok else "FAILED to build ") + str(OUT / "libumbreon_ref.so"))
+    return ok
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=str(DEFAULT_REF))

@@ -239,15 +239,21 @@ def test_adjoint_benchmark_scene_window(ctx):
     target = fd64.Fd64Frame(ctsc, ctopt, seed_window=seeds).record()
     f = fd64.Fd64Frame(csc, copt, seed_window=seeds)
     img = f.record()
-    wt = fd64.interior_mask(f.primary_ids()).astype(np.float64)
-    d_color = np.zeros((opt.height, opt.width, 4), np.float32)
-    d_color[y0:y0 + w, x0:x0 + w, :3] = (2.0 * wt[..., None] * (img[..., :3] - target[..., :3])).astype(np.float32)
     built = ctx.build(sc)
     try:
         fr = ctx.render(built, sc, opt)
-        gid = np.where(fr.hit_geom == 0xFFFFFFFF, -1, fr.hit_prim.astype(np.int64))[y0:y0 + w, x0:x0 + w]
+        gid_full = np.where(fr.hit_geom == 0xFFFFFFFF, -1, fr.hit_prim.astype(np.int64))
+        gid = gid_full[y0:y0 + w, x0:x0 + w]
         fid = f.primary_ids()
         assert np.mean(np.where(fid < 0, -1, keep[np.maximum(fid, 0)]) == gid) >= 0.999
+        # interior samples as the adjoint sees them: the 3x3 neighbourhood in
+        # the WHOLE frame (a window-border sample next to another sphere just
+        # outside the window is not interior), and interior in the window frame
+        wt = (fd64.interior_mask(gid_full)[y0:y0 + w, x0:x0 + w] &
+              fd64.interior_mask(fid)).astype(np.float64)
+        d_color = np.zeros((opt.height, opt.width, 4), np.float32)
+        d_color[y0:y0 + w, x0:x0 + w, :3] = (2.0 * wt[..., None] * (img[..., :3] - target[..., :3])).astype(
+            np.float32)
         g = ctx.adjoint(built, sc, opt, d_color, interior_only=True)
     finally:
         built.release()

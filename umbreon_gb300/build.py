@@ -30,9 +30,6 @@ ORACLE = ROOT / "oracle"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["api.cu", "scene_build.cu", "render.cu", "gi.cu", "adjoint.cu"]
-# The trace / shade units contract multiply-adds (measured 3-4 % faster in the
-# occlusion kernel); the BVH build and the adjoint keep separate IEEE ops.
-FMAD_SOURCES = {"render.cu", "gi.cu"}
 HOST_SOURCES = ["umbreon.cpp"]
 
 
@@ -79,8 +76,7 @@ def build_ubr(verbose: bool = False) -> Path:
         o = objdir / (s.stem + ".o")
         objs.append(o)
         if _stale(o, [s] + hdrs + [Path(__file__)]):
-            flags = [("--fmad=true" if (f == "--fmad=false" and src in FMAD_SOURCES) else f) for f in common]
-            jobs.append([nvcc] + flags + ["-c", str(s), "-o", str(o)])
+            jobs.append([nvcc] + common + ["-c", str(s), "-o", str(o)])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
@@ -128,6 +124,11 @@ def build_all(verbose: bool = False) -> None:
     build_ubr(verbose)
     if (HOST / "umbreon.cpp").exists():
         build_host(verbose)
+    # the reference's own render path as a CPU checker, only where its
+    # sources exist (oracle/build_ref.py)
+    sys.path.insert(0, str(ROOT))
+    from oracle import build_ref
+    build_ref.build_if_stale(verbose=verbose)
 
 
 if __name__ == "__main__":

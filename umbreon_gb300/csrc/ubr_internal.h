@@ -4,7 +4,8 @@
 // ray/primitive intersectors used by the BVH build and the trace kernels.
 // The library is compiled with --fmad=false so shading arithmetic rounds the
 // way the reference's C++ does (each product/sum rounded on its own); the
-// traversal slab test opts back into FMA explicitly with fmaf().
+// traversal slab test and the binary any-hit forms of the sphere and capped
+// cone tests opt back into FMA explicitly with fmaf().
 #pragma once
 
 #include <cuda_runtime.h>
@@ -32,6 +33,18 @@ UBR_HD f3 cross(f3 a, f3 b) {
   return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 UBR_HD float length(f3 a) { return sqrtf(dot(a, a)); }
+// Fused forms for the binary any-hit tests: F = true evaluates a dot product
+// and a*s + c with one rounding per multiply-add (fewer issued instructions in
+// the occlusion kernels); F = false is the separately rounded operation above,
+// bit for bit.
+template <bool F>
+UBR_HD float dotT(f3 a, f3 b) {
+  return F ? fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)) : dot(a, b);
+}
+template <bool F>
+UBR_HD f3 madT(f3 a, float s, f3 c) {
+  return F ? f3{fmaf(a.x, s, c.x), fmaf(a.y, s, c.y), fmaf(a.z, s, c.z)} : c + a * s;
+}
 // umbreon normalize (scene.hpp:36-39): a * (1/l) when l > 0
 UBR_HD f3 normalize(f3 a) {
   float l = length(a);
@@ -224,14 +237,19 @@ UBR_HD bool isectTriangle(const Ray& r, const TriPre& pre, f3 v0, f3 v1, f3 v2, 
 }
 
 // Sphere, perpendicular-distance form; front root first, back root second.
-// ATTR = false (any-hit queries) skips the hit attributes.
+// ATTR = false (any-hit queries) skips the hit attributes and evaluates the
+// same algebra with fused multiply-adds: a binary answer, which can differ
+// from the separately rounded one only for a ray that grazes the sphere or
+// ends within a rounding step of it.  Every query that reports a distance, a
+// normal or a first hit (ATTR = true) keeps the separately rounded form.
 template <bool ATTR = true>
 UBR_HD bool isectSphere(const Ray& r, f3 c, float rad, float tnear, float tmax, Hit& h) {
+  constexpr bool F = !ATTR;
   const f3 c0 = c - r.org;
-  const float rd2 = 1.0f / dot(r.dir, r.dir);
-  const float projC0 = dot(c0, r.dir) * rd2;
-  const f3 perp = c0 - r.dir * projC0;
-  const float l2 = dot(perp, perp);
+  const float rd2 = 1.0f / dotT<F>(r.dir, r.dir);
+  const float projC0 = dotT<F>(c0, r.dir) * rd2;
+  const f3 perp = F ? madT<true>(r.dir, -projC0, c0) : c0 - r.dir * projC0;
+  const float l2 = dotT<F>(perp, perp);
   const float r2 = rad * rad;
   if (!(l2 <= r2)) return false;
   const float td = sqrtf((r2 - l2) * rd2);
@@ -255,27 +273,30 @@ UBR_HD bool isectSphere(const Ray& r, f3 c, float rad, float tnear, float tmax, 
 // the point of the ray closest to the frustum's mid-axis point (parameter
 // ts0), so the quadratic's coefficients stay small and well conditioned;
 // roots are returned in the original ray parameter.  Up to two roots.
+// F = true: fused multiply-adds in the dot products and a*s + c terms (the
+// any-hit form, as in isectSphere).
+template <bool F = false>
 UBR_HD int frustumRoots(const Ray& r, f3 b, f3 a, float h0, float h1, float k0, float k1,
                         float* ts, float* hs) {
-  const f3 mid = b + a * (0.5f * (h0 + h1));
-  const float dd = dot(r.dir, r.dir);
-  const float ts0 = dot(mid - r.org, r.dir) / dd;
-  const f3 o = r.org + r.dir * ts0;
+  const f3 mid = madT<F>(a, 0.5f * (h0 + h1), b);
+  const float dd = dotT<F>(r.dir, r.dir);
+  const float ts0 = dotT<F>(mid - r.org, r.dir) / dd;
+  const f3 o = madT<F>(r.dir, ts0, r.org);
   const f3 w = o - b;
-  const float wa = dot(w, a), da = dot(r.dir, a);
-  const f3 wp = w - a * wa;
-  const f3 dp = r.dir - a * da;
-  const float g0 = k0 + k1 * wa, g1 = k1 * da;
-  const float A = dot(dp, dp) - g1 * g1;
-  const float B = dot(wp, dp) - g0 * g1;  // half of the linear coefficient
-  const float Cc = dot(wp, wp) - g0 * g0;
+  const float wa = dotT<F>(w, a), da = dotT<F>(r.dir, a);
+  const f3 wp = F ? madT<true>(a, -wa, w) : w - a * wa;
+  const f3 dp = F ? madT<true>(a, -da, r.dir) : r.dir - a * da;
+  const float g0 = F ? fmaf(k1, wa, k0) : k0 + k1 * wa, g1 = k1 * da;
+  const float A = F ? fmaf(-g1, g1, dotT<true>(dp, dp)) : dot(dp, dp) - g1 * g1;
+  const float B = F ? fmaf(-g0, g1, dotT<true>(wp, dp)) : dot(wp, dp) - g0 * g1;  // half the linear coefficient
+  const float Cc = F ? fmaf(-g0, g0, dotT<true>(wp, wp)) : dot(wp, wp) - g0 * g0;
   float rr[2];
   int m = 0;
   if (fabsf(A) <= 1e-12f * dd) {
     if (B == 0.0f) return 0;
     rr[m++] = -Cc / (2.0f * B);
   } else {
-    const float disc = B * B - A * Cc;
+    const float disc = F ? fmaf(B, B, -(A * Cc)) : B * B - A * Cc;
     if (disc < 0.0f) return 0;
     const float sq = sqrtf(disc);
     const float q = -(B + copysignf(sq, B));
@@ -290,8 +311,8 @@ UBR_HD int frustumRoots(const Ray& r, f3 b, f3 a, float h0, float h1, float k0, 
   }
   int n = 0;
   for (int i = 0; i < m; ++i) {
-    const float hh = wa + rr[i] * da;
-    if (hh >= h0 && hh <= h1 && k0 + k1 * hh >= 0.0f) {
+    const float hh = F ? fmaf(rr[i], da, wa) : wa + rr[i] * da;
+    if (hh >= h0 && hh <= h1 && (F ? fmaf(k1, hh, k0) : k0 + k1 * hh) >= 0.0f) {
       ts[n] = ts0 + rr[i];
       hs[n] = hh;
       ++n;
@@ -310,14 +331,16 @@ UBR_HD void segmentAxis(f3 p0, f3 p1, f3& a, float& L) {
 
 // Capped cone segment (CONE_LINEAR_CURVE): frustum + flat disks at p0, p1,
 // with its unit axis `a` and length L precomputed by segmentAxis.
-// ATTR = false (any-hit queries) returns at the first valid hit.
+// ATTR = false (any-hit queries) returns at the first valid hit and uses the
+// fused forms (as isectSphere does).
 template <bool ATTR = true>
 UBR_HD bool isectConeCurveAxis(const Ray& r, f3 p0, float r0, f3 p1, float r1, f3 a, float L, float tnear,
                                float tmax, Hit& h) {
+  constexpr bool F = !ATTR;
   if (!(L > 0.0f)) return false;
   const float k1 = (r1 - r0) / L;
   float ts[2], hs[2];
-  const int n = frustumRoots(r, p0, a, 0.0f, L, r0, k1, ts, hs);
+  const int n = frustumRoots<F>(r, p0, a, 0.0f, L, r0, k1, ts, hs);
   bool found = false;
   float best = tmax;
   for (int i = 0; i < n; ++i) {
@@ -333,16 +356,16 @@ UBR_HD bool isectConeCurveAxis(const Ray& r, f3 p0, float r0, f3 p1, float r1, f
       found = true;
     }
   }
-  const float da = dot(r.dir, a);
+  const float da = dotT<F>(r.dir, a);
   if (da != 0.0f) {
     for (int e = 0; e < 2; ++e) {
       const f3 pc = e == 0 ? p0 : p1;
       const float rc = e == 0 ? r0 : r1;
-      const float t = dot(pc - r.org, a) / da;
+      const float t = dotT<F>(pc - r.org, a) / da;
       if (!(t >= tnear && t <= best)) continue;
-      const f3 P = r.org + r.dir * t;
+      const f3 P = madT<F>(r.dir, t, r.org);
       const f3 d = P - pc;
-      if (dot(d, d) > rc * rc) continue;
+      if (dotT<F>(d, d) > rc * rc) continue;
       best = t;
       h.t = t;
       if (!ATTR) return true;
