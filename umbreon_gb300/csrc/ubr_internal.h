@@ -5,7 +5,8 @@
 // The library is compiled with --fmad=false so shading arithmetic rounds the
 // way the reference's C++ does (each product/sum rounded on its own); the
 // traversal slab test and the binary any-hit forms of the sphere and capped
-// cone tests opt back into FMA explicitly with fmaf().
+// cone tests opt back into FMA explicitly with fmaf() (the any-hit forms also
+// use the approximate division and square root).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -44,6 +45,28 @@ UBR_HD float dotT(f3 a, f3 b) {
 template <bool F>
 UBR_HD f3 madT(f3 a, float s, f3 c) {
   return F ? f3{fmaf(a.x, s, c.x), fmaf(a.y, s, c.y), fmaf(a.z, s, c.z)} : c + a * s;
+}
+// Division and square root of the any-hit forms: F = true uses the
+// approximate hardware forms (div.approx via __fdividef, sqrt.approx; a few
+// ulps) in place of the correctly rounded sequences; F = false is `/` and
+// sqrtf.  Host code always takes the correctly rounded form.
+template <bool F>
+UBR_HD float divT(float a, float b) {
+#ifdef __CUDA_ARCH__
+  if (F) return __fdividef(a, b);
+#endif
+  return a / b;
+}
+template <bool F>
+UBR_HD float sqrtT(float x) {
+#ifdef __CUDA_ARCH__
+  if (F) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+#endif
+  return sqrtf(x);
 }
 // umbreon normalize (scene.hpp:36-39): a * (1/l) when l > 0
 UBR_HD f3 normalize(f3 a) {
@@ -238,21 +261,21 @@ UBR_HD bool isectTriangle(const Ray& r, const TriPre& pre, f3 v0, f3 v1, f3 v2, 
 
 // Sphere, perpendicular-distance form; front root first, back root second.
 // ATTR = false (any-hit queries) skips the hit attributes and evaluates the
-// same algebra with fused multiply-adds: a binary answer, which can differ
-// from the separately rounded one only for a ray that grazes the sphere or
-// ends within a rounding step of it.  Every query that reports a distance, a
+// same algebra with fused multiply-adds and the approximate division and
+// square root: a binary answer, which can differ from the correctly rounded
+// one only for a ray that grazes the sphere or ends within a few ulps of it.  Every query that reports a distance, a
 // normal or a first hit (ATTR = true) keeps the separately rounded form.
 template <bool ATTR = true>
 UBR_HD bool isectSphere(const Ray& r, f3 c, float rad, float tnear, float tmax, Hit& h) {
   constexpr bool F = !ATTR;
   const f3 c0 = c - r.org;
-  const float rd2 = 1.0f / dotT<F>(r.dir, r.dir);
+  const float rd2 = divT<F>(1.0f, dotT<F>(r.dir, r.dir));
   const float projC0 = dotT<F>(c0, r.dir) * rd2;
   const f3 perp = F ? madT<true>(r.dir, -projC0, c0) : c0 - r.dir * projC0;
   const float l2 = dotT<F>(perp, perp);
   const float r2 = rad * rad;
   if (!(l2 <= r2)) return false;
-  const float td = sqrtf((r2 - l2) * rd2);
+  const float td = sqrtT<F>((r2 - l2) * rd2);
   const float tf = projC0 - td;
   const float tb = projC0 + td;
   float t;
@@ -273,14 +296,14 @@ UBR_HD bool isectSphere(const Ray& r, f3 c, float rad, float tnear, float tmax, 
 // the point of the ray closest to the frustum's mid-axis point (parameter
 // ts0), so the quadratic's coefficients stay small and well conditioned;
 // roots are returned in the original ray parameter.  Up to two roots.
-// F = true: fused multiply-adds in the dot products and a*s + c terms (the
-// any-hit form, as in isectSphere).
+// F = true: fused multiply-adds in the dot products and a*s + c terms, the
+// approximate division and square root (the any-hit form, as in isectSphere).
 template <bool F = false>
 UBR_HD int frustumRoots(const Ray& r, f3 b, f3 a, float h0, float h1, float k0, float k1,
                         float* ts, float* hs) {
   const f3 mid = madT<F>(a, 0.5f * (h0 + h1), b);
   const float dd = dotT<F>(r.dir, r.dir);
-  const float ts0 = dotT<F>(mid - r.org, r.dir) / dd;
+  const float ts0 = divT<F>(dotT<F>(mid - r.org, r.dir), dd);
   const f3 o = madT<F>(r.dir, ts0, r.org);
   const f3 w = o - b;
   const float wa = dotT<F>(w, a), da = dotT<F>(r.dir, a);
@@ -294,13 +317,13 @@ UBR_HD int frustumRoots(const Ray& r, f3 b, f3 a, float h0, float h1, float k0, 
   int m = 0;
   if (fabsf(A) <= 1e-12f * dd) {
     if (B == 0.0f) return 0;
-    rr[m++] = -Cc / (2.0f * B);
+    rr[m++] = divT<F>(-Cc, 2.0f * B);
   } else {
     const float disc = F ? fmaf(B, B, -(A * Cc)) : B * B - A * Cc;
     if (disc < 0.0f) return 0;
-    const float sq = sqrtf(disc);
+    const float sq = sqrtT<F>(disc);
     const float q = -(B + copysignf(sq, B));
-    float r0 = q / A, r1 = q != 0.0f ? Cc / q : r0;
+    float r0 = divT<F>(q, A), r1 = q != 0.0f ? divT<F>(Cc, q) : r0;
     if (r0 > r1) {
       const float t = r0;
       r0 = r1;
@@ -338,7 +361,7 @@ UBR_HD bool isectConeCurveAxis(const Ray& r, f3 p0, float r0, f3 p1, float r1, f
                                float tmax, Hit& h) {
   constexpr bool F = !ATTR;
   if (!(L > 0.0f)) return false;
-  const float k1 = (r1 - r0) / L;
+  const float k1 = divT<F>(r1 - r0, L);
   float ts[2], hs[2];
   const int n = frustumRoots<F>(r, p0, a, 0.0f, L, r0, k1, ts, hs);
   bool found = false;
@@ -361,7 +384,7 @@ UBR_HD bool isectConeCurveAxis(const Ray& r, f3 p0, float r0, f3 p1, float r1, f
     for (int e = 0; e < 2; ++e) {
       const f3 pc = e == 0 ? p0 : p1;
       const float rc = e == 0 ? r0 : r1;
-      const float t = dotT<F>(pc - r.org, a) / da;
+      const float t = divT<F>(dotT<F>(pc - r.org, a), da);
       if (!(t >= tnear && t <= best)) continue;
       const f3 P = madT<F>(r.dir, t, r.org);
       const f3 d = P - pc;
