@@ -12,6 +12,8 @@
 // functions of (grid index, sample index, pt1Seed), as in the reference, so
 // the oracle draws the same samples and the frames agree up to traversal
 // float order.
+#include <algorithm>
+
 #include "gi.cuh"
 #include "trace.cuh"
 
@@ -360,12 +362,13 @@ UBR_D float emissiveHitWeight(const EmitD& el, int kind, uint32_t prim, f3 O, f3
 // bounce below the geometric horizon adds nothing.  First bounce: pt2 the
 // scrambled Sobol point (blue-noise section or per-point sequence), pt1
 // Hammersley + Cranley-Patterson when ld, else the tea2 stream.  Returns
-// (E, first-bounce hit fraction); `half` gets the sum of the first spp/2
-// samples.
+// (sum of E, number of first bounces that hit or fall below the horizon)
+// over the samples sFirst, sFirst + sStep, ... < spp; `half` gets the sum of
+// those among the first spp/2.
 template <int KM>
 UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, int nLights, f3 P, f3 N, f3 Ng,
-                         float tEps, uint32_t seed, uint32_t px, uint32_t py, int spp, f3& half, uint32_t& rays,
-                         uint32_t& nee, uint32_t& ovf) {
+                         float tEps, uint32_t seed, uint32_t px, uint32_t py, int spp, int sFirst, int sStep,
+                         f3& half, uint32_t& rays, uint32_t& nee, uint32_t& ovf) {
   const Frame3 f = frameFromNormal(N);
   const float eps = selfIntersectEps(P, N, tEps);
   const f3 O{P.x + N.x * eps, P.y + N.y * eps, P.z + N.z * eps};
@@ -390,7 +393,7 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
   f3 Esum{0.0f, 0.0f, 0.0f};
   half = f3{0.0f, 0.0f, 0.0f};
   int nOcc = 0;
-  for (int sI = 0; sI < spp; ++sI) {
+  for (int sI = sFirst; sI < spp; sI += sStep) {
     uint32_t s0 = seed, s1 = uint32_t(sI + g.sampleOffset);
     tea2(s0, s1);
     float u1, u2;
@@ -482,8 +485,7 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
       half.z += L.z;
     }
   }
-  const float invN = 1.0f / float(spp > 0 ? spp : 1);
-  return make_float4(Esum.x * invN, Esum.y * invN, Esum.z * invN, float(nOcc) * invN);
+  return make_float4(Esum.x, Esum.y, Esum.z, float(nOcc));
 }
 
 // gatherPt1Grid (pt1_gather.hpp:525-614): E and the hit fraction of every
@@ -491,36 +493,62 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
 // hashU32(pix ^ hashU32(pt1Seed)); the primary hit distance scales the
 // origin epsilon.  Points not eligible get zero (grid form; a list names
 // eligible points).  `listCount` (device) bounds the list when non-null.
-template <int KM>
+// LANES neighbouring threads share one point, lane k taking its samples
+// k, k + LANES, ...: a warp traces 32 / LANES points' sample fans from a few
+// origins (coherent node fetches, as the AO rays of one hit), and a short
+// list (the edge patch) still fills the GPU.  The lanes' sums meet in a
+// shuffle tree, so E is the same mean summed in another order.
+template <int KM, int LANES>
 __global__ void __launch_bounds__(128) k_gather(GiP g, DScene s, const LightD* lights, int nLights, GiGrid grid,
                                                 const uint32_t* list, const uint32_t* listCount, uint32_t n, int spp,
                                                 float4* E) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t rays = 0, nee = 0, ovf = 0;
   const uint32_t cnt = listCount ? min(n, *listCount) : n;
-  if (i < cnt) {
-    const uint32_t pix = list ? list[i] : i;
-    const float4 ne = grid.ne[pix];
+  const uint64_t total = uint64_t(cnt) * LANES, stride = uint64_t(gridDim.x) * blockDim.x;
+  // grid-stride over (point, lane) pairs; a warp's lanes run the same
+  // iterations, as the shuffles below need
+  for (uint64_t t0 = uint64_t(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); t0 < total; t0 += stride) {
+    const uint64_t t = t0 + (threadIdx.x & 31u);
+    const uint32_t i = uint32_t(t / LANES);
+    const int lane = int(t % LANES);
     float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     f3 half{0.0f, 0.0f, 0.0f};
-    if (ne.w != 0.0f) {
-      const float4 pd = grid.pd[pix];
-      const f3 N{ne.x, ne.y, ne.z};
-      f3 Ng = N;
-      if (grid.ng) {
-        const float4 q = grid.ng[pix];
-        Ng = f3{q.x, q.y, q.z};
+    uint32_t pix = 0;
+    if (i < cnt) {
+      pix = list ? list[i] : i;
+      const float4 ne = grid.ne[pix];
+      if (ne.w != 0.0f) {
+        const float4 pd = grid.pd[pix];
+        const f3 N{ne.x, ne.y, ne.z};
+        f3 Ng = N;
+        if (grid.ng) {
+          const float4 q = grid.ng[pix];
+          Ng = f3{q.x, q.y, q.z};
+        }
+        const uint32_t seed = hashU32(pix ^ g.seedMix);
+        const float tEps = pd.w > 0.0f ? pd.w : 1.0f;
+        e = gatherPoint<KM>(g, s, lights, nLights, f3{pd.x, pd.y, pd.z}, N, Ng, tEps, seed, pix % uint32_t(grid.W),
+                            pix / uint32_t(grid.W), spp, lane, LANES, half, rays, nee, ovf);
       }
-      const uint32_t seed = hashU32(pix ^ g.seedMix);
-      const float tEps = pd.w > 0.0f ? pd.w : 1.0f;
-      e = gatherPoint<KM>(g, s, lights, nLights, f3{pd.x, pd.y, pd.z}, N, Ng, tEps, seed, pix % uint32_t(grid.W),
-                          pix / uint32_t(grid.W), spp, half, rays, nee, ovf);
     }
-    E[pix] = e;
-    if (g.halfE) {
-      g.halfE[3 * size_t(pix)] = half.x;
-      g.halfE[3 * size_t(pix) + 1] = half.y;
-      g.halfE[3 * size_t(pix) + 2] = half.z;
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) {
+      e.x += __shfl_xor_sync(0xFFFFFFFFu, e.x, o);
+      e.y += __shfl_xor_sync(0xFFFFFFFFu, e.y, o);
+      e.z += __shfl_xor_sync(0xFFFFFFFFu, e.z, o);
+      e.w += __shfl_xor_sync(0xFFFFFFFFu, e.w, o);
+      half.x += __shfl_xor_sync(0xFFFFFFFFu, half.x, o);
+      half.y += __shfl_xor_sync(0xFFFFFFFFu, half.y, o);
+      half.z += __shfl_xor_sync(0xFFFFFFFFu, half.z, o);
+    }
+    if (i < cnt && lane == 0) {
+      const float invN = 1.0f / float(spp > 0 ? spp : 1);
+      E[pix] = make_float4(e.x * invN, e.y * invN, e.z * invN, e.w * invN);
+      if (g.halfE) {
+        g.halfE[3 * size_t(pix)] = half.x;
+        g.halfE[3 * size_t(pix) + 1] = half.y;
+        g.halfE[3 * size_t(pix) + 2] = half.z;
+      }
     }
   }
   warpCount(&g.stats[0], rays);
@@ -1163,6 +1191,9 @@ void byKind(int km, F&& f) {
   switch (km) {
     case kMaskMesh: f(std::integral_constant<int, kMaskMesh>{}); break;
     case kMaskSphere: f(std::integral_constant<int, kMaskSphere>{}); break;
+    // ball-and-stick (spheres + capped cylinders), molecular surface + atoms
+    case kMaskSphere | kMaskCone: f(std::integral_constant<int, kMaskSphere | kMaskCone>{}); break;
+    case kMaskMesh | kMaskSphere: f(std::integral_constant<int, kMaskMesh | kMaskSphere>{}); break;
     default: f(std::integral_constant<int, kMaskAll>{});
   }
 }
@@ -1179,11 +1210,26 @@ void giGBuffer(int km, cudaStream_t s, const Params& p, const DScene& sc, int w,
   });
 }
 
+// Lanes per gather point: the sample count rounded down to a power of two,
+// at most 8 (a warp then holds four points' fans).  The grid is at most 16
+// blocks per SM (a list's length is known only on the device).
 void giGather(int km, cudaStream_t s, const GiP& g, const DScene& sc, const LightD* lights, int nLights,
               const GiGrid& grid, const uint32_t* list, const uint32_t* listCount, uint32_t n, int spp, float4* E) {
+  const int lanes = spp >= 8 ? 8 : spp >= 4 ? 4 : spp >= 2 ? 2 : 1;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const uint32_t nb = std::max(1u, std::min(blocks(uint64_t(n) * uint64_t(lanes), 128), uint32_t(std::max(sms, 1)) * 16u));
   byKind(km, [&](auto K) {
-    k_gather<decltype(K)::value><<<blocks(n, 128), 128, 0, s>>>(g, sc, lights, nLights, grid, list, listCount, n,
-                                                                spp, E);
+    constexpr int k = decltype(K)::value;
+    if (lanes == 8)
+      k_gather<k, 8><<<nb, 128, 0, s>>>(g, sc, lights, nLights, grid, list, listCount, n, spp, E);
+    else if (lanes == 4)
+      k_gather<k, 4><<<nb, 128, 0, s>>>(g, sc, lights, nLights, grid, list, listCount, n, spp, E);
+    else if (lanes == 2)
+      k_gather<k, 2><<<nb, 128, 0, s>>>(g, sc, lights, nLights, grid, list, listCount, n, spp, E);
+    else
+      k_gather<k, 1><<<nb, 128, 0, s>>>(g, sc, lights, nLights, grid, list, listCount, n, spp, E);
   });
 }
 
