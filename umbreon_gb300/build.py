@@ -30,7 +30,7 @@ ORACLE = ROOT / "oracle"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["api.cu", "scene_build.cu", "render.cu", "gi.cu", "adjoint.cu"]
-HOST_SOURCES = ["umbreon.cpp"]
+HOST_SOURCES = ["umbreon.cpp", "pov/sdl.cpp", "pov/pov_scene_reader.cpp", "pov/mesh2_reader.cpp"]
 
 
 def _nvcc() -> str:
@@ -94,7 +94,7 @@ def build_host(verbose: bool = False) -> Path:
     LIB.mkdir(exist_ok=True)
     out = LIB / "libumbreon_gb300.so"
     srcs = [HOST / s for s in HOST_SOURCES]
-    hdrs = sorted((HOST / "include").rglob("*.hpp")) + sorted(INCLUDE.glob("*.h"))
+    hdrs = sorted((HOST / "include").rglob("*.hpp")) + sorted((HOST / "pov").glob("*.hpp")) + sorted(INCLUDE.glob("*.h"))
     ubr = LIB / "libubr.so"
     if _stale(out, srcs + hdrs + [ubr]):
         cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
