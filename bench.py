@@ -321,9 +321,10 @@ def _adjoint_timing(ctx, built, sc, opt, flush, ms_forward, rays_forward, steps=
 def gi_workload(args, flush):
     """GI: (1) the pt1 gather at every pixel (8 spp, one bounce, no denoise)
     on workload 0 with its light shadowed, against the same frame without GI;
-    (2) pt1 at the reference's defaults on the ball-and-stick frame (gather
-    grid = the supersample factor, a-trous denoise of E, joint-bilateral
-    upsample, edge patch): the GI stages' device ms and rays."""
+    (2) pt1 and pt2 at the reference's defaults on the ball-and-stick frame
+    (gather grid = the supersample factor, a-trous denoise of E,
+    joint-bilateral upsample, edge patch; pt2 with its Sobol first bounce):
+    the GI stages' device ms and rays."""
     import ctypes as C
     import torch
     from umbreon_gb300 import abi, scenes
@@ -348,42 +349,50 @@ def gi_workload(args, flush):
     out["pt1_gi_space_filling_640x480_8spp"] = {
         "ms_per_frame_direct": round(ms_d, 4), "ms_per_frame_gi": round(ms_gi, 4), "gather_ms": round(g_ms, 4),
         "gather_pixels": hits, "gather_Mpaths_s": round(hits * 8 / g_ms / 1e3, 1), "traversal": knobs}
-    # the reference's pt1 defaults on the headline scene
+    # the reference's pt1 and pt2 defaults on the headline scene
     sc, opt = scenes.ball_and_stick()
     ctx = Context(0, **(_knobs(args) or {}))
     b = ctx.build(sc)
     ms_d, _, _, _ = _device_frames(ctx, b, sc, opt, 5, 3, flush)
-    gi = copy.copy(opt)
-    gi.gi, gi.giIntegrator = True, 1
-    rd, keep = make_render_desc(sc, gi)
-    col = torch.empty((gi.height, gi.width, 4), dtype=torch.float32, device="cuda")
-    frames = []
-    for i in range(3 + 5):
-        flush.zero_()
-        torch.cuda.synchronize()
-        fr = abi.Frame()
-        fr.memory = abi.MEMORY_DEVICE
-        fr.color = C.cast(C.c_void_p(col.data_ptr()), abi.f32p)
-        ctx._check(ctx._L.ubr_render(ctx.handle, b.handle, C.byref(rd), C.byref(fr), None, None))
-        if i >= 3:
-            frames.append(fr)
+    col = torch.empty((opt.height, opt.width, 4), dtype=torch.float32, device="cuda")
+    for integ, key, options in (
+            (1, "pt1_gi_defaults_ball_and_stick_1920x1080_ss2",
+             "giIntegrator 1, pt1Spp 8, giBounces 1, pt1GatherDiv -1 (= ss 2: 1920x1080 gather grid), "
+             "pt1Denoise (a-trous, 5 iterations), upsample, edge patch (spp x4)"),
+            (2, "pt2_gi_defaults_ball_and_stick_1920x1080_ss2",
+             "giIntegrator 2 (the reference's default) with every pt1/pt2 option at its default: the pt1 "
+             "pipeline with the blue-noise Owen-scrambled Sobol first bounce; no emitters, no reflective "
+             "materials in this scene")):
+        gi = copy.copy(opt)
+        gi.gi, gi.giIntegrator = True, integ
+        rd, keep = make_render_desc(sc, gi)
+        frames = []
+        for i in range(3 + 5):
+            flush.zero_()
+            torch.cuda.synchronize()
+            fr = abi.Frame()
+            fr.memory = abi.MEMORY_DEVICE
+            fr.color = C.cast(C.c_void_p(col.data_ptr()), abi.f32p)
+            ctx._check(ctx._L.ubr_render(ctx.handle, b.handle, C.byref(rd), C.byref(fr), None, None))
+            if i >= 3:
+                frames.append(fr)
+        n = len(frames)
+        split = [sum(f.gi_ms[k] for f in frames) / n for k in range(6)]
+        gi_ms = sum(split)
+        rays = (frames[0].gi_gather_rays + frames[0].gi_nee_rays + frames[0].gi_gbuffer_rays)
+        out[key] = {
+            "options": options,
+            "ms_per_frame_direct": round(ms_d, 3),
+            "ms_per_frame_gi": round(sum(f.total_ms for f in frames) / n, 3),
+            "gi_ms": round(gi_ms, 3),
+            "gi_split_ms": {"gbuffer": round(split[0], 3), "gather": round(split[1], 3),
+                            "denoise": round(split[2], 3), "upsample": round(split[3], 3),
+                            "edge_patch": round(split[4], 3), "reflection": round(split[5], 3)},
+            "gather_rays": int(frames[0].gi_gather_rays), "nee_rays": int(frames[0].gi_nee_rays),
+            "gbuffer_rays": int(frames[0].gi_gbuffer_rays), "patched_pixels": int(frames[0].gi_patched_pixels),
+            "gi_Mrays_s": round(rays / gi_ms / 1e3, 1)}
     b.release()
     ctx.close()
-    n = len(frames)
-    split = [sum(f.gi_ms[k] for f in frames) / n for k in range(5)]
-    gi_ms = sum(split)
-    rays = (frames[0].gi_gather_rays + frames[0].gi_nee_rays + frames[0].gi_gbuffer_rays)
-    out["pt1_gi_defaults_ball_and_stick_1920x1080_ss2"] = {
-        "options": "giIntegrator 1, pt1Spp 8, giBounces 1, pt1GatherDiv -1 (= ss 2: 1920x1080 gather grid), "
-                   "pt1Denoise (a-trous, 5 iterations), upsample, edge patch (spp x4)",
-        "ms_per_frame_direct": round(ms_d, 3),
-        "ms_per_frame_gi": round(sum(f.total_ms for f in frames) / n, 3),
-        "gi_ms": round(gi_ms, 3),
-        "gi_split_ms": {"gbuffer": round(split[0], 3), "gather": round(split[1], 3), "denoise": round(split[2], 3),
-                        "upsample": round(split[3], 3), "edge_patch": round(split[4], 3)},
-        "gather_rays": int(frames[0].gi_gather_rays), "nee_rays": int(frames[0].gi_nee_rays),
-        "gbuffer_rays": int(frames[0].gi_gbuffer_rays), "patched_pixels": int(frames[0].gi_patched_pixels),
-        "gi_Mrays_s": round(rays / gi_ms / 1e3, 1)}
     return out
 
 
