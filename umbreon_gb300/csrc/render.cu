@@ -89,6 +89,32 @@ struct Bufs {
 // coordinate table of a fine-lattice pass.
 UBR_D uint32_t latticeOf(const Bufs& b, uint32_t gpix) { return b.coord ? __ldg(&b.coord[gpix]) : gpix; }
 
+// Pixel of slot i in a grid frame's first round (all W x H hi-res pixels, no
+// queue): 8 x 4 pixel tiles in slot order, so a warp's primary rays are a
+// compact bundle and the hits queued after them stay neighbours (a warp of
+// one light's shadow rays covers a tile); the columns and rows that do not
+// fill a tile follow in row order.  A bijection on [0, W H).
+UBR_D uint32_t tiledPixel(uint32_t i, uint32_t W, uint32_t H) {
+  const uint32_t fw = W & ~7u, fh = H & ~3u, nt = fw * fh;
+  if (i < nt) {
+    const uint32_t t = i >> 5, k = i & 31u, tilesX = fw >> 3;
+    return ((t / tilesX) * 4u + (k >> 3)) * W + (t % tilesX) * 8u + (k & 7u);
+  }
+  uint32_t j = i - nt;
+  const uint32_t rw = W - fw;  // right strip of rows [0, fh)
+  if (j < rw * fh) return (j / rw) * W + fw + j % rw;
+  j -= rw * fh;
+  return fh * W + j;  // bottom rows
+}
+// Slot -> global pixel of a round: the queue's entry, else the tiled order of
+// a single frame's full first round, else the slot itself.
+template <bool BATCH>
+UBR_D uint32_t slotPixel(const Params& p, const Bufs& b, const uint32_t* queue, uint32_t i, uint32_t n) {
+  if (queue) return queue[i];
+  if (BATCH || b.coord || n != uint32_t(p.W) * uint32_t(p.H)) return i;
+  return tiledPixel(i, uint32_t(p.W), uint32_t(p.H));
+}
+
 // AO of a coarse grid cell or of an interpolated lookup: openness and the
 // quality-estimator channels (neutral when not gathered).
 struct AoQ {
@@ -192,7 +218,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_closest(Params p1, DScene s1, 
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t traced = 0, ovf = 0;
   if (i < n) {
-    const uint32_t gpix = queue ? queue[i] : i;
+    const uint32_t gpix = slotPixel<BATCH>(p1, b, queue, i, n);
     const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
@@ -224,7 +250,7 @@ __global__ void __launch_bounds__(128) k_surface(Params p1, DScene s1, Batch bt,
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool cast = false;
   if (i < n) {
-    const uint32_t gpix = queue ? queue[i] : i;
+    const uint32_t gpix = slotPixel<BATCH>(p1, b, queue, i, n);
     const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
@@ -834,7 +860,7 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
   bool push = false;
   uint32_t gpix = 0, capped = 0;
   if (i < n) {
-    gpix = queue ? queue[i] : i;
+    gpix = slotPixel<BATCH>(p1, b, queue, i, n);
     const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
