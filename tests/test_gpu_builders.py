@@ -36,16 +36,18 @@ def test_builders_render_identically(name):
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_occlusion_kernels_render_identically(name):
-    """The three occlusion kernels (one thread per ray, persistent refill,
-    resident grid with shared-memory top levels) give the same frame."""
+    """The four occlusion kernels (one thread per ray, persistent refill,
+    resident grid with shared-memory top levels, interleaved node / primitive
+    steps) give the same frame."""
     from umbreon_gb300.api import Context
     sc, opt = CASES[name]()
     out = {}
-    for mode in (1, 2, 3):
+    for mode in (1, 2, 3, 4):
         ctx = Context(0, trace_mode=mode)
         b = ctx.build(sc)
         out[mode] = ctx.render(b, sc, opt).color.copy()
         b.release()
         ctx.close()
-    assert np.array_equal(out[1], out[2])
-    assert np.array_equal(out[1], out[3])
+    for mode in (2, 3, 4):
+        assert np.array_equal(out[1], out[mode]), mode
+

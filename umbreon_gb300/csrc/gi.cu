@@ -499,7 +499,7 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
 // list (the edge patch) still fills the GPU.  The lanes' sums meet in a
 // shuffle tree, so E is the same mean summed in another order.
 template <int KM, int LANES>
-__global__ void __launch_bounds__(128) k_gather(GiP g, DScene s, const LightD* lights, int nLights, GiGrid grid,
+__global__ void __launch_bounds__(128, 8) k_gather(GiP g, DScene s, const LightD* lights, int nLights, GiGrid grid,
                                                 const uint32_t* list, const uint32_t* listCount, uint32_t n, int spp,
                                                 float4* E) {
   uint32_t rays = 0, nee = 0, ovf = 0;
