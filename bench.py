@@ -355,16 +355,21 @@ def gi_workload(args, flush):
     b = ctx.build(sc)
     ms_d, _, _, _ = _device_frames(ctx, b, sc, opt, 5, 3, flush)
     col = torch.empty((opt.height, opt.width, 4), dtype=torch.float32, device="cuda")
-    for integ, key, options in (
+    for integ, key, options, extra in (
             (1, "pt1_gi_defaults_ball_and_stick_1920x1080_ss2",
              "giIntegrator 1, pt1Spp 8, giBounces 1, pt1GatherDiv -1 (= ss 2: 1920x1080 gather grid), "
-             "pt1Denoise (a-trous, 5 iterations), upsample, edge patch (spp x4)"),
+             "pt1Denoise (a-trous, 5 iterations), upsample, edge patch (spp x4)", {}),
             (2, "pt2_gi_defaults_ball_and_stick_1920x1080_ss2",
              "giIntegrator 2 (the reference's default) with every pt1/pt2 option at its default: the pt1 "
              "pipeline with the blue-noise Owen-scrambled Sobol first bounce; no emitters, no reflective "
-             "materials in this scene")):
+             "materials in this scene", {}),
+            (2, "pt2_gi_restir_2_rounds_ball_and_stick_1920x1080_ss2",
+             "the pt2 defaults with pt2Rounds 2 (ReSTIR spatial resampling, off by default): reservoir "
+             "gather (one thread per point) + two spatial rounds, inside gather_ms", {"pt2Rounds": 2})):
         gi = copy.copy(opt)
         gi.gi, gi.giIntegrator = True, integ
+        for k, v in extra.items():
+            setattr(gi, k, v)
         rd, keep = make_render_desc(sc, gi)
         frames = []
         for i in range(3 + 5):

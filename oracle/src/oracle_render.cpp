@@ -644,6 +644,9 @@ struct Opt {  // the RenderOptions fields this path reads
   bool pt2Emissive = true, pt2EmissiveNee = true, pt2Reflect = true, pt2Glossy = true, pt2GlossyDenoise = true;
   bool pt2Adaptive = false;
   float pt2AdaptiveThresh = 0.15f;
+  int pt2Rounds = 0;
+  float pt2Radius = 16.0f, pt2MCap = 100.0f, pt2WClamp = 0.0f;
+  bool pt2Unbiased = false;
   bool pt2() const { return gi && giIntegrator == 2; }
   bool traceRefl() const { return pt2() && pt2Reflect; }
   bool aoEnhanced() const {  // render_options.hpp:79-82
@@ -1601,11 +1604,53 @@ inline float emissiveHitWeight(const Scene& s, int kind, uint32_t prim, const V3
 }
 
 // pt2's gather configuration at one point (Pt1GatherExt / Pt2GatherCfg)
+// pt2_reservoir.hpp:36-42 Pt2Reservoir: one sample point (a first-bounce
+// hit, or an anchor 1e7 along an escaped first segment), the full path
+// radiance leaving it, the candidates it stands for (M) and its unbiased
+// contribution weight W.
+struct Reservoir {
+  V3 pos{0.0f, 0.0f, 0.0f}, nrm{0.0f, 0.0f, 0.0f}, rad{0.0f, 0.0f, 0.0f};
+  float M = 0.0f, W = 0.0f;
+};
+constexpr float kEnvAnchor = 1.0e7f;   // pt2_reservoir.hpp:33
+constexpr float kPiF = 3.14159265358979323846f;
+inline float lum3(const V3& c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+// pt2_reservoir.hpp:55-63 pt2TargetPdf: luminance times the receiver cosine
+inline float targetPdf(const V3& P, const V3& N, const V3& sp, const V3& rad) {
+  const V3 d{sp.x - P.x, sp.y - P.y, sp.z - P.z};
+  const float l2 = dot(d, d);
+  if (l2 <= 0.0f) return 0.0f;
+  const float cs = dot(N, d) / std::sqrt(l2);
+  if (cs <= 0.0f) return 0.0f;
+  return lum3(rad) * cs;
+}
+// pt2_reservoir.hpp:72-89 pt2Jacobian: reconnection Jacobian of moving a
+// sample's receiver, cosines at the sample's normal, clamped to [0, cap]
+inline float reconnectJacobian(const V3& recvNew, const V3& recvOld, const V3& sp, const V3& sn, float cap) {
+  const V3 a{recvNew.x - sp.x, recvNew.y - sp.y, recvNew.z - sp.z};
+  const V3 b{recvOld.x - sp.x, recvOld.y - sp.y, recvOld.z - sp.z};
+  const float ra2 = dot(a, a), rb2 = dot(b, b);
+  if (ra2 <= 0.0f || rb2 <= 0.0f) return 0.0f;
+  const float ca = dot(sn, a) / std::sqrt(ra2);
+  const float cb = dot(sn, b) / std::sqrt(rb2);
+  if (ca <= 0.0f || cb <= 0.0f) return 0.0f;
+  const float j = (rb2 * ca) / (ra2 * cb);
+  if (!std::isfinite(j) || j < 0.0f) return 0.0f;
+  return j > cap ? cap : j;
+}
+// pt2_reservoir.hpp:94-99 pt2ReservoirUpdate: the streaming selection rule
+inline bool reservoirTake(double& wSum, float& M, float w, float m, float u) {
+  wSum += static_cast<double>(w);
+  M += m;
+  return w > 0.0f && static_cast<double>(u) * wSum <= static_cast<double>(w);
+}
+
 struct GatherExt {
   bool pt2 = false;
   uint32_t idxBase = 0, seed = 0;  // the point's Sobol section / scramble seed
   int sampleOffset = 0;
   V3* halfSum = nullptr;
+  Reservoir* rsv = nullptr;        // ReSTIR candidate reservoir of the point, or null
 };
 
 // pt1_gather.hpp:268-523 pt1GatherPoint: E_stored = (1/spp) sum over
@@ -1634,6 +1679,19 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
     cpy = u32ToUnorm(c1);
   }
   V3 Esum{0.0f, 0.0f, 0.0f};
+  // ReSTIR creation stage (pt1_gather.hpp:287-297, 451-470, 486-499): every
+  // sample is one candidate streamed into the point's reservoir with RIS
+  // weight pi * lum(L) (p_hat = lum(L) cos over the cosine pdf), selected by
+  // its own tea2 chain
+  Reservoir* rsv = ext ? ext->rsv : nullptr;
+  uint32_t rs0 = 0, rs1 = 0;
+  double rWSum = 0.0;
+  V3 rPos{0.0f, 0.0f, 0.0f}, rNrm{0.0f, 0.0f, 0.0f}, rRad{0.0f, 0.0f, 0.0f};
+  float rPHat = 0.0f;
+  if (rsv) {
+    rs0 = seed ^ 0x52455354u;
+    rs1 = 0x47490001u;
+  }
   for (int sI = 0; sI < spp; ++sI) {
     uint32_t s0 = seed, s1 = static_cast<uint32_t>(sI + sOff);
     tea2(s0, s1);
@@ -1656,6 +1714,8 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
     V3 org = O;
     float tnear = eps;
     V3 thr{1.0f, 1.0f, 1.0f}, L{0.0f, 0.0f, 0.0f};
+    V3 candPos{0.0f, 0.0f, 0.0f}, candN{0.0f, 0.0f, 0.0f};
+    bool candValid = false;
     for (int b = 1; horizonOk && b <= maxB; ++b) {
       Ray r;
       r.org = org; r.dir = wi; r.tnear = tnear; r.tfar = maxD;
@@ -1665,13 +1725,29 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
         L.x += thr.x * env.x;
         L.y += thr.y * env.y;
         L.z += thr.z * env.z;
+        if (rsv && b == 1) {  // escaped: the candidate sits far along the segment
+          candPos = V3{O.x + wi.x * kEnvAnchor, O.y + wi.y * kEnvAnchor, O.z + wi.z * kEnvAnchor};
+          candN = V3{-wi.x, -wi.y, -wi.z};
+          candValid = true;
+        }
         break;
       }
       if (b == 1) ++nOcc;
       V3 rad, alb, Py, Ny, em{0.0f, 0.0f, 0.0f};
       if (!pt1EvalVertex(c, h, org, wi, rad, alb, Py, Ny, pt2 && c.o.pt2Emissive, pt2 ? &s0 : nullptr,
-                         pt2 ? &s1 : nullptr, &em))
+                         pt2 ? &s1 : nullptr, &em)) {
+        if (rsv && b == 1) {  // absorbed by an outline: a zero-radiance candidate at the hit
+          candPos = V3{org.x + wi.x * h.t, org.y + wi.y * h.t, org.z + wi.z * h.t};
+          candN = V3{-wi.x, -wi.y, -wi.z};
+          candValid = true;
+        }
         break;
+      }
+      if (rsv && b == 1) {
+        candPos = Py;
+        candN = Ny;
+        candValid = true;
+      }
       float emW = 1.0f;
       if (emitNee && b == 1)
         emW = emissiveHitWeight(s, kindOfGeom(s, h.geomID), h.primID, org, wi, h.t, cand0Cos, h.Ng);
@@ -1714,6 +1790,21 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
         L.z *= k;
       }
     }
+    if (rsv) {
+      float w = 0.0f, pHat = 0.0f;
+      if (candValid && cand0Cos > 0.0f) {
+        pHat = lum3(L) * cand0Cos;
+        w = lum3(L) * kPiF;
+      }
+      tea2(rs0, rs1);
+      float unusedM = 0.0f;
+      if (reservoirTake(rWSum, unusedM, w, 0.0f, u32ToUnorm(rs0))) {
+        rPos = candPos;
+        rNrm = candN;
+        rRad = L;
+        rPHat = pHat;
+      }
+    }
     Esum.x += L.x;
     Esum.y += L.y;
     Esum.z += L.z;
@@ -1722,6 +1813,15 @@ inline V3 pt1GatherPoint(const Ctx& c, const V3& P, const V3& N, const V3& Ng, u
       ext->halfSum->y += L.y;
       ext->halfSum->z += L.z;
     }
+  }
+  if (rsv) {  // W = wSum / (M p_hat(selected)), M = every candidate
+    rsv->pos = rPos;
+    rsv->nrm = rNrm;
+    rsv->rad = rRad;
+    rsv->M = static_cast<float>(spp > 0 ? spp : 1);
+    rsv->W = (rPHat > 0.0f && rWSum > 0.0)
+                 ? static_cast<float>(rWSum / (static_cast<double>(rsv->M) * static_cast<double>(rPHat)))
+                 : 0.0f;
   }
   const float invN = 1.0f / static_cast<float>(spp > 0 ? spp : 1);
   if (occOut) *occOut = static_cast<float>(nOcc) * invN;
@@ -2117,6 +2217,7 @@ struct GridPt2 {
   uint32_t sppPow2 = 1;
   int sampleOffset = 0;
   std::vector<float>* halfE = nullptr;
+  std::vector<Reservoir>* rsv = nullptr;  // ReSTIR: one reservoir per grid point
 };
 inline void gatherGrid(const Ctx& c, int W, int H, const float* pos, const float* nrm, const float* gnrm,
                        const uint8_t* mark, const float* dep, int spp, std::vector<float>& E,
@@ -2125,6 +2226,7 @@ inline void gatherGrid(const Ctx& c, int W, int H, const float* pos, const float
   E.assign(n * 3, 0.0f);
   occ.assign(n, 0.0f);
   if (g2.halfE) g2.halfE->assign(n * 3, 0.0f);
+  if (g2.rsv) g2.rsv->assign(n, Reservoir{});
   const uint32_t seedMix = hashU32(c.o.pt1Seed);
   forRows(H, nt, [&](int py) {
     for (int px = 0; px < W; ++px) {
@@ -2151,6 +2253,7 @@ inline void gatherGrid(const Ctx& c, int W, int H, const float* pos, const float
         }
         ext.sampleOffset = g2.sampleOffset;
         if (g2.halfE) ext.halfSum = &half;
+        if (g2.rsv) ext.rsv = &(*g2.rsv)[pix];
       }
       const V3 e = pt1GatherPoint(c, P, N, Ng, seed, tEps, spp, &o, g2.pt2 ? &ext : nullptr);
       E[3 * pix] = e.x; E[3 * pix + 1] = e.y; E[3 * pix + 2] = e.z;
@@ -2349,6 +2452,161 @@ inline void smoothPatchedPixels(int W, int H, const std::vector<uint8_t>& mask, 
     }
 }
 
+// pt2_sampler.hpp:71-78 pt2HashHp
+inline uint32_t hashHp(uint32_t i) {
+  i ^= i >> 16;
+  i *= 0x21f0aaadu;
+  i ^= i >> 15;
+  i *= 0xd35a2d97u;
+  i ^= i >> 15;
+  return i ^ 0xe6fe3bebu;
+}
+
+// pt2_spatial.hpp:66-271 pt2SpatialRound: every eligible point restarts
+// from its own previous-round reservoir and streams in K neighbours (8 in
+// round 0, then 5) on a per-point rotated golden-angle spiral whose radius
+// halves each round (floor 3), rejecting incompatible normals (< 0.5) and
+// depths (> 10 %), empty reservoirs and samples nearer than 4 x the
+// receiver spacing; W is normalised by the balance-heuristic mixture over
+// the contributors (with `unbiased`, a contributor that cannot see the
+// selected sample counts zero).  In the last round (Eout) E is the
+// balance-MIS sum over all contributors' samples; ineligible points keep E.
+inline void spatialRound(const Ctx& c, int W, int H, const float* pos, const float* nrm, const float* dep,
+                         const uint8_t* elig, const std::vector<Reservoir>& in, std::vector<Reservoir>& out,
+                         int round, float* Eout, int nt) {
+  const Opt& o = c.o;
+  const int K = round == 0 ? 8 : 5;
+  float radius = o.pt2Radius / static_cast<float>(1 << round);
+  if (radius < 3.0f) radius = 3.0f;
+  const float kGolden = 2.399963230f;
+  const uint32_t salt = hashHp(hashU32(o.pt1Seed) ^ (0x53504154u + static_cast<uint32_t>(round)));
+  forRows(H, nt, [&](int py) {
+    for (int px = 0; px < W; ++px) {
+      const size_t pix = static_cast<size_t>(py) * W + px;
+      if (!elig[pix]) {
+        out[pix] = Reservoir{};
+        continue;
+      }
+      const V3 P{pos[3 * pix], pos[3 * pix + 1], pos[3 * pix + 2]};
+      const V3 N{nrm[3 * pix], nrm[3 * pix + 1], nrm[3 * pix + 2]};
+      const float d0 = dep[pix];
+      uint32_t s0 = hashHp(static_cast<uint32_t>(pix) ^ salt), s1 = 0x52535452u;
+      Reservoir dst;
+      double wSum = 0.0;
+      float Mtot = 0.0f;
+      V3 cPos[9], cN[9], sPos[9], sRad[9];
+      float cM[9], sW[9], sJ[9];
+      int nc = 0;
+      {
+        const Reservoir& own = in[pix];
+        const float m = own.M > o.pt2MCap ? o.pt2MCap : own.M;
+        const float w = targetPdf(P, N, own.pos, own.rad) * own.W * m;
+        tea2(s0, s1);
+        if (reservoirTake(wSum, Mtot, w, m, u32ToUnorm(s0))) {
+          dst.pos = own.pos;
+          dst.nrm = own.nrm;
+          dst.rad = own.rad;
+        }
+        cPos[nc] = P; cN[nc] = N; cM[nc] = m;
+        sPos[nc] = own.pos; sRad[nc] = own.rad; sW[nc] = own.W; sJ[nc] = 1.0f;
+        ++nc;
+      }
+      tea2(s0, s1);
+      const float rot = u32ToUnorm(s0) * 6.2831853f;
+      for (int k = 0; k < K; ++k) {
+        const float ang = rot + static_cast<float>(k) * kGolden;
+        const float rr = std::sqrt((static_cast<float>(k) + 0.5f) / static_cast<float>(K)) * radius;
+        const int nx = px + static_cast<int>(std::lround(std::cos(ang) * rr));
+        const int ny = py + static_cast<int>(std::lround(std::sin(ang) * rr));
+        if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+        const size_t q = static_cast<size_t>(ny) * W + nx;
+        if (q == pix || !elig[q]) continue;
+        const V3 Nn{nrm[3 * q], nrm[3 * q + 1], nrm[3 * q + 2]};
+        if (dot(N, Nn) < 0.5f) continue;
+        if (std::fabs(d0 - dep[q]) > 0.1f * d0) continue;
+        const Reservoir& nb = in[q];
+        if (nb.M <= 0.0f) continue;
+        const V3 Pn{pos[3 * q], pos[3 * q + 1], pos[3 * q + 2]};
+        const V3 pq{Pn.x - P.x, Pn.y - P.y, Pn.z - P.z};
+        const V3 ps{nb.pos.x - Pn.x, nb.pos.y - Pn.y, nb.pos.z - Pn.z};
+        if (dot(ps, ps) < 4.0f * 4.0f * dot(pq, pq)) continue;
+        const float j = reconnectJacobian(P, Pn, nb.pos, nb.nrm, 10.0f);
+        const float m = nb.M > o.pt2MCap ? o.pt2MCap : nb.M;
+        const float w = targetPdf(P, N, nb.pos, nb.rad) * nb.W * m * j;
+        tea2(s0, s1);
+        if (reservoirTake(wSum, Mtot, w, m, u32ToUnorm(s0))) {
+          dst.pos = nb.pos;
+          dst.nrm = nb.nrm;
+          dst.rad = nb.rad;
+        }
+        cPos[nc] = Pn; cN[nc] = Nn; cM[nc] = m;
+        sPos[nc] = nb.pos; sRad[nc] = nb.rad; sW[nc] = nb.W; sJ[nc] = j;
+        ++nc;
+      }
+      float piSum = 0.0f;
+      if (wSum > 0.0) {
+        for (int k = 0; k < nc; ++k) {
+          float pk = targetPdf(cPos[k], cN[k], dst.pos, dst.rad);
+          if (pk <= 0.0f) continue;
+          if (o.pt2Unbiased) {
+            const V3 toS{dst.pos.x - cPos[k].x, dst.pos.y - cPos[k].y, dst.pos.z - cPos[k].z};
+            const float dist2 = dot(toS, toS);
+            if (dist2 <= 0.0f) continue;
+            const float dist = std::sqrt(dist2);
+            const V3 dir{toS.x / dist, toS.y / dist, toS.z / dist};
+            if (dot(cN[k], dir) <= 0.0f) {
+              pk = 0.0f;
+            } else {
+              const float eps = selfIntersectEps(cPos[k], dir, dist);
+              const V3 O{cPos[k].x + cN[k].x * eps, cPos[k].y + cN[k].y * eps, cPos[k].z + cN[k].z * eps};
+              if (occludedQ(*c.s, O, dir, eps, dist - 2.0f * eps)) pk = 0.0f;
+            }
+          }
+          piSum += pk * cM[k];
+        }
+      }
+      float Wn = 0.0f;
+      if (piSum > 0.0f && wSum > 0.0) Wn = static_cast<float>(wSum) / piSum;
+      dst.W = (o.pt2WClamp > 0.0f && Wn > o.pt2WClamp) ? o.pt2WClamp : Wn;
+      dst.M = Mtot > o.pt2MCap ? o.pt2MCap : Mtot;
+      out[pix] = dst;
+      if (!Eout) continue;
+      V3 E{0.0f, 0.0f, 0.0f};
+      for (int k = 0; k < nc; ++k) {
+        if (sW[k] <= 0.0f || sJ[k] <= 0.0f) continue;
+        const float pq = targetPdf(P, N, sPos[k], sRad[k]);
+        if (pq <= 0.0f) continue;
+        float denom = 0.0f;
+        for (int j2 = 0; j2 < nc; ++j2) denom += cM[j2] * targetPdf(cPos[j2], cN[j2], sPos[k], sRad[k]);
+        if (denom <= 0.0f) continue;
+        const float mis = cM[k] * pq / denom;
+        const float l = lum3(sRad[k]);
+        if (l <= 0.0f) continue;
+        const float g = mis * sW[k] * sJ[k] * (pq / l) * (1.0f / kPiF);
+        E.x += sRad[k].x * g;
+        E.y += sRad[k].y * g;
+        E.z += sRad[k].z * g;
+      }
+      Eout[3 * pix] = E.x;
+      Eout[3 * pix + 1] = E.y;
+      Eout[3 * pix + 2] = E.z;
+    }
+  });
+}
+
+// pt2_spatial.hpp:278-296 pt2SpatialResampleAndResolve: the rounds, ping-pong,
+// the last one writing E
+inline void spatialResample(const Ctx& c, int W, int H, const float* pos, const float* nrm, const float* dep,
+                            const uint8_t* elig, std::vector<Reservoir>& rsv, std::vector<float>& E, int nt) {
+  std::vector<Reservoir> pong(rsv.size());
+  std::vector<Reservoir>* cur = &rsv;
+  std::vector<Reservoir>* nxt = &pong;
+  for (int r = 0; r < c.o.pt2Rounds; ++r) {
+    spatialRound(c, W, H, pos, nrm, dep, elig, *cur, *nxt, r, r == c.o.pt2Rounds - 1 ? E.data() : nullptr, nt);
+    std::swap(cur, nxt);
+  }
+}
+
 // embree_renderer.cpp:560-1086 runPt1GiPass: the gather on the render grid
 // (k = 1) or on a ceil(W/k) x ceil(H/k) grid with its own primary rays (with
 // pt2's adaptive refinement), the denoise of E at gather resolution, the
@@ -2405,10 +2663,13 @@ inline void runPt1GiPass(const Ctx& c, const Cam& cam, int W, int H, const std::
   const int k = std::max(1, o.pt1GatherDiv);
   const int spp = std::max(1, o.pt1Spp);
   const bool pt2 = o.pt2();
-  const bool adapt = pt2 && o.pt2Adaptive && spp >= 2;
+  // ReSTIR rounds (pt2Rounds > 0) exclude adaptive spp (embree_renderer.cpp:626-636)
+  const bool restir = pt2 && o.pt2Rounds > 0;
+  const bool adapt = pt2 && o.pt2Adaptive && !restir && spp >= 2;
   const int extra = adapt ? spp * (std::max(2, o.pt2AdaptiveMul) - 1) : 0;
   std::vector<float> E, occ;
   // the gather over a grid with pt2's adaptive refinement (embree_renderer.cpp:674-706)
+  // or its ReSTIR reservoirs and spatial rounds (:735-767, 861-890)
   auto gather = [&](int gw, int gh, const float* gp, const float* gn, const float* gg, const uint8_t* ge,
                     const float* gd, std::vector<float>& Eo, std::vector<float>& oo) {
     GridPt2 g2;
@@ -2416,7 +2677,10 @@ inline void runPt1GiPass(const Ctx& c, const Cam& cam, int W, int H, const std::
     g2.sppPow2 = nextPow2(static_cast<uint32_t>(spp + extra));
     std::vector<float> halfE;
     if (adapt) g2.halfE = &halfE;
+    std::vector<Reservoir> rsv;
+    if (restir) g2.rsv = &rsv;
     gatherGrid(c, gw, gh, gp, gn, gg, ge, gd, spp, Eo, oo, nt, g2);
+    if (restir) spatialResample(c, gw, gh, gp, gn, gd, ge, rsv, Eo, nt);
     if (!adapt) return;
     std::vector<uint8_t> m0, m1;
     adaptiveMask(gw, gh, Eo, halfE, ge, spp, o.pt2AdaptiveThresh, m0);
@@ -2840,6 +3104,11 @@ int oracle_render_rows(void* sp, const ubr_render_desc* rdsc, ubr_frame* fr, int
   c.o.pt2Adaptive = d.pt2_adaptive != 0;
   c.o.pt2AdaptiveThresh = d.pt2_adaptive_thresh;
   c.o.pt2AdaptiveMul = d.pt2_adaptive_mul;
+  c.o.pt2Rounds = d.pt2_rounds;
+  c.o.pt2Radius = d.pt2_radius;
+  c.o.pt2Unbiased = d.pt2_unbiased != 0;
+  c.o.pt2MCap = d.pt2_m_cap;
+  c.o.pt2WClamp = d.pt2_w_clamp;
   c.o.denoiseIters = d.denoise_iters;
   c.o.denoiseSigmaN = d.denoise_sigma_n;
   c.o.denoiseSigmaZ = d.denoise_sigma_z;

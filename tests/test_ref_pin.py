@@ -93,7 +93,12 @@ def _cases():
             ("pt1_grid3_three_bounces", gi(1, 1, pt1GatherDiv=3, giBounces=3, pt1Ld=False)),
             ("pt2_defaults_ss2", gi(2, 2)), ("pt2_sobol_pattern", gi(2, 1, pt2Pattern=0)),
             ("pt2_mixed_materials_ss2", pt2_mixed(2)), ("pt2_mixed_materials_adaptive", pt2_mixed(1, pt2Adaptive=True)),
-            ("pt2_emissive_mesh", pt2_mixed(1, mesh=True))]
+            ("pt2_emissive_mesh", pt2_mixed(1, mesh=True)),
+            ("pt2_restir_two_rounds_ss2", gi(2, 2, pt2Rounds=2)),
+            ("pt2_restir_unbiased_full_grid", gi(2, 1, pt2Rounds=1, pt1GatherDiv=1, pt2Unbiased=True)),
+            ("pt2_restir_three_rounds_clamped", gi(2, 1, pt2Rounds=3, pt2Radius=6.0, pt2WClamp=4.0, pt2MCap=20.0,
+                                                   pt2Adaptive=True, pt1Spp=6)),
+            ("pt2_restir_emissive_mesh", pt2_mixed(1, mesh=True, pt2Rounds=2, pt2Unbiased=True))]
     return out
 
 

@@ -365,10 +365,13 @@ UBR_D float emissiveHitWeight(const EmitD& el, int kind, uint32_t prim, f3 O, f3
 // (sum of E, number of first bounces that hit or fall below the horizon)
 // over the samples sFirst, sFirst + sStep, ... < spp; `half` gets the sum of
 // those among the first spp/2.
+// ReSTIR (rsv non-null, sFirst 0, sStep 1): every sample is also one
+// candidate streamed, in sample order, into the point's reservoir
+// (pt1_gather.hpp:287-297, 451-470, 486-499).
 template <int KM>
 UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, int nLights, f3 P, f3 N, f3 Ng,
                          float tEps, uint32_t seed, uint32_t px, uint32_t py, int spp, int sFirst, int sStep,
-                         f3& half, uint32_t& rays, uint32_t& nee, uint32_t& ovf) {
+                         f3& half, uint32_t& rays, uint32_t& nee, uint32_t& ovf, float4* rsv = nullptr) {
   const Frame3 f = frameFromNormal(N);
   const float eps = selfIntersectEps(P, N, tEps);
   const f3 O{P.x + N.x * eps, P.y + N.y * eps, P.z + N.z * eps};
@@ -393,6 +396,10 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
   f3 Esum{0.0f, 0.0f, 0.0f};
   half = f3{0.0f, 0.0f, 0.0f};
   int nOcc = 0;
+  uint32_t rs0 = seed ^ 0x52455354u, rs1 = 0x47490001u;
+  double rWSum = 0.0;
+  f3 rPos{0.0f, 0.0f, 0.0f}, rNrm{0.0f, 0.0f, 0.0f}, rRad{0.0f, 0.0f, 0.0f};
+  float rPHat = 0.0f;
   for (int sI = sFirst; sI < spp; sI += sStep) {
     uint32_t s0 = seed, s1 = uint32_t(sI + g.sampleOffset);
     tea2(s0, s1);
@@ -415,6 +422,8 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
     f3 org = O;
     float tnear = eps;
     f3 thr{1.0f, 1.0f, 1.0f}, L{0.0f, 0.0f, 0.0f};
+    f3 candPos{0.0f, 0.0f, 0.0f}, candN{0.0f, 0.0f, 0.0f};
+    bool candValid = false;
     for (int bnc = 1; horizonOk && bnc <= maxB; ++bnc) {
       Ray r{org, wi, tnear, g.maxDist};
       Hit h;
@@ -426,13 +435,29 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
         L.x += thr.x * env.x;
         L.y += thr.y * env.y;
         L.z += thr.z * env.z;
+        if (rsv && bnc == 1) {  // escaped: the candidate sits 1e7 along the segment
+          candPos = f3{O.x + wi.x * 1.0e7f, O.y + wi.y * 1.0e7f, O.z + wi.z * 1.0e7f};
+          candN = neg(wi);
+          candValid = true;
+        }
         break;
       }
       if (bnc == 1) ++nOcc;
       Vertex v;
       if (!evalVertex<KM>(s, lights, nLights, h, org, wi, g.pt2 && g.emissive, g.pt2 ? &s0 : nullptr,
-                          g.pt2 ? &s1 : nullptr, v, nee, ovf))
+                          g.pt2 ? &s1 : nullptr, v, nee, ovf)) {
+        if (rsv && bnc == 1) {  // absorbed by an outline: a zero-radiance candidate at the hit
+          candPos = f3{org.x + wi.x * h.t, org.y + wi.y * h.t, org.z + wi.z * h.t};
+          candN = neg(wi);
+          candValid = true;
+        }
         break;
+      }
+      if (rsv && bnc == 1) {
+        candPos = v.P;
+        candN = v.N;
+        candValid = true;
+      }
       float emW = 1.0f;
       if (emitNee && bnc == 1)
         emW = emissiveHitWeight(g.em, refKind(h.ref), refPrim(h.ref), org, wi, h.t, cand0Cos, h.Ng);
@@ -476,6 +501,21 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
         L.z *= k;
       }
     }
+    if (rsv) {  // RIS weight pi * lum(L): p_hat = lum(L) cos over the cosine pdf
+      float w = 0.0f, pHat = 0.0f;
+      if (candValid && cand0Cos > 0.0f) {
+        pHat = lumOf(L.x, L.y, L.z) * cand0Cos;
+        w = lumOf(L.x, L.y, L.z) * kPiF;
+      }
+      tea2(rs0, rs1);
+      rWSum += double(w);
+      if (w > 0.0f && double(u32ToUnorm(rs0)) * rWSum <= double(w)) {
+        rPos = candPos;
+        rNrm = candN;
+        rRad = L;
+        rPHat = pHat;
+      }
+    }
     Esum.x += L.x;
     Esum.y += L.y;
     Esum.z += L.z;
@@ -484,6 +524,13 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
       half.y += L.y;
       half.z += L.z;
     }
+  }
+  if (rsv) {  // W = wSum / (M p_hat(selected)), M = every candidate
+    const float M = float(spp > 0 ? spp : 1);
+    const float W = (rPHat > 0.0f && rWSum > 0.0) ? float(rWSum / (double(M) * double(rPHat))) : 0.0f;
+    rsv[0] = make_float4(rPos.x, rPos.y, rPos.z, M);
+    rsv[1] = make_float4(rNrm.x, rNrm.y, rNrm.z, W);
+    rsv[2] = make_float4(rRad.x, rRad.y, rRad.z, 0.0f);
   }
   return make_float4(Esum.x, Esum.y, Esum.z, float(nOcc));
 }
@@ -528,7 +575,8 @@ __global__ void __launch_bounds__(128, 8) k_gather(GiP g, DScene s, const LightD
         const uint32_t seed = hashU32(pix ^ g.seedMix);
         const float tEps = pd.w > 0.0f ? pd.w : 1.0f;
         e = gatherPoint<KM>(g, s, lights, nLights, f3{pd.x, pd.y, pd.z}, N, Ng, tEps, seed, pix % uint32_t(grid.W),
-                            pix / uint32_t(grid.W), spp, lane, LANES, half, rays, nee, ovf);
+                            pix / uint32_t(grid.W), spp, lane, LANES, half, rays, nee, ovf,
+                            LANES == 1 && g.rsv ? g.rsv + size_t(kRsvF4) * pix : nullptr);
       }
     }
 #pragma unroll
@@ -950,6 +998,209 @@ __global__ void k_merge(const uint32_t* list, const uint32_t* count, uint32_t n,
   E[p] = make_float4(e.x * wB + r.x * wR, e.y * wB + r.y * wR, e.z * wB + r.z * wR, e.w * wB + r.w * wR);
 }
 
+// ---- pt2 ReSTIR spatial resampling (pt2_reservoir.hpp, pt2_spatial.hpp) ----
+// pt2_sampler.hpp:71-78 pt2HashHp
+UBR_D uint32_t hashHp(uint32_t i) {
+  i ^= i >> 16;
+  i *= 0x21f0aaadu;
+  i ^= i >> 15;
+  i *= 0xd35a2d97u;
+  i ^= i >> 15;
+  return i ^ 0xe6fe3bebu;
+}
+// pt2TargetPdf (pt2_reservoir.hpp:55-63): luminance times the receiver cosine
+UBR_D float targetPdf(f3 P, f3 N, f3 sp, f3 rad) {
+  const f3 d{sp.x - P.x, sp.y - P.y, sp.z - P.z};
+  const float l2 = dot(d, d);
+  if (l2 <= 0.0f) return 0.0f;
+  const float c = dot(N, d) / sqrtf(l2);
+  if (c <= 0.0f) return 0.0f;
+  return lumOf(rad.x, rad.y, rad.z) * c;
+}
+// pt2Jacobian (pt2_reservoir.hpp:72-89): reconnection Jacobian of moving a
+// sample's receiver, cosines at the sample normal, clamped to [0, cap]
+UBR_D float reconnectJacobian(f3 recvNew, f3 recvOld, f3 sp, f3 sn, float cap) {
+  const f3 a{recvNew.x - sp.x, recvNew.y - sp.y, recvNew.z - sp.z};
+  const f3 b{recvOld.x - sp.x, recvOld.y - sp.y, recvOld.z - sp.z};
+  const float ra2 = dot(a, a), rb2 = dot(b, b);
+  if (ra2 <= 0.0f || rb2 <= 0.0f) return 0.0f;
+  const float ca = dot(sn, a) / sqrtf(ra2);
+  const float cb = dot(sn, b) / sqrtf(rb2);
+  if (ca <= 0.0f || cb <= 0.0f) return 0.0f;
+  const float j = (rb2 * ca) / (ra2 * cb);
+  if (!isfinite(j) || j < 0.0f) return 0.0f;
+  return j > cap ? cap : j;
+}
+
+// pt2SpatialRound (pt2_spatial.hpp:66-271), one thread per grid point: the
+// point restarts from its own previous-round reservoir and streams in K
+// neighbours (8 in round 0, then 5) on a golden-angle spiral rotated per
+// point, radius halving per round (floor 3), skipping incompatible normals
+// (< 0.5), depths (> 10 %), empty reservoirs and samples nearer than 4x the
+// receiver spacing; the selection rule runs in double as the reference's
+// wSum does.  W is normalised by the balance-heuristic mixture over the
+// contributors; with `unbiased` a contributor that cannot see the selected
+// sample counts zero (one any-hit ray each).  The last round writes E.xyz as
+// the balance-MIS sum over every contributor's sample.
+struct RsvView {
+  f3 pos, nrm, rad;
+  float M, W;
+};
+UBR_D RsvView loadRsv(const float4* r, uint32_t q) {
+  const float4 a = r[size_t(kRsvF4) * q], b = r[size_t(kRsvF4) * q + 1], c = r[size_t(kRsvF4) * q + 2];
+  return RsvView{f3{a.x, a.y, a.z}, f3{b.x, b.y, b.z}, f3{c.x, c.y, c.z}, a.w, b.w};
+}
+
+template <int KM>
+__global__ void __launch_bounds__(128) k_spatial(GiSpatial sp, DScene sc, GiGrid grid, const float4* in,
+                                                 float4* out, int round, float4* E, unsigned long long* overflow) {
+  const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t n = uint32_t(grid.W) * uint32_t(grid.H);
+  uint32_t ovf = 0;
+  if (pix < n) {
+    const float4 ne = grid.ne[pix];
+    float4* o = out + size_t(kRsvF4) * pix;
+    if (ne.w == 0.0f) {
+      o[0] = o[1] = o[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    } else {
+      const int W = grid.W, H = grid.H, px = int(pix % uint32_t(W)), py = int(pix / uint32_t(W));
+      const int K = round == 0 ? 8 : 5;
+      float radius = sp.radius / float(1 << round);
+      if (radius < 3.0f) radius = 3.0f;
+      const uint32_t salt = hashHp(sp.seedMix ^ (0x53504154u + uint32_t(round)));
+      const float4 pd = grid.pd[pix];
+      const f3 P{pd.x, pd.y, pd.z}, N{ne.x, ne.y, ne.z};
+      const float d0 = pd.w;
+      uint32_t s0 = hashHp(pix ^ salt), s1 = 0x52535452u;
+      f3 dPos{0.0f, 0.0f, 0.0f}, dNrm{0.0f, 0.0f, 0.0f}, dRad{0.0f, 0.0f, 0.0f};
+      double wSum = 0.0;
+      float Mtot = 0.0f;
+      // contributors: receiver geometry and the sample each one offered
+      f3 cPos[9], cN[9], sPos[9], sRad[9];
+      float cM[9], sW[9], sJ[9];
+      int nc = 0;
+      {
+        const RsvView own = loadRsv(in, pix);
+        const float m = own.M > sp.mCap ? sp.mCap : own.M;
+        const float w = targetPdf(P, N, own.pos, own.rad) * own.W * m;
+        tea2(s0, s1);
+        wSum += double(w);
+        Mtot += m;
+        if (w > 0.0f && double(u32ToUnorm(s0)) * wSum <= double(w)) {
+          dPos = own.pos;
+          dNrm = own.nrm;
+          dRad = own.rad;
+        }
+        cPos[0] = P;
+        cN[0] = N;
+        cM[0] = m;
+        sPos[0] = own.pos;
+        sRad[0] = own.rad;
+        sW[0] = own.W;
+        sJ[0] = 1.0f;
+        nc = 1;
+      }
+      tea2(s0, s1);
+      const float rot = u32ToUnorm(s0) * 6.2831853f;
+      for (int k = 0; k < K; ++k) {
+        const float ang = rot + float(k) * 2.399963230f;
+        const float rr = sqrtf((float(k) + 0.5f) / float(K)) * radius;
+        const int nx = px + int(lroundf(cosf(ang) * rr));
+        const int ny = py + int(lroundf(sinf(ang) * rr));
+        if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+        const uint32_t q = uint32_t(ny) * uint32_t(W) + uint32_t(nx);
+        if (q == pix) continue;
+        const float4 nq = grid.ne[q];
+        if (nq.w == 0.0f) continue;
+        const f3 Nn{nq.x, nq.y, nq.z};
+        if (dot(N, Nn) < 0.5f) continue;
+        const float4 pq4 = grid.pd[q];
+        if (fabsf(d0 - pq4.w) > 0.1f * d0) continue;
+        const RsvView nb = loadRsv(in, q);
+        if (nb.M <= 0.0f) continue;
+        const f3 Pn{pq4.x, pq4.y, pq4.z};
+        const f3 dq{Pn.x - P.x, Pn.y - P.y, Pn.z - P.z};
+        const f3 ds{nb.pos.x - Pn.x, nb.pos.y - Pn.y, nb.pos.z - Pn.z};
+        if (dot(ds, ds) < 4.0f * 4.0f * dot(dq, dq)) continue;
+        const float j = reconnectJacobian(P, Pn, nb.pos, nb.nrm, 10.0f);
+        const float m = nb.M > sp.mCap ? sp.mCap : nb.M;
+        const float w = targetPdf(P, N, nb.pos, nb.rad) * nb.W * m * j;
+        tea2(s0, s1);
+        wSum += double(w);
+        Mtot += m;
+        if (w > 0.0f && double(u32ToUnorm(s0)) * wSum <= double(w)) {
+          dPos = nb.pos;
+          dNrm = nb.nrm;
+          dRad = nb.rad;
+        }
+        cPos[nc] = Pn;
+        cN[nc] = Nn;
+        cM[nc] = m;
+        sPos[nc] = nb.pos;
+        sRad[nc] = nb.rad;
+        sW[nc] = nb.W;
+        sJ[nc] = j;
+        ++nc;
+      }
+      // W by the balance-heuristic mixture over the contributors
+      float piSum = 0.0f;
+      if (wSum > 0.0) {
+        const TravScene ts = travOf(sc);
+        for (int k = 0; k < nc; ++k) {
+          float pk = targetPdf(cPos[k], cN[k], dPos, dRad);
+          if (pk <= 0.0f) continue;
+          if (sp.unbiased) {
+            const f3 toS{dPos.x - cPos[k].x, dPos.y - cPos[k].y, dPos.z - cPos[k].z};
+            const float dist2 = dot(toS, toS);
+            if (dist2 <= 0.0f) continue;
+            const float dist = sqrtf(dist2);
+            const f3 dir{toS.x / dist, toS.y / dist, toS.z / dist};
+            if (dot(cN[k], dir) <= 0.0f) {
+              pk = 0.0f;
+            } else {
+              const float eps = selfIntersectEps(cPos[k], dir, dist);
+              const f3 O{cPos[k].x + cN[k].x * eps, cPos[k].y + cN[k].y * eps, cPos[k].z + cN[k].z * eps};
+              Ray r{O, dir, eps, dist - 2.0f * eps};
+              Hit hh;
+              Count cnt;
+              if (traverse<false, KM, true>(ts, r, hh, ovf, &cnt, true)) pk = 0.0f;
+            }
+          }
+          piSum += pk * cM[k];
+        }
+      }
+      float Wn = 0.0f;
+      if (piSum > 0.0f && wSum > 0.0) Wn = float(wSum) / piSum;
+      const float Wd = (sp.wClamp > 0.0f && Wn > sp.wClamp) ? sp.wClamp : Wn;
+      const float Md = Mtot > sp.mCap ? sp.mCap : Mtot;
+      o[0] = make_float4(dPos.x, dPos.y, dPos.z, Md);
+      o[1] = make_float4(dNrm.x, dNrm.y, dNrm.z, Wd);
+      o[2] = make_float4(dRad.x, dRad.y, dRad.z, 0.0f);
+      if (E) {  // last round: every contributor's sample under balance MIS
+        f3 e{0.0f, 0.0f, 0.0f};
+        for (int k = 0; k < nc; ++k) {
+          if (sW[k] <= 0.0f || sJ[k] <= 0.0f) continue;
+          const float pq = targetPdf(P, N, sPos[k], sRad[k]);
+          if (pq <= 0.0f) continue;
+          float denom = 0.0f;
+          for (int j2 = 0; j2 < nc; ++j2) denom += cM[j2] * targetPdf(cPos[j2], cN[j2], sPos[k], sRad[k]);
+          if (denom <= 0.0f) continue;
+          const float mis = cM[k] * pq / denom;
+          const float l = lumOf(sRad[k].x, sRad[k].y, sRad[k].z);
+          if (l <= 0.0f) continue;
+          const float g = mis * sW[k] * sJ[k] * (pq / l) * (1.0f / kPiF);
+          e.x += sRad[k].x * g;
+          e.y += sRad[k].y * g;
+          e.z += sRad[k].z * g;
+        }
+        const float4 e0 = E[pix];
+        E[pix] = make_float4(e.x, e.y, e.z, e0.w);
+      }
+    }
+  }
+  warpCount(overflow, ovf);
+}
+
 // ---- pt2 traced reflection (pt2_reflect.hpp, pt2_glossy.hpp) ----
 UBR_D f3 schlickF3(f3 F0, float u) {
   float c = 1.0f - u;
@@ -1215,7 +1466,8 @@ void giGBuffer(int km, cudaStream_t s, const Params& p, const DScene& sc, int w,
 // blocks per SM (a list's length is known only on the device).
 void giGather(int km, cudaStream_t s, const GiP& g, const DScene& sc, const LightD* lights, int nLights,
               const GiGrid& grid, const uint32_t* list, const uint32_t* listCount, uint32_t n, int spp, float4* E) {
-  const int lanes = spp >= 8 ? 8 : spp >= 4 ? 4 : spp >= 2 ? 2 : 1;
+  // a ReSTIR gather streams each point's samples in order: one thread per point
+  const int lanes = g.rsv ? 1 : spp >= 8 ? 8 : spp >= 4 ? 4 : spp >= 2 ? 2 : 1;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1277,6 +1529,13 @@ void giMaskList(cudaStream_t s, uint32_t n, const uint8_t* mask, uint32_t* list,
 void giMerge(cudaStream_t s, const uint32_t* list, const uint32_t* count, uint32_t n, int spp, int extra,
              const float4* Er, float4* E) {
   k_merge<<<blocks(n, 256), 256, 0, s>>>(list, count, n, spp, extra, Er, E);
+}
+void giSpatialRound(int km, cudaStream_t s, const GiSpatial& sp, const DScene& sc, const GiGrid& grid,
+                    const float4* in, float4* out, int round, float4* E, unsigned long long* overflow) {
+  const uint64_t n = uint64_t(grid.W) * uint64_t(grid.H);
+  byKind(km, [&](auto K) {
+    k_spatial<decltype(K)::value><<<blocks(n, 128), 128, 0, s>>>(sp, sc, grid, in, out, round, E, overflow);
+  });
 }
 void giReflect(int km, cudaStream_t s, const GiP& g, const DScene& sc, const LightD* lights, int nLights,
                const GiGrid& full, const ReflD& r, const GiCam& cam, uint32_t n, float4* color) {

@@ -50,6 +50,21 @@ struct GiP {
   int emissive;        // emission at gather vertices
   float* halfE;        // per grid point: sum of the first spp/2 samples (adaptive), or null
   EmitD em;            // emissive NEE (em.n == 0: none)
+  // ReSTIR candidate reservoirs (pt2Rounds > 0), kRsvF4 float4s per grid
+  // point, or null; a gather that fills them runs one thread per point
+  float4* rsv;
+};
+
+// A ReSTIR reservoir (Pt2Reservoir, integrator/pt2/pt2_reservoir.hpp:36-42)
+// as three float4s: (sample position, M) (sample normal, W) (radiance, 0).
+constexpr int kRsvF4 = 3;
+
+// The spatial rounds' settings (Pt2SpatialParams, pt2_spatial.hpp:51-59).
+struct GiSpatial {
+  int rounds;
+  float radius, mCap, wClamp;
+  int unbiased;
+  uint32_t seedMix;
 };
 
 // A grid the gather runs on, per pixel: the first hit's position and ray
@@ -107,6 +122,10 @@ void giDilate(cudaStream_t s, int W, int H, const uint8_t* in, const float4* ne,
 void giMaskList(cudaStream_t s, uint32_t n, const uint8_t* mask, uint32_t* list, uint32_t* count);
 void giMerge(cudaStream_t s, const uint32_t* list, const uint32_t* count, uint32_t n, int spp, int extra,
              const float4* Er, float4* E);
+// pt2 ReSTIR spatial round `round` over a grid's reservoirs (in -> out); the
+// last round (E non-null) writes E.xyz of the eligible points
+void giSpatialRound(int km, cudaStream_t s, const GiSpatial& sp, const DScene& sc, const GiGrid& grid,
+                    const float4* in, float4* out, int round, float4* E, unsigned long long* overflow);
 // pt2 traced mirror reflection and the glossy GGX gather at the render grid
 void giReflect(int km, cudaStream_t s, const GiP& g, const DScene& sc, const LightD* lights, int nLights,
                const GiGrid& full, const ReflD& r, const GiCam& cam, uint32_t n, float4* color);

@@ -1770,8 +1770,6 @@ ubr_status makeParams(Context* c, const ubr_render_desc& d, Params& p, std::vect
   if (d.gi) {
     if (d.gi_integrator != 1 && d.gi_integrator != 2)
       return setError(c, UBR_INVALID_ARGUMENT, "render desc: gi needs gi_integrator 1 (pt1) or 2 (pt2)");
-    if (d.gi_integrator == 2 && d.pt2_rounds > 0)
-      return setError(c, UBR_INVALID_ARGUMENT, "render desc: pt2 ReSTIR rounds (pt2_rounds > 0) are not built");
     if (d.gi_integrator == 2 && (d.pt2_pattern < 0 || d.pt2_pattern > 1))
       return setError(c, UBR_INVALID_ARGUMENT, "render desc: pt2_pattern must be 0 (Sobol) or 1 (blue noise)");
     if (d.gi_integrator == 2 && d.pt2_reflect && d.pt2_glossy && d.pt2_glossy_spp < 1)
@@ -2649,7 +2647,10 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     gp.em = (pt2 && d0.pt2_emissive && d0.pt2_emissive_nee) ? jobs[0].scene->emit : EmitD{};
     gp.sampleOffset = 0;
     gp.halfE = nullptr;
-    const bool adapt = pt2 && d0.pt2_adaptive && spp >= 2;
+    gp.rsv = nullptr;
+    // ReSTIR rounds exclude adaptive spp (embree_renderer.cpp:626-636)
+    const bool restir = pt2 && d0.pt2_rounds > 0;
+    const bool adapt = pt2 && d0.pt2_adaptive && !restir && spp >= 2;
     const int extra = adapt ? spp * (std::max(2, d0.pt2_adaptive_mul) - 1) : 0;
     auto pow2 = [](uint32_t v) {
       uint32_t q = 1;
@@ -2697,8 +2698,25 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       if (as != UBR_OK) return as;
       GiP g0 = gp;
       g0.halfE = halfE;
+      float4* rsvA = restir ? scratchT<float4>(c, 144, size_t(n) * kRsvF4, as) : nullptr;
+      float4* rsvB = restir ? scratchT<float4>(c, 145, size_t(n) * kRsvF4, as) : nullptr;
+      if (as != UBR_OK) return as;
+      g0.rsv = rsvA;
       giGather(km, s, g0, s1, lt, nL, gr, nullptr, nullptr, n, spp, E);
       ++kernels;
+      if (restir) {
+        // spatial rounds over the reservoirs, ping-pong; the last one writes E
+        // (pt2_spatial.hpp:278-296)
+        const GiSpatial sp{d0.pt2_rounds, d0.pt2_radius, d0.pt2_m_cap, d0.pt2_w_clamp, d0.pt2_unbiased ? 1 : 0,
+                           gp.seedMix};
+        float4* cur = rsvA;
+        float4* nxt = rsvB;
+        for (int r = 0; r < d0.pt2_rounds; ++r) {
+          giSpatialRound(km, s, sp, s1, gr, cur, nxt, r, r == d0.pt2_rounds - 1 ? E : nullptr, gp.overflow);
+          std::swap(cur, nxt);
+          ++kernels;
+        }
+      }
       if (adapt) {
         uint8_t* m0 = scratchT<uint8_t>(c, 130, n, as);
         uint8_t* m1 = scratchT<uint8_t>(c, 131, n, as);
