@@ -495,7 +495,20 @@ def secondary_workloads(args, flush):
     out["differentiable_100k_1024"]["traversal"] = tn
     b.release()
     ctx.close()
-    # workload 3: batched vs one frame per call
+    out["turntable_batch"] = turntable_workload(args, flush)
+    out.update(gi_workload(args, flush))
+    return out
+
+
+def turntable_workload(args, flush):
+    """Workload 3: the 64-frame turntable list rendered as one batch against
+    one frame per call (with and without graph replay), the measured batching
+    ceiling, and the same list at 256^2."""
+    import ctypes as C
+    import torch
+    from umbreon_gb300 import abi, scenes
+    from umbreon_gb300.api import Context, make_render_desc
+    from umbreon_gb300.autotune import autotune
     bases, items = scenes.turntable_batch()
     tune = autotune(items[0][1], items[0][2], pixels=512 * 512)
     res = {"autotune": tune}
@@ -564,9 +577,7 @@ def secondary_workloads(args, flush):
                                                          entry["per_frame_no_graph"]["frames_per_s"], 3)
         entry["pixels"] = int(sum(o.width * o.height for _, _, o in its))
         res[label] = entry
-    out["turntable_batch"] = res
-    out.update(gi_workload(args, flush))
-    return out
+    return res
 
 
 def _knobs(args):

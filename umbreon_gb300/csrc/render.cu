@@ -45,7 +45,8 @@ struct Bufs {
   float4* hitA;       // per queue slot: t, u, v, ref bits
   float4* hitB;       // per queue slot: Ng.xyz
   float4* surfA;      // O.xyz, eps
-  float4* surfB;      // N.xyz, -
+  float4* surfB;      // N.xyz, AO start node
+  float4* surfT;      // AO frame tangent T.xyz (frameFromNormal(N)), written for hits that cast AO
   uint2* surfC;       // pixel, flags (1 hit, 2 AO, 4 shadows)
   uint8_t* occ;       // per slot * raysPerHit
   float* aoT;         // per slot * aoSamples (enhanced AO nearest t)
@@ -105,14 +106,6 @@ UBR_D uint32_t tiledPixel(uint32_t i, uint32_t W, uint32_t H) {
   if (j < rw * fh) return (j / rw) * W + fw + j % rw;
   j -= rw * fh;
   return fh * W + j;  // bottom rows
-}
-// Slot -> global pixel of a round: the queue's entry, else the tiled order of
-// a single frame's full first round, else the slot itself.
-template <bool BATCH>
-UBR_D uint32_t slotPixel(const Params& p, const Bufs& b, const uint32_t* queue, uint32_t i, uint32_t n) {
-  if (queue) return queue[i];
-  if (BATCH || b.coord || n != uint32_t(p.W) * uint32_t(p.H)) return i;
-  return tiledPixel(i, uint32_t(p.W), uint32_t(p.H));
 }
 
 // AO of a coarse grid cell or of an interpolated lookup: openness and the
@@ -195,6 +188,7 @@ struct Batch {
   uint32_t R = 0;         // AO/shadow-ray stride per hit (max over frames)
   uint32_t aoSplit = 0;   // ray index where shadow rays start in the ray order (min AO count)
   uint32_t aoStride = 0;  // enhanced-AO t stride per hit (max over frames)
+  uint32_t nPix = 0;      // hi-res pixels of all frames
 };
 
 // Frame owning global index g in an ascending offset table.
@@ -208,6 +202,23 @@ UBR_D int frameOf(const uint32_t* offs, int n, uint32_t g) {
   return lo;
 }
 
+// Slot -> global pixel of a round: the queue's entry, else, in a full first
+// round (every hi-res pixel of the frame or of each frame of a batch), the
+// tiled order within each frame, else the slot itself.
+template <bool BATCH>
+UBR_D uint32_t slotPixel(const Params& p, const Batch& bt, const Bufs& b, const uint32_t* queue, uint32_t i,
+                         uint32_t n) {
+  if (queue) return queue[i];
+  if (b.coord) return i;
+  if (BATCH) {
+    if (n != bt.nPix) return i;
+    const FrameDesc& fd = bt.frames[frameOf(bt.pixOffs, bt.nFrames, i)];
+    return fd.pixOff + tiledPixel(i - fd.pixOff, uint32_t(fd.p.W), uint32_t(fd.p.H));
+  }
+  if (n != uint32_t(p.W) * uint32_t(p.H)) return i;
+  return tiledPixel(i, uint32_t(p.W), uint32_t(p.H));
+}
+
 // ---------------------------------------------------------------------------
 // kernels
 
@@ -218,7 +229,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_closest(Params p1, DScene s1, 
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t traced = 0, ovf = 0;
   if (i < n) {
-    const uint32_t gpix = slotPixel<BATCH>(p1, b, queue, i, n);
+    const uint32_t gpix = slotPixel<BATCH>(p1, bt, b, queue, i, n);
     const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
@@ -250,7 +261,7 @@ __global__ void __launch_bounds__(128) k_surface(Params p1, DScene s1, Batch bt,
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool cast = false;
   if (i < n) {
-    const uint32_t gpix = slotPixel<BATCH>(p1, b, queue, i, n);
+    const uint32_t gpix = slotPixel<BATCH>(p1, bt, b, queue, i, n);
     const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
@@ -285,6 +296,10 @@ __global__ void __launch_bounds__(128) k_surface(Params p1, DScene s1, Batch bt,
       }
       b.surfA[i] = make_float4(O.x, O.y, O.z, sf.secEps);
       b.surfB[i] = make_float4(sf.N.x, sf.N.y, sf.N.z, __int_as_float(start));
+      if (aoCast) {  // the AO rays' frame, once per hit instead of once per ray
+        const Frame3 fr = frameFromNormal(sf.N);
+        b.surfT[i] = make_float4(fr.t.x, fr.t.y, fr.t.z, 0.0f);
+      }
       // flags: 1 hit, 2 casts AO, 4 casts shadows; bits 8.. the frame index
       // bit 3: principled material (its area-light samples use their own stream)
       const bool pbr = __ldg(&s.mats[sf.mat].model) == 1u;
@@ -327,7 +342,9 @@ UBR_D OccRay occlusionRay(const Params& p, const Bufs& b, uint32_t slot, uint32_
   if (j < p.aoSamples) {
     if (flags & 2u) {
       o.ao = true;
-      const Frame3 f = frameFromNormal(N);
+      // frameFromNormal(N), its tangent computed once per hit
+      const f3 T = ld3(b.surfT[slot]);
+      const Frame3 f{T, cross(N, T), N};
       dir = aoDir(p, f, px, py, j);
       o.grazing = dot(dir, N) < 0.01f;
       o.trace = !o.grazing;
@@ -860,7 +877,7 @@ __global__ void __launch_bounds__(128) k_shade(Params p1, DScene s1, Batch bt, B
   bool push = false;
   uint32_t gpix = 0, capped = 0;
   if (i < n) {
-    gpix = slotPixel<BATCH>(p1, b, queue, i, n);
+    gpix = slotPixel<BATCH>(p1, bt, b, queue, i, n);
     const int f = BATCH ? frameOf(bt.pixOffs, bt.nFrames, gpix) : 0;
     const Params& p = BATCH ? bt.frames[f].p : p1;
     const DScene& s = BATCH ? bt.frames[f].s : s1;
@@ -1546,6 +1563,8 @@ __global__ void __launch_bounds__(128) k_cao_trace(Params pc, DScene s, Bufs b, 
       const int start = boxStartNode(travOf(s), lo, hi);
       b.surfA[cell] = make_float4(O.x, O.y, O.z, eps);
       b.surfB[cell] = make_float4(N.x, N.y, N.z, __int_as_float(start));
+      const Frame3 fr = frameFromNormal(N);
+      b.surfT[cell] = make_float4(fr.t.x, fr.t.y, fr.t.z, 0.0f);
       b.surfC[cell] = make_uint2(cell, 3u);
       cast = true;
     }
@@ -2178,6 +2197,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
   if (secondary) {
     b.surfA = scratchT<float4>(c, 27, nslot, st);
     b.surfB = scratchT<float4>(c, 28, nslot, st);
+    b.surfT = scratchT<float4>(c, 146, nslot, st);
     b.surfC = scratchT<uint2>(c, 29, nslot, st);
     b.occQueue = scratchT<uint32_t>(c, 36, nslot, st);
     b.cursor = scratchT<unsigned long long>(c, 37, 1, st);
@@ -2354,6 +2374,7 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
     bt.R = R;
     bt.aoSplit = aoMin;
     bt.aoStride = aoStride;
+    bt.nPix = uint32_t(npix64);
   }
   if (st != UBR_OK) return st;
   cudaStream_t s = c->stream;
