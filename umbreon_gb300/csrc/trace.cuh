@@ -196,6 +196,23 @@ UBR_D f2x bytePairToFloat2(uint32_t q, int b, f2x bias) {
               bias);
 }
 
+// Slot of the nearest hit internal child (-1: none): the smallest key among
+// the hit slots, a key being the entry distance's bits with the slot in the
+// low three bits (one integer min per child instead of a compare and two
+// selects).  Non-negative floats order as unsigned integers; distances within
+// 8 ulps go to the lower slot.  The visiting order never changes an answer:
+// an any-hit query reports whether some primitive is hit, a closest-hit query
+// the nearest hit with ties to the lowest ids.
+UBR_D int nearestChild(const float (&tmin)[8], uint32_t hitInt) {
+  uint32_t best = 0xFFFFFFFFu;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const uint32_t key = (__float_as_uint(tmin[k]) & ~7u) | uint32_t(k);
+    best = ((hitInt >> k) & 1u) ? min(best, key) : best;
+  }
+  return hitInt ? int(best & 7u) : -1;
+}
+
 // Traversal state of one ray, resumable one node at a time (the persistent
 // occlusion kernel interleaves rays at node granularity).
 struct TravState {
@@ -346,15 +363,7 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
     const uint32_t m = __byte_perm(k < 4 ? meta0 : meta1, 0u, 0x4440u | uint32_t(k & 3));
     primMask |= ((1u << (m >> 5)) - 1u) << (m & 31u);
   }
-  // nearest hit internal child (lowest slot on ties)
-  float nearT = kInfF;
-  int nearK = -1;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const bool nearer = ((hitInt >> k) & 1u) && tminP[k] < nearT;
-    nearT = nearer ? tminP[k] : nearT;
-    nearK = nearer ? k : nearK;
-  }
+  const int nearK = nearestChild(tminP, hitInt);
   // primitives of the hit leaves.  Binary any-hit queries (no filter) of a
   // scene of two analytic kinds split them by kind: all lanes of a warp test
   // one kind, then the other (a mixed loop runs both intersectors in every
@@ -547,14 +556,7 @@ __device__ bool traverseAnyInterleaved(const TravScene& s, const Ray& r, uint32_
     }
     pendBase = primBase;
     pendMask = primMask;
-    float nearT = kInfF;
-    int nearK = -1;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const bool nearer = ((hitInt >> k) & 1u) && tminP[k] < nearT;
-      nearT = nearer ? tminP[k] : nearT;
-      nearK = nearer ? k : nearK;
-    }
+    const int nearK = nearestChild(tminP, hitInt);
     if (nearK >= 0) {
       const uint32_t rest = hitInt & ~(1u << nearK);
       if (rest) {
