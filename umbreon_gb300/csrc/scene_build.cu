@@ -21,6 +21,7 @@
 #include <array>
 #include <chrono>
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <unordered_map>
@@ -59,6 +60,29 @@ struct HostScene {
   uint32_t geomID[4] = {kInvalid, kInvalid, kInvalid, kInvalid};
   bool principled = false;
   bool opaque = true;
+  std::vector<int> openIdx, capIdx;   // scratch of the cylinder split
+
+  // Empty every table but keep its storage: a host thread that builds many
+  // scenes reuses the same pages (first touch of fresh pages was half of the
+  // flatten time of a 40k-primitive scene).
+  void reset() {
+    auto clr = [](auto&... v) { (v.clear(), ...); };
+    clr(pos, nrm, col, idx, triMat, triMatId, sph, rcV, rcIdx, rcFlags, rcClip, ccV, ccIdx, triGroup, mats,
+        openIdx, capIdx);
+    for (int k = 0; k < 4; ++k) clr(color[k], mat[k], fromEdge[k], opacity1[k], group[k], axis[k]);
+    meshMat = baseTri = baseSph = 0;
+    for (int k = 0; k < 4; ++k) geomID[k] = kInvalid;
+    principled = false;
+    opaque = true;
+  }
+  size_t capacityBytes() const {
+    size_t b = 0;
+    auto add = [&](const auto&... v) { ((b += v.capacity() * sizeof(v[0])), ...); };
+    add(pos, nrm, col, idx, triMat, triMatId, sph, rcV, rcIdx, rcFlags, rcClip, ccV, ccIdx, triGroup, mats,
+        openIdx, capIdx);
+    for (int k = 0; k < 4; ++k) add(color[k], mat[k], fromEdge[k], opacity1[k], group[k], axis[k]);
+    return b;
+  }
 };
 
 struct MatKey {
@@ -100,6 +124,36 @@ struct MatTable {
 
 f3 ld3(const float* p, size_t i) { return f3{p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
 
+// The per-primitive side tables of `kind` for n base primitives repeated over
+// ni instances (colour, material index, from-edge flag, group, opacity at the
+// far end), written in place: every instance's block equals the base block.
+template <class MatOf>
+void fillSide(HostScene& s, int kind, size_t n, size_t ni, const float* color, const uint8_t* fromEdge,
+              const uint16_t* group, const float* opacity1, MatOf matOf) {
+  s.color[kind].resize(n * ni);
+  s.mat[kind].resize(n * ni);
+  s.fromEdge[kind].resize(n * ni);
+  s.group[kind].resize(n * ni);
+  if (opacity1) s.opacity1[kind].resize(n * ni);
+  float4* c = s.color[kind].data();
+  uint32_t* m = s.mat[kind].data();
+  uint8_t* fe = s.fromEdge[kind].data();
+  uint16_t* g = s.group[kind].data();
+  std::memcpy(c, color, n * sizeof(float4));
+  for (size_t i = 0; i < n; ++i) m[i] = matOf(i);
+  for (size_t i = 0; i < n; ++i) fe[i] = fromEdge && fromEdge[i] ? 1 : 0;
+  if (group) std::memcpy(g, group, n * sizeof(uint16_t));
+  else std::memset(g, 0, n * sizeof(uint16_t));
+  if (opacity1) std::memcpy(s.opacity1[kind].data(), opacity1, n * sizeof(float));
+  for (size_t ci = 1; ci < ni; ++ci) {
+    std::memcpy(c + ci * n, c, n * sizeof(float4));
+    std::memcpy(m + ci * n, m, n * sizeof(uint32_t));
+    std::memcpy(fe + ci * n, fe, n);
+    std::memcpy(g + ci * n, g, n * sizeof(uint16_t));
+    if (opacity1) std::memcpy(s.opacity1[kind].data() + ci * n, opacity1, n * sizeof(float));
+  }
+}
+
 // curve_build.cpp:41-267, restated: open cylinders are chained into polylines
 // through endpoints quantised at 1e-4 (a vertex of degree 2 continues a chain
 // when group and opacity-gradient kind agree); each chain emits chainLen + 1
@@ -110,7 +164,8 @@ void flattenCylinders(const ubr_scene_desc& d, const std::vector<f3>& offs, Host
                       MatTable& mt) {
   const size_t n = d.cylinder_count;
   if (n == 0) return;
-  std::vector<int> openIdx, capIdx;
+  std::vector<int>& openIdx = s.openIdx;
+  std::vector<int>& capIdx = s.capIdx;
   for (size_t i = 0; i < n; ++i) {
     if (d.cyl_open && d.cyl_open[i]) openIdx.push_back(int(i));
     else capIdx.push_back(int(i));
@@ -206,24 +261,42 @@ void flattenCylinders(const ubr_scene_desc& d, const std::vector<f3>& offs, Host
       s.rcClip.push_back(make_float4(cr.x, cr.y, cr.z, 0.0f));
     }
   }
-  {
-    const size_t nc = capIdx.size() * offs.size();
-    s.ccV.reserve(2 * nc);
-    s.ccIdx.reserve(nc);
-    s.color[kCone].reserve(nc);
-    s.mat[kCone].reserve(nc);
-    s.fromEdge[kCone].reserve(nc);
-    s.opacity1[kCone].reserve(nc);
+  if (capIdx.empty()) return;
+  // capped cylinders: one cone segment each, side tables written in place
+  const size_t nc = capIdx.size(), ni = offs.size();
+  s.ccV.resize(2 * nc * ni);
+  s.ccIdx.resize(nc * ni);
+  s.color[kCone].resize(nc * ni);
+  s.mat[kCone].resize(nc * ni);
+  s.fromEdge[kCone].resize(nc * ni);
+  s.group[kCone].resize(nc * ni);
+  s.opacity1[kCone].resize(nc * ni);
+  for (size_t j = 0; j < nc; ++j) {
+    const int i = capIdx[j];
+    s.color[kCone][j] = make_float4(d.cyl_color[4 * i], d.cyl_color[4 * i + 1], d.cyl_color[4 * i + 2],
+                                    d.cyl_color[4 * i + 3]);
+    s.mat[kCone][j] = mt.get(d.cyl_material[i]);
+    s.fromEdge[kCone][j] = d.cyl_from_edge && d.cyl_from_edge[i] ? 1 : 0;
+    s.group[kCone][j] = grp(i);
+    s.opacity1[kCone][j] = op1(i);
   }
-  for (const f3& off : offs) {
-    for (int i : capIdx) {
-      const uint32_t base = uint32_t(s.ccV.size());
+  for (size_t ci = 1; ci < ni; ++ci) {
+    std::copy_n(s.color[kCone].begin(), nc, s.color[kCone].begin() + ci * nc);
+    std::copy_n(s.mat[kCone].begin(), nc, s.mat[kCone].begin() + ci * nc);
+    std::copy_n(s.fromEdge[kCone].begin(), nc, s.fromEdge[kCone].begin() + ci * nc);
+    std::copy_n(s.group[kCone].begin(), nc, s.group[kCone].begin() + ci * nc);
+    std::copy_n(s.opacity1[kCone].begin(), nc, s.opacity1[kCone].begin() + ci * nc);
+  }
+  for (size_t ci = 0; ci < ni; ++ci) {
+    const f3 off = offs[ci];
+    for (size_t j = 0; j < nc; ++j) {
+      const int i = capIdx[j];
+      const size_t k = ci * nc + j;
       const f3 a = ld3(d.cyl_p0, i) + off, b = ld3(d.cyl_p1, i) + off;
       const float r = d.cyl_radius[i];
-      s.ccV.push_back(make_float4(a.x, a.y, a.z, r));
-      s.ccV.push_back(make_float4(b.x, b.y, b.z, r));
-      s.ccIdx.push_back(base);
-      side(kCone, i);
+      s.ccV[2 * k] = make_float4(a.x, a.y, a.z, r);
+      s.ccV[2 * k + 1] = make_float4(b.x, b.y, b.z, r);
+      s.ccIdx[k] = uint32_t(2 * k);
       if (axisTables) pushAxis(kCone, ld3(d.cyl_p1, i) - ld3(d.cyl_p0, i));
     }
   }
@@ -461,22 +534,20 @@ ubr_status flatten(Context* c, const ubr_scene_desc& d, HostScene& s) {
   }
   if (d.sphere_count > 0) {
     s.geomID[kSphere] = nextGeom++;
-    s.baseSph = uint32_t(d.sphere_count);
-    const size_t ns = d.sphere_count * offs.size();
-    s.sph.reserve(ns);
-    s.color[kSphere].reserve(ns);
-    s.mat[kSphere].reserve(ns);
-    s.fromEdge[kSphere].reserve(ns);
-    for (const f3& off : offs)
-      for (uint64_t i = 0; i < d.sphere_count; ++i) {
+    const size_t n = d.sphere_count, ni = offs.size();
+    s.baseSph = uint32_t(n);
+    s.sph.resize(n * ni);
+    // side tables: one block per instance, all equal to the base spheres'
+    fillSide(s, kSphere, n, ni, d.sphere_color, d.sphere_from_edge, d.sphere_group, nullptr,
+             [&](size_t i) { return mt.get(d.sphere_material[i]); });
+    for (size_t ci = 0; ci < ni; ++ci) {
+      const f3 off = offs[ci];
+      float4* out = s.sph.data() + ci * n;
+      for (size_t i = 0; i < n; ++i) {
         const float* q = d.sphere_center_radius + 4 * i;
-        s.sph.push_back(make_float4(q[0] + off.x, q[1] + off.y, q[2] + off.z, q[3]));
-        s.color[kSphere].push_back(make_float4(d.sphere_color[4 * i], d.sphere_color[4 * i + 1],
-                                               d.sphere_color[4 * i + 2], d.sphere_color[4 * i + 3]));
-        s.mat[kSphere].push_back(mt.get(d.sphere_material[i]));
-        s.fromEdge[kSphere].push_back(d.sphere_from_edge && d.sphere_from_edge[i] ? 1 : 0);
-        s.group[kSphere].push_back(d.sphere_group ? d.sphere_group[i] : uint16_t(0));
+        out[i] = make_float4(q[0] + off.x, q[1] + off.y, q[2] + off.z, q[3]);
       }
+    }
   }
   flattenCylinders(d, offs, s, mt);
   if (!s.rcIdx.empty()) s.geomID[kRound] = nextGeom++;
@@ -1288,7 +1359,18 @@ ubr_status buildScene(Context* c, const ubr_scene_desc& d, Scene** out) {
   const auto t0 = std::chrono::steady_clock::now();
   ubr_status st = validate(c, d);
   if (st != UBR_OK) return st;
-  HostScene hs;
+  // host staging of the flattened tables, reused by this thread's next build
+  // (a copy from pageable memory has left the buffer when cudaMemcpyAsync
+  // returns); released after a build that needed more than 64 MB
+  static thread_local HostScene staging;
+  HostScene& hs = staging;
+  hs.reset();
+  struct Release {
+    HostScene& h;
+    ~Release() {
+      if (h.capacityBytes() > (64u << 20)) h = HostScene();
+    }
+  } release{hs};
   st = flatten(c, d, hs);
   if (st != UBR_OK) return st;
   const auto tFlat = std::chrono::steady_clock::now();
