@@ -207,7 +207,8 @@ int main() {
     c("coarse AO: open quad stays lit", f.color[kC] > 0.3f);
   }
   {  // pt1 GI at its defaults renders (reduced gather grid, denoise, upsample,
-     // edge patch); the irradiance cache is not built and throws
+     // edge patch), pt2 with and without ReSTIR rounds; the irradiance cache
+     // is not built and throws
     umbreon::Scene sc;
     sc.mesh = quad({1, 1, 1, 1});
     sc.camera = cam();
@@ -224,6 +225,10 @@ int main() {
     const umbreon::FrameResult f2 = umbreon::render(sc, o);
     c("pt2 defaults: frame rendered", f2.color.size() == 100 && f2.color[kC] > 0.0f);
     c("pt2 defaults: gather rays counted", f2.pt1Rays.gatherRays > 0);
+    o.pt2Rounds = 2;  // ReSTIR spatial rounds on top of the defaults
+    const umbreon::FrameResult f3 = umbreon::render(sc, o);
+    c("pt2 ReSTIR rounds: frame rendered", f3.color.size() == 100 && f3.color[kC] > 0.0f);
+    o.pt2Rounds = 0;
     o.giIntegrator = 0;
     bool threw = false;
     try {

@@ -463,10 +463,10 @@ __device__ __forceinline__ void occlusionBody(const Params& p1, const DScene& s1
   }
 }
 
-// One thread per AO / shadow ray.  Mesh scenes run 9 blocks per SM (56
-// registers), the others 8 (64 registers): measured best for each.
+// One thread per AO / shadow ray, 9 blocks of 128 per SM (56 registers):
+// measured best for mesh and for sphere + cylinder scenes.
 template <bool COUNT, int KM, bool BATCH>
-__global__ void __launch_bounds__(128, (KM & kMaskMesh) ? 9 : 8)
+__global__ void __launch_bounds__(128, 9)
     k_trace_occlusion(Params p1, DScene s1, Batch bt, Bufs b, uint32_t n) {
   occlusionBody<COUNT, KM, BATCH, false>(p1, s1, bt, b);
 }
