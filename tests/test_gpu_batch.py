@@ -62,3 +62,24 @@ def test_single_frame_graph_replay(gpu_ctx):
         assert np.array_equal(h.color, frames[0].color)
     finally:
         built.release()
+
+
+def test_batch_frames_of_ragged_sizes(gpu_ctx):
+    """Frames whose hi-res grids are not multiples of the 8 x 4 pixel tiles
+    of a first round (a right strip and a bottom band outside the tiles)
+    render in a batch exactly as alone."""
+    a_sc, a_opt = scenes.space_filling(n=500, width=67, height=45)
+    b_sc, b_opt = scenes.ball_and_stick(n=1200, width=53, height=37, supersample=3, ao_samples=4)
+    c_sc, c_opt = scenes.space_filling(n=300, width=13, height=7)
+    items = [(gpu_ctx.build(sc), sc, opt) for sc, opt in ((a_sc, a_opt), (b_sc, b_opt), (c_sc, c_opt))]
+    try:
+        batch, _ = gpu_ctx.render_batch(items)
+        for (built, sc, opt), got in zip(items, batch):
+            ref = gpu_ctx.render(built, sc, opt)
+            assert np.array_equal(got.color, ref.color)
+            assert np.array_equal(got.depth, ref.depth)
+            assert np.array_equal(got.hit_prim, ref.hit_prim)
+            assert np.isfinite(ref.color).all()
+    finally:
+        for built, _, _ in items:
+            built.release()

@@ -54,6 +54,16 @@ def test_ball_and_stick_small(gpu_ctx, oracle_lib):
     _compare(gpu_ctx, oracle_lib, sc, opt)
 
 
+@pytest.mark.parametrize("w,h,ss", [(67, 45, 1), (53, 37, 3), (101, 59, 2)])
+def test_ragged_frame_sizes(gpu_ctx, oracle_lib, w, h, ss):
+    """Hi-res grids that the first round's 8 x 4 pixel tiles do not divide
+    (a right strip and a bottom band rendered outside the tiles): every pixel
+    is rendered once and matches the oracle."""
+    sc, opt = scenes.ball_and_stick(n=1200, width=w, height=h, supersample=ss, ao_samples=4)
+    g, _, _ = _compare(gpu_ctx, oracle_lib, sc, opt)
+    assert g.hit_geom.shape == (h * ss, w * ss) and np.isfinite(g.color).all()
+
+
 def test_perspective_transparent(gpu_ctx, oracle_lib):
     sc, opt = scenes.space_filling(n=600, width=200, height=150)
     sc.sphere_color[:, 3] = 0.5
