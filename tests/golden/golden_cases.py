@@ -41,14 +41,33 @@ def perspective_transparent_160x120():
     return sc, opt
 
 
+def pt2_defaults_ball_and_stick_96x54_ss2():
+    """pt2 GI, the reference's default integrator, every option at its default
+    (reduced gather grid, denoise, upsample, edge patch)."""
+    sc, opt = scenes.ball_and_stick(n=1500, width=96, height=54, supersample=2, ao_samples=4)
+    opt.gi, opt.giIntegrator = True, 2
+    return sc, opt
+
+
+def pt2_restir_two_rounds_64x48():
+    """pt2 with two ReSTIR spatial rounds on the render grid, unbiased."""
+    sc, opt = scenes.ball_and_stick(n=800, width=64, height=48, supersample=1, ao_samples=4)
+    opt.gi, opt.giIntegrator, opt.pt1Spp = True, 2, 4
+    opt.pt2Rounds, opt.pt2Unbiased = 2, True
+    return sc, opt
+
+
 # name -> (generator, uses AO or soft shadows: sample directions come from
-# sin / cos, whose last bit differs between CUDA and the host libm)
+# sin / cos, whose last bit differs between CUDA and the host libm; "gi":
+# path-traced GI, whose gather paths take those directions too)
 CASES = {
     "space_filling_160x120": (space_filling_160x120, False),
     "ball_and_stick_160x90_ss2_ao8": (ball_and_stick_160x90_ss2_ao8, True),
     "molecular_surface_96_ao8_4layers": (molecular_surface_96_ao8_4layers, True),
     "spheres_5k_128_enhanced_ao_fog": (spheres_5k_128_enhanced_ao_fog, True),
     "perspective_transparent_160x120": (perspective_transparent_160x120, False),
+    "pt2_defaults_ball_and_stick_96x54_ss2": (pt2_defaults_ball_and_stick_96x54_ss2, "gi"),
+    "pt2_restir_two_rounds_64x48": (pt2_restir_two_rounds_64x48, "gi"),
 }
 
 

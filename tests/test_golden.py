@@ -8,7 +8,8 @@ under the parity bars of test_gpu_parity.py: first-hit (geomID, primID)
 agreement >= 99.9 %, PSNR >= 45 dB linear and sRGB, max |error| <= 1e-3 on
 output pixels whose subpixels agree on the first hit (at the 0.999 quantile
 and every pixel within 0.3 where AO / soft-shadow sample directions, which
-come from sin / cos, may differ in the last bit).
+come from sin / cos, may differ in the last bit; GI frames at the 99th
+percentile, as the GI parity tests hold them).
 """
 import json
 import sys
@@ -37,7 +38,8 @@ def _bars(color, geom, prim, ref, ss, sampled):
     agree = id_agreement(geom, prim, rg, rp)
     m = agree_mask_final(geom, prim, rg, rp, ss)
     diff = np.abs(color - rc)[m]
-    q = 0.999 if sampled else 1.0
+    # GI: the bars of the GI parity tests (|error| <= 1e-3 at the 99th percentile)
+    q = 0.99 if sampled == "gi" else 0.999 if sampled else 1.0
     err = float(np.quantile(diff, q)) if diff.size else 0.0
     worst = float(diff.max()) if diff.size else 0.0
     info = dict(agree=agree, err=err, worst=worst, psnr_linear=psnr_linear(color, rc),
@@ -45,7 +47,7 @@ def _bars(color, geom, prim, ref, ss, sampled):
     assert agree >= 0.999, info
     assert info["psnr_linear"] >= 45.0 and info["psnr_srgb"] >= 45.0, info
     assert err <= 1e-3, info
-    if sampled:
+    if sampled is True:
         assert worst <= 0.3, info
 
 
