@@ -308,7 +308,7 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
   const float sx = __uint_as_float((hdr & 0xFFu) << 23) * inv.x;
   const float sy = __uint_as_float(((hdr >> 8) & 0xFFu) << 23) * inv.y;
   const float sz = __uint_as_float(((hdr >> 16) & 0xFFu) << 23) * inv.z;
-  const int nInt = int((hdr >> 24) & 0xFu), nCh = int(hdr >> 28);
+  const int nInt = int((hdr >> 24) & 0xFu);
   const float ox = (n0.x - r.org.x) * inv.x, oy = (n0.y - r.org.y) * inv.y, oz = (n0.z - r.org.z) * inv.z;
   const uint32_t childBase = __float_as_uint(n1.x);
   const int primBase = __float_as_int(n1.y);
@@ -350,11 +350,12 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
     up2(mul2(pk2(tmx[0], tmx[1]), grow2), tmaxP[k], tmaxP[k + 1]);
   }
   // slot mask of the hit children; internal children come first (nInt), then
-  // leaves; slots past nCh are empty
+  // leaves.  Slots past the node's children hold inverted boxes (low plane
+  // 255, high plane 0 on every axis), which no ray enters; one that rounding
+  // let through would be a leaf of no primitives, so no mask is applied.
   uint32_t hitMask = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) hitMask |= tminP[k] <= tmaxP[k] ? (1u << k) : 0u;
-  hitMask &= (1u << nCh) - 1u;
   const uint32_t hitInt = hitMask & ((1u << nInt) - 1u);
   // each hit leaf's meta byte (count << 5 | offset) adds its primitives
   uint32_t primMask = 0;
