@@ -14,6 +14,9 @@
 // float order.
 #include <algorithm>
 
+#include <cub/device/device_select.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
 #include "gi.cuh"
 #include "trace.cuh"
 
@@ -794,7 +797,7 @@ __global__ void k_gdn_write(uint32_t n, const uint8_t* valid, const float4* irr,
 // list.  Pixels not eligible get zero.
 __global__ void k_upsample(int W, int H, const float4* fpd, const float4* fne, GiGrid lo, const float4* Elo,
                            float normalPow, float depthScale, int fallbackR, int patchOn, float patchThresh,
-                           float4* E, uint32_t* patchList, uint32_t* patchCount, unsigned long long* holes) {
+                           float4* E, uint8_t* patchFlag, unsigned long long* holes) {
   const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   bool patch = false, hole = false;
   if (pix < uint32_t(W) * uint32_t(H)) {
@@ -868,10 +871,8 @@ __global__ void k_upsample(int W, int H, const float4* fpd, const float4* fne, G
       patch = patch && patchOn;
     }
     E[pix] = out;
+    if (patchFlag) patchFlag[pix] = patch ? 1 : 0;
   }
-  int off;
-  const int base = warpPushBase(patch, patchCount, off);
-  if (patch) patchList[base + off] = pix;
   warpCount(holes, hole ? 1u : 0u);
 }
 
@@ -1501,11 +1502,24 @@ void giDenoiseIter(cudaStream_t s, int W, int H, int step, const uint8_t* valid,
 void giDenoiseWrite(cudaStream_t s, uint32_t n, const uint8_t* valid, const float4* irr, float4* E) {
   k_gdn_write<<<blocks(n, 256), 256, 0, s>>>(n, valid, irr, E);
 }
-void giUpsample(cudaStream_t s, int W, int H, const float4* fpd, const float4* fne, const GiGrid& lo,
-                const float4* Elo, float normalPow, float depthScale, int fallbackR, int patchOn, float patchThresh,
-                float4* E, uint32_t* patchList, uint32_t* patchCount, unsigned long long* holes) {
-  k_upsample<<<blocks(uint64_t(W) * H, 128), 128, 0, s>>>(W, H, fpd, fne, lo, Elo, normalPow, depthScale, fallbackR,
-                                                          patchOn, patchThresh, E, patchList, patchCount, holes);
+size_t giPatchListBytes(uint32_t n) {
+  size_t bytes = 0;
+  cub::DeviceSelect::Flagged(nullptr, bytes, thrust::counting_iterator<uint32_t>(0), static_cast<const uint8_t*>(nullptr),
+                             static_cast<uint32_t*>(nullptr), static_cast<uint32_t*>(nullptr), int(n));
+  return bytes;
+}
+cudaError_t giUpsample(cudaStream_t s, int W, int H, const float4* fpd, const float4* fne, const GiGrid& lo,
+                       const float4* Elo, float normalPow, float depthScale, int fallbackR, int patchOn,
+                       float patchThresh, float4* E, uint8_t* patchFlag, void* listTemp, size_t listTempBytes,
+                       uint32_t* patchList, uint32_t* patchCount, unsigned long long* holes) {
+  const uint32_t n = uint32_t(W) * uint32_t(H);
+  k_upsample<<<blocks(n, 128), 128, 0, s>>>(W, H, fpd, fne, lo, Elo, normalPow, depthScale, fallbackR, patchOn,
+                                            patchThresh, E, patchFlag, holes);
+  if (!patchOn || !patchFlag) return cudaGetLastError();
+  // the pixels to patch, in pixel order (neighbouring rim pixels stay
+  // neighbours in the list the patch gather walks)
+  return cub::DeviceSelect::Flagged(listTemp, listTempBytes, thrust::counting_iterator<uint32_t>(0), patchFlag,
+                                    patchList, patchCount, int(n), s);
 }
 void giSmooth(cudaStream_t s, int W, int H, const uint32_t* list, const uint32_t* count, uint32_t n,
               const float4* fpd, const float4* fne, float normalPow, float depthScale, int radius,

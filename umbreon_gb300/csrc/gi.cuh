@@ -106,9 +106,13 @@ void giDenoiseIter(cudaStream_t s, int W, int H, int step, const uint8_t* valid,
                    const float4* pd, const float4* irr, const float* var, const float* pgrad, float sigmaN,
                    float sigmaZ, float sigmaL, float4* next);
 void giDenoiseWrite(cudaStream_t s, uint32_t n, const uint8_t* valid, const float4* irr, float4* E);
-void giUpsample(cudaStream_t s, int W, int H, const float4* fpd, const float4* fne, const GiGrid& lo,
-                const float4* Elo, float normalPow, float depthScale, int fallbackR, int patchOn, float patchThresh,
-                float4* E, uint32_t* patchList, uint32_t* patchCount, unsigned long long* holes);
+// joint-bilateral upsample of E to the render grid; the pixels that need the
+// edge patch are flagged and listed in pixel order (count on the device)
+size_t giPatchListBytes(uint32_t n);
+cudaError_t giUpsample(cudaStream_t s, int W, int H, const float4* fpd, const float4* fne, const GiGrid& lo,
+                       const float4* Elo, float normalPow, float depthScale, int fallbackR, int patchOn,
+                       float patchThresh, float4* E, uint8_t* patchFlag, void* listTemp, size_t listTempBytes,
+                       uint32_t* patchList, uint32_t* patchCount, unsigned long long* holes);
 void giSmooth(cudaStream_t s, int W, int H, const uint32_t* list, const uint32_t* count, uint32_t n,
               const float4* fpd, const float4* fne, float normalPow, float depthScale, int radius,
               const float4* Esrc, float4* E);

@@ -2769,6 +2769,9 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
       float4* Elo = scratchT<float4>(c, 120, nlo, gs);
       uint32_t* patchList = scratchT<uint32_t>(c, 126, npix, gs);
       uint32_t* patchCount = scratchT<uint32_t>(c, 127, 4, gs);
+      uint8_t* patchFlag = scratchT<uint8_t>(c, 147, npix, gs);
+      const size_t listBytes = giPatchListBytes(npix);
+      void* listTemp = scratchT<uint8_t>(c, 148, listBytes, gs);
       float4* Esnap = d0.pt1_edge_patch ? scratchT<float4>(c, 128, npix, gs) : nullptr;
       if (gs != UBR_OK) return gs;
       UBR_CUDA(c, cudaMemsetAsync(patchCount, 0, 2 * sizeof(uint32_t), s));
@@ -2784,9 +2787,10 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
         if (gs != UBR_OK) return gs;
       }
       cudaEventRecord(c->giEv[3], s);
-      giUpsample(s, p1.W, p1.H, b.giA, b.giB, lo, Elo, d0.pt1_upsample_normal_pow, d0.pt1_upsample_depth_scale,
-                 giDiv <= 2 ? 0 : giDiv, d0.pt1_edge_patch ? 1 : 0, d0.pt1_edge_patch_thresh, Ef, patchList,
-                 patchCount, gp.stats + 3);
+      UBR_CUDA(c, giUpsample(s, p1.W, p1.H, b.giA, b.giB, lo, Elo, d0.pt1_upsample_normal_pow,
+                             d0.pt1_upsample_depth_scale, giDiv <= 2 ? 0 : giDiv, d0.pt1_edge_patch ? 1 : 0,
+                             d0.pt1_edge_patch_thresh, Ef, patchFlag, listTemp, listBytes, patchList, patchCount,
+                             gp.stats + 3));
       ++kernels;
       cudaEventRecord(c->giEv[4], s);
       if (d0.pt1_edge_patch) {
@@ -2847,15 +2851,15 @@ ubr_status runFrames(Context* c, const std::vector<Job>& jobs, ubr_frame* total,
             float4* pdo = scratchT<float4>(c, 137, no, gs);
             float4* neo = scratchT<float4>(c, 138, no, gs);
             float4* gne = scratchT<float4>(c, 139, npix, gs);
-            uint32_t* dummy = scratchT<uint32_t>(c, 140, 4, gs);
             if (gs != UBR_OK) return gs;
             giGlossyDown(s, p1.W, p1.H, ssg, b.rfl, Es, b.giA, b.giB, Eo, pdo, neo);
             gs = denoiseE(Wo, Ho, Eo, neo, pdo);
             if (gs != UBR_OK) return gs;
             giGlossyElig(s, npix, b.rfl, b.giB, gne);
             const GiGrid go{Wo, Ho, pdo, neo, nullptr};
-            giUpsample(s, p1.W, p1.H, b.giA, gne, go, Eo, d0.pt1_upsample_normal_pow, d0.pt1_upsample_depth_scale, 0,
-                       0, 0.0f, Es, dummy, dummy, gp.stats + 3);
+            UBR_CUDA(c, giUpsample(s, p1.W, p1.H, b.giA, gne, go, Eo, d0.pt1_upsample_normal_pow,
+                                   d0.pt1_upsample_depth_scale, 0, 0, 0.0f, Es, nullptr, nullptr, 0, nullptr,
+                                   nullptr, gp.stats + 3));
             kernels += 3;
           }
         }
