@@ -6,12 +6,14 @@
 // and the pt2 extensions layered onto the same gather (integrator/pt2/):
 // the Owen-scrambled Sobol / blue-noise first bounce, area-light NEE jitter,
 // emission at gather vertices, emissive-primitive NEE with MIS, traced mirror
-// and glossy reflection, variance-adaptive spp.
+// and glossy reflection, variance-adaptive spp, ReSTIR spatial rounds
+// (integrator/pt2/pt2_reservoir.hpp, pt2_spatial.hpp).
 //
-// Every gather point is one thread (128 per block); its streams are pure
-// functions of (grid index, sample index, pt1Seed), as in the reference, so
-// the oracle draws the same samples and the frames agree up to traversal
-// float order.
+// Up to eight lanes share a gather point, each taking every eighth sample (a
+// ReSTIR gather, whose reservoir streams the samples in order, runs one
+// thread per point); every stream is a pure function of (grid index, sample
+// index, pt1Seed), as in the reference, so the oracle draws the same samples
+// and the frames agree up to traversal float order.
 #include <algorithm>
 
 #include <cub/device/device_select.cuh>
