@@ -89,12 +89,6 @@ UBR_D void sobol2D(uint32_t index, uint32_t seed, float& u1, float& u2) {
   u1 = sobolDim(index, 0, seed ^ 0xe0aaaf76u);
   u2 = sobolDim(index, 1, seed ^ 0x94964d4eu);
 }
-UBR_D uint32_t nextPow2(uint32_t n) {
-  uint32_t p = 1;
-  while (p < n) p <<= 1;
-  return p;
-}
-
 // environmentRadiance (irradiance_cache.hpp:188-196): the gather's miss term.
 UBR_D f3 giEnvironment(const GiP& g, f3 wi) {
   const float w = 0.5f * (dot(wi, g.envUp) + 1.0f);
