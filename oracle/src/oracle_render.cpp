@@ -243,8 +243,6 @@ void buildEmitters(const ubr_scene_desc& d, const std::vector<V3>& offs, Scene& 
   s.emCdf.back() = 1.0f;
 }
 
-float roundKey(float x) { return x; }
-
 // render/curve_build.cpp:41-267 buildCylinderGeometry (open chains + capped)
 void buildCylinders(const ubr_scene_desc& d, const std::vector<V3>& offs, Scene& s) {
   const size_t n = d.cylinder_count;
