@@ -544,6 +544,21 @@ UBR_D float4 gatherPoint(const GiP& g, const DScene& s, const LightD* lights, in
 // origins (coherent node fetches, as the AO rays of one hit), and a short
 // list (the edge patch) still fills the GPU.  The lanes' sums meet in a
 // shuffle tree, so E is the same mean summed in another order.
+// point i of a grid in 2 x 2 quads (a warp's four points form one quad), the
+// odd column and row in row order: a bijection on [0, W H)
+UBR_D uint32_t quadPixel(uint32_t i, uint32_t W, uint32_t H) {
+  const uint32_t fw = W & ~1u, fh = H & ~1u, nt = fw * fh;
+  if (i < nt) {
+    const uint32_t t = i >> 2, k = i & 3u, qx = fw >> 1;
+    return ((t / qx) * 2u + (k >> 1)) * W + (t % qx) * 2u + (k & 1u);
+  }
+  uint32_t j = i - nt;
+  const uint32_t rw = W - fw;
+  if (j < rw * fh) return (j / rw) * W + fw + j % rw;
+  j -= rw * fh;
+  return fh * W + j;
+}
+
 template <int KM, int LANES>
 __global__ void __launch_bounds__(128, 8) k_gather(GiP g, DScene s, const LightD* lights, int nLights, GiGrid grid,
                                                 const uint32_t* list, const uint32_t* listCount, uint32_t n, int spp,
@@ -561,7 +576,7 @@ __global__ void __launch_bounds__(128, 8) k_gather(GiP g, DScene s, const LightD
     f3 half{0.0f, 0.0f, 0.0f};
     uint32_t pix = 0;
     if (i < cnt) {
-      pix = list ? list[i] : i;
+      pix = list ? list[i] : quadPixel(i, uint32_t(grid.W), uint32_t(grid.H));
       const float4 ne = grid.ne[pix];
       if (ne.w != 0.0f) {
         const float4 pd = grid.pd[pix];
