@@ -120,3 +120,27 @@ def test_bench_refuses_a_rank_count_that_does_not_match_gpus(tmp_path):
     r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--impl", "reference"],
                        env=env, capture_output=True, text=True, timeout=120)
     assert r.returncode != 0 and "--gpus 2 but 1 ranks" in r.stderr
+
+
+def test_clock_summary_keeps_the_timed_region_samples():
+    """The clock record of a bench line: the median SM clock and the throttle
+    reasons of the samples taken inside the timed region; a region shorter
+    than one sampling period reports the sample taken just before it."""
+    import importlib.util
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    c = bench.ClockSampler(0)
+    c.before = ["0, 1980, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active"]
+    c.lines = ["0, 2070, 2070, 1000.0, 0x4, Not Active, Not Active, Not Active, Active",
+               "0, 2040, 2070, 1100.0, 0x4, Not Active, Not Active, Not Active, Active",
+               "0, 2055, 2070, 1050.0, 0x0, Not Active, Not Active, Not Active, Not Active"]
+    s = c.summary()
+    assert s["sm_mhz"] == 2055.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"] and s["samples"] == 3
+    c.lines = []
+    s = c.summary()
+    assert s["sm_mhz"] == 1980.0 and s["samples"] == 0 and s["reasons"] == []
+    c.before = []
+    assert c.summary()["reasons"] == ["unsampled"]
