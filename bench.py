@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import copy
+import hashlib
 import json
 import math
 import os
@@ -128,6 +129,36 @@ class ClockSampler:
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm) if inside else 0, "interval_ms": 25}
+
+
+# the sources that define the trace kernels and their build flags: a DRAM
+# traffic figure captured by ncu holds for the kernels these files built
+TRAFFIC_SOURCES = ("umbreon_gb300/csrc/render.cu", "umbreon_gb300/csrc/trace.cuh",
+                   "umbreon_gb300/csrc/ubr_internal.h", "umbreon_gb300/csrc/gi.cuh", "umbreon_gb300/build.py")
+
+
+def kernel_digest() -> str:
+    h = hashlib.sha256()
+    for f in TRAFFIC_SOURCES:
+        h.update((ROOT / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def _traffic(kernel: str, rays: int):
+    """DRAM bytes of one launch of `kernel`: the committed ncu capture's bytes
+    per ray times the rays this launch traced, and whether the capture was of
+    the kernels built from the current sources."""
+    tfile = ROOT / "profiles" / "traffic.json"
+    if not tfile.exists():
+        return None, None
+    d = json.loads(tfile.read_text()).get(kernel)
+    if not isinstance(d, dict):
+        return None, None
+    cap = d["capture"]
+    per_ray = cap["dram_bytes"] / cap["rays"]
+    info = {"dram_bytes_per_ray": round(per_ray, 3), "captured_rays": cap["rays"],
+            "captured_workload": cap["workload"], "current": d.get("kernel_digest") == kernel_digest()}
+    return int(round(per_ray * rays)), info
 
 
 def _peaks():
@@ -730,13 +761,13 @@ def run_ours(args):
     roof = None
     if alg is not None:
         achieved = alg / (per_launch_ms / 1e3) / 1e9
-        traffic = None
-        tfile = ROOT / "profiles" / "traffic.json"
-        if tfile.exists():
-            traffic = json.loads(tfile.read_text()).get(names[dom])
+        # DRAM traffic: an ncu capture of a smaller frame, scaled to this
+        # launch by the rays it traced; `traffic_source.current` is false when
+        # the kernel sources changed after the capture
+        traffic, tinfo = _traffic(names[dom], ctr["rays"][1 if dom == 2 else 0])
         roof = {"bound": "hbm", "kernel": f"k_{names[dom]}", "achieved": round(achieved, 1), "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": traffic, "algorithmic_bytes_per_launch": int(alg),
+                "traffic": traffic, "traffic_source": tinfo, "algorithmic_bytes_per_launch": int(alg),
                 "launch_ms": round(per_launch_ms, 3)}
         lim = ROOT / "profiles" / "limiter.json"
         if lim.exists():

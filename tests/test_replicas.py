@@ -144,3 +144,30 @@ def test_clock_summary_keeps_the_timed_region_samples():
     assert s["sm_mhz"] == 1980.0 and s["samples"] == 0 and s["reasons"] == []
     c.before = []
     assert c.summary()["reasons"] == ["unsampled"]
+
+
+def test_roofline_traffic_scales_the_capture_and_flags_stale_sources(tmp_path, monkeypatch):
+    """roofline.traffic: the committed ncu capture's DRAM bytes per ray times
+    the rays of the timed launch; `current` says whether the trace kernels'
+    sources still match the capture's digest."""
+    import importlib.util
+    import json
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("bench_mod2", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    committed = json.loads(open(os.path.join(root, "profiles", "traffic.json")).read())["trace_occlusion"]
+    assert committed["capture"]["rays"] > 0 and committed["capture"]["dram_bytes"] > 0
+    (tmp_path / "profiles").mkdir()
+    for f in bench.TRAFFIC_SOURCES:
+        (tmp_path / f).parent.mkdir(parents=True, exist_ok=True)
+        (tmp_path / f).write_text("kernel v1\n")
+    monkeypatch.setattr(bench, "ROOT", tmp_path)
+    rec = {"trace_occlusion": {"capture": {"dram_bytes": 5000, "rays": 1000, "workload": "w"},
+                               "kernel_digest": bench.kernel_digest()}}
+    (tmp_path / "profiles" / "traffic.json").write_text(json.dumps(rec))
+    t, info = bench._traffic("trace_occlusion", 4000)
+    assert t == 20000 and info["dram_bytes_per_ray"] == 5.0 and info["current"] is True
+    (tmp_path / bench.TRAFFIC_SOURCES[1]).write_text("kernel v2\n")
+    assert bench._traffic("trace_occlusion", 4000)[1]["current"] is False
+    assert bench._traffic("trace_closest", 4000) == (None, None)
