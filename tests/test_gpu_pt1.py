@@ -67,6 +67,24 @@ def test_lone_sphere_known_answer(gpu_ctx):
     np.testing.assert_allclose(col[hit], np.broadcast_to(want, col[hit].shape), rtol=1e-5, atol=1e-6)
 
 
+@pytest.mark.parametrize("integrator", [1, 2])
+def test_enclosed_sphere_known_answers(gpu_ctx, integrator):
+    """The closed-form answers of the sphere inside a shadowing shell (every
+    gather path ends on the shell, whose NEE is shadowed: E = 0; with
+    giMaxDistance short of the shell: E = the sky), on the GPU."""
+    from test_oracle_pt1 import enclosed_known_answers
+
+    def render(sc, opt):
+        b = gpu_ctx.build(sc)
+        try:
+            g = gpu_ctx.render(b, sc, opt)
+        finally:
+            b.release()
+        prim = np.where(g.hit_geom.reshape(32, 32) == KINVALID, -1, g.hit_prim.reshape(32, 32).astype(np.int64))
+        return g.color.reshape(32, 32, 4)[..., :3], prim
+    enclosed_known_answers(render, rtol=1e-5, integrator=integrator)
+
+
 @pytest.mark.parametrize("case", ["one_bounce_ld", "three_bounces_tea2"])
 def test_space_filling_gi(gpu_ctx, oracle_lib, case):
     sc, opt = scenes.space_filling(n=600, width=96, height=72)

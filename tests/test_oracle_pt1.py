@@ -21,8 +21,8 @@ def _lone_sphere(**kw):
     mat = scenes.pov_material()
     sc = scenes.material_sphere_scene((0.6, 0.4, 0.2, 1.0), mat, (0.0, 0.0, 0.0))
     sc.lights = []
-    opt = RenderOptions(width=32, height=32, supersample=1, gi=True, giIntegrator=1, pt1Denoise=False,
-                        pt1GatherDiv=1, **kw)
+    kw.setdefault("giIntegrator", 1)
+    opt = RenderOptions(width=32, height=32, supersample=1, gi=True, pt1Denoise=False, pt1GatherDiv=1, **kw)
     return sc, opt, float(mat["diffuse"])
 
 
@@ -224,3 +224,48 @@ def test_pt2_emitter_lights_a_neighbour(oracle_lib):
     assert b == 0.0 and a > 0.0 and c > 0.0
     # both estimators are unbiased: their means agree within Monte-Carlo noise
     assert abs(a - c) < 0.15 * a
+
+
+def _enclosed_sphere(**kw):
+    """The lone sphere inside a closed spherical shell (radius 50, camera
+    inside it), lit by the key light with shadows: every gather ray ends on
+    the shell, and every shadow ray (the primary one and the NEE one at a
+    shell vertex) is blocked by the shell."""
+    sc, opt, kd = _lone_sphere(shadows=True, **kw)
+    sc.sphere_center_radius = np.array([[0, 0, 0, 1], [0, 0, 0, 50]], np.float32)
+    sc.sphere_color = np.array([[0.6, 0.4, 0.2, 1.0], [0.9, 0.9, 0.9, 1.0]], np.float32)
+    sc.sphere_material = np.concatenate([sc.sphere_material] * 2)
+    from umbreon_gb300.scenes import key_light
+    sc.lights = [key_light()]
+    return sc, opt, kd
+
+
+def enclosed_known_answers(render, rtol=1e-6, integrator=1):
+    """Closed-form pt1 answers on the enclosed sphere (pt1_gather.hpp:336-420,
+    pt1EvalVertex :117-220): (1) every gather path ends on the shell, whose
+    vertices' NEE is shadowed, so E = 0 and the inner sphere's pixels are
+    exactly 0 at any bounce count; (2) with giMaxDistance below the gap to
+    the shell every gather ray misses, so E is the sky exactly, as for the
+    lone sphere.  The same holds for pt2 (`integrator` 2), whose extensions
+    add no light here (no emitters, no glossy lobe, a point-like light).
+    `render(scene, options)` returns (colour HxWx3, hit prim)."""
+    for bounces in (1, 2, 3):
+        sc, opt, kd = _enclosed_sphere(pt1Spp=8, giBounces=bounces, giIntegrator=integrator)
+        col, prim = render(sc, opt)
+        inner = prim == 0
+        assert int(inner.sum()) > 50
+        assert np.all(col[inner] == 0.0), (bounces, float(np.abs(col[inner]).max()))
+    sc, opt, kd = _enclosed_sphere(pt1Spp=8, giBounces=2, giMaxDistance=10.0, giIntegrator=integrator)
+    col, prim = render(sc, opt)
+    inner = prim == 0
+    want = kd * np.array([0.6, 0.4, 0.2], np.float32)
+    np.testing.assert_allclose(col[inner], np.broadcast_to(want, col[inner].shape), rtol=rtol, atol=rtol / 10)
+
+
+@pytest.mark.parametrize("integrator", [1, 2])
+def test_enclosed_sphere_known_answers(oracle_lib, integrator):
+    def render(sc, opt):
+        o = oracle_lib.render(sc, opt)
+        prim = np.where(o.hit_geom.reshape(32, 32) == KINVALID, -1, o.hit_prim.reshape(32, 32).astype(np.int64))
+        return o.color.reshape(32, 32, 4)[..., :3], prim
+    enclosed_known_answers(render, integrator=integrator)
