@@ -400,6 +400,19 @@ UBR_D void occlusionWrite(const Params& p, const Bufs& b, uint64_t R, uint64_t a
 // one light's rays of 32 neighbouring hits, one direction).  A bijection onto
 // [0, nq) x [0, R) for any split A.
 UBR_D void occRayOf(uint64_t rid, uint32_t nq, uint64_t R, uint64_t A, uint32_t& q, int& j) {
+  if ((uint64_t(nq) * R) >> 32 == 0) {
+    // every ray id of the launch fits 32 bits (warp-uniform): 32-bit division
+    const uint32_t r32 = uint32_t(rid), a32 = uint32_t(A), nAo32 = nq * a32;
+    if (r32 < nAo32) {
+      q = r32 / a32;
+      j = int(r32 - q * a32);
+    } else {
+      const uint32_t t = r32 - nAo32, d = t / nq;
+      q = t - d * nq;
+      j = int(a32 + d);
+    }
+    return;
+  }
   const uint64_t nAo = uint64_t(nq) * A;
   if (rid < nAo) {
     q = uint32_t(rid / A);

@@ -330,7 +330,8 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
   const f2x bias2 = pk2(-8388608.0f, -8388608.0f), grow2 = pk2(kSlabGrow, kSlabGrow);
   const f2x sx2 = pk2(sx, sx), sy2 = pk2(sy, sy), sz2 = pk2(sz, sz);
   const f2x ox2 = pk2(ox, ox), oy2 = pk2(oy, oy), oz2 = pk2(oz, oz);
-  float tminP[8], tmaxP[8];
+  float tminP[8];
+  uint32_t gap[8];  // bits of tmax * grow - tmin per slot: sign clear = hit
 #pragma unroll
   for (int k = 0; k < 8; k += 2) {
     const int w = k >> 2, b = k & 3;
@@ -347,15 +348,18 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
       tminP[k + j] = fmaxf(fmaxf(tnx[j], tny[j]), fmaxf(tnz[j], r.tnear));
       tmx[j] = fminf(fminf(tfx[j], tfy[j]), fminf(tfz[j], st.tmax));
     }
-    up2(mul2(pk2(tmx[0], tmx[1]), grow2), tmaxP[k], tmaxP[k + 1]);
+    float g0, g1;
+    up2(fma2(pk2(tmx[0], tmx[1]), grow2, pk2(-tminP[k], -tminP[k + 1])), g0, g1);
+    gap[k] = __float_as_uint(g0);
+    gap[k + 1] = __float_as_uint(g1);
   }
-  // slot mask of the hit children; internal children come first (nInt), then
-  // leaves.  Slots past the node's children hold inverted boxes (low plane
-  // 255, high plane 0 on every axis), which no ray enters; one that rounding
-  // let through would be a leaf of no primitives, so no mask is applied.
-  uint32_t hitMask = 0;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) hitMask |= tminP[k] <= tmaxP[k] ? (1u << k) : 0u;
+  // slot mask of the hit children: the sign bytes of the eight gaps gathered
+  // into two words, their sign bits moved to bits 28-31 by one multiply
+  // (partial products land on distinct bits below 28, so nothing carries).
+  const uint32_t sx4 = __byte_perm(__byte_perm(gap[0], gap[1], 0x0073u), __byte_perm(gap[2], gap[3], 0x0073u), 0x5410u);
+  const uint32_t sy4 = __byte_perm(__byte_perm(gap[4], gap[5], 0x0073u), __byte_perm(gap[6], gap[7], 0x0073u), 0x5410u);
+  const uint32_t neg = (((sx4 & 0x80808080u) * 0x00204081u) >> 28) | ((((sy4 & 0x80808080u) * 0x00204081u) >> 24) & 0xF0u);
+  const uint32_t hitMask = ~neg & 0xFFu;
   const uint32_t hitInt = hitMask & ((1u << nInt) - 1u);
   // each hit leaf's meta byte (count << 5 | offset) adds its primitives
   uint32_t primMask = 0;
