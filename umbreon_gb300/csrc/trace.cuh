@@ -289,7 +289,7 @@ UBR_D bool travStep(const TravScene& s, const Ray& r, const f3& inv, const TriPr
   }
   if (COUNT) ++cnt->nodes;
   float4 n0, n1, n2, n3, n4;
-  if (st.node < nTop) {
+  if (nTop > 0 && st.node < nTop) {  // folds away where no nodes are staged
     const float4* nd = top + kWideF4 * st.node;
     n0 = nd[0];
     n1 = nd[1];
