@@ -18,6 +18,8 @@
 
 #include <cub/device/device_select.cuh>
 #include <thrust/iterator/counting_iterator.h>
+#include <thrust/iterator/permutation_iterator.h>
+#include <thrust/iterator/transform_iterator.h>
 
 #include "gi.cuh"
 #include "trace.cuh"
@@ -1513,9 +1515,32 @@ void giDenoiseIter(cudaStream_t s, int W, int H, int step, const uint8_t* valid,
 void giDenoiseWrite(cudaStream_t s, uint32_t n, const uint8_t* valid, const float4* irr, float4* E) {
   k_gdn_write<<<blocks(n, 256), 256, 0, s>>>(n, valid, irr, E);
 }
+// Pixel i of a W x H grid in 16 x 16 tiles (row order inside a tile, tiles in
+// row order), the columns and rows past the last whole tile in row order: a
+// bijection on [0, W H).  The edge-patch list walks its pixels in this order,
+// so the points a warp gathers lie on one stretch of an edge.
+struct TileOrder {
+  uint32_t W, H;
+  UBR_HD uint32_t operator()(uint32_t i) const {
+    const uint32_t fw = W & ~15u, fh = H & ~15u, nt = fw * fh;
+    if (i < nt) {
+      const uint32_t t = i >> 8, k = i & 255u, tx = fw >> 4;
+      return ((t / tx) * 16u + (k >> 4)) * W + (t % tx) * 16u + (k & 15u);
+    }
+    uint32_t j = i - nt;
+    const uint32_t rw = W - fw;
+    if (j < rw * fh) return (j / rw) * W + fw + j % rw;
+    j -= rw * fh;
+    return fh * W + j;
+  }
+};
+using TileIt = thrust::transform_iterator<TileOrder, thrust::counting_iterator<uint32_t>>;
+using TileFlagIt = thrust::permutation_iterator<const uint8_t*, TileIt>;
+
 size_t giPatchListBytes(uint32_t n) {
   size_t bytes = 0;
-  cub::DeviceSelect::Flagged(nullptr, bytes, thrust::counting_iterator<uint32_t>(0), static_cast<const uint8_t*>(nullptr),
+  const TileIt in(thrust::counting_iterator<uint32_t>(0), TileOrder{n, 1});
+  cub::DeviceSelect::Flagged(nullptr, bytes, in, TileFlagIt(static_cast<const uint8_t*>(nullptr), in),
                              static_cast<uint32_t*>(nullptr), static_cast<uint32_t*>(nullptr), int(n));
   return bytes;
 }
@@ -1527,10 +1552,11 @@ cudaError_t giUpsample(cudaStream_t s, int W, int H, const float4* fpd, const fl
   k_upsample<<<blocks(n, 128), 128, 0, s>>>(W, H, fpd, fne, lo, Elo, normalPow, depthScale, fallbackR, patchOn,
                                             patchThresh, E, patchFlag, holes);
   if (!patchOn || !patchFlag) return cudaGetLastError();
-  // the pixels to patch, in pixel order (neighbouring rim pixels stay
+  // the pixels to patch, in 16 x 16 tile order (neighbouring rim pixels stay
   // neighbours in the list the patch gather walks)
-  return cub::DeviceSelect::Flagged(listTemp, listTempBytes, thrust::counting_iterator<uint32_t>(0), patchFlag,
-                                    patchList, patchCount, int(n), s);
+  const TileIt in(thrust::counting_iterator<uint32_t>(0), TileOrder{uint32_t(W), uint32_t(H)});
+  return cub::DeviceSelect::Flagged(listTemp, listTempBytes, in, TileFlagIt(patchFlag, in), patchList, patchCount,
+                                    int(n), s);
 }
 void giSmooth(cudaStream_t s, int W, int H, const uint32_t* list, const uint32_t* count, uint32_t n,
               const float4* fpd, const float4* fne, float normalPow, float depthScale, int radius,
