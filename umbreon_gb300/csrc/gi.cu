@@ -561,6 +561,24 @@ UBR_D uint32_t quadPixel(uint32_t i, uint32_t W, uint32_t H) {
   return fh * W + j;
 }
 
+// point i of a grid in 4 x 4 tiles of 2 x 2 quads (32 points, a warp of one
+// thread per point, cover two adjacent tiles: an 8 x 4 block), the columns
+// and rows past the last whole tile in row order: a bijection on [0, W H)
+UBR_D uint32_t tilePixel4(uint32_t i, uint32_t W, uint32_t H) {
+  const uint32_t fw = W & ~3u, fh = H & ~3u, nt = fw * fh;
+  if (i < nt) {
+    const uint32_t t = i >> 4, k = i & 15u, tx = fw >> 2;
+    const uint32_t x = (t % tx) * 4u + ((k >> 1) & 2u) + (k & 1u);
+    const uint32_t y = (t / tx) * 4u + ((k >> 2) & 2u) + ((k >> 1) & 1u);
+    return y * W + x;
+  }
+  uint32_t j = i - nt;
+  const uint32_t rw = W - fw;
+  if (j < rw * fh) return (j / rw) * W + fw + j % rw;
+  j -= rw * fh;
+  return fh * W + j;
+}
+
 template <int KM, int LANES>
 __global__ void __launch_bounds__(128, 8) k_gather(GiP g, DScene s, const LightD* lights, int nLights, GiGrid grid,
                                                 const uint32_t* list, const uint32_t* listCount, uint32_t n, int spp,
@@ -578,7 +596,12 @@ __global__ void __launch_bounds__(128, 8) k_gather(GiP g, DScene s, const LightD
     f3 half{0.0f, 0.0f, 0.0f};
     uint32_t pix = 0;
     if (i < cnt) {
-      pix = list ? list[i] : quadPixel(i, uint32_t(grid.W), uint32_t(grid.H));
+      // several lanes per point: a warp's points form a quad; one thread per
+      // point (the reservoir gather): its 32 points form an 8 x 4 block
+      // (-15 % against quads along a row)
+      pix = list                ? list[i]
+            : LANES == 1        ? tilePixel4(i, uint32_t(grid.W), uint32_t(grid.H))
+                                : quadPixel(i, uint32_t(grid.W), uint32_t(grid.H));
       const float4 ne = grid.ne[pix];
       if (ne.w != 0.0f) {
         const float4 pd = grid.pd[pix];
