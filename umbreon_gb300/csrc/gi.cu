@@ -1091,10 +1091,12 @@ UBR_D RsvView loadRsv(const float4* r, uint32_t q) {
 template <int KM>
 __global__ void __launch_bounds__(128) k_spatial(GiSpatial sp, DScene sc, GiGrid grid, const float4* in,
                                                  float4* out, int round, float4* E, unsigned long long* overflow) {
-  const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t n = uint32_t(grid.W) * uint32_t(grid.H);
   uint32_t ovf = 0;
-  if (pix < n) {
+  if (i < n) {
+    // a warp's points form an 8 x 4 block (their neighbours overlap)
+    const uint32_t pix = tilePixel4(i, uint32_t(grid.W), uint32_t(grid.H));
     const float4 ne = grid.ne[pix];
     float4* o = out + size_t(kRsvF4) * pix;
     if (ne.w == 0.0f) {
